@@ -1,0 +1,720 @@
+/*
+ * CPU oracle (test infrastructure only): wellbore problem, setup, residual
+ * and tangent assembly, Jacobi-PCG and the load-stepped Newton loop.
+ *
+ * Reference correspondence (labmec/IntPointsFEM):
+ *   orc_element_blocks   TPZNumericalIntegrator.cpp:272-388 (B blocks, row-major
+ *                        (3*npts) x (2*nshape), row order [eps_xx, gamma_xy, eps_yy])
+ *                        and :420-427 (weights w*|detJ|)
+ *   dof map              TPZNumericalIntegrator.cpp:429-443
+ *   orc_greedy_coloring  TPZNumericalIntegrator.cpp:452-536
+ *   orc_gather_strain    TPZNumericalIntegrator.cpp:40-51 + TPZIrregularBlocksMatrix.cpp:97-140 (opt 0)
+ *   orc_scatter_residual TPZNumericalIntegrator.cpp:81-105 (alpha = -1, colour slabs,
+ *                        pairwise slab reduction)
+ *   orc_assemble_residual TPZElastoPlasticIntPointsStructMatrix.cpp:213-230
+ *   orc_assemble         TPZElastoPlasticIntPointsStructMatrix.cpp:175-211 and
+ *                        TPZNumericalIntegrator.cpp:131-182, 236-270 (element
+ *                        tangent, upper triangle, colour-ordered accumulation)
+ *   orc_solve_steps      main.cpp:160-262 (Newton) and main.cpp:487-522 (accept)
+ * The mesh provider (quarter annulus, Q2 Lagrange basis, 3x3 Gauss, tractions,
+ * Dirichlet symmetry) stands in for NeoPZ, which is not part of the reference.
+ * Jacobi-PCG has no reference counterpart (the reference solves with Pardiso).
+ */
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+#include <omp.h>
+#include "orc_problem.h"
+
+#define NB_NODES 256      /* nodes per level-1 reduction block */
+
+/* ------------------------------------------------------------- utilities */
+
+static void *xcalloc(size_t n, size_t s)
+{
+    void *p = calloc(n ? n : 1, s);
+    if (!p) abort();
+    return p;
+}
+
+static uint64_t sm64(uint64_t x)
+{
+    x += 0x9E3779B97F4A7C15ULL;
+    x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ULL;
+    x = (x ^ (x >> 27)) * 0x94D049BB133111EBULL;
+    return x ^ (x >> 31);
+}
+
+static double urand(uint64_t seed, uint64_t e, uint64_t k)
+{
+    return (double)(sm64(seed * 0x100000001B3ULL + 4 * e + k) >> 11) * 0x1.0p-53;
+}
+
+void orc_default_params(orc_params *prm, int n)
+{
+    memset(prm, 0, sizeof *prm);
+    prm->nr = n;
+    prm->nt = n;
+    prm->r_in = 0.1;
+    prm->r_out = 4.0;
+    prm->grading = pow(1.05, 40.0 / (double)n);
+    prm->E = 15000.0;
+    prm->nu = 0.2;
+    prm->cohesion = 10.0;
+    prm->phi_deg = 30.0;
+    prm->psi_deg = 30.0;
+    prm->sxx0 = -40.0;
+    prm->syy0 = -50.0;
+    prm->sxy0 = 0.0;
+    prm->szz0 = 0.2 * (-40.0 + -50.0);
+    prm->pw_final = -10.0;
+    prm->material_mode = 0;
+    prm->c_cv = 0.2;
+    prm->phi_lo_deg = 25.0;
+    prm->phi_hi_deg = 35.0;
+    prm->seed = 20260101ULL;
+}
+
+/* -------------------------------------------------------- mesh provider */
+
+void orc_vertex_coords(const orc_params *prm, double *vxy)
+{
+    const int nr = prm->nr, nt = prm->nt;
+    const double q = prm->grading;
+    double *r = (double *)xcalloc((size_t)nr + 1, sizeof(double));
+    double h0 = (q == 1.0) ? (prm->r_out - prm->r_in) / (double)nr
+                           : (prm->r_out - prm->r_in) * (q - 1.0) / (pow(q, (double)nr) - 1.0);
+    r[0] = prm->r_in;
+    for (int i = 0; i < nr - 1; i++) r[i + 1] = r[i] + h0 * pow(q, (double)i);
+    r[nr] = prm->r_out;
+    const double dth = (0.5 * M_PI) / (double)nt;
+    for (int j = 0; j <= nt; j++) {
+        double th = (double)j * dth;
+        double c = cos(th), s = sin(th);
+        for (int i = 0; i <= nr; i++) {
+            double *v = &vxy[2 * ((size_t)j * (nr + 1) + i)];
+            if (j == 0) { v[0] = r[i]; v[1] = 0.0; }
+            else if (j == nt) { v[0] = 0.0; v[1] = r[i]; }
+            else { v[0] = r[i] * c; v[1] = r[i] * s; }
+        }
+    }
+    free(r);
+}
+
+/* reference coordinates of the 9 connects (PZ quad order) */
+static const int ref_a[9] = {-1, 1, 1, -1, 0, 1, 0, -1, 0};
+static const int ref_b[9] = {-1, -1, 1, 1, -1, 0, 1, 0, 0};
+
+static double lag(int a, double x)
+{
+    if (a < 0) return 0.5 * x * (x - 1.0);
+    if (a == 0) return 1.0 - x * x;
+    return 0.5 * x * (x + 1.0);
+}
+
+static double dlag(int a, double x)
+{
+    if (a < 0) return x - 0.5;
+    if (a == 0) return -2.0 * x;
+    return x + 0.5;
+}
+
+void orc_element_blocks(int32_t n_el, const int32_t *connects, const double *node_xy,
+                        double *B, double *weight)
+{
+    const double g = sqrt(0.6);
+    const double gp[3] = {-g, 0.0, g};
+    const double gw[3] = {5.0 / 9.0, 8.0 / 9.0, 5.0 / 9.0};
+#pragma omp parallel for schedule(static)
+    for (int32_t e = 0; e < n_el; e++) {
+        double X[4], Y[4];
+        for (int v = 0; v < 4; v++) {
+            X[v] = node_xy[2 * (size_t)connects[9 * (size_t)e + v]];
+            Y[v] = node_xy[2 * (size_t)connects[9 * (size_t)e + v] + 1];
+        }
+        double *Be = &B[(size_t)e * 486];
+        memset(Be, 0, 486 * sizeof(double));
+        for (int iq = 0; iq < 9; iq++) {
+            const int ix = iq % 3, iy = iq / 3;
+            const double xi = gp[ix], eta = gp[iy];
+            const double dpx[4] = {-(1.0 - eta) / 4.0, (1.0 - eta) / 4.0, (1.0 + eta) / 4.0, -(1.0 + eta) / 4.0};
+            const double dpe[4] = {-(1.0 - xi) / 4.0, -(1.0 + xi) / 4.0, (1.0 + xi) / 4.0, (1.0 - xi) / 4.0};
+            double x_xi = dpx[0] * X[0], x_eta = dpe[0] * X[0];
+            double y_xi = dpx[0] * Y[0], y_eta = dpe[0] * Y[0];
+            for (int v = 1; v < 4; v++) {
+                x_xi = x_xi + dpx[v] * X[v];
+                x_eta = x_eta + dpe[v] * X[v];
+                y_xi = y_xi + dpx[v] * Y[v];
+                y_eta = y_eta + dpe[v] * Y[v];
+            }
+            const double det = x_xi * y_eta - x_eta * y_xi;
+            const double xi_x = y_eta / det, xi_y = -x_eta / det;
+            const double eta_x = -y_xi / det, eta_y = x_xi / det;
+            weight[(size_t)e * 9 + iq] = (gw[ix] * gw[iy]) * fabs(det);
+            double *r0 = &Be[(3 * iq + 0) * 18];
+            double *r1 = &Be[(3 * iq + 1) * 18];
+            double *r2 = &Be[(3 * iq + 2) * 18];
+            for (int n = 0; n < 9; n++) {
+                const double Nxi = dlag(ref_a[n], xi) * lag(ref_b[n], eta);
+                const double Neta = lag(ref_a[n], xi) * dlag(ref_b[n], eta);
+                const double dNx = Nxi * xi_x + Neta * eta_x;
+                const double dNy = Nxi * xi_y + Neta * eta_y;
+                r0[2 * n] = dNx;
+                r1[2 * n] = dNy;
+                r1[2 * n + 1] = dNx;
+                r2[2 * n + 1] = dNy;
+            }
+        }
+    }
+}
+
+int32_t orc_greedy_coloring(int32_t n_el, int32_t n_nodes, const int32_t *connects, int32_t *el_color)
+{
+    uint8_t *mark = (uint8_t *)xcalloc((size_t)n_nodes, 1);
+    for (int32_t e = 0; e < n_el; e++) el_color[e] = -1;
+    int32_t color = 0;
+    int again = 1;
+    while (again) {
+        again = 0;
+        for (int32_t e = 0; e < n_el; e++) {
+            if (el_color[e] != -1) continue;
+            const int32_t *c = &connects[9 * (size_t)e];
+            int k;
+            for (k = 0; k < 9; k++)
+                if (mark[c[k]]) break;
+            if (k != 9) { again = 1; continue; }
+            el_color[e] = color;
+            for (k = 0; k < 9; k++) mark[c[k]] = 1;
+        }
+        color++;
+        memset(mark, 0, (size_t)n_nodes);
+    }
+    free(mark);
+    return color;
+}
+
+static int cmp_i32(const void *a, const void *b)
+{
+    int32_t x = *(const int32_t *)a, y = *(const int32_t *)b;
+    return (x > y) - (x < y);
+}
+
+/* edge traction of a uniform stress s = (sxx, sxy, syy) on segment P-M-Q,
+ * outward normal sign sgn (+1: (dy,-dx)/L, -1: (-dy,dx)/L); Simpson weights */
+static void seg_load(const double *xy, int32_t P, int32_t M, int32_t Q, int sgn,
+                     double sxx, double sxy, double syy, double *f)
+{
+    const double dx = xy[2 * (size_t)Q] - xy[2 * (size_t)P];
+    const double dy = xy[2 * (size_t)Q + 1] - xy[2 * (size_t)P + 1];
+    const double L = sqrt(dx * dx + dy * dy);
+    const double nx = sgn > 0 ? dy / L : -dy / L;
+    const double ny = sgn > 0 ? -dx / L : dx / L;
+    const double tx = sxx * nx + sxy * ny;
+    const double ty = sxy * nx + syy * ny;
+    const double we = L / 6.0, wm = 2.0 * L / 3.0;
+    f[2 * (size_t)P] += tx * we;
+    f[2 * (size_t)P + 1] += ty * we;
+    f[2 * (size_t)M] += tx * wm;
+    f[2 * (size_t)M + 1] += ty * wm;
+    f[2 * (size_t)Q] += tx * we;
+    f[2 * (size_t)Q + 1] += ty * we;
+}
+
+orc_problem *orc_problem_create(const orc_params *prm, int nthreads)
+{
+    if (nthreads > 0) omp_set_num_threads(nthreads);
+    orc_problem *p = (orc_problem *)xcalloc(1, sizeof *p);
+    p->prm = *prm;
+    p->nthreads = nthreads > 0 ? nthreads : omp_get_max_threads();
+    const int nr = prm->nr, nt = prm->nt;
+    const int gr = 2 * nr + 1, gt = 2 * nt + 1;
+    p->n_el = nr * nt;
+    p->n_nodes = gr * gt;
+    p->neq = 2 * p->n_nodes;
+    p->n_ip = (int64_t)p->n_el * ORC_NPTS;
+
+    /* nodes: vertex grid, then edge / centre nodes on the bilinear map */
+    double *vxy = (double *)xcalloc((size_t)(nr + 1) * (nt + 1) * 2, sizeof(double));
+    orc_vertex_coords(prm, vxy);
+    p->node_xy = (double *)xcalloc((size_t)p->n_nodes * 2, sizeof(double));
+    for (int b = 0; b < gt; b++)
+        for (int a = 0; a < gr; a++) {
+            double *o = &p->node_xy[2 * ((size_t)b * gr + a)];
+            const int i0 = a / 2, j0 = b / 2;
+            const int i1 = (a + 1) / 2, j1 = (b + 1) / 2;
+            const double *v00 = &vxy[2 * ((size_t)j0 * (nr + 1) + i0)];
+            const double *v10 = &vxy[2 * ((size_t)j0 * (nr + 1) + i1)];
+            const double *v11 = &vxy[2 * ((size_t)j1 * (nr + 1) + i1)];
+            const double *v01 = &vxy[2 * ((size_t)j1 * (nr + 1) + i0)];
+            if (!(a & 1) && !(b & 1)) { o[0] = v00[0]; o[1] = v00[1]; }
+            else if ((a & 1) && !(b & 1)) { o[0] = 0.5 * (v00[0] + v10[0]); o[1] = 0.5 * (v00[1] + v10[1]); }
+            else if (!(a & 1) && (b & 1)) { o[0] = 0.5 * (v00[0] + v01[0]); o[1] = 0.5 * (v00[1] + v01[1]); }
+            else {
+                o[0] = 0.25 * (((v00[0] + v10[0]) + v11[0]) + v01[0]);
+                o[1] = 0.25 * (((v00[1] + v10[1]) + v11[1]) + v01[1]);
+            }
+        }
+    free(vxy);
+    /* connects: element (i, j) = j*nr + i; vertices, edges, centre */
+    p->connects = (int32_t *)xcalloc((size_t)p->n_el * 9, sizeof(int32_t));
+    for (int j = 0; j < nt; j++)
+        for (int i = 0; i < nr; i++) {
+            int32_t *c = &p->connects[9 * ((size_t)j * nr + i)];
+            const int a0 = 2 * i, b0 = 2 * j;
+#define NID(a, b) ((int32_t)((b) * gr + (a)))
+            c[0] = NID(a0, b0);         c[1] = NID(a0 + 2, b0);
+            c[2] = NID(a0 + 2, b0 + 2); c[3] = NID(a0, b0 + 2);
+            c[4] = NID(a0 + 1, b0);     c[5] = NID(a0 + 2, b0 + 1);
+            c[6] = NID(a0 + 1, b0 + 2); c[7] = NID(a0, b0 + 1);
+            c[8] = NID(a0 + 1, b0 + 1);
+        }
+    /* Dirichlet: u_y = 0 on y = 0 (b = 0), u_x = 0 on x = 0 (b = 2nt) */
+    p->fixed = (uint8_t *)xcalloc((size_t)p->neq, 1);
+    for (int a = 0; a < gr; a++) {
+        p->fixed[2 * (size_t)NID(a, 0) + 1] = 1;
+        p->fixed[2 * (size_t)NID(a, gt - 1) + 0] = 1;
+    }
+    /* loads: outer arc with sigma0, well arc with sigma0 -> pw I */
+    p->f0 = (double *)xcalloc((size_t)p->neq, sizeof(double));
+    p->df = (double *)xcalloc((size_t)p->neq, sizeof(double));
+    {
+        double *fo = (double *)xcalloc((size_t)p->neq, sizeof(double));
+        double *fw0 = (double *)xcalloc((size_t)p->neq, sizeof(double));
+        double *fw1 = (double *)xcalloc((size_t)p->neq, sizeof(double));
+        for (int j = 0; j < nt; j++) {
+            seg_load(p->node_xy, NID(gr - 1, 2 * j), NID(gr - 1, 2 * j + 1), NID(gr - 1, 2 * j + 2), +1,
+                     prm->sxx0, prm->sxy0, prm->syy0, fo);
+            seg_load(p->node_xy, NID(0, 2 * j), NID(0, 2 * j + 1), NID(0, 2 * j + 2), -1,
+                     prm->sxx0, prm->sxy0, prm->syy0, fw0);
+            seg_load(p->node_xy, NID(0, 2 * j), NID(0, 2 * j + 1), NID(0, 2 * j + 2), -1,
+                     prm->pw_final, 0.0, prm->pw_final, fw1);
+        }
+        for (int32_t i = 0; i < p->neq; i++) {
+            p->f0[i] = fo[i] + fw0[i];
+            p->df[i] = fw1[i] - fw0[i];
+        }
+        free(fo); free(fw0); free(fw1);
+    }
+#undef NID
+    /* material */
+    orc_lame_from_engineering(prm->E, prm->nu, &p->el);
+    p->mats = (orc_mc *)xcalloc((size_t)p->n_el, sizeof(orc_mc));
+    {
+        const double d2r = M_PI / 180.0;
+        const double s2 = log(1.0 + prm->c_cv * prm->c_cv);
+        const double mln = log(prm->cohesion) - 0.5 * s2;
+        const double sln = sqrt(s2);
+#pragma omp parallel for schedule(static)
+        for (int32_t e = 0; e < p->n_el; e++) {
+            double c = prm->cohesion, phi = prm->phi_deg, psi = prm->psi_deg;
+            if (prm->material_mode >= 1) {
+                double u1 = 1.0 - urand(prm->seed, (uint64_t)e, 0);
+                double u2 = urand(prm->seed, (uint64_t)e, 1);
+                double z = sqrt(-2.0 * log(u1)) * cos(2.0 * M_PI * u2);
+                c = exp(mln + sln * z);
+            }
+            if (prm->material_mode >= 2) {
+                phi = prm->phi_lo_deg + (prm->phi_hi_deg - prm->phi_lo_deg) * urand(prm->seed, (uint64_t)e, 2);
+                psi = phi;
+            }
+            orc_mc_from_angles(c, phi * d2r, psi * d2r, &p->mats[e]);
+        }
+    }
+    /* in-situ seed: eps_p0 = -C^{-1} sigma0, ComputeStrain (FunctionsStressStrain.h:73-81) */
+    p->eps_p0 = (double *)xcalloc(6, sizeof(double));
+    {
+        const double lambda = p->el.lambda, mu = p->el.mu;
+        const double s[6] = {prm->sxx0, prm->sxy0, 0.0, prm->syy0, 0.0, prm->szz0};
+        double e6[6];
+        e6[0] = (lambda + mu) / (3 * lambda * mu + 2 * mu * mu) * s[0] - lambda / (6 * lambda * mu + 4 * mu * mu) * (s[3] + s[5]);
+        e6[3] = (lambda + mu) / (3 * lambda * mu + 2 * mu * mu) * s[3] - lambda / (6 * lambda * mu + 4 * mu * mu) * (s[0] + s[5]);
+        e6[5] = (lambda + mu) / (3 * lambda * mu + 2 * mu * mu) * s[5] - lambda / (6 * lambda * mu + 4 * mu * mu) * (s[3] + s[0]);
+        e6[1] = 1 / mu * s[1];
+        e6[2] = 1 / mu * s[2];
+        e6[4] = 1 / mu * s[4];
+        for (int k = 0; k < 6; k++) p->eps_p0[k] = -e6[k];
+    }
+    /* setup: B blocks, weights, dof map, colouring */
+    p->B = (double *)xcalloc((size_t)p->n_el * 486, sizeof(double));
+    p->weight = (double *)xcalloc((size_t)p->n_ip, sizeof(double));
+    orc_element_blocks(p->n_el, p->connects, p->node_xy, p->B, p->weight);
+    p->dofs = (int32_t *)xcalloc((size_t)p->n_el * 18, sizeof(int32_t));
+    for (size_t k = 0; k < (size_t)p->n_el * 9; k++) {
+        p->dofs[2 * k] = 2 * p->connects[k];
+        p->dofs[2 * k + 1] = 2 * p->connects[k] + 1;
+    }
+    p->el_color = (int32_t *)xcalloc((size_t)p->n_el, sizeof(int32_t));
+    p->n_colors = orc_greedy_coloring(p->n_el, p->n_nodes, p->connects, p->el_color);
+    p->color_ptr = (int32_t *)xcalloc((size_t)p->n_colors + 1, sizeof(int32_t));
+    p->color_els = (int32_t *)xcalloc((size_t)p->n_el, sizeof(int32_t));
+    for (int32_t e = 0; e < p->n_el; e++) p->color_ptr[p->el_color[e] + 1]++;
+    for (int c = 0; c < p->n_colors; c++) p->color_ptr[c + 1] += p->color_ptr[c];
+    {
+        int32_t *fill = (int32_t *)xcalloc((size_t)p->n_colors, sizeof(int32_t));
+        for (int32_t e = 0; e < p->n_el; e++) {
+            int c = p->el_color[e];
+            p->color_els[p->color_ptr[c] + fill[c]++] = e;
+        }
+        free(fill);
+    }
+    /* nodal block pattern: node -> sorted coupled nodes */
+    {
+        int32_t *deg = (int32_t *)xcalloc((size_t)p->n_nodes, sizeof(int32_t));
+        int32_t *cnt = (int32_t *)xcalloc((size_t)p->n_nodes, sizeof(int32_t));
+        for (int32_t e = 0; e < p->n_el; e++)
+            for (int m = 0; m < 9; m++) cnt[p->connects[9 * (size_t)e + m]] += 9;
+        int64_t *cap = (int64_t *)xcalloc((size_t)p->n_nodes + 1, sizeof(int64_t));
+        for (int32_t i = 0; i < p->n_nodes; i++) cap[i + 1] = cap[i] + cnt[i];
+        int32_t *tmp = (int32_t *)xcalloc((size_t)cap[p->n_nodes], sizeof(int32_t));
+        for (int32_t e = 0; e < p->n_el; e++)
+            for (int m = 0; m < 9; m++) {
+                int32_t r = p->connects[9 * (size_t)e + m];
+                for (int n = 0; n < 9; n++) tmp[cap[r] + deg[r]++] = p->connects[9 * (size_t)e + n];
+            }
+        p->row_ptr = (int64_t *)xcalloc((size_t)p->n_nodes + 1, sizeof(int64_t));
+        for (int32_t i = 0; i < p->n_nodes; i++) {
+            int32_t *s = &tmp[cap[i]];
+            qsort(s, (size_t)deg[i], sizeof(int32_t), cmp_i32);
+            int32_t u = 0;
+            for (int32_t k = 0; k < deg[i]; k++)
+                if (k == 0 || s[k] != s[k - 1]) s[u++] = s[k];
+            deg[i] = u;
+            p->row_ptr[i + 1] = p->row_ptr[i] + u;
+        }
+        p->n_blocks = p->row_ptr[p->n_nodes];
+        p->col = (int32_t *)xcalloc((size_t)p->n_blocks, sizeof(int32_t));
+        for (int32_t i = 0; i < p->n_nodes; i++)
+            memcpy(&p->col[p->row_ptr[i]], &tmp[cap[i]], (size_t)deg[i] * sizeof(int32_t));
+        free(tmp); free(cap); free(cnt); free(deg);
+        p->el_blk = (int64_t *)xcalloc((size_t)p->n_el * 81, sizeof(int64_t));
+#pragma omp parallel for schedule(static)
+        for (int32_t e = 0; e < p->n_el; e++)
+            for (int m = 0; m < 9; m++) {
+                int32_t r = p->connects[9 * (size_t)e + m];
+                for (int n = 0; n < 9; n++) {
+                    int32_t c = p->connects[9 * (size_t)e + n];
+                    int64_t lo = p->row_ptr[r], hi = p->row_ptr[r + 1] - 1;
+                    while (lo < hi) {
+                        int64_t mid = (lo + hi) / 2;
+                        if (p->col[mid] < c) lo = mid + 1; else hi = mid;
+                    }
+                    p->el_blk[(size_t)e * 81 + m * 9 + n] = lo;
+                }
+            }
+    }
+    /* state */
+    p->eps_p = (double *)xcalloc((size_t)p->n_ip * 6, sizeof(double));
+    p->sigma = (double *)xcalloc((size_t)p->n_ip * 6, sizeof(double));
+    p->mtype = (int8_t *)xcalloc((size_t)p->n_ip, 1);
+    p->alpha = (double *)xcalloc((size_t)p->n_ip, sizeof(double));
+    for (int64_t i = 0; i < p->n_ip; i++) {
+        for (int k = 0; k < 6; k++) p->eps_p[6 * i + k] = p->eps_p0[k];
+        p->sigma[6 * i + 0] = prm->sxx0;
+        p->sigma[6 * i + 1] = prm->sxy0;
+        p->sigma[6 * i + 3] = prm->syy0;
+        p->sigma[6 * i + 5] = prm->szz0;
+    }
+    p->strain = (double *)xcalloc((size_t)p->n_ip * 3, sizeof(double));
+    p->sigma_w = (double *)xcalloc((size_t)p->n_ip * 3, sizeof(double));
+    p->dep = (double *)xcalloc((size_t)p->n_ip * 9, sizeof(double));
+    p->K = (double *)xcalloc((size_t)p->n_blocks * 4, sizeof(double));
+    p->dinv = (double *)xcalloc((size_t)p->neq, sizeof(double));
+    return p;
+}
+
+void orc_problem_destroy(orc_problem *p)
+{
+    if (!p) return;
+    free(p->node_xy); free(p->connects); free(p->fixed); free(p->f0); free(p->df);
+    free(p->mats); free(p->eps_p0); free(p->B); free(p->weight); free(p->dofs);
+    free(p->el_color); free(p->color_ptr); free(p->color_els); free(p->row_ptr);
+    free(p->col); free(p->el_blk); free(p->eps_p); free(p->sigma); free(p->mtype);
+    free(p->alpha); free(p->strain); free(p->sigma_w); free(p->dep); free(p->K); free(p->dinv);
+    free(p);
+}
+
+/* ------------------------------------------------------------ reductions */
+
+static double tree32(double *v)
+{
+    for (int off = 16; off >= 1; off >>= 1)
+        for (int l = 0; l < off; l++) v[l] = v[l] + v[l + off];
+    return v[0];
+}
+
+int64_t orc_dot_partials(int64_t nnodes, const double *a, const double *b, double *partials)
+{
+    const int64_t nb = (nnodes + NB_NODES - 1) / NB_NODES;
+#pragma omp parallel for schedule(static)
+    for (int64_t blk = 0; blk < nb; blk++) {
+        double w[8];
+        for (int s = 0; s < 8; s++) {
+            double v[32];
+            for (int l = 0; l < 32; l++) {
+                int64_t n = blk * NB_NODES + 32 * s + l;
+                double acc = 0.0;
+                if (n < nnodes) {
+                    acc = fma(a[2 * n], b[2 * n], acc);
+                    acc = fma(a[2 * n + 1], b[2 * n + 1], acc);
+                }
+                v[l] = acc;
+            }
+            w[s] = tree32(v);
+        }
+        for (int off = 4; off >= 1; off >>= 1)
+            for (int l = 0; l < off; l++) w[l] = w[l] + w[l + off];
+        partials[blk] = w[0];
+    }
+    return nb;
+}
+
+double orc_dot_final(int64_t np, const double *partials)
+{
+    double acc[1024];
+    for (int t = 0; t < 1024; t++) {
+        double s = 0.0;
+        for (int64_t k = t; k < np; k += 1024) s = s + partials[k];
+        acc[t] = s;
+    }
+    double ws[32];
+    for (int w = 0; w < 32; w++) ws[w] = tree32(&acc[32 * w]);
+    return tree32(ws);
+}
+
+double orc_dot(int64_t nnodes, const double *a, const double *b)
+{
+    const int64_t nb = (nnodes + NB_NODES - 1) / NB_NODES;
+    double *part = (double *)xcalloc((size_t)nb, sizeof(double));
+    orc_dot_partials(nnodes, a, b, part);
+    double r = orc_dot_final(nb, part);
+    free(part);
+    return r;
+}
+
+/* ------------------------------------------------------------- assembly */
+
+void orc_gather_strain(const orc_problem *p, const double *u, double *strain)
+{
+#pragma omp parallel for schedule(static)
+    for (int32_t e = 0; e < p->n_el; e++) {
+        double ue[18];
+        for (int j = 0; j < 18; j++) ue[j] = u[p->dofs[18 * (size_t)e + j]];
+        const double *Be = &p->B[(size_t)e * 486];
+        for (int r = 0; r < 27; r++) {
+            double acc = 0.0;
+            for (int j = 0; j < 18; j++) acc = fma(Be[r * 18 + j], ue[j], acc);
+            strain[(size_t)e * 27 + r] = acc;
+        }
+    }
+}
+
+void orc_scatter_residual(const orc_problem *p, const double *sigma_w, double *res)
+{
+    const int32_t neq = p->neq;
+    const int nc = p->n_colors;
+    double *slab = (double *)xcalloc((size_t)nc * neq, sizeof(double));
+#pragma omp parallel for schedule(static)
+    for (int32_t e = 0; e < p->n_el; e++) {
+        const double *Be = &p->B[(size_t)e * 486];
+        const double *s = &sigma_w[(size_t)e * 27];
+        double *sl = &slab[(size_t)p->el_color[e] * neq];
+        for (int j = 0; j < 18; j++) {
+            double acc = 0.0;
+            for (int r = 0; r < 27; r++) acc = fma(Be[r * 18 + j], s[r], acc);
+            sl[p->dofs[18 * (size_t)e + j]] = -acc;
+        }
+    }
+    int64_t ncol = nc, ca = nc / 2;
+    while (ca > 0) {
+        const int64_t first = (ncol - ca) * (int64_t)neq;
+        const int64_t len = ca * (int64_t)neq;
+#pragma omp parallel for schedule(static)
+        for (int64_t i = 0; i < len; i++) slab[i] = slab[i] + slab[first + i];
+        ncol -= ca;
+        ca = ncol / 2;
+    }
+    memcpy(res, slab, (size_t)neq * sizeof(double));
+    free(slab);
+}
+
+static void finish_rhs(const orc_problem *p, double lambda, double *rhs)
+{
+#pragma omp parallel for schedule(static)
+    for (int32_t i = 0; i < p->neq; i++) {
+        const double lin = fma(lambda, p->df[i], p->f0[i]);
+        rhs[i] = p->fixed[i] ? 0.0 : rhs[i] + lin;
+    }
+}
+
+void orc_assemble_residual(orc_problem *p, const double *u, double lambda, int update_mem, double *rhs)
+{
+    orc_gather_strain(p, u, p->strain);
+    orc_compute_sigma_batch(p->n_ip, ORC_NPTS, &p->el, p->mats, p->strain, p->eps_p, p->weight,
+                            update_mem, p->sigma_w, 0, p->sigma, p->mtype, p->alpha);
+    orc_scatter_residual(p, p->sigma_w, rhs);
+    finish_rhs(p, lambda, rhs);
+}
+
+void orc_assemble(orc_problem *p, const double *u, double lambda, double *rhs)
+{
+    orc_gather_strain(p, u, p->strain);
+    orc_compute_sigma_batch(p->n_ip, ORC_NPTS, &p->el, p->mats, p->strain, p->eps_p, p->weight,
+                            0, p->sigma_w, p->dep, 0, 0, 0);
+    orc_scatter_residual(p, p->sigma_w, rhs);
+    finish_rhs(p, lambda, rhs);
+    memset(p->K, 0, (size_t)p->n_blocks * 4 * sizeof(double));
+    for (int c = 0; c < p->n_colors; c++) {
+#pragma omp parallel for schedule(static)
+        for (int32_t k = p->color_ptr[c]; k < p->color_ptr[c + 1]; k++) {
+            const int32_t e = p->color_els[k];
+            const double *Be = &p->B[(size_t)e * 486];
+            double Kl[18][18];
+            memset(Kl, 0, sizeof Kl);
+            for (int q = 0; q < 9; q++) {
+                const double *Bq = &Be[q * 54];
+                const double *D = &p->dep[((size_t)e * 9 + q) * 9];
+                double DB[3][18];
+                for (int i = 0; i < 3; i++)
+                    for (int j = 0; j < 18; j++) {
+                        double s = D[3 * i + 0] * Bq[0 * 18 + j];
+                        s = fma(D[3 * i + 1], Bq[1 * 18 + j], s);
+                        s = fma(D[3 * i + 2], Bq[2 * 18 + j], s);
+                        DB[i][j] = s;
+                    }
+                for (int a = 0; a < 18; a++)
+                    for (int b = a; b < 18; b++) {
+                        double t = Kl[a][b];
+                        t = fma(Bq[0 * 18 + a], DB[0][b], t);
+                        t = fma(Bq[1 * 18 + a], DB[1][b], t);
+                        t = fma(Bq[2 * 18 + a], DB[2][b], t);
+                        Kl[a][b] = t;
+                    }
+            }
+            const int64_t *eb = &p->el_blk[(size_t)e * 81];
+            for (int a = 0; a < 18; a++)
+                for (int b = a; b < 18; b++) {
+                    const int m = a / 2, ca = a % 2, n = b / 2, cb = b % 2;
+                    const double v = Kl[a][b];
+                    if (m == n) {
+                        double *blk = &p->K[4 * eb[m * 9 + m]];
+                        blk[2 * ca + cb] = blk[2 * ca + cb] + v;
+                        if (ca != cb) blk[2 * cb + ca] = blk[2 * cb + ca] + v;
+                    } else {
+                        double *b1 = &p->K[4 * eb[m * 9 + n]];
+                        double *b2 = &p->K[4 * eb[n * 9 + m]];
+                        b1[2 * ca + cb] = b1[2 * ca + cb] + v;
+                        b2[2 * cb + ca] = b2[2 * cb + ca] + v;
+                    }
+                }
+        }
+    }
+    /* Jacobi: inverse of the nodal-block diagonal entries on free dofs */
+#pragma omp parallel for schedule(static)
+    for (int32_t i = 0; i < p->n_nodes; i++) {
+        int64_t lo = p->row_ptr[i], hi = p->row_ptr[i + 1] - 1;
+        while (lo < hi) {
+            int64_t mid = (lo + hi) / 2;
+            if (p->col[mid] < i) lo = mid + 1; else hi = mid;
+        }
+        const double *blk = &p->K[4 * lo];
+        p->dinv[2 * i] = p->fixed[2 * i] ? 0.0 : 1.0 / blk[0];
+        p->dinv[2 * i + 1] = p->fixed[2 * i + 1] ? 0.0 : 1.0 / blk[3];
+    }
+}
+
+void orc_spmv(const orc_problem *p, const double *x, double *y)
+{
+#pragma omp parallel for schedule(static)
+    for (int32_t i = 0; i < p->n_nodes; i++) {
+        double y0 = 0.0, y1 = 0.0;
+        for (int64_t k = p->row_ptr[i]; k < p->row_ptr[i + 1]; k++) {
+            const double *a = &p->K[4 * k];
+            const double x0 = x[2 * (size_t)p->col[k]], x1 = x[2 * (size_t)p->col[k] + 1];
+            y0 = fma(a[0], x0, y0);
+            y0 = fma(a[1], x1, y0);
+            y1 = fma(a[2], x0, y1);
+            y1 = fma(a[3], x1, y1);
+        }
+        y[2 * (size_t)i] = p->fixed[2 * i] ? 0.0 : y0;
+        y[2 * (size_t)i + 1] = p->fixed[2 * i + 1] ? 0.0 : y1;
+    }
+}
+
+int orc_pcg(const orc_problem *p, const double *b, double *x, double rtol, int max_it, double *work)
+{
+    const int32_t n = p->neq;
+    const int64_t nn = p->n_nodes;
+    double *r = work, *z = work + n, *pv = work + 2 * (size_t)n, *q = work + 3 * (size_t)n;
+#pragma omp parallel for schedule(static)
+    for (int32_t i = 0; i < n; i++) {
+        x[i] = 0.0;
+        r[i] = b[i];
+        z[i] = r[i] * p->dinv[i];
+        pv[i] = z[i];
+    }
+    const double bb = orc_dot(nn, b, b);
+    if (bb == 0.0) return 0;
+    const double thr = (rtol * rtol) * bb;
+    double rz = orc_dot(nn, r, z);
+    for (int k = 1; k <= max_it; k++) {
+        orc_spmv(p, pv, q);
+        const double pq = orc_dot(nn, pv, q);
+        if (!(pq > 0.0)) return -k;
+        const double alpha = rz / pq;
+#pragma omp parallel for schedule(static)
+        for (int32_t i = 0; i < n; i++) {
+            x[i] = fma(alpha, pv[i], x[i]);
+            r[i] = fma(-alpha, q[i], r[i]);
+            z[i] = r[i] * p->dinv[i];
+        }
+        const double rr = orc_dot(nn, r, r);
+        if (rr <= thr) return k;
+        const double rzn = orc_dot(nn, r, z);
+        const double beta = rzn / rz;
+        rz = rzn;
+#pragma omp parallel for schedule(static)
+        for (int32_t i = 0; i < n; i++) pv[i] = fma(beta, pv[i], z[i]);
+    }
+    return -max_it;
+}
+
+void orc_solve_steps(orc_problem *p, const orc_solve_opts *o, int32_t step_begin, int32_t step_end,
+                     double *u, orc_solve_stats *st, double *log, int32_t log_cap)
+{
+    const int32_t n = p->neq;
+    double *R = (double *)xcalloc((size_t)n, sizeof(double));
+    double *du = (double *)xcalloc((size_t)n, sizeof(double));
+    double *work = (double *)xcalloc((size_t)n * 4, sizeof(double));
+    int32_t nlog = 0;
+    memset(st, 0, sizeof *st);
+    st->converged = 1;
+    for (int32_t s = step_begin; s < step_end; s++) {
+        const double lambda = (double)(s + 1) / (double)o->n_steps;
+        orc_assemble(p, u, lambda, R);
+        const double r0 = sqrt(orc_dot(p->n_nodes, R, R));
+        double rn = r0;
+        int conv = (r0 == 0.0);
+        int it = 0;
+        while (!conv && it < o->newton_max_it) {
+            int k = orc_pcg(p, R, du, o->cg_rtol, o->cg_max_it, work);
+            st->cg_iters += k < 0 ? -k : k;
+            for (int32_t i = 0; i < n; i++) u[i] = u[i] + du[i];
+            it++;
+            orc_assemble(p, u, lambda, R);
+            rn = sqrt(orc_dot(p->n_nodes, R, R));
+            if (log && nlog < log_cap) {
+                log[3 * nlog + 0] = (double)s;
+                log[3 * nlog + 1] = (double)k;
+                log[3 * nlog + 2] = rn;
+                nlog++;
+            }
+            conv = rn <= o->newton_rtol * r0;
+        }
+        st->newton_iters += it;
+        st->last_step_iters = it;
+        st->final_res = r0 > 0.0 ? rn / r0 : 0.0;
+        if (!conv) st->converged = 0;
+        orc_assemble_residual(p, u, lambda, 1, R);     /* accept: commit state */
+    }
+    free(R); free(du); free(work);
+}

@@ -1,0 +1,203 @@
+"""ctypes view of the CPU oracle (test infrastructure only).
+
+Imported by tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg,
+never by the product package.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import build as _build
+
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int32)
+_lp = C.POINTER(C.c_int64)
+_bp = C.POINTER(C.c_uint8)
+
+
+class Params(C.Structure):
+    _fields_ = [("nr", C.c_int32), ("nt", C.c_int32), ("r_in", C.c_double), ("r_out", C.c_double),
+                ("grading", C.c_double), ("E", C.c_double), ("nu", C.c_double),
+                ("cohesion", C.c_double), ("phi_deg", C.c_double), ("psi_deg", C.c_double),
+                ("sxx0", C.c_double), ("syy0", C.c_double), ("sxy0", C.c_double), ("szz0", C.c_double),
+                ("pw_final", C.c_double), ("material_mode", C.c_int32), ("c_cv", C.c_double),
+                ("phi_lo_deg", C.c_double), ("phi_hi_deg", C.c_double), ("seed", C.c_uint64)]
+
+
+class MC(C.Structure):
+    _fields_ = [("cohesion", C.c_double), ("sinphi", C.c_double), ("cosphi", C.c_double),
+                ("tanphi", C.c_double), ("sinpsi", C.c_double)]
+
+
+class Elastic(C.Structure):
+    _fields_ = [("lam", C.c_double), ("mu", C.c_double)]
+
+
+class Problem(C.Structure):
+    _fields_ = [("prm", Params), ("n_el", C.c_int32), ("n_nodes", C.c_int32), ("neq", C.c_int32),
+                ("n_ip", C.c_int64), ("node_xy", _dp), ("connects", _ip), ("fixed", _bp),
+                ("f0", _dp), ("df", _dp), ("el", Elastic), ("mats", C.POINTER(MC)), ("eps_p0", _dp),
+                ("B", _dp), ("weight", _dp), ("dofs", _ip), ("n_colors", C.c_int32),
+                ("el_color", _ip), ("color_ptr", _ip), ("color_els", _ip), ("n_blocks", C.c_int64),
+                ("row_ptr", _lp), ("col", _ip), ("el_blk", _lp), ("eps_p", _dp), ("sigma", _dp),
+                ("mtype", C.POINTER(C.c_int8)), ("alpha", _dp), ("strain", _dp), ("sigma_w", _dp),
+                ("dep", _dp), ("K", _dp), ("dinv", _dp), ("nthreads", C.c_int)]
+
+
+class SolveOpts(C.Structure):
+    _fields_ = [("n_steps", C.c_int32), ("newton_rtol", C.c_double), ("newton_max_it", C.c_int32),
+                ("cg_rtol", C.c_double), ("cg_max_it", C.c_int32)]
+
+
+class SolveStats(C.Structure):
+    _fields_ = [("newton_iters", C.c_int32), ("cg_iters", C.c_int64), ("last_step_iters", C.c_int32),
+                ("converged", C.c_int32), ("final_res", C.c_double)]
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        so = _build.build_oracle()
+        L = C.CDLL(so)
+        L.orc_problem_create.restype = C.POINTER(Problem)
+        L.orc_problem_create.argtypes = [C.POINTER(Params), C.c_int]
+        L.orc_problem_destroy.argtypes = [C.POINTER(Problem)]
+        L.orc_default_params.argtypes = [C.POINTER(Params), C.c_int]
+        L.orc_dot.restype = C.c_double
+        L.orc_dot.argtypes = [C.c_int64, _dp, _dp]
+        L.orc_dot_final.restype = C.c_double
+        L.orc_dot_final.argtypes = [C.c_int64, _dp]
+        L.orc_dot_partials.restype = C.c_int64
+        L.orc_dot_partials.argtypes = [C.c_int64, _dp, _dp, _dp]
+        L.orc_assemble_residual.argtypes = [C.POINTER(Problem), _dp, C.c_double, C.c_int, _dp]
+        L.orc_assemble.argtypes = [C.POINTER(Problem), _dp, C.c_double, _dp]
+        L.orc_spmv.argtypes = [C.POINTER(Problem), _dp, _dp]
+        L.orc_pcg.restype = C.c_int
+        L.orc_pcg.argtypes = [C.POINTER(Problem), _dp, _dp, C.c_double, C.c_int, _dp]
+        L.orc_gather_strain.argtypes = [C.POINTER(Problem), _dp, _dp]
+        L.orc_scatter_residual.argtypes = [C.POINTER(Problem), _dp, _dp]
+        L.orc_solve_steps.argtypes = [C.POINTER(Problem), C.POINTER(SolveOpts), C.c_int32, C.c_int32,
+                                      _dp, C.POINTER(SolveStats), _dp, C.c_int32]
+        L.orc_mc_from_angles.argtypes = [C.c_double, C.c_double, C.c_double, C.POINTER(MC)]
+        L.orc_lame_from_engineering.argtypes = [C.c_double, C.c_double, C.POINTER(Elastic)]
+        L.orc_ip_update.argtypes = [C.POINTER(Elastic), C.POINTER(MC), _dp, _dp, C.c_double, _dp, _dp,
+                                    _dp, _dp, _dp, C.POINTER(C.c_int), _dp]
+        L.orc_ip_update_gpu_alias.argtypes = [C.POINTER(Elastic), C.POINTER(MC), _dp, _dp, C.c_double,
+                                              _dp, _dp, _dp, C.POINTER(C.c_int), _dp]
+        L.orc_compute_sigma_batch.argtypes = [C.c_int64, C.c_int, C.POINTER(Elastic), C.POINTER(MC), _dp,
+                                              _dp, _dp, C.c_int, _dp, _dp, _dp, C.POINTER(C.c_int8), _dp]
+        L.orc_greedy_coloring.restype = C.c_int32
+        L.orc_greedy_coloring.argtypes = [C.c_int32, C.c_int32, _ip, _ip]
+        _lib = L
+    return _lib
+
+
+def ptr(a):
+    """data pointer of a contiguous numpy array, typed for ctypes"""
+    if a is None:
+        return None
+    assert a.flags["C_CONTIGUOUS"]
+    t = {np.float64: _dp, np.int32: _ip, np.int64: _lp, np.uint8: _bp, np.int8: C.POINTER(C.c_int8)}[a.dtype.type]
+    return a.ctypes.data_as(t)
+
+
+def default_params(n, **kw):
+    p = Params()
+    lib().orc_default_params(C.byref(p), int(n))
+    for k, v in kw.items():
+        setattr(p, k, v)
+    return p
+
+
+def _view(p, n, dtype):
+    return np.ctypeslib.as_array(p, shape=(int(n),)).view(dtype) if n else np.zeros(0, dtype)
+
+
+class OracleProblem:
+    """Owns an orc_problem; numpy views of its arrays (valid while alive)."""
+
+    def __init__(self, params, nthreads=0):
+        self.params = params
+        self._p = lib().orc_problem_create(C.byref(params), int(nthreads))
+        P = self._p.contents
+        self.P = P
+        self.n_el, self.n_nodes, self.neq, self.n_ip = P.n_el, P.n_nodes, P.neq, P.n_ip
+        self.n_colors = P.n_colors
+        self.n_blocks = P.n_blocks
+
+    def close(self):
+        if self._p:
+            lib().orc_problem_destroy(self._p)
+            self._p = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # array views
+    def arr(self, name):
+        P = self.P
+        sizes = {"node_xy": (2 * self.n_nodes, np.float64), "connects": (9 * self.n_el, np.int32),
+                 "fixed": (self.neq, np.uint8), "f0": (self.neq, np.float64), "df": (self.neq, np.float64),
+                 "B": (486 * self.n_el, np.float64), "weight": (self.n_ip, np.float64),
+                 "dofs": (18 * self.n_el, np.int32), "el_color": (self.n_el, np.int32),
+                 "color_ptr": (self.n_colors + 1, np.int32), "color_els": (self.n_el, np.int32),
+                 "row_ptr": (self.n_nodes + 1, np.int64), "col": (self.n_blocks, np.int32),
+                 "el_blk": (81 * self.n_el, np.int64), "eps_p": (6 * self.n_ip, np.float64),
+                 "sigma": (6 * self.n_ip, np.float64), "mtype": (self.n_ip, np.int8),
+                 "alpha": (self.n_ip, np.float64), "strain": (3 * self.n_ip, np.float64),
+                 "sigma_w": (3 * self.n_ip, np.float64), "dep": (9 * self.n_ip, np.float64),
+                 "K": (4 * self.n_blocks, np.float64), "dinv": (self.neq, np.float64),
+                 "eps_p0": (6, np.float64)}
+        n, dt = sizes[name]
+        return np.ctypeslib.as_array(getattr(P, name), shape=(int(n),))
+
+    def mats(self):
+        P = self.P
+        m = np.ctypeslib.as_array(C.cast(P.mats, _dp), shape=(5 * self.n_el,)).reshape(self.n_el, 5)
+        return m  # columns: cohesion, sinphi, cosphi, tanphi, sinpsi
+
+    def assemble_residual(self, u, lam, update_mem=False):
+        rhs = np.zeros(self.neq)
+        lib().orc_assemble_residual(self._p, ptr(u), float(lam), int(update_mem), ptr(rhs))
+        return rhs
+
+    def assemble(self, u, lam):
+        rhs = np.zeros(self.neq)
+        lib().orc_assemble(self._p, ptr(u), float(lam), ptr(rhs))
+        return rhs
+
+    def spmv(self, x):
+        y = np.zeros(self.neq)
+        lib().orc_spmv(self._p, ptr(x), ptr(y))
+        return y
+
+    def pcg(self, b, rtol=1e-8, max_it=100000):
+        x = np.zeros(self.neq)
+        work = np.zeros(4 * self.neq)
+        k = lib().orc_pcg(self._p, ptr(np.ascontiguousarray(b)), ptr(x), float(rtol), int(max_it), ptr(work))
+        return x, k
+
+    def solve_steps(self, u, n_steps, step_begin=0, step_end=None, newton_rtol=1e-8, newton_max_it=20,
+                    cg_rtol=1e-8, cg_max_it=200000, log_cap=4096):
+        if step_end is None:
+            step_end = n_steps
+        o = SolveOpts(int(n_steps), float(newton_rtol), int(newton_max_it), float(cg_rtol), int(cg_max_it))
+        st = SolveStats()
+        log = np.zeros(3 * log_cap)
+        lib().orc_solve_steps(self._p, C.byref(o), int(step_begin), int(step_end), ptr(u), C.byref(st),
+                              ptr(log), int(log_cap))
+        nlog = st.newton_iters
+        return st, log[:3 * min(nlog, log_cap)].reshape(-1, 3)
+
+
+def dot(a, b):
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    b = np.ascontiguousarray(b, dtype=np.float64)
+    return lib().orc_dot(a.size // 2, ptr(a), ptr(b))

@@ -1,0 +1,93 @@
+"""The CPU oracle against the reference's own constitutive code.
+
+Golden vectors: tests/golden/constitutive.npz, produced by
+tests/golden/make_golden.py from the reference headers compiled unmodified
+(oracle/_ref).  The oracle must reproduce them bit for bit.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+import pytest
+
+from oracle import pyoracle as po
+
+GOLD = os.path.join(os.path.dirname(__file__), "golden", "constitutive.npz")
+
+
+@pytest.fixture(scope="module")
+def gold():
+    return dict(np.load(GOLD))
+
+
+def _mc(g, i):
+    m = po.MC()
+    m.cohesion, m.sinphi, m.cosphi, m.tanphi, m.sinpsi = (
+        g["cohesion"][i], g["sinphi"][i], g["cosphi"][i], g["tanphi"][i], g["sinpsi"][i])
+    return m
+
+
+def _run(g, i, dep, alias=False):
+    el = po.Elastic(g["lam"][i], g["mu"][i])
+    mc = _mc(g, i)
+    s3 = np.ascontiguousarray(g["strain3"][i])
+    p6 = np.ascontiguousarray(g["plastic6"][i])
+    sw, s6, pout, st6 = np.zeros(3), np.zeros(6), np.zeros(6), np.zeros(6)
+    d9 = np.zeros(9) if dep else None
+    mt, al = C.c_int(), C.c_double()
+    L = po.lib()
+    if alias:
+        L.orc_ip_update_gpu_alias(C.byref(el), C.byref(mc), po.ptr(s3), po.ptr(p6), g["weight"][i],
+                                  po.ptr(sw), po.ptr(s6), po.ptr(pout), C.byref(mt), C.byref(al))
+    else:
+        L.orc_ip_update(C.byref(el), C.byref(mc), po.ptr(s3), po.ptr(p6), g["weight"][i], po.ptr(sw),
+                        po.ptr(d9), po.ptr(s6), po.ptr(pout), po.ptr(st6), C.byref(mt), C.byref(al))
+    return sw, d9, s6, pout, mt.value, al.value
+
+
+def _eq(a, b):
+    """bit-level equality up to the sign of zero; NaN equals NaN (the
+    reference itself yields NaN for an exactly repeated in-plane eigenvalue,
+    FunctionsSpectralDecomp.h:203)"""
+    return np.array_equal(np.asarray(a), np.asarray(b), equal_nan=True)
+
+
+def test_golden_covers_every_branch(gold):
+    mt = gold["cpu_mtype"]
+    assert (mt == 0).sum() > 100 and (mt == 1).sum() > 100 and (mt == -1).sum() > 50
+
+
+@pytest.mark.parametrize("tag,dep", [("cpu", False), ("cpu_dep", True)])
+def test_oracle_bit_exact_vs_reference(gold, tag, dep):
+    n = len(gold["lam"])
+    bad = []
+    for i in range(n):
+        sw, d9, s6, pout, mt, al = _run(gold, i, dep)
+        ok = (_eq(sw, gold[tag + "_sigma_w3"][i]) and _eq(s6, gold[tag + "_sigma6"][i])
+              and _eq(pout, gold[tag + "_plastic6"][i]) and mt == gold[tag + "_mtype"][i]
+              and _eq(al, gold[tag + "_alpha"][i]))
+        if dep:
+            ok = ok and _eq(d9, gold["cpu_dep_dep9"][i])
+        if not ok:
+            bad.append(i)
+    assert not bad, "oracle differs from the reference at points %s" % bad[:10]
+
+
+def test_reference_gpu_kernel_aliasing_is_reproduced(gold):
+    """The reference's residual kernel aliases ProjectSigma's input and output
+    (KernelsComputeSigma.h:171); the oracle's aliased variant reproduces it,
+    and it differs from the CPU path on some edge/apex points."""
+    n = len(gold["lam"])
+    for i in range(n):
+        sw, _, s6, pout, mt, al = _run(gold, i, False, alias=True)
+        assert _eq(s6, gold["gpu_sigma6"][i]) and mt == gold["gpu_mtype"][i]
+    a, b = gold["cpu_sigma6"], gold["gpu_sigma6"]
+    differ = np.any((a != b) & ~(np.isnan(a) & np.isnan(b)), axis=1)
+    assert differ.sum() > 0
+    assert np.all(gold["cpu_mtype"][differ] != 0)
+
+
+def test_sigma_and_sigma_dep_agree(gold):
+    """ComputeSigma and ComputeSigmaDep give the same stress bit for bit."""
+    assert _eq(gold["cpu_sigma6"], gold["cpu_dep_sigma6"])
+    assert np.array_equal(gold["cpu_mtype"], gold["cpu_dep_mtype"])
