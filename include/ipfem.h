@@ -1,0 +1,197 @@
+/*
+ * ipfem.h -- C-ABI of the GB300 (sm_103a) integration-point FEM library.
+ *
+ * Drop-in boundary for the integration-point residual / tangent / Newton-CG
+ * path of labmec/IntPointsFEM.  The entry points replace the reference's
+ * TPZCudaCalls (TPZCudaCalls.h:12-51) and back the public API of
+ * TPZElastoPlasticIntPointsStructMatrix (TPZElastoPlasticIntPointsStructMatrix.h:33-42).
+ * Plain C types only: pointers, sizes, status codes.  No exceptions cross the
+ * boundary; every call returns an ipfem_status and the context keeps a
+ * message for ipfem_last_error().
+ *
+ * Memory: a context owns every device buffer it needs (the reference's
+ * TPZVecGPU members of TPZNumericalIntegrator, TPZIrregularBlocksMatrix and
+ * TPZConstitutiveLawProcessor) and one CUDA stream.  Vector arguments are
+ * host or device pointers as selected by the IPFEM_HOST / IPFEM_DEVICE flag
+ * of the call.  One context per host thread; no global mutable state.
+ *
+ * Element type: quadrilateral, order 2 (9 connects x 2 dofs), 3x3 Gauss
+ * points, plane strain.
+ */
+#ifndef IPFEM_H
+#define IPFEM_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    IPFEM_OK = 0,
+    IPFEM_NONCONVERGED = 1,   /* Newton or CG iteration limit reached */
+    IPFEM_NAN = 2,            /* non-finite value detected */
+    IPFEM_BREAKDOWN = 3,      /* CG: p.Kp <= 0 */
+    IPFEM_OOM = 4,            /* device allocation failed */
+    IPFEM_INVALID = 5,        /* bad argument / inconsistent mesh */
+    IPFEM_CUDA = 6,           /* CUDA runtime error */
+    IPFEM_NO_DEVICE = 7       /* no usable sm_100-family device */
+} ipfem_status;
+
+enum { IPFEM_HOST = 0, IPFEM_DEVICE = 1 };
+
+#define IPFEM_NPTS 9     /* integration points per element */
+#define IPFEM_NNODE 9    /* connects per element */
+#define IPFEM_NDOF 18    /* dofs per element */
+
+typedef struct ipfem_ctx ipfem_ctx;
+
+/* ------------------------------------------------------------------ mesh */
+/* Host description of the integration-point data that the reference builds
+ * in TPZElastoPlasticIntPointsStructMatrix::SetUpDataStructure
+ * (TPZElastoPlasticIntPointsStructMatrix.cpp:156-173).  All arrays are read
+ * during ipfem_create only. */
+typedef struct {
+    int32_t n_elements;
+    int32_t n_nodes;          /* connects; equations = 2*n_nodes, dof = 2*node+comp */
+    const int32_t *connects;  /* [n_elements*9] connect order of the element */
+    /* Element blocks, one of the two forms:
+     *  dphi:          [n_elements*9*2*9] d(phi_n)/d(x_d) at point q, index ((e*9+q)*2+d)*9+n
+     *  block_storage: [n_elements*27*18] the reference's fStorage, row-major
+     *                 (3*npts) x (2*nshape) (TPZNumericalIntegrator.cpp:371-386) */
+    const double *dphi;
+    const double *block_storage;
+    const double *weight;     /* [n_elements*9] w*|detJ| (TPZNumericalIntegrator.cpp:425) */
+    const uint8_t *fixed;     /* [2*n_nodes] 1 = Dirichlet dof (may be NULL) */
+    const double *f0;         /* [2*n_nodes] external load at load factor 0 (may be NULL) */
+    const double *df;         /* [2*n_nodes] external load per unit load factor (may be NULL) */
+} ipfem_mesh;
+
+/* Mohr-Coulomb / elastic material (TPZPlasticStepPV<TPZYCMohrCoulombPV,
+ * TPZElasticResponse>, main.cpp:550-561).  Per-element arrays override the
+ * uniform values when not NULL. */
+typedef struct {
+    double E, nu;
+    double cohesion, phi, psi;        /* radians */
+    const double *el_cohesion;        /* [n_elements] or NULL */
+    const double *el_phi;             /* [n_elements] or NULL; psi = phi per element */
+    double sigma0[4];                 /* in-situ stress xx, xy, yy, zz (seeded as eps_p = -C^{-1} sigma0) */
+} ipfem_material;
+
+/* ------------------------------------------------------------- lifecycle */
+ipfem_status ipfem_create(const ipfem_mesh *mesh, const ipfem_material *mat, ipfem_ctx **out);
+void ipfem_destroy(ipfem_ctx *ctx);
+const char *ipfem_last_error(const ipfem_ctx *ctx);
+const char *ipfem_status_string(ipfem_status s);
+/* sizes: n_elements, n_ip, n_nodes, neq, n_colors, n_blocks (nodal 2x2 blocks) */
+ipfem_status ipfem_sizes(const ipfem_ctx *ctx, int64_t out[6]);
+/* the context's CUDA stream (cudaStream_t), for callers that order their own work */
+void *ipfem_stream(ipfem_ctx *ctx);
+
+/* ----------------------------------- TPZElastoPlasticIntPointsStructMatrix */
+/* External load factor: rhs_linear = f0 + lambda*df (the reference's
+ * fRhsLinear, TPZElastoPlasticIntPointsStructMatrix.cpp:232-243). */
+ipfem_status ipfem_set_load_factor(ipfem_ctx *ctx, double lambda);
+/* TPZMatWithMem::SetUpdateMem: when set, the next residual commits the
+ * integration-point state (main.cpp:487-522). */
+ipfem_status ipfem_set_update_mem(ipfem_ctx *ctx, int update);
+/* Assemble(rhs) (TPZElastoPlasticIntPointsStructMatrix.cpp:213-230):
+ * rhs = -B^T sigma(u) + rhs_linear, Dirichlet rows zeroed. */
+ipfem_status ipfem_assemble_residual(ipfem_ctx *ctx, const double *u, double *rhs, int where);
+/* Assemble(K, rhs) (TPZElastoPlasticIntPointsStructMatrix.cpp:175-211):
+ * rhs as above; the tangent K stays on the device for ipfem_solve. */
+ipfem_status ipfem_assemble(ipfem_ctx *ctx, const double *u, double *rhs, int where);
+/* K as nodal 2x2 blocks, rows ascending, columns ascending per row:
+ * row_ptr[n_nodes+1], col[n_blocks], vals[4*n_blocks] (row-major blocks). */
+ipfem_status ipfem_get_stiffness(ipfem_ctx *ctx, int64_t *row_ptr, int32_t *col, double *vals);
+/* Jacobi-preconditioned CG on the current K (replaces the reference's
+ * TPZCudaCalls::SolveCG, TPZCudaCalls.cu:213-290, and the Pardiso solve):
+ * stops when |r|^2 <= rtol^2 |b|^2.  *iters receives the iteration count. */
+ipfem_status ipfem_solve(ipfem_ctx *ctx, const double *b, double *x, double rtol, int max_it,
+                         int where, int *iters);
+
+/* Newton with load stepping (main.cpp:160-262 per step, accept main.cpp:487-522). */
+typedef struct {
+    int32_t n_steps;
+    double newton_rtol;       /* |R| <= newton_rtol |R_0| per step */
+    int32_t newton_max_it;
+    double cg_rtol;
+    int32_t cg_max_it;
+} ipfem_solve_opts;
+
+typedef struct {
+    int32_t newton_iters;
+    int64_t cg_iters;
+    int32_t last_step_iters;
+    int32_t converged;
+    double final_res;
+    double ms_assemble, ms_solve, ms_commit;
+} ipfem_solve_stats;
+
+/* Runs steps [step_begin, step_end); u (neq, host or device per `where`)
+ * holds the displacement on entry and exit.  log (3 doubles per Newton
+ * iteration: step, cg iterations, |R|) may be NULL. */
+ipfem_status ipfem_newton_solve(ipfem_ctx *ctx, const ipfem_solve_opts *opts, int32_t step_begin,
+                                int32_t step_end, double *u, int where, ipfem_solve_stats *stats,
+                                double *log, int32_t log_cap);
+
+/* ------------------------------------------------ TPZCudaCalls replacements */
+/* TPZNumericalIntegrator::Multiply (TPZNumericalIntegrator.cpp:25-37):
+ * gather + B*u.  d_strain: device, SoA [3][n_ip] (eps_xx, gamma_xy, eps_yy). */
+ipfem_status ipfem_gather_strain(ipfem_ctx *ctx, const double *d_u, double *d_strain);
+/* TPZCudaCalls::ComputeSigma / ComputeSigmaDep (TPZCudaCalls.cu:165-191):
+ * d_sigma_w SoA [3][n_ip]; d_dep SoA [9][n_ip] or NULL (no tangent).  Uses
+ * and, if update_mem, commits the context's integration-point state. */
+ipfem_status ipfem_compute_sigma(ipfem_ctx *ctx, int update_mem, const double *d_strain,
+                                 double *d_sigma_w, double *d_dep);
+/* TPZNumericalIntegrator::MultiplyTranspose (TPZNumericalIntegrator.cpp:54-78):
+ * -B^T sigma_w, scattered and reduced over colours (no load, no masking). */
+ipfem_status ipfem_scatter_residual(ipfem_ctx *ctx, const double *d_sigma_w, double *d_res);
+
+/* Integration-point state (TPZConstitutiveLawProcessor members), host copies.
+ * field: 0 plastic strain [4][n_ip] (xx, xy, yy, zz), 1 stress [4][n_ip],
+ *        2 alpha [n_ip], 3 m_type as double [n_ip]. */
+ipfem_status ipfem_get_state(ipfem_ctx *ctx, int field, double *out);
+ipfem_status ipfem_set_state(ipfem_ctx *ctx, int field, const double *in);
+
+/* Setup arrays computed by the library (for verification):
+ * field 0 element colour [n_elements] int32, 1 number of colours (int32),
+ * 2 dof indexes [n_elements*18] int32 (fDoFIndexes),
+ * 3 dphi [n_elements*162] double, 4 weights [n_ip] double. */
+ipfem_status ipfem_get_setup(ipfem_ctx *ctx, int field, void *out);
+
+/* --------------------------------------------------- wellbore mesh provider */
+/* Structured quarter annulus standing in for the reference's NeoPZ/Gmsh mesh
+ * (main.cpp:447-464, 542-607): nr x nt order-2 quads, radial grading,
+ * in-situ stress sigma0 on the outer arc, well traction ramped from sigma0
+ * to pw_final*I, symmetry u_y = 0 on y = 0 and u_x = 0 on x = 0. */
+typedef struct {
+    int32_t nr, nt;
+    double r_in, r_out, grading;
+    double E, nu, cohesion, phi_deg, psi_deg;
+    double sxx0, syy0, sxy0, szz0;
+    double pw_final;
+    int32_t material_mode;    /* 0 uniform, 1 lognormal cohesion, 2 + uniform friction angle */
+    double c_cv, phi_lo_deg, phi_hi_deg;
+    uint64_t seed;
+} ipfem_wellbore_params;
+
+typedef struct {
+    ipfem_mesh mesh;
+    ipfem_material material;
+    double *node_xy;          /* [n_nodes*2] */
+    /* owned storage behind mesh / material */
+    int32_t *connects;
+    double *dphi, *weight, *f0, *df, *el_cohesion, *el_phi;
+    uint8_t *fixed;
+} ipfem_wellbore;
+
+void ipfem_wellbore_default(ipfem_wellbore_params *p, int32_t n);
+ipfem_status ipfem_wellbore_build(const ipfem_wellbore_params *p, ipfem_wellbore **out);
+void ipfem_wellbore_free(ipfem_wellbore *w);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* IPFEM_H */

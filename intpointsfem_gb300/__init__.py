@@ -1,0 +1,315 @@
+"""GB300-native integration-point FEM: Python view of libipfem's C-ABI.
+
+The compute path is libipfem.so (hand-written sm_103a CUDA behind the C-ABI
+of include/ipfem.h).  This module only binds it with ctypes and mirrors the
+reference's TPZElastoPlasticIntPointsStructMatrix interface
+(TPZElastoPlasticIntPointsStructMatrix.h:33-42) so that tests and benchmarks
+read like the reference's own calls.  There is no CPU fallback: if the
+library or a device is missing, every entry point raises.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libipfem.so")
+
+HOST, DEVICE = 0, 1
+STATUS = {0: "ok", 1: "not converged", 2: "non-finite value", 3: "CG breakdown", 4: "out of device memory",
+          5: "invalid argument", 6: "CUDA error", 7: "no sm_103 device"}
+
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int32)
+_lp = C.POINTER(C.c_int64)
+_bp = C.POINTER(C.c_uint8)
+
+
+class IpfemError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__("ipfem: %s (%d): %s" % (STATUS.get(status, "?"), status, msg))
+        self.status = status
+
+
+class Mesh(C.Structure):
+    _fields_ = [("n_elements", C.c_int32), ("n_nodes", C.c_int32), ("connects", _ip), ("dphi", _dp),
+                ("block_storage", _dp), ("weight", _dp), ("fixed", _bp), ("f0", _dp), ("df", _dp)]
+
+
+class Material(C.Structure):
+    _fields_ = [("E", C.c_double), ("nu", C.c_double), ("cohesion", C.c_double), ("phi", C.c_double),
+                ("psi", C.c_double), ("el_cohesion", _dp), ("el_phi", _dp), ("sigma0", C.c_double * 4)]
+
+
+class SolveOpts(C.Structure):
+    _fields_ = [("n_steps", C.c_int32), ("newton_rtol", C.c_double), ("newton_max_it", C.c_int32),
+                ("cg_rtol", C.c_double), ("cg_max_it", C.c_int32)]
+
+
+class SolveStats(C.Structure):
+    _fields_ = [("newton_iters", C.c_int32), ("cg_iters", C.c_int64), ("last_step_iters", C.c_int32),
+                ("converged", C.c_int32), ("final_res", C.c_double), ("ms_assemble", C.c_double),
+                ("ms_solve", C.c_double), ("ms_commit", C.c_double)]
+
+
+class WellboreParams(C.Structure):
+    _fields_ = [("nr", C.c_int32), ("nt", C.c_int32), ("r_in", C.c_double), ("r_out", C.c_double),
+                ("grading", C.c_double), ("E", C.c_double), ("nu", C.c_double), ("cohesion", C.c_double),
+                ("phi_deg", C.c_double), ("psi_deg", C.c_double), ("sxx0", C.c_double), ("syy0", C.c_double),
+                ("sxy0", C.c_double), ("szz0", C.c_double), ("pw_final", C.c_double),
+                ("material_mode", C.c_int32), ("c_cv", C.c_double), ("phi_lo_deg", C.c_double),
+                ("phi_hi_deg", C.c_double), ("seed", C.c_uint64)]
+
+
+class Wellbore(C.Structure):
+    _fields_ = [("mesh", Mesh), ("material", Material), ("node_xy", _dp), ("connects", _ip), ("dphi", _dp),
+                ("weight", _dp), ("f0", _dp), ("df", _dp), ("el_cohesion", _dp), ("el_phi", _dp),
+                ("fixed", _bp)]
+
+
+_lib = None
+
+
+def lib():
+    """Load libipfem.so (in-tree build); raises if it is not built."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError("libipfem.so is not built; run intpointsfem_gb300.build.build()")
+        L = C.CDLL(LIB_PATH)
+        S = C.c_int
+        P = C.c_void_p
+        sig = {
+            "ipfem_create": (S, [C.POINTER(Mesh), C.POINTER(Material), C.POINTER(P)]),
+            "ipfem_destroy": (None, [P]),
+            "ipfem_last_error": (C.c_char_p, [P]),
+            "ipfem_status_string": (C.c_char_p, [S]),
+            "ipfem_sizes": (S, [P, _lp]),
+            "ipfem_stream": (P, [P]),
+            "ipfem_set_load_factor": (S, [P, C.c_double]),
+            "ipfem_set_update_mem": (S, [P, S]),
+            "ipfem_assemble_residual": (S, [P, P, P, S]),
+            "ipfem_assemble": (S, [P, P, P, S]),
+            "ipfem_get_stiffness": (S, [P, _lp, _ip, _dp]),
+            "ipfem_solve": (S, [P, P, P, C.c_double, S, S, C.POINTER(C.c_int)]),
+            "ipfem_newton_solve": (S, [P, C.POINTER(SolveOpts), C.c_int32, C.c_int32, P, S,
+                                       C.POINTER(SolveStats), _dp, C.c_int32]),
+            "ipfem_gather_strain": (S, [P, P, P]),
+            "ipfem_compute_sigma": (S, [P, S, P, P, P]),
+            "ipfem_scatter_residual": (S, [P, P, P]),
+            "ipfem_get_state": (S, [P, S, _dp]),
+            "ipfem_set_state": (S, [P, S, _dp]),
+            "ipfem_get_setup": (S, [P, S, P]),
+            "ipfem_wellbore_default": (None, [C.POINTER(WellboreParams), C.c_int32]),
+            "ipfem_wellbore_build": (S, [C.POINTER(WellboreParams), C.POINTER(C.POINTER(Wellbore))]),
+            "ipfem_wellbore_free": (None, [C.POINTER(Wellbore)]),
+        }
+        for name, (res, args) in sig.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = L
+    return _lib
+
+
+def _ptr(a):
+    """address of a numpy array or torch tensor (host or device)"""
+    if a is None:
+        return None
+    if hasattr(a, "data_ptr"):
+        return C.c_void_p(a.data_ptr())
+    assert a.flags["C_CONTIGUOUS"]
+    return C.c_void_p(a.ctypes.data)
+
+
+def _np_ptr(a, t):
+    return a.ctypes.data_as(t)
+
+
+def wellbore_params(n, **kw):
+    p = WellboreParams()
+    lib().ipfem_wellbore_default(C.byref(p), int(n))
+    for k, v in kw.items():
+        setattr(p, k, v)
+    return p
+
+
+class WellboreMesh:
+    """Quarter-annulus wellbore mesh provider (stand-in for the NeoPZ mesh)."""
+
+    def __init__(self, params):
+        self.params = params
+        self._w = C.POINTER(Wellbore)()
+        st = lib().ipfem_wellbore_build(C.byref(params), C.byref(self._w))
+        if st != 0:
+            raise IpfemError(st, "wellbore mesh build failed")
+        w = self._w.contents
+        self.n_el = w.mesh.n_elements
+        self.n_nodes = w.mesh.n_nodes
+        self.neq = 2 * self.n_nodes
+
+    @property
+    def mesh(self):
+        return self._w.contents.mesh
+
+    @property
+    def material(self):
+        return self._w.contents.material
+
+    def array(self, name):
+        w = self._w.contents
+        n = {"node_xy": 2 * self.n_nodes, "connects": 9 * self.n_el, "dphi": 162 * self.n_el,
+             "weight": 9 * self.n_el, "f0": self.neq, "df": self.neq, "fixed": self.neq,
+             "el_cohesion": self.n_el, "el_phi": self.n_el}[name]
+        p = getattr(w, name)
+        if not p:
+            return None
+        return np.ctypeslib.as_array(p, shape=(n,))
+
+    def close(self):
+        if self._w:
+            lib().ipfem_wellbore_free(self._w)
+            self._w = C.POINTER(Wellbore)()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class ElastoPlasticIntPointsStructMatrix:
+    """Mirror of TPZElastoPlasticIntPointsStructMatrix over one ipfem context.
+
+    Create()/CreateAssemble(rhs) build the integration-point data once;
+    Assemble(K, rhs) computes tangent + residual, Assemble(rhs) the residual
+    (TPZElastoPlasticIntPointsStructMatrix.cpp:110-230).  The solution vector
+    that the reference reads from the PZ mesh is passed explicitly.
+    """
+
+    def __init__(self, mesh, material=None, keep=None):
+        if isinstance(mesh, WellboreMesh):
+            keep, material, mesh = mesh, mesh.material, mesh.mesh
+        self._keep = keep
+        self._mesh = mesh
+        self._material = material
+        self._ctx = C.c_void_p()
+        st = lib().ipfem_create(C.byref(mesh), C.byref(material), C.byref(self._ctx))
+        if st != 0:
+            msg = lib().ipfem_last_error(self._ctx).decode() if self._ctx else ""
+            raise IpfemError(st, msg or "ipfem_create failed")
+        sz = np.zeros(6, np.int64)
+        lib().ipfem_sizes(self._ctx, _np_ptr(sz, _lp))
+        self.n_el, self.n_ip, self.n_nodes, self.neq, self.n_colors, self.n_blocks = map(int, sz)
+        self.u = np.zeros(self.neq)   # the solution the reference reads from fMesh->Solution()
+
+    def _check(self, st):
+        if st != 0:
+            raise IpfemError(st, lib().ipfem_last_error(self._ctx).decode())
+
+    def close(self):
+        if self._ctx:
+            lib().ipfem_destroy(self._ctx)
+            self._ctx = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # -- reference API --------------------------------------------------
+    def Create(self):
+        return self
+
+    def CreateAssemble(self, rhs):
+        self.Assemble(self, rhs)
+        return self
+
+    def Clone(self):
+        return ElastoPlasticIntPointsStructMatrix(self._mesh, self._material, self._keep)
+
+    def Assemble(self, *args):
+        """Assemble(K, rhs) or Assemble(rhs); rhs is filled in place."""
+        if len(args) == 2:
+            _, rhs = args
+            self._check(lib().ipfem_assemble(self._ctx, _ptr(self.u), _ptr(rhs), HOST))
+        else:
+            (rhs,) = args
+            self._check(lib().ipfem_assemble_residual(self._ctx, _ptr(self.u), _ptr(rhs), HOST))
+        return rhs
+
+    def SetUpdateMem(self, flag):
+        self._check(lib().ipfem_set_update_mem(self._ctx, int(bool(flag))))
+
+    def SetLoadFactor(self, lam):
+        self._check(lib().ipfem_set_load_factor(self._ctx, float(lam)))
+
+    # -- extras -----------------------------------------------------------
+    def assemble_residual(self, u, rhs, where=HOST):
+        self._check(lib().ipfem_assemble_residual(self._ctx, _ptr(u), _ptr(rhs), where))
+        return rhs
+
+    def assemble(self, u, rhs, where=HOST):
+        self._check(lib().ipfem_assemble(self._ctx, _ptr(u), _ptr(rhs), where))
+        return rhs
+
+    def stiffness(self):
+        rp = np.zeros(self.n_nodes + 1, np.int64)
+        col = np.zeros(self.n_blocks, np.int32)
+        val = np.zeros(4 * self.n_blocks)
+        self._check(lib().ipfem_get_stiffness(self._ctx, _np_ptr(rp, _lp), _np_ptr(col, _ip), _np_ptr(val, _dp)))
+        return rp, col, val
+
+    def solve(self, b, x=None, rtol=1e-8, max_it=200000, where=HOST, allow_nonconverged=False):
+        if x is None:
+            x = np.zeros(self.neq)
+        it = C.c_int()
+        st = lib().ipfem_solve(self._ctx, _ptr(b), _ptr(x), float(rtol), int(max_it), where, C.byref(it))
+        if not (allow_nonconverged and st == 1):
+            self._check(st)
+        return x, it.value
+
+    def newton(self, u, n_steps, step_begin=0, step_end=None, newton_rtol=1e-8, newton_max_it=20, cg_rtol=1e-8,
+               cg_max_it=200000, where=HOST, log_cap=4096, allow_nonconverged=True):
+        if step_end is None:
+            step_end = n_steps
+        o = SolveOpts(int(n_steps), float(newton_rtol), int(newton_max_it), float(cg_rtol), int(cg_max_it))
+        st = SolveStats()
+        log = np.zeros(3 * log_cap)
+        s = lib().ipfem_newton_solve(self._ctx, C.byref(o), int(step_begin), int(step_end), _ptr(u), where,
+                                     C.byref(st), _np_ptr(log, _dp), int(log_cap))
+        if not (allow_nonconverged and s == 1):
+            self._check(s)
+        return st, log[:3 * min(st.newton_iters, log_cap)].reshape(-1, 3)
+
+    def gather_strain(self, d_u, d_strain):
+        self._check(lib().ipfem_gather_strain(self._ctx, _ptr(d_u), _ptr(d_strain)))
+
+    def compute_sigma(self, update_mem, d_strain, d_sigma_w, d_dep=None):
+        self._check(lib().ipfem_compute_sigma(self._ctx, int(update_mem), _ptr(d_strain), _ptr(d_sigma_w),
+                                              _ptr(d_dep)))
+
+    def scatter_residual(self, d_sigma_w, d_res):
+        self._check(lib().ipfem_scatter_residual(self._ctx, _ptr(d_sigma_w), _ptr(d_res)))
+
+    def get_state(self, field):
+        n = {0: 4 * self.n_ip, 1: 4 * self.n_ip, 2: self.n_ip, 3: self.n_ip}[field]
+        out = np.zeros(n)
+        self._check(lib().ipfem_get_state(self._ctx, int(field), _np_ptr(out, _dp)))
+        return out
+
+    def set_state(self, field, arr):
+        arr = np.ascontiguousarray(arr, dtype=np.float64)
+        self._check(lib().ipfem_set_state(self._ctx, int(field), _np_ptr(arr, _dp)))
+
+    def get_setup(self, field):
+        spec = {0: (self.n_el, np.int32), 1: (1, np.int32), 2: (18 * self.n_el, np.int32),
+                3: (162 * self.n_el, np.float64), 4: (self.n_ip, np.float64)}[field]
+        out = np.zeros(spec[0], spec[1])
+        self._check(lib().ipfem_get_setup(self._ctx, int(field), C.c_void_p(out.ctypes.data)))
+        return out
+
+    @property
+    def stream(self):
+        return lib().ipfem_stream(self._ctx)

@@ -1,0 +1,536 @@
+// C-ABI of libipfem: context lifecycle, the TPZElastoPlasticIntPointsStructMatrix
+// calls (Assemble(rhs), Assemble(K, rhs)), the CG solve, the Newton driver of
+// main.cpp, and the kernel-level replacements of TPZCudaCalls.
+#include <cmath>
+#include <cstring>
+#include <new>
+
+#include "ipfem_internal.h"
+
+using namespace ipfem;
+
+namespace {
+
+ipfem_status fail(ipfem_ctx *c, ipfem_status s, const std::string &msg)
+{
+    if (c) c->err = msg;
+    return s;
+}
+
+#define CK(expr)                                                                          \
+    do {                                                                                  \
+        cudaError_t e_ = (expr);                                                          \
+        if (e_ != cudaSuccess)                                                            \
+            return fail(c, e_ == cudaErrorMemoryAllocation ? IPFEM_OOM : IPFEM_CUDA,      \
+                        std::string(#expr) + ": " + cudaGetErrorString(e_));              \
+    } while (0)
+
+template <class T>
+cudaError_t dalloc(T **p, size_t n)
+{
+    *p = nullptr;
+    return cudaMalloc((void **)p, (n ? n : 1) * sizeof(T));
+}
+
+template <class T>
+cudaError_t upload(T **p, const std::vector<T> &v, cudaStream_t st)
+{
+    cudaError_t e = dalloc(p, v.size());
+    if (e != cudaSuccess || v.empty()) return e;
+    return cudaMemcpyAsync(*p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, st);
+}
+
+void free_all(ipfem_ctx *c)
+{
+    void *ptrs[] = {c->d_dphi, c->d_weight, c->d_mat, c->d_f0, c->d_df, c->d_dofs, c->d_color_els, c->d_inc,
+                    c->d_fixed, c->d_slice_base, c->d_diag_blk, c->d_sell_col, c->d_rowlen, c->d_el_blk, c->d_K,
+                    c->d_dinv, c->d_eps_p, c->d_sigma, c->d_alpha, c->d_mtype, c->d_u, c->d_rhs, c->d_strain,
+                    c->d_sigma_w, c->d_dep, c->d_fe, c->d_x, c->d_r, c->d_z, c->d_p, c->d_q, c->d_b, c->d_part,
+                    c->d_sc, c->d_counters, c->d_dotres, c->d_err};
+    for (void *p : ptrs)
+        if (p) cudaFree(p);
+    if (c->h_sc) cudaFreeHost(c->h_sc);
+    if (c->h_pin) cudaFreeHost(c->h_pin);
+    if (c->cg_exec) cudaGraphExecDestroy(c->cg_exec);
+    if (c->stream) cudaStreamDestroy(c->stream);
+}
+
+// launch-error and device-error-word check after a synchronisation point
+ipfem_status check_device(ipfem_ctx *c)
+{
+    CK(cudaGetLastError());
+    int err = 0;
+    CK(cudaMemcpyAsync(&c->h_pin[7], c->d_err, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    std::memcpy(&err, &c->h_pin[7], sizeof(int));
+    if (err) return fail(c, IPFEM_CUDA, "device wait timed out (bulk copy did not complete)");
+    return IPFEM_OK;
+}
+
+ipfem_status sync_check(ipfem_ctx *c)
+{
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(c->stream));
+    return check_device(c);
+}
+
+// residual of the current load factor at d_u into d_out (device)
+void residual_device(ipfem_ctx *c, const double *d_u, double *d_out, int update_mem)
+{
+    launch_gather_strain(c, d_u, c->d_strain);
+    launch_compute_sigma(c, update_mem, c->d_strain, c->d_sigma_w, nullptr);
+    launch_stress_residual(c, c->d_sigma_w, c->d_fe);
+    launch_color_reduce(c, c->d_fe, c->load_factor, 1, d_out);
+}
+
+void tangent_device(ipfem_ctx *c, const double *d_u, double *d_out, int update_mem)
+{
+    launch_gather_strain(c, d_u, c->d_strain);
+    launch_compute_sigma(c, update_mem, c->d_strain, c->d_sigma_w, c->d_dep);
+    launch_stress_residual(c, c->d_sigma_w, c->d_fe);
+    launch_color_reduce(c, c->d_fe, c->load_factor, 1, d_out);
+    launch_stiffness(c);
+    c->tangent_valid = true;
+}
+
+// CG on the current K with right-hand side d_b (device); solution in c->d_x
+ipfem_status cg_device(ipfem_ctx *c, const double *d_b, double rtol, int max_it, int *iters)
+{
+    launch_cg_init(c, d_b, rtol, max_it);
+    const int batch = 32;
+    if (!c->cg_exec || c->cg_batch != batch) {
+        if (c->cg_exec) {
+            cudaGraphExecDestroy(c->cg_exec);
+            c->cg_exec = nullptr;
+        }
+        cudaGraph_t g = nullptr;
+        CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+        for (int k = 0; k < batch; k++) launch_cg_iteration(c);
+        CK(cudaStreamEndCapture(c->stream, &g));
+        cudaError_t e = cudaGraphInstantiate(&c->cg_exec, g, 0);
+        cudaGraphDestroy(g);
+        CK(e);
+        c->cg_batch = batch;
+    }
+    int launched = 0;
+    for (;;) {
+        CK(cudaGraphLaunch(c->cg_exec, c->stream));
+        launched += batch;
+        CK(cudaMemcpyAsync(c->h_sc, c->d_sc, sizeof(CGScalars), cudaMemcpyDeviceToHost, c->stream));
+        CK(cudaStreamSynchronize(c->stream));
+        if (c->h_sc->done || launched >= max_it + batch) break;
+    }
+    if (iters) *iters = c->h_sc->iters;
+    ipfem_status st = check_device(c);
+    if (st != IPFEM_OK) return st;
+    if (!c->h_sc->done) return fail(c, IPFEM_NONCONVERGED, "CG did not finish");
+    if (c->h_sc->status == IPFEM_BREAKDOWN) return fail(c, IPFEM_BREAKDOWN, "CG breakdown: p.Kp <= 0");
+    if (c->h_sc->status == IPFEM_NONCONVERGED) return fail(c, IPFEM_NONCONVERGED, "CG reached max_it");
+    if (!std::isfinite(c->h_sc->rr)) return fail(c, IPFEM_NAN, "CG residual is not finite");
+    return IPFEM_OK;
+}
+
+// |v|^2 (canonical order) of a device vector, to the host
+ipfem_status dot_host(ipfem_ctx *c, const double *a, const double *b, double *out)
+{
+    launch_dot(c, a, b, c->d_dotres);
+    CK(cudaMemcpyAsync(&c->h_pin[0], c->d_dotres, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    *out = c->h_pin[0];
+    return IPFEM_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *ipfem_status_string(ipfem_status s)
+{
+    switch (s) {
+    case IPFEM_OK: return "ok";
+    case IPFEM_NONCONVERGED: return "not converged";
+    case IPFEM_NAN: return "non-finite value";
+    case IPFEM_BREAKDOWN: return "CG breakdown";
+    case IPFEM_OOM: return "out of device memory";
+    case IPFEM_INVALID: return "invalid argument";
+    case IPFEM_CUDA: return "CUDA error";
+    case IPFEM_NO_DEVICE: return "no sm_103 device";
+    }
+    return "unknown";
+}
+
+const char *ipfem_last_error(const ipfem_ctx *c)
+{
+    return c ? c->err.c_str() : "null context";
+}
+
+void *ipfem_stream(ipfem_ctx *c)
+{
+    return c ? (void *)c->stream : nullptr;
+}
+
+ipfem_status ipfem_create(const ipfem_mesh *mesh, const ipfem_material *mat, ipfem_ctx **out)
+{
+    if (!out) return IPFEM_INVALID;
+    *out = nullptr;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        cudaGetLastError();
+        return IPFEM_NO_DEVICE;
+    }
+    ipfem_ctx *c = new (std::nothrow) ipfem_ctx();
+    if (!c) return IPFEM_OOM;
+    ipfem_status st = IPFEM_OK;
+    auto bail = [&](ipfem_status s) {
+        free_all(c);
+        delete c;
+        return s;
+    };
+    cudaGetDevice(&c->device);
+    cudaDeviceProp prop;
+    if (cudaGetDeviceProperties(&prop, c->device) != cudaSuccess || prop.major != 10 || prop.minor != 3)
+        return bail(IPFEM_NO_DEVICE);
+    std::string msg = build_setup(mesh, mat, c->s);
+    if (!msg.empty()) {
+        c->err = msg;
+        return bail(IPFEM_INVALID);
+    }
+    const Setup &s = c->s;
+    auto ck = [&](cudaError_t e) {
+        if (e != cudaSuccess && st == IPFEM_OK) st = (e == cudaErrorMemoryAllocation) ? IPFEM_OOM : IPFEM_CUDA;
+    };
+    ck(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+    if (st != IPFEM_OK) return bail(st);
+    cudaStream_t t = c->stream;
+    ck(upload(&c->d_dphi, s.dphi, t));
+    ck(upload(&c->d_weight, s.weight, t));
+    ck(upload(&c->d_mat, s.mat, t));
+    ck(upload(&c->d_f0, s.f0, t));
+    ck(upload(&c->d_df, s.df, t));
+    ck(upload(&c->d_dofs, s.dofs, t));
+    ck(upload(&c->d_color_els, s.color_els, t));
+    ck(upload(&c->d_inc, s.inc, t));
+    ck(upload(&c->d_fixed, s.fixed, t));
+    ck(upload(&c->d_slice_base, s.slice_base, t));
+    ck(upload(&c->d_diag_blk, s.diag_blk, t));
+    ck(upload(&c->d_sell_col, s.sell_col, t));
+    ck(upload(&c->d_rowlen, s.rowlen, t));
+    ck(upload(&c->d_el_blk, s.el_blk, t));
+    ck(dalloc(&c->d_K, (size_t)s.n_sell * 4));
+    ck(dalloc(&c->d_dinv, (size_t)s.neq));
+    ck(dalloc(&c->d_eps_p, (size_t)s.n_ip * 4));
+    ck(dalloc(&c->d_sigma, (size_t)s.n_ip * 4));
+    ck(dalloc(&c->d_alpha, (size_t)s.n_ip));
+    ck(dalloc(&c->d_mtype, (size_t)s.n_ip));
+    ck(dalloc(&c->d_u, (size_t)s.neq));
+    ck(dalloc(&c->d_rhs, (size_t)s.neq));
+    ck(dalloc(&c->d_strain, (size_t)s.n_ip * 3));
+    ck(dalloc(&c->d_sigma_w, (size_t)s.n_ip * 3));
+    ck(dalloc(&c->d_dep, (size_t)s.n_ip * 9));
+    ck(dalloc(&c->d_fe, (size_t)s.n_el * 18));
+    ck(dalloc(&c->d_x, (size_t)s.neq));
+    ck(dalloc(&c->d_r, (size_t)s.neq));
+    ck(dalloc(&c->d_z, (size_t)s.neq));
+    ck(dalloc(&c->d_p, (size_t)s.neq));
+    ck(dalloc(&c->d_q, (size_t)s.neq));
+    ck(dalloc(&c->d_b, (size_t)s.neq));
+    c->n_red = (s.n_nodes + kRedBlock - 1) / kRedBlock;
+    ck(dalloc(&c->d_part, (size_t)c->n_red * 3));
+    ck(dalloc(&c->d_sc, 1));
+    ck(dalloc(&c->d_counters, 8));
+    ck(dalloc(&c->d_dotres, 8));
+    ck(dalloc(&c->d_err, 1));
+    ck(cudaMallocHost((void **)&c->h_sc, sizeof(CGScalars)));
+    ck(cudaMallocHost((void **)&c->h_pin, 16 * sizeof(double)));
+    if (st != IPFEM_OK) {
+        c->err = "device allocation failed";
+        return bail(st);
+    }
+    ck(cudaMemsetAsync(c->d_counters, 0, 8 * sizeof(unsigned), t));
+    ck(cudaMemsetAsync(c->d_err, 0, sizeof(int), t));
+    ck(cudaMemsetAsync(c->d_sc, 0, sizeof(CGScalars), t));
+    ck(cudaMemsetAsync(c->d_u, 0, (size_t)s.neq * sizeof(double), t));
+    ck(cudaMemsetAsync(c->d_K, 0, (size_t)s.n_sell * 4 * sizeof(double), t));
+    ck(cudaMemsetAsync(c->d_dinv, 0, (size_t)s.neq * sizeof(double), t));
+    // initial state: in-situ seed
+    {
+        std::vector<double> h((size_t)s.n_ip * 4);
+        for (int k = 0; k < 4; k++) std::fill(h.begin() + k * s.n_ip, h.begin() + (k + 1) * s.n_ip, s.eps_p0[k]);
+        ck(cudaMemcpyAsync(c->d_eps_p, h.data(), h.size() * sizeof(double), cudaMemcpyHostToDevice, t));
+        ck(cudaStreamSynchronize(t));
+        for (int k = 0; k < 4; k++) std::fill(h.begin() + k * s.n_ip, h.begin() + (k + 1) * s.n_ip, s.sigma0[k]);
+        ck(cudaMemcpyAsync(c->d_sigma, h.data(), h.size() * sizeof(double), cudaMemcpyHostToDevice, t));
+        ck(cudaMemsetAsync(c->d_alpha, 0, (size_t)s.n_ip * sizeof(double), t));
+        ck(cudaMemsetAsync(c->d_mtype, 0, (size_t)s.n_ip, t));
+        ck(cudaStreamSynchronize(t));
+    }
+    if (st != IPFEM_OK) {
+        c->err = "device initialisation failed";
+        return bail(st);
+    }
+    *out = c;
+    return IPFEM_OK;
+}
+
+void ipfem_destroy(ipfem_ctx *c)
+{
+    if (!c) return;
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    free_all(c);
+    delete c;
+}
+
+ipfem_status ipfem_sizes(const ipfem_ctx *c, int64_t out[6])
+{
+    if (!c || !out) return IPFEM_INVALID;
+    out[0] = c->s.n_el;
+    out[1] = c->s.n_ip;
+    out[2] = c->s.n_nodes;
+    out[3] = c->s.neq;
+    out[4] = c->s.n_colors;
+    out[5] = c->s.n_blocks;
+    return IPFEM_OK;
+}
+
+ipfem_status ipfem_set_load_factor(ipfem_ctx *c, double lambda)
+{
+    if (!c || !std::isfinite(lambda)) return IPFEM_INVALID;
+    c->load_factor = lambda;
+    return IPFEM_OK;
+}
+
+ipfem_status ipfem_set_update_mem(ipfem_ctx *c, int update)
+{
+    if (!c) return IPFEM_INVALID;
+    c->update_mem = update ? 1 : 0;
+    return IPFEM_OK;
+}
+
+static ipfem_status assemble_common(ipfem_ctx *c, const double *u, double *rhs, int where, bool tangent)
+{
+    if (!c || !u || !rhs || (where != IPFEM_HOST && where != IPFEM_DEVICE)) return fail(c, IPFEM_INVALID, "bad args");
+    const size_t nb = (size_t)c->s.neq * sizeof(double);
+    const double *du = u;
+    double *dr = rhs;
+    if (where == IPFEM_HOST) {
+        CK(cudaMemcpyAsync(c->d_u, u, nb, cudaMemcpyHostToDevice, c->stream));
+        du = c->d_u;
+        dr = c->d_rhs;
+    }
+    if (tangent) tangent_device(c, du, dr, c->update_mem);
+    else residual_device(c, du, dr, c->update_mem);
+    if (where == IPFEM_HOST) CK(cudaMemcpyAsync(rhs, dr, nb, cudaMemcpyDeviceToHost, c->stream));
+    return sync_check(c);
+}
+
+ipfem_status ipfem_assemble_residual(ipfem_ctx *c, const double *u, double *rhs, int where)
+{
+    return assemble_common(c, u, rhs, where, false);
+}
+
+ipfem_status ipfem_assemble(ipfem_ctx *c, const double *u, double *rhs, int where)
+{
+    return assemble_common(c, u, rhs, where, true);
+}
+
+ipfem_status ipfem_get_stiffness(ipfem_ctx *c, int64_t *row_ptr, int32_t *col, double *vals)
+{
+    if (!c) return IPFEM_INVALID;
+    const Setup &s = c->s;
+    if (row_ptr) std::memcpy(row_ptr, s.row_ptr.data(), s.row_ptr.size() * sizeof(int64_t));
+    if (col) std::memcpy(col, s.col.data(), s.col.size() * sizeof(int32_t));
+    if (vals) {
+        std::vector<double> h((size_t)s.n_sell * 4);
+        CK(cudaMemcpyAsync(h.data(), c->d_K, h.size() * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+        CK(cudaStreamSynchronize(c->stream));
+        for (int64_t k = 0; k < s.n_blocks; k++)
+            std::memcpy(vals + 4 * k, h.data() + 4 * s.bsr_to_sell[k], 4 * sizeof(double));
+    }
+    return IPFEM_OK;
+}
+
+ipfem_status ipfem_solve(ipfem_ctx *c, const double *b, double *x, double rtol, int max_it, int where, int *iters)
+{
+    if (!c || !b || !x || !(rtol >= 0) || (where != IPFEM_HOST && where != IPFEM_DEVICE))
+        return fail(c, IPFEM_INVALID, "bad args");
+    if (!c->tangent_valid) return fail(c, IPFEM_INVALID, "no tangent assembled");
+    const size_t nb = (size_t)c->s.neq * sizeof(double);
+    const double *db = b;
+    if (where == IPFEM_HOST) {
+        CK(cudaMemcpyAsync(c->d_b, b, nb, cudaMemcpyHostToDevice, c->stream));
+        db = c->d_b;
+    }
+    ipfem_status st = cg_device(c, db, rtol, max_it, iters);
+    if (where == IPFEM_HOST) CK(cudaMemcpyAsync(x, c->d_x, nb, cudaMemcpyDeviceToHost, c->stream));
+    else if (x != c->d_x) CK(cudaMemcpyAsync(x, c->d_x, nb, cudaMemcpyDeviceToDevice, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    return st;
+}
+
+ipfem_status ipfem_newton_solve(ipfem_ctx *c, const ipfem_solve_opts *o, int32_t s0, int32_t s1, double *u, int where,
+                                ipfem_solve_stats *stats, double *log, int32_t log_cap)
+{
+    if (!c || !o || !u || o->n_steps <= 0 || s0 < 0 || s1 > o->n_steps || s0 > s1 ||
+        (where != IPFEM_HOST && where != IPFEM_DEVICE))
+        return fail(c, IPFEM_INVALID, "bad args");
+    const size_t nb = (size_t)c->s.neq * sizeof(double);
+    double *du = u;
+    if (where == IPFEM_HOST) {
+        CK(cudaMemcpyAsync(c->d_u, u, nb, cudaMemcpyHostToDevice, c->stream));
+        du = c->d_u;
+    }
+    ipfem_solve_stats st{};
+    st.converged = 1;
+    cudaEvent_t ev[2];
+    CK(cudaEventCreate(&ev[0]));
+    CK(cudaEventCreate(&ev[1]));
+    auto elapsed = [&]() {
+        float ms = 0;
+        cudaEventSynchronize(ev[1]);
+        cudaEventElapsedTime(&ms, ev[0], ev[1]);
+        return (double)ms;
+    };
+    ipfem_status ret = IPFEM_OK;
+    int32_t nlog = 0;
+    const int saved_update = c->update_mem;
+    c->update_mem = 0;
+    for (int32_t step = s0; step < s1 && ret == IPFEM_OK; step++) {
+        c->load_factor = (double)(step + 1) / (double)o->n_steps;
+        cudaEventRecord(ev[0], c->stream);
+        tangent_device(c, du, c->d_rhs, 0);
+        cudaEventRecord(ev[1], c->stream);
+        double r0sq = 0;
+        ipfem_status e = dot_host(c, c->d_rhs, c->d_rhs, &r0sq);
+        st.ms_assemble += elapsed();
+        if (e != IPFEM_OK) { ret = e; break; }
+        const double r0 = std::sqrt(r0sq);
+        double rn = r0;
+        bool conv = (r0 == 0.0);
+        int it = 0;
+        if (!std::isfinite(r0)) { ret = fail(c, IPFEM_NAN, "residual is not finite"); break; }
+        while (!conv && it < o->newton_max_it) {
+            int k = 0;
+            cudaEventRecord(ev[0], c->stream);
+            e = cg_device(c, c->d_rhs, o->cg_rtol, o->cg_max_it, &k);
+            cudaEventRecord(ev[1], c->stream);
+            st.ms_solve += elapsed();
+            st.cg_iters += k;
+            if (e != IPFEM_OK && e != IPFEM_NONCONVERGED) { ret = e; break; }
+            launch_axpy_u(c, du, c->d_x);
+            it++;
+            cudaEventRecord(ev[0], c->stream);
+            tangent_device(c, du, c->d_rhs, 0);
+            cudaEventRecord(ev[1], c->stream);
+            double rsq = 0;
+            e = dot_host(c, c->d_rhs, c->d_rhs, &rsq);
+            st.ms_assemble += elapsed();
+            if (e != IPFEM_OK) { ret = e; break; }
+            rn = std::sqrt(rsq);
+            if (!std::isfinite(rn)) { ret = fail(c, IPFEM_NAN, "residual is not finite"); break; }
+            if (log && nlog < log_cap) {
+                log[3 * nlog + 0] = (double)step;
+                log[3 * nlog + 1] = (double)k;
+                log[3 * nlog + 2] = rn;
+                nlog++;
+            }
+            conv = rn <= o->newton_rtol * r0;
+        }
+        if (ret != IPFEM_OK) break;
+        st.newton_iters += it;
+        st.last_step_iters = it;
+        st.final_res = r0 > 0.0 ? rn / r0 : 0.0;
+        if (!conv) st.converged = 0;
+        // accept: commit the integration-point state (main.cpp:487-522)
+        cudaEventRecord(ev[0], c->stream);
+        residual_device(c, du, c->d_b, 1);
+        cudaEventRecord(ev[1], c->stream);
+        st.ms_commit += elapsed();
+        e = sync_check(c);
+        if (e != IPFEM_OK) { ret = e; break; }
+    }
+    c->update_mem = saved_update;
+    cudaEventDestroy(ev[0]);
+    cudaEventDestroy(ev[1]);
+    if (where == IPFEM_HOST) {
+        CK(cudaMemcpyAsync(u, c->d_u, nb, cudaMemcpyDeviceToHost, c->stream));
+        CK(cudaStreamSynchronize(c->stream));
+    }
+    if (stats) *stats = st;
+    if (ret == IPFEM_OK && !st.converged) return fail(c, IPFEM_NONCONVERGED, "Newton did not converge in every step");
+    return ret;
+}
+
+ipfem_status ipfem_gather_strain(ipfem_ctx *c, const double *d_u, double *d_strain)
+{
+    if (!c || !d_u || !d_strain) return fail(c, IPFEM_INVALID, "bad args");
+    launch_gather_strain(c, d_u, d_strain);
+    return sync_check(c);
+}
+
+ipfem_status ipfem_compute_sigma(ipfem_ctx *c, int update_mem, const double *d_strain, double *d_sigma_w,
+                                 double *d_dep)
+{
+    if (!c || !d_strain || !d_sigma_w) return fail(c, IPFEM_INVALID, "bad args");
+    launch_compute_sigma(c, update_mem, d_strain, d_sigma_w, d_dep);
+    return sync_check(c);
+}
+
+ipfem_status ipfem_scatter_residual(ipfem_ctx *c, const double *d_sigma_w, double *d_res)
+{
+    if (!c || !d_sigma_w || !d_res) return fail(c, IPFEM_INVALID, "bad args");
+    launch_stress_residual(c, d_sigma_w, c->d_fe);
+    launch_color_reduce(c, c->d_fe, 0.0, 0, d_res);
+    return sync_check(c);
+}
+
+ipfem_status ipfem_get_state(ipfem_ctx *c, int field, double *out)
+{
+    if (!c || !out) return IPFEM_INVALID;
+    const int64_t n = c->s.n_ip;
+    switch (field) {
+    case 0: CK(cudaMemcpyAsync(out, c->d_eps_p, 4 * n * sizeof(double), cudaMemcpyDeviceToHost, c->stream)); break;
+    case 1: CK(cudaMemcpyAsync(out, c->d_sigma, 4 * n * sizeof(double), cudaMemcpyDeviceToHost, c->stream)); break;
+    case 2: CK(cudaMemcpyAsync(out, c->d_alpha, n * sizeof(double), cudaMemcpyDeviceToHost, c->stream)); break;
+    case 3: {
+        std::vector<int8_t> h((size_t)n);
+        CK(cudaMemcpyAsync(h.data(), c->d_mtype, (size_t)n, cudaMemcpyDeviceToHost, c->stream));
+        CK(cudaStreamSynchronize(c->stream));
+        for (int64_t i = 0; i < n; i++) out[i] = h[i];
+        return IPFEM_OK;
+    }
+    default: return fail(c, IPFEM_INVALID, "bad state field");
+    }
+    CK(cudaStreamSynchronize(c->stream));
+    return IPFEM_OK;
+}
+
+ipfem_status ipfem_set_state(ipfem_ctx *c, int field, const double *in)
+{
+    if (!c || !in) return IPFEM_INVALID;
+    const int64_t n = c->s.n_ip;
+    switch (field) {
+    case 0: CK(cudaMemcpyAsync(c->d_eps_p, in, 4 * n * sizeof(double), cudaMemcpyHostToDevice, c->stream)); break;
+    case 1: CK(cudaMemcpyAsync(c->d_sigma, in, 4 * n * sizeof(double), cudaMemcpyHostToDevice, c->stream)); break;
+    case 2: CK(cudaMemcpyAsync(c->d_alpha, in, n * sizeof(double), cudaMemcpyHostToDevice, c->stream)); break;
+    default: return fail(c, IPFEM_INVALID, "bad state field");
+    }
+    CK(cudaStreamSynchronize(c->stream));
+    return IPFEM_OK;
+}
+
+ipfem_status ipfem_get_setup(ipfem_ctx *c, int field, void *out)
+{
+    if (!c || !out) return IPFEM_INVALID;
+    const Setup &s = c->s;
+    switch (field) {
+    case 0: std::memcpy(out, s.el_color.data(), s.el_color.size() * sizeof(int32_t)); break;
+    case 1: *(int32_t *)out = s.n_colors; break;
+    case 2: std::memcpy(out, s.dofs.data(), s.dofs.size() * sizeof(int32_t)); break;
+    case 3: std::memcpy(out, s.dphi.data(), s.dphi.size() * sizeof(double)); break;
+    case 4: std::memcpy(out, s.weight.data(), s.weight.size() * sizeof(double)); break;
+    default: return fail(c, IPFEM_INVALID, "bad setup field");
+    }
+    return IPFEM_OK;
+}
+
+}  // extern "C"

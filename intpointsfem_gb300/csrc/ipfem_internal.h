@@ -1,0 +1,114 @@
+// Internal declarations shared by the host setup (C++) and the CUDA
+// translation units of libipfem.  Not part of the C-ABI.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/ipfem.h"
+
+namespace ipfem {
+
+constexpr int kMaxColors = 16;
+constexpr int kRedBlock = 256;       // nodes per level-1 reduction block (= CTA size)
+
+struct ElasticConstH {               // mirrors ElasticConst of constitutive.cuh
+    double lambda, mu, K, G, l2m, c1, c2, inv_mu;
+};
+
+// device-side scalars of one CG solve
+struct CGScalars {
+    double rz, pq, alpha, beta, rr, bb, thr;
+    int done, iters, status, max_it;
+};
+
+// Host result of the setup: everything derived from the mesh (colouring,
+// dof map, nodal 2x2 block pattern in SELL-32 layout, colour incidence).
+struct Setup {
+    int32_t n_el = 0, n_nodes = 0, neq = 0, n_colors = 0;
+    int64_t n_ip = 0;
+    std::vector<double> dphi;            // [n_el*162] ((e*9+q)*2+d)*9+n
+    std::vector<double> weight;          // [n_ip]
+    std::vector<int32_t> dofs;           // [n_el*18]
+    std::vector<int32_t> el_color;       // [n_el]
+    std::vector<int32_t> color_ptr;      // [n_colors+1]
+    std::vector<int32_t> color_els;      // [n_el]
+    std::vector<int32_t> inc;            // [n_colors*n_nodes] e*9+local node or -1
+    // nodal block pattern (rows ascending, columns ascending)
+    int64_t n_blocks = 0;
+    std::vector<int64_t> row_ptr;        // [n_nodes+1]
+    std::vector<int32_t> col;            // [n_blocks]
+    // SELL-32 layout of the same blocks
+    int64_t n_sell = 0;                  // padded block slots
+    std::vector<int64_t> slice_base;     // [n_slices+1], in blocks
+    std::vector<int32_t> rowlen;         // [n_nodes]
+    std::vector<int32_t> sell_col;       // [n_sell]
+    std::vector<int64_t> bsr_to_sell;    // [n_blocks]
+    std::vector<int32_t> el_blk;         // [n_el*81] SELL slot of local node pair (m, n)
+    std::vector<int64_t> diag_blk;       // [n_nodes] SELL slot of the diagonal block
+    std::vector<uint8_t> fixed;          // [neq]
+    std::vector<double> f0, df;          // [neq]
+    std::vector<double> mat;             // [5*n_el] SoA: c, sinphi, cosphi, tanphi, sinpsi
+    ElasticConstH el{};
+    double eps_p0[4] = {0, 0, 0, 0};     // in-situ plastic strain seed xx, xy, yy, zz
+    double sigma0[4] = {0, 0, 0, 0};
+};
+
+// builds the setup; returns an empty string or an error message
+std::string build_setup(const ipfem_mesh *mesh, const ipfem_material *mat, Setup &s);
+int32_t greedy_coloring(int32_t n_el, int32_t n_nodes, const int32_t *connects, int32_t *el_color);
+void elastic_constants(double E, double nu, ElasticConstH &el);
+
+}  // namespace ipfem
+
+struct ipfem_ctx {
+    int device = -1;
+    cudaStream_t stream = nullptr;
+    ipfem::Setup s;
+    std::string err;
+    double load_factor = 0.0;
+    int update_mem = 0;
+    // device: setup
+    double *d_dphi = nullptr, *d_weight = nullptr, *d_mat = nullptr, *d_f0 = nullptr, *d_df = nullptr;
+    int32_t *d_dofs = nullptr, *d_color_els = nullptr, *d_inc = nullptr;
+    uint8_t *d_fixed = nullptr;
+    int64_t *d_slice_base = nullptr, *d_diag_blk = nullptr;
+    int32_t *d_sell_col = nullptr, *d_rowlen = nullptr, *d_el_blk = nullptr;
+    // device: tangent
+    double *d_K = nullptr, *d_dinv = nullptr;
+    // device: integration-point state {xx, xy, yy, zz} SoA
+    double *d_eps_p = nullptr, *d_sigma = nullptr, *d_alpha = nullptr;
+    int8_t *d_mtype = nullptr;
+    // device: work
+    double *d_u = nullptr, *d_rhs = nullptr, *d_strain = nullptr, *d_sigma_w = nullptr, *d_dep = nullptr;
+    double *d_fe = nullptr;
+    double *d_x = nullptr, *d_r = nullptr, *d_z = nullptr, *d_p = nullptr, *d_q = nullptr, *d_b = nullptr;
+    double *d_part = nullptr;            // 3 partial arrays of n_red each
+    int64_t n_red = 0;                   // number of reduction blocks
+    ipfem::CGScalars *d_sc = nullptr;
+    unsigned *d_counters = nullptr;      // last-block tickets
+    double *d_dotres = nullptr;          // results of standalone dots
+    int *d_err = nullptr;                // device error word (wait timeouts)
+    ipfem::CGScalars *h_sc = nullptr;    // pinned
+    double *h_pin = nullptr;             // pinned scalars
+    cudaGraphExec_t cg_exec = nullptr;
+    int cg_batch = 0;
+    bool tangent_valid = false;
+};
+
+// ---- kernel launchers (implemented in the .cu files) ----
+namespace ipfem {
+cudaError_t upload_constants(const ElasticConstH &el);
+void launch_gather_strain(ipfem_ctx *c, const double *d_u, double *d_strain);
+void launch_compute_sigma(ipfem_ctx *c, int update_mem, const double *d_strain, double *d_sigma_w, double *d_dep);
+void launch_stress_residual(ipfem_ctx *c, const double *d_sigma_w, double *d_fe);
+void launch_color_reduce(ipfem_ctx *c, const double *d_fe, double lambda, int with_load, double *d_res);
+void launch_stiffness(ipfem_ctx *c);
+void launch_cg_init(ipfem_ctx *c, const double *d_b, double rtol, int max_it);
+void launch_cg_iteration(ipfem_ctx *c);
+void launch_dot(ipfem_ctx *c, const double *a, const double *b, double *d_out);
+void launch_axpy_u(ipfem_ctx *c, double *d_u, const double *d_du);
+}  // namespace ipfem

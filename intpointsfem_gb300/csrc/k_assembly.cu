@@ -1,0 +1,331 @@
+// Element-block kernels of the residual and tangent assembly.
+//
+//  k_gather_strain   TPZNumericalIntegrator::Multiply (TPZNumericalIntegrator.cpp:25-37):
+//                    gather of element dofs + B*u, fused.  The element blocks of
+//                    a tile are staged in shared memory by one bulk (TMA) copy.
+//  k_stress_residual TPZNumericalIntegrator::MultiplyTranspose (…cpp:54-78), first
+//                    half: f_e = -B^T (w sigma) per element, blocks TMA-staged.
+//  k_color_reduce    second half: the colour-slab scatter and pairwise slab
+//                    reduction of the reference, evaluated per node as a
+//                    gather over the (at most one per colour) incident elements,
+//                    in the reference's pairing order; + f0 + lambda*df and
+//                    Dirichlet masking (TPZElastoPlasticIntPointsStructMatrix.cpp:213-230).
+//  k_stiffness       TPZNumericalIntegrator::KAssembly (…cpp:131-214) and
+//                    MatrixAssembleKernel (KernelsMatrixAssemble.h:24-57): one warp
+//                    per element, K_e = sum_q B_q^T (w Dep_q) B_q (upper triangle),
+//                    added colour by colour into the nodal 2x2 block matrix.
+//
+// Element blocks are stored compactly: dphi[e][q][d][n] = d(phi_n)/d(x_d) at
+// point q (the reference's fStorage holds the same numbers in a (27 x 18)
+// block with structural zeros).  Products use fma in the order of the
+// reference's row-major block traversal; skipped terms are exact zeros.
+#include "ipfem_internal.h"
+#include "tma.cuh"
+
+namespace ipfem {
+
+constexpr int kGatherTile = 32;     // elements per CTA (288 threads)
+constexpr int kResTile = 16;        // elements per CTA (288 threads)
+constexpr int kElBytes = 162 * 8;   // compact block bytes per element (multiple of 16)
+
+__global__ void __launch_bounds__(kGatherTile * 9) k_gather_strain(int32_t n_el, int64_t n_ip,
+                                                                   const double *__restrict__ dphi,
+                                                                   const int32_t *__restrict__ dofs,
+                                                                   const double *__restrict__ u,
+                                                                   double *__restrict__ strain,
+                                                                   int *__restrict__ err)
+{
+    extern __shared__ __align__(128) unsigned char smem[];
+    uint64_t *bar = reinterpret_cast<uint64_t *>(smem);
+    double *s_dn = reinterpret_cast<double *>(smem + 128);
+    double *s_u = s_dn + kGatherTile * 162;
+    const int32_t e0 = blockIdx.x * kGatherTile;
+    const int ne = min(kGatherTile, n_el - e0);
+    if (threadIdx.x == 0) mbar_init(bar, 1);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const uint32_t bytes = (uint32_t)ne * kElBytes;
+        mbar_expect_tx(bar, bytes);
+        bulk_g2s(s_dn, dphi + (size_t)e0 * 162, bytes, bar);
+    }
+    for (int k = threadIdx.x; k < ne * 18; k += blockDim.x) s_u[k] = __ldg(&u[__ldg(&dofs[(size_t)e0 * 18 + k])]);
+    const bool ok = mbar_wait_bounded(bar, 0);
+    __syncthreads();
+    if (!ok) {
+        if (threadIdx.x == 0) atomicExch(err, 1);
+        return;
+    }
+    const int el = threadIdx.x / 9, q = threadIdx.x % 9;
+    if (el >= ne) return;
+    const double *dx = s_dn + el * 162 + q * 18;
+    const double *dy = dx + 9;
+    const double *ue = s_u + el * 18;
+    double exx = 0.0, gxy = 0.0, eyy = 0.0;
+#pragma unroll
+    for (int n = 0; n < 9; n++) exx = fma(dx[n], ue[2 * n], exx);
+#pragma unroll
+    for (int n = 0; n < 9; n++) {
+        gxy = fma(dy[n], ue[2 * n], gxy);
+        gxy = fma(dx[n], ue[2 * n + 1], gxy);
+    }
+#pragma unroll
+    for (int n = 0; n < 9; n++) eyy = fma(dy[n], ue[2 * n + 1], eyy);
+    const int64_t ip = (int64_t)(e0 + el) * 9 + q;
+    strain[ip] = exx;
+    strain[n_ip + ip] = gxy;
+    strain[2 * n_ip + ip] = eyy;
+}
+
+__global__ void __launch_bounds__(kResTile * 18) k_stress_residual(int32_t n_el, int64_t n_ip,
+                                                                   const double *__restrict__ dphi,
+                                                                   const double *__restrict__ sigma_w,
+                                                                   double *__restrict__ fe,
+                                                                   int *__restrict__ err)
+{
+    extern __shared__ __align__(128) unsigned char smem[];
+    uint64_t *bar = reinterpret_cast<uint64_t *>(smem);
+    double *s_dn = reinterpret_cast<double *>(smem + 128);
+    double *s_sig = s_dn + kResTile * 162;            // [3][kResTile*9]
+    const int32_t e0 = blockIdx.x * kResTile;
+    const int ne = min(kResTile, n_el - e0);
+    if (threadIdx.x == 0) mbar_init(bar, 1);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const uint32_t bytes = (uint32_t)ne * kElBytes;
+        mbar_expect_tx(bar, bytes);
+        bulk_g2s(s_dn, dphi + (size_t)e0 * 162, bytes, bar);
+    }
+    const int npt = ne * 9;
+    const int64_t ip0 = (int64_t)e0 * 9;
+    for (int k = threadIdx.x; k < 3 * npt; k += blockDim.x) {
+        const int cmp = k / npt, i = k - cmp * npt;
+        s_sig[cmp * kResTile * 9 + i] = sigma_w[cmp * n_ip + ip0 + i];
+    }
+    const bool ok = mbar_wait_bounded(bar, 0);
+    __syncthreads();
+    if (!ok) {
+        if (threadIdx.x == 0) atomicExch(err, 1);
+        return;
+    }
+    const int el = threadIdx.x / 18, j = threadIdx.x % 18;
+    if (el >= ne) return;
+    const int n = j >> 1;
+    const double *dn = s_dn + el * 162;
+    const double *sxx = s_sig + el * 9;
+    const double *sxy = s_sig + kResTile * 9 + el * 9;
+    const double *syy = s_sig + 2 * kResTile * 9 + el * 9;
+    double acc = 0.0;
+    if ((j & 1) == 0) {
+#pragma unroll
+        for (int q = 0; q < 9; q++) {
+            acc = fma(dn[q * 18 + n], sxx[q], acc);
+            acc = fma(dn[q * 18 + 9 + n], sxy[q], acc);
+        }
+    } else {
+#pragma unroll
+        for (int q = 0; q < 9; q++) {
+            acc = fma(dn[q * 18 + n], sxy[q], acc);
+            acc = fma(dn[q * 18 + 9 + n], syy[q], acc);
+        }
+    }
+    fe[(size_t)(e0 + el) * 18 + j] = -acc;
+}
+
+// Per node: contributions of the incident element of each colour (0 if none),
+// summed in the reference's pairwise slab order
+// (TPZNumericalIntegrator.cpp:69-77: slab k += slab (nc-ca)+k, nc -= ca).
+__global__ void __launch_bounds__(256) k_color_reduce(int32_t n_nodes, int n_colors,
+                                                      const int32_t *__restrict__ inc,
+                                                      const double *__restrict__ fe, double lambda,
+                                                      int with_load, const double *__restrict__ f0,
+                                                      const double *__restrict__ df,
+                                                      const uint8_t *__restrict__ fixed,
+                                                      double *__restrict__ res)
+{
+    const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n_nodes) return;
+    double sx[kMaxColors], sy[kMaxColors];
+#pragma unroll
+    for (int c = 0; c < kMaxColors; c++) {
+        sx[c] = 0.0;
+        sy[c] = 0.0;
+        if (c < n_colors) {
+            const int32_t k = __ldg(&inc[(size_t)c * n_nodes + i]);
+            if (k >= 0) {
+                const double2 v = *reinterpret_cast<const double2 *>(&fe[2 * (size_t)k]);
+                sx[c] = v.x;
+                sy[c] = v.y;
+            }
+        }
+    }
+    int nc = n_colors, ca = n_colors / 2;
+    while (ca > 0) {
+        const int first = nc - ca;
+#pragma unroll
+        for (int k = 0; k < kMaxColors / 2; k++)
+            if (k < ca) {
+                sx[k] = sx[k] + sx[first + k];
+                sy[k] = sy[k] + sy[first + k];
+            }
+        nc -= ca;
+        ca = nc / 2;
+    }
+    double rx = sx[0], ry = sy[0];
+    if (with_load) {
+        const double lx = fma(lambda, df[2 * (size_t)i], f0[2 * (size_t)i]);
+        const double ly = fma(lambda, df[2 * (size_t)i + 1], f0[2 * (size_t)i + 1]);
+        rx = fixed[2 * (size_t)i] ? 0.0 : rx + lx;
+        ry = fixed[2 * (size_t)i + 1] ? 0.0 : ry + ly;
+    }
+    res[2 * (size_t)i] = rx;
+    res[2 * (size_t)i + 1] = ry;
+}
+
+constexpr int kStiffWarps = 4;
+
+__global__ void __launch_bounds__(kStiffWarps * 32) k_stiffness(int32_t n_in_color, const int32_t *__restrict__ els,
+                                                                 int64_t n_ip, const double *__restrict__ dphi,
+                                                                 const double *__restrict__ dep,
+                                                                 const int32_t *__restrict__ el_blk,
+                                                                 double *__restrict__ K)
+{
+    __shared__ __align__(16) double s_dn[kStiffWarps][162];
+    __shared__ double s_D[kStiffWarps][81];        // [q][9]
+    __shared__ double s_DB[kStiffWarps][54];       // [3][18]
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int32_t k = blockIdx.x * kStiffWarps + w;
+    if (k >= n_in_color) return;                   // warp-uniform
+    const int32_t e = __ldg(&els[k]);
+    const double *dn_g = dphi + (size_t)e * 162;
+    for (int t = lane; t < 81; t += 32)
+        reinterpret_cast<double2 *>(s_dn[w])[t] = __ldg(reinterpret_cast<const double2 *>(dn_g) + t);
+    for (int t = lane; t < 81; t += 32) {
+        const int cmp = t / 9, q = t - cmp * 9;
+        s_D[w][q * 9 + cmp] = __ldg(&dep[cmp * n_ip + (int64_t)e * 9 + q]);
+    }
+    __syncwarp();
+    const double *dn = s_dn[w];
+    // upper-triangle entries (a <= b, row-major order) owned by this lane
+    int pa[6], pb[6];
+#pragma unroll
+    for (int m = 0; m < 6; m++) {
+        int r = lane + 32 * m, a = 0;
+        if (r < 171)
+            while (r >= 18 - a) {
+                r -= 18 - a;
+                a++;
+            }
+        pa[m] = a;
+        pb[m] = a + r;
+    }
+    double acc[6] = {0, 0, 0, 0, 0, 0};
+#pragma unroll 1
+    for (int q = 0; q < 9; q++) {
+        const double *D = &s_D[w][q * 9];
+        const double *dx = dn + q * 18, *dy = dx + 9;
+        for (int t = lane; t < 54; t += 32) {
+            const int i = t / 18, j = t - i * 18, n = j >> 1;
+            double s;
+            if ((j & 1) == 0) {
+                s = D[3 * i + 0] * dx[n];
+                s = fma(D[3 * i + 1], dy[n], s);
+            } else {
+                s = D[3 * i + 1] * dx[n];
+                s = fma(D[3 * i + 2], dy[n], s);
+            }
+            s_DB[w][t] = s;
+        }
+        __syncwarp();
+        const double *DB = s_DB[w];
+#pragma unroll
+        for (int m = 0; m < 6; m++) {
+            const int p = lane + 32 * m;
+            if (p < 171) {
+                const int a = pa[m], b = pb[m], na = a >> 1;
+                double t = acc[m];
+                if ((a & 1) == 0) {
+                    t = fma(dx[na], DB[b], t);
+                    t = fma(dy[na], DB[18 + b], t);
+                } else {
+                    t = fma(dx[na], DB[18 + b], t);
+                    t = fma(dy[na], DB[36 + b], t);
+                }
+                acc[m] = t;
+            }
+        }
+        __syncwarp();
+    }
+    const int32_t *eb = el_blk + (size_t)e * 81;
+#pragma unroll
+    for (int m = 0; m < 6; m++) {
+        const int p = lane + 32 * m;
+        if (p < 171) {
+            const int a = pa[m], b = pb[m];
+            const int ma = a >> 1, ca = a & 1, nb = b >> 1, cb = b & 1;
+            const double v = acc[m];
+            if (ma == nb) {
+                double *blk = K + 4 * (size_t)__ldg(&eb[ma * 9 + ma]);
+                blk[2 * ca + cb] = blk[2 * ca + cb] + v;
+                if (ca != cb) blk[2 * cb + ca] = blk[2 * cb + ca] + v;
+            } else {
+                double *b1 = K + 4 * (size_t)__ldg(&eb[ma * 9 + nb]);
+                double *b2 = K + 4 * (size_t)__ldg(&eb[nb * 9 + ma]);
+                b1[2 * ca + cb] = b1[2 * ca + cb] + v;
+                b2[2 * cb + ca] = b2[2 * cb + ca] + v;
+            }
+        }
+    }
+}
+
+__global__ void k_jacobi(int32_t n_nodes, const int64_t *__restrict__ diag, const double *__restrict__ K,
+                         const uint8_t *__restrict__ fixed, double *__restrict__ dinv)
+{
+    const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n_nodes) return;
+    const double *blk = K + 4 * (size_t)diag[i];
+    dinv[2 * (size_t)i] = fixed[2 * (size_t)i] ? 0.0 : 1.0 / blk[0];
+    dinv[2 * (size_t)i + 1] = fixed[2 * (size_t)i + 1] ? 0.0 : 1.0 / blk[3];
+}
+
+void launch_gather_strain(ipfem_ctx *c, const double *d_u, double *d_strain)
+{
+    const Setup &s = c->s;
+    const unsigned grid = (unsigned)((s.n_el + kGatherTile - 1) / kGatherTile);
+    const size_t smem = 128 + kGatherTile * 162 * 8 + kGatherTile * 18 * 8;
+    k_gather_strain<<<grid, kGatherTile * 9, smem, c->stream>>>(s.n_el, s.n_ip, c->d_dphi, c->d_dofs, d_u,
+                                                                d_strain, c->d_err);
+}
+
+void launch_stress_residual(ipfem_ctx *c, const double *d_sigma_w, double *d_fe)
+{
+    const Setup &s = c->s;
+    const unsigned grid = (unsigned)((s.n_el + kResTile - 1) / kResTile);
+    const size_t smem = 128 + kResTile * 162 * 8 + 3 * kResTile * 9 * 8;
+    k_stress_residual<<<grid, kResTile * 18, smem, c->stream>>>(s.n_el, s.n_ip, c->d_dphi, d_sigma_w, d_fe,
+                                                                c->d_err);
+}
+
+void launch_color_reduce(ipfem_ctx *c, const double *d_fe, double lambda, int with_load, double *d_res)
+{
+    const Setup &s = c->s;
+    const unsigned grid = (unsigned)((s.n_nodes + 255) / 256);
+    k_color_reduce<<<grid, 256, 0, c->stream>>>(s.n_nodes, s.n_colors, c->d_inc, d_fe, lambda, with_load, c->d_f0,
+                                                 c->d_df, c->d_fixed, d_res);
+}
+
+void launch_stiffness(ipfem_ctx *c)
+{
+    const Setup &s = c->s;
+    cudaMemsetAsync(c->d_K, 0, (size_t)s.n_sell * 4 * sizeof(double), c->stream);
+    for (int col = 0; col < s.n_colors; col++) {
+        const int32_t first = s.color_ptr[col], n = s.color_ptr[col + 1] - first;
+        if (n == 0) continue;
+        const unsigned grid = (unsigned)((n + kStiffWarps - 1) / kStiffWarps);
+        k_stiffness<<<grid, kStiffWarps * 32, 0, c->stream>>>(n, c->d_color_els + first, s.n_ip, c->d_dphi, c->d_dep,
+                                                              c->d_el_blk, c->d_K);
+    }
+    const unsigned g2 = (unsigned)((s.n_nodes + 255) / 256);
+    k_jacobi<<<g2, 256, 0, c->stream>>>(s.n_nodes, c->d_diag_blk, c->d_K, c->d_fixed, c->d_dinv);
+}
+
+}  // namespace ipfem

@@ -1,0 +1,307 @@
+// Jacobi-preconditioned CG on the nodal 2x2 block tangent, FP64.
+//
+// The reference assembles K into a symmetric CSR and solves with Pardiso
+// (main.cpp:283-285); its only CG (TPZCudaCalls::SolveCG, TPZCudaCalls.cu:213-290)
+// is unpreconditioned and unused.  Here the matrix is stored as 2x2 blocks in
+// SELL-32 order (slice of 32 node rows, slot-major, lane-minor) so that a
+// warp reads one slot of 32 rows as 1 KB of contiguous values.
+//
+// Every dot product follows one canonical reduction order (shared with the CPU
+// oracle): per node fma(a0,b0,0) then fma(a1,b1,.), a 32-lane shuffle-down
+// tree, a tree over the 8 warps of a 256-node CTA, and a last-CTA final pass
+// (256 threads strided over the CTA partials, then the same trees).  With
+// fma-ordered SpMV and vector updates, the whole solve is deterministic and
+// equal to the oracle bit for bit.
+//
+// Scalars (alpha, beta, convergence) live in device memory, so an iteration
+// is three kernels with no host round trip; the host replays a captured CUDA
+// graph of several iterations and checks the `done` word between replays.
+#include "ipfem_internal.h"
+
+namespace ipfem {
+
+constexpr unsigned FULL = 0xffffffffu;
+
+__device__ __forceinline__ double warp_tree(double v)
+{
+#pragma unroll
+    for (int off = 16; off >= 1; off >>= 1) v = v + __shfl_down_sync(FULL, v, off);
+    return v;
+}
+
+// tree over the 8 warp sums in shared memory (4, 2, 1); valid in thread 0
+__device__ __forceinline__ double tree8(volatile double *w)
+{
+    double a[8];
+#pragma unroll
+    for (int k = 0; k < 8; k++) a[k] = w[k];
+#pragma unroll
+    for (int off = 4; off >= 1; off >>= 1)
+#pragma unroll
+        for (int l = 0; l < off; l++) a[l] = a[l] + a[l + off];
+    return a[0];
+}
+
+// Level 0+1 for NV values at once: per-CTA partial sums written to part[v][blockIdx].
+// Returns true in every thread of the CTA that finished last (after a fence).
+template <int NV>
+__device__ __forceinline__ bool block_partials(const double (&v)[NV], double *part, int64_t n_red, unsigned *ticket)
+{
+    __shared__ double ws[NV][8];
+    __shared__ int s_last;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+    for (int k = 0; k < NV; k++) {
+        const double t = warp_tree(v[k]);
+        if (lane == 0) ws[k][w] = t;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int k = 0; k < NV; k++) part[k * n_red + blockIdx.x] = tree8(ws[k]);
+        __threadfence();
+        const unsigned t = atomicAdd(ticket, 1u);
+        s_last = (t == gridDim.x - 1);
+    }
+    __syncthreads();
+    return s_last != 0;
+}
+
+// Level 2, executed by all 256 threads of the last CTA; result valid in thread 0.
+template <int NV>
+__device__ __forceinline__ void final_reduce(const double *part, int64_t n_red, double (&out)[NV])
+{
+    __shared__ double ws[NV][8];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+    for (int k = 0; k < NV; k++) {
+        double acc = 0.0;
+        for (int64_t i = threadIdx.x; i < n_red; i += blockDim.x) acc = acc + __ldcg(&part[k * n_red + i]);
+        acc = warp_tree(acc);
+        if (lane == 0) ws[k][w] = acc;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int k = 0; k < NV; k++) out[k] = tree8(ws[k]);
+    }
+}
+
+__global__ void __launch_bounds__(kRedBlock) k_cg_init(int32_t n_nodes, const double *__restrict__ b,
+                                                       const double *__restrict__ dinv, double *__restrict__ x,
+                                                       double *__restrict__ r, double *__restrict__ z,
+                                                       double *__restrict__ p, double *part, int64_t n_red,
+                                                       unsigned *ticket, CGScalars *sc, double rtol, int max_it)
+{
+    const int32_t i = blockIdx.x * kRedBlock + threadIdx.x;
+    double v[2] = {0.0, 0.0};
+    if (i < n_nodes) {
+        const double2 bb = reinterpret_cast<const double2 *>(b)[i];
+        const double2 di = reinterpret_cast<const double2 *>(dinv)[i];
+        const double2 zz = make_double2(bb.x * di.x, bb.y * di.y);
+        reinterpret_cast<double2 *>(x)[i] = make_double2(0.0, 0.0);
+        reinterpret_cast<double2 *>(r)[i] = bb;
+        reinterpret_cast<double2 *>(z)[i] = zz;
+        reinterpret_cast<double2 *>(p)[i] = zz;
+        v[0] = fma(bb.y, bb.y, fma(bb.x, bb.x, 0.0));
+        v[1] = fma(bb.y, zz.y, fma(bb.x, zz.x, 0.0));
+    }
+    if (block_partials<2>(v, part, n_red, ticket)) {
+        double o[2];
+        final_reduce<2>(part, n_red, o);
+        if (threadIdx.x == 0) {
+            sc->bb = o[0];
+            sc->rz = o[1];
+            sc->thr = (rtol * rtol) * o[0];
+            sc->iters = 0;
+            sc->status = 0;
+            sc->max_it = max_it;
+            sc->done = (o[0] == 0.0) ? 1 : (max_it <= 0 ? 1 : 0);
+            if (o[0] != 0.0 && max_it <= 0) sc->status = IPFEM_NONCONVERGED;
+            *ticket = 0u;
+        }
+    }
+}
+
+// q = K p (free dofs), partial sums of p.q; last CTA: alpha = rz / pq
+__global__ void __launch_bounds__(kRedBlock) k_cg_spmv(int32_t n_nodes, const int64_t *__restrict__ slice_base,
+                                                       const int32_t *__restrict__ rowlen,
+                                                       const int32_t *__restrict__ scol,
+                                                       const double *__restrict__ K,
+                                                       const uint8_t *__restrict__ fixed,
+                                                       const double *__restrict__ p, double *__restrict__ q,
+                                                       double *part, int64_t n_red, unsigned *ticket,
+                                                       CGScalars *sc)
+{
+    if (*reinterpret_cast<volatile int *>(&sc->done)) return;
+    const int32_t i = blockIdx.x * kRedBlock + threadIdx.x;
+    double v[1] = {0.0};
+    if (i < n_nodes) {
+        const int64_t base = __ldg(&slice_base[i >> 5]) + (i & 31);
+        const int len = __ldg(&rowlen[i]);
+        const double2 *Kv = reinterpret_cast<const double2 *>(K);
+        const double2 *pv = reinterpret_cast<const double2 *>(p);
+        double y0 = 0.0, y1 = 0.0;
+#pragma unroll 4
+        for (int k = 0; k < len; k++) {
+            const int64_t s = base + (int64_t)k * 32;
+            const int32_t c = __ldg(&scol[s]);
+            const double2 a0 = __ldg(&Kv[2 * s]);
+            const double2 a1 = __ldg(&Kv[2 * s + 1]);
+            const double2 xx = __ldg(&pv[c]);
+            y0 = fma(a0.x, xx.x, y0);
+            y0 = fma(a0.y, xx.y, y0);
+            y1 = fma(a1.x, xx.x, y1);
+            y1 = fma(a1.y, xx.y, y1);
+        }
+        if (fixed[2 * (size_t)i]) y0 = 0.0;
+        if (fixed[2 * (size_t)i + 1]) y1 = 0.0;
+        reinterpret_cast<double2 *>(q)[i] = make_double2(y0, y1);
+        const double2 pp = pv[i];
+        v[0] = fma(pp.y, y1, fma(pp.x, y0, 0.0));
+    }
+    if (block_partials<1>(v, part, n_red, ticket)) {
+        double o[1];
+        final_reduce<1>(part, n_red, o);
+        if (threadIdx.x == 0) {
+            const double pq = o[0];
+            sc->pq = pq;
+            if (!(pq > 0.0)) {
+                sc->done = 1;
+                sc->status = IPFEM_BREAKDOWN;
+            } else {
+                sc->alpha = sc->rz / pq;
+            }
+            *ticket = 0u;
+        }
+    }
+}
+
+// x += alpha p, r -= alpha q, z = D^-1 r; partials of r.r and r.z;
+// last CTA: convergence test, beta
+__global__ void __launch_bounds__(kRedBlock) k_cg_update(int32_t n_nodes, const double *__restrict__ p,
+                                                         const double *__restrict__ q,
+                                                         const double *__restrict__ dinv,
+                                                         double *__restrict__ x, double *__restrict__ r,
+                                                         double *__restrict__ z, double *part, int64_t n_red,
+                                                         unsigned *ticket, CGScalars *sc)
+{
+    if (*reinterpret_cast<volatile int *>(&sc->done)) return;
+    const double alpha = *reinterpret_cast<volatile double *>(&sc->alpha);
+    const int32_t i = blockIdx.x * kRedBlock + threadIdx.x;
+    double v[2] = {0.0, 0.0};
+    if (i < n_nodes) {
+        const double2 pp = reinterpret_cast<const double2 *>(p)[i];
+        const double2 qq = reinterpret_cast<const double2 *>(q)[i];
+        const double2 di = reinterpret_cast<const double2 *>(dinv)[i];
+        double2 xx = reinterpret_cast<double2 *>(x)[i];
+        double2 rr = reinterpret_cast<double2 *>(r)[i];
+        xx.x = fma(alpha, pp.x, xx.x);
+        xx.y = fma(alpha, pp.y, xx.y);
+        rr.x = fma(-alpha, qq.x, rr.x);
+        rr.y = fma(-alpha, qq.y, rr.y);
+        const double2 zz = make_double2(rr.x * di.x, rr.y * di.y);
+        reinterpret_cast<double2 *>(x)[i] = xx;
+        reinterpret_cast<double2 *>(r)[i] = rr;
+        reinterpret_cast<double2 *>(z)[i] = zz;
+        v[0] = fma(rr.y, rr.y, fma(rr.x, rr.x, 0.0));
+        v[1] = fma(rr.y, zz.y, fma(rr.x, zz.x, 0.0));
+    }
+    if (block_partials<2>(v, part, n_red, ticket)) {
+        double o[2];
+        final_reduce<2>(part, n_red, o);
+        if (threadIdx.x == 0) {
+            const double rr = o[0], rzn = o[1];
+            sc->rr = rr;
+            sc->iters += 1;
+            if (rr <= sc->thr) {
+                sc->done = 1;
+            } else if (sc->iters >= sc->max_it) {
+                sc->done = 1;
+                sc->status = IPFEM_NONCONVERGED;
+            } else {
+                sc->beta = rzn / sc->rz;
+                sc->rz = rzn;
+            }
+            *ticket = 0u;
+        }
+    }
+}
+
+__global__ void __launch_bounds__(kRedBlock) k_cg_pupdate(int32_t n_nodes, const double *__restrict__ z,
+                                                          double *__restrict__ p, const CGScalars *sc)
+{
+    if (*reinterpret_cast<const volatile int *>(&sc->done)) return;
+    const double beta = *reinterpret_cast<const volatile double *>(&sc->beta);
+    const int32_t i = blockIdx.x * kRedBlock + threadIdx.x;
+    if (i >= n_nodes) return;
+    const double2 zz = reinterpret_cast<const double2 *>(z)[i];
+    double2 pp = reinterpret_cast<double2 *>(p)[i];
+    pp.x = fma(beta, pp.x, zz.x);
+    pp.y = fma(beta, pp.y, zz.y);
+    reinterpret_cast<double2 *>(p)[i] = pp;
+}
+
+__global__ void __launch_bounds__(kRedBlock) k_dot(int32_t n_nodes, const double *__restrict__ a,
+                                                   const double *__restrict__ b, double *part, int64_t n_red,
+                                                   unsigned *ticket, double *out)
+{
+    const int32_t i = blockIdx.x * kRedBlock + threadIdx.x;
+    double v[1] = {0.0};
+    if (i < n_nodes) {
+        const double2 aa = reinterpret_cast<const double2 *>(a)[i];
+        const double2 bb = reinterpret_cast<const double2 *>(b)[i];
+        v[0] = fma(aa.y, bb.y, fma(aa.x, bb.x, 0.0));
+    }
+    if (block_partials<1>(v, part, n_red, ticket)) {
+        double o[1];
+        final_reduce<1>(part, n_red, o);
+        if (threadIdx.x == 0) {
+            *out = o[0];
+            *ticket = 0u;
+        }
+    }
+}
+
+__global__ void k_add(int64_t n, double *__restrict__ u, const double *__restrict__ du)
+{
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i < n) u[i] = u[i] + du[i];
+}
+
+static unsigned grid_nodes(const ipfem_ctx *c)
+{
+    return (unsigned)((c->s.n_nodes + kRedBlock - 1) / kRedBlock);
+}
+
+void launch_cg_init(ipfem_ctx *c, const double *d_b, double rtol, int max_it)
+{
+    k_cg_init<<<grid_nodes(c), kRedBlock, 0, c->stream>>>(c->s.n_nodes, d_b, c->d_dinv, c->d_x, c->d_r, c->d_z,
+                                                          c->d_p, c->d_part, c->n_red, c->d_counters + 0, c->d_sc,
+                                                          rtol, max_it);
+}
+
+void launch_cg_iteration(ipfem_ctx *c)
+{
+    const unsigned g = grid_nodes(c);
+    k_cg_spmv<<<g, kRedBlock, 0, c->stream>>>(c->s.n_nodes, c->d_slice_base, c->d_rowlen, c->d_sell_col, c->d_K,
+                                              c->d_fixed, c->d_p, c->d_q, c->d_part, c->n_red, c->d_counters + 1,
+                                              c->d_sc);
+    k_cg_update<<<g, kRedBlock, 0, c->stream>>>(c->s.n_nodes, c->d_p, c->d_q, c->d_dinv, c->d_x, c->d_r, c->d_z,
+                                                c->d_part, c->n_red, c->d_counters + 2, c->d_sc);
+    k_cg_pupdate<<<g, kRedBlock, 0, c->stream>>>(c->s.n_nodes, c->d_z, c->d_p, c->d_sc);
+}
+
+void launch_dot(ipfem_ctx *c, const double *a, const double *b, double *d_out)
+{
+    k_dot<<<grid_nodes(c), kRedBlock, 0, c->stream>>>(c->s.n_nodes, a, b, c->d_part, c->n_red, c->d_counters + 3,
+                                                      d_out);
+}
+
+void launch_axpy_u(ipfem_ctx *c, double *d_u, const double *d_du)
+{
+    const int64_t n = c->s.neq;
+    k_add<<<(unsigned)((n + 255) / 256), 256, 0, c->stream>>>(n, d_u, d_du);
+}
+
+}  // namespace ipfem

@@ -95,8 +95,8 @@ void orc_compute_sigma_batch(int64_t npts, int pts_per_mat,
  * 32*s+l: acc = fma(a[2n],b[2n],0); acc = fma(a[2n+1],b[2n+1],acc); the 32
  * lanes are folded by the shuffle-down tree (16,8,4,2,1).  Level 1: the 8
  * slice sums of a 256-node block are folded by the tree (4,2,1).  Level 2:
- * the block partials are strided over 1024 threads (t, t+1024, ... summed in
- * order from 0), each warp folds by (16..1), and the 32 warp sums by (16..1). */
+ * the block partials are strided over 256 threads (t, t+256, ... summed in
+ * order from 0), each warp folds by (16..1), and the 8 warp sums by (4,2,1). */
 double orc_dot(int64_t nnodes, const double *a, const double *b);
 /* the three levels separately (exposed for tests) */
 int64_t orc_dot_partials(int64_t nnodes, const double *a, const double *b, double *partials);

@@ -470,15 +470,17 @@ int64_t orc_dot_partials(int64_t nnodes, const double *a, const double *b, doubl
 
 double orc_dot_final(int64_t np, const double *partials)
 {
-    double acc[1024];
-    for (int t = 0; t < 1024; t++) {
+    double acc[256];
+    for (int t = 0; t < 256; t++) {
         double s = 0.0;
-        for (int64_t k = t; k < np; k += 1024) s = s + partials[k];
+        for (int64_t k = t; k < np; k += 256) s = s + partials[k];
         acc[t] = s;
     }
-    double ws[32];
-    for (int w = 0; w < 32; w++) ws[w] = tree32(&acc[32 * w]);
-    return tree32(ws);
+    double ws[8];
+    for (int w = 0; w < 8; w++) ws[w] = tree32(&acc[32 * w]);
+    for (int off = 4; off >= 1; off >>= 1)
+        for (int l = 0; l < off; l++) ws[l] = ws[l] + ws[l + off];
+    return ws[0];
 }
 
 double orc_dot(int64_t nnodes, const double *a, const double *b)

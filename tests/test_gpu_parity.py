@@ -1,0 +1,112 @@
+"""GPU parity: libipfem (sm_103a) against the CPU oracle, through the C-ABI.
+
+The plain FP64 method is deterministic and follows the oracle's operation
+order, so the comparisons are exact (==, which treats +0 and -0 as equal);
+m_type flags, colours and dof maps are compared bit for bit.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+ip = pytest.importorskip("intpointsfem_gb300")
+from oracle import pyoracle as po  # noqa: E402
+
+
+def _pair(n, **kw):
+    w = ip.WellboreMesh(ip.wellbore_params(n, **kw))
+    sm = ip.ElastoPlasticIntPointsStructMatrix(w)
+    P = po.OracleProblem(po.default_params(n, **kw), nthreads=0)
+    return sm, P
+
+
+def _soa4(p6, n_ip):
+    """oracle 6-component AoS -> device 4-component SoA {xx, xy, yy, zz}"""
+    p = p6.reshape(n_ip, 6)
+    return np.ascontiguousarray(np.stack([p[:, 0], p[:, 1], p[:, 3], p[:, 5]]).ravel())
+
+
+def _eq(a, b):
+    return np.array_equal(np.asarray(a), np.asarray(b), equal_nan=True)
+
+
+@pytest.mark.parametrize("n,mode", [(6, 0), (12, 2)])
+def test_setup_matches_oracle(n, mode):
+    sm, P = _pair(n, material_mode=mode)
+    assert sm.n_colors == P.n_colors == 4
+    assert np.array_equal(sm.get_setup(0), P.arr("el_color"))
+    assert np.array_equal(sm.get_setup(2), P.arr("dofs"))
+    B = P.arr("B").reshape(-1, 9, 3, 18)
+    dn = sm.get_setup(3).reshape(-1, 9, 2, 9)
+    assert np.array_equal(dn[:, :, 0, :], B[:, :, 0, 0::2])
+    assert np.array_equal(dn[:, :, 1, :], B[:, :, 1, 0::2])
+    assert np.array_equal(sm.get_setup(4), P.arr("weight"))
+
+
+@pytest.mark.parametrize("n,mode,lam", [(8, 0, 0.5), (16, 2, 1.0)])
+def test_residual_bit_exact(n, mode, lam):
+    sm, P = _pair(n, material_mode=mode)
+    rng = np.random.default_rng(n)
+    u = rng.normal(size=sm.neq) * 2e-3
+    u[P.arr("fixed").astype(bool)] = 0.0
+    sm.SetLoadFactor(lam)
+    r = sm.assemble_residual(u, np.zeros(sm.neq))
+    ro = P.assemble_residual(u.copy(), lam)
+    assert _eq(r, ro), np.abs(r - ro).max()
+    # commit (update_mem) and compare the integration-point state
+    sm.SetUpdateMem(True)
+    sm.assemble_residual(u, np.zeros(sm.neq))
+    sm.SetUpdateMem(False)
+    P.assemble_residual(u.copy(), lam, update_mem=True)
+    mt = sm.get_state(3)
+    assert np.array_equal(mt, P.arr("mtype").astype(np.float64))
+    assert (mt != 0).sum() > 0, "test point should include plastic points"
+    assert _eq(sm.get_state(0), _soa4(P.arr("eps_p"), P.n_ip))
+    assert _eq(sm.get_state(1), _soa4(P.arr("sigma"), P.n_ip))
+    assert _eq(sm.get_state(2), P.arr("alpha"))
+
+
+@pytest.mark.parametrize("n,mode", [(8, 0), (16, 2)])
+def test_tangent_and_cg_bit_exact(n, mode):
+    sm, P = _pair(n, material_mode=mode)
+    rng = np.random.default_rng(3 * n)
+    u = rng.normal(size=sm.neq) * 2e-3
+    u[P.arr("fixed").astype(bool)] = 0.0
+    sm.SetLoadFactor(0.7)
+    r = sm.assemble(u, np.zeros(sm.neq))
+    ro = P.assemble(u.copy(), 0.7)
+    assert _eq(r, ro)
+    rp, col, K = sm.stiffness()
+    assert np.array_equal(rp, P.arr("row_ptr")) and np.array_equal(col, P.arr("col"))
+    assert _eq(K, P.arr("K"))
+    x, it = sm.solve(r, rtol=1e-9)
+    xo, ito = P.pcg(ro, rtol=1e-9)
+    assert it == ito > 0
+    assert _eq(x, xo)
+
+
+def test_newton_cfg1_bit_exact():
+    """Config 1 (40 x 40, 10 load steps): the whole load-stepped Newton/CG solve."""
+    sm, P = _pair(40)
+    ug, uo = np.zeros(sm.neq), np.zeros(sm.neq)
+    sg, lg = sm.newton(ug, 10, newton_max_it=30)
+    so, lo = P.solve_steps(uo, 10, newton_max_it=30)
+    assert sg.newton_iters == so.newton_iters and sg.cg_iters == so.cg_iters
+    assert _eq(lg, lo)
+    assert _eq(ug, uo)
+    mt = sm.get_state(3)
+    assert np.array_equal(mt, P.arr("mtype").astype(np.float64)) and (mt != 0).sum() > 50
+    assert _eq(sm.get_state(0), _soa4(P.arr("eps_p"), P.n_ip))
+    assert _eq(sm.get_state(1), _soa4(P.arr("sigma"), P.n_ip))
+
+
+def test_deterministic_repeat():
+    sm, _ = _pair(12, material_mode=2)
+    rng = np.random.default_rng(5)
+    u = rng.normal(size=sm.neq) * 1e-3
+    sm.SetLoadFactor(1.0)
+    a = sm.assemble(u, np.zeros(sm.neq))
+    xa, ia = sm.solve(a)
+    b = sm.assemble(u, np.zeros(sm.neq))
+    xb, ib = sm.solve(b)
+    assert ia == ib and np.array_equal(a.view(np.int64), b.view(np.int64)) and np.array_equal(xa.view(np.int64), xb.view(np.int64))
