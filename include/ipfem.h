@@ -81,6 +81,8 @@ typedef struct {
 /* ------------------------------------------------------------- lifecycle */
 ipfem_status ipfem_create(const ipfem_mesh *mesh, const ipfem_material *mat, ipfem_ctx **out);
 void ipfem_destroy(ipfem_ctx *ctx);
+/* message of the last failure on ctx; with ctx == NULL, of the last failed
+ * ipfem_create on the calling thread */
 const char *ipfem_last_error(const ipfem_ctx *ctx);
 const char *ipfem_status_string(ipfem_status s);
 /* sizes: n_elements, n_ip, n_nodes, neq, n_colors, n_blocks (nodal 2x2 blocks) */
@@ -135,7 +137,22 @@ ipfem_status ipfem_newton_solve(ipfem_ctx *ctx, const ipfem_solve_opts *opts, in
                                 int32_t step_end, double *u, int where, ipfem_solve_stats *stats,
                                 double *log, int32_t log_cap);
 
+/* Resumable form of the same loop: begin sets the options and the step range;
+ * each advance performs n_iters Newton iterations (0 = until the last step is
+ * accepted).  An iteration is: CG on the current tangent, u += du,
+ * Assemble(K, rhs), convergence test; a converged step is accepted (state
+ * committed) inside the iteration that converged, and the next step's first
+ * assembly opens the following iteration.  *n_done receives the iterations
+ * performed. */
+ipfem_status ipfem_newton_begin(ipfem_ctx *ctx, const ipfem_solve_opts *opts, int32_t step_begin, int32_t step_end);
+ipfem_status ipfem_newton_advance(ipfem_ctx *ctx, int32_t n_iters, double *u, int where, ipfem_solve_stats *stats,
+                                  double *log, int32_t log_cap, int32_t *n_done);
+
 /* ------------------------------------------------ TPZCudaCalls replacements */
+/* Canonical deterministic dot product of two device vectors of length neq
+ * (the reduction order of the CG; replaces cublasDdot in
+ * TPZCudaCalls::SolveCG, TPZCudaCalls.cu:245-286).  *out is a host double. */
+ipfem_status ipfem_dot(ipfem_ctx *ctx, const double *d_a, const double *d_b, double *out);
 /* TPZNumericalIntegrator::Multiply (TPZNumericalIntegrator.cpp:25-37):
  * gather + B*u.  d_strain: device, SoA [3][n_ip] (eps_xx, gamma_xy, eps_yy). */
 ipfem_status ipfem_gather_strain(ipfem_ctx *ctx, const double *d_u, double *d_strain);
@@ -159,6 +176,16 @@ ipfem_status ipfem_set_state(ipfem_ctx *ctx, int field, const double *in);
  * 2 dof indexes [n_elements*18] int32 (fDoFIndexes),
  * 3 dphi [n_elements*162] double, 4 weights [n_ip] double. */
 ipfem_status ipfem_get_setup(ipfem_ctx *ctx, int field, void *out);
+
+/* ------------------------------------------------------------ diagnostics */
+/* number of kernels this context has launched (graph nodes included) */
+uint64_t ipfem_launch_count(const ipfem_ctx *ctx);
+/* average duration of the CG block SpMV on the current tangent, timed with
+ * CUDA events on the context's stream over `reps` back-to-back launches */
+ipfem_status ipfem_profile_spmv(ipfem_ctx *ctx, int reps, double *ms_per_launch);
+/* FP64 fma issue rate of this device (TFLOP/s, 2 flops per fma), measured with
+ * a dependent-chain probe kernel timed by CUDA events */
+ipfem_status ipfem_measure_fp64_peak(ipfem_ctx *ctx, double *tflops);
 
 /* --------------------------------------------------- wellbore mesh provider */
 /* Structured quarter annulus standing in for the reference's NeoPZ/Gmsh mesh

@@ -94,6 +94,13 @@ def lib():
             "ipfem_solve": (S, [P, P, P, C.c_double, S, S, C.POINTER(C.c_int)]),
             "ipfem_newton_solve": (S, [P, C.POINTER(SolveOpts), C.c_int32, C.c_int32, P, S,
                                        C.POINTER(SolveStats), _dp, C.c_int32]),
+            "ipfem_newton_begin": (S, [P, C.POINTER(SolveOpts), C.c_int32, C.c_int32]),
+            "ipfem_newton_advance": (S, [P, C.c_int32, P, S, C.POINTER(SolveStats), _dp, C.c_int32,
+                                         C.POINTER(C.c_int32)]),
+            "ipfem_dot": (S, [P, P, P, _dp]),
+            "ipfem_launch_count": (C.c_uint64, [P]),
+            "ipfem_profile_spmv": (S, [P, S, _dp]),
+            "ipfem_measure_fp64_peak": (S, [P, _dp]),
             "ipfem_gather_strain": (S, [P, P, P]),
             "ipfem_compute_sigma": (S, [P, S, P, P, P]),
             "ipfem_scatter_residual": (S, [P, P, P]),
@@ -196,8 +203,7 @@ class ElastoPlasticIntPointsStructMatrix:
         self._ctx = C.c_void_p()
         st = lib().ipfem_create(C.byref(mesh), C.byref(material), C.byref(self._ctx))
         if st != 0:
-            msg = lib().ipfem_last_error(self._ctx).decode() if self._ctx else ""
-            raise IpfemError(st, msg or "ipfem_create failed")
+            raise IpfemError(st, lib().ipfem_last_error(None).decode() or "ipfem_create failed")
         sz = np.zeros(6, np.int64)
         lib().ipfem_sizes(self._ctx, _np_ptr(sz, _lp))
         self.n_el, self.n_ip, self.n_nodes, self.neq, self.n_colors, self.n_blocks = map(int, sz)
@@ -282,6 +288,40 @@ class ElastoPlasticIntPointsStructMatrix:
         if not (allow_nonconverged and s == 1):
             self._check(s)
         return st, log[:3 * min(st.newton_iters, log_cap)].reshape(-1, 3)
+
+    def newton_begin(self, n_steps, step_begin=0, step_end=None, newton_rtol=1e-8, newton_max_it=20, cg_rtol=1e-8,
+                     cg_max_it=200000):
+        if step_end is None:
+            step_end = n_steps
+        o = SolveOpts(int(n_steps), float(newton_rtol), int(newton_max_it), float(cg_rtol), int(cg_max_it))
+        self._check(lib().ipfem_newton_begin(self._ctx, C.byref(o), int(step_begin), int(step_end)))
+
+    def newton_advance(self, u, n_iters, where=HOST, log_cap=256):
+        st = SolveStats()
+        log = np.zeros(3 * log_cap)
+        n = C.c_int32()
+        self._check(lib().ipfem_newton_advance(self._ctx, int(n_iters), _ptr(u), where, C.byref(st),
+                                               _np_ptr(log, _dp), int(log_cap), C.byref(n)))
+        return st, log[:3 * min(n.value, log_cap)].reshape(-1, 3)
+
+    def dot(self, d_a, d_b):
+        out = np.zeros(1)
+        self._check(lib().ipfem_dot(self._ctx, _ptr(d_a), _ptr(d_b), _np_ptr(out, _dp)))
+        return float(out[0])
+
+    @property
+    def launch_count(self):
+        return int(lib().ipfem_launch_count(self._ctx))
+
+    def profile_spmv(self, reps=20):
+        out = np.zeros(1)
+        self._check(lib().ipfem_profile_spmv(self._ctx, int(reps), _np_ptr(out, _dp)))
+        return float(out[0])
+
+    def measure_fp64_peak(self):
+        out = np.zeros(1)
+        self._check(lib().ipfem_measure_fp64_peak(self._ctx, _np_ptr(out, _dp)))
+        return float(out[0])
 
     def gather_strain(self, d_u, d_strain):
         self._check(lib().ipfem_gather_strain(self._ctx, _ptr(d_u), _ptr(d_strain)))

@@ -11,6 +11,9 @@ using namespace ipfem;
 
 namespace {
 
+// message of the last failed ipfem_create on this thread (no context exists then)
+thread_local std::string t_create_err;
+
 ipfem_status fail(ipfem_ctx *c, ipfem_status s, const std::string &msg)
 {
     if (c) c->err = msg;
@@ -52,6 +55,10 @@ void free_all(ipfem_ctx *c)
     if (c->h_sc) cudaFreeHost(c->h_sc);
     if (c->h_pin) cudaFreeHost(c->h_pin);
     if (c->cg_exec) cudaGraphExecDestroy(c->cg_exec);
+    if (c->ev_ready) {
+        cudaEventDestroy(c->ev[0]);
+        cudaEventDestroy(c->ev[1]);
+    }
     if (c->stream) cudaStreamDestroy(c->stream);
 }
 
@@ -77,6 +84,7 @@ ipfem_status sync_check(ipfem_ctx *c)
 // residual of the current load factor at d_u into d_out (device)
 void residual_device(ipfem_ctx *c, const double *d_u, double *d_out, int update_mem)
 {
+    c->launches += 4;
     launch_gather_strain(c, d_u, c->d_strain);
     launch_compute_sigma(c, update_mem, c->d_strain, c->d_sigma_w, nullptr);
     launch_stress_residual(c, c->d_sigma_w, c->d_fe);
@@ -85,6 +93,7 @@ void residual_device(ipfem_ctx *c, const double *d_u, double *d_out, int update_
 
 void tangent_device(ipfem_ctx *c, const double *d_u, double *d_out, int update_mem)
 {
+    c->launches += 6 + c->s.n_colors;
     launch_gather_strain(c, d_u, c->d_strain);
     launch_compute_sigma(c, update_mem, c->d_strain, c->d_sigma_w, c->d_dep);
     launch_stress_residual(c, c->d_sigma_w, c->d_fe);
@@ -97,6 +106,7 @@ void tangent_device(ipfem_ctx *c, const double *d_u, double *d_out, int update_m
 ipfem_status cg_device(ipfem_ctx *c, const double *d_b, double rtol, int max_it, int *iters)
 {
     launch_cg_init(c, d_b, rtol, max_it);
+    c->launches += 1;
     const int batch = 32;
     if (!c->cg_exec || c->cg_batch != batch) {
         if (c->cg_exec) {
@@ -116,6 +126,7 @@ ipfem_status cg_device(ipfem_ctx *c, const double *d_b, double rtol, int max_it,
     for (;;) {
         CK(cudaGraphLaunch(c->cg_exec, c->stream));
         launched += batch;
+        c->launches += 3 * batch;
         CK(cudaMemcpyAsync(c->h_sc, c->d_sc, sizeof(CGScalars), cudaMemcpyDeviceToHost, c->stream));
         CK(cudaStreamSynchronize(c->stream));
         if (c->h_sc->done || launched >= max_it + batch) break;
@@ -134,6 +145,7 @@ ipfem_status cg_device(ipfem_ctx *c, const double *d_b, double rtol, int max_it,
 ipfem_status dot_host(ipfem_ctx *c, const double *a, const double *b, double *out)
 {
     launch_dot(c, a, b, c->d_dotres);
+    c->launches += 1;
     CK(cudaMemcpyAsync(&c->h_pin[0], c->d_dotres, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
     CK(cudaStreamSynchronize(c->stream));
     *out = c->h_pin[0];
@@ -161,7 +173,7 @@ const char *ipfem_status_string(ipfem_status s)
 
 const char *ipfem_last_error(const ipfem_ctx *c)
 {
-    return c ? c->err.c_str() : "null context";
+    return c ? c->err.c_str() : t_create_err.c_str();
 }
 
 void *ipfem_stream(ipfem_ctx *c)
@@ -176,20 +188,25 @@ ipfem_status ipfem_create(const ipfem_mesh *mesh, const ipfem_material *mat, ipf
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
         cudaGetLastError();
+        t_create_err = "no CUDA device";
         return IPFEM_NO_DEVICE;
     }
     ipfem_ctx *c = new (std::nothrow) ipfem_ctx();
     if (!c) return IPFEM_OOM;
     ipfem_status st = IPFEM_OK;
     auto bail = [&](ipfem_status s) {
+        t_create_err = c->err.empty() ? ipfem_status_string(s) : c->err;
         free_all(c);
         delete c;
         return s;
     };
+    t_create_err.clear();
     cudaGetDevice(&c->device);
     cudaDeviceProp prop;
-    if (cudaGetDeviceProperties(&prop, c->device) != cudaSuccess || prop.major != 10 || prop.minor != 3)
+    if (cudaGetDeviceProperties(&prop, c->device) != cudaSuccess || prop.major != 10 || prop.minor != 3) {
+        c->err = "libipfem is built for sm_103 (GB300) only";
         return bail(IPFEM_NO_DEVICE);
+    }
     std::string msg = build_setup(mesh, mat, c->s);
     if (!msg.empty()) {
         c->err = msg;
@@ -367,12 +384,111 @@ ipfem_status ipfem_solve(ipfem_ctx *c, const double *b, double *x, double rtol, 
     return st;
 }
 
-ipfem_status ipfem_newton_solve(ipfem_ctx *c, const ipfem_solve_opts *o, int32_t s0, int32_t s1, double *u, int where,
-                                ipfem_solve_stats *stats, double *log, int32_t log_cap)
+// One Newton iteration of the load-stepped solve (main.cpp:185-256): CG on the
+// current tangent, u += du, Assemble(K, rhs), convergence test; a load step
+// that converges (or reaches newton_max_it) is accepted (state commit,
+// main.cpp:487-522) and the next step's first assembly happens at the start
+// of the following iteration.
+static ipfem_status newton_advance(ipfem_ctx *c, int32_t n_iters, double *du, ipfem_solve_stats *st, double *log,
+                                   int32_t log_cap, int32_t *nlog)
 {
-    if (!c || !o || !u || o->n_steps <= 0 || s0 < 0 || s1 > o->n_steps || s0 > s1 ||
-        (where != IPFEM_HOST && where != IPFEM_DEVICE))
+    NewtonState &ns = c->ns;
+    const ipfem_solve_opts &o = ns.opts;
+    cudaEvent_t *ev = c->ev;
+    auto elapsed = [&]() {
+        float ms = 0;
+        cudaEventSynchronize(ev[1]);
+        cudaEventElapsedTime(&ms, ev[0], ev[1]);
+        return (double)ms;
+    };
+    int32_t done = 0;
+    while (done < n_iters && ns.step < ns.step_end) {
+        if (!ns.open) {
+            c->load_factor = (double)(ns.step + 1) / (double)o.n_steps;
+            cudaEventRecord(ev[0], c->stream);
+            tangent_device(c, du, c->d_rhs, 0);
+            cudaEventRecord(ev[1], c->stream);
+            double r0sq = 0;
+            ipfem_status e = dot_host(c, c->d_rhs, c->d_rhs, &r0sq);
+            st->ms_assemble += elapsed();
+            if (e != IPFEM_OK) return e;
+            ns.r0 = std::sqrt(r0sq);
+            ns.rn = ns.r0;
+            ns.it = 0;
+            ns.open = 1;
+            if (!std::isfinite(ns.r0)) return fail(c, IPFEM_NAN, "residual is not finite");
+        }
+        bool conv = (ns.r0 == 0.0);
+        if (!conv) {
+            int k = 0;
+            cudaEventRecord(ev[0], c->stream);
+            ipfem_status e = cg_device(c, c->d_rhs, o.cg_rtol, o.cg_max_it, &k);
+            cudaEventRecord(ev[1], c->stream);
+            st->ms_solve += elapsed();
+            st->cg_iters += k;
+            if (e != IPFEM_OK && e != IPFEM_NONCONVERGED) return e;
+            launch_axpy_u(c, du, c->d_x);
+            ns.it++;
+            done++;
+            st->newton_iters++;
+            cudaEventRecord(ev[0], c->stream);
+            tangent_device(c, du, c->d_rhs, 0);
+            cudaEventRecord(ev[1], c->stream);
+            double rsq = 0;
+            e = dot_host(c, c->d_rhs, c->d_rhs, &rsq);
+            st->ms_assemble += elapsed();
+            if (e != IPFEM_OK) return e;
+            ns.rn = std::sqrt(rsq);
+            if (!std::isfinite(ns.rn)) return fail(c, IPFEM_NAN, "residual is not finite");
+            if (log && *nlog < log_cap) {
+                log[3 * *nlog + 0] = (double)ns.step;
+                log[3 * *nlog + 1] = (double)k;
+                log[3 * *nlog + 2] = ns.rn;
+                (*nlog)++;
+            }
+            conv = ns.rn <= o.newton_rtol * ns.r0;
+        }
+        if (conv || ns.it >= o.newton_max_it) {
+            st->last_step_iters = ns.it;
+            st->final_res = ns.r0 > 0.0 ? ns.rn / ns.r0 : 0.0;
+            if (!conv) ns.all_converged = 0;
+            cudaEventRecord(ev[0], c->stream);
+            residual_device(c, du, c->d_b, 1);
+            cudaEventRecord(ev[1], c->stream);
+            st->ms_commit += elapsed();
+            ipfem_status e = sync_check(c);
+            if (e != IPFEM_OK) return e;
+            ns.step++;
+            ns.open = 0;
+        }
+    }
+    st->converged = ns.all_converged;
+    return IPFEM_OK;
+}
+
+ipfem_status ipfem_newton_begin(ipfem_ctx *c, const ipfem_solve_opts *o, int32_t s0, int32_t s1)
+{
+    if (!c || !o || o->n_steps <= 0 || s0 < 0 || s1 > o->n_steps || s0 > s1 || o->newton_max_it < 1)
+        return fail(c, IPFEM_INVALID, "bad Newton options");
+    c->ns = NewtonState();
+    c->ns.opts = *o;
+    c->ns.step = s0;
+    c->ns.step_end = s1;
+    c->ns.active = 1;
+    if (!c->ev_ready) {
+        CK(cudaEventCreate(&c->ev[0]));
+        CK(cudaEventCreate(&c->ev[1]));
+        c->ev_ready = true;
+    }
+    return IPFEM_OK;
+}
+
+ipfem_status ipfem_newton_advance(ipfem_ctx *c, int32_t n_iters, double *u, int where, ipfem_solve_stats *stats,
+                                  double *log, int32_t log_cap, int32_t *n_done)
+{
+    if (!c || !u || n_iters < 0 || (where != IPFEM_HOST && where != IPFEM_DEVICE))
         return fail(c, IPFEM_INVALID, "bad args");
+    if (!c->ns.active) return fail(c, IPFEM_INVALID, "ipfem_newton_begin not called");
     const size_t nb = (size_t)c->s.neq * sizeof(double);
     double *du = u;
     if (where == IPFEM_HOST) {
@@ -380,84 +496,89 @@ ipfem_status ipfem_newton_solve(ipfem_ctx *c, const ipfem_solve_opts *o, int32_t
         du = c->d_u;
     }
     ipfem_solve_stats st{};
-    st.converged = 1;
-    cudaEvent_t ev[2];
-    CK(cudaEventCreate(&ev[0]));
-    CK(cudaEventCreate(&ev[1]));
-    auto elapsed = [&]() {
-        float ms = 0;
-        cudaEventSynchronize(ev[1]);
-        cudaEventElapsedTime(&ms, ev[0], ev[1]);
-        return (double)ms;
-    };
-    ipfem_status ret = IPFEM_OK;
     int32_t nlog = 0;
     const int saved_update = c->update_mem;
     c->update_mem = 0;
-    for (int32_t step = s0; step < s1 && ret == IPFEM_OK; step++) {
-        c->load_factor = (double)(step + 1) / (double)o->n_steps;
-        cudaEventRecord(ev[0], c->stream);
-        tangent_device(c, du, c->d_rhs, 0);
-        cudaEventRecord(ev[1], c->stream);
-        double r0sq = 0;
-        ipfem_status e = dot_host(c, c->d_rhs, c->d_rhs, &r0sq);
-        st.ms_assemble += elapsed();
-        if (e != IPFEM_OK) { ret = e; break; }
-        const double r0 = std::sqrt(r0sq);
-        double rn = r0;
-        bool conv = (r0 == 0.0);
-        int it = 0;
-        if (!std::isfinite(r0)) { ret = fail(c, IPFEM_NAN, "residual is not finite"); break; }
-        while (!conv && it < o->newton_max_it) {
-            int k = 0;
-            cudaEventRecord(ev[0], c->stream);
-            e = cg_device(c, c->d_rhs, o->cg_rtol, o->cg_max_it, &k);
-            cudaEventRecord(ev[1], c->stream);
-            st.ms_solve += elapsed();
-            st.cg_iters += k;
-            if (e != IPFEM_OK && e != IPFEM_NONCONVERGED) { ret = e; break; }
-            launch_axpy_u(c, du, c->d_x);
-            it++;
-            cudaEventRecord(ev[0], c->stream);
-            tangent_device(c, du, c->d_rhs, 0);
-            cudaEventRecord(ev[1], c->stream);
-            double rsq = 0;
-            e = dot_host(c, c->d_rhs, c->d_rhs, &rsq);
-            st.ms_assemble += elapsed();
-            if (e != IPFEM_OK) { ret = e; break; }
-            rn = std::sqrt(rsq);
-            if (!std::isfinite(rn)) { ret = fail(c, IPFEM_NAN, "residual is not finite"); break; }
-            if (log && nlog < log_cap) {
-                log[3 * nlog + 0] = (double)step;
-                log[3 * nlog + 1] = (double)k;
-                log[3 * nlog + 2] = rn;
-                nlog++;
-            }
-            conv = rn <= o->newton_rtol * r0;
-        }
-        if (ret != IPFEM_OK) break;
-        st.newton_iters += it;
-        st.last_step_iters = it;
-        st.final_res = r0 > 0.0 ? rn / r0 : 0.0;
-        if (!conv) st.converged = 0;
-        // accept: commit the integration-point state (main.cpp:487-522)
-        cudaEventRecord(ev[0], c->stream);
-        residual_device(c, du, c->d_b, 1);
-        cudaEventRecord(ev[1], c->stream);
-        st.ms_commit += elapsed();
-        e = sync_check(c);
-        if (e != IPFEM_OK) { ret = e; break; }
-    }
+    ipfem_status ret = newton_advance(c, n_iters == 0 ? INT32_MAX : n_iters, du, &st, log, log_cap, &nlog);
     c->update_mem = saved_update;
-    cudaEventDestroy(ev[0]);
-    cudaEventDestroy(ev[1]);
     if (where == IPFEM_HOST) {
         CK(cudaMemcpyAsync(u, c->d_u, nb, cudaMemcpyDeviceToHost, c->stream));
         CK(cudaStreamSynchronize(c->stream));
     }
     if (stats) *stats = st;
-    if (ret == IPFEM_OK && !st.converged) return fail(c, IPFEM_NONCONVERGED, "Newton did not converge in every step");
+    if (n_done) *n_done = st.newton_iters;
     return ret;
+}
+
+ipfem_status ipfem_newton_solve(ipfem_ctx *c, const ipfem_solve_opts *o, int32_t s0, int32_t s1, double *u, int where,
+                                ipfem_solve_stats *stats, double *log, int32_t log_cap)
+{
+    ipfem_status st = ipfem_newton_begin(c, o, s0, s1);
+    if (st != IPFEM_OK) return st;
+    st = ipfem_newton_advance(c, 0, u, where, stats, log, log_cap, nullptr);
+    c->ns.active = 0;
+    if (st == IPFEM_OK && stats && !stats->converged)
+        return fail(c, IPFEM_NONCONVERGED, "Newton did not converge in every step");
+    return st;
+}
+
+uint64_t ipfem_launch_count(const ipfem_ctx *c)
+{
+    return c ? c->launches : 0;
+}
+
+ipfem_status ipfem_dot(ipfem_ctx *c, const double *d_a, const double *d_b, double *out)
+{
+    if (!c || !d_a || !d_b || !out) return fail(c, IPFEM_INVALID, "bad args");
+    return dot_host(c, d_a, d_b, out);
+}
+
+ipfem_status ipfem_measure_fp64_peak(ipfem_ctx *c, double *tflops)
+{
+    if (!c || !tflops) return fail(c, IPFEM_INVALID, "bad args");
+    int sms = 0;
+    CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device));
+    const int grid = sms * 8, iters = 4096;
+    double *d = nullptr;
+    CK(cudaMallocAsync((void **)&d, (size_t)grid * 256 * sizeof(double), c->stream));
+    if (!c->ev_ready) {
+        CK(cudaEventCreate(&c->ev[0]));
+        CK(cudaEventCreate(&c->ev[1]));
+        c->ev_ready = true;
+    }
+    launch_fp64_probe(c, d, grid, iters);
+    CK(cudaEventRecord(c->ev[0], c->stream));
+    launch_fp64_probe(c, d, grid, iters);
+    CK(cudaEventRecord(c->ev[1], c->stream));
+    CK(cudaEventSynchronize(c->ev[1]));
+    float ms = 0;
+    CK(cudaEventElapsedTime(&ms, c->ev[0], c->ev[1]));
+    CK(cudaFreeAsync(d, c->stream));
+    c->launches += 2;
+    *tflops = 2.0 * 8.0 * iters * (double)grid * 256 / (ms * 1e-3) / 1e12;
+    return sync_check(c);
+}
+
+ipfem_status ipfem_profile_spmv(ipfem_ctx *c, int reps, double *ms_per_launch)
+{
+    if (!c || reps < 1 || !ms_per_launch) return fail(c, IPFEM_INVALID, "bad args");
+    if (!c->tangent_valid) return fail(c, IPFEM_INVALID, "no tangent assembled");
+    if (!c->ev_ready) {
+        CK(cudaEventCreate(&c->ev[0]));
+        CK(cudaEventCreate(&c->ev[1]));
+        c->ev_ready = true;
+    }
+    launch_cg_init(c, c->d_rhs, 0.0, 1 << 30);
+    launch_cg_spmv_only(c);
+    CK(cudaEventRecord(c->ev[0], c->stream));
+    for (int k = 0; k < reps; k++) launch_cg_spmv_only(c);
+    CK(cudaEventRecord(c->ev[1], c->stream));
+    c->launches += 2 + reps;
+    CK(cudaEventSynchronize(c->ev[1]));
+    float ms = 0;
+    CK(cudaEventElapsedTime(&ms, c->ev[0], c->ev[1]));
+    *ms_per_launch = ms / reps;
+    return sync_check(c);
 }
 
 ipfem_status ipfem_gather_strain(ipfem_ctx *c, const double *d_u, double *d_strain)

@@ -64,6 +64,13 @@ void elastic_constants(double E, double nu, ElasticConstH &el);
 
 }  // namespace ipfem
 
+struct NewtonState {
+    ipfem_solve_opts opts{};
+    int32_t step = 0, step_end = 0, it = 0;
+    int open = 0, active = 0, all_converged = 1;
+    double r0 = 0.0, rn = 0.0;
+};
+
 struct ipfem_ctx {
     int device = -1;
     cudaStream_t stream = nullptr;
@@ -97,6 +104,10 @@ struct ipfem_ctx {
     cudaGraphExec_t cg_exec = nullptr;
     int cg_batch = 0;
     bool tangent_valid = false;
+    NewtonState ns;
+    cudaEvent_t ev[2] = {nullptr, nullptr};
+    bool ev_ready = false;
+    uint64_t launches = 0;               // kernels launched through this context
 };
 
 // ---- kernel launchers (implemented in the .cu files) ----
@@ -109,6 +120,8 @@ void launch_color_reduce(ipfem_ctx *c, const double *d_fe, double lambda, int wi
 void launch_stiffness(ipfem_ctx *c);
 void launch_cg_init(ipfem_ctx *c, const double *d_b, double rtol, int max_it);
 void launch_cg_iteration(ipfem_ctx *c);
+void launch_cg_spmv_only(ipfem_ctx *c);
 void launch_dot(ipfem_ctx *c, const double *a, const double *b, double *d_out);
 void launch_axpy_u(ipfem_ctx *c, double *d_u, const double *d_du);
+void launch_fp64_probe(ipfem_ctx *c, double *d_out, int grid, int iters);
 }  // namespace ipfem

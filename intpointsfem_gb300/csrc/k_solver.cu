@@ -269,6 +269,23 @@ __global__ void k_add(int64_t n, double *__restrict__ u, const double *__restric
     if (i < n) u[i] = u[i] + du[i];
 }
 
+// FP64 FMA issue-rate probe: 8 independent fma chains per thread, bounded loop
+__global__ void __launch_bounds__(256) k_fp64_probe(double *out, int iters, double a, double b)
+{
+    double x0 = threadIdx.x, x1 = x0 + 1, x2 = x0 + 2, x3 = x0 + 3, x4 = x0 + 4, x5 = x0 + 5, x6 = x0 + 6, x7 = x0 + 7;
+#pragma unroll 1
+    for (int i = 0; i < iters; i++) {
+        x0 = fma(x0, a, b); x1 = fma(x1, a, b); x2 = fma(x2, a, b); x3 = fma(x3, a, b);
+        x4 = fma(x4, a, b); x5 = fma(x5, a, b); x6 = fma(x6, a, b); x7 = fma(x7, a, b);
+    }
+    out[blockIdx.x * blockDim.x + threadIdx.x] = ((x0 + x1) + (x2 + x3)) + ((x4 + x5) + (x6 + x7));
+}
+
+void launch_fp64_probe(ipfem_ctx *c, double *d_out, int grid, int iters)
+{
+    k_fp64_probe<<<grid, 256, 0, c->stream>>>(d_out, iters, 0.999, 0.001);
+}
+
 static unsigned grid_nodes(const ipfem_ctx *c)
 {
     return (unsigned)((c->s.n_nodes + kRedBlock - 1) / kRedBlock);
@@ -290,6 +307,13 @@ void launch_cg_iteration(ipfem_ctx *c)
     k_cg_update<<<g, kRedBlock, 0, c->stream>>>(c->s.n_nodes, c->d_p, c->d_q, c->d_dinv, c->d_x, c->d_r, c->d_z,
                                                 c->d_part, c->n_red, c->d_counters + 2, c->d_sc);
     k_cg_pupdate<<<g, kRedBlock, 0, c->stream>>>(c->s.n_nodes, c->d_z, c->d_p, c->d_sc);
+}
+
+void launch_cg_spmv_only(ipfem_ctx *c)
+{
+    k_cg_spmv<<<grid_nodes(c), kRedBlock, 0, c->stream>>>(c->s.n_nodes, c->d_slice_base, c->d_rowlen, c->d_sell_col,
+                                                          c->d_K, c->d_fixed, c->d_p, c->d_q, c->d_part, c->n_red,
+                                                          c->d_counters + 1, c->d_sc);
 }
 
 void launch_dot(ipfem_ctx *c, const double *a, const double *b, double *d_out)
