@@ -165,6 +165,21 @@ ipfem_status ipfem_compute_sigma(ipfem_ctx *ctx, int update_mem, const double *d
  * -B^T sigma_w, scattered and reduced over colours (no load, no masking). */
 ipfem_status ipfem_scatter_residual(ipfem_ctx *ctx, const double *d_sigma_w, double *d_res);
 
+/* The same canonical dot product for callers that cannot allocate device
+ * memory (an application that serves all device memory from its own
+ * preallocated pool, or code running under stream capture, where cudaMalloc
+ * is not allowed).  No counterpart in the reference.  Needs no context: d_a and
+ * d_b are device vectors of n doubles (n even, n <= 33,554,432), the result is
+ * written to the device double *d_out, asynchronously on `stream`
+ * (cudaStream_t, NULL = legacy default stream).  The scratch lives in a
+ * 512 KiB array inside the library that every device keeps until process
+ * exit; it allocates nothing and calls no allocating routine.  The first call
+ * on a device also looks up that array's device address (make it before any
+ * stream capture).  Calls share the array: calls that overlap on the GPU (on
+ * different streams without ordering) race and give wrong results.  Larger n
+ * is rejected with IPFEM_INVALID; the message is in ipfem_last_error(NULL). */
+ipfem_status ipfem_dot_noalloc(const double *d_a, const double *d_b, int64_t n, double *d_out, void *stream);
+
 /* Integration-point state (TPZConstitutiveLawProcessor members), host copies.
  * field: 0 plastic strain [4][n_ip] (xx, xy, yy, zz), 1 stress [4][n_ip],
  *        2 alpha [n_ip], 3 m_type as double [n_ip]. */

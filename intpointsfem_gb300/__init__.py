@@ -98,6 +98,7 @@ def lib():
             "ipfem_newton_advance": (S, [P, C.c_int32, P, S, C.POINTER(SolveStats), _dp, C.c_int32,
                                          C.POINTER(C.c_int32)]),
             "ipfem_dot": (S, [P, P, P, _dp]),
+            "ipfem_dot_noalloc": (S, [P, P, C.c_int64, P, P]),
             "ipfem_launch_count": (C.c_uint64, [P]),
             "ipfem_profile_spmv": (S, [P, S, _dp]),
             "ipfem_measure_fp64_peak": (S, [P, _dp]),

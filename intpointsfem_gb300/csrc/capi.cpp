@@ -154,6 +154,11 @@ ipfem_status dot_host(ipfem_ctx *c, const double *a, const double *b, double *ou
 
 }  // namespace
 
+void ipfem::set_thread_error(const std::string &msg)
+{
+    t_create_err = msg;
+}
+
 extern "C" {
 
 const char *ipfem_status_string(ipfem_status s)

@@ -61,6 +61,8 @@ struct Setup {
 std::string build_setup(const ipfem_mesh *mesh, const ipfem_material *mat, Setup &s);
 int32_t greedy_coloring(int32_t n_el, int32_t n_nodes, const int32_t *connects, int32_t *el_color);
 void elastic_constants(double E, double nu, ElasticConstH &el);
+// message returned by ipfem_last_error(NULL) on the calling thread
+void set_thread_error(const std::string &msg);
 
 }  // namespace ipfem
 

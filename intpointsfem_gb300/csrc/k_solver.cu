@@ -16,6 +16,8 @@
 // Scalars (alpha, beta, convergence) live in device memory, so an iteration
 // is three kernels with no host round trip; the host replays a captured CUDA
 // graph of several iterations and checks the `done` word between replays.
+#include <mutex>
+
 #include "ipfem_internal.h"
 
 namespace ipfem {
@@ -328,4 +330,89 @@ void launch_axpy_u(ipfem_ctx *c, double *d_u, const double *d_du)
     k_add<<<(unsigned)((n + 255) / 256), 256, 0, c->stream>>>(n, d_u, d_du);
 }
 
+// ---------------------------------------------------------------------------
+// Canonical dot product without device allocation.
+//
+// Some callers of this library cannot allocate device memory: a host
+// application that hands every device byte out of its own preallocated pool
+// (so that a solve never triggers cudaMalloc, which synchronises the device
+// and fragments the pool), or code that runs while a stream is being
+// captured, where cudaMalloc is not permitted.  For them the dot kernel above
+// runs with its scratch (the per-CTA partial sums and the last-CTA ticket) in
+// the file-scope array below instead of in a context's buffers.  The array
+// holds kNoAllocMaxPartials partials (512 KiB), so vectors of up to
+// 2 * 256 * kNoAllocMaxPartials doubles are accepted; every GPU that loads the
+// library keeps the array until the process exits.
+// ---------------------------------------------------------------------------
+constexpr int64_t kNoAllocMaxPartials = 65536;
+
+struct NoAllocScratch {
+    double partials[kNoAllocMaxPartials];
+    unsigned ticket;
+};
+
+static __device__ __align__(256) NoAllocScratch g_noalloc_scratch;
+
+namespace {
+std::mutex g_noalloc_mu;
+NoAllocScratch *g_noalloc_ptr[256] = {nullptr};   // device address of the array, per device
+}  // namespace
+
 }  // namespace ipfem
+
+extern "C" ipfem_status ipfem_dot_noalloc(const double *d_a, const double *d_b, int64_t n, double *d_out,
+                                          void *stream)
+{
+    using namespace ipfem;
+    if (!d_a || !d_b || !d_out || n < 0 || (n & 1)) {
+        set_thread_error("ipfem_dot_noalloc: null pointer, negative or odd length");
+        return IPFEM_INVALID;
+    }
+    const int64_t n_nodes = n / 2;
+    const int64_t n_red = (n_nodes + kRedBlock - 1) / kRedBlock;
+    if (n_red > kNoAllocMaxPartials) {
+        set_thread_error("ipfem_dot_noalloc: length " + std::to_string(n) + " exceeds the maximum of " +
+                         std::to_string(2 * kRedBlock * kNoAllocMaxPartials) + " doubles");
+        return IPFEM_INVALID;
+    }
+    int dev = -1;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess || dev < 0 || dev >= 256) {
+        set_thread_error(std::string("ipfem_dot_noalloc: no current device: ") + cudaGetErrorString(e));
+        return IPFEM_NO_DEVICE;
+    }
+    NoAllocScratch *scr = nullptr;
+    {
+        // one-time set-up on this device: the host-side name of the array is
+        // not a device address, so ask the runtime for the device address
+        std::lock_guard<std::mutex> lk(g_noalloc_mu);
+        if (!g_noalloc_ptr[dev]) {
+            void *p = nullptr;
+            e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+            if (e != cudaSuccess || !p) {
+                set_thread_error(std::string("ipfem_dot_noalloc: cudaGetSymbolAddress failed: ") +
+                                 cudaGetErrorString(e));
+                return IPFEM_CUDA;
+            }
+            g_noalloc_ptr[dev] = static_cast<NoAllocScratch *>(p);
+        }
+        scr = g_noalloc_ptr[dev];
+    }
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    if (n_nodes == 0) {
+        e = cudaMemsetAsync(d_out, 0, sizeof(double), st);
+    } else {
+        // the array keeps the previous call's contents: the ticket must start at 0
+        e = cudaMemsetAsync(&scr->ticket, 0, sizeof(unsigned), st);
+        if (e == cudaSuccess) {
+            k_dot<<<(unsigned)n_red, kRedBlock, 0, st>>>((int32_t)n_nodes, d_a, d_b, scr->partials, n_red,
+                                                         &scr->ticket, d_out);
+            e = cudaGetLastError();
+        }
+    }
+    if (e != cudaSuccess) {
+        set_thread_error(std::string("ipfem_dot_noalloc: ") + cudaGetErrorString(e));
+        return IPFEM_CUDA;
+    }
+    return IPFEM_OK;
+}
