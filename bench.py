@@ -145,6 +145,18 @@ class CpuArm:
         self.P.close()
 
 
+def reduce_max(x, dist=None):
+    """max of a per-rank float over all ranks (identity without a process group)"""
+    if dist is None or not dist.is_initialized():
+        return x
+    import torch
+
+    dev = torch.device("cuda", torch.cuda.current_device()) if dist.get_backend() == "nccl" else torch.device("cpu")
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def ddp_env():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -242,10 +254,7 @@ def run_gpu(args):
     clk = clocks.stop()
     ms_dev = e0.elapsed_time(e1) / args.steps
     launches = A.launch_count - l0
-    if dist:
-        t = torch.tensor([ms_dev], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms_dev = float(t.item())
+    ms_dev = reduce_max(ms_dev, dist)
     cg_per_iter = st.cg_iters / max(1, st.newton_iters)
 
     # e2e through the C-ABI with pinned host buffers

@@ -192,6 +192,13 @@ ipfem_status ipfem_set_state(ipfem_ctx *ctx, int field, const double *in);
  * 3 dphi [n_elements*162] double, 4 weights [n_ip] double. */
 ipfem_status ipfem_get_setup(ipfem_ctx *ctx, int field, void *out);
 
+/* Greedy element colouring of TPZNumericalIntegrator::SetUpColoredIndexes
+ * (TPZNumericalIntegrator.cpp:452-536), host only: element e takes, in
+ * repeated passes over the elements in index order, the current colour iff
+ * none of its 9 connects is marked in this pass.  Returns the number of
+ * colours, or -1 on bad arguments. */
+int32_t ipfem_color_elements(int32_t n_elements, int32_t n_nodes, const int32_t *connects, int32_t *el_color);
+
 /* ------------------------------------------------------------ diagnostics */
 /* number of kernels this context has launched (graph nodes included) */
 uint64_t ipfem_launch_count(const ipfem_ctx *ctx);

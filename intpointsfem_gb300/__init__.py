@@ -108,6 +108,7 @@ def lib():
             "ipfem_get_state": (S, [P, S, _dp]),
             "ipfem_set_state": (S, [P, S, _dp]),
             "ipfem_get_setup": (S, [P, S, P]),
+            "ipfem_color_elements": (C.c_int32, [C.c_int32, C.c_int32, _ip, _ip]),
             "ipfem_wellbore_default": (None, [C.POINTER(WellboreParams), C.c_int32]),
             "ipfem_wellbore_build": (S, [C.POINTER(WellboreParams), C.POINTER(C.POINTER(Wellbore))]),
             "ipfem_wellbore_free": (None, [C.POINTER(Wellbore)]),
@@ -132,6 +133,16 @@ def _ptr(a):
 
 def _np_ptr(a, t):
     return a.ctypes.data_as(t)
+
+
+def color_elements(connects, n_nodes):
+    """host greedy colouring (SetUpColoredIndexes); returns (n_colors, colours)"""
+    connects = np.ascontiguousarray(connects, dtype=np.int32)
+    col = np.zeros(connects.size // 9, np.int32)
+    nc = lib().ipfem_color_elements(col.size, int(n_nodes), _np_ptr(connects, _ip), _np_ptr(col, _ip))
+    if nc < 0:
+        raise IpfemError(5, "bad colouring arguments")
+    return int(nc), col
 
 
 def wellbore_params(n, **kw):

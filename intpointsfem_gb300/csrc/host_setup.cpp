@@ -335,6 +335,14 @@ static void seg_load(const double *xy, int32_t P, int32_t M, int32_t Q, int sgn,
 
 using namespace ipfem;
 
+extern "C" int32_t ipfem_color_elements(int32_t n_el, int32_t n_nodes, const int32_t *connects, int32_t *el_color)
+{
+    if (n_el <= 0 || n_nodes <= 0 || !connects || !el_color) return -1;
+    for (int64_t k = 0; k < (int64_t)n_el * 9; k++)
+        if (connects[k] < 0 || connects[k] >= n_nodes) return -1;
+    return greedy_coloring(n_el, n_nodes, connects, el_color);
+}
+
 extern "C" void ipfem_wellbore_default(ipfem_wellbore_params *p, int32_t n)
 {
     std::memset(p, 0, sizeof *p);

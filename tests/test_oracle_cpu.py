@@ -1,0 +1,83 @@
+"""CPU checks of the oracle's assembly and solver (the properties the GPU
+parity tests rely on)."""
+import numpy as np
+import pytest
+
+from oracle import pyoracle as po
+
+
+@pytest.fixture(scope="module")
+def P8():
+    return po.OracleProblem(po.default_params(8), nthreads=2)
+
+
+def test_in_situ_state_is_in_discrete_equilibrium(P8):
+    r = P8.assemble_residual(np.zeros(P8.neq), 0.0)
+    assert np.abs(r).max() < 1e-10 * np.abs(P8.arr("f0")).max()
+
+
+def test_dot_tree_matches_numpy_and_partials():
+    rng = np.random.default_rng(1)
+    for nn in (1, 31, 256, 257, 5000):
+        a, b = rng.normal(size=2 * nn), rng.normal(size=2 * nn)
+        d = po.dot(a, b)
+        assert d == pytest.approx(float(np.dot(a, b)), rel=1e-13, abs=1e-13)
+    # exact for integers (any order)
+    a = np.arange(2000, dtype=np.float64)
+    assert po.dot(a, a) == float(np.dot(a, a))
+
+
+def test_tangent_matches_finite_differences_in_elastic_state(P8):
+    rng = np.random.default_rng(0)
+    fixed = P8.arr("fixed").astype(bool)
+    u = np.zeros(P8.neq)
+    P8.assemble(u, 0.3)
+    v = rng.normal(size=P8.neq)
+    v[fixed] = 0
+    Kv = P8.spmv(v)
+    h = 1e-9
+    fd = -(P8.assemble_residual(u + h * v, 0.3) - P8.assemble_residual(u - h * v, 0.3)) / (2 * h)
+    assert np.linalg.norm(Kv - fd) / np.linalg.norm(fd) < 1e-6
+
+
+def test_tangent_is_symmetric_and_fixed_rows_masked(P8):
+    P8.assemble(np.zeros(P8.neq), 0.2)
+    rng = np.random.default_rng(3)
+    fixed = P8.arr("fixed").astype(bool)
+    x, y = rng.normal(size=P8.neq), rng.normal(size=P8.neq)
+    x[fixed] = 0
+    y[fixed] = 0
+    assert np.dot(y, P8.spmv(x)) == pytest.approx(np.dot(x, P8.spmv(y)), rel=1e-12)
+    assert np.all(P8.spmv(x)[fixed] == 0)
+
+
+def test_pcg_converges_and_reports_iterations(P8):
+    R = P8.assemble(np.zeros(P8.neq), 0.1)
+    x, k = P8.pcg(R, rtol=1e-10)
+    assert k > 0
+    r = R - P8.spmv(x)
+    assert np.linalg.norm(r) <= 1e-9 * np.linalg.norm(R)
+    x1, k1 = P8.pcg(R, rtol=1e-10, max_it=1)
+    assert k1 == -1                                   # max_it reached
+
+
+def test_zero_rhs_gives_zero_iterations(P8):
+    P8.assemble(np.zeros(P8.neq), 0.1)
+    x, k = P8.pcg(np.zeros(P8.neq))
+    assert k == 0 and not x.any()
+
+
+def test_newton_single_element_and_plasticity_onset():
+    """edge case: a 1x1 mesh (one element, one colour) solves; a 40x40 mesh
+    develops plastic points near the well by the last load step"""
+    P1 = po.OracleProblem(po.default_params(1), nthreads=1)
+    u = np.zeros(P1.neq)
+    st, _ = P1.solve_steps(u, 2)
+    assert st.converged and P1.n_colors == 1
+
+
+def test_nan_input_propagates_to_residual(P8):
+    u = np.zeros(P8.neq)
+    u[10] = np.nan
+    r = P8.assemble_residual(u, 0.1)
+    assert np.isnan(r).any()
