@@ -39,6 +39,7 @@ typedef enum {
 } ipfem_status;
 
 enum { IPFEM_HOST = 0, IPFEM_DEVICE = 1 };
+enum { IPFEM_PLAIN_FP64 = 0, IPFEM_MIXED = 1 };
 
 #define IPFEM_NPTS 9     /* integration points per element */
 #define IPFEM_NNODE 9    /* connects per element */
@@ -94,6 +95,16 @@ void *ipfem_stream(ipfem_ctx *ctx);
 /* External load factor: rhs_linear = f0 + lambda*df (the reference's
  * fRhsLinear, TPZElastoPlasticIntPointsStructMatrix.cpp:232-243). */
 ipfem_status ipfem_set_load_factor(ipfem_ctx *ctx, double lambda);
+/* Precision of the tangent and the linear solve (no counterpart in the
+ * reference, whose tangent and solve are FP64):
+ *  IPFEM_PLAIN_FP64  FP64 tangent and Jacobi-CG (default; bit-exact with the oracle)
+ *  IPFEM_MIXED       FP32 tangent (FP32 element blocks and w*Dep, FP32 fma) and
+ *                    FP32 Jacobi-CG with FP32 accumulation on the right-hand side
+ *                    scaled to unit norm; the residual, the return mapping and
+ *                    the Newton update stay FP64, so Newton acts as FP64
+ *                    iterative refinement.  cg_rtol is then the inner FP32
+ *                    tolerance (1e-4 is a good choice). */
+ipfem_status ipfem_set_precision(ipfem_ctx *ctx, int mode);
 /* TPZMatWithMem::SetUpdateMem: when set, the next residual commits the
  * integration-point state (main.cpp:487-522). */
 ipfem_status ipfem_set_update_mem(ipfem_ctx *ctx, int update);
@@ -104,7 +115,8 @@ ipfem_status ipfem_assemble_residual(ipfem_ctx *ctx, const double *u, double *rh
  * rhs as above; the tangent K stays on the device for ipfem_solve. */
 ipfem_status ipfem_assemble(ipfem_ctx *ctx, const double *u, double *rhs, int where);
 /* K as nodal 2x2 blocks, rows ascending, columns ascending per row:
- * row_ptr[n_nodes+1], col[n_blocks], vals[4*n_blocks] (row-major blocks). */
+ * row_ptr[n_nodes+1], col[n_blocks], vals[4*n_blocks] (row-major blocks);
+ * in IPFEM_MIXED mode the FP32 tangent, widened to double. */
 ipfem_status ipfem_get_stiffness(ipfem_ctx *ctx, int64_t *row_ptr, int32_t *col, double *vals);
 /* Jacobi-preconditioned CG on the current K (replaces the reference's
  * TPZCudaCalls::SolveCG, TPZCudaCalls.cu:213-290, and the Pardiso solve):

@@ -16,6 +16,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libipfem.so")
 
 HOST, DEVICE = 0, 1
+PLAIN_FP64, MIXED = 0, 1
 STATUS = {0: "ok", 1: "not converged", 2: "non-finite value", 3: "CG breakdown", 4: "out of device memory",
           5: "invalid argument", 6: "CUDA error", 7: "no sm_103 device"}
 
@@ -88,6 +89,7 @@ def lib():
             "ipfem_stream": (P, [P]),
             "ipfem_set_load_factor": (S, [P, C.c_double]),
             "ipfem_set_update_mem": (S, [P, S]),
+            "ipfem_set_precision": (S, [P, S]),
             "ipfem_assemble_residual": (S, [P, P, P, S]),
             "ipfem_assemble": (S, [P, P, P, S]),
             "ipfem_get_stiffness": (S, [P, _lp, _ip, _dp]),
@@ -259,6 +261,9 @@ class ElastoPlasticIntPointsStructMatrix:
 
     def SetUpdateMem(self, flag):
         self._check(lib().ipfem_set_update_mem(self._ctx, int(bool(flag))))
+
+    def set_precision(self, mode):
+        self._check(lib().ipfem_set_precision(self._ctx, int(mode)))
 
     def SetLoadFactor(self, lam):
         self._check(lib().ipfem_set_load_factor(self._ctx, float(lam)))

@@ -52,6 +52,14 @@ void free_all(ipfem_ctx *c)
                     c->d_sc, c->d_counters, c->d_dotres, c->d_err};
     for (void *p : ptrs)
         if (p) cudaFree(p);
+    {
+        MixedBuffers &m = c->mx;
+        void *mp[] = {m.dphi, m.K, m.dinv, m.x, m.r, m.z, m.p, m.q, m.part, m.sc};
+        for (void *p : mp)
+            if (p) cudaFree(p);
+        if (m.h_sc) cudaFreeHost(m.h_sc);
+        if (m.exec) cudaGraphExecDestroy(m.exec);
+    }
     if (c->h_sc) cudaFreeHost(c->h_sc);
     if (c->h_pin) cudaFreeHost(c->h_pin);
     if (c->cg_exec) cudaGraphExecDestroy(c->cg_exec);
@@ -98,7 +106,8 @@ void tangent_device(ipfem_ctx *c, const double *d_u, double *d_out, int update_m
     launch_compute_sigma(c, update_mem, c->d_strain, c->d_sigma_w, c->d_dep);
     launch_stress_residual(c, c->d_sigma_w, c->d_fe);
     launch_color_reduce(c, c->d_fe, c->load_factor, 1, d_out);
-    launch_stiffness(c);
+    if (c->precision == 1) launch_stiffness32(c);
+    else launch_stiffness(c);
     c->tangent_valid = true;
 }
 
@@ -139,6 +148,76 @@ ipfem_status cg_device(ipfem_ctx *c, const double *d_b, double rtol, int max_it,
     if (c->h_sc->status == IPFEM_NONCONVERGED) return fail(c, IPFEM_NONCONVERGED, "CG reached max_it");
     if (!std::isfinite(c->h_sc->rr)) return fail(c, IPFEM_NAN, "CG residual is not finite");
     return IPFEM_OK;
+}
+
+// FP32 CG on the FP32 tangent for the right-hand side d_b * scale (d_b FP64,
+// scale = 1/|b| so the FP32 system is well scaled); solution in c->mx.x
+ipfem_status cg32_device(ipfem_ctx *c, const double *d_b, double scale, double rtol, int max_it, int *iters)
+{
+    MixedBuffers &m = c->mx;
+    launch_cg32_init(c, d_b, scale, (float)rtol, max_it);
+    c->launches += 1;
+    const int batch = 32;
+    if (!m.exec) {
+        cudaGraph_t g = nullptr;
+        CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+        for (int k = 0; k < batch; k++) launch_cg32_iteration(c);
+        CK(cudaStreamEndCapture(c->stream, &g));
+        cudaError_t e = cudaGraphInstantiate(&m.exec, g, 0);
+        cudaGraphDestroy(g);
+        CK(e);
+    }
+    int launched = 0;
+    for (;;) {
+        CK(cudaGraphLaunch(m.exec, c->stream));
+        launched += batch;
+        c->launches += 3 * batch;
+        CK(cudaMemcpyAsync(m.h_sc, m.sc, sizeof(CGScalarsT<float>), cudaMemcpyDeviceToHost, c->stream));
+        CK(cudaStreamSynchronize(c->stream));
+        if (m.h_sc->done || launched >= max_it + batch) break;
+    }
+    if (iters) *iters = m.h_sc->iters;
+    ipfem_status st = check_device(c);
+    if (st != IPFEM_OK) return st;
+    if (!m.h_sc->done) return fail(c, IPFEM_NONCONVERGED, "CG did not finish");
+    if (m.h_sc->status == IPFEM_BREAKDOWN) return fail(c, IPFEM_BREAKDOWN, "CG breakdown: p.Kp <= 0");
+    if (m.h_sc->status == IPFEM_NONCONVERGED) return fail(c, IPFEM_NONCONVERGED, "CG reached max_it");
+    if (!std::isfinite(m.h_sc->rr)) return fail(c, IPFEM_NAN, "CG residual is not finite");
+    return IPFEM_OK;
+}
+
+ipfem_status dot_host(ipfem_ctx *c, const double *a, const double *b, double *out);
+
+// K du = b in the context's precision; du accumulated into d_u (d_u += du)
+// when add != 0, else written to c->d_x.
+ipfem_status solve_device(ipfem_ctx *c, const double *d_b, double rtol, int max_it, int *iters, double *d_u, int add)
+{
+    if (c->precision == 0) {
+        ipfem_status st = cg_device(c, d_b, rtol, max_it, iters);
+        if (add) {
+            launch_axpy_u(c, d_u, c->d_x);
+            c->launches += 1;
+        }
+        return st;
+    }
+    double bb = 0.0;
+    ipfem_status st = dot_host(c, d_b, d_b, &bb);
+    if (st != IPFEM_OK) return st;
+    const double bn = std::sqrt(bb);
+    if (!(bn > 0.0)) {
+        if (iters) *iters = 0;
+        if (!add) CK(cudaMemsetAsync(c->d_x, 0, (size_t)c->s.neq * sizeof(double), c->stream));
+        return std::isfinite(bn) ? IPFEM_OK : fail(c, IPFEM_NAN, "right-hand side is not finite");
+    }
+    st = cg32_device(c, d_b, 1.0 / bn, rtol, max_it, iters);
+    if (!add) {
+        CK(cudaMemsetAsync(c->d_x, 0, (size_t)c->s.neq * sizeof(double), c->stream));
+        launch_add_scaled32(c, c->d_x, c->mx.x, bn);
+    } else {
+        launch_add_scaled32(c, d_u, c->mx.x, bn);
+    }
+    c->launches += 1;
+    return st;
 }
 
 // |v|^2 (canonical order) of a device vector, to the host
@@ -321,6 +400,37 @@ ipfem_status ipfem_set_load_factor(ipfem_ctx *c, double lambda)
     return IPFEM_OK;
 }
 
+ipfem_status ipfem_set_precision(ipfem_ctx *c, int mode)
+{
+    if (!c || (mode != IPFEM_PLAIN_FP64 && mode != IPFEM_MIXED)) return fail(c, IPFEM_INVALID, "bad precision mode");
+    if (mode == IPFEM_MIXED && !c->mx.K) {
+        const Setup &s = c->s;
+        MixedBuffers &m = c->mx;
+        ipfem_status st = IPFEM_OK;
+        auto ck = [&](cudaError_t e) {
+            if (e != cudaSuccess && st == IPFEM_OK) st = (e == cudaErrorMemoryAllocation) ? IPFEM_OOM : IPFEM_CUDA;
+        };
+        std::vector<float> d32(s.dphi.begin(), s.dphi.end());
+        ck(upload(&m.dphi, d32, c->stream));
+        ck(dalloc(&m.K, (size_t)s.n_sell * 4));
+        ck(dalloc(&m.dinv, (size_t)s.neq));
+        ck(dalloc(&m.x, (size_t)s.neq));
+        ck(dalloc(&m.r, (size_t)s.neq));
+        ck(dalloc(&m.z, (size_t)s.neq));
+        ck(dalloc(&m.p, (size_t)s.neq));
+        ck(dalloc(&m.q, (size_t)s.neq));
+        ck(dalloc(&m.part, (size_t)c->n_red * 2));
+        ck(dalloc(&m.sc, 1));
+        ck(cudaMallocHost((void **)&m.h_sc, sizeof(CGScalarsT<float>)));
+        ck(cudaMemsetAsync(m.sc, 0, sizeof(CGScalarsT<float>), c->stream));
+        ck(cudaStreamSynchronize(c->stream));
+        if (st != IPFEM_OK) return fail(c, st, "allocation of the mixed-precision buffers failed");
+    }
+    if (mode != c->precision) c->tangent_valid = false;
+    c->precision = mode;
+    return IPFEM_OK;
+}
+
 ipfem_status ipfem_set_update_mem(ipfem_ctx *c, int update)
 {
     if (!c) return IPFEM_INVALID;
@@ -361,7 +471,13 @@ ipfem_status ipfem_get_stiffness(ipfem_ctx *c, int64_t *row_ptr, int32_t *col, d
     const Setup &s = c->s;
     if (row_ptr) std::memcpy(row_ptr, s.row_ptr.data(), s.row_ptr.size() * sizeof(int64_t));
     if (col) std::memcpy(col, s.col.data(), s.col.size() * sizeof(int32_t));
-    if (vals) {
+    if (vals && c->precision == 1) {
+        std::vector<float> h((size_t)s.n_sell * 4);
+        CK(cudaMemcpyAsync(h.data(), c->mx.K, h.size() * sizeof(float), cudaMemcpyDeviceToHost, c->stream));
+        CK(cudaStreamSynchronize(c->stream));
+        for (int64_t k = 0; k < s.n_blocks; k++)
+            for (int j = 0; j < 4; j++) vals[4 * k + j] = h[4 * s.bsr_to_sell[k] + j];
+    } else if (vals) {
         std::vector<double> h((size_t)s.n_sell * 4);
         CK(cudaMemcpyAsync(h.data(), c->d_K, h.size() * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
         CK(cudaStreamSynchronize(c->stream));
@@ -382,7 +498,7 @@ ipfem_status ipfem_solve(ipfem_ctx *c, const double *b, double *x, double rtol, 
         CK(cudaMemcpyAsync(c->d_b, b, nb, cudaMemcpyHostToDevice, c->stream));
         db = c->d_b;
     }
-    ipfem_status st = cg_device(c, db, rtol, max_it, iters);
+    ipfem_status st = solve_device(c, db, rtol, max_it, iters, nullptr, 0);
     if (where == IPFEM_HOST) CK(cudaMemcpyAsync(x, c->d_x, nb, cudaMemcpyDeviceToHost, c->stream));
     else if (x != c->d_x) CK(cudaMemcpyAsync(x, c->d_x, nb, cudaMemcpyDeviceToDevice, c->stream));
     CK(cudaStreamSynchronize(c->stream));
@@ -427,12 +543,11 @@ static ipfem_status newton_advance(ipfem_ctx *c, int32_t n_iters, double *du, ip
         if (!conv) {
             int k = 0;
             cudaEventRecord(ev[0], c->stream);
-            ipfem_status e = cg_device(c, c->d_rhs, o.cg_rtol, o.cg_max_it, &k);
+            ipfem_status e = solve_device(c, c->d_rhs, o.cg_rtol, o.cg_max_it, &k, du, 1);
             cudaEventRecord(ev[1], c->stream);
             st->ms_solve += elapsed();
             st->cg_iters += k;
             if (e != IPFEM_OK && e != IPFEM_NONCONVERGED) return e;
-            launch_axpy_u(c, du, c->d_x);
             ns.it++;
             done++;
             st->newton_iters++;
@@ -573,10 +688,19 @@ ipfem_status ipfem_profile_spmv(ipfem_ctx *c, int reps, double *ms_per_launch)
         CK(cudaEventCreate(&c->ev[1]));
         c->ev_ready = true;
     }
-    launch_cg_init(c, c->d_rhs, 0.0, 1 << 30);
-    launch_cg_spmv_only(c);
+    const bool mixed = c->precision == 1;
+    if (mixed) {
+        launch_cg32_init(c, c->d_rhs, 1.0, 0.0f, 1 << 30);
+        launch_cg32_spmv_only(c);
+    } else {
+        launch_cg_init(c, c->d_rhs, 0.0, 1 << 30);
+        launch_cg_spmv_only(c);
+    }
     CK(cudaEventRecord(c->ev[0], c->stream));
-    for (int k = 0; k < reps; k++) launch_cg_spmv_only(c);
+    for (int k = 0; k < reps; k++) {
+        if (mixed) launch_cg32_spmv_only(c);
+        else launch_cg_spmv_only(c);
+    }
     CK(cudaEventRecord(c->ev[1], c->stream));
     c->launches += 2 + reps;
     CK(cudaEventSynchronize(c->ev[1]));

@@ -20,9 +20,23 @@ struct ElasticConstH {               // mirrors ElasticConst of constitutive.cuh
 };
 
 // device-side scalars of one CG solve
-struct CGScalars {
-    double rz, pq, alpha, beta, rr, bb, thr;
+template <class T>
+struct CGScalarsT {
+    T rz, pq, alpha, beta, rr, bb, thr;
     int done, iters, status, max_it;
+};
+typedef CGScalarsT<double> CGScalars;
+
+// buffers of the mixed-precision solve (FP32 tangent and CG)
+struct MixedBuffers {
+    float *dphi = nullptr;        // [n_el*162]
+    float *K = nullptr;           // [n_sell*4]
+    float *dinv = nullptr;        // [neq]
+    float *x = nullptr, *r = nullptr, *z = nullptr, *p = nullptr, *q = nullptr;
+    float *part = nullptr;        // 2 partial arrays
+    CGScalarsT<float> *sc = nullptr;
+    CGScalarsT<float> *h_sc = nullptr;   // pinned
+    cudaGraphExec_t exec = nullptr;
 };
 
 // Host result of the setup: everything derived from the mesh (colouring,
@@ -110,6 +124,8 @@ struct ipfem_ctx {
     cudaEvent_t ev[2] = {nullptr, nullptr};
     bool ev_ready = false;
     uint64_t launches = 0;               // kernels launched through this context
+    int precision = 0;                   // IPFEM_PLAIN_FP64 or IPFEM_MIXED
+    ipfem::MixedBuffers mx;
 };
 
 // ---- kernel launchers (implemented in the .cu files) ----
@@ -126,4 +142,9 @@ void launch_cg_spmv_only(ipfem_ctx *c);
 void launch_dot(ipfem_ctx *c, const double *a, const double *b, double *d_out);
 void launch_axpy_u(ipfem_ctx *c, double *d_u, const double *d_du);
 void launch_fp64_probe(ipfem_ctx *c, double *d_out, int grid, int iters);
+void launch_stiffness32(ipfem_ctx *c);
+void launch_cg32_init(ipfem_ctx *c, const double *d_b, double scale, float rtol, int max_it);
+void launch_cg32_iteration(ipfem_ctx *c);
+void launch_cg32_spmv_only(ipfem_ctx *c);
+void launch_add_scaled32(ipfem_ctx *c, double *d_u, const float *x, double scale);
 }  // namespace ipfem

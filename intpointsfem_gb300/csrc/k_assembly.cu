@@ -183,28 +183,31 @@ __global__ void __launch_bounds__(256) k_color_reduce(int32_t n_nodes, int n_col
 
 constexpr int kStiffWarps = 4;
 
+// T = double: the plain tangent (bit-exact with the oracle); T = float: the
+// FP32 tangent of the mixed-precision solve (blocks and w*Dep rounded to FP32,
+// FP32 fma accumulation).
+template <class T>
 __global__ void __launch_bounds__(kStiffWarps * 32) k_stiffness(int32_t n_in_color, const int32_t *__restrict__ els,
-                                                                 int64_t n_ip, const double *__restrict__ dphi,
+                                                                 int64_t n_ip, const T *__restrict__ dphi,
                                                                  const double *__restrict__ dep,
                                                                  const int32_t *__restrict__ el_blk,
-                                                                 double *__restrict__ K)
+                                                                 T *__restrict__ K)
 {
-    __shared__ __align__(16) double s_dn[kStiffWarps][162];
-    __shared__ double s_D[kStiffWarps][81];        // [q][9]
-    __shared__ double s_DB[kStiffWarps][54];       // [3][18]
+    __shared__ __align__(16) T s_dn[kStiffWarps][162];
+    __shared__ T s_D[kStiffWarps][81];        // [q][9]
+    __shared__ T s_DB[kStiffWarps][54];       // [3][18]
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int32_t k = blockIdx.x * kStiffWarps + w;
-    if (k >= n_in_color) return;                   // warp-uniform
+    if (k >= n_in_color) return;              // warp-uniform
     const int32_t e = __ldg(&els[k]);
-    const double *dn_g = dphi + (size_t)e * 162;
-    for (int t = lane; t < 81; t += 32)
-        reinterpret_cast<double2 *>(s_dn[w])[t] = __ldg(reinterpret_cast<const double2 *>(dn_g) + t);
+    const T *dn_g = dphi + (size_t)e * 162;
+    for (int t = lane; t < 162; t += 32) s_dn[w][t] = __ldg(&dn_g[t]);
     for (int t = lane; t < 81; t += 32) {
         const int cmp = t / 9, q = t - cmp * 9;
-        s_D[w][q * 9 + cmp] = __ldg(&dep[cmp * n_ip + (int64_t)e * 9 + q]);
+        s_D[w][q * 9 + cmp] = (T)__ldg(&dep[cmp * n_ip + (int64_t)e * 9 + q]);
     }
     __syncwarp();
-    const double *dn = s_dn[w];
+    const T *dn = s_dn[w];
     // upper-triangle entries (a <= b, row-major order) owned by this lane
     int pa[6], pb[6];
 #pragma unroll
@@ -218,31 +221,31 @@ __global__ void __launch_bounds__(kStiffWarps * 32) k_stiffness(int32_t n_in_col
         pa[m] = a;
         pb[m] = a + r;
     }
-    double acc[6] = {0, 0, 0, 0, 0, 0};
+    T acc[6] = {T(0), T(0), T(0), T(0), T(0), T(0)};
 #pragma unroll 1
     for (int q = 0; q < 9; q++) {
-        const double *D = &s_D[w][q * 9];
-        const double *dx = dn + q * 18, *dy = dx + 9;
+        const T *D = &s_D[w][q * 9];
+        const T *dx = dn + q * 18, *dy = dx + 9;
         for (int t = lane; t < 54; t += 32) {
             const int i = t / 18, j = t - i * 18, n = j >> 1;
-            double s;
+            T sv;
             if ((j & 1) == 0) {
-                s = D[3 * i + 0] * dx[n];
-                s = fma(D[3 * i + 1], dy[n], s);
+                sv = D[3 * i + 0] * dx[n];
+                sv = fma(D[3 * i + 1], dy[n], sv);
             } else {
-                s = D[3 * i + 1] * dx[n];
-                s = fma(D[3 * i + 2], dy[n], s);
+                sv = D[3 * i + 1] * dx[n];
+                sv = fma(D[3 * i + 2], dy[n], sv);
             }
-            s_DB[w][t] = s;
+            s_DB[w][t] = sv;
         }
         __syncwarp();
-        const double *DB = s_DB[w];
+        const T *DB = s_DB[w];
 #pragma unroll
         for (int m = 0; m < 6; m++) {
             const int p = lane + 32 * m;
             if (p < 171) {
                 const int a = pa[m], b = pb[m], na = a >> 1;
-                double t = acc[m];
+                T t = acc[m];
                 if ((a & 1) == 0) {
                     t = fma(dx[na], DB[b], t);
                     t = fma(dy[na], DB[18 + b], t);
@@ -262,14 +265,14 @@ __global__ void __launch_bounds__(kStiffWarps * 32) k_stiffness(int32_t n_in_col
         if (p < 171) {
             const int a = pa[m], b = pb[m];
             const int ma = a >> 1, ca = a & 1, nb = b >> 1, cb = b & 1;
-            const double v = acc[m];
+            const T v = acc[m];
             if (ma == nb) {
-                double *blk = K + 4 * (size_t)__ldg(&eb[ma * 9 + ma]);
+                T *blk = K + 4 * (size_t)__ldg(&eb[ma * 9 + ma]);
                 blk[2 * ca + cb] = blk[2 * ca + cb] + v;
                 if (ca != cb) blk[2 * cb + ca] = blk[2 * cb + ca] + v;
             } else {
-                double *b1 = K + 4 * (size_t)__ldg(&eb[ma * 9 + nb]);
-                double *b2 = K + 4 * (size_t)__ldg(&eb[nb * 9 + ma]);
+                T *b1 = K + 4 * (size_t)__ldg(&eb[ma * 9 + nb]);
+                T *b2 = K + 4 * (size_t)__ldg(&eb[nb * 9 + ma]);
                 b1[2 * ca + cb] = b1[2 * ca + cb] + v;
                 b2[2 * cb + ca] = b2[2 * cb + ca] + v;
             }
@@ -277,14 +280,15 @@ __global__ void __launch_bounds__(kStiffWarps * 32) k_stiffness(int32_t n_in_col
     }
 }
 
-__global__ void k_jacobi(int32_t n_nodes, const int64_t *__restrict__ diag, const double *__restrict__ K,
-                         const uint8_t *__restrict__ fixed, double *__restrict__ dinv)
+template <class T>
+__global__ void k_jacobi(int32_t n_nodes, const int64_t *__restrict__ diag, const T *__restrict__ K,
+                         const uint8_t *__restrict__ fixed, T *__restrict__ dinv)
 {
     const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n_nodes) return;
-    const double *blk = K + 4 * (size_t)diag[i];
-    dinv[2 * (size_t)i] = fixed[2 * (size_t)i] ? 0.0 : 1.0 / blk[0];
-    dinv[2 * (size_t)i + 1] = fixed[2 * (size_t)i + 1] ? 0.0 : 1.0 / blk[3];
+    const T *blk = K + 4 * (size_t)diag[i];
+    dinv[2 * (size_t)i] = fixed[2 * (size_t)i] ? T(0) : T(1) / blk[0];
+    dinv[2 * (size_t)i + 1] = fixed[2 * (size_t)i + 1] ? T(0) : T(1) / blk[3];
 }
 
 void launch_gather_strain(ipfem_ctx *c, const double *d_u, double *d_strain)
@@ -321,11 +325,27 @@ void launch_stiffness(ipfem_ctx *c)
         const int32_t first = s.color_ptr[col], n = s.color_ptr[col + 1] - first;
         if (n == 0) continue;
         const unsigned grid = (unsigned)((n + kStiffWarps - 1) / kStiffWarps);
-        k_stiffness<<<grid, kStiffWarps * 32, 0, c->stream>>>(n, c->d_color_els + first, s.n_ip, c->d_dphi, c->d_dep,
-                                                              c->d_el_blk, c->d_K);
+        k_stiffness<double><<<grid, kStiffWarps * 32, 0, c->stream>>>(n, c->d_color_els + first, s.n_ip, c->d_dphi,
+                                                                      c->d_dep, c->d_el_blk, c->d_K);
     }
     const unsigned g2 = (unsigned)((s.n_nodes + 255) / 256);
-    k_jacobi<<<g2, 256, 0, c->stream>>>(s.n_nodes, c->d_diag_blk, c->d_K, c->d_fixed, c->d_dinv);
+    k_jacobi<double><<<g2, 256, 0, c->stream>>>(s.n_nodes, c->d_diag_blk, c->d_K, c->d_fixed, c->d_dinv);
+}
+
+void launch_stiffness32(ipfem_ctx *c)
+{
+    const Setup &s = c->s;
+    MixedBuffers &m = c->mx;
+    cudaMemsetAsync(m.K, 0, (size_t)s.n_sell * 4 * sizeof(float), c->stream);
+    for (int col = 0; col < s.n_colors; col++) {
+        const int32_t first = s.color_ptr[col], n = s.color_ptr[col + 1] - first;
+        if (n == 0) continue;
+        const unsigned grid = (unsigned)((n + kStiffWarps - 1) / kStiffWarps);
+        k_stiffness<float><<<grid, kStiffWarps * 32, 0, c->stream>>>(n, c->d_color_els + first, s.n_ip, m.dphi,
+                                                                     c->d_dep, c->d_el_blk, m.K);
+    }
+    const unsigned g2 = (unsigned)((s.n_nodes + 255) / 256);
+    k_jacobi<float><<<g2, 256, 0, c->stream>>>(s.n_nodes, c->d_diag_blk, m.K, c->d_fixed, m.dinv);
 }
 
 }  // namespace ipfem

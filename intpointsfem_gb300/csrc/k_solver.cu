@@ -24,7 +24,8 @@ namespace ipfem {
 
 constexpr unsigned FULL = 0xffffffffu;
 
-__device__ __forceinline__ double warp_tree(double v)
+template <class T>
+__device__ __forceinline__ T warp_tree(T v)
 {
 #pragma unroll
     for (int off = 16; off >= 1; off >>= 1) v = v + __shfl_down_sync(FULL, v, off);
@@ -32,9 +33,10 @@ __device__ __forceinline__ double warp_tree(double v)
 }
 
 // tree over the 8 warp sums in shared memory (4, 2, 1); valid in thread 0
-__device__ __forceinline__ double tree8(volatile double *w)
+template <class T>
+__device__ __forceinline__ T tree8(const volatile T *w)
 {
-    double a[8];
+    T a[8];
 #pragma unroll
     for (int k = 0; k < 8; k++) a[k] = w[k];
 #pragma unroll
@@ -46,21 +48,21 @@ __device__ __forceinline__ double tree8(volatile double *w)
 
 // Level 0+1 for NV values at once: per-CTA partial sums written to part[v][blockIdx].
 // Returns true in every thread of the CTA that finished last (after a fence).
-template <int NV>
-__device__ __forceinline__ bool block_partials(const double (&v)[NV], double *part, int64_t n_red, unsigned *ticket)
+template <class T, int NV>
+__device__ __forceinline__ bool block_partials(const T (&v)[NV], T *part, int64_t n_red, unsigned *ticket)
 {
-    __shared__ double ws[NV][8];
+    __shared__ T ws[NV][8];
     __shared__ int s_last;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
 #pragma unroll
     for (int k = 0; k < NV; k++) {
-        const double t = warp_tree(v[k]);
+        const T t = warp_tree(v[k]);
         if (lane == 0) ws[k][w] = t;
     }
     __syncthreads();
     if (threadIdx.x == 0) {
 #pragma unroll
-        for (int k = 0; k < NV; k++) part[k * n_red + blockIdx.x] = tree8(ws[k]);
+        for (int k = 0; k < NV; k++) part[k * n_red + blockIdx.x] = tree8<T>(ws[k]);
         __threadfence();
         const unsigned t = atomicAdd(ticket, 1u);
         s_last = (t == gridDim.x - 1);
@@ -70,47 +72,83 @@ __device__ __forceinline__ bool block_partials(const double (&v)[NV], double *pa
 }
 
 // Level 2, executed by all 256 threads of the last CTA; result valid in thread 0.
-template <int NV>
-__device__ __forceinline__ void final_reduce(const double *part, int64_t n_red, double (&out)[NV])
+template <class T, int NV>
+__device__ __forceinline__ void final_reduce(const T *part, int64_t n_red, T (&out)[NV])
 {
-    __shared__ double ws[NV][8];
+    __shared__ T ws[NV][8];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
 #pragma unroll
     for (int k = 0; k < NV; k++) {
-        double acc = 0.0;
-        for (int64_t i = threadIdx.x; i < n_red; i += blockDim.x) acc = acc + __ldcg(&part[k * n_red + i]);
+        // strided partials t, t+256, t+512, ... summed in that order; four loads
+        // are issued before their adds so that the pass is not latency-serial
+        const T *pk = part + k * n_red;
+        T acc = T(0);
+        int64_t i = threadIdx.x;
+        for (; i + 3 * kRedBlock < n_red; i += 4 * kRedBlock) {
+            const T v0 = __ldcg(&pk[i]), v1 = __ldcg(&pk[i + kRedBlock]);
+            const T v2 = __ldcg(&pk[i + 2 * kRedBlock]), v3 = __ldcg(&pk[i + 3 * kRedBlock]);
+            acc = acc + v0;
+            acc = acc + v1;
+            acc = acc + v2;
+            acc = acc + v3;
+        }
+        for (; i < n_red; i += kRedBlock) acc = acc + __ldcg(&pk[i]);
         acc = warp_tree(acc);
         if (lane == 0) ws[k][w] = acc;
     }
     __syncthreads();
     if (threadIdx.x == 0) {
 #pragma unroll
-        for (int k = 0; k < NV; k++) out[k] = tree8(ws[k]);
+        for (int k = 0; k < NV; k++) out[k] = tree8<T>(ws[k]);
     }
 }
 
-__global__ void __launch_bounds__(kRedBlock) k_cg_init(int32_t n_nodes, const double *__restrict__ b,
-                                                       const double *__restrict__ dinv, double *__restrict__ x,
-                                                       double *__restrict__ r, double *__restrict__ z,
-                                                       double *__restrict__ p, double *part, int64_t n_red,
-                                                       unsigned *ticket, CGScalars *sc, double rtol, int max_it)
+template <class T> struct Vec2;
+template <> struct Vec2<double> { typedef double2 type; };
+template <> struct Vec2<float> { typedef float2 type; };
+
+__device__ __forceinline__ double2 mk2(double a, double b) { return make_double2(a, b); }
+__device__ __forceinline__ float2 mk2(float a, float b) { return make_float2(a, b); }
+
+// 2x2 block s of a SELL matrix: FP64 as two 16-byte loads, FP32 as one
+__device__ __forceinline__ void load_block(const double *K, int64_t s, double &a, double &b, double &c, double &d)
 {
+    const double2 *Kv = reinterpret_cast<const double2 *>(K);
+    const double2 u = __ldg(&Kv[2 * s]), v = __ldg(&Kv[2 * s + 1]);
+    a = u.x; b = u.y; c = v.x; d = v.y;
+}
+__device__ __forceinline__ void load_block(const float *K, int64_t s, float &a, float &b, float &c, float &d)
+{
+    const float4 u = __ldg(&reinterpret_cast<const float4 *>(K)[s]);
+    a = u.x; b = u.y; c = u.z; d = u.w;
+}
+
+// x = 0, r = b*scale (converted to T), z = D^-1 r, p = z; b.b and r.z
+template <class T>
+__global__ void __launch_bounds__(kRedBlock) k_cg_init(int32_t n_nodes, const double *__restrict__ b, double scale,
+                                                       const T *__restrict__ dinv, T *__restrict__ x,
+                                                       T *__restrict__ r, T *__restrict__ z, T *__restrict__ p,
+                                                       T *part, int64_t n_red, unsigned *ticket, CGScalarsT<T> *sc,
+                                                       T rtol, int max_it)
+{
+    typedef typename Vec2<T>::type V;
     const int32_t i = blockIdx.x * kRedBlock + threadIdx.x;
-    double v[2] = {0.0, 0.0};
+    T v[2] = {T(0), T(0)};
     if (i < n_nodes) {
-        const double2 bb = reinterpret_cast<const double2 *>(b)[i];
-        const double2 di = reinterpret_cast<const double2 *>(dinv)[i];
-        const double2 zz = make_double2(bb.x * di.x, bb.y * di.y);
-        reinterpret_cast<double2 *>(x)[i] = make_double2(0.0, 0.0);
-        reinterpret_cast<double2 *>(r)[i] = bb;
-        reinterpret_cast<double2 *>(z)[i] = zz;
-        reinterpret_cast<double2 *>(p)[i] = zz;
-        v[0] = fma(bb.y, bb.y, fma(bb.x, bb.x, 0.0));
-        v[1] = fma(bb.y, zz.y, fma(bb.x, zz.x, 0.0));
+        const double2 b64 = reinterpret_cast<const double2 *>(b)[i];
+        const V bb = mk2((T)(b64.x * scale), (T)(b64.y * scale));
+        const V di = reinterpret_cast<const V *>(dinv)[i];
+        const V zz = mk2(bb.x * di.x, bb.y * di.y);
+        reinterpret_cast<V *>(x)[i] = mk2(T(0), T(0));
+        reinterpret_cast<V *>(r)[i] = bb;
+        reinterpret_cast<V *>(z)[i] = zz;
+        reinterpret_cast<V *>(p)[i] = zz;
+        v[0] = fma(bb.y, bb.y, fma(bb.x, bb.x, T(0)));
+        v[1] = fma(bb.y, zz.y, fma(bb.x, zz.x, T(0)));
     }
-    if (block_partials<2>(v, part, n_red, ticket)) {
-        double o[2];
-        final_reduce<2>(part, n_red, o);
+    if (block_partials<T, 2>(v, part, n_red, ticket)) {
+        T o[2];
+        final_reduce<T, 2>(part, n_red, o);
         if (threadIdx.x == 0) {
             sc->bb = o[0];
             sc->rz = o[1];
@@ -118,57 +156,56 @@ __global__ void __launch_bounds__(kRedBlock) k_cg_init(int32_t n_nodes, const do
             sc->iters = 0;
             sc->status = 0;
             sc->max_it = max_it;
-            sc->done = (o[0] == 0.0) ? 1 : (max_it <= 0 ? 1 : 0);
-            if (o[0] != 0.0 && max_it <= 0) sc->status = IPFEM_NONCONVERGED;
+            sc->done = (o[0] == T(0)) ? 1 : (max_it <= 0 ? 1 : 0);
+            if (o[0] != T(0) && max_it <= 0) sc->status = IPFEM_NONCONVERGED;
             *ticket = 0u;
         }
     }
 }
 
 // q = K p (free dofs), partial sums of p.q; last CTA: alpha = rz / pq
+template <class T>
 __global__ void __launch_bounds__(kRedBlock) k_cg_spmv(int32_t n_nodes, const int64_t *__restrict__ slice_base,
                                                        const int32_t *__restrict__ rowlen,
-                                                       const int32_t *__restrict__ scol,
-                                                       const double *__restrict__ K,
-                                                       const uint8_t *__restrict__ fixed,
-                                                       const double *__restrict__ p, double *__restrict__ q,
-                                                       double *part, int64_t n_red, unsigned *ticket,
-                                                       CGScalars *sc)
+                                                       const int32_t *__restrict__ scol, const T *__restrict__ K,
+                                                       const uint8_t *__restrict__ fixed, const T *__restrict__ p,
+                                                       T *__restrict__ q, T *part, int64_t n_red, unsigned *ticket,
+                                                       CGScalarsT<T> *sc)
 {
+    typedef typename Vec2<T>::type V;
     if (*reinterpret_cast<volatile int *>(&sc->done)) return;
     const int32_t i = blockIdx.x * kRedBlock + threadIdx.x;
-    double v[1] = {0.0};
+    T v[1] = {T(0)};
     if (i < n_nodes) {
         const int64_t base = __ldg(&slice_base[i >> 5]) + (i & 31);
         const int len = __ldg(&rowlen[i]);
-        const double2 *Kv = reinterpret_cast<const double2 *>(K);
-        const double2 *pv = reinterpret_cast<const double2 *>(p);
-        double y0 = 0.0, y1 = 0.0;
+        const V *pv = reinterpret_cast<const V *>(p);
+        T y0 = T(0), y1 = T(0);
 #pragma unroll 4
         for (int k = 0; k < len; k++) {
             const int64_t s = base + (int64_t)k * 32;
             const int32_t c = __ldg(&scol[s]);
-            const double2 a0 = __ldg(&Kv[2 * s]);
-            const double2 a1 = __ldg(&Kv[2 * s + 1]);
-            const double2 xx = __ldg(&pv[c]);
-            y0 = fma(a0.x, xx.x, y0);
-            y0 = fma(a0.y, xx.y, y0);
-            y1 = fma(a1.x, xx.x, y1);
-            y1 = fma(a1.y, xx.y, y1);
+            T a00, a01, a10, a11;
+            load_block(K, s, a00, a01, a10, a11);
+            const V xx = __ldg(&pv[c]);
+            y0 = fma(a00, xx.x, y0);
+            y0 = fma(a01, xx.y, y0);
+            y1 = fma(a10, xx.x, y1);
+            y1 = fma(a11, xx.y, y1);
         }
-        if (fixed[2 * (size_t)i]) y0 = 0.0;
-        if (fixed[2 * (size_t)i + 1]) y1 = 0.0;
-        reinterpret_cast<double2 *>(q)[i] = make_double2(y0, y1);
-        const double2 pp = pv[i];
-        v[0] = fma(pp.y, y1, fma(pp.x, y0, 0.0));
+        if (fixed[2 * (size_t)i]) y0 = T(0);
+        if (fixed[2 * (size_t)i + 1]) y1 = T(0);
+        reinterpret_cast<V *>(q)[i] = mk2(y0, y1);
+        const V pp = pv[i];
+        v[0] = fma(pp.y, y1, fma(pp.x, y0, T(0)));
     }
-    if (block_partials<1>(v, part, n_red, ticket)) {
-        double o[1];
-        final_reduce<1>(part, n_red, o);
+    if (block_partials<T, 1>(v, part, n_red, ticket)) {
+        T o[1];
+        final_reduce<T, 1>(part, n_red, o);
         if (threadIdx.x == 0) {
-            const double pq = o[0];
+            const T pq = o[0];
             sc->pq = pq;
-            if (!(pq > 0.0)) {
+            if (!(pq > T(0))) {
                 sc->done = 1;
                 sc->status = IPFEM_BREAKDOWN;
             } else {
@@ -181,39 +218,39 @@ __global__ void __launch_bounds__(kRedBlock) k_cg_spmv(int32_t n_nodes, const in
 
 // x += alpha p, r -= alpha q, z = D^-1 r; partials of r.r and r.z;
 // last CTA: convergence test, beta
-__global__ void __launch_bounds__(kRedBlock) k_cg_update(int32_t n_nodes, const double *__restrict__ p,
-                                                         const double *__restrict__ q,
-                                                         const double *__restrict__ dinv,
-                                                         double *__restrict__ x, double *__restrict__ r,
-                                                         double *__restrict__ z, double *part, int64_t n_red,
-                                                         unsigned *ticket, CGScalars *sc)
+template <class T>
+__global__ void __launch_bounds__(kRedBlock) k_cg_update(int32_t n_nodes, const T *__restrict__ p,
+                                                         const T *__restrict__ q, const T *__restrict__ dinv,
+                                                         T *__restrict__ x, T *__restrict__ r, T *__restrict__ z,
+                                                         T *part, int64_t n_red, unsigned *ticket, CGScalarsT<T> *sc)
 {
+    typedef typename Vec2<T>::type V;
     if (*reinterpret_cast<volatile int *>(&sc->done)) return;
-    const double alpha = *reinterpret_cast<volatile double *>(&sc->alpha);
+    const T alpha = *reinterpret_cast<volatile T *>(&sc->alpha);
     const int32_t i = blockIdx.x * kRedBlock + threadIdx.x;
-    double v[2] = {0.0, 0.0};
+    T v[2] = {T(0), T(0)};
     if (i < n_nodes) {
-        const double2 pp = reinterpret_cast<const double2 *>(p)[i];
-        const double2 qq = reinterpret_cast<const double2 *>(q)[i];
-        const double2 di = reinterpret_cast<const double2 *>(dinv)[i];
-        double2 xx = reinterpret_cast<double2 *>(x)[i];
-        double2 rr = reinterpret_cast<double2 *>(r)[i];
+        const V pp = reinterpret_cast<const V *>(p)[i];
+        const V qq = reinterpret_cast<const V *>(q)[i];
+        const V di = reinterpret_cast<const V *>(dinv)[i];
+        V xx = reinterpret_cast<V *>(x)[i];
+        V rr = reinterpret_cast<V *>(r)[i];
         xx.x = fma(alpha, pp.x, xx.x);
         xx.y = fma(alpha, pp.y, xx.y);
         rr.x = fma(-alpha, qq.x, rr.x);
         rr.y = fma(-alpha, qq.y, rr.y);
-        const double2 zz = make_double2(rr.x * di.x, rr.y * di.y);
-        reinterpret_cast<double2 *>(x)[i] = xx;
-        reinterpret_cast<double2 *>(r)[i] = rr;
-        reinterpret_cast<double2 *>(z)[i] = zz;
-        v[0] = fma(rr.y, rr.y, fma(rr.x, rr.x, 0.0));
-        v[1] = fma(rr.y, zz.y, fma(rr.x, zz.x, 0.0));
+        const V zz = mk2(rr.x * di.x, rr.y * di.y);
+        reinterpret_cast<V *>(x)[i] = xx;
+        reinterpret_cast<V *>(r)[i] = rr;
+        reinterpret_cast<V *>(z)[i] = zz;
+        v[0] = fma(rr.y, rr.y, fma(rr.x, rr.x, T(0)));
+        v[1] = fma(rr.y, zz.y, fma(rr.x, zz.x, T(0)));
     }
-    if (block_partials<2>(v, part, n_red, ticket)) {
-        double o[2];
-        final_reduce<2>(part, n_red, o);
+    if (block_partials<T, 2>(v, part, n_red, ticket)) {
+        T o[2];
+        final_reduce<T, 2>(part, n_red, o);
         if (threadIdx.x == 0) {
-            const double rr = o[0], rzn = o[1];
+            const T rr = o[0], rzn = o[1];
             sc->rr = rr;
             sc->iters += 1;
             if (rr <= sc->thr) {
@@ -230,18 +267,20 @@ __global__ void __launch_bounds__(kRedBlock) k_cg_update(int32_t n_nodes, const 
     }
 }
 
-__global__ void __launch_bounds__(kRedBlock) k_cg_pupdate(int32_t n_nodes, const double *__restrict__ z,
-                                                          double *__restrict__ p, const CGScalars *sc)
+template <class T>
+__global__ void __launch_bounds__(kRedBlock) k_cg_pupdate(int32_t n_nodes, const T *__restrict__ z,
+                                                          T *__restrict__ p, const CGScalarsT<T> *sc)
 {
+    typedef typename Vec2<T>::type V;
     if (*reinterpret_cast<const volatile int *>(&sc->done)) return;
-    const double beta = *reinterpret_cast<const volatile double *>(&sc->beta);
+    const T beta = *reinterpret_cast<const volatile T *>(&sc->beta);
     const int32_t i = blockIdx.x * kRedBlock + threadIdx.x;
     if (i >= n_nodes) return;
-    const double2 zz = reinterpret_cast<const double2 *>(z)[i];
-    double2 pp = reinterpret_cast<double2 *>(p)[i];
+    const V zz = reinterpret_cast<const V *>(z)[i];
+    V pp = reinterpret_cast<V *>(p)[i];
     pp.x = fma(beta, pp.x, zz.x);
     pp.y = fma(beta, pp.y, zz.y);
-    reinterpret_cast<double2 *>(p)[i] = pp;
+    reinterpret_cast<V *>(p)[i] = pp;
 }
 
 __global__ void __launch_bounds__(kRedBlock) k_dot(int32_t n_nodes, const double *__restrict__ a,
@@ -255,9 +294,9 @@ __global__ void __launch_bounds__(kRedBlock) k_dot(int32_t n_nodes, const double
         const double2 bb = reinterpret_cast<const double2 *>(b)[i];
         v[0] = fma(aa.y, bb.y, fma(aa.x, bb.x, 0.0));
     }
-    if (block_partials<1>(v, part, n_red, ticket)) {
+    if (block_partials<double, 1>(v, part, n_red, ticket)) {
         double o[1];
-        final_reduce<1>(part, n_red, o);
+        final_reduce<double, 1>(part, n_red, o);
         if (threadIdx.x == 0) {
             *out = o[0];
             *ticket = 0u;
@@ -288,6 +327,12 @@ void launch_fp64_probe(ipfem_ctx *c, double *d_out, int grid, int iters)
     k_fp64_probe<<<grid, 256, 0, c->stream>>>(d_out, iters, 0.999, 0.001);
 }
 
+__global__ void k_add_scaled32(int64_t n, double *__restrict__ u, const float *__restrict__ x, double scale)
+{
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i < n) u[i] = fma(scale, (double)x[i], u[i]);
+}
+
 static unsigned grid_nodes(const ipfem_ctx *c)
 {
     return (unsigned)((c->s.n_nodes + kRedBlock - 1) / kRedBlock);
@@ -295,27 +340,60 @@ static unsigned grid_nodes(const ipfem_ctx *c)
 
 void launch_cg_init(ipfem_ctx *c, const double *d_b, double rtol, int max_it)
 {
-    k_cg_init<<<grid_nodes(c), kRedBlock, 0, c->stream>>>(c->s.n_nodes, d_b, c->d_dinv, c->d_x, c->d_r, c->d_z,
-                                                          c->d_p, c->d_part, c->n_red, c->d_counters + 0, c->d_sc,
-                                                          rtol, max_it);
+    k_cg_init<double><<<grid_nodes(c), kRedBlock, 0, c->stream>>>(c->s.n_nodes, d_b, 1.0, c->d_dinv, c->d_x, c->d_r,
+                                                                  c->d_z, c->d_p, c->d_part, c->n_red,
+                                                                  c->d_counters + 0, c->d_sc, rtol, max_it);
 }
 
 void launch_cg_iteration(ipfem_ctx *c)
 {
     const unsigned g = grid_nodes(c);
-    k_cg_spmv<<<g, kRedBlock, 0, c->stream>>>(c->s.n_nodes, c->d_slice_base, c->d_rowlen, c->d_sell_col, c->d_K,
-                                              c->d_fixed, c->d_p, c->d_q, c->d_part, c->n_red, c->d_counters + 1,
-                                              c->d_sc);
-    k_cg_update<<<g, kRedBlock, 0, c->stream>>>(c->s.n_nodes, c->d_p, c->d_q, c->d_dinv, c->d_x, c->d_r, c->d_z,
-                                                c->d_part, c->n_red, c->d_counters + 2, c->d_sc);
-    k_cg_pupdate<<<g, kRedBlock, 0, c->stream>>>(c->s.n_nodes, c->d_z, c->d_p, c->d_sc);
+    k_cg_spmv<double><<<g, kRedBlock, 0, c->stream>>>(c->s.n_nodes, c->d_slice_base, c->d_rowlen, c->d_sell_col,
+                                                      c->d_K, c->d_fixed, c->d_p, c->d_q, c->d_part, c->n_red,
+                                                      c->d_counters + 1, c->d_sc);
+    k_cg_update<double><<<g, kRedBlock, 0, c->stream>>>(c->s.n_nodes, c->d_p, c->d_q, c->d_dinv, c->d_x, c->d_r,
+                                                        c->d_z, c->d_part, c->n_red, c->d_counters + 2, c->d_sc);
+    k_cg_pupdate<double><<<g, kRedBlock, 0, c->stream>>>(c->s.n_nodes, c->d_z, c->d_p, c->d_sc);
 }
 
 void launch_cg_spmv_only(ipfem_ctx *c)
 {
-    k_cg_spmv<<<grid_nodes(c), kRedBlock, 0, c->stream>>>(c->s.n_nodes, c->d_slice_base, c->d_rowlen, c->d_sell_col,
-                                                          c->d_K, c->d_fixed, c->d_p, c->d_q, c->d_part, c->n_red,
-                                                          c->d_counters + 1, c->d_sc);
+    k_cg_spmv<double><<<grid_nodes(c), kRedBlock, 0, c->stream>>>(c->s.n_nodes, c->d_slice_base, c->d_rowlen,
+                                                                  c->d_sell_col, c->d_K, c->d_fixed, c->d_p, c->d_q,
+                                                                  c->d_part, c->n_red, c->d_counters + 1, c->d_sc);
+}
+
+void launch_cg32_init(ipfem_ctx *c, const double *d_b, double scale, float rtol, int max_it)
+{
+    MixedBuffers &m = c->mx;
+    k_cg_init<float><<<grid_nodes(c), kRedBlock, 0, c->stream>>>(c->s.n_nodes, d_b, scale, m.dinv, m.x, m.r, m.z,
+                                                                 m.p, m.part, c->n_red, c->d_counters + 4, m.sc,
+                                                                 rtol, max_it);
+}
+
+void launch_cg32_iteration(ipfem_ctx *c)
+{
+    MixedBuffers &m = c->mx;
+    const unsigned g = grid_nodes(c);
+    k_cg_spmv<float><<<g, kRedBlock, 0, c->stream>>>(c->s.n_nodes, c->d_slice_base, c->d_rowlen, c->d_sell_col, m.K,
+                                                     c->d_fixed, m.p, m.q, m.part, c->n_red, c->d_counters + 5, m.sc);
+    k_cg_update<float><<<g, kRedBlock, 0, c->stream>>>(c->s.n_nodes, m.p, m.q, m.dinv, m.x, m.r, m.z, m.part,
+                                                       c->n_red, c->d_counters + 6, m.sc);
+    k_cg_pupdate<float><<<g, kRedBlock, 0, c->stream>>>(c->s.n_nodes, m.z, m.p, m.sc);
+}
+
+void launch_cg32_spmv_only(ipfem_ctx *c)
+{
+    MixedBuffers &m = c->mx;
+    k_cg_spmv<float><<<grid_nodes(c), kRedBlock, 0, c->stream>>>(c->s.n_nodes, c->d_slice_base, c->d_rowlen,
+                                                                 c->d_sell_col, m.K, c->d_fixed, m.p, m.q, m.part,
+                                                                 c->n_red, c->d_counters + 5, m.sc);
+}
+
+void launch_add_scaled32(ipfem_ctx *c, double *d_u, const float *x, double scale)
+{
+    const int64_t n = c->s.neq;
+    k_add_scaled32<<<(unsigned)((n + 255) / 256), 256, 0, c->stream>>>(n, d_u, x, scale);
 }
 
 void launch_dot(ipfem_ctx *c, const double *a, const double *b, double *d_out)

@@ -1,0 +1,60 @@
+"""Mixed precision (FP32 tangent and CG, FP64 residual, return mapping and
+Newton update) against the FP64 oracle.  Tolerances are stated per field."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+ip = pytest.importorskip("intpointsfem_gb300")
+from oracle import pyoracle as po  # noqa: E402
+
+
+def _pair(n, **kw):
+    w = ip.WellboreMesh(ip.wellbore_params(n, **kw))
+    sm = ip.ElastoPlasticIntPointsStructMatrix(w)
+    P = po.OracleProblem(po.default_params(n, **kw), nthreads=0)
+    return sm, P
+
+
+def _soa4(p6, n_ip):
+    p = p6.reshape(n_ip, 6)
+    return np.stack([p[:, 0], p[:, 1], p[:, 3], p[:, 5]]).ravel()
+
+
+def test_fp32_tangent_close_to_fp64():
+    sm, P = _pair(16, material_mode=2)
+    rng = np.random.default_rng(2)
+    u = rng.normal(size=sm.neq) * 2e-3
+    u[P.arr("fixed").astype(bool)] = 0.0
+    sm.set_precision(ip.MIXED)
+    sm.SetLoadFactor(0.8)
+    r = sm.assemble(u, np.zeros(sm.neq))
+    ro = P.assemble(u.copy(), 0.8)
+    assert np.array_equal(r, ro)                      # the residual stays FP64, bit-exact
+    _, _, K32 = sm.stiffness()
+    K64 = P.arr("K")
+    assert np.abs(K32 - K64).max() <= 1e-5 * np.abs(K64).max()
+    # the FP32 CG solves the FP64 system to FP32 accuracy
+    x, it = sm.solve(r, rtol=1e-5)
+    res = np.linalg.norm(ro - P.spmv(x)) / np.linalg.norm(ro)
+    assert it > 0 and res < 1e-4
+
+
+def test_mixed_newton_cfg1_against_fp64_oracle():
+    """40 x 40, 10 load steps, Newton to 1e-8 with FP32 inner CG to 1e-4"""
+    sm, P = _pair(40)
+    sm.set_precision(ip.MIXED)
+    ug, uo = np.zeros(sm.neq), np.zeros(sm.neq)
+    sg, _ = sm.newton(ug, 10, newton_max_it=40, cg_rtol=1e-4)
+    so, _ = P.solve_steps(uo, 10, newton_max_it=40)
+    assert sg.converged
+    eu = np.abs(ug - uo).max() / np.abs(uo).max()
+    sig, sigo = sm.get_state(1), _soa4(P.arr("sigma"), P.n_ip)
+    es = np.abs(sig - sigo).max() / np.abs(sigo).max()
+    ep, epo = sm.get_state(0), _soa4(P.arr("eps_p"), P.n_ip)
+    eep = np.abs(ep - epo).max() / np.abs(epo).max()
+    flips = int((sm.get_state(3) != P.arr("mtype")).sum())
+    print("mixed vs FP64: u %.2e  sigma %.2e  eps_p %.2e  flag flips %d  newton %d vs %d"
+          % (eu, es, eep, flips, sg.newton_iters, so.newton_iters))
+    assert eu < 1e-6 and es < 1e-6 and eep < 1e-6
+    assert flips <= 2
