@@ -218,8 +218,14 @@ def run_gpu(args):
     torch.cuda.set_device(dev)
     n = args.n
     wb = ip.WellboreMesh(ip.wellbore_params(n))
+    mixed = args.precision == "mixed"
+    cg_rtol = args.mixed_cg_rtol if mixed else 1e-8
     A = ip.ElastoPlasticIntPointsStructMatrix(wb)         # device-resident arm
-    B = ip.ElastoPlasticIntPointsStructMatrix(wb)         # host-buffer (e2e) arm
+    B = None if args.no_e2e else ip.ElastoPlasticIntPointsStructMatrix(wb)   # host-buffer (e2e) arm
+    if mixed:
+        A.set_precision(ip.MIXED)
+        if B:
+            B.set_precision(ip.MIXED)
     stream = torch.cuda.ExternalStream(A.stream, device=dev)
     fp64_tflops = A.measure_fp64_peak()
 
@@ -239,7 +245,7 @@ def run_gpu(args):
     ms_res = e0.elapsed_time(e1) / nres
 
     # Newton iterations, device-resident
-    A.newton_begin(N_STEPS)
+    A.newton_begin(N_STEPS, newton_max_it=40, cg_rtol=cg_rtol)
     st_w, _ = A.newton_advance(du, args.warmup, ip.DEVICE)
     clocks = ClockSampler(dev.index)
     if dist:
@@ -258,19 +264,44 @@ def run_gpu(args):
     cg_per_iter = st.cg_iters / max(1, st.newton_iters)
 
     # e2e through the C-ABI with pinned host buffers
-    hu = torch.zeros(B.neq, dtype=torch.float64, pin_memory=True)
-    B.newton_begin(N_STEPS)
-    B.newton_advance(hu, args.warmup, ip.HOST)
-    if dist:
-        dist.barrier()
-    t0 = time.perf_counter()
-    st_e, _ = B.newton_advance(hu, args.steps, ip.HOST)
-    ms_e2e = 1e3 * (time.perf_counter() - t0) / args.steps
+    ms_e2e = None
+    if B:
+        hu = torch.zeros(B.neq, dtype=torch.float64, pin_memory=True)
+        B.newton_begin(N_STEPS, newton_max_it=40, cg_rtol=cg_rtol)
+        B.newton_advance(hu, args.warmup, ip.HOST)
+        if dist:
+            dist.barrier()
+        t0 = time.perf_counter()
+        B.newton_advance(hu, args.steps, ip.HOST)
+        ms_e2e = 1e3 * (time.perf_counter() - t0) / args.steps
+        B.close()
+
+    # the chosen method (mixed precision) beside the plain one, same iterations
+    chosen = None
+    if not mixed and args.chosen:
+        C_ = ip.ElastoPlasticIntPointsStructMatrix(wb)
+        C_.set_precision(ip.MIXED)
+        uc = torch.zeros(C_.neq, dtype=torch.float64, device=dev)
+        C_.newton_begin(N_STEPS, newton_max_it=40, cg_rtol=args.mixed_cg_rtol)
+        C_.newton_advance(uc, args.warmup, ip.DEVICE)
+        sc_ = torch.cuda.ExternalStream(C_.stream, device=dev)
+        torch.cuda.synchronize()
+        e0.record(sc_)
+        stc, _ = C_.newton_advance(uc, args.steps, ip.DEVICE)
+        e1.record(sc_)
+        torch.cuda.synchronize()
+        chosen = {"method": "mixed: FP32 tangent + FP32 Jacobi-CG to %g, FP64 residual/return mapping/Newton "
+                            "refinement" % args.mixed_cg_rtol,
+                  "ms_per_newton_iter": e0.elapsed_time(e1) / args.steps,
+                  "cg_iters_per_newton": stc.cg_iters / max(1, stc.newton_iters),
+                  "ms_spmv_fp32": C_.profile_spmv(reps=20)}
+        C_.close()
 
     # roofline of the dominant kernel (CG block SpMV), CUDA events on the library stream
     ms_spmv = A.profile_spmv(reps=20)
     nb, nn = A.n_blocks, A.n_nodes
-    spmv_bytes = nb * (32 + 4) + nn * (2 * 16 + 4 + 2)        # blocks + col; p read, q write, rowlen, fixed
+    vb = 16 if mixed else 32                                   # bytes of one 2x2 block
+    spmv_bytes = nb * (vb + 4) + nn * (2 * vb // 2 + 4 + 2)    # blocks + col; p read, q write, rowlen, fixed
     hbm_peak, peak_kind = measured_peaks()
     achieved = spmv_bytes / (ms_spmv * 1e-3) / 1e9
     spmv_fp64_tflops = 2.0 * (4 * nb + 2 * nn) / (ms_spmv * 1e-3) / 1e12
@@ -287,11 +318,12 @@ def run_gpu(args):
         return 0
     line = {
         "metric": METRIC, "value": ms_dev, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": ms_dev, "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "ms_per_step": ms_dev, "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64" if not mixed else "f32+f64",
         "data": "synthetic",
-        "config": {"workload": "wellbore %dx%d order-2 quads, %d IPs, %d dofs, plain FP64, Jacobi-CG 1e-8, "
+        "config": {"workload": "wellbore %dx%d order-2 quads, %d IPs, %d dofs, %s, Jacobi-CG %g, "
                                "Newton 1e-8, %d load steps; first %d Newton iterations (warm-up %d)"
-                               % (n, n, A.n_ip, A.neq, N_STEPS, args.warmup + args.steps, args.warmup),
+                               % (n, n, A.n_ip, A.neq, "plain FP64" if not mixed else "mixed FP32/FP64", cg_rtol,
+                                  N_STEPS, args.warmup + args.steps, args.warmup),
                    "l2": "inputs larger than L2 (tangent %.0f MB, element blocks %.0f MB)"
                          % (nb * 32 / 1e6, A.n_el * 1296 / 1e6),
                    "replicas": ws},
@@ -301,15 +333,20 @@ def run_gpu(args):
         "newton_iters_timed": st.newton_iters,
         "ms_breakdown": {"assemble": st.ms_assemble / args.steps, "cg": st.ms_solve / args.steps,
                          "commit": st.ms_commit / args.steps},
-        "e2e": {"value": ms_e2e, "unit": UNIT, "h2d_bytes_per_step": 8 * B.neq, "d2h_bytes_per_step": 8 * B.neq},
+        "e2e": ({"value": ms_e2e, "unit": UNIT, "h2d_bytes_per_step": 8 * A.neq, "d2h_bytes_per_step": 8 * A.neq}
+                if ms_e2e is not None else None),
+        "precision": args.precision,
         "roofline": {"kernel": "k_cg_spmv", "bound": "hbm", "achieved": achieved, "peak": hbm_peak,
                      "unit": "GB/s", "frac": achieved / hbm_peak, "peak_kind": peak_kind,
-                     "traffic": SPMV_DRAM_BYTES if n == 400 else None, "algorithmic_bytes": spmv_bytes,
+                     "traffic": SPMV_DRAM_BYTES if (n == 400 and not mixed) else None,
+                     "algorithmic_bytes": spmv_bytes,
                      "ms_per_launch": ms_spmv,
                      "fp64": {"achieved_tflops": spmv_fp64_tflops, "peak_tflops": fp64_tflops,
                               "frac": spmv_fp64_tflops / fp64_tflops, "peak_kind": "measured live (fma probe)"}},
         "gpu_launches": launches,
     }
+    if chosen:
+        line["chosen"] = chosen
     if clk:
         line["clocks"] = clk
     if cpu:
@@ -337,6 +374,10 @@ def main():
     ap.add_argument("--cpu-threads", type=int, default=0)
     ap.add_argument("--cpu-cg-sample", type=int, default=100)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--precision", default="plain", choices=["plain", "mixed"])
+    ap.add_argument("--mixed-cg-rtol", type=float, default=1e-4)
+    ap.add_argument("--no-chosen", dest="chosen", action="store_false")
+    ap.add_argument("--no-e2e", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

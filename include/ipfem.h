@@ -40,6 +40,7 @@ typedef enum {
 
 enum { IPFEM_HOST = 0, IPFEM_DEVICE = 1 };
 enum { IPFEM_PLAIN_FP64 = 0, IPFEM_MIXED = 1 };
+enum { IPFEM_PREC_JACOBI = 0, IPFEM_PREC_MLP = 1 };
 
 #define IPFEM_NPTS 9     /* integration points per element */
 #define IPFEM_NNODE 9    /* connects per element */
@@ -210,6 +211,37 @@ ipfem_status ipfem_get_setup(ipfem_ctx *ctx, int field, void *out);
  * none of its 9 connects is marked in this pass.  Returns the number of
  * colours, or -1 on bad arguments. */
 int32_t ipfem_color_elements(int32_t n_elements, int32_t n_nodes, const int32_t *connects, int32_t *el_color);
+
+/* ------------------------------------------------- learned preconditioner */
+/* None of these has a counterpart in the reference.  A per-node MLP
+ * (32 features -> 128 -> 128 -> 2, BF16 weights, FP32 accumulation on the
+ * tensor cores) maps the residual around a node to a displacement
+ * correction; it runs inside flexible CG (Polak-Ribiere) on the FP32 tangent
+ * and falls back to Jacobi-PCG when FCG stagnates.  Requires IPFEM_MIXED and
+ * a structured node grid (node = b*gr + a).  Parameters are one FP32 vector
+ * of 20994 values: W1[32][128] b1[128] W2[128][128] b2[128] W3[128][2] b3[2]. */
+ipfem_status ipfem_set_node_grid(ipfem_ctx *ctx, int32_t gr, int32_t gt);
+ipfem_status ipfem_mlp_init(ipfem_ctx *ctx, uint64_t seed);
+ipfem_status ipfem_set_preconditioner(ipfem_ctx *ctx, int kind);
+ipfem_status ipfem_mlp_get_params(ipfem_ctx *ctx, float *out);
+ipfem_status ipfem_mlp_set_params(ipfem_ctx *ctx, const float *in);
+/* features [n_nodes][32] and scales [n_nodes] of a device residual (FP64) */
+ipfem_status ipfem_mlp_features(ipfem_ctx *ctx, const double *d_r, float *d_X, float *d_S);
+/* training targets T = e / (S * Dinv) per dof of an error vector e [neq] and
+ * the feature scales S (0 on fixed dofs), all FP32 device arrays */
+ipfem_status ipfem_mlp_targets(ipfem_ctx *ctx, const float *d_e, const float *d_S, float *d_T);
+/* network output [rows][2] for device feature rows [rows][32] */
+ipfem_status ipfem_mlp_forward(ipfem_ctx *ctx, const float *d_X, int64_t rows, float *d_O);
+/* MSE loss and parameter gradients (host, 20994 floats) of one full batch */
+ipfem_status ipfem_mlp_grad(ipfem_ctx *ctx, const float *d_X, const float *d_Y, int64_t rows, float *grads,
+                            float *loss);
+/* mini-batch Adam; loss_per_epoch[epochs] may be NULL */
+ipfem_status ipfem_mlp_train(ipfem_ctx *ctx, const float *d_X, const float *d_Y, int64_t rows, int epochs, int batch,
+                             float lr, uint64_t seed, float *loss_per_epoch);
+/* FP32 Jacobi-CG with (x_k, r_k) snapshots at iterations that are multiples of
+ * 32, plus the final iterate (training data: residual / solution increment) */
+ipfem_status ipfem_cg_snapshots(ipfem_ctx *ctx, const double *d_b, double rtol, int max_it, int n_snap,
+                                const int32_t *snap_iters, float *d_xs, float *d_rs, float *d_xfinal, int *iters);
 
 /* ------------------------------------------------------------ diagnostics */
 /* number of kernels this context has launched (graph nodes included) */

@@ -17,6 +17,8 @@ LIB_PATH = os.path.join(HERE, "libipfem.so")
 
 HOST, DEVICE = 0, 1
 PLAIN_FP64, MIXED = 0, 1
+PREC_JACOBI, PREC_MLP = 0, 1
+MLP_PARAMS = 20994
 STATUS = {0: "ok", 1: "not converged", 2: "non-finite value", 3: "CG breakdown", 4: "out of device memory",
           5: "invalid argument", 6: "CUDA error", 7: "no sm_103 device"}
 
@@ -104,6 +106,17 @@ def lib():
             "ipfem_launch_count": (C.c_uint64, [P]),
             "ipfem_profile_spmv": (S, [P, S, _dp]),
             "ipfem_measure_fp64_peak": (S, [P, _dp]),
+            "ipfem_set_node_grid": (S, [P, C.c_int32, C.c_int32]),
+            "ipfem_mlp_init": (S, [P, C.c_uint64]),
+            "ipfem_set_preconditioner": (S, [P, S]),
+            "ipfem_mlp_get_params": (S, [P, C.POINTER(C.c_float)]),
+            "ipfem_mlp_set_params": (S, [P, C.POINTER(C.c_float)]),
+            "ipfem_mlp_features": (S, [P, P, P, P]),
+            "ipfem_mlp_targets": (S, [P, P, P, P]),
+            "ipfem_mlp_forward": (S, [P, P, C.c_int64, P]),
+            "ipfem_mlp_grad": (S, [P, P, P, C.c_int64, C.POINTER(C.c_float), C.POINTER(C.c_float)]),
+            "ipfem_mlp_train": (S, [P, P, P, C.c_int64, S, S, C.c_float, C.c_uint64, C.POINTER(C.c_float)]),
+            "ipfem_cg_snapshots": (S, [P, P, C.c_double, S, S, _ip, P, P, P, C.POINTER(C.c_int)]),
             "ipfem_gather_strain": (S, [P, P, P]),
             "ipfem_compute_sigma": (S, [P, S, P, P, P]),
             "ipfem_scatter_residual": (S, [P, P, P]),
@@ -334,6 +347,57 @@ class ElastoPlasticIntPointsStructMatrix:
         out = np.zeros(1)
         self._check(lib().ipfem_profile_spmv(self._ctx, int(reps), _np_ptr(out, _dp)))
         return float(out[0])
+
+    # -- learned preconditioner --------------------------------------------
+    def set_node_grid(self, gr, gt):
+        self._check(lib().ipfem_set_node_grid(self._ctx, int(gr), int(gt)))
+
+    def mlp_init(self, seed=0):
+        self._check(lib().ipfem_mlp_init(self._ctx, int(seed)))
+
+    def set_preconditioner(self, kind):
+        self._check(lib().ipfem_set_preconditioner(self._ctx, int(kind)))
+
+    def mlp_params(self):
+        out = np.zeros(MLP_PARAMS, np.float32)
+        self._check(lib().ipfem_mlp_get_params(self._ctx, out.ctypes.data_as(C.POINTER(C.c_float))))
+        return out
+
+    def set_mlp_params(self, p):
+        p = np.ascontiguousarray(p, dtype=np.float32)
+        assert p.size == MLP_PARAMS
+        self._check(lib().ipfem_mlp_set_params(self._ctx, p.ctypes.data_as(C.POINTER(C.c_float))))
+
+    def mlp_features(self, d_r, d_X, d_S):
+        self._check(lib().ipfem_mlp_features(self._ctx, _ptr(d_r), _ptr(d_X), _ptr(d_S)))
+
+    def mlp_targets(self, d_e, d_S, d_T):
+        self._check(lib().ipfem_mlp_targets(self._ctx, _ptr(d_e), _ptr(d_S), _ptr(d_T)))
+
+    def mlp_forward(self, d_X, rows, d_O):
+        self._check(lib().ipfem_mlp_forward(self._ctx, _ptr(d_X), int(rows), _ptr(d_O)))
+
+    def mlp_grad(self, d_X, d_Y, rows):
+        g = np.zeros(MLP_PARAMS, np.float32)
+        loss = np.zeros(1, np.float32)
+        self._check(lib().ipfem_mlp_grad(self._ctx, _ptr(d_X), _ptr(d_Y), int(rows),
+                                         g.ctypes.data_as(C.POINTER(C.c_float)),
+                                         loss.ctypes.data_as(C.POINTER(C.c_float))))
+        return g, float(loss[0])
+
+    def mlp_train(self, d_X, d_Y, rows, epochs=30, batch=2048, lr=2e-3, seed=0):
+        losses = np.zeros(max(1, epochs), np.float32)
+        self._check(lib().ipfem_mlp_train(self._ctx, _ptr(d_X), _ptr(d_Y), int(rows), int(epochs), int(batch),
+                                          float(lr), int(seed), losses.ctypes.data_as(C.POINTER(C.c_float))))
+        return losses[:epochs]
+
+    def cg_snapshots(self, d_b, snap_iters, d_xs, d_rs, d_xfinal, rtol=1e-6, max_it=200000):
+        si = np.ascontiguousarray(snap_iters, dtype=np.int32)
+        it = C.c_int()
+        self._check(lib().ipfem_cg_snapshots(self._ctx, _ptr(d_b), float(rtol), int(max_it), int(si.size),
+                                             si.ctypes.data_as(_ip), _ptr(d_xs), _ptr(d_rs), _ptr(d_xfinal),
+                                             C.byref(it)))
+        return it.value
 
     def measure_fp64_peak(self):
         out = np.zeros(1)

@@ -63,12 +63,23 @@ void free_all(ipfem_ctx *c)
     if (c->h_sc) cudaFreeHost(c->h_sc);
     if (c->h_pin) cudaFreeHost(c->h_pin);
     if (c->cg_exec) cudaGraphExecDestroy(c->cg_exec);
+    if (c->fcg_exec) cudaGraphExecDestroy(c->fcg_exec);
+    {
+        MlpBuffers &l = c->mlp;
+        void *lp[] = {l.params, l.grads, l.m, l.v, l.w1t, l.w2t, l.pfrac, l.pden, l.r_old, l.loss};
+        for (void *p : lp)
+            if (p) cudaFree(p);
+    }
     if (c->ev_ready) {
         cudaEventDestroy(c->ev[0]);
         cudaEventDestroy(c->ev[1]);
     }
     if (c->stream) cudaStreamDestroy(c->stream);
 }
+
+}  // namespace
+
+namespace ipfem {
 
 // launch-error and device-error-word check after a synchronisation point
 ipfem_status check_device(ipfem_ctx *c)
@@ -108,6 +119,7 @@ void tangent_device(ipfem_ctx *c, const double *d_u, double *d_out, int update_m
     launch_color_reduce(c, c->d_fe, c->load_factor, 1, d_out);
     if (c->precision == 1) launch_stiffness32(c);
     else launch_stiffness(c);
+    if (c->precision == 1 && c->mlp.ready) launch_plastic_fraction(c);
     c->tangent_valid = true;
 }
 
@@ -186,8 +198,6 @@ ipfem_status cg32_device(ipfem_ctx *c, const double *d_b, double scale, double r
     return IPFEM_OK;
 }
 
-ipfem_status dot_host(ipfem_ctx *c, const double *a, const double *b, double *out);
-
 // K du = b in the context's precision; du accumulated into d_u (d_u += du)
 // when add != 0, else written to c->d_x.
 ipfem_status solve_device(ipfem_ctx *c, const double *d_b, double rtol, int max_it, int *iters, double *d_u, int add)
@@ -209,7 +219,13 @@ ipfem_status solve_device(ipfem_ctx *c, const double *d_b, double rtol, int max_
         if (!add) CK(cudaMemsetAsync(c->d_x, 0, (size_t)c->s.neq * sizeof(double), c->stream));
         return std::isfinite(bn) ? IPFEM_OK : fail(c, IPFEM_NAN, "right-hand side is not finite");
     }
-    st = cg32_device(c, d_b, 1.0 / bn, rtol, max_it, iters);
+    if (c->preconditioner == IPFEM_PREC_MLP) {
+        int fb = 0;
+        st = fcg_device(c, d_b, 1.0 / bn, rtol, max_it, iters, &fb);
+        c->fcg_fallbacks += fb;
+    } else {
+        st = cg32_device(c, d_b, 1.0 / bn, rtol, max_it, iters);
+    }
     if (!add) {
         CK(cudaMemsetAsync(c->d_x, 0, (size_t)c->s.neq * sizeof(double), c->stream));
         launch_add_scaled32(c, c->d_x, c->mx.x, bn);
@@ -231,7 +247,7 @@ ipfem_status dot_host(ipfem_ctx *c, const double *a, const double *b, double *ou
     return IPFEM_OK;
 }
 
-}  // namespace
+}  // namespace ipfem
 
 void ipfem::set_thread_error(const std::string &msg)
 {

@@ -24,7 +24,10 @@ template <class T>
 struct CGScalarsT {
     T rz, pq, alpha, beta, rr, bb, thr;
     int done, iters, status, max_it;
+    T rr_best;                    // flexible CG: stagnation watch
+    int it_best, fallback;
 };
+constexpr int kStatusFallback = 9;   // flexible CG stagnated: the caller falls back to Jacobi-PCG
 typedef CGScalarsT<double> CGScalars;
 
 // buffers of the mixed-precision solve (FP32 tangent and CG)
@@ -87,6 +90,23 @@ struct NewtonState {
     double r0 = 0.0, rn = 0.0;
 };
 
+namespace ipfem {
+// learned preconditioner (per-node MLP) and its training state
+struct MlpBuffers {
+    float *params = nullptr;      // FP32 master: W1[32][128] b1[128] W2[128][128] b2[128] W3[128][2] b3[2]
+    float *grads = nullptr, *m = nullptr, *v = nullptr;
+    void *w1t = nullptr, *w2t = nullptr;   // BF16 [128][32], [128][128] (n-major, k contiguous)
+    float *pfrac = nullptr, *pden = nullptr;
+    float *r_old = nullptr;       // flexible-CG previous residual
+    float *loss = nullptr;
+    int32_t gr = 0, gt = 0;       // structured node grid (gr x gt)
+    int64_t adam_t = 0;
+    bool ready = false;
+};
+constexpr int kMlpParams = 32 * 128 + 128 + 128 * 128 + 128 + 128 * 2 + 2;
+constexpr int kOffW1 = 0, kOffB1 = 4096, kOffW2 = 4224, kOffB2 = 20608, kOffW3 = 20736, kOffB3 = 20992;
+}  // namespace ipfem
+
 struct ipfem_ctx {
     int device = -1;
     cudaStream_t stream = nullptr;
@@ -126,6 +146,10 @@ struct ipfem_ctx {
     uint64_t launches = 0;               // kernels launched through this context
     int precision = 0;                   // IPFEM_PLAIN_FP64 or IPFEM_MIXED
     ipfem::MixedBuffers mx;
+    int preconditioner = 0;              // IPFEM_PREC_JACOBI or IPFEM_PREC_MLP
+    ipfem::MlpBuffers mlp;
+    cudaGraphExec_t fcg_exec = nullptr;
+    int64_t fcg_fallbacks = 0;
 };
 
 // ---- kernel launchers (implemented in the .cu files) ----
@@ -146,5 +170,23 @@ void launch_stiffness32(ipfem_ctx *c);
 void launch_cg32_init(ipfem_ctx *c, const double *d_b, double scale, float rtol, int max_it);
 void launch_cg32_iteration(ipfem_ctx *c);
 void launch_cg32_spmv_only(ipfem_ctx *c);
+void launch_cg32_pupdate_only(ipfem_ctx *c);
 void launch_add_scaled32(ipfem_ctx *c, double *d_u, const float *x, double scale);
+// solver drivers (capi.cpp, capi_mlp.cu)
+ipfem_status check_device(ipfem_ctx *c);
+ipfem_status cg_device(ipfem_ctx *c, const double *d_b, double rtol, int max_it, int *iters);
+ipfem_status cg32_device(ipfem_ctx *c, const double *d_b, double scale, double rtol, int max_it, int *iters);
+ipfem_status fcg_device(ipfem_ctx *c, const double *d_b, double scale, double rtol, int max_it, int *iters,
+                        int *fell_back);
+ipfem_status dot_host(ipfem_ctx *c, const double *a, const double *b, double *out);
+// learned preconditioner (k_mlp.cu)
+void mlp_pack_weights(ipfem_ctx *c);
+cudaError_t mlp_configure();
+void launch_plastic_fraction(ipfem_ctx *c);
+void launch_features(ipfem_ctx *c, const float *d_r, float *d_X, float *d_S);
+void launch_mlp_infer_rows(ipfem_ctx *c, int64_t rows, const float *d_X, float *d_O);
+void launch_fcg_init(ipfem_ctx *c, const double *d_b, double scale, float rtol, int max_it);
+void launch_fcg_iteration(ipfem_ctx *c);
+void mlp_train_step(ipfem_ctx *c, int64_t rows, const float *X, const float *Y, float *H1, float *H2, float *O,
+                    float *dO, float *dH1, float *dH2, bool update, float lr);
 }  // namespace ipfem

@@ -111,22 +111,15 @@ __global__ void __launch_bounds__(kResTile * 18) k_stress_residual(int32_t n_el,
     if (el >= ne) return;
     const int n = j >> 1;
     const double *dn = s_dn + el * 162;
-    const double *sxx = s_sig + el * 9;
-    const double *sxy = s_sig + kResTile * 9 + el * 9;
-    const double *syy = s_sig + 2 * kResTile * 9 + el * 9;
+    // x-dof: dNx*sxx + dNy*sxy per point; y-dof: dNx*sxy + dNy*syy.  The two
+    // stress rows are selected by pointer so the warp does not diverge.
+    const double *s1 = s_sig + (j & 1) * kResTile * 9 + el * 9;
+    const double *s2 = s1 + kResTile * 9;
     double acc = 0.0;
-    if ((j & 1) == 0) {
 #pragma unroll
-        for (int q = 0; q < 9; q++) {
-            acc = fma(dn[q * 18 + n], sxx[q], acc);
-            acc = fma(dn[q * 18 + 9 + n], sxy[q], acc);
-        }
-    } else {
-#pragma unroll
-        for (int q = 0; q < 9; q++) {
-            acc = fma(dn[q * 18 + n], sxy[q], acc);
-            acc = fma(dn[q * 18 + 9 + n], syy[q], acc);
-        }
+    for (int q = 0; q < 9; q++) {
+        acc = fma(dn[q * 18 + n], s1[q], acc);
+        acc = fma(dn[q * 18 + 9 + n], s2[q], acc);
     }
     fe[(size_t)(e0 + el) * 18 + j] = -acc;
 }
@@ -227,15 +220,10 @@ __global__ void __launch_bounds__(kStiffWarps * 32) k_stiffness(int32_t n_in_col
         const T *D = &s_D[w][q * 9];
         const T *dx = dn + q * 18, *dy = dx + 9;
         for (int t = lane; t < 54; t += 32) {
-            const int i = t / 18, j = t - i * 18, n = j >> 1;
-            T sv;
-            if ((j & 1) == 0) {
-                sv = D[3 * i + 0] * dx[n];
-                sv = fma(D[3 * i + 1], dy[n], sv);
-            } else {
-                sv = D[3 * i + 1] * dx[n];
-                sv = fma(D[3 * i + 2], dy[n], sv);
-            }
+            // x-dof column j: D[i][0] dNx + D[i][1] dNy; y-dof: D[i][1] dNx + D[i][2] dNy
+            const int i = t / 18, j = t - i * 18, n = j >> 1, c0 = 3 * i + (j & 1);
+            T sv = D[c0] * dx[n];
+            sv = fma(D[c0 + 1], dy[n], sv);
             s_DB[w][t] = sv;
         }
         __syncwarp();
@@ -244,15 +232,11 @@ __global__ void __launch_bounds__(kStiffWarps * 32) k_stiffness(int32_t n_in_col
         for (int m = 0; m < 6; m++) {
             const int p = lane + 32 * m;
             if (p < 171) {
-                const int a = pa[m], b = pb[m], na = a >> 1;
+                // x-dof row a: dNx DB[0][b] + dNy DB[1][b]; y-dof: dNx DB[1][b] + dNy DB[2][b]
+                const int a = pa[m], b = pb[m], na = a >> 1, o = (a & 1) * 18 + b;
                 T t = acc[m];
-                if ((a & 1) == 0) {
-                    t = fma(dx[na], DB[b], t);
-                    t = fma(dy[na], DB[18 + b], t);
-                } else {
-                    t = fma(dx[na], DB[18 + b], t);
-                    t = fma(dy[na], DB[36 + b], t);
-                }
+                t = fma(dx[na], DB[o], t);
+                t = fma(dy[na], DB[o + 18], t);
                 acc[m] = t;
             }
         }

@@ -390,6 +390,12 @@ void launch_cg32_spmv_only(ipfem_ctx *c)
                                                                  c->n_red, c->d_counters + 5, m.sc);
 }
 
+void launch_cg32_pupdate_only(ipfem_ctx *c)
+{
+    MixedBuffers &m = c->mx;
+    k_cg_pupdate<float><<<grid_nodes(c), kRedBlock, 0, c->stream>>>(c->s.n_nodes, m.z, m.p, m.sc);
+}
+
 void launch_add_scaled32(ipfem_ctx *c, double *d_u, const float *x, double scale)
 {
     const int64_t n = c->s.neq;
