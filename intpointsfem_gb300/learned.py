@@ -17,7 +17,7 @@ import numpy as np
 from . import (DEVICE, MIXED, PREC_JACOBI, PREC_MLP, ElastoPlasticIntPointsStructMatrix, WellboreMesh,
                wellbore_params)
 
-SNAPS = [0, 32, 64, 128, 256, 512, 1024, 2048]
+SNAPS = [0, 32, 64, 96, 128, 160, 256, 288, 512, 544, 1024, 1056, 2048, 2080]
 
 
 def _torch():
@@ -36,8 +36,14 @@ def make_solver(n, pw, phi, seed=0, n_steps=10):
 
 
 def generate_training_data(n=400, n_samples=50000, n_problems=8, seed=20260101, n_steps=10, cg_rtol=1e-5,
-                           device="cuda"):
-    """Returns (X [samples, 32], Y [samples, 2]) as FP32 device tensors."""
+                           target="increment", s_floor=1e-2, t_cap=100.0, device="cuda"):
+    """Returns (X [samples, 32], Y [samples, 2]) as FP32 device tensors.
+
+    target "increment": the CG solution increment over the next 32 iterations,
+    x_{k+32} - x_k, for the residual r_k; "error": the remaining increment
+    x_final - x_k.  Samples whose patch residual scale s is below s_floor times
+    the RMS scale of the snapshot, or whose scaled target exceeds t_cap, are
+    dropped (the residual there carries no information about the increment)."""
     torch = _torch()
     rng = np.random.default_rng(seed)
     Xs, Ys = [], []
@@ -63,14 +69,31 @@ def generate_training_data(n=400, n_samples=50000, n_problems=8, seed=20260101, 
         S = torch.zeros(sm.n_nodes, dtype=torch.float32, device=device)
         T = torch.zeros(sm.neq, dtype=torch.float32, device=device)
         fixed = torch.tensor(wb.array("fixed").reshape(-1, 2).min(axis=1) == 0, device=device)
-        free_nodes = torch.nonzero(fixed).flatten().cpu().numpy()
+        free_nodes_t = torch.nonzero(fixed).flatten()
         for si in snaps:
+            if target == "increment":
+                nxt = SNAPS[si] + 32
+                if nxt >= its:
+                    continue
+                xn = xs[SNAPS.index(nxt)] if nxt in SNAPS else None
+                if xn is None:
+                    continue
+                e = xn - xs[si]
+            else:
+                e = xf - xs[si]
             sm.mlp_features(rs[si].double(), X, S)
-            sm.mlp_targets(xf - xs[si], S, T)
-            pick = rng.choice(free_nodes, size=min(len(free_nodes), per_problem // len(snaps)), replace=False)
+            sm.mlp_targets(e, S, T)
+            Tn = T.view(-1, 2)
+            srms = torch.sqrt((S[free_nodes_t] ** 2).mean())
+            good = (S > s_floor * srms) & (Tn.abs().max(dim=1).values < t_cap) & torch.isfinite(Tn).all(dim=1)
+            good[~fixed] = False
+            cand = torch.nonzero(good).flatten().cpu().numpy()
+            if len(cand) == 0:
+                continue
+            pick = rng.choice(cand, size=min(len(cand), per_problem // len(snaps)), replace=False)
             idx = torch.tensor(pick, device=device)
             Xs.append(X[idx].clone())
-            Ys.append(T.view(-1, 2)[idx].clone())
+            Ys.append(Tn[idx].clone())
         sm.close()
         wb.close()
     X = torch.cat(Xs)
