@@ -141,6 +141,7 @@ typedef struct {
     int32_t converged;
     double final_res;
     double ms_assemble, ms_solve, ms_commit;
+    int64_t fcg_fallbacks;   /* learned-preconditioner solves that fell back to Jacobi-PCG */
 } ipfem_solve_stats;
 
 /* Runs steps [step_begin, step_end); u (neq, host or device per `where`)
@@ -214,30 +215,39 @@ int32_t ipfem_color_elements(int32_t n_elements, int32_t n_nodes, const int32_t 
 
 /* ------------------------------------------------- learned preconditioner */
 /* None of these has a counterpart in the reference.  A per-node MLP
- * (32 features -> 128 -> 128 -> 2, BF16 weights, FP32 accumulation on the
- * tensor cores) maps the residual around a node to a displacement
- * correction; it runs inside flexible CG (Polak-Ribiere) on the FP32 tangent
- * and falls back to Jacobi-PCG when FCG stagnates.  Requires IPFEM_MIXED and
- * a structured node grid (node = b*gr + a).  Parameters are one FP32 vector
- * of 20994 values: W1[32][128] b1[128] W2[128][128] b2[128] W3[128][2] b3[2]. */
+ * (32 -> 128 -> 128 -> 36, BF16 weights, FP32 accumulation on the tensor
+ * cores) maps the FP32 tangent around node i of a structured node grid
+ * (node = b*gr + a) to one block row O_i[9][2][2] of a 3x3-patch operator
+ * (patch position k = 3*(db+1) + (da+1), da, db in {-1, 0, 1}).  Features:
+ * X_i[4m + 2p + q] = K_ij[p][q] s_i[p] s_j[q] for the 8 neighbours j in k
+ * order without the centre, s = sqrt(Jacobi inverse diagonal), 0 on Dirichlet
+ * dofs.  Operator: M_ik[p][q] = s_i[p] ((O_ik[p][q] + O_j(8-k)[q][p]) / 2 +
+ * (k == 4) (p == q)) s_j[q], symmetric by construction; O = 0 is Jacobi.  The
+ * network runs once per tangent, M is applied in every iteration of flexible
+ * CG (Polak-Ribiere), which falls back to Jacobi-PCG when it stagnates.
+ * Requires IPFEM_MIXED.  Parameters are one FP32 vector of 25380 values:
+ * W1[32][128] b1[128] W2[128][128] b2[128] W3[128][36] b3[36]. */
 ipfem_status ipfem_set_node_grid(ipfem_ctx *ctx, int32_t gr, int32_t gt);
+/* allocates the network (He-uniform W1, W2; W3 = 0, zero biases) */
 ipfem_status ipfem_mlp_init(ipfem_ctx *ctx, uint64_t seed);
 ipfem_status ipfem_set_preconditioner(ipfem_ctx *ctx, int kind);
 ipfem_status ipfem_mlp_get_params(ipfem_ctx *ctx, float *out);
 ipfem_status ipfem_mlp_set_params(ipfem_ctx *ctx, const float *in);
-/* features [n_nodes][32] and scales [n_nodes] of a device residual (FP64) */
-ipfem_status ipfem_mlp_features(ipfem_ctx *ctx, const double *d_r, float *d_X, float *d_S);
-/* training targets T = e / (S * Dinv) per dof of an error vector e [neq] and
- * the feature scales S (0 on fixed dofs), all FP32 device arrays */
-ipfem_status ipfem_mlp_targets(ipfem_ctx *ctx, const float *d_e, const float *d_S, float *d_T);
-/* network output [rows][2] for device feature rows [rows][32] */
+/* features [n_nodes][32] (device) of the current FP32 tangent */
+ipfem_status ipfem_mlp_features(ipfem_ctx *ctx, float *d_X);
+/* network output [rows][36] (device) for device feature rows [rows][32] */
 ipfem_status ipfem_mlp_forward(ipfem_ctx *ctx, const float *d_X, int64_t rows, float *d_O);
-/* MSE loss and parameter gradients (host, 20994 floats) of one full batch */
-ipfem_status ipfem_mlp_grad(ipfem_ctx *ctx, const float *d_X, const float *d_Y, int64_t rows, float *grads,
-                            float *loss);
-/* mini-batch Adam; loss_per_epoch[epochs] may be NULL */
-ipfem_status ipfem_mlp_train(ipfem_ctx *ctx, const float *d_X, const float *d_Y, int64_t rows, int epochs, int batch,
-                             float lr, uint64_t seed, float *loss_per_epoch);
+/* the patch operator of the current tangent, M[9][n_nodes][2][2] (device) */
+ipfem_status ipfem_mlp_operator(ipfem_ctx *ctx, float *d_M);
+/* training pass on the current FP32 tangent over n_pairs (residual r_p,
+ * solution increment e_p) pairs, FP32 device arrays [n_pairs][neq]:
+ * loss = (1/n_pairs) sum_p |K e_p - K M r_p|^2 / |K e_p|^2 and its gradient
+ * (host, 25380 floats; either pointer may be NULL) */
+ipfem_status ipfem_learn_grad(ipfem_ctx *ctx, const float *d_r, const float *d_e, int n_pairs, float *grads,
+                              float *loss);
+/* one Adam step (beta 0.9, 0.999) with the host gradient, or with the
+ * context's last gradient when grads is NULL */
+ipfem_status ipfem_mlp_adam(ipfem_ctx *ctx, const float *grads, float lr);
 /* FP32 Jacobi-CG with (x_k, r_k) snapshots at iterations that are multiples of
  * 32, plus the final iterate (training data: residual / solution increment) */
 ipfem_status ipfem_cg_snapshots(ipfem_ctx *ctx, const double *d_b, double rtol, int max_it, int n_snap,

@@ -18,7 +18,7 @@ LIB_PATH = os.path.join(HERE, "libipfem.so")
 HOST, DEVICE = 0, 1
 PLAIN_FP64, MIXED = 0, 1
 PREC_JACOBI, PREC_MLP = 0, 1
-MLP_PARAMS = 20994
+MLP_PARAMS = 25380
 STATUS = {0: "ok", 1: "not converged", 2: "non-finite value", 3: "CG breakdown", 4: "out of device memory",
           5: "invalid argument", 6: "CUDA error", 7: "no sm_103 device"}
 
@@ -52,7 +52,7 @@ class SolveOpts(C.Structure):
 class SolveStats(C.Structure):
     _fields_ = [("newton_iters", C.c_int32), ("cg_iters", C.c_int64), ("last_step_iters", C.c_int32),
                 ("converged", C.c_int32), ("final_res", C.c_double), ("ms_assemble", C.c_double),
-                ("ms_solve", C.c_double), ("ms_commit", C.c_double)]
+                ("ms_solve", C.c_double), ("ms_commit", C.c_double), ("fcg_fallbacks", C.c_int64)]
 
 
 class WellboreParams(C.Structure):
@@ -111,11 +111,11 @@ def lib():
             "ipfem_set_preconditioner": (S, [P, S]),
             "ipfem_mlp_get_params": (S, [P, C.POINTER(C.c_float)]),
             "ipfem_mlp_set_params": (S, [P, C.POINTER(C.c_float)]),
-            "ipfem_mlp_features": (S, [P, P, P, P]),
-            "ipfem_mlp_targets": (S, [P, P, P, P]),
+            "ipfem_mlp_features": (S, [P, P]),
             "ipfem_mlp_forward": (S, [P, P, C.c_int64, P]),
-            "ipfem_mlp_grad": (S, [P, P, P, C.c_int64, C.POINTER(C.c_float), C.POINTER(C.c_float)]),
-            "ipfem_mlp_train": (S, [P, P, P, C.c_int64, S, S, C.c_float, C.c_uint64, C.POINTER(C.c_float)]),
+            "ipfem_mlp_operator": (S, [P, P]),
+            "ipfem_learn_grad": (S, [P, P, P, S, C.POINTER(C.c_float), C.POINTER(C.c_float)]),
+            "ipfem_mlp_adam": (S, [P, C.POINTER(C.c_float), C.c_float]),
             "ipfem_cg_snapshots": (S, [P, P, C.c_double, S, S, _ip, P, P, P, C.POINTER(C.c_int)]),
             "ipfem_gather_strain": (S, [P, P, P]),
             "ipfem_compute_sigma": (S, [P, S, P, P, P]),
@@ -368,28 +368,35 @@ class ElastoPlasticIntPointsStructMatrix:
         assert p.size == MLP_PARAMS
         self._check(lib().ipfem_mlp_set_params(self._ctx, p.ctypes.data_as(C.POINTER(C.c_float))))
 
-    def mlp_features(self, d_r, d_X, d_S):
-        self._check(lib().ipfem_mlp_features(self._ctx, _ptr(d_r), _ptr(d_X), _ptr(d_S)))
-
-    def mlp_targets(self, d_e, d_S, d_T):
-        self._check(lib().ipfem_mlp_targets(self._ctx, _ptr(d_e), _ptr(d_S), _ptr(d_T)))
+    def mlp_features(self, d_X):
+        """features [n_nodes][32] of the current FP32 tangent into a device array"""
+        self._check(lib().ipfem_mlp_features(self._ctx, _ptr(d_X)))
 
     def mlp_forward(self, d_X, rows, d_O):
+        """network output [rows][36] of device feature rows [rows][32]"""
         self._check(lib().ipfem_mlp_forward(self._ctx, _ptr(d_X), int(rows), _ptr(d_O)))
 
-    def mlp_grad(self, d_X, d_Y, rows):
+    def mlp_operator(self, d_M):
+        """the patch operator [9][n_nodes][2][2] of the current tangent (device)"""
+        self._check(lib().ipfem_mlp_operator(self._ctx, _ptr(d_M)))
+
+    def learn_grad(self, d_r, d_e, n_pairs):
+        """loss and parameter gradient over (residual, increment) pairs [n_pairs][neq] (FP32, device)"""
         g = np.zeros(MLP_PARAMS, np.float32)
         loss = np.zeros(1, np.float32)
-        self._check(lib().ipfem_mlp_grad(self._ctx, _ptr(d_X), _ptr(d_Y), int(rows),
-                                         g.ctypes.data_as(C.POINTER(C.c_float)),
-                                         loss.ctypes.data_as(C.POINTER(C.c_float))))
+        self._check(lib().ipfem_learn_grad(self._ctx, _ptr(d_r), _ptr(d_e), int(n_pairs),
+                                           g.ctypes.data_as(C.POINTER(C.c_float)),
+                                           loss.ctypes.data_as(C.POINTER(C.c_float))))
         return g, float(loss[0])
 
-    def mlp_train(self, d_X, d_Y, rows, epochs=30, batch=2048, lr=2e-3, seed=0):
-        losses = np.zeros(max(1, epochs), np.float32)
-        self._check(lib().ipfem_mlp_train(self._ctx, _ptr(d_X), _ptr(d_Y), int(rows), int(epochs), int(batch),
-                                          float(lr), int(seed), losses.ctypes.data_as(C.POINTER(C.c_float))))
-        return losses[:epochs]
+    def mlp_adam(self, grads, lr):
+        """one Adam step with a host gradient (None: the context's last gradient)"""
+        if grads is None:
+            self._check(lib().ipfem_mlp_adam(self._ctx, None, float(lr)))
+        else:
+            g = np.ascontiguousarray(grads, dtype=np.float32)
+            assert g.size == MLP_PARAMS
+            self._check(lib().ipfem_mlp_adam(self._ctx, g.ctypes.data_as(C.POINTER(C.c_float)), float(lr)))
 
     def cg_snapshots(self, d_b, snap_iters, d_xs, d_rs, d_xfinal, rtol=1e-6, max_it=200000):
         si = np.ascontiguousarray(snap_iters, dtype=np.int32)

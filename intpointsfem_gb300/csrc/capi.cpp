@@ -43,10 +43,37 @@ cudaError_t upload(T **p, const std::vector<T> &v, cudaStream_t st)
     return cudaMemcpyAsync(*p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, st);
 }
 
+cudaError_t upload_sell(const SellLayout &L, bool sorted, SellDev &D, cudaStream_t t)
+{
+    cudaError_t e = cudaSuccess;
+    auto ck = [&](cudaError_t x) {
+        if (x != cudaSuccess && e == cudaSuccess) e = x;
+    };
+    ck(upload(&D.slice_base, L.slice_base, t));
+    ck(upload(&D.diag_blk, L.diag_blk, t));
+    ck(upload(&D.sell_col, L.sell_col, t));
+    ck(upload(&D.rowlen, L.rowlen, t));
+    ck(upload(&D.sell_node, L.sell_node, t));
+    ck(upload(&D.el_blk, L.el_blk, t));
+    D.n_sell = L.n_sell;
+    D.sorted = sorted;
+    return e;
+}
+
+void free_sell(SellDev &D)
+{
+    void *ptrs[] = {D.slice_base, D.diag_blk, D.sell_col, D.rowlen, D.sell_node, D.el_blk};
+    for (void *p : ptrs)
+        if (p) cudaFree(p);
+    D = SellDev();
+}
+
 void free_all(ipfem_ctx *c)
 {
+    free_sell(c->dsell);
+    free_sell(c->mx.dsell);
     void *ptrs[] = {c->d_dphi, c->d_weight, c->d_mat, c->d_f0, c->d_df, c->d_dofs, c->d_color_els, c->d_inc,
-                    c->d_fixed, c->d_slice_base, c->d_diag_blk, c->d_sell_col, c->d_rowlen, c->d_el_blk, c->d_K,
+                    c->d_fixed, c->d_K,
                     c->d_dinv, c->d_eps_p, c->d_sigma, c->d_alpha, c->d_mtype, c->d_u, c->d_rhs, c->d_strain,
                     c->d_sigma_w, c->d_dep, c->d_fe, c->d_x, c->d_r, c->d_z, c->d_p, c->d_q, c->d_b, c->d_part,
                     c->d_sc, c->d_counters, c->d_dotres, c->d_err};
@@ -66,7 +93,8 @@ void free_all(ipfem_ctx *c)
     if (c->fcg_exec) cudaGraphExecDestroy(c->fcg_exec);
     {
         MlpBuffers &l = c->mlp;
-        void *lp[] = {l.params, l.grads, l.m, l.v, l.w1t, l.w2t, l.pfrac, l.pden, l.r_old, l.loss};
+        void *lp[] = {l.params, l.grads, l.m, l.v, l.w1t, l.w2t, l.w3t, l.slot, l.X, l.O, l.M, l.r_old, l.loss,
+                      l.scal, l.H1, l.H2, l.dH1, l.dH2, l.dN, l.part, l.vec};
         for (void *p : lp)
             if (p) cudaFree(p);
     }
@@ -119,7 +147,7 @@ void tangent_device(ipfem_ctx *c, const double *d_u, double *d_out, int update_m
     launch_color_reduce(c, c->d_fe, c->load_factor, 1, d_out);
     if (c->precision == 1) launch_stiffness32(c);
     else launch_stiffness(c);
-    if (c->precision == 1 && c->mlp.ready) launch_plastic_fraction(c);
+    c->mlp.op_valid = false;     // the learned operator belongs to the previous tangent
     c->tangent_valid = true;
 }
 
@@ -328,12 +356,8 @@ ipfem_status ipfem_create(const ipfem_mesh *mesh, const ipfem_material *mat, ipf
     ck(upload(&c->d_color_els, s.color_els, t));
     ck(upload(&c->d_inc, s.inc, t));
     ck(upload(&c->d_fixed, s.fixed, t));
-    ck(upload(&c->d_slice_base, s.slice_base, t));
-    ck(upload(&c->d_diag_blk, s.diag_blk, t));
-    ck(upload(&c->d_sell_col, s.sell_col, t));
-    ck(upload(&c->d_rowlen, s.rowlen, t));
-    ck(upload(&c->d_el_blk, s.el_blk, t));
-    ck(dalloc(&c->d_K, (size_t)s.n_sell * 4));
+    ck(upload_sell(s.sell, true, c->dsell, t));
+    ck(dalloc(&c->d_K, (size_t)s.sell.n_sell * 4));
     ck(dalloc(&c->d_dinv, (size_t)s.neq));
     ck(dalloc(&c->d_eps_p, (size_t)s.n_ip * 4));
     ck(dalloc(&c->d_sigma, (size_t)s.n_ip * 4));
@@ -367,7 +391,7 @@ ipfem_status ipfem_create(const ipfem_mesh *mesh, const ipfem_material *mat, ipf
     ck(cudaMemsetAsync(c->d_err, 0, sizeof(int), t));
     ck(cudaMemsetAsync(c->d_sc, 0, sizeof(CGScalars), t));
     ck(cudaMemsetAsync(c->d_u, 0, (size_t)s.neq * sizeof(double), t));
-    ck(cudaMemsetAsync(c->d_K, 0, (size_t)s.n_sell * 4 * sizeof(double), t));
+    ck(cudaMemsetAsync(c->d_K, 0, (size_t)s.sell.n_sell * 4 * sizeof(double), t));
     ck(cudaMemsetAsync(c->d_dinv, 0, (size_t)s.neq * sizeof(double), t));
     // initial state: in-situ seed
     {
@@ -428,7 +452,10 @@ ipfem_status ipfem_set_precision(ipfem_ctx *c, int mode)
         };
         std::vector<float> d32(s.dphi.begin(), s.dphi.end());
         ck(upload(&m.dphi, d32, c->stream));
-        ck(dalloc(&m.K, (size_t)s.n_sell * 4));
+        const std::string e = build_sell(s, false, m.sell);
+        if (!e.empty()) return fail(c, IPFEM_INVALID, e);
+        ck(upload_sell(m.sell, false, m.dsell, c->stream));
+        ck(dalloc(&m.K, (size_t)m.sell.n_sell * 4));
         ck(dalloc(&m.dinv, (size_t)s.neq));
         ck(dalloc(&m.x, (size_t)s.neq));
         ck(dalloc(&m.r, (size_t)s.neq));
@@ -488,17 +515,18 @@ ipfem_status ipfem_get_stiffness(ipfem_ctx *c, int64_t *row_ptr, int32_t *col, d
     if (row_ptr) std::memcpy(row_ptr, s.row_ptr.data(), s.row_ptr.size() * sizeof(int64_t));
     if (col) std::memcpy(col, s.col.data(), s.col.size() * sizeof(int32_t));
     if (vals && c->precision == 1) {
-        std::vector<float> h((size_t)s.n_sell * 4);
+        const SellLayout &L = c->mx.sell;
+        std::vector<float> h((size_t)L.n_sell * 4);
         CK(cudaMemcpyAsync(h.data(), c->mx.K, h.size() * sizeof(float), cudaMemcpyDeviceToHost, c->stream));
         CK(cudaStreamSynchronize(c->stream));
         for (int64_t k = 0; k < s.n_blocks; k++)
-            for (int j = 0; j < 4; j++) vals[4 * k + j] = h[4 * s.bsr_to_sell[k] + j];
+            for (int j = 0; j < 4; j++) vals[4 * k + j] = h[4 * L.bsr_to_sell[k] + j];
     } else if (vals) {
-        std::vector<double> h((size_t)s.n_sell * 4);
+        std::vector<double> h((size_t)s.sell.n_sell * 4);
         CK(cudaMemcpyAsync(h.data(), c->d_K, h.size() * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
         CK(cudaStreamSynchronize(c->stream));
         for (int64_t k = 0; k < s.n_blocks; k++)
-            std::memcpy(vals + 4 * k, h.data() + 4 * s.bsr_to_sell[k], 4 * sizeof(double));
+            std::memcpy(vals + 4 * k, h.data() + 4 * s.sell.bsr_to_sell[k], 4 * sizeof(double));
     }
     return IPFEM_OK;
 }
@@ -558,8 +586,10 @@ static ipfem_status newton_advance(ipfem_ctx *c, int32_t n_iters, double *du, ip
         bool conv = (ns.r0 == 0.0);
         if (!conv) {
             int k = 0;
+            const int64_t fb0 = c->fcg_fallbacks;
             cudaEventRecord(ev[0], c->stream);
             ipfem_status e = solve_device(c, c->d_rhs, o.cg_rtol, o.cg_max_it, &k, du, 1);
+            st->fcg_fallbacks += c->fcg_fallbacks - fb0;
             cudaEventRecord(ev[1], c->stream);
             st->ms_solve += elapsed();
             st->cg_iters += k;

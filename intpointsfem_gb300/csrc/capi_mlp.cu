@@ -1,6 +1,7 @@
-// C-ABI of the learned preconditioner: initialisation, features, training
-// (BF16 tensor-core forward/backward, Adam), and the flexible-CG solve with its
-// fallback to Jacobi-PCG.  No counterpart in the reference.
+// C-ABI of the learned preconditioner: initialisation, features, the network
+// forward, the training gradient pass and Adam (BF16 tensor-core GEMMs), and
+// the flexible-CG solve with its fallback to Jacobi-PCG.  No counterpart in
+// the reference.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -32,38 +33,39 @@ cudaError_t alloc(T **p, size_t n)
     return cudaMalloc((void **)p, (n ? n : 1) * sizeof(T));
 }
 
-__global__ void k_gather_rows(int64_t rows, int width, const int64_t *__restrict__ idx, const float *__restrict__ src,
-                              float *__restrict__ dst)
-{
-    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (i >= rows * width) return;
-    const int64_t r = i / width, c = i % width;
-    dst[i] = src[idx[r] * width + c];
-}
-
-__global__ void k_to_float(int64_t n, const double *__restrict__ a, float *__restrict__ b)
-{
-    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (i < n) b[i] = (float)a[i];
-}
-
-// T = e / (S * Dinv) per dof (0 where the dof is fixed)
-__global__ void k_targets(int32_t n_nodes, const float *__restrict__ e, const float *__restrict__ S,
-                          const float *__restrict__ dinv, float *__restrict__ T)
-{
-    const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n_nodes) return;
-    for (int k = 0; k < 2; k++) {
-        const float d = dinv[2 * (int64_t)i + k];
-        T[2 * (int64_t)i + k] = d > 0.f ? e[2 * (int64_t)i + k] / (S[i] * d) : 0.f;
-    }
-}
-
 ipfem_status need_mlp(ipfem_ctx *c)
 {
     if (!c) return IPFEM_INVALID;
     if (!c->mlp.ready) return mfail(c, IPFEM_INVALID, "ipfem_mlp_init not called");
     return IPFEM_OK;
+}
+
+ipfem_status need_tangent(ipfem_ctx *c)
+{
+    ipfem_status st = need_mlp(c);
+    if (st != IPFEM_OK) return st;
+    if (c->precision != IPFEM_MIXED || !c->tangent_valid)
+        return mfail(c, IPFEM_INVALID, "needs an assembled FP32 (IPFEM_MIXED) tangent");
+    return IPFEM_OK;
+}
+
+// slot[k][i]: FP32-tangent slot of block (i, nbr(i, k)) or -1
+std::vector<int32_t> patch_slots(const Setup &s, const SellLayout &L, int32_t gr, int32_t gt)
+{
+    const int64_t n = s.n_nodes;
+    std::vector<int32_t> slot((size_t)9 * n, -1);
+    for (int64_t i = 0; i < n; i++) {
+        const int a = (int)(i % gr), b = (int)(i / gr);
+        const int32_t *c0 = s.col.data() + s.row_ptr[i], *c1 = s.col.data() + s.row_ptr[i + 1];
+        for (int k = 0; k < 9; k++) {
+            const int aa = a + k % 3 - 1, bb = b + k / 3 - 1;
+            if (aa < 0 || bb < 0 || aa >= gr || bb >= gt) continue;
+            const int32_t j = bb * gr + aa;
+            const int32_t *f = std::lower_bound(c0, c1, j);
+            if (f != c1 && *f == j) slot[(size_t)k * n + i] = (int32_t)L.bsr_to_sell[s.row_ptr[i] + (f - c0)];
+        }
+    }
+    return slot;
 }
 
 }  // namespace
@@ -76,6 +78,7 @@ ipfem_status fcg_device(ipfem_ctx *c, const double *d_b, double scale, double rt
 {
     MixedBuffers &m = c->mx;
     *fell_back = 0;
+    if (!c->mlp.op_valid) launch_patch_operator(c);
     launch_fcg_init(c, d_b, scale, (float)rtol, max_it);
     c->launches += 3;
     const int batch = 16;
@@ -118,6 +121,8 @@ ipfem_status ipfem_set_node_grid(ipfem_ctx *c, int32_t gr, int32_t gt)
 {
     if (!c || gr < 1 || gt < 1 || (int64_t)gr * gt != c->s.n_nodes)
         return mfail(c, IPFEM_INVALID, "node grid does not match the number of nodes");
+    if (c->mlp.ready && (gr != c->mlp.gr || gt != c->mlp.gt))
+        return mfail(c, IPFEM_INVALID, "node grid is fixed once ipfem_mlp_init has run");
     c->mlp.gr = gr;
     c->mlp.gt = gt;
     return IPFEM_OK;
@@ -127,6 +132,7 @@ ipfem_status ipfem_mlp_init(ipfem_ctx *c, uint64_t seed)
 {
     if (!c) return IPFEM_INVALID;
     if (c->precision != IPFEM_MIXED) return mfail(c, IPFEM_INVALID, "the learned preconditioner needs IPFEM_MIXED");
+    if (c->mlp.gr == 0) return mfail(c, IPFEM_INVALID, "ipfem_set_node_grid not called");
     MlpBuffers &m = c->mlp;
     const Setup &s = c->s;
     if (!m.params) {
@@ -136,12 +142,19 @@ ipfem_status ipfem_mlp_init(ipfem_ctx *c, uint64_t seed)
         MK(alloc(&m.v, kMlpParams));
         MK(cudaMalloc(&m.w1t, 128 * 32 * 2));
         MK(cudaMalloc(&m.w2t, 128 * 128 * 2));
-        MK(alloc(&m.pfrac, (size_t)s.n_nodes));
-        MK(alloc(&m.pden, (size_t)s.n_nodes));
+        MK(cudaMalloc(&m.w3t, 40 * 128 * 2));
+        MK(alloc(&m.X, (size_t)s.n_nodes * 32));
+        MK(alloc(&m.O, (size_t)s.n_nodes * 36));
+        MK(alloc(&m.M, (size_t)s.n_nodes * 36));
         MK(alloc(&m.r_old, (size_t)s.neq));
         MK(alloc(&m.loss, 1));
+        MK(alloc(&m.scal, 2));
+        const std::vector<int32_t> slot = patch_slots(s, c->mx.sell, m.gr, m.gt);
+        MK(alloc(&m.slot, slot.size()));
+        MK(cudaMemcpyAsync(m.slot, slot.data(), slot.size() * sizeof(int32_t), cudaMemcpyHostToDevice, c->stream));
+        MK(cudaStreamSynchronize(c->stream));
     }
-    // He-uniform W1, W2; W3 = 0 and zero biases, so the initial network is Jacobi
+    // He-uniform W1, W2; W3 = 0 and zero biases, so the initial operator is Jacobi
     std::vector<float> p(kMlpParams, 0.f);
     std::mt19937_64 rng(seed);
     std::uniform_real_distribution<float> u(-1.f, 1.f);
@@ -152,7 +165,6 @@ ipfem_status ipfem_mlp_init(ipfem_ctx *c, uint64_t seed)
     MK(cudaMemsetAsync(m.m, 0, kMlpParams * sizeof(float), c->stream));
     MK(cudaMemsetAsync(m.v, 0, kMlpParams * sizeof(float), c->stream));
     MK(cudaMemsetAsync(m.grads, 0, kMlpParams * sizeof(float), c->stream));
-    MK(cudaMemsetAsync(m.pfrac, 0, (size_t)s.n_nodes * sizeof(float), c->stream));
     m.adam_t = 0;
     MK(mlp_configure());
     mlp_pack_weights(c);
@@ -168,7 +180,6 @@ ipfem_status ipfem_set_preconditioner(ipfem_ctx *c, int kind)
     if (kind == IPFEM_PREC_MLP) {
         if (c->precision != IPFEM_MIXED) return mfail(c, IPFEM_INVALID, "the learned preconditioner needs IPFEM_MIXED");
         if (!c->mlp.ready) return mfail(c, IPFEM_INVALID, "ipfem_mlp_init not called");
-        if (c->mlp.gr == 0) return mfail(c, IPFEM_INVALID, "ipfem_set_node_grid not called");
     }
     c->preconditioner = kind;
     return IPFEM_OK;
@@ -178,6 +189,7 @@ ipfem_status ipfem_mlp_get_params(ipfem_ctx *c, float *out)
 {
     ipfem_status st = need_mlp(c);
     if (st != IPFEM_OK) return st;
+    if (!out) return mfail(c, IPFEM_INVALID, "bad args");
     MK(cudaMemcpyAsync(out, c->mlp.params, kMlpParams * sizeof(float), cudaMemcpyDeviceToHost, c->stream));
     MK(cudaStreamSynchronize(c->stream));
     return IPFEM_OK;
@@ -187,33 +199,21 @@ ipfem_status ipfem_mlp_set_params(ipfem_ctx *c, const float *in)
 {
     ipfem_status st = need_mlp(c);
     if (st != IPFEM_OK) return st;
+    if (!in) return mfail(c, IPFEM_INVALID, "bad args");
+    for (int i = 0; i < kMlpParams; i++)
+        if (!std::isfinite(in[i])) return mfail(c, IPFEM_INVALID, "parameters are not finite");
     MK(cudaMemcpyAsync(c->mlp.params, in, kMlpParams * sizeof(float), cudaMemcpyHostToDevice, c->stream));
     mlp_pack_weights(c);
     MK(cudaStreamSynchronize(c->stream));
     return IPFEM_OK;
 }
 
-ipfem_status ipfem_mlp_features(ipfem_ctx *c, const double *d_r, float *d_X, float *d_S)
+ipfem_status ipfem_mlp_features(ipfem_ctx *c, float *d_X)
 {
-    ipfem_status st = need_mlp(c);
+    ipfem_status st = need_tangent(c);
     if (st != IPFEM_OK) return st;
-    if (!d_r || !d_X || !d_S || c->mlp.gr == 0) return mfail(c, IPFEM_INVALID, "bad args or no node grid");
-    const int64_t n = c->s.neq;
-    k_to_float<<<(unsigned)((n + 255) / 256), 256, 0, c->stream>>>(n, d_r, c->mx.q);
-    launch_plastic_fraction(c);
-    launch_features(c, c->mx.q, d_X, d_S);
-    c->launches += 5;
-    MK(cudaStreamSynchronize(c->stream));
-    MK(cudaGetLastError());
-    return IPFEM_OK;
-}
-
-ipfem_status ipfem_mlp_targets(ipfem_ctx *c, const float *d_e, const float *d_S, float *d_T)
-{
-    ipfem_status st = need_mlp(c);
-    if (st != IPFEM_OK) return st;
-    if (!d_e || !d_S || !d_T) return mfail(c, IPFEM_INVALID, "bad args");
-    k_targets<<<(c->s.n_nodes + 255) / 256, 256, 0, c->stream>>>(c->s.n_nodes, d_e, d_S, c->mx.dinv, d_T);
+    if (!d_X) return mfail(c, IPFEM_INVALID, "bad args");
+    launch_patch_features(c, d_X);
     c->launches += 1;
     MK(cudaStreamSynchronize(c->stream));
     MK(cudaGetLastError());
@@ -224,80 +224,66 @@ ipfem_status ipfem_mlp_forward(ipfem_ctx *c, const float *d_X, int64_t rows, flo
 {
     ipfem_status st = need_mlp(c);
     if (st != IPFEM_OK) return st;
-    if (!d_X || !d_O || rows < 0 || rows > ((int64_t)1 << 31) * 64) return mfail(c, IPFEM_INVALID, "bad args");
+    if (!d_X || !d_O || rows < 0) return mfail(c, IPFEM_INVALID, "bad args");
     if (rows == 0) return IPFEM_OK;
-    launch_mlp_infer_rows(c, rows, d_X, d_O);
+    launch_patch_net(c, rows, d_X, d_O);
     c->launches += 1;
     MK(cudaStreamSynchronize(c->stream));
     MK(cudaGetLastError());
     return IPFEM_OK;
 }
 
-ipfem_status ipfem_mlp_grad(ipfem_ctx *c, const float *d_X, const float *d_Y, int64_t rows, float *grads, float *loss)
+ipfem_status ipfem_mlp_operator(ipfem_ctx *c, float *d_M)
 {
-    ipfem_status st = need_mlp(c);
+    ipfem_status st = need_tangent(c);
     if (st != IPFEM_OK) return st;
-    if (!d_X || !d_Y || rows < 1 || rows > 65535LL * 64) return mfail(c, IPFEM_INVALID, "bad args (rows <= 4194240)");
-    float *H1, *H2, *O, *dO, *dH1, *dH2;
-    MK(alloc(&H1, (size_t)rows * 128));
-    MK(alloc(&H2, (size_t)rows * 128));
-    MK(alloc(&O, (size_t)rows * 2));
-    MK(alloc(&dO, (size_t)rows * 2));
-    MK(alloc(&dH1, (size_t)rows * 128));
-    MK(alloc(&dH2, (size_t)rows * 128));
-    mlp_train_step(c, rows, d_X, d_Y, H1, H2, O, dO, dH1, dH2, false, 0.f);
-    c->launches += 16;
-    if (grads) MK(cudaMemcpyAsync(grads, c->mlp.grads, kMlpParams * sizeof(float), cudaMemcpyDeviceToHost, c->stream));
-    if (loss) MK(cudaMemcpyAsync(loss, c->mlp.loss, sizeof(float), cudaMemcpyDeviceToHost, c->stream));
+    if (!d_M) return mfail(c, IPFEM_INVALID, "bad args");
+    if (!c->mlp.op_valid) launch_patch_operator(c);
+    MK(cudaMemcpyAsync(d_M, c->mlp.M, (size_t)c->s.n_nodes * 36 * sizeof(float), cudaMemcpyDeviceToDevice,
+                       c->stream));
     MK(cudaStreamSynchronize(c->stream));
-    cudaFree(H1); cudaFree(H2); cudaFree(O); cudaFree(dO); cudaFree(dH1); cudaFree(dH2);
     MK(cudaGetLastError());
     return IPFEM_OK;
 }
 
-ipfem_status ipfem_mlp_train(ipfem_ctx *c, const float *d_X, const float *d_Y, int64_t rows, int epochs, int batch,
-                             float lr, uint64_t seed, float *loss_per_epoch)
+ipfem_status ipfem_learn_grad(ipfem_ctx *c, const float *d_r, const float *d_e, int n_pairs, float *grads,
+                              float *loss)
+{
+    ipfem_status st = need_tangent(c);
+    if (st != IPFEM_OK) return st;
+    if (!d_r || !d_e || n_pairs < 1) return mfail(c, IPFEM_INVALID, "bad args");
+    MlpBuffers &m = c->mlp;
+    const Setup &s = c->s;
+    if (!m.H1) {
+        const size_t n = (size_t)s.n_nodes;
+        MK(alloc(&m.H1, n * 128));
+        MK(alloc(&m.H2, n * 128));
+        MK(alloc(&m.dH1, n * 128));
+        MK(alloc(&m.dH2, n * 128));
+        MK(alloc(&m.dN, n * 36));
+        MK(alloc(&m.vec, (size_t)s.neq * 5));
+        MK(alloc(&m.part, std::max(patch_part_floats(s.n_nodes), (size_t)2 * ((s.neq + 255) / 256))));
+    }
+    patch_learn_grad(c, d_r, d_e, n_pairs);
+    if (grads) MK(cudaMemcpyAsync(grads, m.grads, kMlpParams * sizeof(float), cudaMemcpyDeviceToHost, c->stream));
+    if (loss) MK(cudaMemcpyAsync(loss, m.loss, sizeof(float), cudaMemcpyDeviceToHost, c->stream));
+    MK(cudaStreamSynchronize(c->stream));
+    MK(cudaGetLastError());
+    return IPFEM_OK;
+}
+
+ipfem_status ipfem_mlp_adam(ipfem_ctx *c, const float *grads, float lr)
 {
     ipfem_status st = need_mlp(c);
     if (st != IPFEM_OK) return st;
-    if (!d_X || !d_Y || rows < 1 || epochs < 0 || batch < 1 || batch > 65535 * 64)
-        return mfail(c, IPFEM_INVALID, "bad args");
-    const int64_t B = std::min<int64_t>(batch, rows);
-    float *Xb, *Yb, *H1, *H2, *O, *dO, *dH1, *dH2;
-    int64_t *d_idx;
-    MK(alloc(&Xb, (size_t)B * 32));
-    MK(alloc(&Yb, (size_t)B * 2));
-    MK(alloc(&H1, (size_t)B * 128));
-    MK(alloc(&H2, (size_t)B * 128));
-    MK(alloc(&O, (size_t)B * 2));
-    MK(alloc(&dO, (size_t)B * 2));
-    MK(alloc(&dH1, (size_t)B * 128));
-    MK(alloc(&dH2, (size_t)B * 128));
-    MK(alloc(&d_idx, (size_t)rows));
-    std::vector<int64_t> perm((size_t)rows);
-    for (int64_t i = 0; i < rows; i++) perm[i] = i;
-    std::mt19937_64 rng(seed);
-    for (int ep = 0; ep < epochs; ep++) {
-        std::shuffle(perm.begin(), perm.end(), rng);
-        MK(cudaMemcpyAsync(d_idx, perm.data(), perm.size() * sizeof(int64_t), cudaMemcpyHostToDevice, c->stream));
-        double ls = 0.0;
-        int nb = 0;
-        for (int64_t b0 = 0; b0 + B <= rows; b0 += B) {
-            k_gather_rows<<<(unsigned)((B * 32 + 255) / 256), 256, 0, c->stream>>>(B, 32, d_idx + b0, d_X, Xb);
-            k_gather_rows<<<(unsigned)((B * 2 + 255) / 256), 256, 0, c->stream>>>(B, 2, d_idx + b0, d_Y, Yb);
-            mlp_train_step(c, B, Xb, Yb, H1, H2, O, dO, dH1, dH2, true, lr);
-            c->launches += 20;
-            float l = 0.f;
-            MK(cudaMemcpyAsync(&l, c->mlp.loss, sizeof(float), cudaMemcpyDeviceToHost, c->stream));
-            MK(cudaStreamSynchronize(c->stream));
-            ls += l;
-            nb++;
-        }
-        if (loss_per_epoch) loss_per_epoch[ep] = nb ? (float)(ls / nb) : 0.f;
+    if (!(lr > 0.f) || !std::isfinite(lr)) return mfail(c, IPFEM_INVALID, "bad learning rate");
+    if (grads) {
+        for (int i = 0; i < kMlpParams; i++)
+            if (!std::isfinite(grads[i])) return mfail(c, IPFEM_NAN, "gradient is not finite");
+        MK(cudaMemcpyAsync(c->mlp.grads, grads, kMlpParams * sizeof(float), cudaMemcpyHostToDevice, c->stream));
     }
+    mlp_adam_step(c, lr);
     MK(cudaStreamSynchronize(c->stream));
-    cudaFree(Xb); cudaFree(Yb); cudaFree(H1); cudaFree(H2); cudaFree(O); cudaFree(dO); cudaFree(dH1); cudaFree(dH2);
-    cudaFree(d_idx);
     MK(cudaGetLastError());
     return IPFEM_OK;
 }

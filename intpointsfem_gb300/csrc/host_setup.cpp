@@ -80,6 +80,63 @@ static void parallel_for(int64_t n, F f)
     for (auto &x : th) x.join();
 }
 
+// SELL-32 layout of the block pattern.  With sorted rows the warps of a
+// slice run rows of one length, while every row keeps its own block order
+// and stays inside the reduction block that owns it in node order.
+std::string build_sell(const Setup &s, bool sorted, SellLayout &L)
+{
+    const int64_t ns = (s.n_nodes + 31) / 32;
+    std::vector<int32_t> deg(s.n_nodes);
+    for (int32_t i = 0; i < s.n_nodes; i++) deg[i] = (int32_t)(s.row_ptr[i + 1] - s.row_ptr[i]);
+    L.sell_node.resize(s.n_nodes);
+    for (int32_t i = 0; i < s.n_nodes; i++) L.sell_node[i] = i;
+    if (sorted)
+        for (int64_t w0 = 0; w0 < s.n_nodes; w0 += kRedBlock) {
+            const int64_t w1 = std::min<int64_t>(s.n_nodes, w0 + kRedBlock);
+            std::stable_sort(L.sell_node.begin() + w0, L.sell_node.begin() + w1,
+                             [&](int32_t a, int32_t b) { return deg[a] > deg[b]; });
+        }
+    L.rowlen.resize(s.n_nodes);
+    for (int32_t t = 0; t < s.n_nodes; t++) L.rowlen[t] = deg[L.sell_node[t]];
+    L.slice_base.assign((size_t)ns + 1, 0);
+    for (int64_t sl = 0; sl < ns; sl++) {
+        int32_t w = 0;
+        for (int64_t t = sl * 32; t < std::min<int64_t>(s.n_nodes, sl * 32 + 32); t++) w = std::max(w, L.rowlen[t]);
+        L.slice_base[sl + 1] = L.slice_base[sl] + 32 * (int64_t)w;
+    }
+    L.n_sell = L.slice_base[ns];
+    if (L.n_sell > INT32_MAX) return "matrix too large for 32-bit block slots";
+    L.sell_col.assign((size_t)L.n_sell, 0);
+    L.bsr_to_sell.resize((size_t)s.n_blocks);
+    L.diag_blk.resize(s.n_nodes);
+    for (int32_t t = 0; t < s.n_nodes; t++) {
+        const int32_t i = L.sell_node[t];
+        const int64_t base = L.slice_base[t / 32] + (t % 32);
+        for (int64_t j = 0; j < L.rowlen[t]; j++) {
+            const int64_t slot = base + j * 32;
+            const int32_t c = s.col[s.row_ptr[i] + j];
+            L.sell_col[slot] = c;
+            L.bsr_to_sell[s.row_ptr[i] + j] = slot;
+            if (c == i) L.diag_blk[i] = slot;
+        }
+        for (int64_t j = L.rowlen[t]; j < (int64_t)(L.slice_base[t / 32 + 1] - L.slice_base[t / 32]) / 32; j++)
+            L.sell_col[base + j * 32] = i;
+    }
+    L.el_blk.resize((size_t)s.n_el * 81);
+    parallel_for(s.n_el, [&](int64_t e) {
+        for (int a = 0; a < 9; a++) {
+            const int32_t r = s.dofs[(size_t)e * 18 + 2 * a] >> 1;
+            const int32_t *b0 = s.col.data() + s.row_ptr[r], *b1 = s.col.data() + s.row_ptr[r + 1];
+            for (int b = 0; b < 9; b++) {
+                const int32_t c = s.dofs[(size_t)e * 18 + 2 * b] >> 1;
+                const int64_t j = std::lower_bound(b0, b1, c) - b0;
+                L.el_blk[(size_t)e * 81 + a * 9 + b] = (int32_t)L.bsr_to_sell[s.row_ptr[r] + j];
+            }
+        }
+    });
+    return "";
+}
+
 std::string build_setup(const ipfem_mesh *m, const ipfem_material *mat, Setup &s)
 {
     if (!m || !mat) return "null mesh or material";
@@ -168,46 +225,9 @@ std::string build_setup(const ipfem_mesh *m, const ipfem_material *mat, Setup &s
         for (int32_t i = 0; i < s.n_nodes; i++)
             std::memcpy(s.col.data() + s.row_ptr[i], tmp.data() + cap[i], (size_t)deg[i] * sizeof(int32_t));
     }
-    // SELL-32
     {
-        const int64_t ns = (s.n_nodes + 31) / 32;
-        s.slice_base.assign((size_t)ns + 1, 0);
-        s.rowlen.resize(s.n_nodes);
-        for (int32_t i = 0; i < s.n_nodes; i++) s.rowlen[i] = (int32_t)(s.row_ptr[i + 1] - s.row_ptr[i]);
-        for (int64_t sl = 0; sl < ns; sl++) {
-            int32_t w = 0;
-            for (int64_t i = sl * 32; i < std::min<int64_t>(s.n_nodes, sl * 32 + 32); i++) w = std::max(w, s.rowlen[i]);
-            s.slice_base[sl + 1] = s.slice_base[sl] + 32 * (int64_t)w;
-        }
-        s.n_sell = s.slice_base[ns];
-        if (s.n_sell > INT32_MAX) return "matrix too large for 32-bit block slots";
-        s.sell_col.assign((size_t)s.n_sell, 0);
-        s.bsr_to_sell.resize((size_t)s.n_blocks);
-        s.diag_blk.resize(s.n_nodes);
-        for (int32_t i = 0; i < s.n_nodes; i++) {
-            const int64_t base = s.slice_base[i / 32] + (i % 32);
-            for (int64_t j = 0; j < s.rowlen[i]; j++) {
-                const int64_t slot = base + j * 32;
-                const int32_t c = s.col[s.row_ptr[i] + j];
-                s.sell_col[slot] = c;
-                s.bsr_to_sell[s.row_ptr[i] + j] = slot;
-                if (c == i) s.diag_blk[i] = slot;
-            }
-            for (int64_t j = s.rowlen[i]; j < (int64_t)(s.slice_base[i / 32 + 1] - s.slice_base[i / 32]) / 32; j++)
-                s.sell_col[base + j * 32] = i;
-        }
-        s.el_blk.resize((size_t)s.n_el * 81);
-        parallel_for(s.n_el, [&](int64_t e) {
-            for (int a = 0; a < 9; a++) {
-                const int32_t r = m->connects[9 * e + a];
-                const int32_t *b0 = s.col.data() + s.row_ptr[r], *b1 = s.col.data() + s.row_ptr[r + 1];
-                for (int b = 0; b < 9; b++) {
-                    const int32_t c = m->connects[9 * e + b];
-                    const int64_t j = std::lower_bound(b0, b1, c) - b0;
-                    s.el_blk[(size_t)e * 81 + a * 9 + b] = (int32_t)s.bsr_to_sell[s.row_ptr[r] + j];
-                }
-            }
-        });
+        const std::string e = build_sell(s, true, s.sell);
+        if (!e.empty()) return e;
     }
     // boundary conditions and loads
     s.fixed.assign((size_t)s.neq, 0);

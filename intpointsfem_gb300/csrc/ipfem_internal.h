@@ -30,10 +30,34 @@ struct CGScalarsT {
 constexpr int kStatusFallback = 9;   // flexible CG stagnated: the caller falls back to Jacobi-PCG
 typedef CGScalarsT<double> CGScalars;
 
+// SELL-32 layout of the nodal 2x2 block pattern: row position t of slice
+// t/32 holds node sell_node[t] (identity when the rows keep node order), its
+// block k sits in slot slice_base[t/32] + 32*k + t%32.
+struct SellLayout {
+    int64_t n_sell = 0;                  // padded block slots
+    std::vector<int64_t> slice_base;     // [n_slices+1], in blocks
+    std::vector<int32_t> sell_node;      // [n_nodes] node at each row position
+    std::vector<int32_t> rowlen;         // [n_nodes] blocks of the row at each row position
+    std::vector<int32_t> sell_col;       // [n_sell]
+    std::vector<int64_t> bsr_to_sell;    // [n_blocks]
+    std::vector<int32_t> el_blk;         // [n_el*81] slot of local node pair (m, n)
+    std::vector<int64_t> diag_blk;       // [n_nodes] slot of the diagonal block
+};
+
+// the same on the device
+struct SellDev {
+    int64_t n_sell = 0;
+    int64_t *slice_base = nullptr, *diag_blk = nullptr;
+    int32_t *sell_col = nullptr, *rowlen = nullptr, *sell_node = nullptr, *el_blk = nullptr;
+    bool sorted = false;
+};
+
 // buffers of the mixed-precision solve (FP32 tangent and CG)
 struct MixedBuffers {
     float *dphi = nullptr;        // [n_el*162]
-    float *K = nullptr;           // [n_sell*4]
+    float *K = nullptr;           // [sell.n_sell*4]
+    SellLayout sell;              // node-ordered rows (the FP32 SpMV is gather-bound)
+    SellDev dsell;
     float *dinv = nullptr;        // [neq]
     float *x = nullptr, *r = nullptr, *z = nullptr, *p = nullptr, *q = nullptr;
     float *part = nullptr;        // 2 partial arrays
@@ -58,14 +82,9 @@ struct Setup {
     int64_t n_blocks = 0;
     std::vector<int64_t> row_ptr;        // [n_nodes+1]
     std::vector<int32_t> col;            // [n_blocks]
-    // SELL-32 layout of the same blocks
-    int64_t n_sell = 0;                  // padded block slots
-    std::vector<int64_t> slice_base;     // [n_slices+1], in blocks
-    std::vector<int32_t> rowlen;         // [n_nodes]
-    std::vector<int32_t> sell_col;       // [n_sell]
-    std::vector<int64_t> bsr_to_sell;    // [n_blocks]
-    std::vector<int32_t> el_blk;         // [n_el*81] SELL slot of local node pair (m, n)
-    std::vector<int64_t> diag_blk;       // [n_nodes] SELL slot of the diagonal block
+    // SELL-32 layout of the same blocks for the FP64 tangent: rows sorted by
+    // length inside each kRedBlock window (the FP64 SpMV is FP64-pipe-bound)
+    SellLayout sell;
     std::vector<uint8_t> fixed;          // [neq]
     std::vector<double> f0, df;          // [neq]
     std::vector<double> mat;             // [5*n_el] SoA: c, sinphi, cosphi, tanphi, sinpsi
@@ -76,6 +95,9 @@ struct Setup {
 
 // builds the setup; returns an empty string or an error message
 std::string build_setup(const ipfem_mesh *mesh, const ipfem_material *mat, Setup &s);
+// SELL-32 layout of s's block pattern; sorted: rows by length inside each
+// kRedBlock-node window (stable, longest first)
+std::string build_sell(const Setup &s, bool sorted, SellLayout &L);
 int32_t greedy_coloring(int32_t n_el, int32_t n_nodes, const int32_t *connects, int32_t *el_color);
 void elastic_constants(double E, double nu, ElasticConstH &el);
 // message returned by ipfem_last_error(NULL) on the calling thread
@@ -91,20 +113,28 @@ struct NewtonState {
 };
 
 namespace ipfem {
-// learned preconditioner (per-node MLP) and its training state
+// learned preconditioner (per-node MLP -> symmetric 3x3-patch operator) and
+// its training state
 struct MlpBuffers {
-    float *params = nullptr;      // FP32 master: W1[32][128] b1[128] W2[128][128] b2[128] W3[128][2] b3[2]
+    float *params = nullptr;      // FP32 master: W1[32][128] b1[128] W2[128][128] b2[128] W3[128][36] b3[36]
     float *grads = nullptr, *m = nullptr, *v = nullptr;
-    void *w1t = nullptr, *w2t = nullptr;   // BF16 [128][32], [128][128] (n-major, k contiguous)
-    float *pfrac = nullptr, *pden = nullptr;
+    void *w1t = nullptr, *w2t = nullptr, *w3t = nullptr;   // BF16 [128][32], [128][128], [40][128] (n, k)
+    int32_t *slot = nullptr;      // [9][n_nodes] FP32-tangent slot of block (i, nbr(i, k)) or -1
+    float *X = nullptr;           // [n_nodes][32] features of the current tangent
+    float *O = nullptr;           // [n_nodes][36] network output
+    float *M = nullptr;           // [9][n_nodes][4] patch operator
     float *r_old = nullptr;       // flexible-CG previous residual
-    float *loss = nullptr;
+    float *loss = nullptr, *scal = nullptr;
+    // training scratch (allocated by the first gradient pass)
+    float *H1 = nullptr, *H2 = nullptr, *dH1 = nullptr, *dH2 = nullptr, *dN = nullptr, *part = nullptr;
+    float *vec = nullptr;         // 5 x neq
     int32_t gr = 0, gt = 0;       // structured node grid (gr x gt)
     int64_t adam_t = 0;
-    bool ready = false;
+    bool ready = false, op_valid = false;
 };
-constexpr int kMlpParams = 32 * 128 + 128 + 128 * 128 + 128 + 128 * 2 + 2;
-constexpr int kOffW1 = 0, kOffB1 = 4096, kOffW2 = 4224, kOffB2 = 20608, kOffW3 = 20736, kOffB3 = 20992;
+constexpr int kMlpParams = 32 * 128 + 128 + 128 * 128 + 128 + 128 * 36 + 36;
+constexpr int kOffW1 = 0, kOffB1 = 4096, kOffW2 = 4224, kOffB2 = 20608, kOffW3 = 20736, kOffB3 = 25344;
+static_assert(kOffB3 + 36 == kMlpParams, "parameter layout");
 }  // namespace ipfem
 
 struct ipfem_ctx {
@@ -118,8 +148,7 @@ struct ipfem_ctx {
     double *d_dphi = nullptr, *d_weight = nullptr, *d_mat = nullptr, *d_f0 = nullptr, *d_df = nullptr;
     int32_t *d_dofs = nullptr, *d_color_els = nullptr, *d_inc = nullptr;
     uint8_t *d_fixed = nullptr;
-    int64_t *d_slice_base = nullptr, *d_diag_blk = nullptr;
-    int32_t *d_sell_col = nullptr, *d_rowlen = nullptr, *d_el_blk = nullptr;
+    ipfem::SellDev dsell;                // FP64 tangent layout
     // device: tangent
     double *d_K = nullptr, *d_dinv = nullptr;
     // device: integration-point state {xx, xy, yy, zz} SoA
@@ -182,11 +211,12 @@ ipfem_status dot_host(ipfem_ctx *c, const double *a, const double *b, double *ou
 // learned preconditioner (k_mlp.cu)
 void mlp_pack_weights(ipfem_ctx *c);
 cudaError_t mlp_configure();
-void launch_plastic_fraction(ipfem_ctx *c);
-void launch_features(ipfem_ctx *c, const float *d_r, float *d_X, float *d_S);
-void launch_mlp_infer_rows(ipfem_ctx *c, int64_t rows, const float *d_X, float *d_O);
+void launch_patch_features(ipfem_ctx *c, float *d_X);
+void launch_patch_net(ipfem_ctx *c, int64_t rows, const float *d_X, float *d_O);
+void launch_patch_operator(ipfem_ctx *c);
 void launch_fcg_init(ipfem_ctx *c, const double *d_b, double scale, float rtol, int max_it);
 void launch_fcg_iteration(ipfem_ctx *c);
-void mlp_train_step(ipfem_ctx *c, int64_t rows, const float *X, const float *Y, float *H1, float *H2, float *O,
-                    float *dO, float *dH1, float *dH2, bool update, float lr);
+size_t patch_part_floats(int64_t n_nodes);
+void patch_learn_grad(ipfem_ctx *c, const float *d_r, const float *d_e, int P);
+void mlp_adam_step(ipfem_ctx *c, float lr);
 }  // namespace ipfem

@@ -304,32 +304,32 @@ void launch_color_reduce(ipfem_ctx *c, const double *d_fe, double lambda, int wi
 void launch_stiffness(ipfem_ctx *c)
 {
     const Setup &s = c->s;
-    cudaMemsetAsync(c->d_K, 0, (size_t)s.n_sell * 4 * sizeof(double), c->stream);
+    cudaMemsetAsync(c->d_K, 0, (size_t)c->dsell.n_sell * 4 * sizeof(double), c->stream);
     for (int col = 0; col < s.n_colors; col++) {
         const int32_t first = s.color_ptr[col], n = s.color_ptr[col + 1] - first;
         if (n == 0) continue;
         const unsigned grid = (unsigned)((n + kStiffWarps - 1) / kStiffWarps);
         k_stiffness<double><<<grid, kStiffWarps * 32, 0, c->stream>>>(n, c->d_color_els + first, s.n_ip, c->d_dphi,
-                                                                      c->d_dep, c->d_el_blk, c->d_K);
+                                                                      c->d_dep, c->dsell.el_blk, c->d_K);
     }
     const unsigned g2 = (unsigned)((s.n_nodes + 255) / 256);
-    k_jacobi<double><<<g2, 256, 0, c->stream>>>(s.n_nodes, c->d_diag_blk, c->d_K, c->d_fixed, c->d_dinv);
+    k_jacobi<double><<<g2, 256, 0, c->stream>>>(s.n_nodes, c->dsell.diag_blk, c->d_K, c->d_fixed, c->d_dinv);
 }
 
 void launch_stiffness32(ipfem_ctx *c)
 {
     const Setup &s = c->s;
     MixedBuffers &m = c->mx;
-    cudaMemsetAsync(m.K, 0, (size_t)s.n_sell * 4 * sizeof(float), c->stream);
+    cudaMemsetAsync(m.K, 0, (size_t)m.dsell.n_sell * 4 * sizeof(float), c->stream);
     for (int col = 0; col < s.n_colors; col++) {
         const int32_t first = s.color_ptr[col], n = s.color_ptr[col + 1] - first;
         if (n == 0) continue;
         const unsigned grid = (unsigned)((n + kStiffWarps - 1) / kStiffWarps);
         k_stiffness<float><<<grid, kStiffWarps * 32, 0, c->stream>>>(n, c->d_color_els + first, s.n_ip, m.dphi,
-                                                                     c->d_dep, c->d_el_blk, m.K);
+                                                                     c->d_dep, m.dsell.el_blk, m.K);
     }
     const unsigned g2 = (unsigned)((s.n_nodes + 255) / 256);
-    k_jacobi<float><<<g2, 256, 0, c->stream>>>(s.n_nodes, c->d_diag_blk, m.K, c->d_fixed, m.dinv);
+    k_jacobi<float><<<g2, 256, 0, c->stream>>>(s.n_nodes, m.dsell.diag_blk, m.K, c->d_fixed, m.dinv);
 }
 
 }  // namespace ipfem

@@ -1,17 +1,18 @@
-// Learned preconditioner: a per-node MLP (32 -> 128 -> 128 -> 2) applied inside
-// flexible CG on the FP32 tangent.  No counterpart in the reference.
+// Learned preconditioner: a per-node MLP (32 -> 128 -> 128 -> 36) that maps the
+// FP32 tangent around a node to one block row of a symmetric 3x3-patch
+// operator M, applied inside flexible CG.  No counterpart in the reference.
 //
-// Features of node i (structured node grid, neighbours outside the mesh read 0):
-//   f[0..17]  residual of the 3x3 node patch (x, y), row by row, divided by
-//             s_i = RMS of the patch residual
-//   f[18..21] |r| of the four second-ring axial neighbours / s_i
-//   f[22]     Dinv_x / Dinv_y of node i
-//   f[23..26] Dinv_x(i) / Dinv_x(neighbour) for the four axial neighbours
-//   f[27]     fraction of plastic integration points in the elements around i
-//   f[28..29] grid coordinates a/(gr-1), b/(gt-1)
-//   f[30..31] Dirichlet flags
-// Output: z_i = (f[8..9] + W3^T h2 + b3) * s_i * Dinv_i.  With W3 = 0 the
-// network is exactly Jacobi; training learns the correction on top of it.
+// Node i = b*gr + a of a structured node grid; patch position k = 3*(db+1) +
+// (da+1) for da, db in {-1, 0, 1} (k = 4 is the node itself, 8 - k the mirror).
+// With sigma = sqrt(Dinv) per dof (0 on Dirichlet dofs):
+//   features  X_i[4m + 2p + q] = K_ij[p][q] sigma_i[p] sigma_j[q] for the 8
+//             neighbours j (m-th non-centre position), 0 outside the grid or
+//             where the couplings are absent from the tangent;
+//   network   O_i[9][2][2] = W3^T relu(W2^T relu(W1^T X_i + b1) + b2) + b3;
+//   operator  Mhat_ik = (O_ik + O_{j,8-k}^T) / 2 + (k == 4 ? I : 0),
+//             M_ik[p][q] = sigma_i[p] Mhat_ik[p][q] sigma_j[q],
+// so M is symmetric by construction and O = 0 gives Jacobi exactly.  The
+// network runs once per tangent; each CG iteration applies M, a 9-block stencil.
 //
 // GEMMs run on the tensor cores in BF16 (operands rounded to BF16 in shared
 // memory) with FP32 accumulation (mma.m16n8k16).
@@ -29,6 +30,11 @@ __device__ __forceinline__ uint32_t pack_bf16(float lo, float hi)
     return *reinterpret_cast<uint32_t *>(&v);
 }
 
+__device__ __forceinline__ float bf16r(float x)
+{
+    return __bfloat162float(__float2bfloat16_rn(x));
+}
+
 __device__ __forceinline__ void mma_bf16(float (&d)[4], const uint32_t (&a)[4], const uint32_t (&b)[2])
 {
     asm volatile(
@@ -39,20 +45,24 @@ __device__ __forceinline__ void mma_bf16(float (&d)[4], const uint32_t (&a)[4], 
 }
 
 // ------------------------------------------------------------------ GEMM
-// C[M][N] = alpha * op(A)[M][K] op(B)[K][N] (+ C if beta).  A and B are FP32 in
-// global memory and rounded to BF16 when staged; FP32 accumulation.
+// C[M][N] = op(A)[M][K] op(B)[K][N].  A and B are FP32 in global memory and
+// rounded to BF16 when staged; FP32 accumulation.
 //   transA = 0: A[m][k] = A[m*lda + k];   transA = 1: A[m][k] = A[k*lda + m]
 //   transB = 0: B[k][n] = B[k*ldb + n];   transB = 1: B[k][n] = B[n*ldb + k]
 // 64x64 tile per CTA, K step 32, 4 warps as 2 x 2, each warp 32 x 32.
+// Split K: CTA z covers k in [z*kchunk, (z+1)*kchunk) and writes its partial
+// product to C + z*M*ldc (kchunk a multiple of 32; one split writes C itself).
 constexpr int GT = 64, GK = 32, GPAD = 8;
 
 __global__ void __launch_bounds__(128) k_gemm_bf16(int M, int N, int K, const float *__restrict__ A, int lda, int transA,
                                                    const float *__restrict__ B, int ldb, int transB,
-                                                   float *__restrict__ C, int ldc, float alpha, int beta)
+                                                   float *__restrict__ C, int ldc, int kchunk)
 {
     __shared__ __align__(16) __nv_bfloat16 sA[GT][GK + GPAD];   // [m][k]
     __shared__ __align__(16) __nv_bfloat16 sB[GT][GK + GPAD];   // [n][k]
     const int m0 = blockIdx.y * GT, n0 = blockIdx.x * GT;
+    const int kb = blockIdx.z * kchunk, ke = min(K, kb + kchunk);
+    C += (size_t)blockIdx.z * M * ldc;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int wm = (warp >> 1) * 32, wn = (warp & 1) * 32;
     const int g = lane >> 2, t = lane & 3;
@@ -63,13 +73,13 @@ __global__ void __launch_bounds__(128) k_gemm_bf16(int M, int N, int K, const fl
         for (int j = 0; j < 4; j++)
 #pragma unroll
             for (int r = 0; r < 4; r++) acc[i][j][r] = 0.f;
-    for (int k0 = 0; k0 < K; k0 += GK) {
+    for (int k0 = kb; k0 < ke; k0 += GK) {
         for (int e = threadIdx.x; e < GT * GK; e += 128) {
             int mm, kk;
             if (transA) { kk = e / GT; mm = e % GT; } else { mm = e / GK; kk = e % GK; }
             const int gm = m0 + mm, gk = k0 + kk;
             float v = 0.f;
-            if (gm < M && gk < K) v = transA ? A[(size_t)gk * lda + gm] : A[(size_t)gm * lda + gk];
+            if (gm < M && gk < ke) v = transA ? A[(size_t)gk * lda + gm] : A[(size_t)gm * lda + gk];
             sA[mm][kk] = __float2bfloat16_rn(v);
         }
         for (int e = threadIdx.x; e < GT * GK; e += 128) {
@@ -77,7 +87,7 @@ __global__ void __launch_bounds__(128) k_gemm_bf16(int M, int N, int K, const fl
             if (transB) { nn = e / GK; kk = e % GK; } else { kk = e / GT; nn = e % GT; }
             const int gn = n0 + nn, gk = k0 + kk;
             float v = 0.f;
-            if (gn < N && gk < K) v = transB ? B[(size_t)gn * ldb + gk] : B[(size_t)gk * ldb + gn];
+            if (gn < N && gk < ke) v = transB ? B[(size_t)gn * ldb + gk] : B[(size_t)gk * ldb + gn];
             sB[nn][kk] = __float2bfloat16_rn(v);
         }
         __syncthreads();
@@ -113,21 +123,27 @@ __global__ void __launch_bounds__(128) k_gemm_bf16(int M, int N, int K, const fl
             for (int r = 0; r < 4; r++) {
                 const int gm = m0 + wm + 16 * i + g + ((r >> 1) << 3);
                 const int gn = n0 + wn + 8 * j + 2 * t + (r & 1);
-                if (gm < M && gn < N) {
-                    float v = alpha * acc[i][j][r];
-                    if (beta) v += C[(size_t)gm * ldc + gn];
-                    C[(size_t)gm * ldc + gn] = v;
-                }
+                if (gm < M && gn < N) C[(size_t)gm * ldc + gn] = acc[i][j][r];
             }
 }
 
+// out[i] = sum_z part[z*n + i] (split-K partials, in z order)
+__global__ void k_sum_splits(int64_t n, int splits, const float *__restrict__ part, float *__restrict__ out)
+{
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float s = 0.f;
+    for (int z = 0; z < splits; z++) s += part[(size_t)z * n + i];
+    out[i] = s;
+}
+
 // ---------------------------------------------------- elementwise helpers
-// H = relu(H + b) (b broadcast over rows of width n)
-__global__ void k_bias_relu(int64_t rows, int n, float *__restrict__ H, const float *__restrict__ b, int relu)
+// H = act(H + b) (b broadcast over rows of width n)
+__global__ void k_bias_act(int64_t rows, int n, float *__restrict__ H, const float *__restrict__ b, int relu)
 {
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= rows * n) return;
-    float v = H[i] + b[i % n];
+    const float v = H[i] + b[i % n];
     H[i] = relu ? fmaxf(v, 0.f) : v;
 }
 
@@ -138,52 +154,25 @@ __global__ void k_relu_mask(int64_t count, float *__restrict__ D, const float *_
     if (i < count && !(H[i] > 0.f)) D[i] = 0.f;
 }
 
-// Output layer on CUDA cores: O[r][j] = X[r][8+j] + sum_n H2[r][n] W3[n][j] + b3[j]
-__global__ void k_out_layer(int64_t rows, const float *__restrict__ X, const float *__restrict__ H2,
-                            const float *__restrict__ W3, const float *__restrict__ b3, float *__restrict__ O)
+// column sums of D[rows][n], level 1: CTA (x, y) sums columns 32x..32x+31 over
+// rows y*chunk .. (y+1)*chunk-1 into part[y][n]
+constexpr int kColChunk = 4096;
+__global__ void __launch_bounds__(256) k_colsum_part(int64_t rows, int n, const float *__restrict__ D,
+                                                     float *__restrict__ part)
 {
-    const int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (r >= rows) return;
-    float o0 = 0.f, o1 = 0.f;
-    for (int n = 0; n < 128; n++) {
-        const float h = __bfloat162float(__float2bfloat16_rn(H2[r * 128 + n]));
-        o0 = fmaf(h, __bfloat162float(__float2bfloat16_rn(W3[2 * n])), o0);
-        o1 = fmaf(h, __bfloat162float(__float2bfloat16_rn(W3[2 * n + 1])), o1);
+    __shared__ float s[8][33];
+    const int c = blockIdx.x * 32 + (threadIdx.x & 31), w = threadIdx.x >> 5;
+    const int64_t r0 = (int64_t)blockIdx.y * kColChunk, r1 = min(rows, r0 + kColChunk);
+    float a = 0.f;
+    if (c < n)
+        for (int64_t r = r0 + w; r < r1; r += 8) a += D[r * n + c];
+    s[w][threadIdx.x & 31] = a;
+    __syncthreads();
+    if (w == 0 && c < n) {
+        float t = 0.f;
+        for (int k = 0; k < 8; k++) t += s[k][threadIdx.x];
+        part[(size_t)blockIdx.y * n + c] = t;
     }
-    O[2 * r] = X[r * 32 + 8] + o0 + b3[0];
-    O[2 * r + 1] = X[r * 32 + 9] + o1 + b3[1];
-}
-
-// loss = sum (O - Y)^2 / rows; dO = 2 (O - Y) / rows;  dH2 = dO W3^T (masked later)
-__global__ void k_out_backward(int64_t rows, const float *__restrict__ O, const float *__restrict__ Y,
-                               const float *__restrict__ W3, float *__restrict__ dO, float *__restrict__ dH2,
-                               float *__restrict__ loss_part)
-{
-    const int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    float l = 0.f;
-    if (r < rows) {
-        const float e0 = O[2 * r] - Y[2 * r], e1 = O[2 * r + 1] - Y[2 * r + 1];
-        l = e0 * e0 + e1 * e1;
-        const float s = 2.f / (float)rows;
-        const float d0 = s * e0, d1 = s * e1;
-        dO[2 * r] = d0;
-        dO[2 * r + 1] = d1;
-        for (int n = 0; n < 128; n++)
-            dH2[r * 128 + n] = d0 * __bfloat162float(__float2bfloat16_rn(W3[2 * n])) +
-                               d1 * __bfloat162float(__float2bfloat16_rn(W3[2 * n + 1]));
-    }
-    for (int off = 16; off; off >>= 1) l += __shfl_down_sync(FULLM, l, off);
-    if ((threadIdx.x & 31) == 0) atomicAdd(loss_part, l / (float)rows);
-}
-
-// column sums of D[rows][n] into g[n] (bias gradients); one thread per column
-__global__ void k_colsum(int64_t rows, int n, const float *__restrict__ D, float *__restrict__ g)
-{
-    const int c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= n) return;
-    float s = 0.f;
-    for (int64_t r = 0; r < rows; r++) s += D[r * n + c];
-    g[c] = s;
 }
 
 // Adam on the FP32 parameter vector
@@ -200,136 +189,133 @@ __global__ void k_adam(int n, float *__restrict__ p, const float *__restrict__ g
     p[i] -= lr * (mi / c1) / (sqrtf(vi / c2) + eps);
 }
 
-// ------------------------------------------------------------ features
+// grads *= s
+__global__ void k_scale(int n, float *__restrict__ g, float s)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) g[i] *= s;
+}
+
+// ------------------------------------------------------------ node grid
 struct GridInfo {
     int32_t gr, gt;
 };
 
-__device__ __forceinline__ float2 rd_r(const float2 *__restrict__ r, GridInfo G, int a, int b)
+// neighbour of node i at patch position k, or -1 outside the grid
+__device__ __forceinline__ int32_t patch_nbr(int32_t i, int k, GridInfo G)
 {
-    if (a < 0 || b < 0 || a >= G.gr || b >= G.gt) return make_float2(0.f, 0.f);
-    return r[(int64_t)b * G.gr + a];
+    const int a = i % G.gr + k % 3 - 1, b = i / G.gr + k / 3 - 1;
+    if (a < 0 || b < 0 || a >= G.gr || b >= G.gt) return -1;
+    return b * G.gr + a;
 }
 
-__device__ __forceinline__ float2 rd_d(const float2 *__restrict__ d, GridInfo G, int a, int b, bool &ok)
+__device__ __forceinline__ float2 sqrt2(float2 d)
 {
-    ok = !(a < 0 || b < 0 || a >= G.gr || b >= G.gt);
-    if (!ok) return make_float2(0.f, 0.f);
-    return d[(int64_t)b * G.gr + a];
+    return make_float2(sqrtf(d.x), sqrtf(d.y));
 }
 
-__device__ __forceinline__ float safe_ratio(float a, float b)
+// features X[n][32] from the FP32 tangent: scaled couplings to the 8
+// neighbours (slot[k][n] = SELL slot of block (i, nbr(i, k)) or -1)
+__global__ void __launch_bounds__(256) k_patch_features(int32_t n, GridInfo G, const float4 *__restrict__ K,
+                                                        const int32_t *__restrict__ slot,
+                                                        const float2 *__restrict__ dinv, float *__restrict__ X)
 {
-    return (a > 0.f && b > 0.f) ? a / b : 1.f;
-}
-
-// features of node i into f[32]; returns the scale s_i
-__device__ __forceinline__ float node_features(int32_t i, GridInfo G, const float2 *__restrict__ r,
-                                               const float2 *__restrict__ dinv, const float *__restrict__ pfrac,
-                                               const uint8_t *__restrict__ fixed, float *f)
-{
-    const int a = i % G.gr, b = i / G.gr;
-    float ss = 0.f;
-    int k = 0;
+    const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float2 si = sqrt2(dinv[i]);
+    float4 *xo = reinterpret_cast<float4 *>(X + (int64_t)i * 32);
+    int m = 0;
 #pragma unroll
-    for (int db = -1; db <= 1; db++)
-#pragma unroll
-        for (int da = -1; da <= 1; da++) {
-            const float2 v = rd_r(r, G, a + da, b + db);
-            f[k++] = v.x;
-            f[k++] = v.y;
-            ss = fmaf(v.x, v.x, fmaf(v.y, v.y, ss));
+    for (int k = 0; k < 9; k++) {
+        if (k == 4) continue;
+        const int32_t s = slot[(int64_t)k * n + i];
+        float4 f = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (s >= 0) {
+            const float4 blk = K[s];
+            const float2 sj = sqrt2(dinv[patch_nbr(i, k, G)]);
+            f = make_float4(blk.x * si.x * sj.x, blk.y * si.x * sj.y, blk.z * si.y * sj.x, blk.w * si.y * sj.y);
         }
-    const float s = sqrtf(ss / 9.f) + 1e-30f;
-    const float inv = 1.f / s;
-#pragma unroll
-    for (int j = 0; j < 18; j++) f[j] *= inv;
-    const int ra[4] = {-2, 2, 0, 0}, rb[4] = {0, 0, -2, 2};
-#pragma unroll
-    for (int j = 0; j < 4; j++) {
-        const float2 v = rd_r(r, G, a + ra[j], b + rb[j]);
-        f[18 + j] = sqrtf(v.x * v.x + v.y * v.y) * inv;
-    }
-    bool ok;
-    const float2 d0 = rd_d(dinv, G, a, b, ok);
-    f[22] = safe_ratio(d0.x, d0.y);
-    const int na[4] = {-1, 1, 0, 0}, nb[4] = {0, 0, -1, 1};
-#pragma unroll
-    for (int j = 0; j < 4; j++) {
-        const float2 dn = rd_d(dinv, G, a + na[j], b + nb[j], ok);
-        f[23 + j] = ok ? safe_ratio(d0.x, dn.x) : 1.f;
-    }
-    f[27] = pfrac[i];
-    f[28] = G.gr > 1 ? (float)a / (float)(G.gr - 1) : 0.f;
-    f[29] = G.gt > 1 ? (float)b / (float)(G.gt - 1) : 0.f;
-    f[30] = fixed[2 * (int64_t)i] ? 1.f : 0.f;
-    f[31] = fixed[2 * (int64_t)i + 1] ? 1.f : 0.f;
-    return s;
-}
-
-// features (rows of 32) and scales of all nodes, from an FP32 residual
-__global__ void k_features(int32_t n_nodes, GridInfo G, const float *__restrict__ r, const float *__restrict__ dinv,
-                           const float *__restrict__ pfrac, const uint8_t *__restrict__ fixed,
-                           float *__restrict__ X, float *__restrict__ S)
-{
-    const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n_nodes) return;
-    float f[32];
-    const float s = node_features(i, G, reinterpret_cast<const float2 *>(r), reinterpret_cast<const float2 *>(dinv),
-                                  pfrac, fixed, f);
-#pragma unroll
-    for (int j = 0; j < 32; j++) X[(int64_t)i * 32 + j] = f[j];
-    S[i] = s;
-}
-
-// fraction of plastic points (committed m_type != 0) of the elements around each node
-__global__ void k_plastic_fraction(int32_t n_el, const int32_t *__restrict__ dofs, const int8_t *__restrict__ mtype,
-                                   float *__restrict__ num, float *__restrict__ den)
-{
-    const int32_t e = blockIdx.x * blockDim.x + threadIdx.x;
-    if (e >= n_el) return;
-    float p = 0.f;
-    for (int q = 0; q < 9; q++) p += mtype[(int64_t)e * 9 + q] != 0 ? 1.f : 0.f;
-    for (int n = 0; n < 9; n++) {
-        const int32_t node = dofs[(int64_t)e * 18 + 2 * n] >> 1;
-        atomicAdd(&num[node], p);
-        atomicAdd(&den[node], 9.f);
+        xo[m++] = f;
     }
 }
 
-__global__ void k_ratio(int32_t n, float *__restrict__ num, const float *__restrict__ den)
-{
-    const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) num[i] = den[i] > 0.f ? num[i] / den[i] : 0.f;
-}
+// ------------------------------------------------ fused network (inference)
+// One CTA = 128 nodes, 8 warps; warp w owns rows 16w..16w+15 through all three
+// layers (A operands are the warp's own rows, so the layers need only
+// __syncwarp).  Weights are staged once per persistent CTA.
+constexpr int PT = 128;          // nodes per tile
+constexpr int NOUT = 36, NOUTP = 40;
 
-// ------------------------------------------------ fused preconditioner
-// One CTA = 128 nodes, 8 warps; warp w owns rows 16w..16w+15.  Features ->
-// smem (BF16), layer 1 and 2 on the tensor cores (FP32 accumulators in
-// registers), layer 3 from the layer-2 accumulator fragments with a 4-lane
-// shuffle reduction, then z = o * s * Dinv.  Also produces the partial dots
-// r.z and r_old.z for the flexible-CG beta.
-struct MlpDev {
+struct NetDev {
     const __nv_bfloat16 *w1t;   // [128][32]  (n, k)
     const __nv_bfloat16 *w2t;   // [128][128] (n, k)
-    const float *b1, *b2;       // [128]
-    const float *w3;            // [128][2]
-    const float *b3;            // [2]
+    const __nv_bfloat16 *w3t;   // [40][128]  (n, k), rows 36..39 zero
+    const float *b1, *b2, *b3;  // [128], [128], [36]
 };
 
-constexpr int PT = 128;          // nodes per CTA
-
-struct __align__(16) PrecSmem {
+struct __align__(16) NetSmem {
     __nv_bfloat16 x[PT][32 + 8];
     __nv_bfloat16 h[PT][128 + 8];
     __nv_bfloat16 w1[128][32 + 8];
     __nv_bfloat16 w2[128][128 + 8];
-    float b1[128], b2[128], w3[128][2], b3[2];
-    float own[PT][2];
-    float sc[PT];
+    __nv_bfloat16 w3[NOUTP][128 + 8];
+    float b1[128], b2[128], b3[NOUTP];
 };
 
-__device__ void mlp_tile(PrecSmem &S, int warp, int lane, float (&o)[2][2])
+__device__ void net_load_weights(NetSmem &S, const NetDev &W)
+{
+    for (int e = threadIdx.x; e < 128 * 32; e += blockDim.x) S.w1[e / 32][e % 32] = W.w1t[e];
+    for (int e = threadIdx.x; e < 128 * 128; e += blockDim.x) S.w2[e / 128][e % 128] = W.w2t[e];
+    for (int e = threadIdx.x; e < NOUTP * 128; e += blockDim.x) S.w3[e / 128][e % 128] = W.w3t[e];
+    for (int e = threadIdx.x; e < 128; e += blockDim.x) {
+        S.b1[e] = W.b1[e];
+        S.b2[e] = W.b2[e];
+    }
+    for (int e = threadIdx.x; e < NOUTP; e += blockDim.x) S.b3[e] = e < NOUT ? W.b3[e] : 0.f;
+}
+
+// acc[j][r]: rows r0 = 16*warp + g (r = 0, 1) and r0 + 8 (r = 2, 3), columns
+// 8j + 2t + (r & 1) of [16 x K] x [K x 128] from smem operands
+template <int K, int LDA>
+__device__ __forceinline__ void warp_gemm128(const __nv_bfloat16 (*A)[LDA], const __nv_bfloat16 (*B)[LDA], int r0,
+                                             int g, int t, float (&acc)[16][4])
+{
+#pragma unroll
+    for (int ks = 0; ks < K; ks += 16) {
+        uint32_t af[4];
+        af[0] = *reinterpret_cast<const uint32_t *>(&A[r0][ks + 2 * t]);
+        af[1] = *reinterpret_cast<const uint32_t *>(&A[r0 + 8][ks + 2 * t]);
+        af[2] = *reinterpret_cast<const uint32_t *>(&A[r0][ks + 8 + 2 * t]);
+        af[3] = *reinterpret_cast<const uint32_t *>(&A[r0 + 8][ks + 8 + 2 * t]);
+#pragma unroll
+        for (int j = 0; j < 16; j++) {
+            uint32_t bf[2];
+            bf[0] = *reinterpret_cast<const uint32_t *>(&B[8 * j + g][ks + 2 * t]);
+            bf[1] = *reinterpret_cast<const uint32_t *>(&B[8 * j + g][ks + 8 + 2 * t]);
+            mma_bf16(acc[j], af, bf);
+        }
+    }
+}
+
+// bias + relu of the accumulators into the warp's rows of S.h (BF16)
+__device__ __forceinline__ void warp_store_hidden(NetSmem &S, const float *b, int r0, int t, float (&acc)[16][4])
+{
+    __syncwarp();
+#pragma unroll
+    for (int j = 0; j < 16; j++) {
+        const int c = 8 * j + 2 * t;
+        *reinterpret_cast<uint32_t *>(&S.h[r0][c]) =
+            pack_bf16(fmaxf(acc[j][0] + b[c], 0.f), fmaxf(acc[j][1] + b[c + 1], 0.f));
+        *reinterpret_cast<uint32_t *>(&S.h[r0 + 8][c]) =
+            pack_bf16(fmaxf(acc[j][2] + b[c], 0.f), fmaxf(acc[j][3] + b[c + 1], 0.f));
+#pragma unroll
+        for (int r = 0; r < 4; r++) acc[j][r] = 0.f;
+    }
+    __syncwarp();
+}
+
+// network of the warp's 16 rows of S.x; out[j][r] as acc above for 40 columns
+__device__ void net_tile(NetSmem &S, int warp, int lane, float (&out)[5][4])
 {
     const int g = lane >> 2, t = lane & 3;
     const int r0 = 16 * warp + g;
@@ -338,35 +324,14 @@ __device__ void mlp_tile(PrecSmem &S, int warp, int lane, float (&o)[2][2])
     for (int j = 0; j < 16; j++)
 #pragma unroll
         for (int r = 0; r < 4; r++) acc[j][r] = 0.f;
-    // layer 1: [16 x 32] x [32 x 128]
+    warp_gemm128<32, 40>(S.x, S.w1, r0, g, t, acc);
+    warp_store_hidden(S, S.b1, r0, t, acc);
+    warp_gemm128<128, 136>(S.h, S.w2, r0, g, t, acc);
+    warp_store_hidden(S, S.b2, r0, t, acc);
 #pragma unroll
-    for (int ks = 0; ks < 32; ks += 16) {
-        uint32_t af[4];
-        af[0] = *reinterpret_cast<const uint32_t *>(&S.x[r0][ks + 2 * t]);
-        af[1] = *reinterpret_cast<const uint32_t *>(&S.x[r0 + 8][ks + 2 * t]);
-        af[2] = *reinterpret_cast<const uint32_t *>(&S.x[r0][ks + 8 + 2 * t]);
-        af[3] = *reinterpret_cast<const uint32_t *>(&S.x[r0 + 8][ks + 8 + 2 * t]);
+    for (int j = 0; j < 5; j++)
 #pragma unroll
-        for (int j = 0; j < 16; j++) {
-            uint32_t bf[2];
-            bf[0] = *reinterpret_cast<const uint32_t *>(&S.w1[8 * j + g][ks + 2 * t]);
-            bf[1] = *reinterpret_cast<const uint32_t *>(&S.w1[8 * j + g][ks + 8 + 2 * t]);
-            mma_bf16(acc[j], af, bf);
-        }
-    }
-    // bias + relu -> h (BF16), this warp's 16 rows only
-#pragma unroll
-    for (int j = 0; j < 16; j++) {
-        const int c = 8 * j + 2 * t;
-        const float v0 = fmaxf(acc[j][0] + S.b1[c], 0.f), v1 = fmaxf(acc[j][1] + S.b1[c + 1], 0.f);
-        const float v2 = fmaxf(acc[j][2] + S.b1[c], 0.f), v3 = fmaxf(acc[j][3] + S.b1[c + 1], 0.f);
-        *reinterpret_cast<uint32_t *>(&S.h[r0][c]) = pack_bf16(v0, v1);
-        *reinterpret_cast<uint32_t *>(&S.h[r0 + 8][c]) = pack_bf16(v2, v3);
-#pragma unroll
-        for (int r = 0; r < 4; r++) acc[j][r] = 0.f;
-    }
-    __syncwarp();
-    // layer 2: [16 x 128] x [128 x 128]
+        for (int r = 0; r < 4; r++) out[j][r] = 0.f;
 #pragma unroll
     for (int ks = 0; ks < 128; ks += 16) {
         uint32_t af[4];
@@ -375,89 +340,111 @@ __device__ void mlp_tile(PrecSmem &S, int warp, int lane, float (&o)[2][2])
         af[2] = *reinterpret_cast<const uint32_t *>(&S.h[r0][ks + 8 + 2 * t]);
         af[3] = *reinterpret_cast<const uint32_t *>(&S.h[r0 + 8][ks + 8 + 2 * t]);
 #pragma unroll
-        for (int j = 0; j < 16; j++) {
+        for (int j = 0; j < 5; j++) {
             uint32_t bf[2];
-            bf[0] = *reinterpret_cast<const uint32_t *>(&S.w2[8 * j + g][ks + 2 * t]);
-            bf[1] = *reinterpret_cast<const uint32_t *>(&S.w2[8 * j + g][ks + 8 + 2 * t]);
-            mma_bf16(acc[j], af, bf);
+            bf[0] = *reinterpret_cast<const uint32_t *>(&S.w3[8 * j + g][ks + 2 * t]);
+            bf[1] = *reinterpret_cast<const uint32_t *>(&S.w3[8 * j + g][ks + 8 + 2 * t]);
+            mma_bf16(out[j], af, bf);
         }
     }
-    // layer 3 from the fragments: rows r0 (regs 0,1) and r0+8 (regs 2,3)
-    float p00 = 0.f, p01 = 0.f, p10 = 0.f, p11 = 0.f;
 #pragma unroll
-    for (int j = 0; j < 16; j++) {
+    for (int j = 0; j < 5; j++) {
         const int c = 8 * j + 2 * t;
-        const float h0 = __bfloat162float(__float2bfloat16_rn(fmaxf(acc[j][0] + S.b2[c], 0.f)));
-        const float h1 = __bfloat162float(__float2bfloat16_rn(fmaxf(acc[j][1] + S.b2[c + 1], 0.f)));
-        const float h2 = __bfloat162float(__float2bfloat16_rn(fmaxf(acc[j][2] + S.b2[c], 0.f)));
-        const float h3 = __bfloat162float(__float2bfloat16_rn(fmaxf(acc[j][3] + S.b2[c + 1], 0.f)));
-        p00 = fmaf(h0, S.w3[c][0], fmaf(h1, S.w3[c + 1][0], p00));
-        p01 = fmaf(h0, S.w3[c][1], fmaf(h1, S.w3[c + 1][1], p01));
-        p10 = fmaf(h2, S.w3[c][0], fmaf(h3, S.w3[c + 1][0], p10));
-        p11 = fmaf(h2, S.w3[c][1], fmaf(h3, S.w3[c + 1][1], p11));
+        out[j][0] += S.b3[c];
+        out[j][1] += S.b3[c + 1];
+        out[j][2] += S.b3[c];
+        out[j][3] += S.b3[c + 1];
     }
-#pragma unroll
-    for (int off = 1; off <= 2; off <<= 1) {
-        p00 += __shfl_xor_sync(FULLM, p00, off);
-        p01 += __shfl_xor_sync(FULLM, p01, off);
-        p10 += __shfl_xor_sync(FULLM, p10, off);
-        p11 += __shfl_xor_sync(FULLM, p11, off);
-    }
-    o[0][0] = p00 + S.b3[0];
-    o[0][1] = p01 + S.b3[1];
-    o[1][0] = p10 + S.b3[0];
-    o[1][1] = p11 + S.b3[1];
 }
 
-__device__ void load_weights(PrecSmem &S, const MlpDev &W)
-{
-    for (int e = threadIdx.x; e < 128 * 32; e += blockDim.x) S.w1[e / 32][e % 32] = W.w1t[e];
-    for (int e = threadIdx.x; e < 128 * 128; e += blockDim.x) S.w2[e / 128][e % 128] = W.w2t[e];
-    for (int e = threadIdx.x; e < 128; e += blockDim.x) {
-        S.b1[e] = W.b1[e];
-        S.b2[e] = W.b2[e];
-        S.w3[e][0] = __bfloat162float(__float2bfloat16_rn(W.w3[2 * e]));
-        S.w3[e][1] = __bfloat162float(__float2bfloat16_rn(W.w3[2 * e + 1]));
-    }
-    if (threadIdx.x < 2) S.b3[threadIdx.x] = W.b3[threadIdx.x];
-}
-
-// inference on given feature rows (testing / training evaluation): O[row][2]
-__global__ void __launch_bounds__(256) k_mlp_infer_rows(int64_t rows, const float *__restrict__ X, MlpDev W,
-                                                        float *__restrict__ O)
+// O[rows][36] = network(X[rows][32]); persistent CTAs over 128-row tiles
+__global__ void __launch_bounds__(256) k_patch_net(int64_t rows, const float *__restrict__ X, NetDev W,
+                                                   float *__restrict__ O)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    PrecSmem &S = *reinterpret_cast<PrecSmem *>(smem_raw);
-    load_weights(S, W);
-    const int64_t base = (int64_t)blockIdx.x * PT;
-    for (int e = threadIdx.x; e < PT * 32; e += blockDim.x) {
-        const int row = e / 32, col = e % 32;
-        const float v = (base + row < rows) ? X[(base + row) * 32 + col] : 0.f;
-        S.x[row][col] = __float2bfloat16_rn(v);
-        if (col == 8 || col == 9) S.own[row][col - 8] = v;
-    }
-    __syncthreads();
+    NetSmem &S = *reinterpret_cast<NetSmem *>(smem_raw);
+    net_load_weights(S, W);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    float o[2][2];
-    mlp_tile(S, warp, lane, o);
-    if ((lane & 3) == 0) {
+    const int g = lane >> 2, t = lane & 3;
+    const int64_t n_tiles = (rows + PT - 1) / PT;
+    for (int64_t tile = blockIdx.x; tile < n_tiles; tile += gridDim.x) {
+        const int64_t base = tile * PT;
+        __syncthreads();   // weights staged / previous tile done with S.x
+        for (int e = threadIdx.x; e < PT * 16; e += blockDim.x) {
+            const int row = e / 16, c2 = 2 * (e % 16);
+            float2 v = make_float2(0.f, 0.f);
+            if (base + row < rows) v = *reinterpret_cast<const float2 *>(X + (base + row) * 32 + c2);
+            *reinterpret_cast<uint32_t *>(&S.x[row][c2]) = pack_bf16(v.x, v.y);
+        }
+        __syncthreads();
+        float out[5][4];
+        net_tile(S, warp, lane, out);
 #pragma unroll
         for (int h = 0; h < 2; h++) {
-            const int row = 16 * warp + (lane >> 2) + 8 * h;
-            if (base + row < rows) {
-                O[2 * (base + row)] = S.own[row][0] + o[h][0];
-                O[2 * (base + row) + 1] = S.own[row][1] + o[h][1];
+            const int64_t row = base + 16 * warp + g + 8 * h;
+            if (row >= rows) continue;
+#pragma unroll
+            for (int j = 0; j < 5; j++) {
+                const int c = 8 * j + 2 * t;
+                if (c < NOUT)
+                    *reinterpret_cast<float2 *>(O + row * NOUT + c) = make_float2(out[j][2 * h], out[j][2 * h + 1]);
             }
         }
     }
 }
 
-}  // namespace ipfem
+// M[k][i] (float4, row-major 2x2) from the network output O[n][36]
+__global__ void __launch_bounds__(256) k_patch_build(int32_t n, GridInfo G, const float *__restrict__ O,
+                                                     const float2 *__restrict__ dinv, float4 *__restrict__ M)
+{
+    const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float2 si = sqrt2(dinv[i]);
+    const float *oi = O + (int64_t)i * NOUT;
+#pragma unroll
+    for (int k = 0; k < 9; k++) {
+        const int32_t j = patch_nbr(i, k, G);
+        float4 mk = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (j >= 0) {
+            const float *oj = O + (int64_t)j * NOUT + 4 * (8 - k);
+            const float e = (k == 4) ? 1.f : 0.f;
+            const float m00 = 0.5f * (oi[4 * k + 0] + oj[0]) + e;
+            const float m01 = 0.5f * (oi[4 * k + 1] + oj[2]);
+            const float m10 = 0.5f * (oi[4 * k + 2] + oj[1]);
+            const float m11 = 0.5f * (oi[4 * k + 3] + oj[3]) + e;
+            const float2 sj = sqrt2(dinv[j]);
+            mk = make_float4(si.x * m00 * sj.x, si.x * m01 * sj.y, si.y * m10 * sj.x, si.y * m11 * sj.y);
+        }
+        M[(int64_t)k * n + i] = mk;
+    }
+}
 
-namespace ipfem {
+// z_i = sum_k M[k][i] r_nbr(i,k)
+__device__ __forceinline__ float2 patch_apply(int32_t i, int32_t n, GridInfo G, const float4 *__restrict__ M,
+                                              const float2 *__restrict__ r)
+{
+    float2 z = make_float2(0.f, 0.f);
+#pragma unroll
+    for (int k = 0; k < 9; k++) {
+        const int32_t j = patch_nbr(i, k, G);
+        if (j < 0) continue;
+        const float4 m = __ldg(&M[(int64_t)k * n + i]);
+        const float2 v = __ldg(&r[j]);
+        z.x = fmaf(m.x, v.x, fmaf(m.y, v.y, z.x));
+        z.y = fmaf(m.z, v.x, fmaf(m.w, v.y, z.y));
+    }
+    return z;
+}
+
+__global__ void __launch_bounds__(256) k_patch_apply(int32_t n, GridInfo G, const float4 *__restrict__ M,
+                                                     const float2 *__restrict__ r, float2 *__restrict__ z)
+{
+    const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) z[i] = patch_apply(i, n, G, M, r);
+}
 
 // ------------------------------------------------------ flexible CG (FP32)
-// Reductions follow the tree of k_solver.cu (warp tree, 8-warp tree, last CTA).
+// Reductions: warp tree, in-order sum over the CTA's warps, last CTA.
 __device__ __forceinline__ float wsum(float v)
 {
 #pragma unroll
@@ -514,7 +501,7 @@ __device__ void fcg_final(const float *part, int64_t n_part, float (&out)[NV])
     }
 }
 
-// x = 0, p = 0, r = b*scale (FP64 -> FP32); b.b
+// x = 0, p = 0, r = b*scale (FP64 -> FP32), r_old = 0; b.b
 __global__ void __launch_bounds__(256) k_fcg_init(int32_t n_nodes, const double *__restrict__ b, double scale,
                                                   float *__restrict__ x, float *__restrict__ r, float *__restrict__ p,
                                                   float *__restrict__ r_old, float *part, int64_t n_part,
@@ -603,69 +590,24 @@ __global__ void __launch_bounds__(256) k_fcg_update(int32_t n_nodes, const float
     }
 }
 
-// z = M(r) (fused features + MLP), partial r.z and r_old.z; last CTA:
-// Polak-Ribiere beta = (r.z - r_old.z) / rz_prev (clipped at 0), rz = r.z.
-// Persistent CTAs over 128-node tiles so the weights are staged once per CTA.
-__global__ void __launch_bounds__(256) k_mlp_precond(int32_t n_nodes, GridInfo G, const float *__restrict__ r,
-                                                     const float *__restrict__ r_old, const float *__restrict__ dinv,
-                                                     const float *__restrict__ pfrac,
-                                                     const uint8_t *__restrict__ fixed, MlpDev W,
-                                                     float *__restrict__ z, float *part, int64_t n_part,
-                                                     unsigned *ticket, CGScalarsT<float> *sc)
+// z = M r, partial r.z and r_old.z; last CTA: Polak-Ribiere
+// beta = (r.z - r_old.z) / rz_prev (clipped at 0), rz = r.z
+__global__ void __launch_bounds__(256) k_patch_precond(int32_t n, GridInfo G, const float4 *__restrict__ M,
+                                                       const float *__restrict__ r, const float *__restrict__ r_old,
+                                                       float *__restrict__ z, float *part, int64_t n_part,
+                                                       unsigned *ticket, CGScalarsT<float> *sc)
 {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    PrecSmem &S = *reinterpret_cast<PrecSmem *>(smem_raw);
     if (*reinterpret_cast<volatile int *>(&sc->done)) return;
-    load_weights(S, W);
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int64_t n_tiles = ((int64_t)n_nodes + PT - 1) / PT;
-    float vz = 0.f, vc = 0.f;
-    const float2 *r2 = reinterpret_cast<const float2 *>(r);
-    const float2 *ro2 = reinterpret_cast<const float2 *>(r_old);
-    const float2 *d2 = reinterpret_cast<const float2 *>(dinv);
-    for (int64_t tile = blockIdx.x; tile < n_tiles; tile += gridDim.x) {
-        const int64_t base = tile * PT;
-        __syncthreads();   // weights staged / previous tile finished with S.x, S.h
-        if (threadIdx.x < PT) {
-            const int64_t node = base + threadIdx.x;
-            float f[32];
-            float s = 1.f;
-            if (node < n_nodes) {
-                s = node_features((int32_t)node, G, r2, d2, pfrac, fixed, f);
-            } else {
-#pragma unroll
-                for (int j = 0; j < 32; j++) f[j] = 0.f;
-            }
-#pragma unroll
-            for (int j = 0; j < 32; j += 2)
-                *reinterpret_cast<uint32_t *>(&S.x[threadIdx.x][j]) = pack_bf16(f[j], f[j + 1]);
-            S.own[threadIdx.x][0] = f[8];
-            S.own[threadIdx.x][1] = f[9];
-            S.sc[threadIdx.x] = s;
-        }
-        __syncthreads();
-        float o[2][2];
-        mlp_tile(S, warp, lane, o);
-        if ((lane & 3) == 0) {
-#pragma unroll
-            for (int h = 0; h < 2; h++) {
-                const int row = 16 * warp + (lane >> 2) + 8 * h;
-                const int64_t node = base + row;
-                if (node < n_nodes) {
-                    const float2 di = d2[node];
-                    const float s = S.sc[row];
-                    float2 zz;
-                    zz.x = (S.own[row][0] + o[h][0]) * s * di.x;
-                    zz.y = (S.own[row][1] + o[h][1]) * s * di.y;
-                    reinterpret_cast<float2 *>(z)[node] = zz;
-                    const float2 rr = r2[node], ro = ro2[node];
-                    vz = fmaf(rr.y, zz.y, fmaf(rr.x, zz.x, vz));
-                    vc = fmaf(ro.y, zz.y, fmaf(ro.x, zz.x, vc));
-                }
-            }
-        }
+    const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    float v[2] = {0.f, 0.f};
+    if (i < n) {
+        const float2 *r2 = reinterpret_cast<const float2 *>(r);
+        const float2 zz = patch_apply(i, n, G, M, r2);
+        reinterpret_cast<float2 *>(z)[i] = zz;
+        const float2 rr = r2[i], ro = reinterpret_cast<const float2 *>(r_old)[i];
+        v[0] = fmaf(rr.y, zz.y, rr.x * zz.x);
+        v[1] = fmaf(ro.y, zz.y, ro.x * zz.x);
     }
-    float v[2] = {vz, vc};
     if (fcg_partials<2>(v, part, n_part, ticket)) {
         float out[2];
         fcg_final<2>(part, n_part, out);
@@ -675,7 +617,7 @@ __global__ void __launch_bounds__(256) k_mlp_precond(int32_t n_nodes, GridInfo G
             if (!(beta > 0.f)) beta = 0.f;
             sc->beta = beta;
             sc->rz = rz;
-            if (!(rz > 0.f)) {          // the learned step is not a descent direction
+            if (!(rz > 0.f)) {          // M r is not a descent direction
                 sc->done = 1;
                 sc->status = kStatusFallback;
             }
@@ -684,23 +626,141 @@ __global__ void __launch_bounds__(256) k_mlp_precond(int32_t n_nodes, GridInfo G
     }
 }
 
+// ------------------------------------------------------------- training
+// y = K x on an FP32 SELL tangent (Dirichlet rows 0), no reductions
+__global__ void __launch_bounds__(256) k_spmv32(int32_t n, const int64_t *__restrict__ slice_base,
+                                                const int32_t *__restrict__ rowlen,
+                                                const int32_t *__restrict__ sell_node,
+                                                const int32_t *__restrict__ scol, const float4 *__restrict__ K,
+                                                const uint8_t *__restrict__ fixed, const float2 *__restrict__ x,
+                                                float2 *__restrict__ y)
+{
+    const int32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    const int32_t i = sell_node[t];
+    const int64_t base = slice_base[t >> 5] + (t & 31);
+    const int len = rowlen[t];
+    float y0 = 0.f, y1 = 0.f;
+    for (int k = 0; k < len; k++) {
+        const int64_t s = base + (int64_t)k * 32;
+        const float4 a = __ldg(&K[s]);
+        const float2 v = __ldg(&x[scol[s]]);
+        y0 = fmaf(a.x, v.x, fmaf(a.y, v.y, y0));
+        y1 = fmaf(a.z, v.x, fmaf(a.w, v.y, y1));
+    }
+    if (fixed[2 * (int64_t)i]) y0 = 0.f;
+    if (fixed[2 * (int64_t)i + 1]) y1 = 0.f;
+    y[i] = make_float2(y0, y1);
+}
+
+// res = ae - az; CTA partials of ae.ae and res.res into part[2][gridDim.x]
+__global__ void __launch_bounds__(256) k_res_part(int64_t neq, const float *__restrict__ ae,
+                                                  const float *__restrict__ az, float *__restrict__ res,
+                                                  float *__restrict__ part)
+{
+    __shared__ float ws[2][8];
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    float a = 0.f, b = 0.f;
+    if (i < neq) {
+        const float e = ae[i], d = e - az[i];
+        res[i] = d;
+        a = e * e;
+        b = d * d;
+    }
+    a = wsum(a);
+    b = wsum(b);
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if (lane == 0) {
+        ws[0][w] = a;
+        ws[1][w] = b;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        float sa = 0.f, sb = 0.f;
+        for (int k = 0; k < 8; k++) {
+            sa += ws[0][k];
+            sb += ws[1][k];
+        }
+        part[blockIdx.x] = sa;
+        part[gridDim.x + blockIdx.x] = sb;
+    }
+}
+
+// scal[0] = ae.ae, scal[1] = res.res; loss += res.res / ae.ae * w
+__global__ void __launch_bounds__(256) k_res_final(int n_part, const float *__restrict__ part, float *__restrict__ scal,
+                                                   float *__restrict__ loss, float w)
+{
+    __shared__ float ws[2][8];
+    float a = 0.f, b = 0.f;
+    for (int i = threadIdx.x; i < n_part; i += blockDim.x) {
+        a += part[i];
+        b += part[n_part + i];
+    }
+    a = wsum(a);
+    b = wsum(b);
+    const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
+    if (lane == 0) {
+        ws[0][wp] = a;
+        ws[1][wp] = b;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        float sa = 0.f, sb = 0.f;
+        for (int k = 0; k < 8; k++) {
+            sa += ws[0][k];
+            sb += ws[1][k];
+        }
+        scal[0] = sa;
+        scal[1] = sb;
+        if (sa > 0.f) *loss += sb / sa * w;
+    }
+}
+
+// dO_ik[p][q] += c/2 (ghat_i[p] rhat_j[q] + rhat_i[p] ghat_j[q]) for the pair's
+// r and g = K (ae - az), with hats = sigma * (.) and c = -2 w / ae.ae
+__global__ void __launch_bounds__(256) k_patch_grad(int32_t n, GridInfo G, const float2 *__restrict__ dinv,
+                                                    const float2 *__restrict__ r, const float2 *__restrict__ g,
+                                                    const float *__restrict__ scal, float w, float *__restrict__ dO)
+{
+    const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n || !(scal[0] > 0.f)) return;
+    const float c = -w / scal[0];          // (-2 w / ae.ae) * 1/2
+    const float2 si = sqrt2(dinv[i]);
+    const float2 ri = make_float2(si.x * r[i].x, si.y * r[i].y);
+    const float2 gi = make_float2(si.x * g[i].x, si.y * g[i].y);
+    float *o = dO + (int64_t)i * NOUT;
+#pragma unroll
+    for (int k = 0; k < 9; k++) {
+        const int32_t j = patch_nbr(i, k, G);
+        if (j < 0) continue;
+        const float2 sj = sqrt2(dinv[j]);
+        const float2 rj = make_float2(sj.x * r[j].x, sj.y * r[j].y);
+        const float2 gj = make_float2(sj.x * g[j].x, sj.y * g[j].y);
+        o[4 * k + 0] += c * (gi.x * rj.x + ri.x * gj.x);
+        o[4 * k + 1] += c * (gi.x * rj.y + ri.x * gj.y);
+        o[4 * k + 2] += c * (gi.y * rj.x + ri.y * gj.x);
+        o[4 * k + 3] += c * (gi.y * rj.y + ri.y * gj.y);
+    }
+}
+
 // ---------------------------------------------------------------- host side
 
-static MlpDev mlp_dev(ipfem_ctx *c)
+static NetDev net_dev(ipfem_ctx *c)
 {
     MlpBuffers &m = c->mlp;
-    MlpDev W;
+    NetDev W;
     W.w1t = static_cast<const __nv_bfloat16 *>(m.w1t);
     W.w2t = static_cast<const __nv_bfloat16 *>(m.w2t);
+    W.w3t = static_cast<const __nv_bfloat16 *>(m.w3t);
     W.b1 = m.params + kOffB1;
     W.b2 = m.params + kOffB2;
-    W.w3 = m.params + kOffW3;
     W.b3 = m.params + kOffB3;
     return W;
 }
 
-// BF16 copies of W1, W2 in the (n, k) layout of the tensor-core B operand
-__global__ void k_pack_w(const float *__restrict__ P, __nv_bfloat16 *__restrict__ w1t, __nv_bfloat16 *__restrict__ w2t)
+// BF16 copies of W1, W2, W3 in the (n, k) layout of the tensor-core B operand
+__global__ void k_pack_w(const float *__restrict__ P, __nv_bfloat16 *__restrict__ w1t, __nv_bfloat16 *__restrict__ w2t,
+                         __nv_bfloat16 *__restrict__ w3t)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < 128 * 32) {
@@ -711,44 +771,61 @@ __global__ void k_pack_w(const float *__restrict__ P, __nv_bfloat16 *__restrict_
         const int n = i / 128, k = i % 128;
         w2t[i] = __float2bfloat16_rn(P[kOffW2 + k * 128 + n]);
     }
+    if (i < NOUTP * 128) {
+        const int n = i / 128, k = i % 128;
+        w3t[i] = __float2bfloat16_rn(n < NOUT ? P[kOffW3 + k * NOUT + n] : 0.f);
+    }
 }
 
 void mlp_pack_weights(ipfem_ctx *c)
 {
-    k_pack_w<<<64, 256, 0, c->stream>>>(c->mlp.params, static_cast<__nv_bfloat16 *>(c->mlp.w1t),
-                                        static_cast<__nv_bfloat16 *>(c->mlp.w2t));
+    MlpBuffers &m = c->mlp;
+    k_pack_w<<<64, 256, 0, c->stream>>>(m.params, static_cast<__nv_bfloat16 *>(m.w1t),
+                                        static_cast<__nv_bfloat16 *>(m.w2t), static_cast<__nv_bfloat16 *>(m.w3t));
+    m.op_valid = false;
 }
 
-void launch_plastic_fraction(ipfem_ctx *c)
-{
-    const Setup &s = c->s;
-    cudaMemsetAsync(c->mlp.pfrac, 0, (size_t)s.n_nodes * sizeof(float), c->stream);
-    cudaMemsetAsync(c->mlp.pden, 0, (size_t)s.n_nodes * sizeof(float), c->stream);
-    k_plastic_fraction<<<(s.n_el + 255) / 256, 256, 0, c->stream>>>(s.n_el, c->d_dofs, c->d_mtype, c->mlp.pfrac,
-                                                                    c->mlp.pden);
-    k_ratio<<<(s.n_nodes + 255) / 256, 256, 0, c->stream>>>(s.n_nodes, c->mlp.pfrac, c->mlp.pden);
-}
-
-void launch_features(ipfem_ctx *c, const float *d_r, float *d_X, float *d_S)
-{
-    GridInfo G{c->mlp.gr, c->mlp.gt};
-    k_features<<<(c->s.n_nodes + 127) / 128, 128, 0, c->stream>>>(c->s.n_nodes, G, d_r, c->mx.dinv, c->mlp.pfrac,
-                                                                  c->d_fixed, d_X, d_S);
-}
-
-// opt-in to the shared memory the fused kernels need (once, outside any capture)
+// opt-in to the shared memory of the fused network kernel (once, outside any capture)
 cudaError_t mlp_configure()
 {
-    const int sm = (int)sizeof(PrecSmem);
-    cudaError_t e = cudaFuncSetAttribute(k_mlp_infer_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
-    if (e != cudaSuccess) return e;
-    return cudaFuncSetAttribute(k_mlp_precond, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+    return cudaFuncSetAttribute(k_patch_net, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(NetSmem));
 }
 
-void launch_mlp_infer_rows(ipfem_ctx *c, int64_t rows, const float *d_X, float *d_O)
+static int sm_count(const ipfem_ctx *c)
 {
-    const size_t sm = sizeof(PrecSmem);
-    k_mlp_infer_rows<<<(unsigned)((rows + PT - 1) / PT), 256, sm, c->stream>>>(rows, d_X, mlp_dev(c), d_O);
+    int sms = 152;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device);
+    return sms;
+}
+
+void launch_patch_net(ipfem_ctx *c, int64_t rows, const float *d_X, float *d_O)
+{
+    const int64_t tiles = (rows + PT - 1) / PT;
+    const unsigned grid = (unsigned)std::max<int64_t>(1, std::min<int64_t>(tiles, 2 * (int64_t)sm_count(c)));
+    k_patch_net<<<grid, 256, sizeof(NetSmem), c->stream>>>(rows, d_X, net_dev(c), d_O);
+}
+
+void launch_patch_features(ipfem_ctx *c, float *d_X)
+{
+    const int32_t n = c->s.n_nodes;
+    GridInfo G{c->mlp.gr, c->mlp.gt};
+    k_patch_features<<<(n + 255) / 256, 256, 0, c->stream>>>(n, G, reinterpret_cast<const float4 *>(c->mx.K),
+                                                             c->mlp.slot, reinterpret_cast<const float2 *>(c->mx.dinv),
+                                                             d_X);
+}
+
+// features -> network -> symmetric patch operator, for the current FP32 tangent
+void launch_patch_operator(ipfem_ctx *c)
+{
+    MlpBuffers &m = c->mlp;
+    const int32_t n = c->s.n_nodes;
+    GridInfo G{m.gr, m.gt};
+    launch_patch_features(c, m.X);
+    launch_patch_net(c, n, m.X, m.O);
+    k_patch_build<<<(n + 255) / 256, 256, 0, c->stream>>>(n, G, m.O, reinterpret_cast<const float2 *>(c->mx.dinv),
+                                                          reinterpret_cast<float4 *>(m.M));
+    c->launches += 3;
+    m.op_valid = true;
 }
 
 static unsigned fcg_grid(const ipfem_ctx *c)
@@ -756,24 +833,15 @@ static unsigned fcg_grid(const ipfem_ctx *c)
     return (unsigned)((c->s.n_nodes + 255) / 256);
 }
 
-static unsigned precond_grid(const ipfem_ctx *c)
-{
-    int sms = 152;
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device);
-    const int64_t tiles = ((int64_t)c->s.n_nodes + PT - 1) / PT;
-    return (unsigned)std::min<int64_t>(tiles, 2 * (int64_t)sms);
-}
-
 static void launch_precond(ipfem_ctx *c)
 {
-    const size_t sm = sizeof(PrecSmem);
     GridInfo G{c->mlp.gr, c->mlp.gt};
     MixedBuffers &m = c->mx;
-    // the precond partials use the third slot of the FP64 partial array (as floats)
+    // the precond partials use the FP64 partial array (as 2 x n_red floats)
     float *part = reinterpret_cast<float *>(c->d_part);
-    k_mlp_precond<<<precond_grid(c), 256, sm, c->stream>>>(c->s.n_nodes, G, m.r, c->mlp.r_old, m.dinv,
-                                                          c->mlp.pfrac, c->d_fixed, mlp_dev(c), m.z, part,
-                                                          precond_grid(c), c->d_counters + 7, m.sc);
+    k_patch_precond<<<fcg_grid(c), 256, 0, c->stream>>>(c->s.n_nodes, G, reinterpret_cast<const float4 *>(c->mlp.M),
+                                                        m.r, c->mlp.r_old, m.z, part, (int64_t)fcg_grid(c),
+                                                        c->d_counters + 7, m.sc);
 }
 
 void launch_fcg_init(ipfem_ctx *c, const double *d_b, double scale, float rtol, int max_it)
@@ -795,46 +863,119 @@ void launch_fcg_iteration(ipfem_ctx *c)
     launch_cg32_pupdate_only(c);
 }
 
-// One forward (and backward + Adam step if update) over `rows` training rows.
-void mlp_train_step(ipfem_ctx *c, int64_t rows, const float *X, const float *Y, float *H1, float *H2, float *O,
-                    float *dO, float *dH1, float *dH2, bool update, float lr)
+// ------------------------------------------------------------ training pass
+constexpr int kSplitK = 4096;    // rows per split of the weight-gradient GEMMs
+
+static void gemm(ipfem_ctx *c, int M, int N, int K, const float *A, int lda, int tA, const float *B, int ldb, int tB,
+                 float *C, int ldc)
+{
+    dim3 grid((N + GT - 1) / GT, (M + GT - 1) / GT, 1);
+    k_gemm_bf16<<<grid, 128, 0, c->stream>>>(M, N, K, A, lda, tA, B, ldb, tB, C, ldc, ((K + GK - 1) / GK) * GK);
+}
+
+// C[M][N] = A^T B over K = rows (both row-major with rows as the K index), split K
+static void gemm_tn_split(ipfem_ctx *c, int M, int N, int64_t rows, const float *A, int lda, const float *B, int ldb,
+                          float *C)
 {
     MlpBuffers &m = c->mlp;
+    const int splits = (int)((rows + kSplitK - 1) / kSplitK);
+    dim3 grid((N + GT - 1) / GT, (M + GT - 1) / GT, splits);
+    k_gemm_bf16<<<grid, 128, 0, c->stream>>>(M, N, (int)rows, A, lda, 1, B, ldb, 0, m.part, N, kSplitK);
+    const int64_t n = (int64_t)M * N;
+    k_sum_splits<<<(unsigned)((n + 255) / 256), 256, 0, c->stream>>>(n, splits, m.part, C);
+}
+
+static void colsum(ipfem_ctx *c, int64_t rows, int n, const float *D, float *out)
+{
+    MlpBuffers &m = c->mlp;
+    const int chunks = (int)((rows + kColChunk - 1) / kColChunk);
+    k_colsum_part<<<dim3((n + 31) / 32, chunks), 256, 0, c->stream>>>(rows, n, D, m.part);
+    k_sum_splits<<<(n + 255) / 256, 256, 0, c->stream>>>(n, chunks, m.part, out);
+}
+
+size_t patch_part_floats(int64_t n_nodes)
+{
+    const int64_t splits = (n_nodes + kSplitK - 1) / kSplitK;
+    const int64_t chunks = (n_nodes + kColChunk - 1) / kColChunk;
+    return (size_t)std::max<int64_t>(splits * 128 * 128, chunks * 128);
+}
+
+// Gradient of L = (1/P) sum_p |K e_p - K M r_p|^2 / |K e_p|^2 with respect to
+// the parameters (into mlp.grads) and L (into mlp.loss), for P pairs of
+// FP32 device vectors r_p = d_r + p*neq, e_p = d_e + p*neq on this tangent.
+void patch_learn_grad(ipfem_ctx *c, const float *d_r, const float *d_e, int P)
+{
+    MlpBuffers &m = c->mlp;
+    MixedBuffers &x = c->mx;
+    const Setup &s = c->s;
+    const int32_t n = s.n_nodes;
+    const int64_t neq = s.neq;
+    const float *W = m.params;
     cudaStream_t st = c->stream;
-    const int R = (int)rows;
-    auto gemm = [&](int M, int N, int K, const float *A, int lda, int tA, const float *B, int ldb, int tB, float *C_,
-                    int ldc) {
-        dim3 grid((N + GT - 1) / GT, (M + GT - 1) / GT);
-        k_gemm_bf16<<<grid, 128, 0, st>>>(M, N, K, A, lda, tA, B, ldb, tB, C_, ldc, 1.f, 0);
-    };
-    const unsigned eb = (unsigned)((rows * 128 + 255) / 256);
-    // forward
-    gemm(R, 128, 32, X, 32, 0, m.params + kOffW1, 128, 0, H1, 128);
-    k_bias_relu<<<eb, 256, 0, st>>>(rows, 128, H1, m.params + kOffB1, 1);
-    gemm(R, 128, 128, H1, 128, 0, m.params + kOffW2, 128, 0, H2, 128);
-    k_bias_relu<<<eb, 256, 0, st>>>(rows, 128, H2, m.params + kOffB2, 1);
-    const unsigned rb = (unsigned)((rows + 255) / 256);
-    k_out_layer<<<rb, 256, 0, st>>>(rows, X, H2, m.params + kOffW3, m.params + kOffB3, O);
-    // backward
+    GridInfo G{m.gr, m.gt};
+    const unsigned gn = (unsigned)((n + 255) / 256);
+    const unsigned ge = (unsigned)((neq + 255) / 256);
+    const unsigned eh = (unsigned)(((int64_t)n * 128 + 255) / 256);
+    // forward through the GEMM path (keeps the hidden layers for the backward)
+    launch_patch_features(c, m.X);
+    gemm(c, n, 128, 32, m.X, 32, 0, W + kOffW1, 128, 0, m.H1, 128);
+    k_bias_act<<<eh, 256, 0, st>>>(n, 128, m.H1, W + kOffB1, 1);
+    gemm(c, n, 128, 128, m.H1, 128, 0, W + kOffW2, 128, 0, m.H2, 128);
+    k_bias_act<<<eh, 256, 0, st>>>(n, 128, m.H2, W + kOffB2, 1);
+    gemm(c, n, NOUT, 128, m.H2, 128, 0, W + kOffW3, NOUT, 0, m.O, NOUT);
+    k_bias_act<<<(unsigned)(((int64_t)n * NOUT + 255) / 256), 256, 0, st>>>(n, NOUT, m.O, W + kOffB3, 0);
+    k_patch_build<<<gn, 256, 0, st>>>(n, G, m.O, reinterpret_cast<const float2 *>(x.dinv),
+                                      reinterpret_cast<float4 *>(m.M));
+    m.op_valid = false;     // the operator now belongs to these parameters only if nothing changes them
+    // pairs
+    cudaMemsetAsync(m.dN, 0, (size_t)n * NOUT * sizeof(float), st);
     cudaMemsetAsync(m.loss, 0, sizeof(float), st);
-    k_out_backward<<<rb, 256, 0, st>>>(rows, O, Y, m.params + kOffW3, dO, dH2, m.loss);
-    k_relu_mask<<<eb, 256, 0, st>>>(rows * 128, dH2, H2);
-    gemm(128, 2, R, H2, 128, 1, dO, 2, 0, m.grads + kOffW3, 2);            // dW3 = H2^T dO
-    k_colsum<<<1, 32, 0, st>>>(rows, 2, dO, m.grads + kOffB3);
-    gemm(128, 128, R, H1, 128, 1, dH2, 128, 0, m.grads + kOffW2, 128);     // dW2 = H1^T dH2
-    k_colsum<<<1, 128, 0, st>>>(rows, 128, dH2, m.grads + kOffB2);
-    gemm(R, 128, 128, dH2, 128, 0, m.params + kOffW2, 128, 1, dH1, 128);   // dH1 = dH2 W2^T
-    k_relu_mask<<<eb, 256, 0, st>>>(rows * 128, dH1, H1);
-    gemm(32, 128, R, X, 32, 1, dH1, 128, 0, m.grads + kOffW1, 128);        // dW1 = X^T dH1
-    k_colsum<<<1, 128, 0, st>>>(rows, 128, dH1, m.grads + kOffB1);
-    if (update) {
-        m.adam_t += 1;
-        const float b1 = 0.9f, b2 = 0.999f;
-        const float c1 = 1.f - powf(b1, (float)m.adam_t), c2 = 1.f - powf(b2, (float)m.adam_t);
-        k_adam<<<(kMlpParams + 255) / 256, 256, 0, st>>>(kMlpParams, m.params, m.grads, m.m, m.v, lr, b1, b2, 1e-8f,
-                                                         c1, c2);
-        mlp_pack_weights(c);
+    float *z = m.vec, *ae = m.vec + neq, *az = m.vec + 2 * neq, *res = m.vec + 3 * neq, *g = m.vec + 4 * neq;
+    const SellDev &L = x.dsell;
+    const float4 *K4 = reinterpret_cast<const float4 *>(x.K);
+    const float w = 1.f / (float)P;
+    for (int p = 0; p < P; p++) {
+        const float *r = d_r + (size_t)p * neq, *e = d_e + (size_t)p * neq;
+        k_patch_apply<<<gn, 256, 0, st>>>(n, G, reinterpret_cast<const float4 *>(m.M),
+                                          reinterpret_cast<const float2 *>(r), reinterpret_cast<float2 *>(z));
+        k_spmv32<<<gn, 256, 0, st>>>(n, L.slice_base, L.rowlen, L.sell_node, L.sell_col, K4, c->d_fixed,
+                                     reinterpret_cast<const float2 *>(e), reinterpret_cast<float2 *>(ae));
+        k_spmv32<<<gn, 256, 0, st>>>(n, L.slice_base, L.rowlen, L.sell_node, L.sell_col, K4, c->d_fixed,
+                                     reinterpret_cast<const float2 *>(z), reinterpret_cast<float2 *>(az));
+        k_res_part<<<ge, 256, 0, st>>>(neq, ae, az, res, m.part);
+        k_res_final<<<1, 256, 0, st>>>((int)ge, m.part, m.scal, m.loss, w);
+        k_spmv32<<<gn, 256, 0, st>>>(n, L.slice_base, L.rowlen, L.sell_node, L.sell_col, K4, c->d_fixed,
+                                     reinterpret_cast<const float2 *>(res), reinterpret_cast<float2 *>(g));
+        k_patch_grad<<<gn, 256, 0, st>>>(n, G, reinterpret_cast<const float2 *>(x.dinv),
+                                         reinterpret_cast<const float2 *>(r), reinterpret_cast<const float2 *>(g),
+                                         m.scal, w, m.dN);
     }
+    // backward
+    float *gr = m.grads;
+    gemm_tn_split(c, 128, NOUT, n, m.H2, 128, m.dN, NOUT, gr + kOffW3);              // dW3 = H2^T dO
+    colsum(c, n, NOUT, m.dN, gr + kOffB3);
+    gemm(c, n, 128, NOUT, m.dN, NOUT, 0, W + kOffW3, NOUT, 1, m.dH2, 128);           // dH2 = dO W3^T
+    k_relu_mask<<<eh, 256, 0, st>>>((int64_t)n * 128, m.dH2, m.H2);
+    gemm_tn_split(c, 128, 128, n, m.H1, 128, m.dH2, 128, gr + kOffW2);              // dW2 = H1^T dH2
+    colsum(c, n, 128, m.dH2, gr + kOffB2);
+    gemm(c, n, 128, 128, m.dH2, 128, 0, W + kOffW2, 128, 1, m.dH1, 128);             // dH1 = dH2 W2^T
+    k_relu_mask<<<eh, 256, 0, st>>>((int64_t)n * 128, m.dH1, m.H1);
+    gemm_tn_split(c, 32, 128, n, m.X, 32, m.dH1, 128, gr + kOffW1);                  // dW1 = X^T dH1
+    colsum(c, n, 128, m.dH1, gr + kOffB1);
+    c->launches += 7 + 6 * (uint64_t)P + 14;
+}
+
+// one Adam step on the parameters with the gradient in mlp.grads
+void mlp_adam_step(ipfem_ctx *c, float lr)
+{
+    MlpBuffers &m = c->mlp;
+    m.adam_t += 1;
+    const float b1 = 0.9f, b2 = 0.999f;
+    const float c1 = 1.f - powf(b1, (float)m.adam_t), c2 = 1.f - powf(b2, (float)m.adam_t);
+    k_adam<<<(kMlpParams + 255) / 256, 256, 0, c->stream>>>(kMlpParams, m.params, m.grads, m.m, m.v, lr, b1, b2,
+                                                             1e-8f, c1, c2);
+    mlp_pack_weights(c);
+    c->launches += 2;
 }
 
 }  // namespace ipfem

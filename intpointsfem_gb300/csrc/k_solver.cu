@@ -163,22 +163,28 @@ __global__ void __launch_bounds__(kRedBlock) k_cg_init(int32_t n_nodes, const do
     }
 }
 
-// q = K p (free dofs), partial sums of p.q; last CTA: alpha = rz / pq
-template <class T>
+// q = K p (free dofs), partial sums of p.q; last CTA: alpha = rz / pq.
+// SORTED: thread t runs SELL row position t, i.e. node sell_node[t] of the
+// same kRedBlock window, and its p.q term goes through shared memory back to
+// the node's own slot, so the block tree adds in node order either way.
+template <class T, bool SORTED>
 __global__ void __launch_bounds__(kRedBlock) k_cg_spmv(int32_t n_nodes, const int64_t *__restrict__ slice_base,
                                                        const int32_t *__restrict__ rowlen,
+                                                       const int32_t *__restrict__ sell_node,
                                                        const int32_t *__restrict__ scol, const T *__restrict__ K,
                                                        const uint8_t *__restrict__ fixed, const T *__restrict__ p,
                                                        T *__restrict__ q, T *part, int64_t n_red, unsigned *ticket,
                                                        CGScalarsT<T> *sc)
 {
     typedef typename Vec2<T>::type V;
+    __shared__ T s_pq[SORTED ? kRedBlock : 1];
     if (*reinterpret_cast<volatile int *>(&sc->done)) return;
-    const int32_t i = blockIdx.x * kRedBlock + threadIdx.x;
+    const int32_t t = blockIdx.x * kRedBlock + threadIdx.x;
     T v[1] = {T(0)};
-    if (i < n_nodes) {
-        const int64_t base = __ldg(&slice_base[i >> 5]) + (i & 31);
-        const int len = __ldg(&rowlen[i]);
+    if (t < n_nodes) {
+        const int32_t i = SORTED ? __ldg(&sell_node[t]) : t;
+        const int64_t base = __ldg(&slice_base[t >> 5]) + (t & 31);
+        const int len = __ldg(&rowlen[t]);
         const V *pv = reinterpret_cast<const V *>(p);
         T y0 = T(0), y1 = T(0);
 #pragma unroll 4
@@ -198,6 +204,13 @@ __global__ void __launch_bounds__(kRedBlock) k_cg_spmv(int32_t n_nodes, const in
         reinterpret_cast<V *>(q)[i] = mk2(y0, y1);
         const V pp = pv[i];
         v[0] = fma(pp.y, y1, fma(pp.x, y0, T(0)));
+        if (SORTED) s_pq[i - blockIdx.x * kRedBlock] = v[0];
+    } else if (SORTED) {
+        s_pq[threadIdx.x] = T(0);
+    }
+    if (SORTED) {
+        __syncthreads();
+        v[0] = s_pq[threadIdx.x];
     }
     if (block_partials<T, 1>(v, part, n_red, ticket)) {
         T o[1];
@@ -345,12 +358,24 @@ void launch_cg_init(ipfem_ctx *c, const double *d_b, double rtol, int max_it)
                                                                   c->d_counters + 0, c->d_sc, rtol, max_it);
 }
 
+template <class T>
+void launch_spmv(ipfem_ctx *c, const SellDev &L, const T *K, const T *p, T *q, T *part, unsigned *ticket,
+                 CGScalarsT<T> *sc)
+{
+    if (L.sorted)
+        k_cg_spmv<T, true><<<grid_nodes(c), kRedBlock, 0, c->stream>>>(
+            c->s.n_nodes, L.slice_base, L.rowlen, L.sell_node, L.sell_col, K, c->d_fixed, p, q, part, c->n_red,
+            ticket, sc);
+    else
+        k_cg_spmv<T, false><<<grid_nodes(c), kRedBlock, 0, c->stream>>>(
+            c->s.n_nodes, L.slice_base, L.rowlen, L.sell_node, L.sell_col, K, c->d_fixed, p, q, part, c->n_red,
+            ticket, sc);
+}
+
 void launch_cg_iteration(ipfem_ctx *c)
 {
     const unsigned g = grid_nodes(c);
-    k_cg_spmv<double><<<g, kRedBlock, 0, c->stream>>>(c->s.n_nodes, c->d_slice_base, c->d_rowlen, c->d_sell_col,
-                                                      c->d_K, c->d_fixed, c->d_p, c->d_q, c->d_part, c->n_red,
-                                                      c->d_counters + 1, c->d_sc);
+    launch_spmv<double>(c, c->dsell, c->d_K, c->d_p, c->d_q, c->d_part, c->d_counters + 1, c->d_sc);
     k_cg_update<double><<<g, kRedBlock, 0, c->stream>>>(c->s.n_nodes, c->d_p, c->d_q, c->d_dinv, c->d_x, c->d_r,
                                                         c->d_z, c->d_part, c->n_red, c->d_counters + 2, c->d_sc);
     k_cg_pupdate<double><<<g, kRedBlock, 0, c->stream>>>(c->s.n_nodes, c->d_z, c->d_p, c->d_sc);
@@ -358,9 +383,7 @@ void launch_cg_iteration(ipfem_ctx *c)
 
 void launch_cg_spmv_only(ipfem_ctx *c)
 {
-    k_cg_spmv<double><<<grid_nodes(c), kRedBlock, 0, c->stream>>>(c->s.n_nodes, c->d_slice_base, c->d_rowlen,
-                                                                  c->d_sell_col, c->d_K, c->d_fixed, c->d_p, c->d_q,
-                                                                  c->d_part, c->n_red, c->d_counters + 1, c->d_sc);
+    launch_spmv<double>(c, c->dsell, c->d_K, c->d_p, c->d_q, c->d_part, c->d_counters + 1, c->d_sc);
 }
 
 void launch_cg32_init(ipfem_ctx *c, const double *d_b, double scale, float rtol, int max_it)
@@ -375,8 +398,7 @@ void launch_cg32_iteration(ipfem_ctx *c)
 {
     MixedBuffers &m = c->mx;
     const unsigned g = grid_nodes(c);
-    k_cg_spmv<float><<<g, kRedBlock, 0, c->stream>>>(c->s.n_nodes, c->d_slice_base, c->d_rowlen, c->d_sell_col, m.K,
-                                                     c->d_fixed, m.p, m.q, m.part, c->n_red, c->d_counters + 5, m.sc);
+    launch_spmv<float>(c, m.dsell, m.K, m.p, m.q, m.part, c->d_counters + 5, m.sc);
     k_cg_update<float><<<g, kRedBlock, 0, c->stream>>>(c->s.n_nodes, m.p, m.q, m.dinv, m.x, m.r, m.z, m.part,
                                                        c->n_red, c->d_counters + 6, m.sc);
     k_cg_pupdate<float><<<g, kRedBlock, 0, c->stream>>>(c->s.n_nodes, m.z, m.p, m.sc);
@@ -385,9 +407,7 @@ void launch_cg32_iteration(ipfem_ctx *c)
 void launch_cg32_spmv_only(ipfem_ctx *c)
 {
     MixedBuffers &m = c->mx;
-    k_cg_spmv<float><<<grid_nodes(c), kRedBlock, 0, c->stream>>>(c->s.n_nodes, c->d_slice_base, c->d_rowlen,
-                                                                 c->d_sell_col, m.K, c->d_fixed, m.p, m.q, m.part,
-                                                                 c->n_red, c->d_counters + 5, m.sc);
+    launch_spmv<float>(c, m.dsell, m.K, m.p, m.q, m.part, c->d_counters + 5, m.sc);
 }
 
 void launch_cg32_pupdate_only(ipfem_ctx *c)

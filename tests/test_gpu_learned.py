@@ -1,6 +1,7 @@
-"""Learned preconditioner: tensor-core forward and gradients against the CPU
-oracle (oracle/orc_mlp.py), FCG with the untrained network equals Jacobi,
-training on the GPU, and what the trained network gains over Jacobi-PCG."""
+"""Learned preconditioner: features, tensor-core forward, the symmetric patch
+operator and the training gradients against the CPU oracle
+(oracle/orc_mlp.py); FCG with the untrained network equals Jacobi; training
+on the GPU and what the trained network gains over Jacobi-PCG."""
 import numpy as np
 import pytest
 
@@ -12,52 +13,135 @@ from intpointsfem_gb300 import learned  # noqa: E402
 from oracle import orc_mlp  # noqa: E402
 
 
-def _host():
-    wb, sm = learned.make_solver(8, -10.0, 30.0, seed=3)
-    return wb, sm
-
-
-def _random_params(rng, scale3=0.2):
+def _random_params(rng, scale3=0.05):
     d = {"W1": rng.normal(size=(32, 128)) * np.sqrt(2 / 32), "b1": rng.normal(size=128) * 0.1,
          "W2": rng.normal(size=(128, 128)) * np.sqrt(2 / 128), "b2": rng.normal(size=128) * 0.1,
-         "W3": rng.normal(size=(128, 2)) * scale3, "b3": rng.normal(size=2) * 0.1}
+         "W3": rng.normal(size=(128, 36)) * scale3, "b3": rng.normal(size=36) * 0.02}
     return orc_mlp.pack(d)
 
 
-def test_forward_matches_cpu_oracle():
+def _problem(n=6, step=5):
+    """mixed-precision wellbore with an assembled FP32 tangent at load step `step` of 10"""
+    wb, sm = learned.make_solver(n, -15.0, 30.0, seed=3)
+    u = torch.zeros(sm.neq, dtype=torch.float64, device="cuda")
+    sm.newton_begin(10, 0, step, newton_max_it=15, cg_rtol=1e-5)
+    sm.newton_advance(u, 0, ip.DEVICE)
+    sm.SetLoadFactor((step + 1) / 10)
+    R = torch.zeros_like(u)
+    sm.assemble(u, R, ip.DEVICE)
+    return wb, sm, R
+
+
+def _tangent(sm, wb):
+    rp, col, val = sm.stiffness()
+    K = val.reshape(-1, 2, 2)
+    fixed = wb.array("fixed").astype(bool)
+    d = np.zeros(sm.neq)
+    rows = np.repeat(np.arange(sm.n_nodes), np.diff(rp))
+    for t in np.nonzero(rows == col)[0]:
+        d[2 * rows[t]] = K[t, 0, 0]
+        d[2 * rows[t] + 1] = K[t, 1, 1]
+    dinv = np.where(fixed, 0.0, 1.0 / np.where(d == 0, 1.0, d))
+
+    def matvec(v):
+        y = np.zeros(sm.neq)
+        vb = v.reshape(-1, 2)
+        yb = y.reshape(-1, 2)
+        np.add.at(yb, rows, np.einsum("tpq,tq->tp", K, vb[col]))
+        y[fixed] = 0.0
+        return y
+
+    return rp, col, K, dinv, matvec
+
+
+def test_features_match_oracle():
+    wb, sm, _ = _problem()
+    gr = 13
+    X = torch.zeros(sm.n_nodes, 32, device="cuda")
+    sm.mlp_features(X)
+    rp, col, K, dinv, _ = _tangent(sm, wb)
+    Xr = orc_mlp.features(gr, gr, rp, col, K, dinv)
+    Xg = X.cpu().numpy()
+    assert np.abs(Xr).max() > 0.1
+    assert np.abs(Xg - Xr).max() <= 1e-5 * np.abs(Xr).max()
+
+
+def test_forward_matches_oracle():
     rng = np.random.default_rng(0)
-    wb, sm = _host()
-    p = _random_params(rng)
-    sm.set_mlp_params(p)
+    wb, sm = learned.make_solver(4, -10.0, 30.0, seed=3)
+    sm.set_mlp_params(_random_params(rng, 0.2))
     X = rng.normal(size=(1000, 32)).astype(np.float32)
-    dX = torch.tensor(X, device="cuda")
-    dO = torch.zeros(1000, 2, device="cuda")
-    sm.mlp_forward(dX, 1000, dO)
+    dO = torch.zeros(1000, 36, device="cuda")
+    sm.mlp_forward(torch.tensor(X, device="cuda"), 1000, dO)
     O_ref, _ = orc_mlp.forward(sm.mlp_params(), X)
-    O = dO.cpu().numpy()
-    err = np.abs(O - O_ref).max() / np.abs(O_ref).max()
+    err = np.abs(dO.cpu().numpy() - O_ref).max() / np.abs(O_ref).max()
     assert err < 2e-3, err
 
 
-def test_gradients_match_cpu_oracle():
+def test_operator_is_symmetric_and_matches_oracle():
     rng = np.random.default_rng(1)
-    wb, sm = _host()
+    wb, sm, _ = _problem()
+    gr, n = 13, sm.n_nodes
+    sm.set_mlp_params(_random_params(rng))
+    X = torch.zeros(n, 32, device="cuda")
+    sm.mlp_features(X)
+    O = torch.zeros(n, 36, device="cuda")
+    sm.mlp_forward(X, n, O)
+    M = torch.zeros(9, n, 2, 2, device="cuda")
+    sm.mlp_operator(M)
+    Mg = M.cpu().numpy().astype(np.float64)
+    _, _, _, dinv, _ = _tangent(sm, wb)
+    Mr = orc_mlp.operator(gr, gr, O.cpu().numpy(), dinv)
+    assert np.abs(Mg - Mr).max() <= 1e-5 * np.abs(Mr).max()
+    # dense symmetric check
+    nb = orc_mlp.neighbours(gr, gr)
+    D = np.zeros((2 * n, 2 * n))
+    for k in range(9):
+        for i in np.nonzero(nb[:, k] >= 0)[0]:
+            j = nb[i, k]
+            D[2 * i:2 * i + 2, 2 * j:2 * j + 2] += Mg[k, i]
+    assert np.abs(D - D.T).max() <= 1e-6 * np.abs(D).max()
+    # untrained parameters give Jacobi
+    sm.mlp_init(0)
+    sm.mlp_operator(M)
+    Mj = M.cpu().numpy()
+    assert np.array_equal(Mj[[0, 1, 2, 3, 5, 6, 7, 8]], np.zeros_like(Mj[[0, 1, 2, 3, 5, 6, 7, 8]]))
+    diag = np.stack([Mj[4, :, 0, 0], Mj[4, :, 1, 1]], 1).ravel()
+    assert np.allclose(diag, dinv, rtol=1e-6, atol=0)
+
+
+def test_learn_grad_matches_oracle():
+    rng = np.random.default_rng(2)
+    wb, sm, R0 = _problem()
+    gr = 13
     p = _random_params(rng)
     sm.set_mlp_params(p)
-    n = 3000
-    X = rng.normal(size=(n, 32)).astype(np.float32)
-    Y = rng.normal(size=(n, 2)).astype(np.float32)
-    g, loss = sm.mlp_grad(torch.tensor(X, device="cuda"), torch.tensor(Y, device="cuda"), n)
-    loss_ref, g_ref = orc_mlp.loss_and_grads(sm.mlp_params(), X, Y)
+    snaps = [0, 32, 64]
+    xs = torch.zeros(len(snaps), sm.neq, dtype=torch.float32, device="cuda")
+    rs = torch.zeros_like(xs)
+    xf = torch.zeros(sm.neq, dtype=torch.float32, device="cuda")
+    its = sm.cg_snapshots(R0, snaps, xs, rs, xf, rtol=1e-6, max_it=4000)
+    assert its > 64
+    E = (xf[None] - xs).contiguous()
+    g, loss = sm.learn_grad(rs, E, len(snaps))
+    X = torch.zeros(sm.n_nodes, 32, device="cuda")
+    sm.mlp_features(X)
+    _, _, _, dinv, matvec = _tangent(sm, wb)
+    loss_ref, g_ref = orc_mlp.loss_and_grads(sm.mlp_params(), X.cpu().numpy(), matvec, gr, gr, dinv,
+                                             rs.cpu().numpy(), E.cpu().numpy())
     assert loss == pytest.approx(loss_ref, rel=2e-3)
     gd, rd = orc_mlp.unpack(g), orc_mlp.unpack(g_ref)
     for name, _ in orc_mlp.SIZES:
         e = np.linalg.norm(gd[name] - rd[name]) / np.linalg.norm(rd[name])
-        assert e < 1e-2, (name, e)
+        assert e < 2e-2, (name, e)
+    # a small Adam step along the gradient lowers the loss
+    sm.mlp_adam(g, 1e-4)
+    _, loss2 = sm.learn_grad(rs, E, len(snaps))
+    assert loss2 < loss
 
 
 def test_untrained_network_is_jacobi_inside_fcg():
-    """W3 = 0 at initialisation: the preconditioner is Jacobi, so FCG and
+    """W3 = 0 at initialisation: the operator is Jacobi, so FCG and
     Jacobi-PCG take the same number of iterations to the same tolerance."""
     wb, sm = learned.make_solver(32, -10.0, 30.0, seed=0)
     u = torch.zeros(sm.neq, dtype=torch.float64, device="cuda")
@@ -72,19 +156,25 @@ def test_untrained_network_is_jacobi_inside_fcg():
 
 
 def test_training_and_gain_over_jacobi():
-    """Small wellbore (48 x 48): data from the plain solver, training on the
-    GPU, then the same Newton iterations with Jacobi-PCG and with the learned
-    FCG.  Both must reach the same Newton tolerance; the gain (CG iterations
-    and solve time) is reported."""
-    X, Y = learned.generate_training_data(n=48, n_samples=16000, n_problems=4, seed=11)
-    assert X.shape[0] > 8000
-    p, losses = learned.train(X, Y, epochs=25, batch=1024, lr=2e-3, seed=2)
-    assert np.isfinite(losses).all() and losses[-1] < losses[0]
+    """Training on three 24 x 24 problems (GPU forward/backward and Adam),
+    evaluation on a 48 x 48 problem with another well pressure and friction
+    angle: the same Newton iterations with Jacobi-PCG and with the learned
+    FCG.  Both reach the same Newton tolerance; the learned operator needs
+    clearly fewer CG iterations."""
+    probs = learned.generate_problems(n=24, n_problems=3, seed=11)
+    try:
+        p, losses = learned.train(probs, steps=240, lr=1e-3, pairs_per_step=6, seed=2)
+    finally:
+        for pb in probs:
+            pb.close()
+    assert np.isfinite(losses).all() and losses[-30:].mean() < 0.8 * losses[:3].mean()
     res = learned.compare(p, n=48, pw=-12.0, phi=28.0, newton_iters=6)
     j, m = res["jacobi"], res["mlp"]
-    print("learned vs Jacobi (48x48): CG iterations %d vs %d, solve ms %.1f vs %.1f, loss %.3g -> %.3g"
-          % (m["cg_iters"], j["cg_iters"], m["ms_solve"], j["ms_solve"], losses[0], losses[-1]))
+    print("learned vs Jacobi (48x48): CG iterations %d vs %d, solve ms %.1f vs %.1f, fallbacks %d, loss %.3g -> %.3g"
+          % (m["cg_iters"], j["cg_iters"], m["ms_solve"], j["ms_solve"], m["fallbacks"], losses[:3].mean(),
+             losses[-30:].mean()))
     assert m["newton_iters"] == j["newton_iters"]
-    # both Newton sequences reach the same displacement to the Newton tolerance
     du = np.abs(m["u"] - j["u"]).max() / np.abs(j["u"]).max()
     assert du < 1e-4, du
+    assert m["fallbacks"] == 0
+    assert m["cg_iters"] < 0.75 * j["cg_iters"], (m["cg_iters"], j["cg_iters"])

@@ -81,3 +81,36 @@ def test_nan_input_propagates_to_residual(P8):
     u[10] = np.nan
     r = P8.assemble_residual(u, 0.1)
     assert np.isnan(r).any()
+
+
+def test_patch_operator_gradient_matches_finite_differences():
+    """the oracle's dL/dO of the learned patch operator (oracle/orc_mlp.py)
+    against central differences, on the oracle's own tangent of a 3 x 3 mesh"""
+    import scipy.sparse as sp
+    from oracle import orc_mlp
+    n = 3
+    P = po.OracleProblem(po.default_params(n), nthreads=0)
+    P.assemble(np.zeros(P.neq), 0.5)
+    rp, col, K = P.arr("row_ptr"), P.arr("col"), P.arr("K").reshape(-1, 2, 2)
+    nn = P.n_nodes
+    fixed = P.arr("fixed").astype(bool)
+    A = sp.bsr_matrix((K.copy(), col.copy(), rp.copy()), shape=(2 * nn, 2 * nn)).tocsr()
+    keep = sp.diags((~fixed).astype(float))
+    A = (keep @ A @ keep).tocsr()
+    dinv = np.where(fixed, 0.0, 1.0 / A.diagonal().clip(min=1e-300))
+    rng = np.random.default_rng(0)
+    R = [rng.normal(size=P.neq) * ~fixed for _ in range(2)]
+    E = [rng.normal(size=P.neq) * ~fixed for _ in range(2)]
+    gr = 2 * n + 1
+    O = rng.normal(size=(nn, 36)) * 0.1
+    mv = lambda v: A @ v  # noqa: E731
+    loss, dO = orc_mlp.patch_loss_grad(O, mv, gr, gr, dinv, R, E)
+    assert loss > 0
+    for t in rng.choice(O.size, size=25, replace=False):
+        h = 1e-6
+        Op, Om = O.copy(), O.copy()
+        Op.flat[t] += h
+        Om.flat[t] -= h
+        fd = (orc_mlp.patch_loss_grad(Op, mv, gr, gr, dinv, R, E)[0] -
+              orc_mlp.patch_loss_grad(Om, mv, gr, gr, dinv, R, E)[0]) / (2 * h)
+        assert abs(fd - dO.flat[t]) <= 1e-6 * max(1.0, abs(dO).max()), (t, fd, dO.flat[t])
