@@ -276,26 +276,47 @@ def run_gpu(args):
         ms_e2e = 1e3 * (time.perf_counter() - t0) / args.steps
         B.close()
 
-    # the chosen method (mixed precision) beside the plain one, same iterations
+    # the chosen method (mixed precision + learned preconditioner) and mixed
+    # precision with Jacobi beside the plain one, same Newton iterations
     chosen = None
     if not mixed and args.chosen:
-        C_ = ip.ElastoPlasticIntPointsStructMatrix(wb)
-        C_.set_precision(ip.MIXED)
-        uc = torch.zeros(C_.neq, dtype=torch.float64, device=dev)
-        C_.newton_begin(N_STEPS, newton_max_it=40, cg_rtol=args.mixed_cg_rtol)
-        C_.newton_advance(uc, args.warmup, ip.DEVICE)
-        sc_ = torch.cuda.ExternalStream(C_.stream, device=dev)
-        torch.cuda.synchronize()
-        e0.record(sc_)
-        stc, _ = C_.newton_advance(uc, args.steps, ip.DEVICE)
-        e1.record(sc_)
-        torch.cuda.synchronize()
-        chosen = {"method": "mixed: FP32 tangent + FP32 Jacobi-CG to %g, FP64 residual/return mapping/Newton "
-                            "refinement" % args.mixed_cg_rtol,
-                  "ms_per_newton_iter": e0.elapsed_time(e1) / args.steps,
-                  "cg_iters_per_newton": stc.cg_iters / max(1, stc.newton_iters),
-                  "ms_spmv_fp32": C_.profile_spmv(reps=20)}
-        C_.close()
+        from intpointsfem_gb300 import train_preconditioner as tp
+
+        def mixed_arm(learned_prec):
+            C_ = ip.ElastoPlasticIntPointsStructMatrix(wb)
+            C_.set_precision(ip.MIXED)
+            if learned_prec:
+                C_.set_node_grid(2 * n + 1, 2 * n + 1)
+                C_.mlp_init(0)
+                C_.set_mlp_params(tp.load_weights())
+                C_.set_preconditioner(ip.PREC_MLP)
+            uc = torch.zeros(C_.neq, dtype=torch.float64, device=dev)
+            C_.newton_begin(N_STEPS, newton_max_it=40, cg_rtol=args.mixed_cg_rtol)
+            C_.newton_advance(uc, args.warmup, ip.DEVICE)
+            sc_ = torch.cuda.ExternalStream(C_.stream, device=dev)
+            torch.cuda.synchronize()
+            l0c = C_.launch_count
+            e0.record(sc_)
+            stc, _ = C_.newton_advance(uc, args.steps, ip.DEVICE)
+            e1.record(sc_)
+            torch.cuda.synchronize()
+            out = {"ms_per_newton_iter": e0.elapsed_time(e1) / args.steps,
+                   "cg_iters_per_newton": stc.cg_iters / max(1, stc.newton_iters),
+                   "newton_iters_timed": stc.newton_iters, "fcg_fallbacks": stc.fcg_fallbacks,
+                   "ms_cg_per_newton": stc.ms_solve / args.steps, "gpu_launches": C_.launch_count - l0c}
+            if not learned_prec:
+                out["ms_spmv_fp32"] = C_.profile_spmv(reps=20)
+            C_.close()
+            return out
+
+        chosen = mixed_arm(True)
+        chosen["method"] = ("mixed + learned: FP32 tangent, flexible CG to %g preconditioned by the learned "
+                            "triangular factor (weights shipped in intpointsfem_gb300/weights), FP64 residual/"
+                            "return mapping/Newton refinement" % args.mixed_cg_rtol)
+        chosen["mixed_jacobi"] = mixed_arm(False)
+        chosen["mixed_jacobi"]["method"] = "mixed: FP32 tangent + FP32 Jacobi-CG to %g, FP64 Newton refinement" % (
+            args.mixed_cg_rtol)
+        chosen["speedup_vs_plain"] = ms_dev / chosen["ms_per_newton_iter"]
 
     # roofline of the dominant kernel (CG block SpMV), CUDA events on the library stream
     ms_spmv = A.profile_spmv(reps=20)

@@ -215,18 +215,21 @@ int32_t ipfem_color_elements(int32_t n_elements, int32_t n_nodes, const int32_t 
 
 /* ------------------------------------------------- learned preconditioner */
 /* None of these has a counterpart in the reference.  A per-node MLP
- * (32 -> 128 -> 128 -> 36, BF16 weights, FP32 accumulation on the tensor
+ * (32 -> 128 -> 128 -> 20, BF16 weights, FP32 accumulation on the tensor
  * cores) maps the FP32 tangent around node i of a structured node grid
- * (node = b*gr + a) to one block row O_i[9][2][2] of a 3x3-patch operator
+ * (node = b*gr + a) to its block row of a sparse triangular factor G
  * (patch position k = 3*(db+1) + (da+1), da, db in {-1, 0, 1}).  Features:
  * X_i[4m + 2p + q] = K_ij[p][q] s_i[p] s_j[q] for the 8 neighbours j in k
  * order without the centre, s = sqrt(Jacobi inverse diagonal), 0 on Dirichlet
- * dofs.  Operator: M_ik[p][q] = s_i[p] ((O_ik[p][q] + O_j(8-k)[q][p]) / 2 +
- * (k == 4) (p == q)) s_j[q], symmetric by construction; O = 0 is Jacobi.  The
- * network runs once per tangent, M is applied in every iteration of flexible
- * CG (Polak-Ribiere), which falls back to Jacobi-PCG when it stagnates.
- * Requires IPFEM_MIXED.  Parameters are one FP32 vector of 25380 values:
- * W1[32][128] b1[128] W2[128][128] b2[128] W3[128][36] b3[36]. */
+ * dofs.  Factor: G_ik = O_i[4k..4k+3] (row-major 2x2) for k = 0..3,
+ * G_i4 = [[exp(O_i[16]), 0], [O_i[17], exp(O_i[18])]], entries touching a
+ * Dirichlet dof 0.  Operator: M = diag(s) G^T G diag(s), symmetric positive
+ * definite on the free dofs by construction; O = 0 is Jacobi.  The network
+ * runs once per tangent; G and G^T are applied (two stencil passes) in every
+ * iteration of flexible CG (Polak-Ribiere), which falls back to Jacobi-PCG
+ * when it stagnates.  Requires IPFEM_MIXED.  Parameters are one FP32 vector
+ * of 23316 values: W1[32][128] b1[128] W2[128][128] b2[128] W3[128][20]
+ * b3[20]. */
 ipfem_status ipfem_set_node_grid(ipfem_ctx *ctx, int32_t gr, int32_t gt);
 /* allocates the network (He-uniform W1, W2; W3 = 0, zero biases) */
 ipfem_status ipfem_mlp_init(ipfem_ctx *ctx, uint64_t seed);
@@ -235,16 +238,20 @@ ipfem_status ipfem_mlp_get_params(ipfem_ctx *ctx, float *out);
 ipfem_status ipfem_mlp_set_params(ipfem_ctx *ctx, const float *in);
 /* features [n_nodes][32] (device) of the current FP32 tangent */
 ipfem_status ipfem_mlp_features(ipfem_ctx *ctx, float *d_X);
-/* network output [rows][36] (device) for device feature rows [rows][32] */
+/* network output [rows][20] (device) for device feature rows [rows][32] */
 ipfem_status ipfem_mlp_forward(ipfem_ctx *ctx, const float *d_X, int64_t rows, float *d_O);
-/* the patch operator of the current tangent, M[9][n_nodes][2][2] (device) */
+/* the factor G[5][n_nodes][2][2] of the current tangent (device) */
 ipfem_status ipfem_mlp_operator(ipfem_ctx *ctx, float *d_M);
-/* training pass on the current FP32 tangent over n_pairs (residual r_p,
- * solution increment e_p) pairs, FP32 device arrays [n_pairs][neq]:
- * loss = (1/n_pairs) sum_p |K e_p - K M r_p|^2 / |K e_p|^2 and its gradient
- * (host, 25380 floats; either pointer may be NULL) */
-ipfem_status ipfem_learn_grad(ipfem_ctx *ctx, const float *d_r, const float *d_e, int n_pairs, float *grads,
-                              float *loss);
+/* training pass on the current FP32 tangent: the loss
+ *   w_kaporin * (log(tr(G A G^T) / nf) - (2/nf) log det G)
+ *   + w_pairs * (1/n_pairs) sum_p |K e_p - K M r_p|^2 / |K e_p|^2
+ * (A = diag(s) K diag(s), nf free dofs; the first line is the log of
+ * Kaporin's condition number of M K up to a constant) over n_pairs >= 0
+ * (residual r_p, solution increment e_p) pairs, FP32 device arrays
+ * [n_pairs][neq], and its gradient (host, 23316 floats; grads and loss may
+ * be NULL) */
+ipfem_status ipfem_learn_grad(ipfem_ctx *ctx, const float *d_r, const float *d_e, int n_pairs, float w_kaporin,
+                              float w_pairs, float *grads, float *loss);
 /* one Adam step (beta 0.9, 0.999) with the host gradient, or with the
  * context's last gradient when grads is NULL */
 ipfem_status ipfem_mlp_adam(ipfem_ctx *ctx, const float *grads, float lr);

@@ -18,7 +18,7 @@ LIB_PATH = os.path.join(HERE, "libipfem.so")
 HOST, DEVICE = 0, 1
 PLAIN_FP64, MIXED = 0, 1
 PREC_JACOBI, PREC_MLP = 0, 1
-MLP_PARAMS = 25380
+MLP_PARAMS = 23316
 STATUS = {0: "ok", 1: "not converged", 2: "non-finite value", 3: "CG breakdown", 4: "out of device memory",
           5: "invalid argument", 6: "CUDA error", 7: "no sm_103 device"}
 
@@ -114,7 +114,7 @@ def lib():
             "ipfem_mlp_features": (S, [P, P]),
             "ipfem_mlp_forward": (S, [P, P, C.c_int64, P]),
             "ipfem_mlp_operator": (S, [P, P]),
-            "ipfem_learn_grad": (S, [P, P, P, S, C.POINTER(C.c_float), C.POINTER(C.c_float)]),
+            "ipfem_learn_grad": (S, [P, P, P, S, C.c_float, C.c_float, C.POINTER(C.c_float), C.POINTER(C.c_float)]),
             "ipfem_mlp_adam": (S, [P, C.POINTER(C.c_float), C.c_float]),
             "ipfem_cg_snapshots": (S, [P, P, C.c_double, S, S, _ip, P, P, P, C.POINTER(C.c_int)]),
             "ipfem_gather_strain": (S, [P, P, P]),
@@ -373,18 +373,21 @@ class ElastoPlasticIntPointsStructMatrix:
         self._check(lib().ipfem_mlp_features(self._ctx, _ptr(d_X)))
 
     def mlp_forward(self, d_X, rows, d_O):
-        """network output [rows][36] of device feature rows [rows][32]"""
+        """network output [rows][20] of device feature rows [rows][32]"""
         self._check(lib().ipfem_mlp_forward(self._ctx, _ptr(d_X), int(rows), _ptr(d_O)))
 
     def mlp_operator(self, d_M):
-        """the patch operator [9][n_nodes][2][2] of the current tangent (device)"""
+        """the triangular factor G[5][n_nodes][2][2] of the current tangent (device)"""
         self._check(lib().ipfem_mlp_operator(self._ctx, _ptr(d_M)))
 
-    def learn_grad(self, d_r, d_e, n_pairs):
-        """loss and parameter gradient over (residual, increment) pairs [n_pairs][neq] (FP32, device)"""
+    def learn_grad(self, d_r, d_e, n_pairs, w_kaporin=1.0, w_pairs=1.0):
+        """loss and parameter gradient: Kaporin term plus the (residual, increment)
+        pairs [n_pairs][neq] (FP32, device; None with n_pairs = 0)"""
         g = np.zeros(MLP_PARAMS, np.float32)
         loss = np.zeros(1, np.float32)
-        self._check(lib().ipfem_learn_grad(self._ctx, _ptr(d_r), _ptr(d_e), int(n_pairs),
+        self._check(lib().ipfem_learn_grad(self._ctx, _ptr(d_r) if d_r is not None else None,
+                                           _ptr(d_e) if d_e is not None else None, int(n_pairs),
+                                           float(w_kaporin), float(w_pairs),
                                            g.ctypes.data_as(C.POINTER(C.c_float)),
                                            loss.ctypes.data_as(C.POINTER(C.c_float))))
         return g, float(loss[0])

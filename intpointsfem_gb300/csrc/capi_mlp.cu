@@ -49,22 +49,47 @@ ipfem_status need_tangent(ipfem_ctx *c)
     return IPFEM_OK;
 }
 
+// SELL slot of block (row, col) or -1
+int32_t block_slot(const Setup &s, const SellLayout &L, int32_t row, int32_t col)
+{
+    const int32_t *c0 = s.col.data() + s.row_ptr[row], *c1 = s.col.data() + s.row_ptr[row + 1];
+    const int32_t *f = std::lower_bound(c0, c1, col);
+    return (f != c1 && *f == col) ? (int32_t)L.bsr_to_sell[s.row_ptr[row] + (f - c0)] : -1;
+}
+
+int32_t grid_nbr(int64_t i, int k, int32_t gr, int32_t gt)
+{
+    const int a = (int)(i % gr) + k % 3 - 1, b = (int)(i / gr) + k / 3 - 1;
+    return (a < 0 || b < 0 || a >= gr || b >= gt) ? -1 : b * gr + a;
+}
+
 // slot[k][i]: FP32-tangent slot of block (i, nbr(i, k)) or -1
 std::vector<int32_t> patch_slots(const Setup &s, const SellLayout &L, int32_t gr, int32_t gt)
 {
     const int64_t n = s.n_nodes;
     std::vector<int32_t> slot((size_t)9 * n, -1);
-    for (int64_t i = 0; i < n; i++) {
-        const int a = (int)(i % gr), b = (int)(i / gr);
-        const int32_t *c0 = s.col.data() + s.row_ptr[i], *c1 = s.col.data() + s.row_ptr[i + 1];
+    for (int64_t i = 0; i < n; i++)
         for (int k = 0; k < 9; k++) {
-            const int aa = a + k % 3 - 1, bb = b + k / 3 - 1;
-            if (aa < 0 || bb < 0 || aa >= gr || bb >= gt) continue;
-            const int32_t j = bb * gr + aa;
-            const int32_t *f = std::lower_bound(c0, c1, j);
-            if (f != c1 && *f == j) slot[(size_t)k * n + i] = (int32_t)L.bsr_to_sell[s.row_ptr[i] + (f - c0)];
+            const int32_t j = grid_nbr(i, k, gr, gt);
+            if (j >= 0) slot[(size_t)k * n + i] = block_slot(s, L, (int32_t)i, j);
         }
-    }
+    return slot;
+}
+
+// pslot[5k + l][i]: slot of block (nbr(i, k), nbr(i, l)) for k, l < 5, or -1
+std::vector<int32_t> pair_slots(const Setup &s, const SellLayout &L, int32_t gr, int32_t gt)
+{
+    const int64_t n = s.n_nodes;
+    std::vector<int32_t> slot((size_t)25 * n, -1);
+    for (int64_t i = 0; i < n; i++)
+        for (int k = 0; k < 5; k++) {
+            const int32_t jk = grid_nbr(i, k, gr, gt);
+            if (jk < 0) continue;
+            for (int l = 0; l < 5; l++) {
+                const int32_t jl = grid_nbr(i, l, gr, gt);
+                if (jl >= 0) slot[(size_t)(5 * k + l) * n + i] = block_slot(s, L, jk, jl);
+            }
+        }
     return slot;
 }
 
@@ -142,17 +167,25 @@ ipfem_status ipfem_mlp_init(ipfem_ctx *c, uint64_t seed)
         MK(alloc(&m.v, kMlpParams));
         MK(cudaMalloc(&m.w1t, 128 * 32 * 2));
         MK(cudaMalloc(&m.w2t, 128 * 128 * 2));
-        MK(cudaMalloc(&m.w3t, 40 * 128 * 2));
+        MK(cudaMalloc(&m.w3t, 24 * 128 * 2));
         MK(alloc(&m.X, (size_t)s.n_nodes * 32));
-        MK(alloc(&m.O, (size_t)s.n_nodes * 36));
-        MK(alloc(&m.M, (size_t)s.n_nodes * 36));
+        MK(alloc(&m.O, (size_t)s.n_nodes * 20));
+        MK(alloc(&m.M, (size_t)s.n_nodes * 20));
         MK(alloc(&m.r_old, (size_t)s.neq));
+        MK(alloc(&m.y, (size_t)s.neq));
         MK(alloc(&m.loss, 1));
         MK(alloc(&m.scal, 2));
         const std::vector<int32_t> slot = patch_slots(s, c->mx.sell, m.gr, m.gt);
         MK(alloc(&m.slot, slot.size()));
         MK(cudaMemcpyAsync(m.slot, slot.data(), slot.size() * sizeof(int32_t), cudaMemcpyHostToDevice, c->stream));
+        const std::vector<int32_t> pslot = pair_slots(s, c->mx.sell, m.gr, m.gt);
+        MK(alloc(&m.pslot, pslot.size()));
+        MK(cudaMemcpyAsync(m.pslot, pslot.data(), pslot.size() * sizeof(int32_t), cudaMemcpyHostToDevice,
+                           c->stream));
         MK(cudaStreamSynchronize(c->stream));
+        int64_t nf = 0;
+        for (uint8_t f : s.fixed) nf += f ? 0 : 1;
+        m.nf = (float)std::max<int64_t>(1, nf);
     }
     // He-uniform W1, W2; W3 = 0 and zero biases, so the initial operator is Jacobi
     std::vector<float> p(kMlpParams, 0.f);
@@ -239,19 +272,21 @@ ipfem_status ipfem_mlp_operator(ipfem_ctx *c, float *d_M)
     if (st != IPFEM_OK) return st;
     if (!d_M) return mfail(c, IPFEM_INVALID, "bad args");
     if (!c->mlp.op_valid) launch_patch_operator(c);
-    MK(cudaMemcpyAsync(d_M, c->mlp.M, (size_t)c->s.n_nodes * 36 * sizeof(float), cudaMemcpyDeviceToDevice,
+    MK(cudaMemcpyAsync(d_M, c->mlp.M, (size_t)c->s.n_nodes * 20 * sizeof(float), cudaMemcpyDeviceToDevice,
                        c->stream));
     MK(cudaStreamSynchronize(c->stream));
     MK(cudaGetLastError());
     return IPFEM_OK;
 }
 
-ipfem_status ipfem_learn_grad(ipfem_ctx *c, const float *d_r, const float *d_e, int n_pairs, float *grads,
-                              float *loss)
+ipfem_status ipfem_learn_grad(ipfem_ctx *c, const float *d_r, const float *d_e, int n_pairs, float w_kaporin,
+                              float w_pairs, float *grads, float *loss)
 {
     ipfem_status st = need_tangent(c);
     if (st != IPFEM_OK) return st;
-    if (!d_r || !d_e || n_pairs < 1) return mfail(c, IPFEM_INVALID, "bad args");
+    if (n_pairs < 0 || (n_pairs > 0 && (!d_r || !d_e)) || !(w_kaporin >= 0.f) || !(w_pairs >= 0.f) ||
+        !std::isfinite(w_kaporin) || !std::isfinite(w_pairs))
+        return mfail(c, IPFEM_INVALID, "bad args");
     MlpBuffers &m = c->mlp;
     const Setup &s = c->s;
     if (!m.H1) {
@@ -260,11 +295,11 @@ ipfem_status ipfem_learn_grad(ipfem_ctx *c, const float *d_r, const float *d_e, 
         MK(alloc(&m.H2, n * 128));
         MK(alloc(&m.dH1, n * 128));
         MK(alloc(&m.dH2, n * 128));
-        MK(alloc(&m.dN, n * 36));
-        MK(alloc(&m.vec, (size_t)s.neq * 5));
+        MK(alloc(&m.dN, n * 20));
+        MK(alloc(&m.vec, (size_t)s.neq * 7));
         MK(alloc(&m.part, std::max(patch_part_floats(s.n_nodes), (size_t)2 * ((s.neq + 255) / 256))));
     }
-    patch_learn_grad(c, d_r, d_e, n_pairs);
+    patch_learn_grad(c, d_r, d_e, n_pairs, w_kaporin, w_pairs);
     if (grads) MK(cudaMemcpyAsync(grads, m.grads, kMlpParams * sizeof(float), cudaMemcpyDeviceToHost, c->stream));
     if (loss) MK(cudaMemcpyAsync(loss, m.loss, sizeof(float), cudaMemcpyDeviceToHost, c->stream));
     MK(cudaStreamSynchronize(c->stream));

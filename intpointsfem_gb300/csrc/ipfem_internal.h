@@ -116,25 +116,28 @@ namespace ipfem {
 // learned preconditioner (per-node MLP -> symmetric 3x3-patch operator) and
 // its training state
 struct MlpBuffers {
-    float *params = nullptr;      // FP32 master: W1[32][128] b1[128] W2[128][128] b2[128] W3[128][36] b3[36]
+    float *params = nullptr;      // FP32 master: W1[32][128] b1[128] W2[128][128] b2[128] W3[128][20] b3[20]
     float *grads = nullptr, *m = nullptr, *v = nullptr;
-    void *w1t = nullptr, *w2t = nullptr, *w3t = nullptr;   // BF16 [128][32], [128][128], [40][128] (n, k)
+    void *w1t = nullptr, *w2t = nullptr, *w3t = nullptr;   // BF16 [128][32], [128][128], [24][128] (n, k)
     int32_t *slot = nullptr;      // [9][n_nodes] FP32-tangent slot of block (i, nbr(i, k)) or -1
+    int32_t *pslot = nullptr;     // [25][n_nodes] slot of block (nbr(i, k), nbr(i, l)), k, l < 5, or -1
+    float nf = 0.f;               // number of free dofs
     float *X = nullptr;           // [n_nodes][32] features of the current tangent
-    float *O = nullptr;           // [n_nodes][36] network output
-    float *M = nullptr;           // [9][n_nodes][4] patch operator
+    float *O = nullptr;           // [n_nodes][20] network output
+    float *M = nullptr;           // [5][n_nodes][4] triangular factor G (M = sigma G^T G sigma)
+    float *y = nullptr;           // [neq] first stencil pass of the preconditioner
     float *r_old = nullptr;       // flexible-CG previous residual
     float *loss = nullptr, *scal = nullptr;
     // training scratch (allocated by the first gradient pass)
     float *H1 = nullptr, *H2 = nullptr, *dH1 = nullptr, *dH2 = nullptr, *dN = nullptr, *part = nullptr;
-    float *vec = nullptr;         // 5 x neq
+    float *vec = nullptr;         // 7 x neq
     int32_t gr = 0, gt = 0;       // structured node grid (gr x gt)
     int64_t adam_t = 0;
     bool ready = false, op_valid = false;
 };
-constexpr int kMlpParams = 32 * 128 + 128 + 128 * 128 + 128 + 128 * 36 + 36;
-constexpr int kOffW1 = 0, kOffB1 = 4096, kOffW2 = 4224, kOffB2 = 20608, kOffW3 = 20736, kOffB3 = 25344;
-static_assert(kOffB3 + 36 == kMlpParams, "parameter layout");
+constexpr int kMlpParams = 32 * 128 + 128 + 128 * 128 + 128 + 128 * 20 + 20;
+constexpr int kOffW1 = 0, kOffB1 = 4096, kOffW2 = 4224, kOffB2 = 20608, kOffW3 = 20736, kOffB3 = 23296;
+static_assert(kOffB3 + 20 == kMlpParams, "parameter layout");
 }  // namespace ipfem
 
 struct ipfem_ctx {
@@ -217,6 +220,6 @@ void launch_patch_operator(ipfem_ctx *c);
 void launch_fcg_init(ipfem_ctx *c, const double *d_b, double scale, float rtol, int max_it);
 void launch_fcg_iteration(ipfem_ctx *c);
 size_t patch_part_floats(int64_t n_nodes);
-void patch_learn_grad(ipfem_ctx *c, const float *d_r, const float *d_e, int P);
+void patch_learn_grad(ipfem_ctx *c, const float *d_r, const float *d_e, int P, float wk, float wp);
 void mlp_adam_step(ipfem_ctx *c, float lr);
 }  // namespace ipfem

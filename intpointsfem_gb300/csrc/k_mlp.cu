@@ -1,18 +1,25 @@
-// Learned preconditioner: a per-node MLP (32 -> 128 -> 128 -> 36) that maps the
-// FP32 tangent around a node to one block row of a symmetric 3x3-patch
-// operator M, applied inside flexible CG.  No counterpart in the reference.
+// Learned preconditioner: a per-node MLP (32 -> 128 -> 128 -> 20) that maps the
+// FP32 tangent around a node to its block row of a sparse triangular factor
+// G, used as M = diag(sigma) G^T G diag(sigma) inside flexible CG.  No
+// counterpart in the reference.
 //
 // Node i = b*gr + a of a structured node grid; patch position k = 3*(db+1) +
 // (da+1) for da, db in {-1, 0, 1} (k = 4 is the node itself, 8 - k the mirror).
-// With sigma = sqrt(Dinv) per dof (0 on Dirichlet dofs):
+// With sigma = sqrt(Dinv) per dof (0 on Dirichlet dofs) and f = (sigma > 0):
 //   features  X_i[4m + 2p + q] = K_ij[p][q] sigma_i[p] sigma_j[q] for the 8
 //             neighbours j (m-th non-centre position), 0 outside the grid or
 //             where the couplings are absent from the tangent;
-//   network   O_i[9][2][2] = W3^T relu(W2^T relu(W1^T X_i + b1) + b2) + b3;
-//   operator  Mhat_ik = (O_ik + O_{j,8-k}^T) / 2 + (k == 4 ? I : 0),
-//             M_ik[p][q] = sigma_i[p] Mhat_ik[p][q] sigma_j[q],
-// so M is symmetric by construction and O = 0 gives Jacobi exactly.  The
-// network runs once per tangent; each CG iteration applies M, a 9-block stencil.
+//   network   O_i[20] = W3^T relu(W2^T relu(W1^T X_i + b1) + b2) + b3;
+//   factor    G_ik = O_i[4k..4k+3] (row-major 2x2) for the lower neighbours
+//             k = 0..3, G_i4 = [[exp(O_i[16]), 0], [O_i[17], exp(O_i[18])]],
+//             each entry times f_i[p] f_j[q];
+//   operator  M = diag(sigma) G^T G diag(sigma),
+// symmetric positive definite on the free dofs by construction (G is block
+// triangular in node order with a positive diagonal) and Jacobi for O = 0.
+// The network runs once per tangent; each CG iteration applies G and G^T
+// (two 5-block stencil passes).  Training minimises the log of Kaporin's
+// condition number of M K plus the residual of the plain solver's
+// (residual, increment) pairs.
 //
 // GEMMs run on the tensor cores in BF16 (operands rounded to BF16 in shared
 // memory) with FP32 accumulation (mma.m16n8k16).
@@ -244,13 +251,13 @@ __global__ void __launch_bounds__(256) k_patch_features(int32_t n, GridInfo G, c
 // layers (A operands are the warp's own rows, so the layers need only
 // __syncwarp).  Weights are staged once per persistent CTA.
 constexpr int PT = 128;          // nodes per tile
-constexpr int NOUT = 36, NOUTP = 40;
+constexpr int NOUT = 20, NOUTP = 24;
 
 struct NetDev {
     const __nv_bfloat16 *w1t;   // [128][32]  (n, k)
     const __nv_bfloat16 *w2t;   // [128][128] (n, k)
-    const __nv_bfloat16 *w3t;   // [40][128]  (n, k), rows 36..39 zero
-    const float *b1, *b2, *b3;  // [128], [128], [36]
+    const __nv_bfloat16 *w3t;   // [24][128]  (n, k), rows 20..23 zero
+    const float *b1, *b2, *b3;  // [128], [128], [20]
 };
 
 struct __align__(16) NetSmem {
@@ -314,8 +321,8 @@ __device__ __forceinline__ void warp_store_hidden(NetSmem &S, const float *b, in
     __syncwarp();
 }
 
-// network of the warp's 16 rows of S.x; out[j][r] as acc above for 40 columns
-__device__ void net_tile(NetSmem &S, int warp, int lane, float (&out)[5][4])
+// network of the warp's 16 rows of S.x; out[j][r] as acc above for 24 columns
+__device__ void net_tile(NetSmem &S, int warp, int lane, float (&out)[3][4])
 {
     const int g = lane >> 2, t = lane & 3;
     const int r0 = 16 * warp + g;
@@ -329,7 +336,7 @@ __device__ void net_tile(NetSmem &S, int warp, int lane, float (&out)[5][4])
     warp_gemm128<128, 136>(S.h, S.w2, r0, g, t, acc);
     warp_store_hidden(S, S.b2, r0, t, acc);
 #pragma unroll
-    for (int j = 0; j < 5; j++)
+    for (int j = 0; j < 3; j++)
 #pragma unroll
         for (int r = 0; r < 4; r++) out[j][r] = 0.f;
 #pragma unroll
@@ -340,7 +347,7 @@ __device__ void net_tile(NetSmem &S, int warp, int lane, float (&out)[5][4])
         af[2] = *reinterpret_cast<const uint32_t *>(&S.h[r0][ks + 8 + 2 * t]);
         af[3] = *reinterpret_cast<const uint32_t *>(&S.h[r0 + 8][ks + 8 + 2 * t]);
 #pragma unroll
-        for (int j = 0; j < 5; j++) {
+        for (int j = 0; j < 3; j++) {
             uint32_t bf[2];
             bf[0] = *reinterpret_cast<const uint32_t *>(&S.w3[8 * j + g][ks + 2 * t]);
             bf[1] = *reinterpret_cast<const uint32_t *>(&S.w3[8 * j + g][ks + 8 + 2 * t]);
@@ -348,7 +355,7 @@ __device__ void net_tile(NetSmem &S, int warp, int lane, float (&out)[5][4])
         }
     }
 #pragma unroll
-    for (int j = 0; j < 5; j++) {
+    for (int j = 0; j < 3; j++) {
         const int c = 8 * j + 2 * t;
         out[j][0] += S.b3[c];
         out[j][1] += S.b3[c + 1];
@@ -357,7 +364,7 @@ __device__ void net_tile(NetSmem &S, int warp, int lane, float (&out)[5][4])
     }
 }
 
-// O[rows][36] = network(X[rows][32]); persistent CTAs over 128-row tiles
+// O[rows][20] = network(X[rows][32]); persistent CTAs over 128-row tiles
 __global__ void __launch_bounds__(256) k_patch_net(int64_t rows, const float *__restrict__ X, NetDev W,
                                                    float *__restrict__ O)
 {
@@ -377,14 +384,14 @@ __global__ void __launch_bounds__(256) k_patch_net(int64_t rows, const float *__
             *reinterpret_cast<uint32_t *>(&S.x[row][c2]) = pack_bf16(v.x, v.y);
         }
         __syncthreads();
-        float out[5][4];
+        float out[3][4];
         net_tile(S, warp, lane, out);
 #pragma unroll
         for (int h = 0; h < 2; h++) {
             const int64_t row = base + 16 * warp + g + 8 * h;
             if (row >= rows) continue;
 #pragma unroll
-            for (int j = 0; j < 5; j++) {
+            for (int j = 0; j < 3; j++) {
                 const int c = 8 * j + 2 * t;
                 if (c < NOUT)
                     *reinterpret_cast<float2 *>(O + row * NOUT + c) = make_float2(out[j][2 * h], out[j][2 * h + 1]);
@@ -393,54 +400,89 @@ __global__ void __launch_bounds__(256) k_patch_net(int64_t rows, const float *__
     }
 }
 
-// M[k][i] (float4, row-major 2x2) from the network output O[n][36]
-__global__ void __launch_bounds__(256) k_patch_build(int32_t n, GridInfo G, const float *__restrict__ O,
-                                                     const float2 *__restrict__ dinv, float4 *__restrict__ M)
+__device__ __forceinline__ float2 free2(float2 d)
+{
+    return make_float2(d.x > 0.f ? 1.f : 0.f, d.y > 0.f ? 1.f : 0.f);
+}
+
+constexpr int NTRI = 5;          // factor blocks per node: k = 0..3 and the node (k = 4)
+
+// G[k][i] (float4, row-major 2x2, k = 0..4) from the network output O[n][20]
+__global__ void __launch_bounds__(256) k_tri_build(int32_t n, GridInfo G, const float *__restrict__ O,
+                                                   const float2 *__restrict__ dinv, float4 *__restrict__ Gm)
 {
     const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    const float2 si = sqrt2(dinv[i]);
+    const float2 fi = free2(dinv[i]);
     const float *oi = O + (int64_t)i * NOUT;
 #pragma unroll
-    for (int k = 0; k < 9; k++) {
+    for (int k = 0; k < 4; k++) {
         const int32_t j = patch_nbr(i, k, G);
-        float4 mk = make_float4(0.f, 0.f, 0.f, 0.f);
+        float4 gk = make_float4(0.f, 0.f, 0.f, 0.f);
         if (j >= 0) {
-            const float *oj = O + (int64_t)j * NOUT + 4 * (8 - k);
-            const float e = (k == 4) ? 1.f : 0.f;
-            const float m00 = 0.5f * (oi[4 * k + 0] + oj[0]) + e;
-            const float m01 = 0.5f * (oi[4 * k + 1] + oj[2]);
-            const float m10 = 0.5f * (oi[4 * k + 2] + oj[1]);
-            const float m11 = 0.5f * (oi[4 * k + 3] + oj[3]) + e;
-            const float2 sj = sqrt2(dinv[j]);
-            mk = make_float4(si.x * m00 * sj.x, si.x * m01 * sj.y, si.y * m10 * sj.x, si.y * m11 * sj.y);
+            const float2 fj = free2(dinv[j]);
+            gk = make_float4(oi[4 * k] * fi.x * fj.x, oi[4 * k + 1] * fi.x * fj.y, oi[4 * k + 2] * fi.y * fj.x,
+                             oi[4 * k + 3] * fi.y * fj.y);
         }
-        M[(int64_t)k * n + i] = mk;
+        Gm[(int64_t)k * n + i] = gk;
     }
+    Gm[(int64_t)4 * n + i] = make_float4(expf(oi[16]) * fi.x, 0.f, oi[17] * fi.y * fi.x, expf(oi[18]) * fi.y);
 }
 
-// z_i = sum_k M[k][i] r_nbr(i,k)
-__device__ __forceinline__ float2 patch_apply(int32_t i, int32_t n, GridInfo G, const float4 *__restrict__ M,
-                                              const float2 *__restrict__ r)
+// y_i = sum_k G_ik (sigma * x)_nbr(i,k)
+__device__ __forceinline__ float2 tri_mul(int32_t i, int32_t n, GridInfo G, const float4 *__restrict__ Gm,
+                                          const float2 *__restrict__ dinv, const float2 *__restrict__ x)
+{
+    float2 y = make_float2(0.f, 0.f);
+#pragma unroll
+    for (int k = 0; k < NTRI; k++) {
+        const int32_t j = patch_nbr(i, k, G);
+        if (j < 0) continue;
+        const float4 m = __ldg(&Gm[(int64_t)k * n + i]);
+        const float2 s = sqrt2(__ldg(&dinv[j])), v = __ldg(&x[j]);
+        const float vx = s.x * v.x, vy = s.y * v.y;
+        y.x = fmaf(m.x, vx, fmaf(m.y, vy, y.x));
+        y.y = fmaf(m.z, vx, fmaf(m.w, vy, y.y));
+    }
+    return y;
+}
+
+// z_j = sigma_j * sum_k G_{i,k}^T y_i over the nodes i = nbr(j, 8-k) that
+// hold j at position k (gather form of G^T)
+__device__ __forceinline__ float2 trit_mul(int32_t j, int32_t n, GridInfo G, const float4 *__restrict__ Gm,
+                                           const float2 *__restrict__ dinv, const float2 *__restrict__ y)
 {
     float2 z = make_float2(0.f, 0.f);
 #pragma unroll
-    for (int k = 0; k < 9; k++) {
-        const int32_t j = patch_nbr(i, k, G);
-        if (j < 0) continue;
-        const float4 m = __ldg(&M[(int64_t)k * n + i]);
-        const float2 v = __ldg(&r[j]);
-        z.x = fmaf(m.x, v.x, fmaf(m.y, v.y, z.x));
-        z.y = fmaf(m.z, v.x, fmaf(m.w, v.y, z.y));
+    for (int k = 0; k < NTRI; k++) {
+        const int32_t i = patch_nbr(j, 8 - k, G);
+        if (i < 0) continue;
+        const float4 m = __ldg(&Gm[(int64_t)k * n + i]);
+        const float2 v = __ldg(&y[i]);
+        z.x = fmaf(m.x, v.x, fmaf(m.z, v.y, z.x));
+        z.y = fmaf(m.y, v.x, fmaf(m.w, v.y, z.y));
     }
-    return z;
+    const float2 s = sqrt2(dinv[j]);
+    return make_float2(s.x * z.x, s.y * z.y);
 }
 
-__global__ void __launch_bounds__(256) k_patch_apply(int32_t n, GridInfo G, const float4 *__restrict__ M,
-                                                     const float2 *__restrict__ r, float2 *__restrict__ z)
+// y = G (sigma * r); skipped once the solve is done when sc is given
+__global__ void __launch_bounds__(256) k_tri_first(int32_t n, GridInfo G, const float4 *__restrict__ Gm,
+                                                   const float2 *__restrict__ dinv, const float2 *__restrict__ r,
+                                                   float2 *__restrict__ y, const CGScalarsT<float> *sc)
 {
+    if (sc && *reinterpret_cast<const volatile int *>(&sc->done)) return;
     const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) z[i] = patch_apply(i, n, G, M, r);
+    if (i < n) y[i] = tri_mul(i, n, G, Gm, dinv, r);
+}
+
+// z = sigma * (G^T y)
+__global__ void __launch_bounds__(256) k_tri_second(int32_t n, GridInfo G, const float4 *__restrict__ Gm,
+                                                    const float2 *__restrict__ dinv, const float2 *__restrict__ y,
+                                                    float2 *__restrict__ z)
+{
+    const int32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j < n) z[j] = trit_mul(j, n, G, Gm, dinv, y);
 }
 
 // ------------------------------------------------------ flexible CG (FP32)
@@ -590,21 +632,22 @@ __global__ void __launch_bounds__(256) k_fcg_update(int32_t n_nodes, const float
     }
 }
 
-// z = M r, partial r.z and r_old.z; last CTA: Polak-Ribiere
-// beta = (r.z - r_old.z) / rz_prev (clipped at 0), rz = r.z
-__global__ void __launch_bounds__(256) k_patch_precond(int32_t n, GridInfo G, const float4 *__restrict__ M,
-                                                       const float *__restrict__ r, const float *__restrict__ r_old,
-                                                       float *__restrict__ z, float *part, int64_t n_part,
-                                                       unsigned *ticket, CGScalarsT<float> *sc)
+// z = M r = sigma * (G^T y) with y = G (sigma * r) from k_tri_first; partial
+// r.z and r_old.z; last CTA: Polak-Ribiere beta = (r.z - r_old.z) / rz_prev
+// (clipped at 0), rz = r.z
+__global__ void __launch_bounds__(256) k_tri_precond(int32_t n, GridInfo G, const float4 *__restrict__ Gm,
+                                                     const float2 *__restrict__ dinv, const float2 *__restrict__ y,
+                                                     const float *__restrict__ r, const float *__restrict__ r_old,
+                                                     float *__restrict__ z, float *part, int64_t n_part,
+                                                     unsigned *ticket, CGScalarsT<float> *sc)
 {
     if (*reinterpret_cast<volatile int *>(&sc->done)) return;
     const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     float v[2] = {0.f, 0.f};
     if (i < n) {
-        const float2 *r2 = reinterpret_cast<const float2 *>(r);
-        const float2 zz = patch_apply(i, n, G, M, r2);
+        const float2 zz = trit_mul(i, n, G, Gm, dinv, y);
         reinterpret_cast<float2 *>(z)[i] = zz;
-        const float2 rr = r2[i], ro = reinterpret_cast<const float2 *>(r_old)[i];
+        const float2 rr = reinterpret_cast<const float2 *>(r)[i], ro = reinterpret_cast<const float2 *>(r_old)[i];
         v[0] = fmaf(rr.y, zz.y, rr.x * zz.x);
         v[1] = fmaf(ro.y, zz.y, ro.x * zz.x);
     }
@@ -716,31 +759,160 @@ __global__ void __launch_bounds__(256) k_res_final(int n_part, const float *__re
     }
 }
 
-// dO_ik[p][q] += c/2 (ghat_i[p] rhat_j[q] + rhat_i[p] ghat_j[q]) for the pair's
-// r and g = K (ae - az), with hats = sigma * (.) and c = -2 w / ae.ae
-__global__ void __launch_bounds__(256) k_patch_grad(int32_t n, GridInfo G, const float2 *__restrict__ dinv,
-                                                    const float2 *__restrict__ r, const float2 *__restrict__ g,
-                                                    const float *__restrict__ scal, float w, float *__restrict__ dO)
+// Pair term of dL/dG for z = sigma G^T G sigma r: with rh = sigma*r,
+// u = sigma*g (g = K (ae - az)), y = G rh, v = G u and c = -2 w / ae.ae,
+// dG_ik[p][q] += c (y_i[p] u_j[q] + v_i[p] rh_j[q]),  j = nbr(i, k)
+__global__ void __launch_bounds__(256) k_tri_grad_pairs(int32_t n, GridInfo G, const float2 *__restrict__ dinv,
+                                                        const float2 *__restrict__ r, const float2 *__restrict__ g,
+                                                        const float2 *__restrict__ y, const float2 *__restrict__ v,
+                                                        const float *__restrict__ scal, float w,
+                                                        float *__restrict__ dG)
 {
     const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n || !(scal[0] > 0.f)) return;
-    const float c = -w / scal[0];          // (-2 w / ae.ae) * 1/2
-    const float2 si = sqrt2(dinv[i]);
-    const float2 ri = make_float2(si.x * r[i].x, si.y * r[i].y);
-    const float2 gi = make_float2(si.x * g[i].x, si.y * g[i].y);
-    float *o = dO + (int64_t)i * NOUT;
+    const float c = -2.f * w / scal[0];
+    const float2 yi = y[i], vi = v[i];
+    float *o = dG + (int64_t)i * NOUT;
 #pragma unroll
-    for (int k = 0; k < 9; k++) {
+    for (int k = 0; k < NTRI; k++) {
         const int32_t j = patch_nbr(i, k, G);
         if (j < 0) continue;
         const float2 sj = sqrt2(dinv[j]);
         const float2 rj = make_float2(sj.x * r[j].x, sj.y * r[j].y);
-        const float2 gj = make_float2(sj.x * g[j].x, sj.y * g[j].y);
-        o[4 * k + 0] += c * (gi.x * rj.x + ri.x * gj.x);
-        o[4 * k + 1] += c * (gi.x * rj.y + ri.x * gj.y);
-        o[4 * k + 2] += c * (gi.y * rj.x + ri.y * gj.x);
-        o[4 * k + 3] += c * (gi.y * rj.y + ri.y * gj.y);
+        const float2 uj = make_float2(sj.x * g[j].x, sj.y * g[j].y);
+        o[4 * k + 0] += c * (yi.x * uj.x + vi.x * rj.x);
+        o[4 * k + 1] += c * (yi.x * uj.y + vi.x * rj.y);
+        o[4 * k + 2] += c * (yi.y * uj.x + vi.y * rj.x);
+        o[4 * k + 3] += c * (yi.y * uj.y + vi.y * rj.y);
     }
+}
+
+// Kaporin term, per node i with patch nodes j_k = nbr(i, k), k = 0..4:
+// H_ik[p][q] = sum_l sum_t Ahat[(j_k, q), (j_l, t)] G_il[p][t] with
+// Ahat = sigma K sigma (pslot[5k + l][i] = slot of block (j_k, j_l) or -1);
+// CTA partials of sum G.H (= the node's share of tr(G Ahat G^T)) and of the
+// log-diagonal sum f0 O[16] + f1 O[18] into part[2][gridDim.x]
+__global__ void __launch_bounds__(256) k_kap_H(int32_t n, GridInfo G, const float4 *__restrict__ Gm,
+                                               const float4 *__restrict__ K, const int32_t *__restrict__ pslot,
+                                               const float2 *__restrict__ dinv, const float *__restrict__ O,
+                                               float *__restrict__ H, float *__restrict__ part)
+{
+    __shared__ float ws[2][8];
+    const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    float tr = 0.f, ld = 0.f;
+    if (i < n) {
+        float4 gl[NTRI];
+        float2 sl[NTRI];
+#pragma unroll
+        for (int l = 0; l < NTRI; l++) {
+            gl[l] = Gm[(int64_t)l * n + i];
+            const int32_t j = patch_nbr(i, l, G);
+            sl[l] = j >= 0 ? sqrt2(dinv[j]) : make_float2(0.f, 0.f);
+        }
+        float *h = H + (int64_t)i * NOUT;
+#pragma unroll
+        for (int k = 0; k < NTRI; k++) {
+            float h00 = 0.f, h01 = 0.f, h10 = 0.f, h11 = 0.f;
+#pragma unroll
+            for (int l = 0; l < NTRI; l++) {
+                const int32_t s = pslot[(int64_t)(NTRI * k + l) * n + i];
+                if (s < 0) continue;
+                const float4 kb = K[s];
+                // Ahat[q][t] for q (row, node j_k), t (column, node j_l)
+                const float a00 = sl[k].x * kb.x * sl[l].x, a01 = sl[k].x * kb.y * sl[l].y;
+                const float a10 = sl[k].y * kb.z * sl[l].x, a11 = sl[k].y * kb.w * sl[l].y;
+                // H[p][q] += sum_t G_l[p][t] Ahat[q][t]
+                h00 += gl[l].x * a00 + gl[l].y * a01;
+                h01 += gl[l].x * a10 + gl[l].y * a11;
+                h10 += gl[l].z * a00 + gl[l].w * a01;
+                h11 += gl[l].z * a10 + gl[l].w * a11;
+            }
+            h[4 * k + 0] = h00;
+            h[4 * k + 1] = h01;
+            h[4 * k + 2] = h10;
+            h[4 * k + 3] = h11;
+            tr += gl[k].x * h00 + gl[k].y * h01 + gl[k].z * h10 + gl[k].w * h11;
+        }
+        const float2 f = free2(dinv[i]);
+        ld = f.x * O[(int64_t)i * NOUT + 16] + f.y * O[(int64_t)i * NOUT + 18];
+    }
+    tr = wsum(tr);
+    ld = wsum(ld);
+    const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
+    if (lane == 0) {
+        ws[0][wp] = tr;
+        ws[1][wp] = ld;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        float a = 0.f, b = 0.f;
+        for (int k = 0; k < 8; k++) {
+            a += ws[0][k];
+            b += ws[1][k];
+        }
+        part[blockIdx.x] = a;
+        part[gridDim.x + blockIdx.x] = b;
+    }
+}
+
+// scal[2] = T = tr(G Ahat G^T), scal[3] = sum of the log-diagonal;
+// loss += wk (log(T / nf) - 2 LD / nf)
+__global__ void __launch_bounds__(256) k_kap_final(int n_part, const float *__restrict__ part,
+                                                   float *__restrict__ scal, float *__restrict__ loss, float wk,
+                                                   float nf)
+{
+    __shared__ float ws[2][8];
+    float a = 0.f, b = 0.f;
+    for (int i = threadIdx.x; i < n_part; i += blockDim.x) {
+        a += part[i];
+        b += part[n_part + i];
+    }
+    a = wsum(a);
+    b = wsum(b);
+    const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
+    if (lane == 0) {
+        ws[0][wp] = a;
+        ws[1][wp] = b;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        float sa = 0.f, sb = 0.f;
+        for (int k = 0; k < 8; k++) {
+            sa += ws[0][k];
+            sb += ws[1][k];
+        }
+        scal[2] = sa;
+        scal[3] = sb;
+        *loss += wk * (logf(sa / nf) - 2.f * sb / nf);
+    }
+}
+
+// dL/dO from dG (pair term) + wk (2/T) H (Kaporin trace) through G(O), plus
+// the log-determinant term -2 wk / nf on O[16], O[18] of free dofs
+__global__ void __launch_bounds__(256) k_tri_dO(int32_t n, GridInfo G, const float *__restrict__ O,
+                                                const float2 *__restrict__ dinv, const float *__restrict__ dG,
+                                                const float *__restrict__ H, const float *__restrict__ scal, float wk,
+                                                float nf, float *__restrict__ dO)
+{
+    const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float ck = scal[2] > 0.f ? 2.f * wk / scal[2] : 0.f;
+    const float2 fi = free2(dinv[i]);
+    const float *gi = dG + (int64_t)i * NOUT, *hi = H + (int64_t)i * NOUT, *oi = O + (int64_t)i * NOUT;
+    float *d = dO + (int64_t)i * NOUT;
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        const int32_t j = patch_nbr(i, k, G);
+        const float2 fj = j >= 0 ? free2(dinv[j]) : make_float2(0.f, 0.f);
+        d[4 * k + 0] = (gi[4 * k + 0] + ck * hi[4 * k + 0]) * fi.x * fj.x;
+        d[4 * k + 1] = (gi[4 * k + 1] + ck * hi[4 * k + 1]) * fi.x * fj.y;
+        d[4 * k + 2] = (gi[4 * k + 2] + ck * hi[4 * k + 2]) * fi.y * fj.x;
+        d[4 * k + 3] = (gi[4 * k + 3] + ck * hi[4 * k + 3]) * fi.y * fj.y;
+    }
+    d[16] = ((gi[16] + ck * hi[16]) * expf(oi[16]) - 2.f * wk / nf) * fi.x;
+    d[17] = (gi[18] + ck * hi[18]) * fi.y * fi.x;
+    d[18] = ((gi[19] + ck * hi[19]) * expf(oi[18]) - 2.f * wk / nf) * fi.y;
+    d[19] = 0.f;
 }
 
 // ---------------------------------------------------------------- host side
@@ -814,7 +986,7 @@ void launch_patch_features(ipfem_ctx *c, float *d_X)
                                                              d_X);
 }
 
-// features -> network -> symmetric patch operator, for the current FP32 tangent
+// features -> network -> triangular factor, for the current FP32 tangent
 void launch_patch_operator(ipfem_ctx *c)
 {
     MlpBuffers &m = c->mlp;
@@ -822,11 +994,16 @@ void launch_patch_operator(ipfem_ctx *c)
     GridInfo G{m.gr, m.gt};
     launch_patch_features(c, m.X);
     launch_patch_net(c, n, m.X, m.O);
-    k_patch_build<<<(n + 255) / 256, 256, 0, c->stream>>>(n, G, m.O, reinterpret_cast<const float2 *>(c->mx.dinv),
-                                                          reinterpret_cast<float4 *>(m.M));
+    k_tri_build<<<(n + 255) / 256, 256, 0, c->stream>>>(n, G, m.O, reinterpret_cast<const float2 *>(c->mx.dinv),
+                                                        reinterpret_cast<float4 *>(m.M));
     c->launches += 3;
     m.op_valid = true;
 }
+
+// FCG gives up (and the caller falls back to Jacobi-PCG) after this many
+// iterations without a 2 % drop of |r|^2; M is SPD, so this only guards
+// against a network evaluated far outside its training data
+constexpr int kStallWindow = 2000;
 
 static unsigned fcg_grid(const ipfem_ctx *c)
 {
@@ -839,9 +1016,13 @@ static void launch_precond(ipfem_ctx *c)
     MixedBuffers &m = c->mx;
     // the precond partials use the FP64 partial array (as 2 x n_red floats)
     float *part = reinterpret_cast<float *>(c->d_part);
-    k_patch_precond<<<fcg_grid(c), 256, 0, c->stream>>>(c->s.n_nodes, G, reinterpret_cast<const float4 *>(c->mlp.M),
-                                                        m.r, c->mlp.r_old, m.z, part, (int64_t)fcg_grid(c),
-                                                        c->d_counters + 7, m.sc);
+    const float4 *Gm = reinterpret_cast<const float4 *>(c->mlp.M);
+    const float2 *d2 = reinterpret_cast<const float2 *>(m.dinv);
+    float2 *y = reinterpret_cast<float2 *>(c->mlp.y);
+    k_tri_first<<<fcg_grid(c), 256, 0, c->stream>>>(c->s.n_nodes, G, Gm, d2, reinterpret_cast<const float2 *>(m.r), y,
+                                                    m.sc);
+    k_tri_precond<<<fcg_grid(c), 256, 0, c->stream>>>(c->s.n_nodes, G, Gm, d2, y, m.r, c->mlp.r_old, m.z, part,
+                                                      (int64_t)fcg_grid(c), c->d_counters + 7, m.sc);
 }
 
 void launch_fcg_init(ipfem_ctx *c, const double *d_b, double scale, float rtol, int max_it)
@@ -858,7 +1039,7 @@ void launch_fcg_iteration(ipfem_ctx *c)
     MixedBuffers &m = c->mx;
     launch_cg32_spmv_only(c);
     k_fcg_update<<<fcg_grid(c), 256, 0, c->stream>>>(c->s.n_nodes, m.p, m.q, m.x, m.r, c->mlp.r_old, m.part,
-                                                     (int64_t)fcg_grid(c), c->d_counters + 6, m.sc, 400);
+                                                     (int64_t)fcg_grid(c), c->d_counters + 6, m.sc, kStallWindow);
     launch_precond(c);
     launch_cg32_pupdate_only(c);
 }
@@ -900,10 +1081,13 @@ size_t patch_part_floats(int64_t n_nodes)
     return (size_t)std::max<int64_t>(splits * 128 * 128, chunks * 128);
 }
 
-// Gradient of L = (1/P) sum_p |K e_p - K M r_p|^2 / |K e_p|^2 with respect to
-// the parameters (into mlp.grads) and L (into mlp.loss), for P pairs of
-// FP32 device vectors r_p = d_r + p*neq, e_p = d_e + p*neq on this tangent.
-void patch_learn_grad(ipfem_ctx *c, const float *d_r, const float *d_e, int P)
+// Gradient of
+//   L = wk (log(tr(G Ahat G^T) / nf) - (2/nf) log det G)
+//     + wp (1/P) sum_p |K e_p - K M r_p|^2 / |K e_p|^2   (M = sigma G^T G sigma)
+// with respect to the parameters (into mlp.grads) and L (into mlp.loss), for
+// P >= 0 pairs of FP32 device vectors r_p = d_r + p*neq, e_p = d_e + p*neq on
+// this tangent; nf = number of free dofs.
+void patch_learn_grad(ipfem_ctx *c, const float *d_r, const float *d_e, int P, float wk, float wp)
 {
     MlpBuffers &m = c->mlp;
     MixedBuffers &x = c->mx;
@@ -916,6 +1100,8 @@ void patch_learn_grad(ipfem_ctx *c, const float *d_r, const float *d_e, int P)
     const unsigned gn = (unsigned)((n + 255) / 256);
     const unsigned ge = (unsigned)((neq + 255) / 256);
     const unsigned eh = (unsigned)(((int64_t)n * 128 + 255) / 256);
+    const float2 *d2 = reinterpret_cast<const float2 *>(x.dinv);
+    float4 *Gm = reinterpret_cast<float4 *>(m.M);
     // forward through the GEMM path (keeps the hidden layers for the backward)
     launch_patch_features(c, m.X);
     gemm(c, n, 128, 32, m.X, 32, 0, W + kOffW1, 128, 0, m.H1, 128);
@@ -924,32 +1110,43 @@ void patch_learn_grad(ipfem_ctx *c, const float *d_r, const float *d_e, int P)
     k_bias_act<<<eh, 256, 0, st>>>(n, 128, m.H2, W + kOffB2, 1);
     gemm(c, n, NOUT, 128, m.H2, 128, 0, W + kOffW3, NOUT, 0, m.O, NOUT);
     k_bias_act<<<(unsigned)(((int64_t)n * NOUT + 255) / 256), 256, 0, st>>>(n, NOUT, m.O, W + kOffB3, 0);
-    k_patch_build<<<gn, 256, 0, st>>>(n, G, m.O, reinterpret_cast<const float2 *>(x.dinv),
-                                      reinterpret_cast<float4 *>(m.M));
-    m.op_valid = false;     // the operator now belongs to these parameters only if nothing changes them
-    // pairs
+    k_tri_build<<<gn, 256, 0, st>>>(n, G, m.O, d2, Gm);
+    m.op_valid = false;
     cudaMemsetAsync(m.dN, 0, (size_t)n * NOUT * sizeof(float), st);
     cudaMemsetAsync(m.loss, 0, sizeof(float), st);
+    // pair term
     float *z = m.vec, *ae = m.vec + neq, *az = m.vec + 2 * neq, *res = m.vec + 3 * neq, *g = m.vec + 4 * neq;
+    float *y = m.vec + 5 * neq, *v = m.vec + 6 * neq;
     const SellDev &L = x.dsell;
     const float4 *K4 = reinterpret_cast<const float4 *>(x.K);
-    const float w = 1.f / (float)P;
-    for (int p = 0; p < P; p++) {
-        const float *r = d_r + (size_t)p * neq, *e = d_e + (size_t)p * neq;
-        k_patch_apply<<<gn, 256, 0, st>>>(n, G, reinterpret_cast<const float4 *>(m.M),
-                                          reinterpret_cast<const float2 *>(r), reinterpret_cast<float2 *>(z));
-        k_spmv32<<<gn, 256, 0, st>>>(n, L.slice_base, L.rowlen, L.sell_node, L.sell_col, K4, c->d_fixed,
-                                     reinterpret_cast<const float2 *>(e), reinterpret_cast<float2 *>(ae));
+    const float w = P > 0 ? wp / (float)P : 0.f;
+    for (int p = 0; p < P && wp > 0.f; p++) {
+        const float2 *r2 = reinterpret_cast<const float2 *>(d_r + (size_t)p * neq);
+        const float2 *e2 = reinterpret_cast<const float2 *>(d_e + (size_t)p * neq);
+        k_tri_first<<<gn, 256, 0, st>>>(n, G, Gm, d2, r2, reinterpret_cast<float2 *>(y), nullptr);
+        k_tri_second<<<gn, 256, 0, st>>>(n, G, Gm, d2, reinterpret_cast<const float2 *>(y),
+                                         reinterpret_cast<float2 *>(z));
+        k_spmv32<<<gn, 256, 0, st>>>(n, L.slice_base, L.rowlen, L.sell_node, L.sell_col, K4, c->d_fixed, e2,
+                                     reinterpret_cast<float2 *>(ae));
         k_spmv32<<<gn, 256, 0, st>>>(n, L.slice_base, L.rowlen, L.sell_node, L.sell_col, K4, c->d_fixed,
                                      reinterpret_cast<const float2 *>(z), reinterpret_cast<float2 *>(az));
         k_res_part<<<ge, 256, 0, st>>>(neq, ae, az, res, m.part);
         k_res_final<<<1, 256, 0, st>>>((int)ge, m.part, m.scal, m.loss, w);
         k_spmv32<<<gn, 256, 0, st>>>(n, L.slice_base, L.rowlen, L.sell_node, L.sell_col, K4, c->d_fixed,
                                      reinterpret_cast<const float2 *>(res), reinterpret_cast<float2 *>(g));
-        k_patch_grad<<<gn, 256, 0, st>>>(n, G, reinterpret_cast<const float2 *>(x.dinv),
-                                         reinterpret_cast<const float2 *>(r), reinterpret_cast<const float2 *>(g),
-                                         m.scal, w, m.dN);
+        k_tri_first<<<gn, 256, 0, st>>>(n, G, Gm, d2, reinterpret_cast<const float2 *>(g),
+                                        reinterpret_cast<float2 *>(v), nullptr);
+        k_tri_grad_pairs<<<gn, 256, 0, st>>>(n, G, d2, r2, reinterpret_cast<const float2 *>(g),
+                                             reinterpret_cast<const float2 *>(y), reinterpret_cast<const float2 *>(v),
+                                             m.scal, w, m.dN);
     }
+    // Kaporin term (H in the dH1 buffer, free before the backward)
+    float *H = m.dH1;
+    k_kap_H<<<gn, 256, 0, st>>>(n, G, Gm, K4, m.pslot, d2, m.O, H, m.part);
+    k_kap_final<<<1, 256, 0, st>>>((int)gn, m.part, m.scal, m.loss, wk, m.nf);
+    float *dO = m.dH2;                      // [n][20], free until dH2 is formed
+    k_tri_dO<<<gn, 256, 0, st>>>(n, G, m.O, d2, m.dN, H, m.scal, wk, m.nf, dO);
+    cudaMemcpyAsync(m.dN, dO, (size_t)n * NOUT * sizeof(float), cudaMemcpyDeviceToDevice, st);
     // backward
     float *gr = m.grads;
     gemm_tn_split(c, 128, NOUT, n, m.H2, 128, m.dN, NOUT, gr + kOffW3);              // dW3 = H2^T dO
@@ -962,7 +1159,7 @@ void patch_learn_grad(ipfem_ctx *c, const float *d_r, const float *d_e, int P)
     k_relu_mask<<<eh, 256, 0, st>>>((int64_t)n * 128, m.dH1, m.H1);
     gemm_tn_split(c, 32, 128, n, m.X, 32, m.dH1, 128, gr + kOffW1);                  // dW1 = X^T dH1
     colsum(c, n, 128, m.dH1, gr + kOffB1);
-    c->launches += 7 + 6 * (uint64_t)P + 14;
+    c->launches += 10 + 9 * (uint64_t)(wp > 0.f ? P : 0) + 14;
 }
 
 // one Adam step on the parameters with the gradient in mlp.grads

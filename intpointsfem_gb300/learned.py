@@ -8,9 +8,10 @@ Newton to a random load step; their FP32 tangent stays resident in one
 library context per problem.  Training pairs: the residual r_k of the plain
 (Jacobi) FP32 CG on the Newton right-hand side at iterations k = 0, 64,
 128, ... and the remaining solution increment e_k = x_final - x_k.  The loss
-of a pair is |K e_k - K M r_k|^2 / |K e_k|^2 (M the learned operator), its
-gradient comes from the library (ipfem_learn_grad) and Adam runs on the
-library's kernels (ipfem_mlp_adam).
+of a problem is the log of Kaporin's condition number of M K (M the learned
+operator) plus the mean over the drawn pairs of |K e_k - K M r_k|^2 /
+|K e_k|^2; its gradient comes from the library (ipfem_learn_grad) and Adam
+runs on the library's kernels (ipfem_mlp_adam).
 """
 import time
 
@@ -76,7 +77,7 @@ def generate_problems(n=64, n_problems=4, seed=20260101, n_steps=10, cg_rtol=1e-
     return out
 
 
-def train(problems, steps=300, lr=1e-3, pairs_per_step=8, seed=1):
+def train(problems, steps=300, lr=1e-3, pairs_per_step=8, seed=1, w_kaporin=1.0, w_pairs=1.0):
     """Adam over the problems in turn; returns (parameters, loss per step).
     The first problem's context holds the parameters and the Adam state."""
     torch = _torch()
@@ -90,7 +91,7 @@ def train(problems, steps=300, lr=1e-3, pairs_per_step=8, seed=1):
         npair = pb.R.shape[0]
         idx = torch.tensor(np.sort(rng.choice(npair, size=min(pairs_per_step, npair), replace=False)),
                            device=pb.R.device)
-        g, loss = pb.sm.learn_grad(pb.R[idx].contiguous(), pb.E[idx].contiguous(), len(idx))
+        g, loss = pb.sm.learn_grad(pb.R[idx].contiguous(), pb.E[idx].contiguous(), len(idx), w_kaporin, w_pairs)
         trainer.mlp_adam(g, lr)
         losses.append(loss)
     return trainer.mlp_params(), np.array(losses)

@@ -1,0 +1,96 @@
+"""Train the learned patch preconditioner on the GPU and write its weights.
+
+    python -m intpointsfem_gb300.train_preconditioner --n 400 --problems 4 --steps 400 \\
+        --out intpointsfem_gb300/weights/patch_net.npy
+
+Problems: n x n wellbore meshes with well pressure U[-30, -5] MPa and
+friction angle U[25, 35] deg (seeded), each advanced by Newton to a random
+load step; pairs: (residual, solution increment) snapshots of the plain FP32
+Jacobi-CG on the Newton right-hand side (learned.generate_problems).  The
+gradient pass and Adam run on the library's kernels.  The report (JSON beside
+the weights) records the data, the loss curve and, for held-out problems, the
+CG iterations and solve times of Jacobi-PCG and of the learned FCG over the
+same Newton iterations.
+"""
+import argparse
+import json
+import os
+import time
+
+import numpy as np
+
+from . import learned
+
+WEIGHTS = os.path.join(os.path.dirname(os.path.abspath(__file__)), "weights", "patch_net.npy")
+
+
+def load_weights(path=WEIGHTS):
+    """the shipped network parameters (FP32, 23316 values)"""
+    return np.load(path).astype(np.float32)
+
+
+def evaluate(params, n, newton_iters, cases=((-12.0, 28.0), (-25.0, 33.0))):
+    """Jacobi-PCG vs learned FCG over the same Newton iterations of held-out problems"""
+    out = []
+    for pw, phi in cases:
+        res = learned.compare(params, n=n, pw=pw, phi=phi, newton_iters=newton_iters)
+        j, m = res["jacobi"], res["mlp"]
+        out.append({"n": n, "pw": pw, "phi": phi, "newton_iters": m["newton_iters"],
+                    "cg_iters_jacobi": j["cg_iters"], "cg_iters_learned": m["cg_iters"],
+                    "ms_solve_jacobi": j["ms_solve"], "ms_solve_learned": m["ms_solve"],
+                    "fallbacks": m["fallbacks"],
+                    "max_rel_du": float(np.abs(m["u"] - j["u"]).max() / np.abs(j["u"]).max())})
+    return out
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--n", type=int, default=400)
+    ap.add_argument("--problems", type=int, default=4)
+    ap.add_argument("--steps", type=int, default=400)
+    ap.add_argument("--lr", type=float, default=1e-3)
+    ap.add_argument("--pairs-per-step", type=int, default=8)
+    ap.add_argument("--seed", type=int, default=20260101)
+    ap.add_argument("--eval-n", type=int, default=0, help="mesh of the held-out comparison (0: --n)")
+    ap.add_argument("--eval-newton", type=int, default=4)
+    ap.add_argument("--out", default=WEIGHTS)
+    ap.add_argument("--eval-only", default="", help="evaluate these weights instead of training")
+    a = ap.parse_args(argv)
+    if a.eval_only:
+        params = load_weights(a.eval_only)
+        for row in evaluate(params, a.eval_n or a.n, a.eval_newton):
+            print("eval", json.dumps(row), flush=True)
+        return
+    t0 = time.time()
+    probs = learned.generate_problems(n=a.n, n_problems=a.problems, seed=a.seed)
+    t_data = time.time() - t0
+    info = [pb.info for pb in probs]
+    n_pairs = sum(pb.R.shape[0] for pb in probs)
+    neq = probs[0].sm.neq
+    print("data: %d problems, %d (residual, increment) pairs of %d dofs, %.1f s" % (len(probs), n_pairs, neq, t_data),
+          flush=True)
+    t0 = time.time()
+    try:
+        params, losses = learned.train(probs, steps=a.steps, lr=a.lr, pairs_per_step=a.pairs_per_step,
+                                       seed=a.seed + 1)
+    finally:
+        for pb in probs:
+            pb.close()
+    t_train = time.time() - t0
+    print("train: %d Adam steps, %.1f s, loss %.4g -> %.4g" % (a.steps, t_train, losses[:5].mean(),
+                                                                losses[-20:].mean()), flush=True)
+    os.makedirs(os.path.dirname(os.path.abspath(a.out)), exist_ok=True)
+    np.save(a.out, params.astype(np.float32))
+    ev = evaluate(params, a.eval_n or a.n, a.eval_newton)
+    for row in ev:
+        print("eval", json.dumps(row), flush=True)
+    report = {"n": a.n, "problems": info, "pairs": n_pairs, "dofs_per_pair": neq, "steps": a.steps, "lr": a.lr,
+              "pairs_per_step": a.pairs_per_step, "seconds_data": t_data, "seconds_train": t_train,
+              "loss_first5": float(losses[:5].mean()), "loss_last20": float(losses[-20:].mean()),
+              "loss": [float(x) for x in losses[::10]], "eval": ev}
+    with open(os.path.splitext(a.out)[0] + ".json", "w") as f:
+        json.dump(report, f, indent=1)
+
+
+if __name__ == "__main__":
+    main()

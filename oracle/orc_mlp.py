@@ -1,19 +1,28 @@
 """CPU oracle of the learned preconditioner (test infrastructure only).
 
-numpy restatement of the per-node network (32 -> 128 -> 128 -> 36), of the
-symmetric 3x3-patch operator it parameterises, and of the training loss
-L = (1/P) sum_p |K e_p - K M r_p|^2 / |K e_p|^2 with its parameter gradients.
+numpy restatement of the per-node network (32 -> 128 -> 128 -> 20), of the
+sparse triangular factor G it parameterises and the operator
+M = diag(s) G^T G diag(s) (s = sqrt of the Jacobi inverse diagonal, 0 on
+Dirichlet dofs), and of the training loss
+    L = wk * log(tr(G A^ G^T) / Nf) - wk * (2/Nf) log det G
+      + wp * (1/P) sum_p |K e_p - K M r_p|^2 / |K e_p|^2
+(A^ = diag(s) K diag(s), Nf free dofs; the first line is the log of Kaporin's
+condition number of M K up to a constant) with its parameter gradients.
 Every tensor-core operand is rounded to BF16 (round to nearest even) as the
 device kernels do; products and sums run in FP64.
 
-Parameter layout of the library: W1[32][128] b1[128] W2[128][128] b2[128]
-W3[128][36] b3[36].  Node i = b*gr + a; patch position k = 3*(db+1) + (da+1),
-k = 4 the node itself, 8 - k the mirror position.
+Node i = b*gr + a; patch position k = 3*(db+1) + (da+1) for da, db in
+{-1, 0, 1}.  G has the blocks k = 0..3 (the lower neighbours) and k = 4 (the
+node): G_ik = O_i[4k .. 4k+3] as row-major 2x2 for k < 4 and
+G_i4 = [[exp(O_i[16]), 0], [O_i[17], exp(O_i[18])]]; O_i[19] is unused.
+Entries that touch a Dirichlet dof are 0.  Parameter layout of the library:
+W1[32][128] b1[128] W2[128][128] b2[128] W3[128][20] b3[20].
 """
 import numpy as np
 
-SIZES = [("W1", (32, 128)), ("b1", (128,)), ("W2", (128, 128)), ("b2", (128,)), ("W3", (128, 36)), ("b3", (36,))]
+SIZES = [("W1", (32, 128)), ("b1", (128,)), ("W2", (128, 128)), ("b2", (128,)), ("W3", (128, 20)), ("b3", (20,))]
 N_PARAMS = sum(int(np.prod(s)) for _, s in SIZES)
+NOUT = 20
 
 
 def unpack(p):
@@ -81,71 +90,163 @@ def forward(p, X):
     return O, (X, H1, H2)
 
 
-def operator(gr, gt, O, dinv):
-    """M[9][n][2][2] = s_i ((O_ik + O_j(8-k)^T)/2 + [k == 4] I) s_j"""
+def factor(gr, gt, O, dinv):
+    """G[5][n][2][2] from the network output O[n][20]"""
     nb = neighbours(gr, gt)
     n = gr * gt
-    s = np.sqrt(np.asarray(dinv, dtype=np.float64)).reshape(n, 2)
-    Ob = np.asarray(O, dtype=np.float64).reshape(n, 9, 2, 2)
-    M = np.zeros((9, n, 2, 2))
-    for k in range(9):
+    f = (np.asarray(dinv, dtype=np.float64) > 0).astype(np.float64).reshape(n, 2)
+    O = np.asarray(O, dtype=np.float64)
+    G = np.zeros((5, n, 2, 2))
+    for k in range(4):
         ok = nb[:, k] >= 0
         i = np.nonzero(ok)[0]
         j = nb[i, k]
-        mh = 0.5 * (Ob[i, k] + np.transpose(Ob[j, 8 - k], (0, 2, 1)))
-        if k == 4:
-            mh = mh + np.eye(2)
-        M[k, i] = s[i][:, :, None] * mh * s[j][:, None, :]
-    return M
+        G[k, i] = O[i, 4 * k:4 * k + 4].reshape(-1, 2, 2) * f[i][:, :, None] * f[j][:, None, :]
+    G[4, :, 0, 0] = np.exp(O[:, 16]) * f[:, 0]
+    G[4, :, 1, 0] = O[:, 17] * f[:, 1] * f[:, 0]
+    G[4, :, 1, 1] = np.exp(O[:, 18]) * f[:, 1]
+    return G
 
 
-def apply(gr, gt, M, r):
+def g_mul(gr, gt, G, x):
+    """y = G x"""
     nb = neighbours(gr, gt)
     n = gr * gt
-    rb = np.asarray(r, dtype=np.float64).reshape(n, 2)
-    z = np.zeros((n, 2))
-    for k in range(9):
+    xb = np.asarray(x, dtype=np.float64).reshape(n, 2)
+    y = np.zeros((n, 2))
+    for k in range(5):
         ok = nb[:, k] >= 0
-        z[ok] += np.einsum("ipq,iq->ip", M[k, ok], rb[nb[ok, k]])
-    return z.ravel()
+        y[ok] += np.einsum("ipq,iq->ip", G[k, ok], xb[nb[ok, k]])
+    return y.ravel()
 
 
-def patch_loss_grad(O, matvec, gr, gt, dinv, R, E):
-    """loss L = (1/P) sum_p |K e_p - K M r_p|^2 / |K e_p|^2 of the operator
-    built from O[n][36] and dL/dO[n][36]"""
-    n = gr * gt
-    M = operator(gr, gt, O, dinv)
+def gt_mul(gr, gt, G, y):
+    """x = G^T y"""
     nb = neighbours(gr, gt)
-    s = np.sqrt(np.asarray(dinv, dtype=np.float64)).reshape(n, 2)
+    n = gr * gt
+    yb = np.asarray(y, dtype=np.float64).reshape(n, 2)
+    x = np.zeros((n, 2))
+    for k in range(5):
+        ok = nb[:, k] >= 0
+        i = np.nonzero(ok)[0]
+        np.add.at(x, nb[i, k], np.einsum("ipq,ip->iq", G[k, i], yb[i]))
+    return x.ravel()
+
+
+def apply(gr, gt, G, dinv, r):
+    """M r = s * G^T (G (s * r))"""
+    s = np.sqrt(np.asarray(dinv, dtype=np.float64))
+    return s * gt_mul(gr, gt, G, g_mul(gr, gt, G, s * np.asarray(r, dtype=np.float64)))
+
+
+def kaporin_loss_grad(G, O, Ahat_mul_rows, dinv):
+    """log(tr(G A^ G^T)/Nf) - (2/Nf) log det G and its gradient with
+    respect to G[5][n][2][2] (the log-det part separately, with respect to
+    O[:, 16] and O[:, 18]).  Ahat_mul_rows(G) returns H[5][n][2][2] with
+    H_ik[p][q] = (A^ g_ip)[nbr(i, k), q], g_ip row p of G."""
+    f = (np.asarray(dinv) > 0).astype(np.float64).reshape(-1, 2)
+    nf = f.sum()
+    H = Ahat_mul_rows(G)
+    T = float((G * H).sum())
+    loss = np.log(T / nf) - 2.0 / nf * float((O[:, 16] * f[:, 0]).sum() + (O[:, 18] * f[:, 1]).sum())
+    dG = 2.0 / T * H
+    dlogdet = np.zeros((O.shape[0], 2))
+    dlogdet[:, 0] = -2.0 / nf * f[:, 0]
+    dlogdet[:, 1] = -2.0 / nf * f[:, 1]
+    return loss, dG, dlogdet
+
+
+def dO_from_dG(O, dG, dinv, gr, gt, dlogdet=None):
+    """chain rule G(O) -> dL/dO[n][20]"""
+    nb = neighbours(gr, gt)
+    n = O.shape[0]
+    f = (np.asarray(dinv) > 0).astype(np.float64).reshape(n, 2)
+    dO = np.zeros((n, NOUT))
+    for k in range(4):
+        ok = nb[:, k] >= 0
+        i = np.nonzero(ok)[0]
+        j = nb[i, k]
+        dO[i, 4 * k:4 * k + 4] = (dG[k, i] * f[i][:, :, None] * f[j][:, None, :]).reshape(-1, 4)
+    dO[:, 16] = dG[4, :, 0, 0] * np.exp(O[:, 16]) * f[:, 0]
+    dO[:, 17] = dG[4, :, 1, 0] * f[:, 1] * f[:, 0]
+    dO[:, 18] = dG[4, :, 1, 1] * np.exp(O[:, 18]) * f[:, 1]
+    if dlogdet is not None:
+        dO[:, 16] += dlogdet[:, 0]
+        dO[:, 18] += dlogdet[:, 1]
+    return dO
+
+
+def pair_loss_grad(G, matvec, gr, gt, dinv, R, E):
+    """(1/P) sum_p |K e_p - K M r_p|^2 / |K e_p|^2 and its gradient w.r.t. G"""
+    nb = neighbours(gr, gt)
+    n = gr * gt
+    s = np.sqrt(np.asarray(dinv, dtype=np.float64))
     npair = len(R)
-    dO = np.zeros((n, 9, 2, 2))
+    dG = np.zeros_like(G)
     loss = 0.0
     for r, e in zip(R, E):
         r = np.asarray(r, dtype=np.float64)
         ae = matvec(np.asarray(e, dtype=np.float64))
-        az = matvec(apply(gr, gt, M, r))
-        res = ae - az
+        rh = s * r
+        y = g_mul(gr, gt, G, rh)
+        z = s * gt_mul(gr, gt, G, y)
+        res = ae - matvec(z)
         aa = ae @ ae
         if not aa > 0:
             continue
         loss += (res @ res) / aa / npair
-        g = matvec(res)
-        c = -1.0 / (aa * npair)
-        rh = s * r.reshape(n, 2)
-        gh = s * g.reshape(n, 2)
-        for k in range(9):
+        u = s * (-2.0 / (aa * npair)) * matvec(res)        # dL/d(G^T y) premultiplied by s
+        v = g_mul(gr, gt, G, u)
+        yb, ub, vb, rb = y.reshape(n, 2), u.reshape(n, 2), v.reshape(n, 2), rh.reshape(n, 2)
+        for k in range(5):
             i = np.nonzero(nb[:, k] >= 0)[0]
             j = nb[i, k]
-            dO[i, k] += c * (gh[i][:, :, None] * rh[j][:, None, :] + rh[i][:, :, None] * gh[j][:, None, :])
-    return loss, dO.reshape(n, 36)
+            dG[k, i] += yb[i][:, :, None] * ub[j][:, None, :] + vb[i][:, :, None] * rb[j][:, None, :]
+    return loss, dG
 
 
-def loss_and_grads(p, X, matvec, gr, gt, dinv, R, E):
-    """loss and parameter gradient (packed) for pairs R[P][neq], E[P][neq];
-    matvec(v) applies the symmetric tangent (Dirichlet rows and columns 0)"""
+def ahat_rows(gr, gt, blocks, dinv):
+    """Ahat_mul_rows for the 5-node lower patches: blocks(j, l) returns the
+    2x2 tangent block K_jl (zeros if absent)"""
+    nb = neighbours(gr, gt)
+    n = gr * gt
+    s = np.sqrt(np.asarray(dinv, dtype=np.float64)).reshape(n, 2)
+
+    def mul(G):
+        H = np.zeros_like(G)
+        for i in range(n):
+            for k in range(5):
+                jk = nb[i, k]
+                if jk < 0:
+                    continue
+                for l in range(5):
+                    jl = nb[i, l]
+                    if jl < 0:
+                        continue
+                    Ah = s[jk][:, None] * blocks(jk, jl) * s[jl][None, :]
+                    # H_ik[p][q] += sum_t Ahat[jk q][jl t] G_il[p][t]
+                    H[k, i] += G[l, i] @ Ah.T
+        return H
+    return mul
+
+
+def loss_grad_O(O, matvec, blocks, gr, gt, dinv, R, E, wk=1.0, wp=1.0):
+    """the combined loss and dL/dO[n][20]"""
+    G = factor(gr, gt, O, dinv)
+    lk, dGk, dld = kaporin_loss_grad(G, O, ahat_rows(gr, gt, blocks, dinv), dinv)
+    loss, dG, dlogdet = wk * lk, wk * dGk, wk * dld
+    if wp > 0 and len(R):
+        lp, dGp = pair_loss_grad(G, matvec, gr, gt, dinv, R, E)
+        loss += wp * lp
+        dG = dG + wp * dGp
+    return loss, dO_from_dG(O, dG, dinv, gr, gt, dlogdet)
+
+
+def loss_and_grads(p, X, matvec, blocks, gr, gt, dinv, R, E, wk=1.0, wp=1.0):
+    """loss and parameter gradient (packed)"""
     P = unpack(p)
     O, (X, H1, H2) = forward(p, X)
-    loss, dO = patch_loss_grad(O, matvec, gr, gt, dinv, R, E)
+    loss, dO = loss_grad_O(O, matvec, blocks, gr, gt, dinv, R, E, wk, wp)
     grads = {}
     grads["W3"] = bf16(H2).T @ bf16(dO)
     grads["b3"] = dO.sum(0)

@@ -1,7 +1,7 @@
-"""Learned preconditioner: features, tensor-core forward, the symmetric patch
-operator and the training gradients against the CPU oracle
-(oracle/orc_mlp.py); FCG with the untrained network equals Jacobi; training
-on the GPU and what the trained network gains over Jacobi-PCG."""
+"""Learned preconditioner: features, tensor-core forward, the triangular
+factor and the training gradients (Kaporin and pair terms) against the CPU
+oracle (oracle/orc_mlp.py); FCG with the untrained network equals Jacobi;
+training on the GPU and what the trained network gains over Jacobi-PCG."""
 import numpy as np
 import pytest
 
@@ -16,7 +16,7 @@ from oracle import orc_mlp  # noqa: E402
 def _random_params(rng, scale3=0.05):
     d = {"W1": rng.normal(size=(32, 128)) * np.sqrt(2 / 32), "b1": rng.normal(size=128) * 0.1,
          "W2": rng.normal(size=(128, 128)) * np.sqrt(2 / 128), "b2": rng.normal(size=128) * 0.1,
-         "W3": rng.normal(size=(128, 36)) * scale3, "b3": rng.normal(size=36) * 0.02}
+         "W3": rng.normal(size=(128, 20)) * scale3, "b3": rng.normal(size=20) * 0.02}
     return orc_mlp.pack(d)
 
 
@@ -51,6 +51,13 @@ def _tangent(sm, wb):
         y[fixed] = 0.0
         return y
 
+    lut = {(int(rows[t]), int(col[t])): t for t in range(len(col))}
+
+    def blocks(j, l):
+        t = lut.get((int(j), int(l)))
+        return K[t] if t is not None else np.zeros((2, 2))
+
+    matvec.blocks = blocks
     return rp, col, K, dinv, matvec
 
 
@@ -71,43 +78,41 @@ def test_forward_matches_oracle():
     wb, sm = learned.make_solver(4, -10.0, 30.0, seed=3)
     sm.set_mlp_params(_random_params(rng, 0.2))
     X = rng.normal(size=(1000, 32)).astype(np.float32)
-    dO = torch.zeros(1000, 36, device="cuda")
+    dO = torch.zeros(1000, 20, device="cuda")
     sm.mlp_forward(torch.tensor(X, device="cuda"), 1000, dO)
     O_ref, _ = orc_mlp.forward(sm.mlp_params(), X)
     err = np.abs(dO.cpu().numpy() - O_ref).max() / np.abs(O_ref).max()
     assert err < 2e-3, err
 
 
-def test_operator_is_symmetric_and_matches_oracle():
+def test_factor_matches_oracle_and_operator_is_spd():
     rng = np.random.default_rng(1)
     wb, sm, _ = _problem()
     gr, n = 13, sm.n_nodes
     sm.set_mlp_params(_random_params(rng))
     X = torch.zeros(n, 32, device="cuda")
     sm.mlp_features(X)
-    O = torch.zeros(n, 36, device="cuda")
+    O = torch.zeros(n, 20, device="cuda")
     sm.mlp_forward(X, n, O)
-    M = torch.zeros(9, n, 2, 2, device="cuda")
-    sm.mlp_operator(M)
-    Mg = M.cpu().numpy().astype(np.float64)
+    Gd = torch.zeros(5, n, 2, 2, device="cuda")
+    sm.mlp_operator(Gd)
+    Gg = Gd.cpu().numpy().astype(np.float64)
     _, _, _, dinv, _ = _tangent(sm, wb)
-    Mr = orc_mlp.operator(gr, gr, O.cpu().numpy(), dinv)
-    assert np.abs(Mg - Mr).max() <= 1e-5 * np.abs(Mr).max()
-    # dense symmetric check
-    nb = orc_mlp.neighbours(gr, gr)
-    D = np.zeros((2 * n, 2 * n))
-    for k in range(9):
-        for i in np.nonzero(nb[:, k] >= 0)[0]:
-            j = nb[i, k]
-            D[2 * i:2 * i + 2, 2 * j:2 * j + 2] += Mg[k, i]
-    assert np.abs(D - D.T).max() <= 1e-6 * np.abs(D).max()
-    # untrained parameters give Jacobi
+    Gr = orc_mlp.factor(gr, gr, O.cpu().numpy(), dinv)
+    assert np.abs(Gg - Gr).max() <= 1e-5 * np.abs(Gr).max()
+    # M = s G^T G s: symmetric positive definite on the free dofs
+    free = dinv > 0
+    M = np.stack([orc_mlp.apply(gr, gr, Gg, dinv, np.eye(sm.neq)[c]) for c in range(sm.neq)], 1)
+    assert np.abs(M - M.T).max() <= 1e-12 * np.abs(M).max()
+    assert np.linalg.eigvalsh(M[free][:, free]).min() > 0
+    # untrained parameters: G = I on the free dofs, so M is Jacobi
     sm.mlp_init(0)
-    sm.mlp_operator(M)
-    Mj = M.cpu().numpy()
-    assert np.array_equal(Mj[[0, 1, 2, 3, 5, 6, 7, 8]], np.zeros_like(Mj[[0, 1, 2, 3, 5, 6, 7, 8]]))
-    diag = np.stack([Mj[4, :, 0, 0], Mj[4, :, 1, 1]], 1).ravel()
-    assert np.allclose(diag, dinv, rtol=1e-6, atol=0)
+    sm.mlp_operator(Gd)
+    Gj = Gd.cpu().numpy()
+    assert np.array_equal(Gj[:4], np.zeros_like(Gj[:4]))
+    assert np.array_equal(Gj[4, :, 0, 1], np.zeros(n)) and np.array_equal(Gj[4, :, 1, 0], np.zeros(n))
+    diag = np.stack([Gj[4, :, 0, 0], Gj[4, :, 1, 1]], 1).ravel()
+    assert np.array_equal(diag, free.astype(np.float32))
 
 
 def test_learn_grad_matches_oracle():
@@ -123,18 +128,20 @@ def test_learn_grad_matches_oracle():
     its = sm.cg_snapshots(R0, snaps, xs, rs, xf, rtol=1e-6, max_it=4000)
     assert its > 64
     E = (xf[None] - xs).contiguous()
-    g, loss = sm.learn_grad(rs, E, len(snaps))
     X = torch.zeros(sm.n_nodes, 32, device="cuda")
     sm.mlp_features(X)
     _, _, _, dinv, matvec = _tangent(sm, wb)
-    loss_ref, g_ref = orc_mlp.loss_and_grads(sm.mlp_params(), X.cpu().numpy(), matvec, gr, gr, dinv,
-                                             rs.cpu().numpy(), E.cpu().numpy())
-    assert loss == pytest.approx(loss_ref, rel=2e-3)
-    gd, rd = orc_mlp.unpack(g), orc_mlp.unpack(g_ref)
-    for name, _ in orc_mlp.SIZES:
-        e = np.linalg.norm(gd[name] - rd[name]) / np.linalg.norm(rd[name])
-        assert e < 2e-2, (name, e)
+    for wk, wp, npair in ((1.0, 1.0, len(snaps)), (1.0, 0.0, 0), (0.0, 1.0, len(snaps))):
+        g, loss = sm.learn_grad(rs, E, npair, wk, wp)
+        loss_ref, g_ref = orc_mlp.loss_and_grads(sm.mlp_params(), X.cpu().numpy(), matvec, matvec.blocks, gr, gr,
+                                                 dinv, rs.cpu().numpy()[:npair], E.cpu().numpy()[:npair], wk, wp)
+        assert loss == pytest.approx(loss_ref, rel=2e-3, abs=1e-5), (wk, wp)
+        gd, rd = orc_mlp.unpack(g), orc_mlp.unpack(g_ref)
+        for name, _ in orc_mlp.SIZES:
+            e = np.linalg.norm(gd[name] - rd[name]) / np.linalg.norm(rd[name])
+            assert e < 2e-2, (wk, wp, name, e)
     # a small Adam step along the gradient lowers the loss
+    g, loss = sm.learn_grad(rs, E, len(snaps))
     sm.mlp_adam(g, 1e-4)
     _, loss2 = sm.learn_grad(rs, E, len(snaps))
     assert loss2 < loss
@@ -167,7 +174,7 @@ def test_training_and_gain_over_jacobi():
     finally:
         for pb in probs:
             pb.close()
-    assert np.isfinite(losses).all() and losses[-30:].mean() < 0.8 * losses[:3].mean()
+    assert np.isfinite(losses).all() and losses[-30:].mean() < losses[:3].mean() - 0.05
     res = learned.compare(p, n=48, pw=-12.0, phi=28.0, newton_iters=6)
     j, m = res["jacobi"], res["mlp"]
     print("learned vs Jacobi (48x48): CG iterations %d vs %d, solve ms %.1f vs %.1f, fallbacks %d, loss %.3g -> %.3g"

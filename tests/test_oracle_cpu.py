@@ -83,34 +83,47 @@ def test_nan_input_propagates_to_residual(P8):
     assert np.isnan(r).any()
 
 
-def test_patch_operator_gradient_matches_finite_differences():
-    """the oracle's dL/dO of the learned patch operator (oracle/orc_mlp.py)
-    against central differences, on the oracle's own tangent of a 3 x 3 mesh"""
+def test_learned_factor_gradient_matches_finite_differences():
+    """the oracle's loss of the learned preconditioner (log Kaporin number of
+    the triangular factor plus the (residual, increment) pair term,
+    oracle/orc_mlp.py) against central differences of its gradient, on the
+    oracle's own tangent of a 3 x 3 mesh; M is symmetric positive definite"""
     import scipy.sparse as sp
     from oracle import orc_mlp
     n = 3
     P = po.OracleProblem(po.default_params(n), nthreads=0)
     P.assemble(np.zeros(P.neq), 0.5)
-    rp, col, K = P.arr("row_ptr"), P.arr("col"), P.arr("K").reshape(-1, 2, 2)
+    rp, col, K = P.arr("row_ptr").copy(), P.arr("col").copy(), P.arr("K").reshape(-1, 2, 2).copy()
     nn = P.n_nodes
     fixed = P.arr("fixed").astype(bool)
-    A = sp.bsr_matrix((K.copy(), col.copy(), rp.copy()), shape=(2 * nn, 2 * nn)).tocsr()
+    A = sp.bsr_matrix((K, col, rp), shape=(2 * nn, 2 * nn)).tocsr()
     keep = sp.diags((~fixed).astype(float))
     A = (keep @ A @ keep).tocsr()
     dinv = np.where(fixed, 0.0, 1.0 / A.diagonal().clip(min=1e-300))
+    rows = np.repeat(np.arange(nn), np.diff(rp))
+    lut = {(int(rows[t]), int(col[t])): t for t in range(len(col))}
+
+    def blocks(j, l):
+        t = lut.get((int(j), int(l)))
+        return K[t] if t is not None else np.zeros((2, 2))
+
     rng = np.random.default_rng(0)
     R = [rng.normal(size=P.neq) * ~fixed for _ in range(2)]
     E = [rng.normal(size=P.neq) * ~fixed for _ in range(2)]
     gr = 2 * n + 1
-    O = rng.normal(size=(nn, 36)) * 0.1
+    O = rng.normal(size=(nn, 20)) * 0.1
     mv = lambda v: A @ v  # noqa: E731
-    loss, dO = orc_mlp.patch_loss_grad(O, mv, gr, gr, dinv, R, E)
-    assert loss > 0
-    for t in rng.choice(O.size, size=25, replace=False):
+    G = orc_mlp.factor(gr, gr, O, dinv)
+    M = np.stack([orc_mlp.apply(gr, gr, G, dinv, np.eye(P.neq)[c]) for c in range(P.neq)], 1)
+    assert np.abs(M - M.T).max() <= 1e-12 * np.abs(M).max()
+    ev = np.linalg.eigvalsh(M[~fixed][:, ~fixed])
+    assert ev.min() > 0
+    loss, dO = orc_mlp.loss_grad_O(O, mv, blocks, gr, gr, dinv, R, E)
+    for t in rng.choice(O.size, size=30, replace=False):
         h = 1e-6
         Op, Om = O.copy(), O.copy()
         Op.flat[t] += h
         Om.flat[t] -= h
-        fd = (orc_mlp.patch_loss_grad(Op, mv, gr, gr, dinv, R, E)[0] -
-              orc_mlp.patch_loss_grad(Om, mv, gr, gr, dinv, R, E)[0]) / (2 * h)
+        fd = (orc_mlp.loss_grad_O(Op, mv, blocks, gr, gr, dinv, R, E)[0] -
+              orc_mlp.loss_grad_O(Om, mv, blocks, gr, gr, dinv, R, E)[0]) / (2 * h)
         assert abs(fd - dO.flat[t]) <= 1e-6 * max(1.0, abs(dO).max()), (t, fd, dO.flat[t])
