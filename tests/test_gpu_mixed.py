@@ -58,3 +58,32 @@ def test_mixed_newton_cfg1_against_fp64_oracle():
           % (eu, es, eep, flips, sg.newton_iters, so.newton_iters))
     assert eu < 1e-6 and es < 1e-6 and eep < 1e-6
     assert flips <= 2
+
+
+def test_mixed_learned_newton_cfg1_against_fp64_oracle():
+    """the chosen method: FP32 tangent, flexible CG to 1e-4 with the shipped
+    learned preconditioner (trained on 400 x 400 problems), FP64 Newton to
+    1e-8; 40 x 40, 10 load steps, against the FP64 oracle"""
+    from intpointsfem_gb300 import train_preconditioner as tp
+    n = 40
+    sm, P = _pair(n)
+    sm.set_precision(ip.MIXED)
+    sm.set_node_grid(2 * n + 1, 2 * n + 1)
+    sm.mlp_init(0)
+    sm.set_mlp_params(tp.load_weights())
+    sm.set_preconditioner(ip.PREC_MLP)
+    ug, uo = np.zeros(sm.neq), np.zeros(sm.neq)
+    sg, _ = sm.newton(ug, 10, newton_max_it=40, cg_rtol=1e-4)
+    so, _ = P.solve_steps(uo, 10, newton_max_it=40)
+    assert sg.converged
+    eu = np.abs(ug - uo).max() / np.abs(uo).max()
+    sig, sigo = sm.get_state(1), _soa4(P.arr("sigma"), P.n_ip)
+    es = np.abs(sig - sigo).max() / np.abs(sigo).max()
+    ep, epo = sm.get_state(0), _soa4(P.arr("eps_p"), P.n_ip)
+    eep = np.abs(ep - epo).max() / np.abs(epo).max()
+    flips = int((sm.get_state(3) != P.arr("mtype")).sum())
+    print("mixed+learned vs FP64: u %.2e  sigma %.2e  eps_p %.2e  flag flips %d  newton %d vs %d  CG %d vs %d  "
+          "fallbacks %d" % (eu, es, eep, flips, sg.newton_iters, so.newton_iters, sg.cg_iters, so.cg_iters,
+                            sg.fcg_fallbacks))
+    assert eu < 1e-6 and es < 1e-6 and eep < 1e-6
+    assert flips <= 2
