@@ -97,12 +97,15 @@ def train(problems, steps=300, lr=1e-3, pairs_per_step=8, seed=1, w_kaporin=1.0,
     return trainer.mlp_params(), np.array(losses)
 
 
-def compare(params, n=400, pw=-12.0, phi=28.0, n_steps=10, newton_iters=6, cg_rtol=1e-4, device="cuda", **kw):
+def compare(params, n=400, pw=-12.0, phi=28.0, n_steps=10, newton_iters=6, cg_rtol=1e-4, device="cuda",
+            arms=("jacobi", "mlp"), **kw):
     """Runs the same Newton iterations with Jacobi-PCG and with the learned
     FCG (both FP32 inner solves, FP64 Newton); returns per-method statistics."""
     torch = _torch()
     out = {}
     for name, kind in (("jacobi", PREC_JACOBI), ("mlp", PREC_MLP)):
+        if name not in arms:
+            continue
         wb, sm = make_solver(n, pw, phi, 0, **kw)
         sm.set_mlp_params(params)
         sm.set_preconditioner(kind)

@@ -55,7 +55,14 @@ def main(argv=None):
     ap.add_argument("--eval-newton", type=int, default=4)
     ap.add_argument("--out", default=WEIGHTS)
     ap.add_argument("--eval-only", default="", help="evaluate these weights instead of training")
+    ap.add_argument("--learned-only", action="store_true",
+                    help="with --eval-only: run only the learned arm of the first case (profiling)")
     a = ap.parse_args(argv)
+    if a.eval_only and a.learned_only:
+        res = learned.compare(load_weights(a.eval_only), n=a.eval_n or a.n, newton_iters=a.eval_newton,
+                              arms=("mlp",))["mlp"]
+        print("learned", json.dumps({k: v for k, v in res.items() if k != "u"}), flush=True)
+        return
     if a.eval_only:
         params = load_weights(a.eval_only)
         for row in evaluate(params, a.eval_n or a.n, a.eval_newton):
