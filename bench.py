@@ -36,6 +36,15 @@ sys.path.insert(0, ROOT)
 METRIC = "ms/Newton iter & IP/s at 1e-8 rel residual, chosen vs plain FP64, 1 GB300"
 UNIT = "ms/Newton iter"
 N_STEPS = 20
+# the configurations the metric is quoted on: mesh n x n, load steps, material
+CONFIGS = {
+    1: {"n": 40, "n_steps": 10, "wb": {}},
+    2: {"n": 400, "n_steps": 20, "wb": {}},
+    3: {"n": 1000, "n_steps": 20, "wb": {"material_mode": 1, "c_cv": 0.2}},
+    4: {"n": 400, "n_steps": 20, "wb": {}},
+    5: {"n": 2000, "n_steps": 30, "wb": {"material_mode": 2, "c_cv": 0.3, "phi_lo_deg": 25.0, "phi_hi_deg": 35.0,
+                                         "pw_final": -5.0}},
+}
 # CG iterations of the first Newton iterations of the 400 x 400 solve, as run on
 # the GPU (identical on the CPU oracle); used by --impl reference to scale its
 # bounded CG sample to whole Newton iterations.
@@ -112,7 +121,7 @@ class ClockSampler:
 class CpuArm:
     """The C oracle on the host cores (bounded samples of the same workload)."""
 
-    def __init__(self, n, threads):
+    def __init__(self, n, threads, n_steps=N_STEPS, wb=None):
         import numpy as np
 
         from oracle import pyoracle as po
@@ -120,14 +129,15 @@ class CpuArm:
         self.n = n
         self.threads = threads
         t0 = time.perf_counter()
-        self.P = po.OracleProblem(po.default_params(n), nthreads=threads)
+        self.P = po.OracleProblem(po.default_params(n, **(wb or {})), nthreads=threads)
+        self.n_steps = n_steps
         self.t_setup = time.perf_counter() - t0
         self.u = np.zeros(self.P.neq)
 
     def sample(self, cg_per_iter, cg_sample):
         """one tangent assembly + cg_sample CG iterations + one residual,
         scaled to a Newton iteration of cg_per_iter CG iterations"""
-        lam = 1.0 / N_STEPS
+        lam = 1.0 / self.n_steps
         t0 = time.perf_counter()
         R = self.P.assemble(self.u, lam)
         t_asm = time.perf_counter() - t0
@@ -170,11 +180,20 @@ def run_reference(args):
         return 0
     threads = args.cpu_threads or os.cpu_count()
     n = args.n
-    mean_cg = sum(CFG2_CG_ITERS) / len(CFG2_CG_ITERS)
-    arm = CpuArm(n, threads)
+    arm = CpuArm(n, threads, args.n_steps, args.wb)
+    if n <= 100:
+        # small meshes: the oracle's own CG iteration count to 1e-8 on the first tangent
+        R = arm.P.assemble(arm.u, 1.0 / args.n_steps)
+        _, k = arm.P.pcg(R, rtol=1e-8, max_it=200000)
+        cg_iters, cg_note = [abs(k)], "the oracle's CG iterations to 1e-8 on the first tangent"
+    else:
+        # the measured 400 x 400 counts, scaled by n / 400 (CG iterations grow linearly with n here)
+        cg_iters = [c * n / 400.0 for c in CFG2_CG_ITERS]
+        cg_note = "the GPU's CG iterations per Newton iteration at 400x400 scaled by n/400"
+    mean_cg = sum(cg_iters) / len(cg_iters)
     samples = []
     for i in range(args.warmup + args.steps):
-        cg = CFG2_CG_ITERS[i] if i < len(CFG2_CG_ITERS) else mean_cg
+        cg = cg_iters[i] if i < len(cg_iters) else mean_cg
         r = arm.sample(cg, args.cpu_cg_sample if i >= args.warmup else 5)
         if i >= args.warmup:
             samples.append(r)
@@ -185,12 +204,12 @@ def run_reference(args):
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": False, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": "wellbore %dx%d order-2 quads, %d IPs, plain FP64, Jacobi-CG 1e-8, Newton 1e-8, "
-                               "%d load steps" % (n, n, 9 * n * n, N_STEPS)},
+                               "%d load steps (configuration %d)" % (n, n, 9 * n * n, args.n_steps, args.config)},
         "ip_per_s": statistics.mean(s["ip_per_s"] for s in samples),
         "cpu_baseline": {"value": ms, "unit": UNIT, "cores": threads, "kind": "port",
                          "sample": "per step: one tangent assembly + %d Jacobi-CG iterations of the C oracle, "
-                                   "scaled by the GPU's CG iteration count per Newton iteration (%.0f)"
-                                   % (samples[0]["cg_sample"], mean_cg)},
+                                   "scaled to %.0f CG iterations per Newton iteration (%s)"
+                                   % (samples[0]["cg_sample"], mean_cg, cg_note)},
         "e2e": {"value": ms, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
@@ -217,7 +236,8 @@ def run_gpu(args):
     dev = torch.device("cuda", local if ws > 1 else 0)
     torch.cuda.set_device(dev)
     n = args.n
-    wb = ip.WellboreMesh(ip.wellbore_params(n))
+    wb = ip.WellboreMesh(ip.wellbore_params(n, **args.wb))
+    N_STEPS = args.n_steps
     mixed = args.precision == "mixed"
     cg_rtol = args.mixed_cg_rtol if mixed else 1e-8
     A = ip.ElastoPlasticIntPointsStructMatrix(wb)         # device-resident arm
@@ -329,7 +349,7 @@ def run_gpu(args):
 
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
-        arm = CpuArm(n, args.cpu_threads or os.cpu_count())
+        arm = CpuArm(n, args.cpu_threads or os.cpu_count(), args.n_steps, args.wb)
         cpu = arm.sample(cg_per_iter, args.cpu_cg_sample)
         arm.close()
 
@@ -342,9 +362,11 @@ def run_gpu(args):
         "ms_per_step": ms_dev, "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64" if not mixed else "f32+f64",
         "data": "synthetic",
         "config": {"workload": "wellbore %dx%d order-2 quads, %d IPs, %d dofs, %s, Jacobi-CG %g, "
-                               "Newton 1e-8, %d load steps; first %d Newton iterations (warm-up %d)"
+                               "Newton 1e-8, %d load steps%s; first %d Newton iterations (warm-up %d); "
+                               "configuration %d"
                                % (n, n, A.n_ip, A.neq, "plain FP64" if not mixed else "mixed FP32/FP64", cg_rtol,
-                                  N_STEPS, args.warmup + args.steps, args.warmup),
+                                  N_STEPS, (", material %s" % json.dumps(args.wb)) if args.wb else "",
+                                  args.warmup + args.steps, args.warmup, args.config),
                    "l2": "inputs larger than L2 (tangent %.0f MB, element blocks %.0f MB)"
                          % (nb * 32 / 1e6, A.n_el * 1296 / 1e6),
                    "replicas": ws},
@@ -391,7 +413,8 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ipfem", choices=["ipfem", "reference"])
-    ap.add_argument("--n", type=int, default=400)
+    ap.add_argument("--config", type=int, default=2, choices=sorted(CONFIGS))
+    ap.add_argument("--n", type=int, default=0, help="mesh size (default: the configuration's)")
     ap.add_argument("--cpu-threads", type=int, default=0)
     ap.add_argument("--cpu-cg-sample", type=int, default=100)
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -402,6 +425,10 @@ def main():
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
+    cfg = CONFIGS[args.config]
+    args.n = args.n or cfg["n"]
+    args.n_steps = cfg["n_steps"]
+    args.wb = dict(cfg["wb"])
     if args.impl == "reference":
         return run_reference(args)
     return run_gpu(args)
