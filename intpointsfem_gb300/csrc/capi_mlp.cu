@@ -110,7 +110,7 @@ ipfem_status fcg_device(ipfem_ctx *c, const double *d_b, double scale, double rt
     if (!c->fcg_exec) {
         cudaGraph_t g = nullptr;
         MK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
-        for (int k = 0; k < batch; k++) launch_fcg_iteration(c);
+        for (int k = 0; k < batch; k++) launch_fcg_iteration(c, k & 1);
         MK(cudaStreamEndCapture(c->stream, &g));
         cudaError_t e = cudaGraphInstantiate(&c->fcg_exec, g, 0);
         cudaGraphDestroy(g);
@@ -120,7 +120,7 @@ ipfem_status fcg_device(ipfem_ctx *c, const double *d_b, double scale, double rt
     for (;;) {
         MK(cudaGraphLaunch(c->fcg_exec, c->stream));
         launched += batch;
-        c->launches += 4 * batch;
+        c->launches += 3 * batch;
         MK(cudaMemcpyAsync(m.h_sc, m.sc, sizeof(CGScalarsT<float>), cudaMemcpyDeviceToHost, c->stream));
         MK(cudaStreamSynchronize(c->stream));
         if (m.h_sc->done || launched >= max_it + batch) break;
@@ -173,6 +173,8 @@ ipfem_status ipfem_mlp_init(ipfem_ctx *c, uint64_t seed)
         MK(alloc(&m.M, (size_t)s.n_nodes * 20));
         MK(alloc(&m.r_old, (size_t)s.neq));
         MK(alloc(&m.y, (size_t)s.neq));
+        MK(alloc(&m.p2, (size_t)s.neq));
+        MK(cudaMalloc(&m.Gh, (size_t)s.n_nodes * 5 * 8));
         MK(alloc(&m.loss, 1));
         MK(alloc(&m.scal, 2));
         const std::vector<int32_t> slot = patch_slots(s, c->mx.sell, m.gr, m.gt);

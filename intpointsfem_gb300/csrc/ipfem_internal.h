@@ -126,6 +126,8 @@ struct MlpBuffers {
     float *O = nullptr;           // [n_nodes][20] network output
     float *M = nullptr;           // [5][n_nodes][4] triangular factor G (M = sigma G^T G sigma)
     float *y = nullptr;           // [neq] first stencil pass of the preconditioner
+    void *Gh = nullptr;           // [5][n_nodes] FP16 copy of G (4 halves per block) for the solves
+    float *p2 = nullptr;          // [neq] second search-direction buffer of the fused flexible CG
     float *r_old = nullptr;       // flexible-CG previous residual
     float *loss = nullptr, *scal = nullptr;
     // training scratch (allocated by the first gradient pass)
@@ -218,7 +220,7 @@ void launch_patch_features(ipfem_ctx *c, float *d_X);
 void launch_patch_net(ipfem_ctx *c, int64_t rows, const float *d_X, float *d_O);
 void launch_patch_operator(ipfem_ctx *c);
 void launch_fcg_init(ipfem_ctx *c, const double *d_b, double scale, float rtol, int max_it);
-void launch_fcg_iteration(ipfem_ctx *c);
+void launch_fcg_iteration(ipfem_ctx *c, int par);
 size_t patch_part_floats(int64_t n_nodes);
 void patch_learn_grad(ipfem_ctx *c, const float *d_r, const float *d_e, int P, float wk, float wp);
 void mlp_adam_step(ipfem_ctx *c, float lr);

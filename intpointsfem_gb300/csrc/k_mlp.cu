@@ -24,6 +24,7 @@
 // GEMMs run on the tensor cores in BF16 (operands rounded to BF16 in shared
 // memory) with FP32 accumulation (mma.m16n8k16).
 #include <cuda_bf16.h>
+#include <cuda_fp16.h>
 
 #include "ipfem_internal.h"
 
@@ -407,9 +408,30 @@ __device__ __forceinline__ float2 free2(float2 d)
 
 constexpr int NTRI = 5;          // factor blocks per node: k = 0..3 and the node (k = 4)
 
-// G[k][i] (float4, row-major 2x2, k = 0..4) from the network output O[n][20]
+__device__ __forceinline__ uint2 half4(float4 v)
+{
+    const __half2 a = __floats2half2_rn(v.x, v.y), b = __floats2half2_rn(v.z, v.w);
+    return make_uint2(*reinterpret_cast<const uint32_t *>(&a), *reinterpret_cast<const uint32_t *>(&b));
+}
+
+__device__ __forceinline__ float4 load_g(const float4 *__restrict__ g, int64_t idx)
+{
+    return __ldg(&g[idx]);
+}
+
+__device__ __forceinline__ float4 load_g(const uint2 *__restrict__ g, int64_t idx)
+{
+    const uint2 u = __ldg(&g[idx]);
+    const float2 a = __half22float2(*reinterpret_cast<const __half2 *>(&u.x));
+    const float2 b = __half22float2(*reinterpret_cast<const __half2 *>(&u.y));
+    return make_float4(a.x, a.y, b.x, b.y);
+}
+
+// G[k][i] (float4, row-major 2x2, k = 0..4) from the network output O[n][20],
+// and its FP16 copy Gh for the solves when given
 __global__ void __launch_bounds__(256) k_tri_build(int32_t n, GridInfo G, const float *__restrict__ O,
-                                                   const float2 *__restrict__ dinv, float4 *__restrict__ Gm)
+                                                   const float2 *__restrict__ dinv, float4 *__restrict__ Gm,
+                                                   uint2 *__restrict__ Gh)
 {
     const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
@@ -425,12 +447,16 @@ __global__ void __launch_bounds__(256) k_tri_build(int32_t n, GridInfo G, const 
                              oi[4 * k + 3] * fi.y * fj.y);
         }
         Gm[(int64_t)k * n + i] = gk;
+        if (Gh) Gh[(int64_t)k * n + i] = half4(gk);
     }
-    Gm[(int64_t)4 * n + i] = make_float4(expf(oi[16]) * fi.x, 0.f, oi[17] * fi.y * fi.x, expf(oi[18]) * fi.y);
+    const float4 g4 = make_float4(expf(oi[16]) * fi.x, 0.f, oi[17] * fi.y * fi.x, expf(oi[18]) * fi.y);
+    Gm[(int64_t)4 * n + i] = g4;
+    if (Gh) Gh[(int64_t)4 * n + i] = half4(g4);
 }
 
 // y_i = sum_k G_ik (sigma * x)_nbr(i,k)
-__device__ __forceinline__ float2 tri_mul(int32_t i, int32_t n, GridInfo G, const float4 *__restrict__ Gm,
+template <class GT>
+__device__ __forceinline__ float2 tri_mul(int32_t i, int32_t n, GridInfo G, const GT *__restrict__ Gm,
                                           const float2 *__restrict__ dinv, const float2 *__restrict__ x)
 {
     float2 y = make_float2(0.f, 0.f);
@@ -438,7 +464,7 @@ __device__ __forceinline__ float2 tri_mul(int32_t i, int32_t n, GridInfo G, cons
     for (int k = 0; k < NTRI; k++) {
         const int32_t j = patch_nbr(i, k, G);
         if (j < 0) continue;
-        const float4 m = __ldg(&Gm[(int64_t)k * n + i]);
+        const float4 m = load_g(Gm, (int64_t)k * n + i);
         const float2 s = sqrt2(__ldg(&dinv[j])), v = __ldg(&x[j]);
         const float vx = s.x * v.x, vy = s.y * v.y;
         y.x = fmaf(m.x, vx, fmaf(m.y, vy, y.x));
@@ -449,7 +475,8 @@ __device__ __forceinline__ float2 tri_mul(int32_t i, int32_t n, GridInfo G, cons
 
 // z_j = sigma_j * sum_k G_{i,k}^T y_i over the nodes i = nbr(j, 8-k) that
 // hold j at position k (gather form of G^T)
-__device__ __forceinline__ float2 trit_mul(int32_t j, int32_t n, GridInfo G, const float4 *__restrict__ Gm,
+template <class GT>
+__device__ __forceinline__ float2 trit_mul(int32_t j, int32_t n, GridInfo G, const GT *__restrict__ Gm,
                                            const float2 *__restrict__ dinv, const float2 *__restrict__ y)
 {
     float2 z = make_float2(0.f, 0.f);
@@ -457,7 +484,7 @@ __device__ __forceinline__ float2 trit_mul(int32_t j, int32_t n, GridInfo G, con
     for (int k = 0; k < NTRI; k++) {
         const int32_t i = patch_nbr(j, 8 - k, G);
         if (i < 0) continue;
-        const float4 m = __ldg(&Gm[(int64_t)k * n + i]);
+        const float4 m = load_g(Gm, (int64_t)k * n + i);
         const float2 v = __ldg(&y[i]);
         z.x = fmaf(m.x, v.x, fmaf(m.z, v.y, z.x));
         z.y = fmaf(m.y, v.x, fmaf(m.w, v.y, z.y));
@@ -467,7 +494,8 @@ __device__ __forceinline__ float2 trit_mul(int32_t j, int32_t n, GridInfo G, con
 }
 
 // y = G (sigma * r); skipped once the solve is done when sc is given
-__global__ void __launch_bounds__(256) k_tri_first(int32_t n, GridInfo G, const float4 *__restrict__ Gm,
+template <class GT>
+__global__ void __launch_bounds__(256) k_tri_first(int32_t n, GridInfo G, const GT *__restrict__ Gm,
                                                    const float2 *__restrict__ dinv, const float2 *__restrict__ r,
                                                    float2 *__restrict__ y, const CGScalarsT<float> *sc)
 {
@@ -582,60 +610,10 @@ __global__ void __launch_bounds__(256) k_fcg_init(int32_t n_nodes, const double 
     }
 }
 
-// x += alpha p, r_old = r, r -= alpha q; r.r; convergence / stagnation
-__global__ void __launch_bounds__(256) k_fcg_update(int32_t n_nodes, const float *__restrict__ p,
-                                                    const float *__restrict__ q, float *__restrict__ x,
-                                                    float *__restrict__ r, float *__restrict__ r_old, float *part,
-                                                    int64_t n_part, unsigned *ticket, CGScalarsT<float> *sc,
-                                                    int stall_window)
-{
-    if (*reinterpret_cast<volatile int *>(&sc->done)) return;
-    const float alpha = *reinterpret_cast<volatile float *>(&sc->alpha);
-    const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    float v[1] = {0.f};
-    if (i < n_nodes) {
-        const float2 pp = reinterpret_cast<const float2 *>(p)[i];
-        const float2 qq = reinterpret_cast<const float2 *>(q)[i];
-        float2 xx = reinterpret_cast<float2 *>(x)[i];
-        float2 rr = reinterpret_cast<float2 *>(r)[i];
-        reinterpret_cast<float2 *>(r_old)[i] = rr;
-        xx.x = fmaf(alpha, pp.x, xx.x);
-        xx.y = fmaf(alpha, pp.y, xx.y);
-        rr.x = fmaf(-alpha, qq.x, rr.x);
-        rr.y = fmaf(-alpha, qq.y, rr.y);
-        reinterpret_cast<float2 *>(x)[i] = xx;
-        reinterpret_cast<float2 *>(r)[i] = rr;
-        v[0] = fmaf(rr.y, rr.y, rr.x * rr.x);
-    }
-    if (fcg_partials<1>(v, part, n_part, ticket)) {
-        float o[1];
-        fcg_final<1>(part, n_part, o);
-        if (threadIdx.x == 0) {
-            const float rr = o[0];
-            sc->rr = rr;
-            sc->iters += 1;
-            if (rr < 0.98f * sc->rr_best) {
-                sc->rr_best = rr;
-                sc->it_best = sc->iters;
-            }
-            if (rr <= sc->thr) {
-                sc->done = 1;
-            } else if (!(rr == rr) || sc->iters - sc->it_best > stall_window) {
-                sc->done = 1;
-                sc->status = kStatusFallback;
-            } else if (sc->iters >= sc->max_it) {
-                sc->done = 1;
-                sc->status = IPFEM_NONCONVERGED;
-            }
-            *ticket = 0u;
-        }
-    }
-}
-
 // z = M r = sigma * (G^T y) with y = G (sigma * r) from k_tri_first; partial
 // r.z and r_old.z; last CTA: Polak-Ribiere beta = (r.z - r_old.z) / rz_prev
 // (clipped at 0), rz = r.z
-__global__ void __launch_bounds__(256) k_tri_precond(int32_t n, GridInfo G, const float4 *__restrict__ Gm,
+__global__ void __launch_bounds__(256) k_tri_precond(int32_t n, GridInfo G, const uint2 *__restrict__ Gm,
                                                      const float2 *__restrict__ dinv, const float2 *__restrict__ y,
                                                      const float *__restrict__ r, const float *__restrict__ r_old,
                                                      float *__restrict__ z, float *part, int64_t n_part,
@@ -663,6 +641,131 @@ __global__ void __launch_bounds__(256) k_tri_precond(int32_t n, GridInfo G, cons
             if (!(rz > 0.f)) {          // M r is not a descent direction
                 sc->done = 1;
                 sc->status = kStatusFallback;
+            }
+            *ticket = 0u;
+        }
+    }
+}
+
+// ----------------------------------------- fused flexible-CG iteration (FP32)
+// One iteration = k_fcg_spmv, k_fcg_update_first, k_tri_precond, with the
+// search direction and the residual double-buffered (the caller alternates
+// the buffers): the p-update of the previous iteration is formed on the fly
+// inside the SpMV, the x/r update inside the first factor pass.
+
+// p_new = z + beta p_old (the owner stores it, gatherers form it for their
+// columns), q = K p_new, partials of p_new.q; last CTA: alpha = rz / pq.
+// Node-ordered SELL rows; the tangent and its column indices are streamed
+// (evict-first) so that z and p_old stay in L2.
+__global__ void __launch_bounds__(256) k_fcg_spmv(int32_t n, const int64_t *__restrict__ slice_base,
+                                                  const int32_t *__restrict__ rowlen, const int32_t *__restrict__ scol,
+                                                  const float4 *__restrict__ K, const uint8_t *__restrict__ fixed,
+                                                  const float2 *__restrict__ z, const float2 *__restrict__ p_old,
+                                                  float2 *__restrict__ p_new, float2 *__restrict__ q, float *part,
+                                                  int64_t n_part, unsigned *ticket, CGScalarsT<float> *sc)
+{
+    if (*reinterpret_cast<volatile int *>(&sc->done)) return;
+    const float beta = *reinterpret_cast<volatile float *>(&sc->beta);
+    const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    float v[1] = {0.f};
+    if (i < n) {
+        const int64_t base = __ldg(&slice_base[i >> 5]) + (i & 31);
+        const int len = __ldg(&rowlen[i]);
+        float y0 = 0.f, y1 = 0.f;
+#pragma unroll 4
+        for (int k = 0; k < len; k++) {
+            const int64_t s = base + (int64_t)k * 32;
+            const int32_t c = __ldcs(&scol[s]);
+            const float4 a = __ldcs(&K[s]);
+            const float2 zz = __ldg(&z[c]), pp = __ldg(&p_old[c]);
+            const float px = fmaf(beta, pp.x, zz.x), py = fmaf(beta, pp.y, zz.y);
+            y0 = fmaf(a.y, py, fmaf(a.x, px, y0));
+            y1 = fmaf(a.w, py, fmaf(a.z, px, y1));
+        }
+        if (fixed[2 * (int64_t)i]) y0 = 0.f;
+        if (fixed[2 * (int64_t)i + 1]) y1 = 0.f;
+        q[i] = make_float2(y0, y1);
+        const float2 zi = z[i], pi = p_old[i];
+        const float2 pn = make_float2(fmaf(beta, pi.x, zi.x), fmaf(beta, pi.y, zi.y));
+        p_new[i] = pn;
+        v[0] = fmaf(pn.y, y1, pn.x * y0);
+    }
+    if (fcg_partials<1>(v, part, n_part, ticket)) {
+        float o[1];
+        fcg_final<1>(part, n_part, o);
+        if (threadIdx.x == 0) {
+            const float pq = o[0];
+            sc->pq = pq;
+            if (!(pq > 0.f)) {
+                sc->done = 1;
+                sc->status = kStatusFallback;
+            } else {
+                sc->alpha = sc->rz / pq;
+            }
+            *ticket = 0u;
+        }
+    }
+}
+
+// x += alpha p, r_new = r_old - alpha q (the owner stores it, the factor
+// pass forms it for its neighbours), y = G (sigma * r_new); partials of
+// r_new.r_new; last CTA: convergence, stagnation and iteration limit
+__global__ void __launch_bounds__(256) k_fcg_update_first(int32_t n, GridInfo G, const uint2 *__restrict__ Gm,
+                                                          const float2 *__restrict__ dinv,
+                                                          const float2 *__restrict__ p, const float2 *__restrict__ q,
+                                                          float2 *__restrict__ x, const float2 *__restrict__ r_old,
+                                                          float2 *__restrict__ r_new, float2 *__restrict__ y,
+                                                          float *part, int64_t n_part, unsigned *ticket,
+                                                          CGScalarsT<float> *sc, int stall_window)
+{
+    if (*reinterpret_cast<volatile int *>(&sc->done)) return;
+    const float alpha = *reinterpret_cast<volatile float *>(&sc->alpha);
+    const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    float v[1] = {0.f};
+    if (i < n) {
+        const float2 pp = p[i];
+        float2 xx = x[i];
+        xx.x = fmaf(alpha, pp.x, xx.x);
+        xx.y = fmaf(alpha, pp.y, xx.y);
+        x[i] = xx;
+        float2 acc = make_float2(0.f, 0.f);
+#pragma unroll
+        for (int k = 0; k < NTRI; k++) {
+            const int32_t j = patch_nbr(i, k, G);
+            if (j < 0) continue;
+            const float2 ro = __ldg(&r_old[j]), qq = __ldg(&q[j]);
+            const float2 rn = make_float2(fmaf(-alpha, qq.x, ro.x), fmaf(-alpha, qq.y, ro.y));
+            if (k == 4) {
+                r_new[i] = rn;
+                v[0] = fmaf(rn.y, rn.y, rn.x * rn.x);
+            }
+            const float4 m = load_g(Gm, (int64_t)k * n + i);
+            const float2 s = sqrt2(__ldg(&dinv[j]));
+            const float vx = s.x * rn.x, vy = s.y * rn.y;
+            acc.x = fmaf(m.x, vx, fmaf(m.y, vy, acc.x));
+            acc.y = fmaf(m.z, vx, fmaf(m.w, vy, acc.y));
+        }
+        y[i] = acc;
+    }
+    if (fcg_partials<1>(v, part, n_part, ticket)) {
+        float o[1];
+        fcg_final<1>(part, n_part, o);
+        if (threadIdx.x == 0) {
+            const float rr = o[0];
+            sc->rr = rr;
+            sc->iters += 1;
+            if (rr < 0.98f * sc->rr_best) {
+                sc->rr_best = rr;
+                sc->it_best = sc->iters;
+            }
+            if (rr <= sc->thr) {
+                sc->done = 1;
+            } else if (!(rr == rr) || sc->iters - sc->it_best > stall_window) {
+                sc->done = 1;
+                sc->status = kStatusFallback;
+            } else if (sc->iters >= sc->max_it) {
+                sc->done = 1;
+                sc->status = IPFEM_NONCONVERGED;
             }
             *ticket = 0u;
         }
@@ -995,7 +1098,8 @@ void launch_patch_operator(ipfem_ctx *c)
     launch_patch_features(c, m.X);
     launch_patch_net(c, n, m.X, m.O);
     k_tri_build<<<(n + 255) / 256, 256, 0, c->stream>>>(n, G, m.O, reinterpret_cast<const float2 *>(c->mx.dinv),
-                                                        reinterpret_cast<float4 *>(m.M));
+                                                        reinterpret_cast<float4 *>(m.M),
+                                                        reinterpret_cast<uint2 *>(m.Gh));
     c->launches += 3;
     m.op_valid = true;
 }
@@ -1010,38 +1114,61 @@ static unsigned fcg_grid(const ipfem_ctx *c)
     return (unsigned)((c->s.n_nodes + 255) / 256);
 }
 
-static void launch_precond(ipfem_ctx *c)
+// z = M r for r = R[par] (r_old = R[1 - par]), the two factor passes
+static void launch_precond(ipfem_ctx *c, int par)
 {
     GridInfo G{c->mlp.gr, c->mlp.gt};
     MixedBuffers &m = c->mx;
+    float *R[2] = {m.r, c->mlp.r_old};
     // the precond partials use the FP64 partial array (as 2 x n_red floats)
     float *part = reinterpret_cast<float *>(c->d_part);
-    const float4 *Gm = reinterpret_cast<const float4 *>(c->mlp.M);
+    const uint2 *Gh = reinterpret_cast<const uint2 *>(c->mlp.Gh);
     const float2 *d2 = reinterpret_cast<const float2 *>(m.dinv);
     float2 *y = reinterpret_cast<float2 *>(c->mlp.y);
-    k_tri_first<<<fcg_grid(c), 256, 0, c->stream>>>(c->s.n_nodes, G, Gm, d2, reinterpret_cast<const float2 *>(m.r), y,
-                                                    m.sc);
-    k_tri_precond<<<fcg_grid(c), 256, 0, c->stream>>>(c->s.n_nodes, G, Gm, d2, y, m.r, c->mlp.r_old, m.z, part,
+    k_tri_first<<<fcg_grid(c), 256, 0, c->stream>>>(c->s.n_nodes, G, Gh, d2, reinterpret_cast<const float2 *>(R[par]),
+                                                    y, m.sc);
+    k_tri_precond<<<fcg_grid(c), 256, 0, c->stream>>>(c->s.n_nodes, G, Gh, d2, y, R[par], R[1 - par], m.z, part,
                                                       (int64_t)fcg_grid(c), c->d_counters + 7, m.sc);
 }
 
+// r = R[0] = b*scale, x = 0, P[0] = 0, R[1] = 0; z = M r and beta = 0
 void launch_fcg_init(ipfem_ctx *c, const double *d_b, double scale, float rtol, int max_it)
 {
     MixedBuffers &m = c->mx;
     k_fcg_init<<<fcg_grid(c), 256, 0, c->stream>>>(c->s.n_nodes, d_b, scale, m.x, m.r, m.p, c->mlp.r_old, m.part,
                                                    (int64_t)fcg_grid(c), c->d_counters + 4, m.sc, rtol, max_it);
-    launch_precond(c);
-    launch_cg32_pupdate_only(c);
+    launch_precond(c, 0);
 }
 
-void launch_fcg_iteration(ipfem_ctx *c)
+// iteration k (par = k % 2): P[par] -> P[1-par] in the SpMV, R[par] -> R[1-par]
+// in the update, z from R[1-par]
+void launch_fcg_iteration(ipfem_ctx *c, int par)
 {
     MixedBuffers &m = c->mx;
-    launch_cg32_spmv_only(c);
-    k_fcg_update<<<fcg_grid(c), 256, 0, c->stream>>>(c->s.n_nodes, m.p, m.q, m.x, m.r, c->mlp.r_old, m.part,
-                                                     (int64_t)fcg_grid(c), c->d_counters + 6, m.sc, kStallWindow);
-    launch_precond(c);
-    launch_cg32_pupdate_only(c);
+    MlpBuffers &l = c->mlp;
+    const SellDev &L = m.dsell;
+    GridInfo G{l.gr, l.gt};
+    const int32_t n = c->s.n_nodes;
+    float2 *P[2] = {reinterpret_cast<float2 *>(m.p), reinterpret_cast<float2 *>(l.p2)};
+    float2 *R[2] = {reinterpret_cast<float2 *>(m.r), reinterpret_cast<float2 *>(l.r_old)};
+    const float2 *d2 = reinterpret_cast<const float2 *>(m.dinv);
+    float *part = m.part;
+    k_fcg_spmv<<<fcg_grid(c), 256, 0, c->stream>>>(n, L.slice_base, L.rowlen, L.sell_col,
+                                                   reinterpret_cast<const float4 *>(m.K), c->d_fixed,
+                                                   reinterpret_cast<const float2 *>(m.z), P[par], P[1 - par],
+                                                   reinterpret_cast<float2 *>(m.q), part, (int64_t)fcg_grid(c),
+                                                   c->d_counters + 5, m.sc);
+    k_fcg_update_first<<<fcg_grid(c), 256, 0, c->stream>>>(n, G, reinterpret_cast<const uint2 *>(l.Gh), d2,
+                                                           P[1 - par], reinterpret_cast<const float2 *>(m.q),
+                                                           reinterpret_cast<float2 *>(m.x), R[par], R[1 - par],
+                                                           reinterpret_cast<float2 *>(l.y), part, (int64_t)fcg_grid(c),
+                                                           c->d_counters + 6, m.sc, kStallWindow);
+    float *part2 = reinterpret_cast<float *>(c->d_part);
+    k_tri_precond<<<fcg_grid(c), 256, 0, c->stream>>>(n, G, reinterpret_cast<const uint2 *>(l.Gh), d2,
+                                                      reinterpret_cast<const float2 *>(l.y),
+                                                      reinterpret_cast<const float *>(R[1 - par]),
+                                                      reinterpret_cast<const float *>(R[par]), m.z, part2,
+                                                      (int64_t)fcg_grid(c), c->d_counters + 7, m.sc);
 }
 
 // ------------------------------------------------------------ training pass
@@ -1110,7 +1237,7 @@ void patch_learn_grad(ipfem_ctx *c, const float *d_r, const float *d_e, int P, f
     k_bias_act<<<eh, 256, 0, st>>>(n, 128, m.H2, W + kOffB2, 1);
     gemm(c, n, NOUT, 128, m.H2, 128, 0, W + kOffW3, NOUT, 0, m.O, NOUT);
     k_bias_act<<<(unsigned)(((int64_t)n * NOUT + 255) / 256), 256, 0, st>>>(n, NOUT, m.O, W + kOffB3, 0);
-    k_tri_build<<<gn, 256, 0, st>>>(n, G, m.O, d2, Gm);
+    k_tri_build<<<gn, 256, 0, st>>>(n, G, m.O, d2, Gm, nullptr);
     m.op_valid = false;
     cudaMemsetAsync(m.dN, 0, (size_t)n * NOUT * sizeof(float), st);
     cudaMemsetAsync(m.loss, 0, sizeof(float), st);

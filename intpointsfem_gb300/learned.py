@@ -119,7 +119,8 @@ def compare(params, n=400, pw=-12.0, phi=28.0, n_steps=10, newton_iters=6, cg_rt
         out[name] = {"newton_iters": st.newton_iters, "cg_iters": int(st.cg_iters),
                      "ms_per_newton": 1e3 * dt / max(1, st.newton_iters), "ms_solve": st.ms_solve,
                      "fallbacks": int(getattr(st, "fcg_fallbacks", 0)),
-                     "residuals": log[:, 2].tolist(), "u": u.cpu().numpy()}
+                     "residuals": log[:, 2].tolist(), "steps": [int(x) for x in log[:, 0]],
+                     "cg_per_newton": [int(x) for x in log[:, 1]], "u": u.cpu().numpy()}
         sm.close()
         wb.close()
     return out

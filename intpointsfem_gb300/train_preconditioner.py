@@ -39,6 +39,8 @@ def evaluate(params, n, newton_iters, cases=((-12.0, 28.0), (-25.0, 33.0))):
                     "cg_iters_jacobi": j["cg_iters"], "cg_iters_learned": m["cg_iters"],
                     "ms_solve_jacobi": j["ms_solve"], "ms_solve_learned": m["ms_solve"],
                     "fallbacks": m["fallbacks"],
+                    "load_steps_jacobi": j["steps"], "load_steps_learned": m["steps"],
+                    "cg_per_newton_jacobi": j["cg_per_newton"], "cg_per_newton_learned": m["cg_per_newton"],
                     "max_rel_du": float(np.abs(m["u"] - j["u"]).max() / np.abs(j["u"]).max())})
     return out
 
