@@ -24,7 +24,6 @@
 // GEMMs run on the tensor cores in BF16 (operands rounded to BF16 in shared
 // memory) with FP32 accumulation (mma.m16n8k16).
 #include <cuda_bf16.h>
-#include <cuda_fp16.h>
 
 #include "ipfem_internal.h"
 
@@ -408,10 +407,18 @@ __device__ __forceinline__ float2 free2(float2 d)
 
 constexpr int NTRI = 5;          // factor blocks per node: k = 0..3 and the node (k = 4)
 
+// the log-diagonal outputs are clamped to [-30, 30] before exp (a network far
+// outside its training data cannot overflow the factor)
+__device__ __forceinline__ float clamp_log(float o)
+{
+    return fminf(fmaxf(o, -30.f), 30.f);
+}
+
+// BF16 copy of a factor block for the solves (FP32 range, so no overflow for
+// any finite factor; the same rounded G enters both passes, so M stays SPD)
 __device__ __forceinline__ uint2 half4(float4 v)
 {
-    const __half2 a = __floats2half2_rn(v.x, v.y), b = __floats2half2_rn(v.z, v.w);
-    return make_uint2(*reinterpret_cast<const uint32_t *>(&a), *reinterpret_cast<const uint32_t *>(&b));
+    return make_uint2(pack_bf16(v.x, v.y), pack_bf16(v.z, v.w));
 }
 
 __device__ __forceinline__ float4 load_g(const float4 *__restrict__ g, int64_t idx)
@@ -422,13 +429,13 @@ __device__ __forceinline__ float4 load_g(const float4 *__restrict__ g, int64_t i
 __device__ __forceinline__ float4 load_g(const uint2 *__restrict__ g, int64_t idx)
 {
     const uint2 u = __ldg(&g[idx]);
-    const float2 a = __half22float2(*reinterpret_cast<const __half2 *>(&u.x));
-    const float2 b = __half22float2(*reinterpret_cast<const __half2 *>(&u.y));
+    const float2 a = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162 *>(&u.x));
+    const float2 b = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162 *>(&u.y));
     return make_float4(a.x, a.y, b.x, b.y);
 }
 
 // G[k][i] (float4, row-major 2x2, k = 0..4) from the network output O[n][20],
-// and its FP16 copy Gh for the solves when given
+// and its BF16 copy Gh for the solves when given
 __global__ void __launch_bounds__(256) k_tri_build(int32_t n, GridInfo G, const float *__restrict__ O,
                                                    const float2 *__restrict__ dinv, float4 *__restrict__ Gm,
                                                    uint2 *__restrict__ Gh)
@@ -449,7 +456,8 @@ __global__ void __launch_bounds__(256) k_tri_build(int32_t n, GridInfo G, const 
         Gm[(int64_t)k * n + i] = gk;
         if (Gh) Gh[(int64_t)k * n + i] = half4(gk);
     }
-    const float4 g4 = make_float4(expf(oi[16]) * fi.x, 0.f, oi[17] * fi.y * fi.x, expf(oi[18]) * fi.y);
+    const float4 g4 = make_float4(expf(clamp_log(oi[16])) * fi.x, 0.f, oi[17] * fi.y * fi.x,
+                                  expf(clamp_log(oi[18])) * fi.y);
     Gm[(int64_t)4 * n + i] = g4;
     if (Gh) Gh[(int64_t)4 * n + i] = half4(g4);
 }
@@ -648,7 +656,8 @@ __global__ void __launch_bounds__(256) k_tri_precond(int32_t n, GridInfo G, cons
 }
 
 // ----------------------------------------- fused flexible-CG iteration (FP32)
-// One iteration = k_fcg_spmv, k_fcg_update_first, k_tri_precond, with the
+// One iteration = k_fcg_spmv, k_fcg_update_first, k_tri_precond (factor in
+// BF16), with the
 // search direction and the residual double-buffered (the caller alternates
 // the buffers): the p-update of the previous iteration is formed on the fly
 // inside the SpMV, the x/r update inside the first factor pass.
@@ -760,7 +769,7 @@ __global__ void __launch_bounds__(256) k_fcg_update_first(int32_t n, GridInfo G,
             }
             if (rr <= sc->thr) {
                 sc->done = 1;
-            } else if (!(rr == rr) || sc->iters - sc->it_best > stall_window) {
+            } else if (!(rr == rr) || sc->iters - sc->it_best > max(stall_window, sc->it_best)) {
                 sc->done = 1;
                 sc->status = kStatusFallback;
             } else if (sc->iters >= sc->max_it) {
@@ -1012,9 +1021,10 @@ __global__ void __launch_bounds__(256) k_tri_dO(int32_t n, GridInfo G, const flo
         d[4 * k + 2] = (gi[4 * k + 2] + ck * hi[4 * k + 2]) * fi.y * fj.x;
         d[4 * k + 3] = (gi[4 * k + 3] + ck * hi[4 * k + 3]) * fi.y * fj.y;
     }
-    d[16] = ((gi[16] + ck * hi[16]) * expf(oi[16]) - 2.f * wk / nf) * fi.x;
+    const bool in16 = fabsf(oi[16]) < 30.f, in18 = fabsf(oi[18]) < 30.f;
+    d[16] = in16 ? ((gi[16] + ck * hi[16]) * expf(oi[16]) - 2.f * wk / nf) * fi.x : 0.f;
     d[17] = (gi[18] + ck * hi[18]) * fi.y * fi.x;
-    d[18] = ((gi[19] + ck * hi[19]) * expf(oi[18]) - 2.f * wk / nf) * fi.y;
+    d[18] = in18 ? ((gi[19] + ck * hi[19]) * expf(oi[18]) - 2.f * wk / nf) * fi.y : 0.f;
     d[19] = 0.f;
 }
 
@@ -1104,9 +1114,10 @@ void launch_patch_operator(ipfem_ctx *c)
     m.op_valid = true;
 }
 
-// FCG gives up (and the caller falls back to Jacobi-PCG) after this many
-// iterations without a 2 % drop of |r|^2; M is SPD, so this only guards
-// against a network evaluated far outside its training data
+// FCG gives up (and the caller falls back to Jacobi-PCG) when |r|^2 has not
+// dropped by 2 % for max(this, iterations to the best |r|^2 so far)
+// iterations; M is SPD, so this only guards against a network evaluated far
+// outside its training data
 constexpr int kStallWindow = 2000;
 
 static unsigned fcg_grid(const ipfem_ctx *c)

@@ -29,11 +29,11 @@ def load_weights(path=WEIGHTS):
     return np.load(path).astype(np.float32)
 
 
-def evaluate(params, n, newton_iters, cases=((-12.0, 28.0), (-25.0, 33.0))):
+def evaluate(params, n, newton_iters, cases=((-12.0, 28.0), (-25.0, 33.0)), **kw):
     """Jacobi-PCG vs learned FCG over the same Newton iterations of held-out problems"""
     out = []
     for pw, phi in cases:
-        res = learned.compare(params, n=n, pw=pw, phi=phi, newton_iters=newton_iters)
+        res = learned.compare(params, n=n, pw=pw, phi=phi, newton_iters=newton_iters, **kw)
         j, m = res["jacobi"], res["mlp"]
         out.append({"n": n, "pw": pw, "phi": phi, "newton_iters": m["newton_iters"],
                     "cg_iters_jacobi": j["cg_iters"], "cg_iters_learned": m["cg_iters"],
@@ -57,17 +57,21 @@ def main(argv=None):
     ap.add_argument("--eval-newton", type=int, default=4)
     ap.add_argument("--out", default=WEIGHTS)
     ap.add_argument("--eval-only", default="", help="evaluate these weights instead of training")
+    ap.add_argument("--material-mode", type=int, default=0, help="0 uniform, 1 lognormal cohesion, 2 + friction angle")
+    ap.add_argument("--c-cv", type=float, default=0.2)
+    ap.add_argument("--n-steps", type=int, default=10)
     ap.add_argument("--learned-only", action="store_true",
                     help="with --eval-only: run only the learned arm of the first case (profiling)")
     a = ap.parse_args(argv)
+    mat = {"material_mode": a.material_mode, "c_cv": a.c_cv} if a.material_mode else {}
     if a.eval_only and a.learned_only:
         res = learned.compare(load_weights(a.eval_only), n=a.eval_n or a.n, newton_iters=a.eval_newton,
-                              arms=("mlp",))["mlp"]
+                              n_steps=a.n_steps, arms=("mlp",), **mat)["mlp"]
         print("learned", json.dumps({k: v for k, v in res.items() if k != "u"}), flush=True)
         return
     if a.eval_only:
         params = load_weights(a.eval_only)
-        for row in evaluate(params, a.eval_n or a.n, a.eval_newton):
+        for row in evaluate(params, a.eval_n or a.n, a.eval_newton, n_steps=a.n_steps, **mat):
             print("eval", json.dumps(row), flush=True)
         return
     t0 = time.time()

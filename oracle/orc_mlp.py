@@ -14,7 +14,8 @@ device kernels do; products and sums run in FP64.
 Node i = b*gr + a; patch position k = 3*(db+1) + (da+1) for da, db in
 {-1, 0, 1}.  G has the blocks k = 0..3 (the lower neighbours) and k = 4 (the
 node): G_ik = O_i[4k .. 4k+3] as row-major 2x2 for k < 4 and
-G_i4 = [[exp(O_i[16]), 0], [O_i[17], exp(O_i[18])]]; O_i[19] is unused.
+G_i4 = [[exp(O_i[16]), 0], [O_i[17], exp(O_i[18])]] with O_i[16], O_i[18]
+clamped to [-30, 30]; O_i[19] is unused.
 Entries that touch a Dirichlet dof are 0.  Parameter layout of the library:
 W1[32][128] b1[128] W2[128][128] b2[128] W3[128][20] b3[20].
 """
@@ -102,9 +103,9 @@ def factor(gr, gt, O, dinv):
         i = np.nonzero(ok)[0]
         j = nb[i, k]
         G[k, i] = O[i, 4 * k:4 * k + 4].reshape(-1, 2, 2) * f[i][:, :, None] * f[j][:, None, :]
-    G[4, :, 0, 0] = np.exp(O[:, 16]) * f[:, 0]
+    G[4, :, 0, 0] = np.exp(np.clip(O[:, 16], -30.0, 30.0)) * f[:, 0]
     G[4, :, 1, 0] = O[:, 17] * f[:, 1] * f[:, 0]
-    G[4, :, 1, 1] = np.exp(O[:, 18]) * f[:, 1]
+    G[4, :, 1, 1] = np.exp(np.clip(O[:, 18], -30.0, 30.0)) * f[:, 1]
     return G
 
 
@@ -167,12 +168,14 @@ def dO_from_dG(O, dG, dinv, gr, gt, dlogdet=None):
         i = np.nonzero(ok)[0]
         j = nb[i, k]
         dO[i, 4 * k:4 * k + 4] = (dG[k, i] * f[i][:, :, None] * f[j][:, None, :]).reshape(-1, 4)
-    dO[:, 16] = dG[4, :, 0, 0] * np.exp(O[:, 16]) * f[:, 0]
+    in16 = (np.abs(O[:, 16]) < 30.0).astype(np.float64)
+    in18 = (np.abs(O[:, 18]) < 30.0).astype(np.float64)
+    dO[:, 16] = dG[4, :, 0, 0] * np.exp(O[:, 16]) * f[:, 0] * in16
     dO[:, 17] = dG[4, :, 1, 0] * f[:, 1] * f[:, 0]
-    dO[:, 18] = dG[4, :, 1, 1] * np.exp(O[:, 18]) * f[:, 1]
+    dO[:, 18] = dG[4, :, 1, 1] * np.exp(O[:, 18]) * f[:, 1] * in18
     if dlogdet is not None:
-        dO[:, 16] += dlogdet[:, 0]
-        dO[:, 18] += dlogdet[:, 1]
+        dO[:, 16] += dlogdet[:, 0] * in16
+        dO[:, 18] += dlogdet[:, 1] * in18
     return dO
 
 
