@@ -181,8 +181,9 @@ ipfem_status ipfem_scatter_residual(ipfem_ctx *ctx, const double *d_sigma_w, dou
 
 /* The same canonical dot product for callers that cannot allocate device
  * memory (an application that serves all device memory from its own
- * preallocated pool, or code running under stream capture, where cudaMalloc
- * is not allowed).  No counterpart in the reference.  Needs no context: d_a and
+ * preallocated pool, or a latency-critical pipeline that must not call
+ * cudaMalloc, which synchronises the device).  No counterpart in the
+ * reference.  Needs no context: d_a and
  * d_b are device vectors of n doubles (n even, n <= 33,554,432), the result is
  * written to the device double *d_out, asynchronously on `stream`
  * (cudaStream_t, NULL = legacy default stream).  The scratch lives in a

@@ -440,8 +440,8 @@ void launch_axpy_u(ipfem_ctx *c, double *d_u, const double *d_du)
 // Some callers of this library cannot allocate device memory: a host
 // application that hands every device byte out of its own preallocated pool
 // (so that a solve never triggers cudaMalloc, which synchronises the device
-// and fragments the pool), or code that runs while a stream is being
-// captured, where cudaMalloc is not permitted.  For them the dot kernel above
+// and fragments the pool), or a latency-critical pipeline that must never
+// stall on an allocation.  For them the dot kernel above
 // runs with its scratch (the per-CTA partial sums and the last-CTA ticket) in
 // the file-scope array below instead of in a context's buffers.  The array
 // holds kNoAllocMaxPartials partials (512 KiB), so vectors of up to

@@ -1,8 +1,9 @@
 """The allocation-free dot product (ipfem_dot_noalloc) against the context dot.
 
 ipfem_dot_noalloc serves callers that must not allocate device memory: an
-application that owns all device memory through its own pool, or code that
-runs under stream capture.  It keeps its scratch in a fixed array inside the
+application that owns all device memory through its own pool, or a
+latency-critical pipeline that must not stall on cudaMalloc (which
+synchronises the device).  It keeps its scratch in a fixed array inside the
 library instead of in a context, so this file checks, through the C-ABI,
 that two consecutive calls give exactly the context dot's result (the same
 canonical reduction order, so the comparison is exact), and that a length
