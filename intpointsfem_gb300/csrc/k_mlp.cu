@@ -25,6 +25,9 @@
 // memory) with FP32 accumulation (mma.m16n8k16).
 #include <cuda_bf16.h>
 
+#include <algorithm>
+#include <cmath>
+
 #include "ipfem_internal.h"
 
 namespace ipfem {
@@ -1115,10 +1118,15 @@ void launch_patch_operator(ipfem_ctx *c)
 }
 
 // FCG gives up (and the caller falls back to Jacobi-PCG) when |r|^2 has not
-// dropped by 2 % for max(this, iterations to the best |r|^2 so far)
-// iterations; M is SPD, so this only guards against a network evaluated far
-// outside its training data
-constexpr int kStallWindow = 2000;
+// dropped by 2 % for max(stall window, iterations to the best |r|^2 so far)
+// iterations.  CG minimises the energy norm of the error, not |r|, and its
+// residual can stay near its initial value for a number of iterations that
+// grows with the grid width, so the window is max(2000, 2 sqrt(neq)).  M is
+// SPD, so this only guards against a network far outside its training data.
+static int stall_window(const ipfem_ctx *c)
+{
+    return (int)std::max(2000.0, 2.0 * std::sqrt((double)c->s.neq));
+}
 
 static unsigned fcg_grid(const ipfem_ctx *c)
 {
@@ -1173,7 +1181,7 @@ void launch_fcg_iteration(ipfem_ctx *c, int par)
                                                            P[1 - par], reinterpret_cast<const float2 *>(m.q),
                                                            reinterpret_cast<float2 *>(m.x), R[par], R[1 - par],
                                                            reinterpret_cast<float2 *>(l.y), part, (int64_t)fcg_grid(c),
-                                                           c->d_counters + 6, m.sc, kStallWindow);
+                                                           c->d_counters + 6, m.sc, stall_window(c));
     float *part2 = reinterpret_cast<float *>(c->d_part);
     k_tri_precond<<<fcg_grid(c), 256, 0, c->stream>>>(n, G, reinterpret_cast<const uint2 *>(l.Gh), d2,
                                                       reinterpret_cast<const float2 *>(l.y),
