@@ -49,9 +49,9 @@ CONFIGS = {
 # the GPU (identical on the CPU oracle); used by --impl reference to scale its
 # bounded CG sample to whole Newton iterations.
 CFG2_CG_ITERS = [10119, 9495]
-# DRAM bytes (read + write) of one SpMV launch at 400 x 400, from the ncu capture
-# summarised in profiles/k_cg_spmv_400x400.md
-SPMV_DRAM_BYTES = 484.026112e6 + 10.761216e6
+# DRAM bytes (read + write) of one SpMV launch at 400 x 400 (rows sorted by
+# length), from the ncu capture summarised in profiles/k_cg_spmv_400x400.md
+SPMV_DRAM_BYTES = 388.405504e6 + 9.274112e6
 FALLBACK_HBM_GBS = 6800.0
 
 
