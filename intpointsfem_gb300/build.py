@@ -17,7 +17,7 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libipfem.so")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 
-CU = ["k_constitutive.cu", "k_assembly.cu", "k_solver.cu", "k_mlp.cu", "capi_mlp.cu"]
+CU = ["k_constitutive.cu", "k_assembly.cu", "k_solver.cu", "k_mlp.cu", "k_net_tc.cu", "capi_mlp.cu"]
 CPP = ["capi.cpp", "host_setup.cpp"]
 HEADERS = ["ipfem_internal.h", "constitutive.cuh", "tma.cuh"]
 

@@ -218,6 +218,9 @@ void mlp_pack_weights(ipfem_ctx *c);
 cudaError_t mlp_configure();
 void launch_patch_features(ipfem_ctx *c, float *d_X);
 void launch_patch_net(ipfem_ctx *c, int64_t rows, const float *d_X, float *d_O);
+// tcgen05 network kernel (k_net_tc.cu)
+cudaError_t net_tc_configure();
+void launch_patch_net_tc(ipfem_ctx *c, int64_t rows, const float *d_X, float *d_O);
 void launch_patch_operator(ipfem_ctx *c);
 void launch_fcg_init(ipfem_ctx *c, const double *d_b, double scale, float rtol, int max_it);
 void launch_fcg_iteration(ipfem_ctx *c, int par);

@@ -21,8 +21,10 @@
 // condition number of M K plus the residual of the plain solver's
 // (residual, increment) pairs.
 //
-// GEMMs run on the tensor cores in BF16 (operands rounded to BF16 in shared
-// memory) with FP32 accumulation (mma.m16n8k16).
+// The inference network runs on the 5th-generation tensor cores (tcgen05.mma,
+// TMEM accumulators; k_net_tc.cu).  The training GEMMs below run on the tensor
+// cores in BF16 (operands rounded to BF16 in shared memory) with FP32
+// accumulation (mma.m16n8k16).
 #include <cuda_bf16.h>
 
 #include <algorithm>
@@ -249,159 +251,9 @@ __global__ void __launch_bounds__(256) k_patch_features(int32_t n, GridInfo G, c
     }
 }
 
-// ------------------------------------------------ fused network (inference)
-// One CTA = 128 nodes, 8 warps; warp w owns rows 16w..16w+15 through all three
-// layers (A operands are the warp's own rows, so the layers need only
-// __syncwarp).  Weights are staged once per persistent CTA.
-constexpr int PT = 128;          // nodes per tile
-constexpr int NOUT = 20, NOUTP = 24;
-
-struct NetDev {
-    const __nv_bfloat16 *w1t;   // [128][32]  (n, k)
-    const __nv_bfloat16 *w2t;   // [128][128] (n, k)
-    const __nv_bfloat16 *w3t;   // [24][128]  (n, k), rows 20..23 zero
-    const float *b1, *b2, *b3;  // [128], [128], [20]
-};
-
-struct __align__(16) NetSmem {
-    __nv_bfloat16 x[PT][32 + 8];
-    __nv_bfloat16 h[PT][128 + 8];
-    __nv_bfloat16 w1[128][32 + 8];
-    __nv_bfloat16 w2[128][128 + 8];
-    __nv_bfloat16 w3[NOUTP][128 + 8];
-    float b1[128], b2[128], b3[NOUTP];
-};
-
-__device__ void net_load_weights(NetSmem &S, const NetDev &W)
-{
-    for (int e = threadIdx.x; e < 128 * 32; e += blockDim.x) S.w1[e / 32][e % 32] = W.w1t[e];
-    for (int e = threadIdx.x; e < 128 * 128; e += blockDim.x) S.w2[e / 128][e % 128] = W.w2t[e];
-    for (int e = threadIdx.x; e < NOUTP * 128; e += blockDim.x) S.w3[e / 128][e % 128] = W.w3t[e];
-    for (int e = threadIdx.x; e < 128; e += blockDim.x) {
-        S.b1[e] = W.b1[e];
-        S.b2[e] = W.b2[e];
-    }
-    for (int e = threadIdx.x; e < NOUTP; e += blockDim.x) S.b3[e] = e < NOUT ? W.b3[e] : 0.f;
-}
-
-// acc[j][r]: rows r0 = 16*warp + g (r = 0, 1) and r0 + 8 (r = 2, 3), columns
-// 8j + 2t + (r & 1) of [16 x K] x [K x 128] from smem operands
-template <int K, int LDA>
-__device__ __forceinline__ void warp_gemm128(const __nv_bfloat16 (*A)[LDA], const __nv_bfloat16 (*B)[LDA], int r0,
-                                             int g, int t, float (&acc)[16][4])
-{
-#pragma unroll
-    for (int ks = 0; ks < K; ks += 16) {
-        uint32_t af[4];
-        af[0] = *reinterpret_cast<const uint32_t *>(&A[r0][ks + 2 * t]);
-        af[1] = *reinterpret_cast<const uint32_t *>(&A[r0 + 8][ks + 2 * t]);
-        af[2] = *reinterpret_cast<const uint32_t *>(&A[r0][ks + 8 + 2 * t]);
-        af[3] = *reinterpret_cast<const uint32_t *>(&A[r0 + 8][ks + 8 + 2 * t]);
-#pragma unroll
-        for (int j = 0; j < 16; j++) {
-            uint32_t bf[2];
-            bf[0] = *reinterpret_cast<const uint32_t *>(&B[8 * j + g][ks + 2 * t]);
-            bf[1] = *reinterpret_cast<const uint32_t *>(&B[8 * j + g][ks + 8 + 2 * t]);
-            mma_bf16(acc[j], af, bf);
-        }
-    }
-}
-
-// bias + relu of the accumulators into the warp's rows of S.h (BF16)
-__device__ __forceinline__ void warp_store_hidden(NetSmem &S, const float *b, int r0, int t, float (&acc)[16][4])
-{
-    __syncwarp();
-#pragma unroll
-    for (int j = 0; j < 16; j++) {
-        const int c = 8 * j + 2 * t;
-        *reinterpret_cast<uint32_t *>(&S.h[r0][c]) =
-            pack_bf16(fmaxf(acc[j][0] + b[c], 0.f), fmaxf(acc[j][1] + b[c + 1], 0.f));
-        *reinterpret_cast<uint32_t *>(&S.h[r0 + 8][c]) =
-            pack_bf16(fmaxf(acc[j][2] + b[c], 0.f), fmaxf(acc[j][3] + b[c + 1], 0.f));
-#pragma unroll
-        for (int r = 0; r < 4; r++) acc[j][r] = 0.f;
-    }
-    __syncwarp();
-}
-
-// network of the warp's 16 rows of S.x; out[j][r] as acc above for 24 columns
-__device__ void net_tile(NetSmem &S, int warp, int lane, float (&out)[3][4])
-{
-    const int g = lane >> 2, t = lane & 3;
-    const int r0 = 16 * warp + g;
-    float acc[16][4];
-#pragma unroll
-    for (int j = 0; j < 16; j++)
-#pragma unroll
-        for (int r = 0; r < 4; r++) acc[j][r] = 0.f;
-    warp_gemm128<32, 40>(S.x, S.w1, r0, g, t, acc);
-    warp_store_hidden(S, S.b1, r0, t, acc);
-    warp_gemm128<128, 136>(S.h, S.w2, r0, g, t, acc);
-    warp_store_hidden(S, S.b2, r0, t, acc);
-#pragma unroll
-    for (int j = 0; j < 3; j++)
-#pragma unroll
-        for (int r = 0; r < 4; r++) out[j][r] = 0.f;
-#pragma unroll
-    for (int ks = 0; ks < 128; ks += 16) {
-        uint32_t af[4];
-        af[0] = *reinterpret_cast<const uint32_t *>(&S.h[r0][ks + 2 * t]);
-        af[1] = *reinterpret_cast<const uint32_t *>(&S.h[r0 + 8][ks + 2 * t]);
-        af[2] = *reinterpret_cast<const uint32_t *>(&S.h[r0][ks + 8 + 2 * t]);
-        af[3] = *reinterpret_cast<const uint32_t *>(&S.h[r0 + 8][ks + 8 + 2 * t]);
-#pragma unroll
-        for (int j = 0; j < 3; j++) {
-            uint32_t bf[2];
-            bf[0] = *reinterpret_cast<const uint32_t *>(&S.w3[8 * j + g][ks + 2 * t]);
-            bf[1] = *reinterpret_cast<const uint32_t *>(&S.w3[8 * j + g][ks + 8 + 2 * t]);
-            mma_bf16(out[j], af, bf);
-        }
-    }
-#pragma unroll
-    for (int j = 0; j < 3; j++) {
-        const int c = 8 * j + 2 * t;
-        out[j][0] += S.b3[c];
-        out[j][1] += S.b3[c + 1];
-        out[j][2] += S.b3[c];
-        out[j][3] += S.b3[c + 1];
-    }
-}
-
-// O[rows][20] = network(X[rows][32]); persistent CTAs over 128-row tiles
-__global__ void __launch_bounds__(256) k_patch_net(int64_t rows, const float *__restrict__ X, NetDev W,
-                                                   float *__restrict__ O)
-{
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    NetSmem &S = *reinterpret_cast<NetSmem *>(smem_raw);
-    net_load_weights(S, W);
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int g = lane >> 2, t = lane & 3;
-    const int64_t n_tiles = (rows + PT - 1) / PT;
-    for (int64_t tile = blockIdx.x; tile < n_tiles; tile += gridDim.x) {
-        const int64_t base = tile * PT;
-        __syncthreads();   // weights staged / previous tile done with S.x
-        for (int e = threadIdx.x; e < PT * 16; e += blockDim.x) {
-            const int row = e / 16, c2 = 2 * (e % 16);
-            float2 v = make_float2(0.f, 0.f);
-            if (base + row < rows) v = *reinterpret_cast<const float2 *>(X + (base + row) * 32 + c2);
-            *reinterpret_cast<uint32_t *>(&S.x[row][c2]) = pack_bf16(v.x, v.y);
-        }
-        __syncthreads();
-        float out[3][4];
-        net_tile(S, warp, lane, out);
-#pragma unroll
-        for (int h = 0; h < 2; h++) {
-            const int64_t row = base + 16 * warp + g + 8 * h;
-            if (row >= rows) continue;
-#pragma unroll
-            for (int j = 0; j < 3; j++) {
-                const int c = 8 * j + 2 * t;
-                if (c < NOUT)
-                    *reinterpret_cast<float2 *>(O + row * NOUT + c) = make_float2(out[j][2 * h], out[j][2 * h + 1]);
-            }
-        }
-    }
-}
+// ------------------------------------------------ network output width
+// The inference network itself runs on the tcgen05 tensor cores (k_net_tc.cu).
+constexpr int NOUT = 20, NOUTP = 24;    // outputs per node; W3^T rows stored (padded to 24)
 
 __device__ __forceinline__ float2 free2(float2 d)
 {
@@ -1033,19 +885,6 @@ __global__ void __launch_bounds__(256) k_tri_dO(int32_t n, GridInfo G, const flo
 
 // ---------------------------------------------------------------- host side
 
-static NetDev net_dev(ipfem_ctx *c)
-{
-    MlpBuffers &m = c->mlp;
-    NetDev W;
-    W.w1t = static_cast<const __nv_bfloat16 *>(m.w1t);
-    W.w2t = static_cast<const __nv_bfloat16 *>(m.w2t);
-    W.w3t = static_cast<const __nv_bfloat16 *>(m.w3t);
-    W.b1 = m.params + kOffB1;
-    W.b2 = m.params + kOffB2;
-    W.b3 = m.params + kOffB3;
-    return W;
-}
-
 // BF16 copies of W1, W2, W3 in the (n, k) layout of the tensor-core B operand
 __global__ void k_pack_w(const float *__restrict__ P, __nv_bfloat16 *__restrict__ w1t, __nv_bfloat16 *__restrict__ w2t,
                          __nv_bfloat16 *__restrict__ w3t)
@@ -1076,21 +915,12 @@ void mlp_pack_weights(ipfem_ctx *c)
 // opt-in to the shared memory of the fused network kernel (once, outside any capture)
 cudaError_t mlp_configure()
 {
-    return cudaFuncSetAttribute(k_patch_net, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(NetSmem));
-}
-
-static int sm_count(const ipfem_ctx *c)
-{
-    int sms = 152;
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device);
-    return sms;
+    return net_tc_configure();
 }
 
 void launch_patch_net(ipfem_ctx *c, int64_t rows, const float *d_X, float *d_O)
 {
-    const int64_t tiles = (rows + PT - 1) / PT;
-    const unsigned grid = (unsigned)std::max<int64_t>(1, std::min<int64_t>(tiles, 2 * (int64_t)sm_count(c)));
-    k_patch_net<<<grid, 256, sizeof(NetSmem), c->stream>>>(rows, d_X, net_dev(c), d_O);
+    launch_patch_net_tc(c, rows, d_X, d_O);
 }
 
 void launch_patch_features(ipfem_ctx *c, float *d_X)

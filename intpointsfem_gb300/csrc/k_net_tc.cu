@@ -1,0 +1,300 @@
+// Fused per-node network (32 -> 128 -> 128 -> 20) on the 5th-generation tensor
+// cores: tcgen05.mma (kind::f16, BF16 operands from shared memory, FP32
+// accumulators in tensor memory), tcgen05.ld for the epilogues.  One CTA of
+// 128 threads runs tiles of 128 nodes; thread t owns node row t, which is
+// TMEM lane t.  Layer 1 accumulates in TMEM columns 0..127, layer 2 in
+// 128..255, layer 3 (N padded to 32) reuses columns 0..31.
+//
+// Shared-memory operands use the canonical K-major layout without swizzle:
+// core matrices of 8 rows x 16 bytes (8 BF16 along K) stored as 128
+// contiguous bytes; the 8-row groups of one K chunk follow each other (stride
+// SBO = 128 B), and the K chunks follow at stride LBO = rows * 16 B.
+#include <cuda_bf16.h>
+
+#include "ipfem_internal.h"
+#include "tma.cuh"
+
+namespace ipfem {
+
+namespace {
+
+constexpr int TC_ROWS = 128;          // nodes per tile (MMA M)
+constexpr int TC_NOUT = 20, TC_N3 = 32;
+constexpr uint32_t TC_TMEM_COLS = 256;
+
+// byte offsets of the operands inside the dynamic shared memory
+constexpr uint32_t OFF_X = 0;                        // 128 x 32  : 8 KB
+constexpr uint32_t OFF_W1 = OFF_X + 128 * 32 * 2;    // 128 x 32  : 8 KB
+constexpr uint32_t OFF_H = OFF_W1 + 128 * 32 * 2;    // 128 x 128 : 32 KB
+constexpr uint32_t OFF_W2 = OFF_H + 128 * 128 * 2;   // 128 x 128 : 32 KB
+constexpr uint32_t OFF_W3 = OFF_W2 + 128 * 128 * 2;  // 32 x 128  : 8 KB
+constexpr uint32_t OFF_B1 = OFF_W3 + 32 * 128 * 2;   // 128 floats
+constexpr uint32_t OFF_B2 = OFF_B1 + 512;
+constexpr uint32_t OFF_B3 = OFF_B2 + 512;            // 32 floats
+constexpr uint32_t OFF_BAR = OFF_B3 + 128;           // mbarrier
+constexpr uint32_t OFF_TMEM = OFF_BAR + 8;           // TMEM base written by tcgen05.alloc
+constexpr uint32_t TC_SMEM = OFF_TMEM + 8;
+
+// canonical offset of element (r, k) of an operand with `rows` rows
+__device__ __forceinline__ uint32_t cano(uint32_t r, uint32_t k, uint32_t rows)
+{
+    return (k >> 3) * (rows * 16u) + (r >> 3) * 128u + (r & 7u) * 16u + (k & 7u) * 2u;
+}
+
+// shared-memory matrix descriptor (tcgen05): start, LBO, SBO, version 1, no swizzle
+__device__ __forceinline__ uint64_t sdesc(uint32_t saddr, uint32_t lbo, uint32_t sbo)
+{
+    return (uint64_t)((saddr & 0x3FFFFu) >> 4) | ((uint64_t)((lbo >> 4) & 0x3FFFu) << 16) |
+           ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46);
+}
+
+// instruction descriptor: D FP32, A and B BF16, both K-major, M x N
+__host__ __device__ constexpr uint32_t idesc_bf16(uint32_t m, uint32_t n)
+{
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((n >> 3) << 17) | ((m >> 4) << 24);
+}
+
+__device__ __forceinline__ void tc_mma(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc)
+{
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tsetp.ne.u32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
+        "l"(a), "l"(b), "r"(idesc), "r"(acc)
+        : "memory");
+}
+
+__device__ __forceinline__ void tc_commit(uint32_t bar)
+{
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar)
+                 : "memory");
+}
+
+__device__ __forceinline__ void tc_fence_before()
+{
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+}
+
+__device__ __forceinline__ void tc_fence_after()
+{
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+
+__device__ __forceinline__ void fence_async_smem()
+{
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+// 32 consecutive FP32 columns of this thread's TMEM lane
+__device__ __forceinline__ void tc_ld32(uint32_t taddr, float (&v)[32])
+{
+    uint32_t r[32];
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+                 : "r"(taddr)
+                 : "memory");
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 32; i++) v[i] = __uint_as_float(r[i]);
+}
+
+__device__ __forceinline__ uint32_t pk_bf16(float lo, float hi)
+{
+    __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
+    return *reinterpret_cast<uint32_t *>(&v);
+}
+
+// all threads wait for the barrier phase (bounded); uniform result
+__device__ __forceinline__ bool wait_all(uint64_t *bar, uint32_t phase)
+{
+    const bool ok = mbar_wait_bounded(bar, phase);
+    return __syncthreads_and(ok ? 1 : 0) != 0;
+}
+
+// relu(v + b) of 32 columns starting at column c0 as BF16 into H (row r)
+__device__ __forceinline__ void store_hidden(unsigned char *smem, uint32_t r, uint32_t c0, const float (&v)[32],
+                                             const float *b)
+{
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+        uint4 w;
+        w.x = pk_bf16(fmaxf(v[8 * q + 0] + b[c0 + 8 * q + 0], 0.f), fmaxf(v[8 * q + 1] + b[c0 + 8 * q + 1], 0.f));
+        w.y = pk_bf16(fmaxf(v[8 * q + 2] + b[c0 + 8 * q + 2], 0.f), fmaxf(v[8 * q + 3] + b[c0 + 8 * q + 3], 0.f));
+        w.z = pk_bf16(fmaxf(v[8 * q + 4] + b[c0 + 8 * q + 4], 0.f), fmaxf(v[8 * q + 5] + b[c0 + 8 * q + 5], 0.f));
+        w.w = pk_bf16(fmaxf(v[8 * q + 6] + b[c0 + 8 * q + 6], 0.f), fmaxf(v[8 * q + 7] + b[c0 + 8 * q + 7], 0.f));
+        *reinterpret_cast<uint4 *>(smem + OFF_H + cano(r, c0 + 8 * q, 128)) = w;
+    }
+}
+
+}  // namespace
+
+// O[rows][20] = network(X[rows][32]); persistent CTAs of 128 threads over
+// 128-row tiles.  A barrier wait that runs out sets *err = 3 and the CTA stops.
+__global__ void __launch_bounds__(128) k_patch_net_tc(int64_t rows, const float *__restrict__ X,
+                                                      const __nv_bfloat16 *__restrict__ w1t,
+                                                      const __nv_bfloat16 *__restrict__ w2t,
+                                                      const __nv_bfloat16 *__restrict__ w3t,
+                                                      const float *__restrict__ b1, const float *__restrict__ b2,
+                                                      const float *__restrict__ b3, float *__restrict__ O, int *err)
+{
+    extern __shared__ __align__(1024) unsigned char smem[];
+    const uint32_t tid = threadIdx.x, warp = tid >> 5;
+    const uint32_t sbase = smem_u32(smem);
+    uint64_t *bar = reinterpret_cast<uint64_t *>(smem + OFF_BAR);
+    // weights and biases into the canonical layouts (16 bytes = 8 BF16 along K per copy)
+    for (uint32_t e = tid; e < 128 * 4; e += blockDim.x) {          // W1^T: 128 x 32
+        const uint32_t n = e >> 2, q = e & 3;
+        *reinterpret_cast<uint4 *>(smem + OFF_W1 + cano(n, 8 * q, 128)) =
+            *reinterpret_cast<const uint4 *>(w1t + n * 32 + 8 * q);
+    }
+    for (uint32_t e = tid; e < 128 * 16; e += blockDim.x) {         // W2^T: 128 x 128
+        const uint32_t n = e >> 4, q = e & 15;
+        *reinterpret_cast<uint4 *>(smem + OFF_W2 + cano(n, 8 * q, 128)) =
+            *reinterpret_cast<const uint4 *>(w2t + n * 128 + 8 * q);
+    }
+    for (uint32_t e = tid; e < TC_N3 * 16; e += blockDim.x) {       // W3^T: 32 x 128 (rows >= 24 zero)
+        const uint32_t n = e >> 4, q = e & 15;
+        uint4 v = make_uint4(0u, 0u, 0u, 0u);
+        if (n < 24) v = *reinterpret_cast<const uint4 *>(w3t + n * 128 + 8 * q);
+        *reinterpret_cast<uint4 *>(smem + OFF_W3 + cano(n, 8 * q, TC_N3)) = v;
+    }
+    float *sb1 = reinterpret_cast<float *>(smem + OFF_B1), *sb2 = reinterpret_cast<float *>(smem + OFF_B2);
+    float *sb3 = reinterpret_cast<float *>(smem + OFF_B3);
+    sb1[tid] = b1[tid];
+    sb2[tid] = b2[tid];
+    if (tid < TC_N3) sb3[tid] = tid < TC_NOUT ? b3[tid] : 0.f;
+    if (tid == 0) mbar_init(bar, 1);
+    // tensor memory: one warp allocates 256 columns
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(sbase + OFF_TMEM),
+                     "r"(TC_TMEM_COLS)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    fence_async_smem();
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *reinterpret_cast<volatile uint32_t *>(smem + OFF_TMEM);
+    const uint32_t lane_t = tmem + ((warp * 32u) << 16);             // this warp's TMEM lanes
+    constexpr uint32_t ID128 = idesc_bf16(128, 128), ID32 = idesc_bf16(128, TC_N3);
+    uint32_t phase = 0;
+    bool ok = true;
+    const int64_t n_tiles = (rows + TC_ROWS - 1) / TC_ROWS;
+    for (int64_t tile = blockIdx.x; tile < n_tiles && ok; tile += gridDim.x) {
+        const int64_t row = tile * TC_ROWS + tid;
+        // features of this thread's node -> BF16 A operand
+        {
+            float4 f[8];
+#pragma unroll
+            for (int j = 0; j < 8; j++)
+                f[j] = row < rows ? reinterpret_cast<const float4 *>(X + row * 32)[j] : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                const uint4 w = make_uint4(pk_bf16(f[2 * q].x, f[2 * q].y), pk_bf16(f[2 * q].z, f[2 * q].w),
+                                           pk_bf16(f[2 * q + 1].x, f[2 * q + 1].y),
+                                           pk_bf16(f[2 * q + 1].z, f[2 * q + 1].w));
+                *reinterpret_cast<uint4 *>(smem + OFF_X + cano(tid, 8 * q, 128)) = w;
+            }
+        }
+        fence_async_smem();
+        tc_fence_before();
+        __syncthreads();
+        // layer 1: D[0..127] = X W1 (K = 32: two K-steps of 16)
+        if (tid == 0) {
+            tc_fence_after();
+#pragma unroll
+            for (uint32_t kk = 0; kk < 2; kk++)
+                tc_mma(tmem, sdesc(sbase + OFF_X + kk * 2 * 2048, 2048, 128),
+                       sdesc(sbase + OFF_W1 + kk * 2 * 2048, 2048, 128), ID128, kk);
+            tc_commit(sbase + OFF_BAR);
+        }
+        ok = wait_all(bar, phase);
+        phase ^= 1u;
+        if (!ok) break;
+        tc_fence_after();
+#pragma unroll 1
+        for (uint32_t c = 0; c < 4; c++) {
+            float v[32];
+            tc_ld32(lane_t + 32 * c, v);
+            store_hidden(smem, tid, 32 * c, v, sb1);
+        }
+        fence_async_smem();
+        tc_fence_before();
+        __syncthreads();
+        // layer 2: D[128..255] = H1 W2 (K = 128)
+        if (tid == 0) {
+            tc_fence_after();
+#pragma unroll
+            for (uint32_t kk = 0; kk < 8; kk++)
+                tc_mma(tmem + 128, sdesc(sbase + OFF_H + kk * 2 * 2048, 2048, 128),
+                       sdesc(sbase + OFF_W2 + kk * 2 * 2048, 2048, 128), ID128, kk);
+            tc_commit(sbase + OFF_BAR);
+        }
+        ok = wait_all(bar, phase);
+        phase ^= 1u;
+        if (!ok) break;
+        tc_fence_after();
+#pragma unroll 1
+        for (uint32_t c = 0; c < 4; c++) {
+            float v[32];
+            tc_ld32(lane_t + 128 + 32 * c, v);
+            store_hidden(smem, tid, 32 * c, v, sb2);
+        }
+        fence_async_smem();
+        tc_fence_before();
+        __syncthreads();
+        // layer 3: D[0..31] = H2 W3 (N = 32, K = 128)
+        if (tid == 0) {
+            tc_fence_after();
+#pragma unroll
+            for (uint32_t kk = 0; kk < 8; kk++)
+                tc_mma(tmem, sdesc(sbase + OFF_H + kk * 2 * 2048, 2048, 128),
+                       sdesc(sbase + OFF_W3 + kk * 2 * 512, 512, 128), ID32, kk);
+            tc_commit(sbase + OFF_BAR);
+        }
+        ok = wait_all(bar, phase);
+        phase ^= 1u;
+        if (!ok) break;
+        tc_fence_after();
+        {
+            float v[32];
+            tc_ld32(lane_t, v);
+            if (row < rows) {
+                float4 *o = reinterpret_cast<float4 *>(O + row * TC_NOUT);
+#pragma unroll
+                for (int j = 0; j < 5; j++)
+                    o[j] = make_float4(v[4 * j] + sb3[4 * j], v[4 * j + 1] + sb3[4 * j + 1],
+                                       v[4 * j + 2] + sb3[4 * j + 2], v[4 * j + 3] + sb3[4 * j + 3]);
+            }
+        }
+        tc_fence_before();
+        __syncthreads();
+    }
+    if (!ok && tid == 0) atomicExch(err, 3);
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TC_TMEM_COLS)
+                     : "memory");
+}
+
+cudaError_t net_tc_configure()
+{
+    return cudaFuncSetAttribute(k_patch_net_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TC_SMEM);
+}
+
+void launch_patch_net_tc(ipfem_ctx *c, int64_t rows, const float *d_X, float *d_O)
+{
+    int sms = 152;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device);
+    const int64_t tiles = (rows + TC_ROWS - 1) / TC_ROWS;
+    const unsigned grid = (unsigned)std::max<int64_t>(1, std::min<int64_t>(tiles, 2 * (int64_t)sms));
+    const MlpBuffers &m = c->mlp;
+    k_patch_net_tc<<<grid, 128, TC_SMEM, c->stream>>>(
+        rows, d_X, static_cast<const __nv_bfloat16 *>(m.w1t), static_cast<const __nv_bfloat16 *>(m.w2t),
+        static_cast<const __nv_bfloat16 *>(m.w3t), m.params + kOffB1, m.params + kOffB2, m.params + kOffB3, d_O,
+        c->d_err);
+}
+
+}  // namespace ipfem
