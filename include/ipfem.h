@@ -151,6 +151,15 @@ ipfem_status ipfem_newton_solve(ipfem_ctx *ctx, const ipfem_solve_opts *opts, in
                                 int32_t step_end, double *u, int where, ipfem_solve_stats *stats,
                                 double *log, int32_t log_cap);
 
+/* Newton variant of the load-stepped solve: 0 = the plain iteration (below),
+ * 1 = the modified-Thomas accelerated iteration of Solution(...,
+ * modified_thomas_accel_Q = true) (main.cpp:194-217): u += alpha du, residual
+ * at u, a second solve with the same tangent for du~, alpha += (alpha du .
+ * du~) / (alpha du . alpha du), u += du~; alpha starts at 1 in every load
+ * step.  Convergence is still judged on |R| / |R0| after the tangent
+ * assembly at the new u. */
+ipfem_status ipfem_set_newton_accel(ipfem_ctx *ctx, int mode);
+
 /* Resumable form of the same loop: begin sets the options and the step range;
  * each advance performs n_iters Newton iterations (0 = until the last step is
  * accepted).  An iteration is: CG on the current tangent, u += du,

@@ -99,6 +99,7 @@ def lib():
             "ipfem_newton_solve": (S, [P, C.POINTER(SolveOpts), C.c_int32, C.c_int32, P, S,
                                        C.POINTER(SolveStats), _dp, C.c_int32]),
             "ipfem_newton_begin": (S, [P, C.POINTER(SolveOpts), C.c_int32, C.c_int32]),
+            "ipfem_set_newton_accel": (S, [P, S]),
             "ipfem_newton_advance": (S, [P, C.c_int32, P, S, C.POINTER(SolveStats), _dp, C.c_int32,
                                          C.POINTER(C.c_int32)]),
             "ipfem_dot": (S, [P, P, P, _dp]),
@@ -274,6 +275,10 @@ class ElastoPlasticIntPointsStructMatrix:
 
     def SetUpdateMem(self, flag):
         self._check(lib().ipfem_set_update_mem(self._ctx, int(bool(flag))))
+
+    def set_newton_accel(self, mode):
+        """0: plain Newton iteration; 1: modified-Thomas acceleration (main.cpp:194-217)"""
+        self._check(lib().ipfem_set_newton_accel(self._ctx, int(mode)))
 
     def set_precision(self, mode):
         self._check(lib().ipfem_set_precision(self._ctx, int(mode)))

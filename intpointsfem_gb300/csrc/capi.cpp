@@ -76,7 +76,7 @@ void free_all(ipfem_ctx *c)
                     c->d_fixed, c->d_K,
                     c->d_dinv, c->d_eps_p, c->d_sigma, c->d_alpha, c->d_mtype, c->d_u, c->d_rhs, c->d_strain,
                     c->d_sigma_w, c->d_dep, c->d_fe, c->d_x, c->d_r, c->d_z, c->d_p, c->d_q, c->d_b, c->d_part,
-                    c->d_sc, c->d_counters, c->d_dotres, c->d_err};
+                    c->d_sc, c->d_counters, c->d_dotres, c->d_err, c->d_acc};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     {
@@ -503,6 +503,17 @@ ipfem_status ipfem_assemble_residual(ipfem_ctx *c, const double *u, double *rhs,
     return assemble_common(c, u, rhs, where, false);
 }
 
+ipfem_status ipfem_set_newton_accel(ipfem_ctx *c, int mode)
+{
+    if (!c || (mode != 0 && mode != 1)) return fail(c, IPFEM_INVALID, "bad Newton acceleration mode");
+    if (mode == 1 && !c->d_acc) {
+        cudaError_t e = dalloc(&c->d_acc, (size_t)c->s.neq);
+        if (e != cudaSuccess) return fail(c, IPFEM_OOM, "allocation of the acceleration vector failed");
+    }
+    c->newton_accel = mode;
+    return IPFEM_OK;
+}
+
 ipfem_status ipfem_assemble(ipfem_ctx *c, const double *u, double *rhs, int where)
 {
     return assemble_common(c, u, rhs, where, true);
@@ -580,6 +591,7 @@ static ipfem_status newton_advance(ipfem_ctx *c, int32_t n_iters, double *du, ip
             ns.r0 = std::sqrt(r0sq);
             ns.rn = ns.r0;
             ns.it = 0;
+            ns.alpha = 1.0;
             ns.open = 1;
             if (!std::isfinite(ns.r0)) return fail(c, IPFEM_NAN, "residual is not finite");
         }
@@ -588,12 +600,39 @@ static ipfem_status newton_advance(ipfem_ctx *c, int32_t n_iters, double *du, ip
             int k = 0;
             const int64_t fb0 = c->fcg_fallbacks;
             cudaEventRecord(ev[0], c->stream);
-            ipfem_status e = solve_device(c, c->d_rhs, o.cg_rtol, o.cg_max_it, &k, du, 1);
+            ipfem_status e = solve_device(c, c->d_rhs, o.cg_rtol, o.cg_max_it, &k, du, c->newton_accel ? 0 : 1);
             st->fcg_fallbacks += c->fcg_fallbacks - fb0;
             cudaEventRecord(ev[1], c->stream);
             st->ms_solve += elapsed();
             st->cg_iters += k;
             if (e != IPFEM_OK && e != IPFEM_NONCONVERGED) return e;
+            if (c->newton_accel) {
+                // modified-Thomas acceleration (main.cpp:194-217): u += alpha du,
+                // residual at u, a second solve with the same tangent, alpha +=
+                // (alpha du . du~) / (alpha du . alpha du), u += du~
+                launch_scale_add(c, du, c->d_x, ns.alpha, c->d_acc);
+                cudaEventRecord(ev[0], c->stream);
+                residual_device(c, du, c->d_rhs, 0);
+                cudaEventRecord(ev[1], c->stream);
+                st->ms_assemble += elapsed();
+                int k2 = 0;
+                const int64_t fb1 = c->fcg_fallbacks;
+                cudaEventRecord(ev[0], c->stream);
+                e = solve_device(c, c->d_rhs, o.cg_rtol, o.cg_max_it, &k2, du, 0);
+                st->fcg_fallbacks += c->fcg_fallbacks - fb1;
+                cudaEventRecord(ev[1], c->stream);
+                st->ms_solve += elapsed();
+                st->cg_iters += k2;
+                k += k2;
+                if (e != IPFEM_OK && e != IPFEM_NONCONVERGED) return e;
+                double num = 0.0, dem = 0.0;
+                e = dot_host(c, c->d_acc, c->d_x, &num);
+                if (e == IPFEM_OK) e = dot_host(c, c->d_acc, c->d_acc, &dem);
+                if (e != IPFEM_OK) return e;
+                if (dem > 0.0) ns.alpha = ns.alpha + num / dem;
+                launch_axpy_u(c, du, c->d_x);
+                c->launches += 2;
+            }
             ns.it++;
             done++;
             st->newton_iters++;

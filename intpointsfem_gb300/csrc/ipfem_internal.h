@@ -110,6 +110,7 @@ struct NewtonState {
     int32_t step = 0, step_end = 0, it = 0;
     int open = 0, active = 0, all_converged = 1;
     double r0 = 0.0, rn = 0.0;
+    double alpha = 1.0;           // modified-Thomas acceleration factor of the open load step
 };
 
 namespace ipfem {
@@ -168,6 +169,8 @@ struct ipfem_ctx {
     ipfem::CGScalars *d_sc = nullptr;
     unsigned *d_counters = nullptr;      // last-block tickets
     double *d_dotres = nullptr;          // results of standalone dots
+    int newton_accel = 0;                // 1: modified-Thomas accelerated Newton (main.cpp:194-224)
+    double *d_acc = nullptr;             // [neq] alpha * du of the accelerated step
     int *d_err = nullptr;                // device error word (wait timeouts)
     ipfem::CGScalars *h_sc = nullptr;    // pinned
     double *h_pin = nullptr;             // pinned scalars
@@ -199,6 +202,7 @@ void launch_cg_iteration(ipfem_ctx *c);
 void launch_cg_spmv_only(ipfem_ctx *c);
 void launch_dot(ipfem_ctx *c, const double *a, const double *b, double *d_out);
 void launch_axpy_u(ipfem_ctx *c, double *d_u, const double *d_du);
+void launch_scale_add(ipfem_ctx *c, double *d_u, const double *d_x, double alpha, double *d_t);
 void launch_fp64_probe(ipfem_ctx *c, double *d_out, int grid, int iters);
 void launch_stiffness32(ipfem_ctx *c);
 void launch_cg32_init(ipfem_ctx *c, const double *d_b, double scale, float rtol, int max_it);

@@ -340,6 +340,17 @@ void launch_fp64_probe(ipfem_ctx *c, double *d_out, int grid, int iters)
     k_fp64_probe<<<grid, 256, 0, c->stream>>>(d_out, iters, 0.999, 0.001);
 }
 
+// t = alpha * x, u = u + t (two rounded operations, in this order)
+__global__ void k_scale_add(int64_t n, double *__restrict__ u, const double *__restrict__ x, double alpha,
+                            double *__restrict__ t)
+{
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double ti = alpha * x[i];
+    t[i] = ti;
+    u[i] = u[i] + ti;
+}
+
 __global__ void k_add_scaled32(int64_t n, double *__restrict__ u, const float *__restrict__ x, double scale)
 {
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -426,6 +437,12 @@ void launch_dot(ipfem_ctx *c, const double *a, const double *b, double *d_out)
 {
     k_dot<<<grid_nodes(c), kRedBlock, 0, c->stream>>>(c->s.n_nodes, a, b, c->d_part, c->n_red, c->d_counters + 3,
                                                       d_out);
+}
+
+void launch_scale_add(ipfem_ctx *c, double *d_u, const double *d_x, double alpha, double *d_t)
+{
+    const int64_t n = c->s.neq;
+    k_scale_add<<<(unsigned)((n + 255) / 256), 256, 0, c->stream>>>(n, d_u, d_x, alpha, d_t);
 }
 
 void launch_axpy_u(ipfem_ctx *c, double *d_u, const double *d_du)

@@ -687,6 +687,7 @@ void orc_solve_steps(orc_problem *p, const orc_solve_opts *o, int32_t step_begin
     double *R = (double *)xcalloc((size_t)n, sizeof(double));
     double *du = (double *)xcalloc((size_t)n, sizeof(double));
     double *work = (double *)xcalloc((size_t)n * 4, sizeof(double));
+    double *t = o->accel ? (double *)xcalloc((size_t)n, sizeof(double)) : NULL;
     int32_t nlog = 0;
     memset(st, 0, sizeof *st);
     st->converged = 1;
@@ -697,9 +698,25 @@ void orc_solve_steps(orc_problem *p, const orc_solve_opts *o, int32_t step_begin
         double rn = r0;
         int conv = (r0 == 0.0);
         int it = 0;
+        double alpha = 1.0;                          /* main.cpp:170, reset per load step */
         while (!conv && it < o->newton_max_it) {
             int k = orc_pcg(p, R, du, o->cg_rtol, o->cg_max_it, work);
             st->cg_iters += k < 0 ? -k : k;
+            if (o->accel) {
+                /* main.cpp:194-217: u += alpha du, residual at u, second solve
+                 * with the same tangent, alpha += (alpha du . du~) / |alpha du|^2,
+                 * u += du~ (alpha unchanged when alpha du = 0) */
+                for (int32_t i = 0; i < n; i++) {
+                    t[i] = alpha * du[i];
+                    u[i] = u[i] + t[i];
+                }
+                orc_assemble_residual(p, u, lambda, 0, R);
+                int k2 = orc_pcg(p, R, du, o->cg_rtol, o->cg_max_it, work);
+                st->cg_iters += k2 < 0 ? -k2 : k2;
+                k = (k < 0 ? -k : k) + (k2 < 0 ? -k2 : k2);
+                const double num = orc_dot(p->n_nodes, t, du), dem = orc_dot(p->n_nodes, t, t);
+                if (dem > 0.0) alpha = alpha + num / dem;
+            }
             for (int32_t i = 0; i < n; i++) u[i] = u[i] + du[i];
             it++;
             orc_assemble(p, u, lambda, R);
@@ -718,5 +735,5 @@ void orc_solve_steps(orc_problem *p, const orc_solve_opts *o, int32_t step_begin
         if (!conv) st->converged = 0;
         orc_assemble_residual(p, u, lambda, 1, R);     /* accept: commit state */
     }
-    free(R); free(du); free(work);
+    free(R); free(du); free(work); free(t);
 }

@@ -101,6 +101,7 @@ typedef struct {
     int32_t newton_max_it;
     double cg_rtol;
     int32_t cg_max_it;
+    int32_t accel;             /* 1: modified-Thomas acceleration (main.cpp:194-217) */
 } orc_solve_opts;
 
 typedef struct {

@@ -47,7 +47,7 @@ class Problem(C.Structure):
 
 class SolveOpts(C.Structure):
     _fields_ = [("n_steps", C.c_int32), ("newton_rtol", C.c_double), ("newton_max_it", C.c_int32),
-                ("cg_rtol", C.c_double), ("cg_max_it", C.c_int32)]
+                ("cg_rtol", C.c_double), ("cg_max_it", C.c_int32), ("accel", C.c_int32)]
 
 
 class SolveStats(C.Structure):
@@ -185,10 +185,11 @@ class OracleProblem:
         return x, k
 
     def solve_steps(self, u, n_steps, step_begin=0, step_end=None, newton_rtol=1e-8, newton_max_it=20,
-                    cg_rtol=1e-8, cg_max_it=200000, log_cap=4096):
+                    cg_rtol=1e-8, cg_max_it=200000, log_cap=4096, accel=0):
         if step_end is None:
             step_end = n_steps
-        o = SolveOpts(int(n_steps), float(newton_rtol), int(newton_max_it), float(cg_rtol), int(cg_max_it))
+        o = SolveOpts(int(n_steps), float(newton_rtol), int(newton_max_it), float(cg_rtol), int(cg_max_it),
+                      int(accel))
         st = SolveStats()
         log = np.zeros(3 * log_cap)
         lib().orc_solve_steps(self._p, C.byref(o), int(step_begin), int(step_end), ptr(u), C.byref(st),

@@ -127,3 +127,18 @@ def test_learned_factor_gradient_matches_finite_differences():
         fd = (orc_mlp.loss_grad_O(Op, mv, blocks, gr, gr, dinv, R, E)[0] -
               orc_mlp.loss_grad_O(Om, mv, blocks, gr, gr, dinv, R, E)[0]) / (2 * h)
         assert abs(fd - dO.flat[t]) <= 1e-6 * max(1.0, abs(dO).max()), (t, fd, dO.flat[t])
+
+
+def test_modified_thomas_newton_converges_in_fewer_iterations():
+    """oracle: the accelerated load-stepped solve (main.cpp:194-217) reaches
+    the same Newton tolerance in fewer iterations than the plain one, and both
+    end at the same displacement to that tolerance"""
+    out = {}
+    for accel in (0, 1):
+        P = po.OracleProblem(po.default_params(12), nthreads=0)
+        u = np.zeros(P.neq)
+        st, _ = P.solve_steps(u, 10, newton_max_it=40, accel=accel)
+        assert st.converged
+        out[accel] = (st.newton_iters, u)
+    assert out[1][0] < out[0][0]
+    assert np.abs(out[1][1] - out[0][1]).max() <= 1e-6 * np.abs(out[0][1]).max()
