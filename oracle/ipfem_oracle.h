@@ -68,6 +68,12 @@ void orc_ip_update(const orc_elastic *el, const orc_mc *mc,
                    double sigma6[6], double eps_p6_out[6], double strain6[6],
                    int *mtype, double *alpha);
 
+/* Point update with the full 6x6 tangent (XX XY XZ YY YZ ZZ; row = stress,
+ * column = strain), as TPZPlasticStepPV::ApplyStrainComputeSigma's Dep that
+ * TRKSolution::RKProcess reads (TRKSolution.cpp:189-191). */
+void orc_ip_tangent6(const orc_elastic *el, const orc_mc *mc, const double strain6[6], const double eps_p6[6],
+                     double sigma6[6], double eps_p6_out[6], double T36[36], int *mtype);
+
 /* Same, but with the argument aliasing of the reference GPU residual kernel
  * (KernelsComputeSigma.h:171: ProjectSigma(sigma_projected, sigma_projected, ...)).
  * Only used to document the CPU/GPU discrepancy of the reference. */

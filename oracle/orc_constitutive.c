@@ -591,6 +591,44 @@ static void tangent_operator(const double *grad, const double *sev, const double
     }
 }
 
+/* ----------------------------------------- full tangent (verification) */
+
+/* The point update of orc_ip_update with the full 6x6 tangent T (row l =
+ * stress component, column k = strain component, order XX XY XZ YY YZ ZZ)
+ * instead of its plane-strain extraction: what TPZPlasticStepPV::
+ * ApplyStrainComputeSigma returns as Dep and TRKSolution::RKProcess reads
+ * (TRKSolution.cpp:189-191).  strain6 is the total strain (tensor shear). */
+void orc_ip_tangent6(const orc_elastic *el, const orc_mc *mc, const double strain6_in[6], const double eps_p6[6],
+                     double sigma6[6], double eps_p6_out[6], double T36[36], int *mtype)
+{
+    const double lambda = el->lambda, mu = el->mu;
+    const double G = mu;
+    const double K = lambda + 2 * mu / 3;
+    double strain[6], ee[6], sig[6], pl[6];
+    double sev[3], svec[9], sp[3], grad[9], eev[3], evec[9];
+    double a = 0.0;
+    int mt = 0;
+    for (int i = 0; i < 6; i++) {
+        strain[i] = strain6_in[i];
+        pl[i] = eps_p6[i];
+    }
+    elastic_strain(pl, strain, ee);
+    trial_stress(ee, sig, mu, lambda);
+    spectral(sig, sev, svec);
+    ee[1] = ee[1] / 2;
+    spectral(ee, eev, evec);
+    project_sigma(sev, sp, &mt, &a, mc, K, G, grad, 1);
+    tangent_operator(grad, sev, eev, evec, T36, G, lambda);
+    reconstruct(sp, svec, sig);
+    strain_from_stress(sig, ee, mu, lambda);
+    plastic_strain(strain, ee, pl);
+    for (int i = 0; i < 6; i++) {
+        sigma6[i] = sig[i];
+        eps_p6_out[i] = pl[i];
+    }
+    if (mtype) *mtype = mt;
+}
+
 /* -------------------------------------------------- per-point update */
 
 void orc_ip_update(const orc_elastic *el, const orc_mc *mc,
