@@ -46,29 +46,73 @@ __device__ __forceinline__ T tree8(const volatile T *w)
     return a[0];
 }
 
-// Level 0+1 for NV values at once: per-CTA partial sums written to part[v][blockIdx].
-// Returns true in every thread of the CTA that finished last (after a fence).
-template <class T, int NV>
-__device__ __forceinline__ bool block_partials(const T (&v)[NV], T *part, int64_t n_red, unsigned *ticket)
+// Level 0+1 of one 256-node window, evaluated by a single warp.  The pairing
+// is exactly the shuffle-down tree above (node t = 32 w + l, l = l4..l0: pairs
+// over l4, l3, l2, l1, l0) followed by tree8 over the warps (w2, w1, w0), so
+// the sum is bit-identical to warp_tree + tree8; only its evaluation differs.
+// The values are staged in shared memory at stage(t) = 34 (t >> 5) + (t & 31)
+// (stride 34 keeps the gathers below free of bank conflicts for FP64).  Lane
+// j = 16 l1 + 8 l0 + w of warp 0 loads the 8 values with its (l1, l0, w),
+// adds over l4, l3, l2 in registers (7 adds, every lane useful) and over
+// l1, l0, w2, w1, w0 by shuffles.  That is 12 warp-wide FP64 adds per value
+// against 47 for the 8 shuffle trees plus tree8 — the FP64 pipe bounds the
+// vector-update kernels on this part.
+constexpr int kRedPad = 34;
+constexpr int kRedStage = 8 * kRedPad;
+__device__ __forceinline__ int red_stage(int t) { return (t >> 5) * kRedPad + (t & 31); }
+
+template <class T>
+__device__ __forceinline__ T tree256_warp(const T *s)
 {
-    __shared__ T ws[NV][8];
+    const int lane = threadIdx.x & 31;
+    const T *b = s + (lane & 7) * kRedPad + 2 * (lane >> 4) + ((lane >> 3) & 1);
+    T x[8];
+#pragma unroll
+    for (int m = 0; m < 8; m++) x[m] = b[4 * m];
+#pragma unroll
+    for (int m = 0; m < 4; m++) x[m] = x[m] + x[m + 4];
+    x[0] = x[0] + x[2];
+    x[1] = x[1] + x[3];
+    T u = x[0] + x[1];
+#pragma unroll
+    for (int off = 16; off >= 1; off >>= 1) u = u + __shfl_down_sync(FULL, u, off);
+    return u;
+}
+
+// Per-CTA partial sums of values the caller has staged (s[k][red_stage(t)]
+// for the node in slot t, zero for empty slots) and synchronised; written to
+// part[k][blockIdx].  Returns true in every thread of the CTA that finished
+// last (after a fence).
+template <class T, int NV>
+__device__ __forceinline__ bool block_partials_staged(const T (*s)[kRedStage], T *part, int64_t n_red,
+                                                      unsigned *ticket)
+{
     __shared__ int s_last;
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if (threadIdx.x < 32) {
+        T o[NV];
 #pragma unroll
-    for (int k = 0; k < NV; k++) {
-        const T t = warp_tree(v[k]);
-        if (lane == 0) ws[k][w] = t;
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
+        for (int k = 0; k < NV; k++) o[k] = tree256_warp<T>(s[k]);
+        if (threadIdx.x == 0) {
 #pragma unroll
-        for (int k = 0; k < NV; k++) part[k * n_red + blockIdx.x] = tree8<T>(ws[k]);
-        __threadfence();
-        const unsigned t = atomicAdd(ticket, 1u);
-        s_last = (t == gridDim.x - 1);
+            for (int k = 0; k < NV; k++) part[k * n_red + blockIdx.x] = o[k];
+            __threadfence();
+            const unsigned t = atomicAdd(ticket, 1u);
+            s_last = (t == gridDim.x - 1);
+        }
     }
     __syncthreads();
     return s_last != 0;
+}
+
+// The same for one value per thread, thread t holding node slot t.
+template <class T, int NV>
+__device__ __forceinline__ bool block_partials(const T (&v)[NV], T *part, int64_t n_red, unsigned *ticket)
+{
+    __shared__ T s[NV][kRedStage];
+#pragma unroll
+    for (int k = 0; k < NV; k++) s[k][red_stage(threadIdx.x)] = v[k];
+    __syncthreads();
+    return block_partials_staged<T, NV>(s, part, n_red, ticket);
 }
 
 // Level 2, executed by all 256 threads of the last CTA; result valid in thread 0.
@@ -177,14 +221,19 @@ __global__ void __launch_bounds__(kRedBlock) k_cg_spmv(int32_t n_nodes, const in
                                                        CGScalarsT<T> *sc)
 {
     typedef typename Vec2<T>::type V;
-    __shared__ T s_pq[SORTED ? kRedBlock : 1];
-    if (*reinterpret_cast<volatile int *>(&sc->done)) return;
+    __shared__ T s_pq[1][kRedStage];
     const int32_t t = blockIdx.x * kRedBlock + threadIdx.x;
-    T v[1] = {T(0)};
+    // row metadata is loaded before the flag so that the two latencies overlap
+    int32_t i = t, len = 0;
+    int64_t base = 0;
     if (t < n_nodes) {
-        const int32_t i = SORTED ? __ldg(&sell_node[t]) : t;
-        const int64_t base = __ldg(&slice_base[t >> 5]) + (t & 31);
-        const int len = __ldg(&rowlen[t]);
+        if (SORTED) i = __ldg(&sell_node[t]);
+        base = __ldg(&slice_base[t >> 5]) + (t & 31);
+        len = __ldg(&rowlen[t]);
+    }
+    if (*reinterpret_cast<volatile int *>(&sc->done)) return;
+    T v = T(0);
+    if (t < n_nodes) {
         const V *pv = reinterpret_cast<const V *>(p);
         T y0 = T(0), y1 = T(0);
 #pragma unroll 4
@@ -203,16 +252,13 @@ __global__ void __launch_bounds__(kRedBlock) k_cg_spmv(int32_t n_nodes, const in
         if (fixed[2 * (size_t)i + 1]) y1 = T(0);
         reinterpret_cast<V *>(q)[i] = mk2(y0, y1);
         const V pp = pv[i];
-        v[0] = fma(pp.y, y1, fma(pp.x, y0, T(0)));
-        if (SORTED) s_pq[i - blockIdx.x * kRedBlock] = v[0];
-    } else if (SORTED) {
-        s_pq[threadIdx.x] = T(0);
+        v = fma(pp.y, y1, fma(pp.x, y0, T(0)));
     }
-    if (SORTED) {
-        __syncthreads();
-        v[0] = s_pq[threadIdx.x];
-    }
-    if (block_partials<T, 1>(v, part, n_red, ticket)) {
+    // the node's own slot of the window (sorted rows are a permutation of it;
+    // slots past the last node get the zeros of the threads past it)
+    s_pq[0][red_stage(i - blockIdx.x * kRedBlock)] = v;
+    __syncthreads();
+    if (block_partials_staged<T, 1>(s_pq, part, n_red, ticket)) {
         T o[1];
         final_reduce<T, 1>(part, n_red, o);
         if (threadIdx.x == 0) {
@@ -238,16 +284,20 @@ __global__ void __launch_bounds__(kRedBlock) k_cg_update(int32_t n_nodes, const 
                                                          T *part, int64_t n_red, unsigned *ticket, CGScalarsT<T> *sc)
 {
     typedef typename Vec2<T>::type V;
+    const int32_t i = blockIdx.x * kRedBlock + threadIdx.x;
+    // operands first, then the flag and alpha, so that the latencies overlap
+    V pp, qq, di, xx, rr;
+    if (i < n_nodes) {
+        pp = reinterpret_cast<const V *>(p)[i];
+        qq = reinterpret_cast<const V *>(q)[i];
+        di = reinterpret_cast<const V *>(dinv)[i];
+        xx = reinterpret_cast<V *>(x)[i];
+        rr = reinterpret_cast<V *>(r)[i];
+    }
     if (*reinterpret_cast<volatile int *>(&sc->done)) return;
     const T alpha = *reinterpret_cast<volatile T *>(&sc->alpha);
-    const int32_t i = blockIdx.x * kRedBlock + threadIdx.x;
     T v[2] = {T(0), T(0)};
     if (i < n_nodes) {
-        const V pp = reinterpret_cast<const V *>(p)[i];
-        const V qq = reinterpret_cast<const V *>(q)[i];
-        const V di = reinterpret_cast<const V *>(dinv)[i];
-        V xx = reinterpret_cast<V *>(x)[i];
-        V rr = reinterpret_cast<V *>(r)[i];
         xx.x = fma(alpha, pp.x, xx.x);
         xx.y = fma(alpha, pp.y, xx.y);
         rr.x = fma(-alpha, qq.x, rr.x);
@@ -285,12 +335,12 @@ __global__ void __launch_bounds__(kRedBlock) k_cg_pupdate(int32_t n_nodes, const
                                                           T *__restrict__ p, const CGScalarsT<T> *sc)
 {
     typedef typename Vec2<T>::type V;
-    if (*reinterpret_cast<const volatile int *>(&sc->done)) return;
-    const T beta = *reinterpret_cast<const volatile T *>(&sc->beta);
     const int32_t i = blockIdx.x * kRedBlock + threadIdx.x;
     if (i >= n_nodes) return;
     const V zz = reinterpret_cast<const V *>(z)[i];
     V pp = reinterpret_cast<V *>(p)[i];
+    if (*reinterpret_cast<const volatile int *>(&sc->done)) return;
+    const T beta = *reinterpret_cast<const volatile T *>(&sc->beta);
     pp.x = fma(beta, pp.x, zz.x);
     pp.y = fma(beta, pp.y, zz.y);
     reinterpret_cast<V *>(p)[i] = pp;
