@@ -160,6 +160,15 @@ ipfem_status ipfem_newton_solve(ipfem_ctx *ctx, const ipfem_solve_opts *opts, in
  * assembly at the new u. */
 ipfem_status ipfem_set_newton_accel(ipfem_ctx *ctx, int mode);
 
+/* Tangent of the Newton iteration: 0 = Assemble(K, rhs) at every iteration
+ * (the shipped Solution(), main.cpp:229-233); 1 = initial stiffness, the
+ * iteration of the reference's logged runs (the Results folders
+ * CPU_NOT_MODIFIED, CPU_MODIFIED and their GPU and PZ twins: K assembled once,
+ * then only AssembleResidual per iteration, main.cpp:219-228): the tangent of the first assembly after
+ * ipfem_newton_begin is kept for every later linear solve, and later
+ * assemblies compute the residual only. */
+ipfem_status ipfem_set_newton_tangent(ipfem_ctx *ctx, int mode);
+
 /* Resumable form of the same loop: begin sets the options and the step range;
  * each advance performs n_iters Newton iterations (0 = until the last step is
  * accepted).  An iteration is: CG on the current tangent, u += du,
@@ -309,6 +318,59 @@ typedef struct {
 void ipfem_wellbore_default(ipfem_wellbore_params *p, int32_t n);
 ipfem_status ipfem_wellbore_build(const ipfem_wellbore_params *p, ipfem_wellbore **out);
 void ipfem_wellbore_free(ipfem_wellbore *w);
+
+/* ------------------------------------------------------------ Gmsh meshes */
+/* The reference reads its geometry with NeoPZ's TPZGmshReader
+ * (ReadGeometry, main.cpp:447-464; gmsh/wellbore_*.msh).  This reads the
+ * same files: Gmsh 4.1 ASCII with 4-node quadrilaterals (element type 3),
+ * 2-node lines (type 1) and points (type 15); every element carries the first
+ * physical tag of its entity (0 when it has none).  Node indices are 0-based
+ * in file order.  Other element types, binary files and other format versions
+ * are rejected (IPFEM_INVALID, message in ipfem_last_error(NULL)). */
+typedef struct {
+    int32_t n_nodes;
+    double *xy;                       /* [2*n_nodes] */
+    int32_t n_quads;
+    int32_t *quads, *quad_phys;       /* [4*n_quads] (file node order), [n_quads] */
+    int32_t n_lines;
+    int32_t *lines, *line_phys;       /* [2*n_lines], [n_lines] */
+    int32_t n_points;
+    int32_t *points, *point_phys;     /* [n_points], [n_points] */
+    int32_t n_phys;
+    int32_t *phys_dim, *phys_tag;     /* [n_phys] $PhysicalNames */
+    char **phys_name;                 /* [n_phys] */
+} ipfem_gmsh;
+
+ipfem_status ipfem_gmsh_read(const char *path, ipfem_gmsh **out);
+void ipfem_gmsh_free(ipfem_gmsh *g);
+
+/* A boundary condition on the lines and points of one physical tag: the
+ * reference's TBCData (id, type, value; main.cpp:374-446) as NeoPZ's
+ * elastoplastic material applies it:
+ *   0  u = 0 (both components; non-zero values are rejected)
+ *   1  traction (val[0], val[1]) per unit length
+ *   3  directional Dirichlet: u_k = 0 for every k with val[k] != 0
+ *   6  normal stress: traction val[0] * n, n the outward unit normal
+ * The Dirichlet types act on every node of the tagged entities (for a line,
+ * its two vertices and its midpoint connect). */
+typedef struct {
+    int32_t phys;
+    int32_t type;
+    double val[2];
+} ipfem_bc;
+
+/* Order-2 problem on a Gmsh mesh (CmeshElastoplasticity with p_order 2,
+ * main.cpp:546-601): every quadrilateral whose physical tag is domain_phys
+ * (every quadrilateral if domain_phys < 0) becomes a 9-connect element, its
+ * edge connects at the straight-edge midpoints and its centre connect at the
+ * bilinear centre (the geometric elements are linear).  Connects are numbered
+ * in order of first use by the elements, so that elements close in file
+ * order share nearby rows.  Loads go into df (f0 = 0): load factor 1 applies
+ * them in full.  mat supplies E, nu, cohesion, phi, psi and sigma0
+ * (el_cohesion and el_phi must be NULL).  The result has the layout of the
+ * wellbore provider's and is released with ipfem_wellbore_free. */
+ipfem_status ipfem_gmsh_problem(const ipfem_gmsh *g, int32_t domain_phys, const ipfem_bc *bcs, int32_t n_bc,
+                                const ipfem_material *mat, ipfem_wellbore **out);
 
 #ifdef __cplusplus
 }

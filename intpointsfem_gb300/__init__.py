@@ -70,6 +70,17 @@ class Wellbore(C.Structure):
                 ("fixed", _bp)]
 
 
+class GmshData(C.Structure):
+    _fields_ = [("n_nodes", C.c_int32), ("xy", _dp), ("n_quads", C.c_int32), ("quads", _ip), ("quad_phys", _ip),
+                ("n_lines", C.c_int32), ("lines", _ip), ("line_phys", _ip), ("n_points", C.c_int32),
+                ("points", _ip), ("point_phys", _ip), ("n_phys", C.c_int32), ("phys_dim", _ip),
+                ("phys_tag", _ip), ("phys_name", C.POINTER(C.c_char_p))]
+
+
+class BC(C.Structure):
+    _fields_ = [("phys", C.c_int32), ("type", C.c_int32), ("val", C.c_double * 2)]
+
+
 _lib = None
 
 
@@ -128,6 +139,11 @@ def lib():
             "ipfem_wellbore_default": (None, [C.POINTER(WellboreParams), C.c_int32]),
             "ipfem_wellbore_build": (S, [C.POINTER(WellboreParams), C.POINTER(C.POINTER(Wellbore))]),
             "ipfem_wellbore_free": (None, [C.POINTER(Wellbore)]),
+            "ipfem_set_newton_tangent": (S, [P, S]),
+            "ipfem_gmsh_read": (S, [C.c_char_p, C.POINTER(C.POINTER(GmshData))]),
+            "ipfem_gmsh_free": (None, [C.POINTER(GmshData)]),
+            "ipfem_gmsh_problem": (S, [C.POINTER(GmshData), C.c_int32, C.POINTER(BC), C.c_int32,
+                                       C.POINTER(Material), C.POINTER(C.POINTER(Wellbore))]),
         }
         for name, (res, args) in sig.items():
             f = getattr(L, name)
@@ -213,6 +229,75 @@ class WellboreMesh:
             pass
 
 
+class GmshMesh:
+    """A Gmsh 4.1 mesh as the reference reads it (TPZGmshReader, main.cpp:447-464):
+    vertices, 4-node quadrilaterals, boundary lines and points with their
+    physical tags, and the $PhysicalNames table (name -> (dim, tag))."""
+
+    def __init__(self, path):
+        self._g = C.POINTER(GmshData)()
+        st = lib().ipfem_gmsh_read(os.fsencode(path), C.byref(self._g))
+        if st != 0:
+            raise IpfemError(st, lib().ipfem_last_error(None).decode())
+        g = self._g.contents
+
+        def arr(p, n):
+            return np.ctypeslib.as_array(p, shape=(n,)).copy() if n else np.zeros(0, np.int32)
+
+        self.xy = arr(g.xy, 2 * g.n_nodes).reshape(-1, 2) if g.n_nodes else np.zeros((0, 2))
+        self.quads = arr(g.quads, 4 * g.n_quads).reshape(-1, 4)
+        self.quad_phys = arr(g.quad_phys, g.n_quads)
+        self.lines = arr(g.lines, 2 * g.n_lines).reshape(-1, 2)
+        self.line_phys = arr(g.line_phys, g.n_lines)
+        self.points = arr(g.points, g.n_points)
+        self.point_phys = arr(g.point_phys, g.n_points)
+        self.physical = {g.phys_name[i].decode(): (int(g.phys_dim[i]), int(g.phys_tag[i])) for i in range(g.n_phys)}
+
+    def tag(self, name_or_tag):
+        return self.physical[name_or_tag][1] if isinstance(name_or_tag, str) else int(name_or_tag)
+
+    def close(self):
+        if self._g:
+            lib().ipfem_gmsh_free(self._g)
+            self._g = C.POINTER(GmshData)()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class GmshProblem(WellboreMesh):
+    """Order-2 elastoplastic problem on a Gmsh mesh (CmeshElastoplasticity,
+    main.cpp:546-601).  bcs: (physical name or tag, type, value...) with the
+    reference's TBCData types: 0 u = 0, 1 traction (tx, ty), 3 directional
+    Dirichlet (fix the components with non-zero value), 6 normal stress
+    (value * outward normal).  Loads are applied at load factor 1; angles in
+    degrees; domain: physical name or tag of the quadrilaterals (None: all)."""
+
+    def __init__(self, gmsh, bcs, E, nu, cohesion, phi_deg, psi_deg=None, domain=None, sigma0=(0.0, 0.0, 0.0, 0.0)):
+        self.params = None
+        arr = (BC * max(1, len(bcs)))()
+        for i, b in enumerate(bcs):
+            v = list(b[2:]) + [0.0, 0.0]
+            arr[i] = BC(gmsh.tag(b[0]), int(b[1]), (C.c_double * 2)(float(v[0]), float(v[1])))
+        m = Material()
+        m.E, m.nu, m.cohesion = float(E), float(nu), float(cohesion)
+        m.phi = np.deg2rad(float(phi_deg))
+        m.psi = np.deg2rad(float(phi_deg if psi_deg is None else psi_deg))
+        m.sigma0 = (C.c_double * 4)(*[float(x) for x in sigma0])
+        self._w = C.POINTER(Wellbore)()
+        dom = -1 if domain is None else gmsh.tag(domain)
+        st = lib().ipfem_gmsh_problem(gmsh._g, int(dom), arr, len(bcs), C.byref(m), C.byref(self._w))
+        if st != 0:
+            raise IpfemError(st, lib().ipfem_last_error(None).decode())
+        w = self._w.contents
+        self.n_el = w.mesh.n_elements
+        self.n_nodes = w.mesh.n_nodes
+        self.neq = 2 * self.n_nodes
+
+
 class ElastoPlasticIntPointsStructMatrix:
     """Mirror of TPZElastoPlasticIntPointsStructMatrix over one ipfem context.
 
@@ -279,6 +364,11 @@ class ElastoPlasticIntPointsStructMatrix:
     def set_newton_accel(self, mode):
         """0: plain Newton iteration; 1: modified-Thomas acceleration (main.cpp:194-217)"""
         self._check(lib().ipfem_set_newton_accel(self._ctx, int(mode)))
+
+    def set_newton_tangent(self, mode):
+        """0: Assemble(K, rhs) every iteration; 1: initial stiffness, the K of the
+        first assembly kept (the reference's logged runs, main.cpp:219-228)"""
+        self._check(lib().ipfem_set_newton_tangent(self._ctx, int(mode)))
 
     def set_precision(self, mode):
         self._check(lib().ipfem_set_precision(self._ctx, int(mode)))

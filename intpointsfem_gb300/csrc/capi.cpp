@@ -514,6 +514,13 @@ ipfem_status ipfem_set_newton_accel(ipfem_ctx *c, int mode)
     return IPFEM_OK;
 }
 
+ipfem_status ipfem_set_newton_tangent(ipfem_ctx *c, int mode)
+{
+    if (!c || (mode != 0 && mode != 1)) return fail(c, IPFEM_INVALID, "bad Newton tangent mode");
+    c->newton_tangent = mode;
+    return IPFEM_OK;
+}
+
 ipfem_status ipfem_assemble(ipfem_ctx *c, const double *u, double *rhs, int where)
 {
     return assemble_common(c, u, rhs, where, true);
@@ -565,6 +572,20 @@ ipfem_status ipfem_solve(ipfem_ctx *c, const double *b, double *x, double rtol, 
 // that converges (or reaches newton_max_it) is accepted (state commit,
 // main.cpp:487-522) and the next step's first assembly happens at the start
 // of the following iteration.
+// Assemble(K, rhs) of a Newton iteration, or Assemble(rhs) alone in the
+// initial-stiffness mode once a tangent exists (the reference's logged runs:
+// the linear solve reuses the K of the first assembly, main.cpp:219-228 with
+// AssembleResidual per iteration)
+static void newton_assemble(ipfem_ctx *c, double *du)
+{
+    if (c->newton_tangent == 1 && c->ns.have_k) {
+        residual_device(c, du, c->d_rhs, 0);
+    } else {
+        tangent_device(c, du, c->d_rhs, 0);
+        c->ns.have_k = 1;
+    }
+}
+
 static ipfem_status newton_advance(ipfem_ctx *c, int32_t n_iters, double *du, ipfem_solve_stats *st, double *log,
                                    int32_t log_cap, int32_t *nlog)
 {
@@ -582,7 +603,7 @@ static ipfem_status newton_advance(ipfem_ctx *c, int32_t n_iters, double *du, ip
         if (!ns.open) {
             c->load_factor = (double)(ns.step + 1) / (double)o.n_steps;
             cudaEventRecord(ev[0], c->stream);
-            tangent_device(c, du, c->d_rhs, 0);
+            newton_assemble(c, du);
             cudaEventRecord(ev[1], c->stream);
             double r0sq = 0;
             ipfem_status e = dot_host(c, c->d_rhs, c->d_rhs, &r0sq);
@@ -637,7 +658,7 @@ static ipfem_status newton_advance(ipfem_ctx *c, int32_t n_iters, double *du, ip
             done++;
             st->newton_iters++;
             cudaEventRecord(ev[0], c->stream);
-            tangent_device(c, du, c->d_rhs, 0);
+            newton_assemble(c, du);
             cudaEventRecord(ev[1], c->stream);
             double rsq = 0;
             e = dot_host(c, c->d_rhs, c->d_rhs, &rsq);

@@ -1,0 +1,465 @@
+// Gmsh meshes on the host: the reader that stands in for NeoPZ's
+// TPZGmshReader (ReadGeometry, main.cpp:447-464; the reference's meshes are
+// gmsh/wellbore_*.msh, Gmsh 4.1 ASCII), and the order-2 problem built on them
+// as CmeshElastoplasticity does (main.cpp:546-601): the elastoplastic domain
+// on the quadrilaterals and the TBCData boundary conditions (main.cpp:374-446)
+// on the tagged lines and points.
+//
+// Compiled with -ffp-contract=off: coordinates, element blocks and loads are
+// the separately rounded results of the written expressions on every host.
+#include <cmath>
+#include <cstdint>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <new>
+#include <string>
+#include <unordered_map>
+#include <vector>
+
+#include "ipfem_internal.h"
+
+using namespace ipfem;
+
+namespace {
+
+// whitespace tokenizer over the whole file
+struct Tokens {
+    std::string buf;
+    size_t pos = 0;
+    bool bad = false;
+
+    void skip_ws()
+    {
+        while (pos < buf.size() && (buf[pos] == ' ' || buf[pos] == '\t' || buf[pos] == '\r' || buf[pos] == '\n'))
+            pos++;
+    }
+    std::string word()
+    {
+        skip_ws();
+        const size_t b = pos;
+        while (pos < buf.size() && !(buf[pos] == ' ' || buf[pos] == '\t' || buf[pos] == '\r' || buf[pos] == '\n'))
+            pos++;
+        if (b == pos) bad = true;
+        return buf.substr(b, pos - b);
+    }
+    // rest of the current line (after the last token read), without the newline
+    std::string rest_of_line()
+    {
+        const size_t b = pos;
+        while (pos < buf.size() && buf[pos] != '\n') pos++;
+        std::string s = buf.substr(b, pos - b);
+        if (pos < buf.size()) pos++;
+        while (!s.empty() && (s.back() == '\r' || s.back() == ' ')) s.pop_back();
+        return s;
+    }
+    long long integer()
+    {
+        const std::string w = word();
+        char *end = nullptr;
+        const long long v = std::strtoll(w.c_str(), &end, 10);
+        if (w.empty() || *end) bad = true;
+        return v;
+    }
+    double real()
+    {
+        const std::string w = word();
+        char *end = nullptr;
+        const double v = std::strtod(w.c_str(), &end);
+        if (w.empty() || *end) bad = true;
+        return v;
+    }
+};
+
+ipfem_status gmsh_fail(const std::string &msg)
+{
+    set_thread_error("Gmsh: " + msg);
+    return IPFEM_INVALID;
+}
+
+int32_t *dup_i32(const std::vector<int32_t> &v)
+{
+    int32_t *p = (int32_t *)std::malloc((v.size() ? v.size() : 1) * sizeof(int32_t));
+    if (p && !v.empty()) std::memcpy(p, v.data(), v.size() * sizeof(int32_t));
+    return p;
+}
+
+uint64_t edge_key(int32_t a, int32_t b)
+{
+    const uint32_t lo = (uint32_t)(a < b ? a : b), hi = (uint32_t)(a < b ? b : a);
+    return ((uint64_t)lo << 32) | hi;
+}
+
+// consistent load of a constant traction (tx, ty) on a straight 3-connect
+// edge A-M-B: the Q2 trace functions integrate to L/6, 2L/3, L/6
+void edge_load(const double *xy, int32_t A, int32_t M, int32_t B, double tx, double ty, double *f)
+{
+    const double dx = xy[2 * (size_t)B] - xy[2 * (size_t)A];
+    const double dy = xy[2 * (size_t)B + 1] - xy[2 * (size_t)A + 1];
+    const double L = std::sqrt(dx * dx + dy * dy);
+    const double we = L / 6.0, wm = 2.0 * L / 3.0;
+    f[2 * (size_t)A] += tx * we;
+    f[2 * (size_t)A + 1] += ty * we;
+    f[2 * (size_t)M] += tx * wm;
+    f[2 * (size_t)M + 1] += ty * wm;
+    f[2 * (size_t)B] += tx * we;
+    f[2 * (size_t)B + 1] += ty * we;
+}
+
+}  // namespace
+
+extern "C" void ipfem_gmsh_free(ipfem_gmsh *g)
+{
+    if (!g) return;
+    std::free(g->xy);
+    std::free(g->quads);
+    std::free(g->quad_phys);
+    std::free(g->lines);
+    std::free(g->line_phys);
+    std::free(g->points);
+    std::free(g->point_phys);
+    std::free(g->phys_dim);
+    std::free(g->phys_tag);
+    if (g->phys_name)
+        for (int32_t i = 0; i < g->n_phys; i++) std::free(g->phys_name[i]);
+    std::free(g->phys_name);
+    delete g;
+}
+
+extern "C" ipfem_status ipfem_gmsh_read(const char *path, ipfem_gmsh **out)
+{
+    if (!path || !out) return gmsh_fail("null argument");
+    *out = nullptr;
+    Tokens t;
+    {
+        FILE *f = std::fopen(path, "rb");
+        if (!f) return gmsh_fail(std::string("cannot open ") + path);
+        char chunk[1 << 16];
+        size_t n;
+        while ((n = std::fread(chunk, 1, sizeof chunk, f)) > 0) t.buf.append(chunk, n);
+        std::fclose(f);
+    }
+    bool have_format = false, have_nodes = false, have_elements = false;
+    // (dim, entity tag) -> first physical tag
+    std::unordered_map<uint64_t, int32_t> ent_phys;
+    auto ent_key = [](long long dim, long long tag) { return ((uint64_t)dim << 40) ^ (uint64_t)tag; };
+    std::unordered_map<long long, int32_t> node_index;
+    std::vector<double> xy;
+    std::vector<int32_t> quads, quad_phys, lines, line_phys, points, point_phys, pdim, ptag;
+    std::vector<std::string> pname;
+    while (true) {
+        t.skip_ws();
+        if (t.pos >= t.buf.size()) break;
+        const std::string sec = t.word();
+        if (sec.empty() || sec[0] != '$') return gmsh_fail("expected a section, found '" + sec + "'");
+        const std::string name = sec.substr(1);
+        if (name == "MeshFormat") {
+            const std::string ver = t.word();
+            const long long ftype = t.integer();
+            t.integer();   // data size
+            if (ver.compare(0, 3, "4.1") != 0) return gmsh_fail("format " + ver + " (4.1 is supported)");
+            if (ftype != 0) return gmsh_fail("binary files are not supported");
+            have_format = true;
+        } else if (name == "PhysicalNames") {
+            const long long n = t.integer();
+            t.rest_of_line();
+            for (long long i = 0; i < n && !t.bad; i++) {
+                pdim.push_back((int32_t)t.integer());
+                ptag.push_back((int32_t)t.integer());
+                std::string s = t.rest_of_line();
+                const size_t a = s.find('"'), b = s.rfind('"');
+                pname.push_back(a != std::string::npos && b > a ? s.substr(a + 1, b - a - 1) : s);
+            }
+        } else if (name == "Entities") {
+            long long cnt[4];
+            for (int d = 0; d < 4; d++) cnt[d] = t.integer();
+            for (int d = 0; d < 4 && !t.bad; d++)
+                for (long long i = 0; i < cnt[d] && !t.bad; i++) {
+                    const long long tag = t.integer();
+                    for (int k = 0; k < (d == 0 ? 3 : 6); k++) t.real();
+                    const long long np = t.integer();
+                    int32_t phys = 0;
+                    for (long long k = 0; k < np; k++) {
+                        const long long ph = t.integer();
+                        if (k == 0) phys = (int32_t)ph;
+                    }
+                    if (d > 0) {
+                        const long long nb = t.integer();
+                        for (long long k = 0; k < nb; k++) t.integer();
+                    }
+                    ent_phys[ent_key(d, tag)] = phys;
+                }
+        } else if (name == "Nodes") {
+            const long long nblocks = t.integer(), nnodes = t.integer();
+            t.integer();
+            t.integer();
+            if (t.bad || nnodes < 0 || nnodes > INT32_MAX / 2) return gmsh_fail("bad $Nodes header");
+            xy.reserve((size_t)nnodes * 2);
+            for (long long b = 0; b < nblocks && !t.bad; b++) {
+                const long long edim = t.integer();
+                t.integer();
+                const long long parametric = t.integer(), n = t.integer();
+                if (t.bad || n < 0 || edim < 0 || edim > 3) return gmsh_fail("bad node block");
+                std::vector<long long> tags((size_t)n);
+                for (long long i = 0; i < n; i++) tags[(size_t)i] = t.integer();
+                for (long long i = 0; i < n && !t.bad; i++) {
+                    const double x = t.real(), y = t.real(), z = t.real();
+                    if (parametric) for (long long k = 0; k < edim; k++) t.real();
+                    if (z != 0.0) return gmsh_fail("node outside the z = 0 plane");
+                    if (!node_index.emplace(tags[(size_t)i], (int32_t)(xy.size() / 2)).second)
+                        return gmsh_fail("duplicate node tag " + std::to_string(tags[(size_t)i]));
+                    xy.push_back(x);
+                    xy.push_back(y);
+                }
+            }
+            have_nodes = true;
+        } else if (name == "Elements") {
+            if (!have_nodes) return gmsh_fail("$Elements before $Nodes");
+            const long long nblocks = t.integer();
+            t.integer();
+            t.integer();
+            t.integer();
+            for (long long b = 0; b < nblocks && !t.bad; b++) {
+                const long long edim = t.integer(), etag = t.integer(), type = t.integer(), n = t.integer();
+                if (t.bad || n < 0) return gmsh_fail("bad element block");
+                int nn;
+                std::vector<int32_t> *conn, *phys;
+                if (type == 15) { nn = 1; conn = &points; phys = &point_phys; }
+                else if (type == 1) { nn = 2; conn = &lines; phys = &line_phys; }
+                else if (type == 3) { nn = 4; conn = &quads; phys = &quad_phys; }
+                else
+                    return gmsh_fail("element type " + std::to_string(type) +
+                                     " is not supported (4-node quadrilaterals, 2-node lines and points)");
+                auto it = ent_phys.find(ent_key(edim, etag));
+                const int32_t ph = it == ent_phys.end() ? 0 : it->second;
+                for (long long i = 0; i < n && !t.bad; i++) {
+                    t.integer();   // element tag
+                    for (int k = 0; k < nn; k++) {
+                        const long long nt = t.integer();
+                        auto f = node_index.find(nt);
+                        if (f == node_index.end()) return gmsh_fail("unknown node tag " + std::to_string(nt));
+                        conn->push_back(f->second);
+                    }
+                    phys->push_back(ph);
+                }
+            }
+            have_elements = true;
+        } else {
+            // sections without a bearing on the problem ($Periodic, $NodeData, ...)
+            const std::string end = "$End" + name;
+            const size_t e = t.buf.find(end, t.pos);
+            if (e == std::string::npos) return gmsh_fail("unterminated section " + sec);
+            t.pos = e;
+        }
+        if (t.bad) return gmsh_fail("malformed section " + sec);
+        const std::string end = t.word();
+        if (end != "$End" + name) return gmsh_fail("expected $End" + name + ", found '" + end + "'");
+    }
+    if (!have_format || !have_nodes || !have_elements) return gmsh_fail("missing $MeshFormat, $Nodes or $Elements");
+    ipfem_gmsh *g = new (std::nothrow) ipfem_gmsh();
+    if (!g) return IPFEM_OOM;
+    std::memset(g, 0, sizeof *g);
+    g->n_nodes = (int32_t)(xy.size() / 2);
+    g->xy = (double *)std::malloc((xy.size() ? xy.size() : 1) * sizeof(double));
+    if (g->xy && !xy.empty()) std::memcpy(g->xy, xy.data(), xy.size() * sizeof(double));
+    g->n_quads = (int32_t)quad_phys.size();
+    g->quads = dup_i32(quads);
+    g->quad_phys = dup_i32(quad_phys);
+    g->n_lines = (int32_t)line_phys.size();
+    g->lines = dup_i32(lines);
+    g->line_phys = dup_i32(line_phys);
+    g->n_points = (int32_t)point_phys.size();
+    g->points = dup_i32(points);
+    g->point_phys = dup_i32(point_phys);
+    g->n_phys = (int32_t)pname.size();
+    g->phys_dim = dup_i32(pdim);
+    g->phys_tag = dup_i32(ptag);
+    g->phys_name = (char **)std::calloc(pname.size() ? pname.size() : 1, sizeof(char *));
+    bool ok = g->xy && g->quads && g->quad_phys && g->lines && g->line_phys && g->points && g->point_phys &&
+              g->phys_dim && g->phys_tag && g->phys_name;
+    for (size_t i = 0; ok && i < pname.size(); i++) {
+        g->phys_name[i] = (char *)std::malloc(pname[i].size() + 1);
+        if (!g->phys_name[i]) ok = false;
+        else std::memcpy(g->phys_name[i], pname[i].c_str(), pname[i].size() + 1);
+    }
+    if (!ok) {
+        ipfem_gmsh_free(g);
+        return IPFEM_OOM;
+    }
+    *out = g;
+    return IPFEM_OK;
+}
+
+extern "C" ipfem_status ipfem_gmsh_problem(const ipfem_gmsh *g, int32_t domain_phys, const ipfem_bc *bcs, int32_t n_bc,
+                                           const ipfem_material *mat, ipfem_wellbore **out)
+{
+    if (!g || !mat || !out || (n_bc > 0 && !bcs) || n_bc < 0) return gmsh_fail("null argument");
+    *out = nullptr;
+    if (mat->el_cohesion || mat->el_phi) return gmsh_fail("per-element material arrays are not supported here");
+    for (int32_t b = 0; b < n_bc; b++) {
+        const int ty = bcs[b].type;
+        if (ty != 0 && ty != 1 && ty != 3 && ty != 6)
+            return gmsh_fail("boundary condition type " + std::to_string(ty) + " (0, 1, 3 and 6 are supported)");
+        if (ty == 0 && (bcs[b].val[0] != 0.0 || bcs[b].val[1] != 0.0))
+            return gmsh_fail("non-zero Dirichlet values are not supported");
+    }
+    // the domain's quadrilaterals, in file order
+    std::vector<int32_t> els;
+    for (int32_t q = 0; q < g->n_quads; q++)
+        if (domain_phys < 0 || g->quad_phys[q] == domain_phys) els.push_back(q);
+    if (els.empty()) return gmsh_fail("no quadrilateral carries physical tag " + std::to_string(domain_phys));
+    const int64_t n_el = (int64_t)els.size();
+    // edges: key -> edge index; first element and number of elements per edge
+    std::unordered_map<uint64_t, int32_t> edge_of;
+    edge_of.reserve((size_t)n_el * 2);
+    std::vector<int32_t> edge_el, edge_uses;
+    std::vector<int32_t> el_edge((size_t)n_el * 4);
+    for (int64_t e = 0; e < n_el; e++) {
+        const int32_t *v = &g->quads[4 * (size_t)els[(size_t)e]];
+        for (int k = 0; k < 4; k++) {
+            const int32_t a = v[k], b = v[(k + 1) & 3];
+            if (a == b) return gmsh_fail("degenerate quadrilateral");
+            auto ins = edge_of.emplace(edge_key(a, b), (int32_t)edge_el.size());
+            if (ins.second) {
+                edge_el.push_back((int32_t)e);
+                edge_uses.push_back(0);
+            }
+            if (++edge_uses[(size_t)ins.first->second] > 2) return gmsh_fail("an edge is shared by more than two quadrilaterals");
+            el_edge[4 * (size_t)e + k] = ins.first->second;
+        }
+    }
+    const int64_t n_edges = (int64_t)edge_el.size();
+    const int64_t n_nodes_max = (int64_t)g->n_nodes + n_edges + n_el;
+    if (2 * n_nodes_max > INT32_MAX || n_el * 81 > INT32_MAX) return gmsh_fail("mesh too large");
+    // connects numbered in order of first use by the elements
+    std::vector<int32_t> vnew((size_t)g->n_nodes, -1), enew((size_t)n_edges, -1);
+    std::vector<int32_t> conn((size_t)n_el * 9);
+    int32_t next = 0;
+    for (int64_t e = 0; e < n_el; e++) {
+        const int32_t *v = &g->quads[4 * (size_t)els[(size_t)e]];
+        int32_t *c = &conn[9 * (size_t)e];
+        for (int k = 0; k < 4; k++) {
+            if (vnew[(size_t)v[k]] < 0) vnew[(size_t)v[k]] = next++;
+            c[k] = vnew[(size_t)v[k]];
+        }
+        for (int k = 0; k < 4; k++) {
+            int32_t &en = enew[(size_t)el_edge[4 * (size_t)e + k]];
+            if (en < 0) en = next++;
+            c[4 + k] = en;
+        }
+        c[8] = next++;
+    }
+    const int64_t n_nodes = next, neq = 2 * n_nodes;
+    ipfem_wellbore *w = new (std::nothrow) ipfem_wellbore();
+    if (!w) return IPFEM_OOM;
+    std::memset(w, 0, sizeof *w);
+    w->node_xy = (double *)std::calloc((size_t)n_nodes * 2, sizeof(double));
+    w->connects = (int32_t *)std::calloc((size_t)n_el * 9, sizeof(int32_t));
+    w->dphi = (double *)std::calloc((size_t)n_el * 162, sizeof(double));
+    w->weight = (double *)std::calloc((size_t)n_el * 9, sizeof(double));
+    w->f0 = (double *)std::calloc((size_t)neq, sizeof(double));
+    w->df = (double *)std::calloc((size_t)neq, sizeof(double));
+    w->fixed = (uint8_t *)std::calloc((size_t)neq, 1);
+    if (!w->node_xy || !w->connects || !w->dphi || !w->weight || !w->f0 || !w->df || !w->fixed) {
+        ipfem_wellbore_free(w);
+        return IPFEM_OOM;
+    }
+    std::memcpy(w->connects, conn.data(), conn.size() * sizeof(int32_t));
+    // coordinates: vertices, straight-edge midpoints, bilinear centres
+    for (int64_t e = 0; e < n_el; e++) {
+        const int32_t *v = &g->quads[4 * (size_t)els[(size_t)e]];
+        const int32_t *c = &conn[9 * (size_t)e];
+        const double *p[4];
+        for (int k = 0; k < 4; k++) {
+            p[k] = &g->xy[2 * (size_t)v[k]];
+            w->node_xy[2 * (size_t)c[k]] = p[k][0];
+            w->node_xy[2 * (size_t)c[k] + 1] = p[k][1];
+        }
+        for (int k = 0; k < 4; k++) {
+            const double *a = p[k], *b = p[(k + 1) & 3];
+            w->node_xy[2 * (size_t)c[4 + k]] = 0.5 * (a[0] + b[0]);
+            w->node_xy[2 * (size_t)c[4 + k] + 1] = 0.5 * (a[1] + b[1]);
+        }
+        w->node_xy[2 * (size_t)c[8]] = 0.25 * (((p[0][0] + p[1][0]) + p[2][0]) + p[3][0]);
+        w->node_xy[2 * (size_t)c[8] + 1] = 0.25 * (((p[0][1] + p[1][1]) + p[2][1]) + p[3][1]);
+    }
+    element_blocks_dphi(n_el, w->connects, w->node_xy, w->dphi, w->weight);
+    // boundary conditions
+    for (int32_t b = 0; b < n_bc; b++) {
+        const ipfem_bc &bc = bcs[b];
+        int64_t hits = 0;
+        auto fix_node = [&](int32_t node) {
+            for (int k = 0; k < 2; k++)
+                if (bc.type == 0 || bc.val[k] != 0.0) w->fixed[2 * (size_t)node + k] = 1;
+        };
+        for (int32_t l = 0; l < g->n_lines; l++) {
+            if (g->line_phys[l] != bc.phys) continue;
+            hits++;
+            const int32_t a = g->lines[2 * (size_t)l], bb = g->lines[2 * (size_t)l + 1];
+            auto f = edge_of.find(edge_key(a, bb));
+            if (f == edge_of.end()) {
+                ipfem_wellbore_free(w);
+                return gmsh_fail("a line of physical tag " + std::to_string(bc.phys) + " is not an element edge");
+            }
+            const int32_t A = vnew[(size_t)a], B = vnew[(size_t)bb], M = enew[(size_t)f->second];
+            if (bc.type == 0 || bc.type == 3) {
+                fix_node(A);
+                fix_node(M);
+                fix_node(B);
+            } else if (bc.type == 1) {
+                edge_load(w->node_xy, A, M, B, bc.val[0], bc.val[1], w->df);
+            } else {
+                if (edge_uses[(size_t)f->second] != 1) {
+                    ipfem_wellbore_free(w);
+                    return gmsh_fail("a normal-stress line of physical tag " + std::to_string(bc.phys) +
+                                     " is not on the boundary");
+                }
+                // outward normal: away from the adjacent element's centre
+                const double *pa = &w->node_xy[2 * (size_t)A], *pb = &w->node_xy[2 * (size_t)B];
+                const double dx = pb[0] - pa[0], dy = pb[1] - pa[1];
+                const double L = std::sqrt(dx * dx + dy * dy);
+                double nx = dy / L, ny = -dx / L;
+                const double *pc = &w->node_xy[2 * (size_t)conn[9 * (size_t)edge_el[(size_t)f->second] + 8]];
+                const double *pm = &w->node_xy[2 * (size_t)M];
+                if ((pc[0] - pm[0]) * nx + (pc[1] - pm[1]) * ny > 0.0) {
+                    nx = -nx;
+                    ny = -ny;
+                }
+                edge_load(w->node_xy, A, M, B, bc.val[0] * nx, bc.val[0] * ny, w->df);
+            }
+        }
+        for (int32_t q = 0; q < g->n_points; q++) {
+            if (g->point_phys[q] != bc.phys) continue;
+            hits++;
+            const int32_t node = vnew[(size_t)g->points[q]];
+            if (node < 0) {
+                ipfem_wellbore_free(w);
+                return gmsh_fail("a point of physical tag " + std::to_string(bc.phys) + " is not an element vertex");
+            }
+            if (bc.type == 1 || bc.type == 6) {
+                ipfem_wellbore_free(w);
+                return gmsh_fail("traction boundary conditions need lines (physical tag " + std::to_string(bc.phys) +
+                                 " has points)");
+            }
+            fix_node(node);
+        }
+        if (hits == 0) {
+            ipfem_wellbore_free(w);
+            return gmsh_fail("no line or point carries physical tag " + std::to_string(bc.phys));
+        }
+    }
+    w->material = *mat;
+    w->material.el_cohesion = nullptr;
+    w->material.el_phi = nullptr;
+    w->mesh.n_elements = (int32_t)n_el;
+    w->mesh.n_nodes = (int32_t)n_nodes;
+    w->mesh.connects = w->connects;
+    w->mesh.dphi = w->dphi;
+    w->mesh.block_storage = nullptr;
+    w->mesh.weight = w->weight;
+    w->mesh.fixed = w->fixed;
+    w->mesh.f0 = w->f0;
+    w->mesh.df = w->df;
+    *out = w;
+    return IPFEM_OK;
+}

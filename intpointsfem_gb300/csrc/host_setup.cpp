@@ -332,6 +332,19 @@ static void element_dphi(const double *X, const double *Y, double *dphi, double 
     }
 }
 
+void element_blocks_dphi(int64_t n_el, const int32_t *connects, const double *node_xy, double *dphi,
+                         double *weight)
+{
+    parallel_for(n_el, [&](int64_t e) {
+        double X[4], Y[4];
+        for (int v = 0; v < 4; v++) {
+            X[v] = node_xy[2 * (size_t)connects[9 * e + v]];
+            Y[v] = node_xy[2 * (size_t)connects[9 * e + v] + 1];
+        }
+        element_dphi(X, Y, dphi + e * 162, weight + e * 9);
+    });
+}
+
 static void seg_load(const double *xy, int32_t P, int32_t M, int32_t Q, int sgn, double sxx, double sxy, double syy,
                      double *f)
 {
@@ -472,14 +485,7 @@ extern "C" ipfem_status ipfem_wellbore_build(const ipfem_wellbore_params *prm, i
             c[4] = nid(a0 + 1, b0); c[5] = nid(a0 + 2, b0 + 1); c[6] = nid(a0 + 1, b0 + 2); c[7] = nid(a0, b0 + 1);
             c[8] = nid(a0 + 1, b0 + 1);
         }
-    parallel_for(n_el, [&](int64_t e) {
-        double X[4], Y[4];
-        for (int v = 0; v < 4; v++) {
-            X[v] = w->node_xy[2 * (size_t)w->connects[9 * e + v]];
-            Y[v] = w->node_xy[2 * (size_t)w->connects[9 * e + v] + 1];
-        }
-        element_dphi(X, Y, w->dphi + e * 162, w->weight + e * 9);
-    });
+    element_blocks_dphi(n_el, w->connects, w->node_xy, w->dphi, w->weight);
     for (int a = 0; a < gr; a++) {
         w->fixed[2 * (size_t)nid(a, 0) + 1] = 1;
         w->fixed[2 * (size_t)nid(a, gt - 1) + 0] = 1;

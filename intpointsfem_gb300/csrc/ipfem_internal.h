@@ -95,6 +95,10 @@ struct Setup {
 
 // builds the setup; returns an empty string or an error message
 std::string build_setup(const ipfem_mesh *mesh, const ipfem_material *mat, Setup &s);
+// d(phi)/dx, d(phi)/dy and w|detJ| at the 3x3 Gauss points of Q2 elements
+// with bilinear geometry from their 4 vertex connects (host, threaded)
+void element_blocks_dphi(int64_t n_el, const int32_t *connects, const double *node_xy, double *dphi,
+                         double *weight);
 // SELL-32 layout of s's block pattern; sorted: rows by length inside each
 // kRedBlock-node window (stable, longest first)
 std::string build_sell(const Setup &s, bool sorted, SellLayout &L);
@@ -111,6 +115,7 @@ struct NewtonState {
     int open = 0, active = 0, all_converged = 1;
     double r0 = 0.0, rn = 0.0;
     double alpha = 1.0;           // modified-Thomas acceleration factor of the open load step
+    int have_k = 0;               // a tangent has been assembled since newton_begin
 };
 
 namespace ipfem {
@@ -170,6 +175,7 @@ struct ipfem_ctx {
     unsigned *d_counters = nullptr;      // last-block tickets
     double *d_dotres = nullptr;          // results of standalone dots
     int newton_accel = 0;                // 1: modified-Thomas accelerated Newton (main.cpp:194-224)
+    int newton_tangent = 0;              // 1: initial stiffness (tangent of the first assembly kept)
     double *d_acc = nullptr;             // [neq] alpha * du of the accelerated step
     int *d_err = nullptr;                // device error word (wait timeouts)
     ipfem::CGScalars *h_sc = nullptr;    // pinned

@@ -220,6 +220,8 @@ static void seg_load(const double *xy, int32_t P, int32_t M, int32_t Q, int sgn,
     f[2 * (size_t)Q + 1] += ty * we;
 }
 
+static void problem_setup(orc_problem *p, const orc_params *prm);
+
 orc_problem *orc_problem_create(const orc_params *prm, int nthreads)
 {
     if (nthreads > 0) omp_set_num_threads(nthreads);
@@ -296,6 +298,40 @@ orc_problem *orc_problem_create(const orc_params *prm, int nthreads)
         free(fo); free(fw0); free(fw1);
     }
 #undef NID
+    problem_setup(p, prm);
+    return p;
+}
+
+/* The same problem on a caller's order-2 quadrilateral mesh (connect order of
+ * each element: 4 vertices, 4 edge midpoints, centre; bilinear geometry from
+ * the vertices): material, in-situ seed, setup and state as above. */
+orc_problem *orc_problem_from_mesh(const orc_mesh_in *m, const orc_params *prm, int nthreads)
+{
+    if (nthreads > 0) omp_set_num_threads(nthreads);
+    orc_problem *p = (orc_problem *)xcalloc(1, sizeof *p);
+    p->prm = *prm;
+    p->nthreads = nthreads > 0 ? nthreads : omp_get_max_threads();
+    p->n_el = m->n_el;
+    p->n_nodes = m->n_nodes;
+    p->neq = 2 * m->n_nodes;
+    p->n_ip = (int64_t)p->n_el * ORC_NPTS;
+    p->node_xy = (double *)xcalloc((size_t)p->n_nodes * 2, sizeof(double));
+    memcpy(p->node_xy, m->node_xy, (size_t)p->n_nodes * 2 * sizeof(double));
+    p->connects = (int32_t *)xcalloc((size_t)p->n_el * 9, sizeof(int32_t));
+    memcpy(p->connects, m->connects, (size_t)p->n_el * 9 * sizeof(int32_t));
+    p->fixed = (uint8_t *)xcalloc((size_t)p->neq, 1);
+    if (m->fixed) memcpy(p->fixed, m->fixed, (size_t)p->neq);
+    p->f0 = (double *)xcalloc((size_t)p->neq, sizeof(double));
+    p->df = (double *)xcalloc((size_t)p->neq, sizeof(double));
+    if (m->f0) memcpy(p->f0, m->f0, (size_t)p->neq * sizeof(double));
+    if (m->df) memcpy(p->df, m->df, (size_t)p->neq * sizeof(double));
+    problem_setup(p, prm);
+    return p;
+}
+
+/* material, in-situ seed, B blocks, dof map, colouring, block pattern, state */
+static void problem_setup(orc_problem *p, const orc_params *prm)
+{
     /* material */
     orc_lame_from_engineering(prm->E, prm->nu, &p->el);
     p->mats = (orc_mc *)xcalloc((size_t)p->n_el, sizeof(orc_mc));
@@ -419,7 +455,6 @@ orc_problem *orc_problem_create(const orc_params *prm, int nthreads)
     p->dep = (double *)xcalloc((size_t)p->n_ip * 9, sizeof(double));
     p->K = (double *)xcalloc((size_t)p->n_blocks * 4, sizeof(double));
     p->dinv = (double *)xcalloc((size_t)p->neq, sizeof(double));
-    return p;
 }
 
 void orc_problem_destroy(orc_problem *p)
@@ -689,11 +724,25 @@ void orc_solve_steps(orc_problem *p, const orc_solve_opts *o, int32_t step_begin
     double *work = (double *)xcalloc((size_t)n * 4, sizeof(double));
     double *t = o->accel ? (double *)xcalloc((size_t)n, sizeof(double)) : NULL;
     int32_t nlog = 0;
+    int have_k = 0;
     memset(st, 0, sizeof *st);
     st->converged = 1;
+    /* tangent_mode 1, the initial-stiffness iteration of the reference's
+     * logged runs (Solution(), main.cpp:219-228, with only the residual
+     * assembled per iteration): K and the Jacobi diagonal of the first
+     * assembly are kept, later assemblies compute the residual alone */
+#define ASSEMBLE_ITER()                                          \
+    do {                                                         \
+        if (o->tangent_mode == 1 && have_k) {                    \
+            orc_assemble_residual(p, u, lambda, 0, R);           \
+        } else {                                                 \
+            orc_assemble(p, u, lambda, R);                       \
+            have_k = 1;                                          \
+        }                                                        \
+    } while (0)
     for (int32_t s = step_begin; s < step_end; s++) {
         const double lambda = (double)(s + 1) / (double)o->n_steps;
-        orc_assemble(p, u, lambda, R);
+        ASSEMBLE_ITER();
         const double r0 = sqrt(orc_dot(p->n_nodes, R, R));
         double rn = r0;
         int conv = (r0 == 0.0);
@@ -719,7 +768,7 @@ void orc_solve_steps(orc_problem *p, const orc_solve_opts *o, int32_t step_begin
             }
             for (int32_t i = 0; i < n; i++) u[i] = u[i] + du[i];
             it++;
-            orc_assemble(p, u, lambda, R);
+            ASSEMBLE_ITER();
             rn = sqrt(orc_dot(p->n_nodes, R, R));
             if (log && nlog < log_cap) {
                 log[3 * nlog + 0] = (double)s;
@@ -736,4 +785,5 @@ void orc_solve_steps(orc_problem *p, const orc_solve_opts *o, int32_t step_begin
         orc_assemble_residual(p, u, lambda, 1, R);     /* accept: commit state */
     }
     free(R); free(du); free(work); free(t);
+#undef ASSEMBLE_ITER
 }

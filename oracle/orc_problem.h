@@ -71,6 +71,16 @@ typedef struct {
 } orc_problem;
 
 orc_problem *orc_problem_create(const orc_params *prm, int nthreads);
+/* a caller's order-2 mesh; prm supplies the material and in-situ stress
+ * (its mesh fields are ignored) */
+typedef struct {
+    int32_t n_el, n_nodes;
+    const double *node_xy;     /* [n_nodes*2] */
+    const int32_t *connects;   /* [n_el*9] */
+    const uint8_t *fixed;      /* [2*n_nodes] or NULL */
+    const double *f0, *df;     /* [2*n_nodes] or NULL */
+} orc_mesh_in;
+orc_problem *orc_problem_from_mesh(const orc_mesh_in *m, const orc_params *prm, int nthreads);
 void orc_problem_destroy(orc_problem *p);
 void orc_default_params(orc_params *prm, int n);
 
@@ -102,6 +112,7 @@ typedef struct {
     double cg_rtol;
     int32_t cg_max_it;
     int32_t accel;             /* 1: modified-Thomas acceleration (main.cpp:194-217) */
+    int32_t tangent_mode;      /* 1: initial stiffness (K of the first assembly kept) */
 } orc_solve_opts;
 
 typedef struct {

@@ -47,7 +47,13 @@ class Problem(C.Structure):
 
 class SolveOpts(C.Structure):
     _fields_ = [("n_steps", C.c_int32), ("newton_rtol", C.c_double), ("newton_max_it", C.c_int32),
-                ("cg_rtol", C.c_double), ("cg_max_it", C.c_int32), ("accel", C.c_int32)]
+                ("cg_rtol", C.c_double), ("cg_max_it", C.c_int32), ("accel", C.c_int32),
+                ("tangent_mode", C.c_int32)]
+
+
+class MeshIn(C.Structure):
+    _fields_ = [("n_el", C.c_int32), ("n_nodes", C.c_int32), ("node_xy", _dp), ("connects", _ip),
+                ("fixed", _bp), ("f0", _dp), ("df", _dp)]
 
 
 class SolveStats(C.Structure):
@@ -65,6 +71,8 @@ def lib():
         L = C.CDLL(so)
         L.orc_problem_create.restype = C.POINTER(Problem)
         L.orc_problem_create.argtypes = [C.POINTER(Params), C.c_int]
+        L.orc_problem_from_mesh.restype = C.POINTER(Problem)
+        L.orc_problem_from_mesh.argtypes = [C.POINTER(MeshIn), C.POINTER(Params), C.c_int]
         L.orc_problem_destroy.argtypes = [C.POINTER(Problem)]
         L.orc_default_params.argtypes = [C.POINTER(Params), C.c_int]
         L.orc_dot.restype = C.c_double
@@ -120,9 +128,20 @@ def _view(p, n, dtype):
 class OracleProblem:
     """Owns an orc_problem; numpy views of its arrays (valid while alive)."""
 
-    def __init__(self, params, nthreads=0):
+    def __init__(self, params, nthreads=0, mesh=None):
+        """the structured quarter annulus of `params`, or with mesh = dict(node_xy,
+        connects, fixed, f0, df) a caller's order-2 mesh (params then give the
+        material and in-situ stress only)"""
         self.params = params
-        self._p = lib().orc_problem_create(C.byref(params), int(nthreads))
+        if mesh is None:
+            self._p = lib().orc_problem_create(C.byref(params), int(nthreads))
+        else:
+            a = {k: np.ascontiguousarray(mesh[k], dtype=t) for k, t in
+                 (("node_xy", np.float64), ("connects", np.int32), ("fixed", np.uint8), ("f0", np.float64),
+                  ("df", np.float64))}
+            m = MeshIn(a["connects"].size // 9, a["node_xy"].size // 2, ptr(a["node_xy"]), ptr(a["connects"]),
+                       ptr(a["fixed"]), ptr(a["f0"]), ptr(a["df"]))
+            self._p = lib().orc_problem_from_mesh(C.byref(m), C.byref(params), int(nthreads))
         P = self._p.contents
         self.P = P
         self.n_el, self.n_nodes, self.neq, self.n_ip = P.n_el, P.n_nodes, P.neq, P.n_ip
@@ -185,11 +204,11 @@ class OracleProblem:
         return x, k
 
     def solve_steps(self, u, n_steps, step_begin=0, step_end=None, newton_rtol=1e-8, newton_max_it=20,
-                    cg_rtol=1e-8, cg_max_it=200000, log_cap=4096, accel=0):
+                    cg_rtol=1e-8, cg_max_it=200000, log_cap=4096, accel=0, tangent_mode=0):
         if step_end is None:
             step_end = n_steps
         o = SolveOpts(int(n_steps), float(newton_rtol), int(newton_max_it), float(cg_rtol), int(cg_max_it),
-                      int(accel))
+                      int(accel), int(tangent_mode))
         st = SolveStats()
         log = np.zeros(3 * log_cap)
         lib().orc_solve_steps(self._p, C.byref(o), int(step_begin), int(step_end), ptr(u), C.byref(st),

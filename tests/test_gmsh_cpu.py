@@ -1,0 +1,144 @@
+"""Gmsh meshes on the host: the reader (the reference reads its geometry with
+TPZGmshReader, main.cpp:447-464), the generator of the reference's wellbore
+meshes (gmsh/wellbore.geo), the order-2 problem with the reference's boundary
+conditions (main.cpp:397-446, 546-601), and the oracle replaying the
+reference's logged Newton runs on the reference's own mesh."""
+import os
+
+import numpy as np
+import pytest
+
+ip = pytest.importorskip("intpointsfem_gb300")
+from intpointsfem_gb300 import gmsh_wellbore as gw  # noqa: E402
+from oracle import pyoracle as po  # noqa: E402
+
+import replay_helpers as rh  # noqa: E402
+
+REF_GMSH = "/root/reference/gmsh"
+
+
+def _mesh(tmp_path, k):
+    n, q = gw.REFERENCE_MESHES[k]
+    path = str(tmp_path / ("wellbore_%d.msh" % k))
+    gw.write_wellbore_msh(path, n, q)
+    return ip.GmshMesh(path)
+
+
+def _problem(g, cohesion=5.0):
+    bcs, mat = gw.reference_bcs(cohesion)
+    return ip.GmshProblem(g, bcs, **mat)
+
+
+@pytest.mark.parametrize("k", [1, 2, 3])
+def test_equation_and_colour_counts_match_the_logs(tmp_path, k):
+    """order-2 equations and greedy colours of meshes 1-3 equal the
+    reference's logged "DOF" and "Number of colors" for them"""
+    g = _mesh(tmp_path, k)
+    pb = _problem(g)
+    run = rh.reference_run("CPU_NOT_MODIFIED/order2-mesh%d" % k)
+    nc, _ = ip.color_elements(pb.array("connects"), pb.n_nodes)
+    assert pb.neq == run["dof"]
+    assert nc == run["colors"] == 4
+    n = gw.REFERENCE_MESHES[k][0]
+    assert len(g.quads) == 4 * (n - 1) ** 2 and len(g.lines) == 8 * (n - 1) and len(g.points) == 4
+
+
+@pytest.mark.skipif(not os.path.isdir(REF_GMSH), reason="reference meshes not present")
+@pytest.mark.parametrize("k", [1, 2])
+def test_generator_reproduces_the_reference_meshes(tmp_path, k):
+    """same quadrilaterals, boundary lines, tagged points and physical names as
+    gmsh/wellbore_k.msh; coordinates within Gmsh's progression round-off"""
+    a = _mesh(tmp_path, k)
+    b = ip.GmshMesh(os.path.join(REF_GMSH, "wellbore_%d.msh" % k))
+    assert a.physical == b.physical
+    assert a.xy.shape == b.xy.shape
+    spatial = pytest.importorskip("scipy.spatial")
+    dist, idx = spatial.cKDTree(a.xy).query(b.xy)
+    assert dist.max() < 1e-7
+    assert set(map(tuple, np.sort(a.quads, 1))) == set(map(tuple, np.sort(idx[b.quads], 1)))
+    assert set(map(tuple, np.sort(a.lines, 1))) == set(map(tuple, np.sort(idx[b.lines], 1)))
+    assert set(zip(a.points.tolist(), a.point_phys.tolist())) == set(zip(idx[b.points].tolist(),
+                                                                          b.point_phys.tolist()))
+
+
+def test_boundary_loads_and_constraints(tmp_path):
+    """normal stress v on the well: zero net force, and sum f.x = v * (-2 A)
+    for the polygonal hole of area A (divergence theorem); fixed_x / fixed_y
+    fix one component at two points each"""
+    g = _mesh(tmp_path, 1)
+    v = -10.0
+    pb = ip.GmshProblem(g, [("bc_wellbore", 6, v), ("fixed_x", 3, 1, 0), ("fixed_y", 3, 0, 1)], 2000.0, 0.2, 5.0,
+                        20.0)
+    f = pb.array("df").reshape(-1, 2)
+    xy = pb.array("node_xy").reshape(-1, 2)
+    assert abs(f[:, 0].sum()) < 1e-12 and abs(f[:, 1].sum()) < 1e-12
+    th = gw.wellbore_nodes(*gw.REFERENCE_MESHES[1])[1]
+    area = 0.5 * len(th) * 0.1 ** 2 * np.sin(2 * np.pi / len(th))
+    assert abs((f * xy).sum() - v * (-2.0 * area)) < 1e-12
+    fixed = pb.array("fixed").reshape(-1, 2)
+    assert fixed.sum() == 4
+    for comp, pts in ((0, [(0.0, 4.0), (0.0, -4.0)]), (1, [(4.0, 0.0), (-4.0, 0.0)])):
+        for p in pts:
+            node = np.argmin(((xy - p) ** 2).sum(1))
+            assert fixed[node, comp] == 1 and fixed[node, 1 - comp] == 0
+
+
+def test_reader_and_problem_reject_what_they_do_not_support(tmp_path):
+    good = tmp_path / "good.msh"
+    gw.write_wellbore_msh(str(good), 4, 1.2)
+    txt = good.read_text()
+    cases = {
+        "ver.msh": txt.replace("4.1 0 8", "2.2 0 8"),
+        "bin.msh": txt.replace("4.1 0 8", "4.1 1 8"),
+        "tri.msh": txt.replace("2 1 3 9", "2 1 2 9", 1),
+        "z.msh": txt.replace("\n0.10000000000000001 0 0\n", "\n0.10000000000000001 0 1\n", 1),
+    }
+    for name, body in cases.items():
+        p = tmp_path / name
+        p.write_text(body)
+        with pytest.raises(ip.IpfemError):
+            ip.GmshMesh(str(p))
+    with pytest.raises(ip.IpfemError):
+        ip.GmshMesh(str(tmp_path / "missing.msh"))
+    g = ip.GmshMesh(str(good))
+    with pytest.raises(ip.IpfemError):
+        ip.GmshProblem(g, [(99, 6, -1.0)], 2000.0, 0.2, 5.0, 20.0)         # no entity with that tag
+    with pytest.raises(ip.IpfemError):
+        ip.GmshProblem(g, [("fixed_x", 6, -1.0)], 2000.0, 0.2, 5.0, 20.0)  # traction on points
+    with pytest.raises(ip.IpfemError):
+        ip.GmshProblem(g, [("bc_wellbore", 0, 1.0)], 2000.0, 0.2, 5.0, 20.0)  # non-zero Dirichlet
+    with pytest.raises(ip.IpfemError):
+        ip.GmshProblem(g, [("bc_wellbore", 2, 1.0)], 2000.0, 0.2, 5.0, 20.0)  # unsupported type
+
+
+def _oracle(pb, cohesion=5.0):
+    prm = po.default_params(4, E=2000.0, nu=0.2, cohesion=cohesion, phi_deg=20.0, psi_deg=20.0, sxx0=0.0,
+                            syy0=0.0, szz0=0.0, sxy0=0.0)
+    return po.OracleProblem(prm, mesh={k: pb.array(k) for k in ("node_xy", "connects", "fixed", "f0", "df")})
+
+
+@pytest.mark.parametrize("accel,variant,iters,tol_early,tol_late", [
+    (0, "CPU_NOT_MODIFIED", 12, 0.03, 0.006),
+    (1, "CPU_MODIFIED", 7, 0.01, 0.02),
+])
+def test_oracle_replays_the_logged_runs(tmp_path, accel, variant, iters, tol_early, tol_late):
+    """The oracle, on mesh 1 with the verification configuration, runs the
+    initial-stiffness iteration (plain and modified-Thomas) that produced the
+    reference's logs; the successive residual ratios agree with the logged
+    ones (0.5426 in the limit of the plain iteration) and the reference's
+    total residual reduction takes the same number of iterations."""
+    pb = _problem(_mesh(tmp_path, 1))
+    P = _oracle(pb)
+    u = np.zeros(P.neq)
+    ref = rh.reference_run(variant + "/order2-mesh1")
+    n_run = iters if accel == 0 else ref["iterations"]
+    st, log = P.solve_steps(u, 1, newton_rtol=1e-14, newton_max_it=n_run, cg_rtol=1e-11, tangent_mode=1, accel=accel)
+    ours = log[:, 2]
+    assert len(ours) == n_run
+    early, late, it_ours, it_ref = rh.compare(ours, ref["residue"][:n_run], n_run - 1)
+    print("%s: ratio differences %.4f / %.4f" % (variant, early, late))
+    assert early < tol_early and late < tol_late
+    if accel == 0:
+        assert abs(rh.ratios(ours)[-1] - rh.ratios(ref["residue"])[-1]) < 1e-3
+    else:
+        assert it_ours == it_ref == ref["iterations"]
