@@ -164,9 +164,10 @@ ipfem_status ipfem_set_newton_accel(ipfem_ctx *ctx, int mode);
  * (the shipped Solution(), main.cpp:229-233); 1 = initial stiffness, the
  * iteration of the reference's logged runs (the Results folders
  * CPU_NOT_MODIFIED, CPU_MODIFIED and their GPU and PZ twins: K assembled once,
- * then only AssembleResidual per iteration, main.cpp:219-228): the tangent of the first assembly after
- * ipfem_newton_begin is kept for every later linear solve, and later
- * assemblies compute the residual only. */
+ * then only AssembleResidual per iteration: main.cpp:218-222 with
+ * AssembleResidual in place of the Assemble of main.cpp:229-233): the
+ * tangent of the first assembly after ipfem_newton_begin is kept for every
+ * later linear solve, and later assemblies compute the residual only. */
 ipfem_status ipfem_set_newton_tangent(ipfem_ctx *ctx, int mode);
 
 /* Resumable form of the same loop: begin sets the options and the step range;

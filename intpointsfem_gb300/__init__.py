@@ -367,7 +367,8 @@ class ElastoPlasticIntPointsStructMatrix:
 
     def set_newton_tangent(self, mode):
         """0: Assemble(K, rhs) every iteration; 1: initial stiffness, the K of the
-        first assembly kept (the reference's logged runs, main.cpp:219-228)"""
+        first assembly kept (the reference's logged runs: main.cpp:218-222 with
+        AssembleResidual in place of the Assemble of main.cpp:229-233)"""
         self._check(lib().ipfem_set_newton_tangent(self._ctx, int(mode)))
 
     def set_precision(self, mode):

@@ -567,14 +567,9 @@ ipfem_status ipfem_solve(ipfem_ctx *c, const double *b, double *x, double rtol, 
     return st;
 }
 
-// One Newton iteration of the load-stepped solve (main.cpp:185-256): CG on the
-// current tangent, u += du, Assemble(K, rhs), convergence test; a load step
-// that converges (or reaches newton_max_it) is accepted (state commit,
-// main.cpp:487-522) and the next step's first assembly happens at the start
-// of the following iteration.
 // Assemble(K, rhs) of a Newton iteration, or Assemble(rhs) alone in the
 // initial-stiffness mode once a tangent exists (the reference's logged runs:
-// the linear solve reuses the K of the first assembly, main.cpp:219-228 with
+// the linear solve reuses the K of the first assembly, main.cpp:218-222 with
 // AssembleResidual per iteration)
 static void newton_assemble(ipfem_ctx *c, double *du)
 {
@@ -586,6 +581,11 @@ static void newton_assemble(ipfem_ctx *c, double *du)
     }
 }
 
+// One Newton iteration of the load-stepped solve (main.cpp:185-256): CG on the
+// current tangent, u += du, Assemble(K, rhs), convergence test; a load step
+// that converges (or reaches newton_max_it) is accepted (state commit,
+// main.cpp:487-522) and the next step's first assembly happens at the start
+// of the following iteration.
 static ipfem_status newton_advance(ipfem_ctx *c, int32_t n_iters, double *du, ipfem_solve_stats *st, double *log,
                                    int32_t log_cap, int32_t *nlog)
 {

@@ -728,7 +728,7 @@ void orc_solve_steps(orc_problem *p, const orc_solve_opts *o, int32_t step_begin
     memset(st, 0, sizeof *st);
     st->converged = 1;
     /* tangent_mode 1, the initial-stiffness iteration of the reference's
-     * logged runs (Solution(), main.cpp:219-228, with only the residual
+     * logged runs (the initial-stiffness branch of Solution(), main.cpp:218-222, with only the residual
      * assembled per iteration): K and the Jacobi diagonal of the first
      * assembly are kept, later assemblies compute the residual alone */
 #define ASSEMBLE_ITER()                                          \
