@@ -24,6 +24,18 @@ namespace ipfem {
 
 constexpr unsigned FULL = 0xffffffffu;
 
+// Programmatic dependent launch.  The CG iteration kernels are launched with
+// programmatic stream serialisation: a kernel's CTAs may become resident while
+// the previous kernel's last wave still runs.  Before pdl_wait() a kernel
+// reads only data that the previous kernel does not write (written two or
+// more launches earlier, or static); pdl_wait() returns once the previous
+// kernel has completed and its writes are visible.  Every kernel triggers its
+// dependents right after its own wait, so a kernel two launches back has
+// always completed when a kernel starts.  Without the launch attribute both
+// are no-ops.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_launch_dependents() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
 template <class T>
 __device__ __forceinline__ T warp_tree(T v)
 {
@@ -82,19 +94,43 @@ __device__ __forceinline__ T tree256_warp(const T *s)
 // Per-CTA partial sums of values the caller has staged (s[k][red_stage(t)]
 // for the node in slot t, zero for empty slots) and synchronised; written to
 // part[k][blockIdx].  Returns true in every thread of the CTA that finished
-// last (after a fence).
+// last (after a fence).  Value k is summed by warp (blockIdx + 2k) mod 4: a
+// warp-wide FP64 add occupies its SM sub-partition's FP64 unit for many
+// cycles, and warps w, w+4 of a CTA share a sub-partition, so rotating the
+// summing warp over the CTAs resident on an SM (and giving the two values of
+// one CTA different warps) spreads the trees over all four sub-partitions
+// instead of stacking every resident CTA's tree on one.
 template <class T, int NV>
 __device__ __forceinline__ bool block_partials_staged(const T (*s)[kRedStage], T *part, int64_t n_red,
                                                       unsigned *ticket)
 {
+    static_assert(NV == 1 || NV == 2, "one or two values");
     __shared__ int s_last;
-    if (threadIdx.x < 32) {
-        T o[NV];
+    __shared__ T s_res[NV];
+    const int w = threadIdx.x >> 5;
+    const int w0 = (int)(blockIdx.x & 3u);
+    // one thread writes every partial, fences and takes the ticket
+    if (NV == 1) {
+        if (w == w0) {
+            const T o = tree256_warp<T>(s[0]);
+            if ((threadIdx.x & 31) == 0) {
+                part[blockIdx.x] = o;
+                __threadfence();
+                const unsigned t = atomicAdd(ticket, 1u);
+                s_last = (t == gridDim.x - 1);
+            }
+        }
+    } else {
 #pragma unroll
-        for (int k = 0; k < NV; k++) o[k] = tree256_warp<T>(s[k]);
+        for (int k = 0; k < NV; k++)
+            if (w == ((w0 + 2 * k) & 3)) {
+                const T o = tree256_warp<T>(s[k]);
+                if ((threadIdx.x & 31) == 0) s_res[k] = o;
+            }
+        __syncthreads();
         if (threadIdx.x == 0) {
 #pragma unroll
-            for (int k = 0; k < NV; k++) part[k * n_red + blockIdx.x] = o[k];
+            for (int k = 0; k < NV; k++) part[k * n_red + blockIdx.x] = s_res[k];
             __threadfence();
             const unsigned t = atomicAdd(ticket, 1u);
             s_last = (t == gridDim.x - 1);
@@ -231,6 +267,8 @@ __global__ void __launch_bounds__(kRedBlock) k_cg_spmv(int32_t n_nodes, const in
         base = __ldg(&slice_base[t >> 5]) + (t & 31);
         len = __ldg(&rowlen[t]);
     }
+    pdl_wait();
+    pdl_launch_dependents();
     if (*reinterpret_cast<volatile int *>(&sc->done)) return;
     T v = T(0);
     if (t < n_nodes) {
@@ -285,15 +323,17 @@ __global__ void __launch_bounds__(kRedBlock) k_cg_update(int32_t n_nodes, const 
 {
     typedef typename Vec2<T>::type V;
     const int32_t i = blockIdx.x * kRedBlock + threadIdx.x;
-    // operands first, then the flag and alpha, so that the latencies overlap
+    // p, dinv, x and r (not written by the SpMV) before the wait, q after it
     V pp, qq, di, xx, rr;
     if (i < n_nodes) {
         pp = reinterpret_cast<const V *>(p)[i];
-        qq = reinterpret_cast<const V *>(q)[i];
         di = reinterpret_cast<const V *>(dinv)[i];
         xx = reinterpret_cast<V *>(x)[i];
         rr = reinterpret_cast<V *>(r)[i];
     }
+    pdl_wait();
+    pdl_launch_dependents();
+    if (i < n_nodes) qq = reinterpret_cast<const V *>(q)[i];
     if (*reinterpret_cast<volatile int *>(&sc->done)) return;
     const T alpha = *reinterpret_cast<volatile T *>(&sc->alpha);
     T v[2] = {T(0), T(0)};
@@ -330,20 +370,36 @@ __global__ void __launch_bounds__(kRedBlock) k_cg_update(int32_t n_nodes, const 
     }
 }
 
+// p = z + beta p, kPupNodes nodes per thread (strided by the CTA size) so that
+// each thread has several loads in flight: the kernel moves 48 bytes per node
+// and is bound by memory latency, not bandwidth, at one node per thread
+constexpr int kPupNodes = 4;
+
 template <class T>
 __global__ void __launch_bounds__(kRedBlock) k_cg_pupdate(int32_t n_nodes, const T *__restrict__ z,
                                                           T *__restrict__ p, const CGScalarsT<T> *sc)
 {
     typedef typename Vec2<T>::type V;
-    const int32_t i = blockIdx.x * kRedBlock + threadIdx.x;
-    if (i >= n_nodes) return;
-    const V zz = reinterpret_cast<const V *>(z)[i];
-    V pp = reinterpret_cast<V *>(p)[i];
+    const int32_t i0 = blockIdx.x * (kRedBlock * kPupNodes) + threadIdx.x;
+    // p (not written by the update) before the wait, z after it
+    V pp[kPupNodes], zz[kPupNodes];
+#pragma unroll
+    for (int j = 0; j < kPupNodes; j++)
+        if (i0 + j * kRedBlock < n_nodes) pp[j] = reinterpret_cast<V *>(p)[i0 + j * kRedBlock];
+    pdl_wait();
+    pdl_launch_dependents();
+#pragma unroll
+    for (int j = 0; j < kPupNodes; j++)
+        if (i0 + j * kRedBlock < n_nodes) zz[j] = reinterpret_cast<const V *>(z)[i0 + j * kRedBlock];
     if (*reinterpret_cast<const volatile int *>(&sc->done)) return;
     const T beta = *reinterpret_cast<const volatile T *>(&sc->beta);
-    pp.x = fma(beta, pp.x, zz.x);
-    pp.y = fma(beta, pp.y, zz.y);
-    reinterpret_cast<V *>(p)[i] = pp;
+#pragma unroll
+    for (int j = 0; j < kPupNodes; j++)
+        if (i0 + j * kRedBlock < n_nodes) {
+            pp[j].x = fma(beta, pp[j].x, zz[j].x);
+            pp[j].y = fma(beta, pp[j].y, zz[j].y);
+            reinterpret_cast<V *>(p)[i0 + j * kRedBlock] = pp[j];
+        }
 }
 
 __global__ void __launch_bounds__(kRedBlock) k_dot(int32_t n_nodes, const double *__restrict__ a,
@@ -419,27 +475,47 @@ void launch_cg_init(ipfem_ctx *c, const double *d_b, double rtol, int max_it)
                                                                   c->d_counters + 0, c->d_sc, rtol, max_it);
 }
 
+static unsigned grid_pupdate(const ipfem_ctx *c)
+{
+    return (unsigned)((c->s.n_nodes + kRedBlock * kPupNodes - 1) / (kRedBlock * kPupNodes));
+}
+
+// launch with programmatic stream serialisation (see pdl_wait); the kernels
+// of one CG iteration are launched this way, also inside graph capture
+template <typename... KArgs, typename... Args>
+static void launch_pdl(void (*kern)(KArgs...), unsigned grid, cudaStream_t stream, Args... args)
+{
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(kRedBlock);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = stream;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    cudaLaunchKernelEx(&cfg, kern, static_cast<KArgs>(args)...);
+}
+
 template <class T>
 void launch_spmv(ipfem_ctx *c, const SellDev &L, const T *K, const T *p, T *q, T *part, unsigned *ticket,
                  CGScalarsT<T> *sc)
 {
-    if (L.sorted)
-        k_cg_spmv<T, true><<<grid_nodes(c), kRedBlock, 0, c->stream>>>(
-            c->s.n_nodes, L.slice_base, L.rowlen, L.sell_node, L.sell_col, K, c->d_fixed, p, q, part, c->n_red,
-            ticket, sc);
-    else
-        k_cg_spmv<T, false><<<grid_nodes(c), kRedBlock, 0, c->stream>>>(
-            c->s.n_nodes, L.slice_base, L.rowlen, L.sell_node, L.sell_col, K, c->d_fixed, p, q, part, c->n_red,
-            ticket, sc);
+    launch_pdl(L.sorted ? k_cg_spmv<T, true> : k_cg_spmv<T, false>, grid_nodes(c), c->stream, c->s.n_nodes,
+               (const int64_t *)L.slice_base, (const int32_t *)L.rowlen, (const int32_t *)L.sell_node,
+               (const int32_t *)L.sell_col, (const T *)K, (const uint8_t *)c->d_fixed, (const T *)p, q, part,
+               c->n_red, ticket, sc);
 }
 
 void launch_cg_iteration(ipfem_ctx *c)
 {
     const unsigned g = grid_nodes(c);
     launch_spmv<double>(c, c->dsell, c->d_K, c->d_p, c->d_q, c->d_part, c->d_counters + 1, c->d_sc);
-    k_cg_update<double><<<g, kRedBlock, 0, c->stream>>>(c->s.n_nodes, c->d_p, c->d_q, c->d_dinv, c->d_x, c->d_r,
-                                                        c->d_z, c->d_part, c->n_red, c->d_counters + 2, c->d_sc);
-    k_cg_pupdate<double><<<g, kRedBlock, 0, c->stream>>>(c->s.n_nodes, c->d_z, c->d_p, c->d_sc);
+    launch_pdl(k_cg_update<double>, g, c->stream, c->s.n_nodes, (const double *)c->d_p, (const double *)c->d_q,
+               (const double *)c->d_dinv, c->d_x, c->d_r, c->d_z, c->d_part, c->n_red, c->d_counters + 2, c->d_sc);
+    launch_pdl(k_cg_pupdate<double>, grid_pupdate(c), c->stream, c->s.n_nodes, (const double *)c->d_z, c->d_p,
+               (const CGScalarsT<double> *)c->d_sc);
 }
 
 void launch_cg_spmv_only(ipfem_ctx *c)
@@ -460,9 +536,10 @@ void launch_cg32_iteration(ipfem_ctx *c)
     MixedBuffers &m = c->mx;
     const unsigned g = grid_nodes(c);
     launch_spmv<float>(c, m.dsell, m.K, m.p, m.q, m.part, c->d_counters + 5, m.sc);
-    k_cg_update<float><<<g, kRedBlock, 0, c->stream>>>(c->s.n_nodes, m.p, m.q, m.dinv, m.x, m.r, m.z, m.part,
-                                                       c->n_red, c->d_counters + 6, m.sc);
-    k_cg_pupdate<float><<<g, kRedBlock, 0, c->stream>>>(c->s.n_nodes, m.z, m.p, m.sc);
+    launch_pdl(k_cg_update<float>, g, c->stream, c->s.n_nodes, (const float *)m.p, (const float *)m.q,
+               (const float *)m.dinv, m.x, m.r, m.z, m.part, c->n_red, c->d_counters + 6, m.sc);
+    launch_pdl(k_cg_pupdate<float>, grid_pupdate(c), c->stream, c->s.n_nodes, (const float *)m.z, m.p,
+               (const CGScalarsT<float> *)m.sc);
 }
 
 void launch_cg32_spmv_only(ipfem_ctx *c)
@@ -474,7 +551,7 @@ void launch_cg32_spmv_only(ipfem_ctx *c)
 void launch_cg32_pupdate_only(ipfem_ctx *c)
 {
     MixedBuffers &m = c->mx;
-    k_cg_pupdate<float><<<grid_nodes(c), kRedBlock, 0, c->stream>>>(c->s.n_nodes, m.z, m.p, m.sc);
+    k_cg_pupdate<float><<<grid_pupdate(c), kRedBlock, 0, c->stream>>>(c->s.n_nodes, m.z, m.p, m.sc);
 }
 
 void launch_add_scaled32(ipfem_ctx *c, double *d_u, const float *x, double scale)
