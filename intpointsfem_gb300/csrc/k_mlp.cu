@@ -31,6 +31,7 @@
 #include <cmath>
 
 #include "ipfem_internal.h"
+#include "pdl.cuh"
 
 namespace ipfem {
 
@@ -281,12 +282,17 @@ __device__ __forceinline__ float4 load_g(const float4 *__restrict__ g, int64_t i
     return __ldg(&g[idx]);
 }
 
-__device__ __forceinline__ float4 load_g(const uint2 *__restrict__ g, int64_t idx)
+// four BF16 values (one 2x2 factor block) widened to FP32
+__device__ __forceinline__ float4 bf16x4(uint2 u)
 {
-    const uint2 u = __ldg(&g[idx]);
     const float2 a = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162 *>(&u.x));
     const float2 b = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162 *>(&u.y));
     return make_float4(a.x, a.y, b.x, b.y);
+}
+
+__device__ __forceinline__ float4 load_g(const uint2 *__restrict__ g, int64_t idx)
+{
+    return bf16x4(__ldg(&g[idx]));
 }
 
 // G[k][i] (float4, row-major 2x2, k = 0..4) from the network output O[n][20],
@@ -482,13 +488,19 @@ __global__ void __launch_bounds__(256) k_tri_precond(int32_t n, GridInfo G, cons
                                                      float *__restrict__ z, float *part, int64_t n_part,
                                                      unsigned *ticket, CGScalarsT<float> *sc)
 {
-    if (*reinterpret_cast<volatile int *>(&sc->done)) return;
     const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    // r_old (not written by the update pass) before the wait; y, r and the
+    // flag after it
+    float2 ro = make_float2(0.f, 0.f);
+    if (i < n) ro = reinterpret_cast<const float2 *>(r_old)[i];
+    pdl_wait();
+    pdl_launch_dependents();
+    if (*reinterpret_cast<volatile int *>(&sc->done)) return;
     float v[2] = {0.f, 0.f};
     if (i < n) {
         const float2 zz = trit_mul(i, n, G, Gm, dinv, y);
         reinterpret_cast<float2 *>(z)[i] = zz;
-        const float2 rr = reinterpret_cast<const float2 *>(r)[i], ro = reinterpret_cast<const float2 *>(r_old)[i];
+        const float2 rr = reinterpret_cast<const float2 *>(r)[i];
         v[0] = fmaf(rr.y, zz.y, rr.x * zz.x);
         v[1] = fmaf(ro.y, zz.y, ro.x * zz.x);
     }
@@ -528,13 +540,21 @@ __global__ void __launch_bounds__(256) k_fcg_spmv(int32_t n, const int64_t *__re
                                                   float2 *__restrict__ p_new, float2 *__restrict__ q, float *part,
                                                   int64_t n_part, unsigned *ticket, CGScalarsT<float> *sc)
 {
+    const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    // row metadata before the wait; z, beta and the flag (written by the
+    // preconditioner pass) after it
+    int64_t base = 0;
+    int len = 0;
+    if (i < n) {
+        base = __ldg(&slice_base[i >> 5]) + (i & 31);
+        len = __ldg(&rowlen[i]);
+    }
+    pdl_wait();
+    pdl_launch_dependents();
     if (*reinterpret_cast<volatile int *>(&sc->done)) return;
     const float beta = *reinterpret_cast<volatile float *>(&sc->beta);
-    const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     float v[1] = {0.f};
     if (i < n) {
-        const int64_t base = __ldg(&slice_base[i >> 5]) + (i & 31);
-        const int len = __ldg(&rowlen[i]);
         float y0 = 0.f, y1 = 0.f;
 #pragma unroll 4
         for (int k = 0; k < len; k++) {
@@ -574,7 +594,7 @@ __global__ void __launch_bounds__(256) k_fcg_spmv(int32_t n, const int64_t *__re
 // x += alpha p, r_new = r_old - alpha q (the owner stores it, the factor
 // pass forms it for its neighbours), y = G (sigma * r_new); partials of
 // r_new.r_new; last CTA: convergence, stagnation and iteration limit
-__global__ void __launch_bounds__(256) k_fcg_update_first(int32_t n, GridInfo G, const uint2 *__restrict__ Gm,
+__global__ void __launch_bounds__(256, 8) k_fcg_update_first(int32_t n, GridInfo G, const uint2 *__restrict__ Gm,
                                                           const float2 *__restrict__ dinv,
                                                           const float2 *__restrict__ p, const float2 *__restrict__ q,
                                                           float2 *__restrict__ x, const float2 *__restrict__ r_old,
@@ -582,30 +602,42 @@ __global__ void __launch_bounds__(256) k_fcg_update_first(int32_t n, GridInfo G,
                                                           float *part, int64_t n_part, unsigned *ticket,
                                                           CGScalarsT<float> *sc, int stall_window)
 {
+    const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    // x and r_old (not written by the SpMV) before the wait; p, q, alpha and
+    // the flag after it
+    float2 xx = make_float2(0.f, 0.f), ro[NTRI];
+    int32_t jn[NTRI];
+    if (i < n) {
+        xx = x[i];
+#pragma unroll
+        for (int k = 0; k < NTRI; k++) {
+            jn[k] = patch_nbr(i, k, G);
+            if (jn[k] >= 0) ro[k] = __ldg(&r_old[jn[k]]);
+        }
+    }
+    pdl_wait();
+    pdl_launch_dependents();
     if (*reinterpret_cast<volatile int *>(&sc->done)) return;
     const float alpha = *reinterpret_cast<volatile float *>(&sc->alpha);
-    const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     float v[1] = {0.f};
     if (i < n) {
         const float2 pp = p[i];
-        float2 xx = x[i];
         xx.x = fmaf(alpha, pp.x, xx.x);
         xx.y = fmaf(alpha, pp.y, xx.y);
         x[i] = xx;
         float2 acc = make_float2(0.f, 0.f);
 #pragma unroll
         for (int k = 0; k < NTRI; k++) {
-            const int32_t j = patch_nbr(i, k, G);
-            if (j < 0) continue;
-            const float2 ro = __ldg(&r_old[j]), qq = __ldg(&q[j]);
-            const float2 rn = make_float2(fmaf(-alpha, qq.x, ro.x), fmaf(-alpha, qq.y, ro.y));
+            if (jn[k] < 0) continue;
+            const float2 qq = __ldg(&q[jn[k]]);
+            const float2 rn = make_float2(fmaf(-alpha, qq.x, ro[k].x), fmaf(-alpha, qq.y, ro[k].y));
             if (k == 4) {
                 r_new[i] = rn;
                 v[0] = fmaf(rn.y, rn.y, rn.x * rn.x);
             }
             const float4 m = load_g(Gm, (int64_t)k * n + i);
-            const float2 s = sqrt2(__ldg(&dinv[j]));
-            const float vx = s.x * rn.x, vy = s.y * rn.y;
+            const float2 sg = sqrt2(__ldg(&dinv[jn[k]]));
+            const float vx = sg.x * rn.x, vy = sg.y * rn.y;
             acc.x = fmaf(m.x, vx, fmaf(m.y, vy, acc.x));
             acc.y = fmaf(m.z, vx, fmaf(m.w, vy, acc.y));
         }
@@ -1002,22 +1034,18 @@ void launch_fcg_iteration(ipfem_ctx *c, int par)
     float2 *R[2] = {reinterpret_cast<float2 *>(m.r), reinterpret_cast<float2 *>(l.r_old)};
     const float2 *d2 = reinterpret_cast<const float2 *>(m.dinv);
     float *part = m.part;
-    k_fcg_spmv<<<fcg_grid(c), 256, 0, c->stream>>>(n, L.slice_base, L.rowlen, L.sell_col,
-                                                   reinterpret_cast<const float4 *>(m.K), c->d_fixed,
-                                                   reinterpret_cast<const float2 *>(m.z), P[par], P[1 - par],
-                                                   reinterpret_cast<float2 *>(m.q), part, (int64_t)fcg_grid(c),
-                                                   c->d_counters + 5, m.sc);
-    k_fcg_update_first<<<fcg_grid(c), 256, 0, c->stream>>>(n, G, reinterpret_cast<const uint2 *>(l.Gh), d2,
-                                                           P[1 - par], reinterpret_cast<const float2 *>(m.q),
-                                                           reinterpret_cast<float2 *>(m.x), R[par], R[1 - par],
-                                                           reinterpret_cast<float2 *>(l.y), part, (int64_t)fcg_grid(c),
-                                                           c->d_counters + 6, m.sc, stall_window(c));
+    launch_pdl(k_fcg_spmv, fcg_grid(c), 256, c->stream, n, (const int64_t *)L.slice_base,
+               (const int32_t *)L.rowlen, (const int32_t *)L.sell_col, reinterpret_cast<const float4 *>(m.K),
+               (const uint8_t *)c->d_fixed, reinterpret_cast<const float2 *>(m.z), (const float2 *)P[par],
+               P[1 - par], reinterpret_cast<float2 *>(m.q), part, (int64_t)fcg_grid(c), c->d_counters + 5, m.sc);
+    launch_pdl(k_fcg_update_first, fcg_grid(c), 256, c->stream, n, G, reinterpret_cast<const uint2 *>(l.Gh), d2,
+               (const float2 *)P[1 - par], reinterpret_cast<const float2 *>(m.q), reinterpret_cast<float2 *>(m.x),
+               (const float2 *)R[par], R[1 - par], reinterpret_cast<float2 *>(l.y), part, (int64_t)fcg_grid(c),
+               c->d_counters + 6, m.sc, stall_window(c));
     float *part2 = reinterpret_cast<float *>(c->d_part);
-    k_tri_precond<<<fcg_grid(c), 256, 0, c->stream>>>(n, G, reinterpret_cast<const uint2 *>(l.Gh), d2,
-                                                      reinterpret_cast<const float2 *>(l.y),
-                                                      reinterpret_cast<const float *>(R[1 - par]),
-                                                      reinterpret_cast<const float *>(R[par]), m.z, part2,
-                                                      (int64_t)fcg_grid(c), c->d_counters + 7, m.sc);
+    launch_pdl(k_tri_precond, fcg_grid(c), 256, c->stream, n, G, reinterpret_cast<const uint2 *>(l.Gh), d2,
+               reinterpret_cast<const float2 *>(l.y), reinterpret_cast<const float *>(R[1 - par]),
+               reinterpret_cast<const float *>(R[par]), m.z, part2, (int64_t)fcg_grid(c), c->d_counters + 7, m.sc);
 }
 
 // ------------------------------------------------------------ training pass

@@ -19,22 +19,12 @@
 #include <mutex>
 
 #include "ipfem_internal.h"
+#include "pdl.cuh"
 
 namespace ipfem {
 
 constexpr unsigned FULL = 0xffffffffu;
 
-// Programmatic dependent launch.  The CG iteration kernels are launched with
-// programmatic stream serialisation: a kernel's CTAs may become resident while
-// the previous kernel's last wave still runs.  Before pdl_wait() a kernel
-// reads only data that the previous kernel does not write (written two or
-// more launches earlier, or static); pdl_wait() returns once the previous
-// kernel has completed and its writes are visible.  Every kernel triggers its
-// dependents right after its own wait, so a kernel two launches back has
-// always completed when a kernel starts.  Without the launch attribute both
-// are no-ops.
-__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
-__device__ __forceinline__ void pdl_launch_dependents() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
 
 template <class T>
 __device__ __forceinline__ T warp_tree(T v)
@@ -480,30 +470,12 @@ static unsigned grid_pupdate(const ipfem_ctx *c)
     return (unsigned)((c->s.n_nodes + kRedBlock * kPupNodes - 1) / (kRedBlock * kPupNodes));
 }
 
-// launch with programmatic stream serialisation (see pdl_wait); the kernels
-// of one CG iteration are launched this way, also inside graph capture
-template <typename... KArgs, typename... Args>
-static void launch_pdl(void (*kern)(KArgs...), unsigned grid, cudaStream_t stream, Args... args)
-{
-    cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3(grid);
-    cfg.blockDim = dim3(kRedBlock);
-    cfg.dynamicSmemBytes = 0;
-    cfg.stream = stream;
-    cudaLaunchAttribute at[1];
-    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-    at[0].val.programmaticStreamSerializationAllowed = 1;
-    cfg.attrs = at;
-    cfg.numAttrs = 1;
-    cudaLaunchKernelEx(&cfg, kern, static_cast<KArgs>(args)...);
-}
-
 template <class T>
 void launch_spmv(ipfem_ctx *c, const SellDev &L, const T *K, const T *p, T *q, T *part, unsigned *ticket,
                  CGScalarsT<T> *sc)
 {
-    launch_pdl(L.sorted ? k_cg_spmv<T, true> : k_cg_spmv<T, false>, grid_nodes(c), c->stream, c->s.n_nodes,
-               (const int64_t *)L.slice_base, (const int32_t *)L.rowlen, (const int32_t *)L.sell_node,
+    launch_pdl(L.sorted ? k_cg_spmv<T, true> : k_cg_spmv<T, false>, grid_nodes(c), kRedBlock, c->stream,
+               c->s.n_nodes, (const int64_t *)L.slice_base, (const int32_t *)L.rowlen, (const int32_t *)L.sell_node,
                (const int32_t *)L.sell_col, (const T *)K, (const uint8_t *)c->d_fixed, (const T *)p, q, part,
                c->n_red, ticket, sc);
 }
@@ -512,10 +484,11 @@ void launch_cg_iteration(ipfem_ctx *c)
 {
     const unsigned g = grid_nodes(c);
     launch_spmv<double>(c, c->dsell, c->d_K, c->d_p, c->d_q, c->d_part, c->d_counters + 1, c->d_sc);
-    launch_pdl(k_cg_update<double>, g, c->stream, c->s.n_nodes, (const double *)c->d_p, (const double *)c->d_q,
-               (const double *)c->d_dinv, c->d_x, c->d_r, c->d_z, c->d_part, c->n_red, c->d_counters + 2, c->d_sc);
-    launch_pdl(k_cg_pupdate<double>, grid_pupdate(c), c->stream, c->s.n_nodes, (const double *)c->d_z, c->d_p,
-               (const CGScalarsT<double> *)c->d_sc);
+    launch_pdl(k_cg_update<double>, g, kRedBlock, c->stream, c->s.n_nodes, (const double *)c->d_p,
+               (const double *)c->d_q, (const double *)c->d_dinv, c->d_x, c->d_r, c->d_z, c->d_part, c->n_red,
+               c->d_counters + 2, c->d_sc);
+    launch_pdl(k_cg_pupdate<double>, grid_pupdate(c), kRedBlock, c->stream, c->s.n_nodes,
+               (const double *)c->d_z, c->d_p, (const CGScalarsT<double> *)c->d_sc);
 }
 
 void launch_cg_spmv_only(ipfem_ctx *c)
@@ -536,10 +509,11 @@ void launch_cg32_iteration(ipfem_ctx *c)
     MixedBuffers &m = c->mx;
     const unsigned g = grid_nodes(c);
     launch_spmv<float>(c, m.dsell, m.K, m.p, m.q, m.part, c->d_counters + 5, m.sc);
-    launch_pdl(k_cg_update<float>, g, c->stream, c->s.n_nodes, (const float *)m.p, (const float *)m.q,
-               (const float *)m.dinv, m.x, m.r, m.z, m.part, c->n_red, c->d_counters + 6, m.sc);
-    launch_pdl(k_cg_pupdate<float>, grid_pupdate(c), c->stream, c->s.n_nodes, (const float *)m.z, m.p,
-               (const CGScalarsT<float> *)m.sc);
+    launch_pdl(k_cg_update<float>, g, kRedBlock, c->stream, c->s.n_nodes, (const float *)m.p,
+               (const float *)m.q, (const float *)m.dinv, m.x, m.r, m.z, m.part, c->n_red, c->d_counters + 6,
+               m.sc);
+    launch_pdl(k_cg_pupdate<float>, grid_pupdate(c), kRedBlock, c->stream, c->s.n_nodes, (const float *)m.z,
+               m.p, (const CGScalarsT<float> *)m.sc);
 }
 
 void launch_cg32_spmv_only(ipfem_ctx *c)
