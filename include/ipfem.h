@@ -42,9 +42,14 @@ enum { IPFEM_HOST = 0, IPFEM_DEVICE = 1 };
 enum { IPFEM_PLAIN_FP64 = 0, IPFEM_MIXED = 1 };
 enum { IPFEM_PREC_JACOBI = 0, IPFEM_PREC_MLP = 1 };
 
-#define IPFEM_NPTS 9     /* integration points per element */
-#define IPFEM_NNODE 9    /* connects per element */
-#define IPFEM_NDOF 18    /* dofs per element */
+/* Element order p = 1, 2 or 3 (the reference's O_LINEAR, O_QUADRATIC and
+ * O_CUBIC builds, KernelsMatrixAssemble.h:3-12): (p+1)^2 connects and
+ * (p+1)^2 Gauss points per quadrilateral, 2 (p+1)^2 dofs.  The sizes below
+ * are those of order 2, the default. */
+#define IPFEM_NPTS 9     /* integration points per element (order 2) */
+#define IPFEM_NNODE 9    /* connects per element (order 2) */
+#define IPFEM_NDOF 18    /* dofs per element (order 2) */
+#define IPFEM_MAX_ORDER 3
 
 typedef struct ipfem_ctx ipfem_ctx;
 
@@ -52,21 +57,25 @@ typedef struct ipfem_ctx ipfem_ctx;
 /* Host description of the integration-point data that the reference builds
  * in TPZElastoPlasticIntPointsStructMatrix::SetUpDataStructure
  * (TPZElastoPlasticIntPointsStructMatrix.cpp:156-173).  All arrays are read
- * during ipfem_create only. */
+ * during ipfem_create only.  nn = nq = (order+1)^2 connects and points per
+ * element. */
 typedef struct {
     int32_t n_elements;
     int32_t n_nodes;          /* connects; equations = 2*n_nodes, dof = 2*node+comp */
-    const int32_t *connects;  /* [n_elements*9] connect order of the element */
+    const int32_t *connects;  /* [n_elements*nn] connect order of the element: 4 vertices, the
+                                 order-1 nodes of each edge in traversal order (edges v0v1, v1v2,
+                                 v2v3, v3v0), interior nodes row by row */
     /* Element blocks, one of the two forms:
-     *  dphi:          [n_elements*9*2*9] d(phi_n)/d(x_d) at point q, index ((e*9+q)*2+d)*9+n
-     *  block_storage: [n_elements*27*18] the reference's fStorage, row-major
+     *  dphi:          [n_elements*nq*2*nn] d(phi_n)/d(x_d) at point q, index ((e*nq+q)*2+d)*nn+n
+     *  block_storage: [n_elements*(3*nq)*(2*nn)] the reference's fStorage, row-major
      *                 (3*npts) x (2*nshape) (TPZNumericalIntegrator.cpp:371-386) */
     const double *dphi;
     const double *block_storage;
-    const double *weight;     /* [n_elements*9] w*|detJ| (TPZNumericalIntegrator.cpp:425) */
+    const double *weight;     /* [n_elements*nq] w*|detJ| (TPZNumericalIntegrator.cpp:425) */
     const uint8_t *fixed;     /* [2*n_nodes] 1 = Dirichlet dof (may be NULL) */
     const double *f0;         /* [2*n_nodes] external load at load factor 0 (may be NULL) */
     const double *df;         /* [2*n_nodes] external load per unit load factor (may be NULL) */
+    int32_t order;            /* element order 1, 2 or 3 (0 = 2) */
 } ipfem_mesh;
 
 /* Mohr-Coulomb / elastic material (TPZPlasticStepPV<TPZYCMohrCoulombPV,
@@ -222,8 +231,8 @@ ipfem_status ipfem_set_state(ipfem_ctx *ctx, int field, const double *in);
 
 /* Setup arrays computed by the library (for verification):
  * field 0 element colour [n_elements] int32, 1 number of colours (int32),
- * 2 dof indexes [n_elements*18] int32 (fDoFIndexes),
- * 3 dphi [n_elements*162] double, 4 weights [n_ip] double. */
+ * 2 dof indexes [n_elements*2*nn] int32 (fDoFIndexes),
+ * 3 dphi [n_elements*nq*2*nn] double, 4 weights [n_ip] double. */
 ipfem_status ipfem_get_setup(ipfem_ctx *ctx, int field, void *out);
 
 /* Greedy element colouring of TPZNumericalIntegrator::SetUpColoredIndexes
@@ -232,6 +241,9 @@ ipfem_status ipfem_get_setup(ipfem_ctx *ctx, int field, void *out);
  * none of its 9 connects is marked in this pass.  Returns the number of
  * colours, or -1 on bad arguments. */
 int32_t ipfem_color_elements(int32_t n_elements, int32_t n_nodes, const int32_t *connects, int32_t *el_color);
+/* the same for nn connects per element */
+int32_t ipfem_color_elements_nn(int32_t n_elements, int32_t n_nodes, int32_t nn, const int32_t *connects,
+                                int32_t *el_color);
 
 /* ------------------------------------------------- learned preconditioner */
 /* None of these has a counterpart in the reference.  A per-node MLP
@@ -353,25 +365,27 @@ void ipfem_gmsh_free(ipfem_gmsh *g);
  *   3  directional Dirichlet: u_k = 0 for every k with val[k] != 0
  *   6  normal stress: traction val[0] * n, n the outward unit normal
  * The Dirichlet types act on every node of the tagged entities (for a line,
- * its two vertices and its midpoint connect). */
+ * its two vertices and its edge connects). */
 typedef struct {
     int32_t phys;
     int32_t type;
     double val[2];
 } ipfem_bc;
 
-/* Order-2 problem on a Gmsh mesh (CmeshElastoplasticity with p_order 2,
- * main.cpp:546-601): every quadrilateral whose physical tag is domain_phys
- * (every quadrilateral if domain_phys < 0) becomes a 9-connect element, its
- * edge connects at the straight-edge midpoints and its centre connect at the
- * bilinear centre (the geometric elements are linear).  Connects are numbered
+/* Problem of order 1, 2 or 3 on a Gmsh mesh (CmeshElastoplasticity with
+ * p_order = order, main.cpp:546-601): every quadrilateral whose physical tag
+ * is domain_phys (every quadrilateral if domain_phys < 0) becomes an element
+ * of (order+1)^2 connects, its edge connects equally spaced on the straight
+ * edges and its interior connects on the bilinear map (the geometric elements
+ * are linear); a shared edge's connects are numbered from its lower-numbered
+ * vertex, so that both elements use the same ones.  Connects are numbered
  * in order of first use by the elements, so that elements close in file
  * order share nearby rows.  Loads go into df (f0 = 0): load factor 1 applies
  * them in full.  mat supplies E, nu, cohesion, phi, psi and sigma0
  * (el_cohesion and el_phi must be NULL).  The result has the layout of the
  * wellbore provider's and is released with ipfem_wellbore_free. */
-ipfem_status ipfem_gmsh_problem(const ipfem_gmsh *g, int32_t domain_phys, const ipfem_bc *bcs, int32_t n_bc,
-                                const ipfem_material *mat, ipfem_wellbore **out);
+ipfem_status ipfem_gmsh_problem(const ipfem_gmsh *g, int32_t order, int32_t domain_phys, const ipfem_bc *bcs,
+                                int32_t n_bc, const ipfem_material *mat, ipfem_wellbore **out);
 
 #ifdef __cplusplus
 }

@@ -36,7 +36,8 @@ class IpfemError(RuntimeError):
 
 class Mesh(C.Structure):
     _fields_ = [("n_elements", C.c_int32), ("n_nodes", C.c_int32), ("connects", _ip), ("dphi", _dp),
-                ("block_storage", _dp), ("weight", _dp), ("fixed", _bp), ("f0", _dp), ("df", _dp)]
+                ("block_storage", _dp), ("weight", _dp), ("fixed", _bp), ("f0", _dp), ("df", _dp),
+                ("order", C.c_int32)]
 
 
 class Material(C.Structure):
@@ -136,13 +137,14 @@ def lib():
             "ipfem_set_state": (S, [P, S, _dp]),
             "ipfem_get_setup": (S, [P, S, P]),
             "ipfem_color_elements": (C.c_int32, [C.c_int32, C.c_int32, _ip, _ip]),
+            "ipfem_color_elements_nn": (C.c_int32, [C.c_int32, C.c_int32, C.c_int32, _ip, _ip]),
             "ipfem_wellbore_default": (None, [C.POINTER(WellboreParams), C.c_int32]),
             "ipfem_wellbore_build": (S, [C.POINTER(WellboreParams), C.POINTER(C.POINTER(Wellbore))]),
             "ipfem_wellbore_free": (None, [C.POINTER(Wellbore)]),
             "ipfem_set_newton_tangent": (S, [P, S]),
             "ipfem_gmsh_read": (S, [C.c_char_p, C.POINTER(C.POINTER(GmshData))]),
             "ipfem_gmsh_free": (None, [C.POINTER(GmshData)]),
-            "ipfem_gmsh_problem": (S, [C.POINTER(GmshData), C.c_int32, C.POINTER(BC), C.c_int32,
+            "ipfem_gmsh_problem": (S, [C.POINTER(GmshData), C.c_int32, C.c_int32, C.POINTER(BC), C.c_int32,
                                        C.POINTER(Material), C.POINTER(C.POINTER(Wellbore))]),
         }
         for name, (res, args) in sig.items():
@@ -167,11 +169,12 @@ def _np_ptr(a, t):
     return a.ctypes.data_as(t)
 
 
-def color_elements(connects, n_nodes):
-    """host greedy colouring (SetUpColoredIndexes); returns (n_colors, colours)"""
+def color_elements(connects, n_nodes, nn=9):
+    """host greedy colouring (SetUpColoredIndexes) of elements with nn connects;
+    returns (n_colors, colours)"""
     connects = np.ascontiguousarray(connects, dtype=np.int32)
-    col = np.zeros(connects.size // 9, np.int32)
-    nc = lib().ipfem_color_elements(col.size, int(n_nodes), _np_ptr(connects, _ip), _np_ptr(col, _ip))
+    col = np.zeros(connects.size // nn, np.int32)
+    nc = lib().ipfem_color_elements_nn(col.size, int(n_nodes), int(nn), _np_ptr(connects, _ip), _np_ptr(col, _ip))
     if nc < 0:
         raise IpfemError(5, "bad colouring arguments")
     return int(nc), col
@@ -198,6 +201,7 @@ class WellboreMesh:
         self.n_el = w.mesh.n_elements
         self.n_nodes = w.mesh.n_nodes
         self.neq = 2 * self.n_nodes
+        self.order = 2
 
     @property
     def mesh(self):
@@ -209,8 +213,9 @@ class WellboreMesh:
 
     def array(self, name):
         w = self._w.contents
-        n = {"node_xy": 2 * self.n_nodes, "connects": 9 * self.n_el, "dphi": 162 * self.n_el,
-             "weight": 9 * self.n_el, "f0": self.neq, "df": self.neq, "fixed": self.neq,
+        nn = (self.order + 1) ** 2
+        n = {"node_xy": 2 * self.n_nodes, "connects": nn * self.n_el, "dphi": 2 * nn * nn * self.n_el,
+             "weight": nn * self.n_el, "f0": self.neq, "df": self.neq, "fixed": self.neq,
              "el_cohesion": self.n_el, "el_phi": self.n_el}[name]
         p = getattr(w, name)
         if not p:
@@ -269,14 +274,16 @@ class GmshMesh:
 
 
 class GmshProblem(WellboreMesh):
-    """Order-2 elastoplastic problem on a Gmsh mesh (CmeshElastoplasticity,
-    main.cpp:546-601).  bcs: (physical name or tag, type, value...) with the
-    reference's TBCData types: 0 u = 0, 1 traction (tx, ty), 3 directional
-    Dirichlet (fix the components with non-zero value), 6 normal stress
-    (value * outward normal).  Loads are applied at load factor 1; angles in
-    degrees; domain: physical name or tag of the quadrilaterals (None: all)."""
+    """Elastoplastic problem of order 1, 2 or 3 on a Gmsh mesh
+    (CmeshElastoplasticity, main.cpp:546-601).  bcs: (physical name or tag,
+    type, value...) with the reference's TBCData types: 0 u = 0, 1 traction
+    (tx, ty), 3 directional Dirichlet (fix the components with non-zero
+    value), 6 normal stress (value * outward normal).  Loads are applied at
+    load factor 1; angles in degrees; domain: physical name or tag of the
+    quadrilaterals (None: all)."""
 
-    def __init__(self, gmsh, bcs, E, nu, cohesion, phi_deg, psi_deg=None, domain=None, sigma0=(0.0, 0.0, 0.0, 0.0)):
+    def __init__(self, gmsh, bcs, E, nu, cohesion, phi_deg, psi_deg=None, domain=None, sigma0=(0.0, 0.0, 0.0, 0.0),
+                 order=2):
         self.params = None
         arr = (BC * max(1, len(bcs)))()
         for i, b in enumerate(bcs):
@@ -289,13 +296,14 @@ class GmshProblem(WellboreMesh):
         m.sigma0 = (C.c_double * 4)(*[float(x) for x in sigma0])
         self._w = C.POINTER(Wellbore)()
         dom = -1 if domain is None else gmsh.tag(domain)
-        st = lib().ipfem_gmsh_problem(gmsh._g, int(dom), arr, len(bcs), C.byref(m), C.byref(self._w))
+        st = lib().ipfem_gmsh_problem(gmsh._g, int(order), int(dom), arr, len(bcs), C.byref(m), C.byref(self._w))
         if st != 0:
             raise IpfemError(st, lib().ipfem_last_error(None).decode())
         w = self._w.contents
         self.n_el = w.mesh.n_elements
         self.n_nodes = w.mesh.n_nodes
         self.neq = 2 * self.n_nodes
+        self.order = int(w.mesh.order)
 
 
 class ElastoPlasticIntPointsStructMatrix:
@@ -531,8 +539,9 @@ class ElastoPlasticIntPointsStructMatrix:
         self._check(lib().ipfem_set_state(self._ctx, int(field), _np_ptr(arr, _dp)))
 
     def get_setup(self, field):
-        spec = {0: (self.n_el, np.int32), 1: (1, np.int32), 2: (18 * self.n_el, np.int32),
-                3: (162 * self.n_el, np.float64), 4: (self.n_ip, np.float64)}[field]
+        nn = self.n_ip // self.n_el
+        spec = {0: (self.n_el, np.int32), 1: (1, np.int32), 2: (2 * nn * self.n_el, np.int32),
+                3: (2 * nn * nn * self.n_el, np.float64), 4: (self.n_ip, np.float64)}[field]
         out = np.zeros(spec[0], spec[1])
         self._check(lib().ipfem_get_setup(self._ctx, int(field), C.c_void_p(out.ctypes.data)))
         return out

@@ -368,7 +368,7 @@ ipfem_status ipfem_create(const ipfem_mesh *mesh, const ipfem_material *mat, ipf
     ck(dalloc(&c->d_strain, (size_t)s.n_ip * 3));
     ck(dalloc(&c->d_sigma_w, (size_t)s.n_ip * 3));
     ck(dalloc(&c->d_dep, (size_t)s.n_ip * 9));
-    ck(dalloc(&c->d_fe, (size_t)s.n_el * 18));
+    ck(dalloc(&c->d_fe, (size_t)s.n_el * s.nd));
     ck(dalloc(&c->d_x, (size_t)s.neq));
     ck(dalloc(&c->d_r, (size_t)s.neq));
     ck(dalloc(&c->d_z, (size_t)s.neq));

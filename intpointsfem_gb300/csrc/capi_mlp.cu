@@ -146,6 +146,8 @@ ipfem_status ipfem_set_node_grid(ipfem_ctx *c, int32_t gr, int32_t gt)
 {
     if (!c || gr < 1 || gt < 1 || (int64_t)gr * gt != c->s.n_nodes)
         return mfail(c, IPFEM_INVALID, "node grid does not match the number of nodes");
+    if (c->s.order != 2)
+        return mfail(c, IPFEM_INVALID, "the learned preconditioner needs a grid of order-2 elements");
     if (c->mlp.ready && (gr != c->mlp.gr || gt != c->mlp.gt))
         return mfail(c, IPFEM_INVALID, "node grid is fixed once ipfem_mlp_init has run");
     c->mlp.gr = gr;

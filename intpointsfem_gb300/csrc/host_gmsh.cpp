@@ -1,12 +1,13 @@
 // Gmsh meshes on the host: the reader that stands in for NeoPZ's
 // TPZGmshReader (ReadGeometry, main.cpp:447-464; the reference's meshes are
-// gmsh/wellbore_*.msh, Gmsh 4.1 ASCII), and the order-2 problem built on them
-// as CmeshElastoplasticity does (main.cpp:546-601): the elastoplastic domain
-// on the quadrilaterals and the TBCData boundary conditions (main.cpp:374-446)
-// on the tagged lines and points.
+// gmsh/wellbore_*.msh, Gmsh 4.1 ASCII), and the problem of order 1, 2 or 3
+// built on them as CmeshElastoplasticity does (main.cpp:546-601): the
+// elastoplastic domain on the quadrilaterals and the TBCData boundary
+// conditions (main.cpp:374-446) on the tagged lines and points.
 //
 // Compiled with -ffp-contract=off: coordinates, element blocks and loads are
 // the separately rounded results of the written expressions on every host.
+#include <algorithm>
 #include <cmath>
 #include <cstdint>
 #include <cstdio>
@@ -290,11 +291,15 @@ extern "C" ipfem_status ipfem_gmsh_read(const char *path, ipfem_gmsh **out)
     return IPFEM_OK;
 }
 
-extern "C" ipfem_status ipfem_gmsh_problem(const ipfem_gmsh *g, int32_t domain_phys, const ipfem_bc *bcs, int32_t n_bc,
-                                           const ipfem_material *mat, ipfem_wellbore **out)
+extern "C" ipfem_status ipfem_gmsh_problem(const ipfem_gmsh *g, int32_t order, int32_t domain_phys,
+                                           const ipfem_bc *bcs, int32_t n_bc, const ipfem_material *mat,
+                                           ipfem_wellbore **out)
 {
     if (!g || !mat || !out || (n_bc > 0 && !bcs) || n_bc < 0) return gmsh_fail("null argument");
     *out = nullptr;
+    const int p = order == 0 ? 2 : order;
+    if (p < 1 || p > IPFEM_MAX_ORDER) return gmsh_fail("element order must be 1, 2 or 3");
+    const int nn = (p + 1) * (p + 1), ne1 = p - 1;      // connects per element, per edge interior
     if (mat->el_cohesion || mat->el_phi) return gmsh_fail("per-element material arrays are not supported here");
     for (int32_t b = 0; b < n_bc; b++) {
         const int ty = bcs[b].type;
@@ -324,39 +329,46 @@ extern "C" ipfem_status ipfem_gmsh_problem(const ipfem_gmsh *g, int32_t domain_p
                 edge_el.push_back((int32_t)e);
                 edge_uses.push_back(0);
             }
-            if (++edge_uses[(size_t)ins.first->second] > 2) return gmsh_fail("an edge is shared by more than two quadrilaterals");
+            if (++edge_uses[(size_t)ins.first->second] > 2)
+                return gmsh_fail("an edge is shared by more than two quadrilaterals");
             el_edge[4 * (size_t)e + k] = ins.first->second;
         }
     }
     const int64_t n_edges = (int64_t)edge_el.size();
-    const int64_t n_nodes_max = (int64_t)g->n_nodes + n_edges + n_el;
-    if (2 * n_nodes_max > INT32_MAX || n_el * 81 > INT32_MAX) return gmsh_fail("mesh too large");
-    // connects numbered in order of first use by the elements
-    std::vector<int32_t> vnew((size_t)g->n_nodes, -1), enew((size_t)n_edges, -1);
-    std::vector<int32_t> conn((size_t)n_el * 9);
+    const int64_t n_nodes_max = (int64_t)g->n_nodes + n_edges * ne1 + n_el * ne1 * ne1;
+    if (2 * n_nodes_max > INT32_MAX || n_el * nn * nn > INT32_MAX) return gmsh_fail("mesh too large");
+    // connects numbered in order of first use by the elements; the interior
+    // connects of a shared edge are numbered from its lower-numbered vertex
+    std::vector<int32_t> vnew((size_t)g->n_nodes, -1), enew((size_t)(n_edges * ne1), -1);
+    std::vector<int32_t> conn((size_t)n_el * nn);
     int32_t next = 0;
     for (int64_t e = 0; e < n_el; e++) {
         const int32_t *v = &g->quads[4 * (size_t)els[(size_t)e]];
-        int32_t *c = &conn[9 * (size_t)e];
+        int32_t *c = &conn[(size_t)nn * e];
         for (int k = 0; k < 4; k++) {
             if (vnew[(size_t)v[k]] < 0) vnew[(size_t)v[k]] = next++;
             c[k] = vnew[(size_t)v[k]];
         }
         for (int k = 0; k < 4; k++) {
-            int32_t &en = enew[(size_t)el_edge[4 * (size_t)e + k]];
-            if (en < 0) en = next++;
-            c[4 + k] = en;
+            const int32_t ed = el_edge[4 * (size_t)e + k];
+            const bool fwd = v[k] < v[(k + 1) & 3];
+            for (int i = 1; i <= ne1; i++) {
+                const int j = fwd ? i : p - i;          // position from the lower vertex
+                int32_t &en = enew[(size_t)ed * ne1 + (j - 1)];
+                if (en < 0) en = next++;
+                c[4 + k * ne1 + (i - 1)] = en;
+            }
         }
-        c[8] = next++;
+        for (int k = 4 + 4 * ne1; k < nn; k++) c[k] = next++;
     }
     const int64_t n_nodes = next, neq = 2 * n_nodes;
     ipfem_wellbore *w = new (std::nothrow) ipfem_wellbore();
     if (!w) return IPFEM_OOM;
     std::memset(w, 0, sizeof *w);
     w->node_xy = (double *)std::calloc((size_t)n_nodes * 2, sizeof(double));
-    w->connects = (int32_t *)std::calloc((size_t)n_el * 9, sizeof(int32_t));
-    w->dphi = (double *)std::calloc((size_t)n_el * 162, sizeof(double));
-    w->weight = (double *)std::calloc((size_t)n_el * 9, sizeof(double));
+    w->connects = (int32_t *)std::calloc((size_t)n_el * nn, sizeof(int32_t));
+    w->dphi = (double *)std::calloc((size_t)n_el * nn * 2 * nn, sizeof(double));
+    w->weight = (double *)std::calloc((size_t)n_el * nn, sizeof(double));
     w->f0 = (double *)std::calloc((size_t)neq, sizeof(double));
     w->df = (double *)std::calloc((size_t)neq, sizeof(double));
     w->fixed = (uint8_t *)std::calloc((size_t)neq, 1);
@@ -365,25 +377,44 @@ extern "C" ipfem_status ipfem_gmsh_problem(const ipfem_gmsh *g, int32_t domain_p
         return IPFEM_OOM;
     }
     std::memcpy(w->connects, conn.data(), conn.size() * sizeof(int32_t));
-    // coordinates: vertices, straight-edge midpoints, bilinear centres
+    // coordinates: vertices, equally spaced edge connects, interior connects on
+    // the bilinear map (order 2: the straight-edge midpoints and the centre)
     for (int64_t e = 0; e < n_el; e++) {
         const int32_t *v = &g->quads[4 * (size_t)els[(size_t)e]];
-        const int32_t *c = &conn[9 * (size_t)e];
-        const double *p[4];
+        const int32_t *c = &conn[(size_t)nn * e];
+        const double *pv[4];
         for (int k = 0; k < 4; k++) {
-            p[k] = &g->xy[2 * (size_t)v[k]];
-            w->node_xy[2 * (size_t)c[k]] = p[k][0];
-            w->node_xy[2 * (size_t)c[k] + 1] = p[k][1];
+            pv[k] = &g->xy[2 * (size_t)v[k]];
+            w->node_xy[2 * (size_t)c[k]] = pv[k][0];
+            w->node_xy[2 * (size_t)c[k] + 1] = pv[k][1];
         }
         for (int k = 0; k < 4; k++) {
-            const double *a = p[k], *b = p[(k + 1) & 3];
-            w->node_xy[2 * (size_t)c[4 + k]] = 0.5 * (a[0] + b[0]);
-            w->node_xy[2 * (size_t)c[4 + k] + 1] = 0.5 * (a[1] + b[1]);
+            const int32_t va = v[k], vb = v[(k + 1) & 3];
+            const double *lo = &g->xy[2 * (size_t)std::min(va, vb)], *hi = &g->xy[2 * (size_t)std::max(va, vb)];
+            const int32_t ed = el_edge[4 * (size_t)e + k];
+            for (int j = 1; j <= ne1; j++) {
+                const int32_t node = enew[(size_t)ed * ne1 + (j - 1)];
+                for (int d = 0; d < 2; d++)
+                    w->node_xy[2 * (size_t)node + d] = p == 2 ? 0.5 * (lo[d] + hi[d])
+                                                              : (lo[d] * (p - j) + hi[d] * j) / p;
+            }
         }
-        w->node_xy[2 * (size_t)c[8]] = 0.25 * (((p[0][0] + p[1][0]) + p[2][0]) + p[3][0]);
-        w->node_xy[2 * (size_t)c[8] + 1] = 0.25 * (((p[0][1] + p[1][1]) + p[2][1]) + p[3][1]);
+        for (int k = 4 + 4 * ne1; k < nn; k++) {
+            const int m = k - 4 - 4 * ne1, ia = m % ne1 + 1, ib = m / ne1 + 1;
+            for (int d = 0; d < 2; d++) {
+                double x;
+                if (p == 2) {
+                    x = 0.25 * (((pv[0][d] + pv[1][d]) + pv[2][d]) + pv[3][d]);
+                } else {
+                    const double u = (double)ia / p, t = (double)ib / p;
+                    x = (1.0 - u) * (1.0 - t) * pv[0][d] + u * (1.0 - t) * pv[1][d] + u * t * pv[2][d] +
+                        (1.0 - u) * t * pv[3][d];
+                }
+                w->node_xy[2 * (size_t)c[k] + d] = x;
+            }
+        }
     }
-    element_blocks_dphi(n_el, w->connects, w->node_xy, w->dphi, w->weight);
+    element_blocks_dphi(p, n_el, w->connects, w->node_xy, w->dphi, w->weight);
     // boundary conditions
     for (int32_t b = 0; b < n_bc; b++) {
         const ipfem_bc &bc = bcs[b];
@@ -401,31 +432,57 @@ extern "C" ipfem_status ipfem_gmsh_problem(const ipfem_gmsh *g, int32_t domain_p
                 ipfem_wellbore_free(w);
                 return gmsh_fail("a line of physical tag " + std::to_string(bc.phys) + " is not an element edge");
             }
-            const int32_t A = vnew[(size_t)a], B = vnew[(size_t)bb], M = enew[(size_t)f->second];
+            const int32_t ed = f->second;
+            const int32_t A = vnew[(size_t)std::min(a, bb)], B = vnew[(size_t)std::max(a, bb)];
+            // connects of the line from its lower vertex: A, edge connects, B
+            std::vector<int32_t> line_nodes;
+            line_nodes.push_back(A);
+            for (int j = 1; j <= ne1; j++) line_nodes.push_back(enew[(size_t)ed * ne1 + (j - 1)]);
+            line_nodes.push_back(B);
             if (bc.type == 0 || bc.type == 3) {
-                fix_node(A);
-                fix_node(M);
-                fix_node(B);
-            } else if (bc.type == 1) {
-                edge_load(w->node_xy, A, M, B, bc.val[0], bc.val[1], w->df);
-            } else {
-                if (edge_uses[(size_t)f->second] != 1) {
+                for (int32_t node : line_nodes) fix_node(node);
+                continue;
+            }
+            double tx = bc.val[0], ty = bc.val[1];
+            if (bc.type == 6) {
+                if (edge_uses[(size_t)ed] != 1) {
                     ipfem_wellbore_free(w);
                     return gmsh_fail("a normal-stress line of physical tag " + std::to_string(bc.phys) +
                                      " is not on the boundary");
                 }
-                // outward normal: away from the adjacent element's centre
+                // outward normal: away from the adjacent element's vertex centre
                 const double *pa = &w->node_xy[2 * (size_t)A], *pb = &w->node_xy[2 * (size_t)B];
                 const double dx = pb[0] - pa[0], dy = pb[1] - pa[1];
                 const double L = std::sqrt(dx * dx + dy * dy);
                 double nx = dy / L, ny = -dx / L;
-                const double *pc = &w->node_xy[2 * (size_t)conn[9 * (size_t)edge_el[(size_t)f->second] + 8]];
-                const double *pm = &w->node_xy[2 * (size_t)M];
-                if ((pc[0] - pm[0]) * nx + (pc[1] - pm[1]) * ny > 0.0) {
+                const int32_t *ce = &conn[(size_t)nn * edge_el[(size_t)ed]];
+                double cx = 0.0, cy = 0.0;
+                for (int k = 0; k < 4; k++) {
+                    cx += 0.25 * w->node_xy[2 * (size_t)ce[k]];
+                    cy += 0.25 * w->node_xy[2 * (size_t)ce[k] + 1];
+                }
+                if ((cx - 0.5 * (pa[0] + pb[0])) * nx + (cy - 0.5 * (pa[1] + pb[1])) * ny > 0.0) {
                     nx = -nx;
                     ny = -ny;
                 }
-                edge_load(w->node_xy, A, M, B, bc.val[0] * nx, bc.val[0] * ny, w->df);
+                tx = bc.val[0] * nx;
+                ty = bc.val[0] * ny;
+            }
+            if (p == 2) {
+                edge_load(w->node_xy, A, line_nodes[1], B, tx, ty, w->df);
+            } else {
+                // consistent load of a constant traction: the order-p Lagrange trace
+                // functions on equispaced nodes integrate to L/2 (p = 1) and
+                // L/8, 3L/8, 3L/8, L/8 (p = 3)
+                const double *pa = &w->node_xy[2 * (size_t)A], *pb = &w->node_xy[2 * (size_t)B];
+                const double dx = pb[0] - pa[0], dy = pb[1] - pa[1];
+                const double L = std::sqrt(dx * dx + dy * dy);
+                const double w1[2] = {0.5, 0.5}, w3[4] = {0.125, 0.375, 0.375, 0.125};
+                for (int k = 0; k <= p; k++) {
+                    const double wk = (p == 1 ? w1[k] : w3[k]) * L;
+                    w->df[2 * (size_t)line_nodes[(size_t)k]] += tx * wk;
+                    w->df[2 * (size_t)line_nodes[(size_t)k] + 1] += ty * wk;
+                }
             }
         }
         for (int32_t q = 0; q < g->n_points; q++) {
@@ -460,6 +517,7 @@ extern "C" ipfem_status ipfem_gmsh_problem(const ipfem_gmsh *g, int32_t domain_p
     w->mesh.fixed = w->fixed;
     w->mesh.f0 = w->f0;
     w->mesh.df = w->df;
+    w->mesh.order = p;
     *out = w;
     return IPFEM_OK;
 }

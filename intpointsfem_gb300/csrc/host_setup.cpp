@@ -34,7 +34,7 @@ void elastic_constants(double E, double nu, ElasticConstH &el)
 // TPZNumericalIntegrator::SetUpColoredIndexes (TPZNumericalIntegrator.cpp:452-536):
 // repeated passes over the elements in index order; an element takes the
 // current colour iff none of its connects is marked in this pass.
-int32_t greedy_coloring(int32_t n_el, int32_t n_nodes, const int32_t *connects, int32_t *el_color)
+int32_t greedy_coloring_nn(int32_t n_el, int32_t n_nodes, int32_t nn, const int32_t *connects, int32_t *el_color)
 {
     std::vector<uint8_t> mark((size_t)n_nodes, 0);
     std::fill(el_color, el_color + n_el, -1);
@@ -44,20 +44,25 @@ int32_t greedy_coloring(int32_t n_el, int32_t n_nodes, const int32_t *connects, 
         again = false;
         for (int32_t e = 0; e < n_el; e++) {
             if (el_color[e] != -1) continue;
-            const int32_t *c = connects + 9 * (size_t)e;
+            const int32_t *c = connects + (size_t)nn * e;
             int k = 0;
-            while (k < 9 && !mark[c[k]]) k++;
-            if (k != 9) {
+            while (k < nn && !mark[c[k]]) k++;
+            if (k != nn) {
                 again = true;
                 continue;
             }
             el_color[e] = color;
-            for (k = 0; k < 9; k++) mark[c[k]] = 1;
+            for (k = 0; k < nn; k++) mark[c[k]] = 1;
         }
         color++;
         std::fill(mark.begin(), mark.end(), 0);
     }
     return color;
+}
+
+int32_t greedy_coloring(int32_t n_el, int32_t n_nodes, const int32_t *connects, int32_t *el_color)
+{
+    return greedy_coloring_nn(n_el, n_nodes, 9, connects, el_color);
 }
 
 template <class F>
@@ -122,15 +127,16 @@ std::string build_sell(const Setup &s, bool sorted, SellLayout &L)
         for (int64_t j = L.rowlen[t]; j < (int64_t)(L.slice_base[t / 32 + 1] - L.slice_base[t / 32]) / 32; j++)
             L.sell_col[base + j * 32] = i;
     }
-    L.el_blk.resize((size_t)s.n_el * 81);
+    const int nn = s.nn, nd = s.nd;
+    L.el_blk.resize((size_t)s.n_el * nn * nn);
     parallel_for(s.n_el, [&](int64_t e) {
-        for (int a = 0; a < 9; a++) {
-            const int32_t r = s.dofs[(size_t)e * 18 + 2 * a] >> 1;
+        for (int a = 0; a < nn; a++) {
+            const int32_t r = s.dofs[(size_t)e * nd + 2 * a] >> 1;
             const int32_t *b0 = s.col.data() + s.row_ptr[r], *b1 = s.col.data() + s.row_ptr[r + 1];
-            for (int b = 0; b < 9; b++) {
-                const int32_t c = s.dofs[(size_t)e * 18 + 2 * b] >> 1;
+            for (int b = 0; b < nn; b++) {
+                const int32_t c = s.dofs[(size_t)e * nd + 2 * b] >> 1;
                 const int64_t j = std::lower_bound(b0, b1, c) - b0;
-                L.el_blk[(size_t)e * 81 + a * 9 + b] = (int32_t)L.bsr_to_sell[s.row_ptr[r] + j];
+                L.el_blk[((size_t)e * nn + a) * nn + b] = (int32_t)L.bsr_to_sell[s.row_ptr[r] + j];
             }
         }
     });
@@ -143,48 +149,53 @@ std::string build_setup(const ipfem_mesh *m, const ipfem_material *mat, Setup &s
     if (m->n_elements <= 0 || m->n_nodes <= 0) return "empty mesh";
     if (!m->connects || !m->weight || (!m->dphi && !m->block_storage)) return "mesh arrays missing";
     if ((int64_t)m->n_nodes * 2 > INT32_MAX) return "too many nodes";
+    if (m->order < 0 || m->order > IPFEM_MAX_ORDER) return "element order must be 1, 2 or 3";
+    s.order = m->order == 0 ? 2 : m->order;
+    s.nn = s.nq = (s.order + 1) * (s.order + 1);
+    s.nd = 2 * s.nn;
+    const int nn = s.nn, nq = s.nq, nd = s.nd;
     s.n_el = m->n_elements;
     s.n_nodes = m->n_nodes;
     s.neq = 2 * m->n_nodes;
-    s.n_ip = (int64_t)s.n_el * IPFEM_NPTS;
-    for (int64_t k = 0; k < (int64_t)s.n_el * 9; k++)
+    s.n_ip = (int64_t)s.n_el * nq;
+    for (int64_t k = 0; k < (int64_t)s.n_el * nn; k++)
         if (m->connects[k] < 0 || m->connects[k] >= s.n_nodes) return "connect index out of range";
     for (int32_t e = 0; e < s.n_el; e++) {
-        const int32_t *c = m->connects + 9 * (size_t)e;
-        for (int a = 0; a < 9; a++)
-            for (int b = a + 1; b < 9; b++)
+        const int32_t *c = m->connects + (size_t)nn * e;
+        for (int a = 0; a < nn; a++)
+            for (int b = a + 1; b < nn; b++)
                 if (c[a] == c[b]) return "repeated connect in an element";
     }
     // element blocks
-    s.dphi.resize((size_t)s.n_el * 162);
+    s.dphi.resize((size_t)s.n_el * nq * 2 * nn);
     if (m->dphi) {
         std::memcpy(s.dphi.data(), m->dphi, s.dphi.size() * sizeof(double));
     } else {
         // fStorage (3*npts) x (2*nshape) row-major: row 3q+comp+jdim, column 2n+comp
         // (TPZNumericalIntegrator.cpp:371-381)
         for (int32_t e = 0; e < s.n_el; e++) {
-            const double *B = m->block_storage + (size_t)e * 486;
-            for (int q = 0; q < 9; q++)
-                for (int n = 0; n < 9; n++) {
-                    const double dx = B[(3 * q + 0) * 18 + 2 * n], dy = B[(3 * q + 1) * 18 + 2 * n];
-                    if (B[(3 * q + 1) * 18 + 2 * n + 1] != dx || B[(3 * q + 2) * 18 + 2 * n + 1] != dy ||
-                        B[(3 * q + 0) * 18 + 2 * n + 1] != 0.0 || B[(3 * q + 2) * 18 + 2 * n] != 0.0)
+            const double *B = m->block_storage + (size_t)e * 3 * nq * nd;
+            for (int q = 0; q < nq; q++)
+                for (int n = 0; n < nn; n++) {
+                    const double dx = B[(3 * q + 0) * nd + 2 * n], dy = B[(3 * q + 1) * nd + 2 * n];
+                    if (B[(3 * q + 1) * nd + 2 * n + 1] != dx || B[(3 * q + 2) * nd + 2 * n + 1] != dy ||
+                        B[(3 * q + 0) * nd + 2 * n + 1] != 0.0 || B[(3 * q + 2) * nd + 2 * n] != 0.0)
                         return "block_storage is not a 2-D strain block (element " + std::to_string(e) + ")";
-                    s.dphi[((size_t)e * 9 + q) * 18 + n] = dx;
-                    s.dphi[((size_t)e * 9 + q) * 18 + 9 + n] = dy;
+                    s.dphi[((size_t)e * nq + q) * 2 * nn + n] = dx;
+                    s.dphi[((size_t)e * nq + q) * 2 * nn + nn + n] = dy;
                 }
         }
     }
     s.weight.assign(m->weight, m->weight + s.n_ip);
     // dof map (TPZNumericalIntegrator.cpp:429-443): connect sequence x 2
-    s.dofs.resize((size_t)s.n_el * 18);
-    for (size_t k = 0; k < (size_t)s.n_el * 9; k++) {
+    s.dofs.resize((size_t)s.n_el * nd);
+    for (size_t k = 0; k < (size_t)s.n_el * nn; k++) {
         s.dofs[2 * k] = 2 * m->connects[k];
         s.dofs[2 * k + 1] = 2 * m->connects[k] + 1;
     }
     // colouring
     s.el_color.resize(s.n_el);
-    s.n_colors = greedy_coloring(s.n_el, s.n_nodes, m->connects, s.el_color.data());
+    s.n_colors = greedy_coloring_nn(s.n_el, s.n_nodes, nn, m->connects, s.el_color.data());
     if (s.n_colors > kMaxColors) return "more than 16 colours";
     s.color_ptr.assign(s.n_colors + 1, 0);
     for (int32_t e = 0; e < s.n_el; e++) s.color_ptr[s.el_color[e] + 1]++;
@@ -199,19 +210,19 @@ std::string build_setup(const ipfem_mesh *m, const ipfem_material *mat, Setup &s
     }
     s.inc.assign((size_t)s.n_colors * s.n_nodes, -1);
     for (int32_t e = 0; e < s.n_el; e++)
-        for (int ln = 0; ln < 9; ln++)
-            s.inc[(size_t)s.el_color[e] * s.n_nodes + m->connects[9 * (size_t)e + ln]] = e * 9 + ln;
+        for (int ln = 0; ln < nn; ln++)
+            s.inc[(size_t)s.el_color[e] * s.n_nodes + m->connects[(size_t)nn * e + ln]] = e * nn + ln;
     // nodal block pattern
     {
         std::vector<int64_t> cap((size_t)s.n_nodes + 1, 0);
-        for (size_t k = 0; k < (size_t)s.n_el * 9; k++) cap[m->connects[k] + 1] += 9;
+        for (size_t k = 0; k < (size_t)s.n_el * nn; k++) cap[m->connects[k] + 1] += nn;
         for (int32_t i = 0; i < s.n_nodes; i++) cap[i + 1] += cap[i];
         std::vector<int32_t> tmp((size_t)cap[s.n_nodes]);
         std::vector<int32_t> deg((size_t)s.n_nodes, 0);
         for (int32_t e = 0; e < s.n_el; e++)
-            for (int a = 0; a < 9; a++) {
-                const int32_t r = m->connects[9 * (size_t)e + a];
-                for (int b = 0; b < 9; b++) tmp[cap[r] + deg[r]++] = m->connects[9 * (size_t)e + b];
+            for (int a = 0; a < nn; a++) {
+                const int32_t r = m->connects[(size_t)nn * e + a];
+                for (int b = 0; b < nn; b++) tmp[cap[r] + deg[r]++] = m->connects[(size_t)nn * e + b];
             }
         s.row_ptr.assign((size_t)s.n_nodes + 1, 0);
         parallel_for(s.n_nodes, [&](int64_t i) {
@@ -284,6 +295,7 @@ static double urand(uint64_t seed, uint64_t e, uint64_t k)
 static const int kRefA[9] = {-1, 1, 1, -1, 0, 1, 0, -1, 0};
 static const int kRefB[9] = {-1, -1, 1, 1, -1, 0, 1, 0, 0};
 
+// order-2 Lagrange functions on -1, 0, 1 (closed forms)
 static double lag(int a, double x)
 {
     if (a < 0) return 0.5 * x * (x - 1.0);
@@ -298,16 +310,93 @@ static double dlag(int a, double x)
     return x + 0.5;
 }
 
-// d(phi)/dx, d(phi)/dy and w|detJ| of a bilinear-geometry Q2 element at the
-// 3x3 Gauss points (point q = 3*i_eta + i_xi); shape functions are the
-// tensor-product quadratic Lagrange functions of the 9 connects.
-static void element_dphi(const double *X, const double *Y, double *dphi, double *w)
+// 1-D Lagrange function a of order p on the equispaced nodes t_m = -1 + 2m/p
+// and its derivative (orders 1 and 3)
+static double lagp(int p, int a, double x)
 {
-    const double g = std::sqrt(0.6);
-    const double gp[3] = {-g, 0.0, g};
-    const double gw[3] = {5.0 / 9.0, 8.0 / 9.0, 5.0 / 9.0};
-    for (int iq = 0; iq < 9; iq++) {
-        const int ix = iq % 3, iy = iq / 3;
+    const double ta = -1.0 + 2.0 * a / p;
+    double num = 1.0, den = 1.0;
+    for (int m = 0; m <= p; m++) {
+        if (m == a) continue;
+        const double tm = -1.0 + 2.0 * m / p;
+        num = num * (x - tm);
+        den = den * (ta - tm);
+    }
+    return num / den;
+}
+
+static double dlagp(int p, int a, double x)
+{
+    const double ta = -1.0 + 2.0 * a / p;
+    double s = 0.0;
+    for (int k = 0; k <= p; k++) {
+        if (k == a) continue;
+        const double tk = -1.0 + 2.0 * k / p;
+        double prod = 1.0 / (ta - tk);
+        for (int m = 0; m <= p; m++) {
+            if (m == a || m == k) continue;
+            const double tm = -1.0 + 2.0 * m / p;
+            prod = prod * ((x - tm) / (ta - tm));
+        }
+        s = s + prod;
+    }
+    return s;
+}
+
+// index-space position (a, b) in [0, p]^2 of connect n of an order-p element:
+// vertices, the p-1 nodes of each edge in traversal order, interior row by row
+static void ref_node(int p, int n, int &a, int &b)
+{
+    const int vx[4] = {0, p, p, 0}, vy[4] = {0, 0, p, p};
+    if (n < 4) {
+        a = vx[n];
+        b = vy[n];
+        return;
+    }
+    n -= 4;
+    if (n < 4 * (p - 1)) {
+        const int e = n / (p - 1), k = n % (p - 1) + 1;
+        if (e == 0) { a = k; b = 0; }
+        else if (e == 1) { a = p; b = k; }
+        else if (e == 2) { a = p - k; b = p; }
+        else { a = 0; b = p - k; }
+        return;
+    }
+    n -= 4 * (p - 1);
+    a = n % (p - 1) + 1;
+    b = n / (p - 1) + 1;
+}
+
+// Gauss points and weights, p + 1 per direction
+static void gauss(int p, double *gp, double *gw)
+{
+    if (p == 1) {
+        const double g = 1.0 / std::sqrt(3.0);
+        gp[0] = -g; gp[1] = g;
+        gw[0] = 1.0; gw[1] = 1.0;
+    } else if (p == 2) {
+        const double g = std::sqrt(0.6);
+        gp[0] = -g; gp[1] = 0.0; gp[2] = g;
+        gw[0] = 5.0 / 9.0; gw[1] = 8.0 / 9.0; gw[2] = 5.0 / 9.0;
+    } else {
+        const double a = std::sqrt(3.0 / 7.0 - 2.0 / 7.0 * std::sqrt(6.0 / 5.0));
+        const double b = std::sqrt(3.0 / 7.0 + 2.0 / 7.0 * std::sqrt(6.0 / 5.0));
+        const double wa = (18.0 + std::sqrt(30.0)) / 36.0, wb = (18.0 - std::sqrt(30.0)) / 36.0;
+        gp[0] = -b; gp[1] = -a; gp[2] = a; gp[3] = b;
+        gw[0] = wb; gw[1] = wa; gw[2] = wa; gw[3] = wb;
+    }
+}
+
+// d(phi)/dx, d(phi)/dy and w|detJ| of a bilinear-geometry element of order p
+// at its Gauss points (point q = (p+1)*i_eta + i_xi); shape functions are the
+// tensor-product Lagrange functions of its connects
+static void element_dphi(int p, const double *X, const double *Y, double *dphi, double *w)
+{
+    const int n1 = p + 1, nn = n1 * n1, nq = n1 * n1;
+    double gp[4], gw[4];
+    gauss(p, gp, gw);
+    for (int iq = 0; iq < nq; iq++) {
+        const int ix = iq % n1, iy = iq / n1;
         const double xi = gp[ix], eta = gp[iy];
         const double dpx[4] = {-(1.0 - eta) / 4.0, (1.0 - eta) / 4.0, (1.0 + eta) / 4.0, -(1.0 + eta) / 4.0};
         const double dpe[4] = {-(1.0 - xi) / 4.0, -(1.0 + xi) / 4.0, (1.0 + xi) / 4.0, (1.0 - xi) / 4.0};
@@ -323,25 +412,34 @@ static void element_dphi(const double *X, const double *Y, double *dphi, double 
         const double xi_x = y_eta / det, xi_y = -x_eta / det;
         const double eta_x = -y_xi / det, eta_y = x_xi / det;
         w[iq] = (gw[ix] * gw[iy]) * std::fabs(det);
-        for (int n = 0; n < 9; n++) {
-            const double Nxi = dlag(kRefA[n], xi) * lag(kRefB[n], eta);
-            const double Neta = lag(kRefA[n], xi) * dlag(kRefB[n], eta);
-            dphi[iq * 18 + n] = Nxi * xi_x + Neta * eta_x;
-            dphi[iq * 18 + 9 + n] = Nxi * xi_y + Neta * eta_y;
+        for (int n = 0; n < nn; n++) {
+            double Nxi, Neta;
+            if (p == 2) {
+                Nxi = dlag(kRefA[n], xi) * lag(kRefB[n], eta);
+                Neta = lag(kRefA[n], xi) * dlag(kRefB[n], eta);
+            } else {
+                int a, b;
+                ref_node(p, n, a, b);
+                Nxi = dlagp(p, a, xi) * lagp(p, b, eta);
+                Neta = lagp(p, a, xi) * dlagp(p, b, eta);
+            }
+            dphi[iq * 2 * nn + n] = Nxi * xi_x + Neta * eta_x;
+            dphi[iq * 2 * nn + nn + n] = Nxi * xi_y + Neta * eta_y;
         }
     }
 }
 
-void element_blocks_dphi(int64_t n_el, const int32_t *connects, const double *node_xy, double *dphi,
+void element_blocks_dphi(int order, int64_t n_el, const int32_t *connects, const double *node_xy, double *dphi,
                          double *weight)
 {
+    const int nn = (order + 1) * (order + 1), nq = nn;
     parallel_for(n_el, [&](int64_t e) {
         double X[4], Y[4];
         for (int v = 0; v < 4; v++) {
-            X[v] = node_xy[2 * (size_t)connects[9 * e + v]];
-            Y[v] = node_xy[2 * (size_t)connects[9 * e + v] + 1];
+            X[v] = node_xy[2 * (size_t)connects[(size_t)nn * e + v]];
+            Y[v] = node_xy[2 * (size_t)connects[(size_t)nn * e + v] + 1];
         }
-        element_dphi(X, Y, dphi + e * 162, weight + e * 9);
+        element_dphi(order, X, Y, dphi + e * nq * 2 * nn, weight + e * nq);
     });
 }
 
@@ -368,12 +466,18 @@ static void seg_load(const double *xy, int32_t P, int32_t M, int32_t Q, int sgn,
 
 using namespace ipfem;
 
+extern "C" int32_t ipfem_color_elements_nn(int32_t n_el, int32_t n_nodes, int32_t nn, const int32_t *connects,
+                                           int32_t *el_color)
+{
+    if (n_el <= 0 || n_nodes <= 0 || nn < 4 || !connects || !el_color) return -1;
+    for (int64_t k = 0; k < (int64_t)n_el * nn; k++)
+        if (connects[k] < 0 || connects[k] >= n_nodes) return -1;
+    return greedy_coloring_nn(n_el, n_nodes, nn, connects, el_color);
+}
+
 extern "C" int32_t ipfem_color_elements(int32_t n_el, int32_t n_nodes, const int32_t *connects, int32_t *el_color)
 {
-    if (n_el <= 0 || n_nodes <= 0 || !connects || !el_color) return -1;
-    for (int64_t k = 0; k < (int64_t)n_el * 9; k++)
-        if (connects[k] < 0 || connects[k] >= n_nodes) return -1;
-    return greedy_coloring(n_el, n_nodes, connects, el_color);
+    return ipfem_color_elements_nn(n_el, n_nodes, 9, connects, el_color);
 }
 
 extern "C" void ipfem_wellbore_default(ipfem_wellbore_params *p, int32_t n)
@@ -485,7 +589,7 @@ extern "C" ipfem_status ipfem_wellbore_build(const ipfem_wellbore_params *prm, i
             c[4] = nid(a0 + 1, b0); c[5] = nid(a0 + 2, b0 + 1); c[6] = nid(a0 + 1, b0 + 2); c[7] = nid(a0, b0 + 1);
             c[8] = nid(a0 + 1, b0 + 1);
         }
-    element_blocks_dphi(n_el, w->connects, w->node_xy, w->dphi, w->weight);
+    element_blocks_dphi(2, n_el, w->connects, w->node_xy, w->dphi, w->weight);
     for (int a = 0; a < gr; a++) {
         w->fixed[2 * (size_t)nid(a, 0) + 1] = 1;
         w->fixed[2 * (size_t)nid(a, gt - 1) + 0] = 1;
@@ -553,6 +657,7 @@ extern "C" ipfem_status ipfem_wellbore_build(const ipfem_wellbore_params *prm, i
     w->mesh.fixed = w->fixed;
     w->mesh.f0 = w->f0;
     w->mesh.df = w->df;
+    w->mesh.order = 2;
     *out = w;
     return IPFEM_OK;
 }

@@ -40,7 +40,7 @@ struct SellLayout {
     std::vector<int32_t> rowlen;         // [n_nodes] blocks of the row at each row position
     std::vector<int32_t> sell_col;       // [n_sell]
     std::vector<int64_t> bsr_to_sell;    // [n_blocks]
-    std::vector<int32_t> el_blk;         // [n_el*81] slot of local node pair (m, n)
+    std::vector<int32_t> el_blk;         // [n_el*nn*nn] slot of local node pair (m, n)
     std::vector<int64_t> diag_blk;       // [n_nodes] slot of the diagonal block
 };
 
@@ -54,7 +54,7 @@ struct SellDev {
 
 // buffers of the mixed-precision solve (FP32 tangent and CG)
 struct MixedBuffers {
-    float *dphi = nullptr;        // [n_el*162]
+    float *dphi = nullptr;        // [n_el*nq*2*nn]
     float *K = nullptr;           // [sell.n_sell*4]
     SellLayout sell;              // node-ordered rows (the FP32 SpMV is gather-bound)
     SellDev dsell;
@@ -70,14 +70,15 @@ struct MixedBuffers {
 // dof map, nodal 2x2 block pattern in SELL-32 layout, colour incidence).
 struct Setup {
     int32_t n_el = 0, n_nodes = 0, neq = 0, n_colors = 0;
+    int32_t order = 2, nn = 9, nq = 9, nd = 18;   // element order; connects, points, dofs per element
     int64_t n_ip = 0;
-    std::vector<double> dphi;            // [n_el*162] ((e*9+q)*2+d)*9+n
+    std::vector<double> dphi;            // [n_el*nq*2*nn] ((e*nq+q)*2+d)*nn+n
     std::vector<double> weight;          // [n_ip]
-    std::vector<int32_t> dofs;           // [n_el*18]
+    std::vector<int32_t> dofs;           // [n_el*nd]
     std::vector<int32_t> el_color;       // [n_el]
     std::vector<int32_t> color_ptr;      // [n_colors+1]
     std::vector<int32_t> color_els;      // [n_el]
-    std::vector<int32_t> inc;            // [n_colors*n_nodes] e*9+local node or -1
+    std::vector<int32_t> inc;            // [n_colors*n_nodes] e*nn+local node or -1
     // nodal block pattern (rows ascending, columns ascending)
     int64_t n_blocks = 0;
     std::vector<int64_t> row_ptr;        // [n_nodes+1]
@@ -95,10 +96,12 @@ struct Setup {
 
 // builds the setup; returns an empty string or an error message
 std::string build_setup(const ipfem_mesh *mesh, const ipfem_material *mat, Setup &s);
-// d(phi)/dx, d(phi)/dy and w|detJ| at the 3x3 Gauss points of Q2 elements
-// with bilinear geometry from their 4 vertex connects (host, threaded)
-void element_blocks_dphi(int64_t n_el, const int32_t *connects, const double *node_xy, double *dphi,
+// d(phi)/dx, d(phi)/dy and w|detJ| at the (p+1)^2 Gauss points of order-p
+// Lagrange elements with bilinear geometry from their 4 vertex connects
+// (host, threaded)
+void element_blocks_dphi(int order, int64_t n_el, const int32_t *connects, const double *node_xy, double *dphi,
                          double *weight);
+int32_t greedy_coloring_nn(int32_t n_el, int32_t n_nodes, int32_t nn, const int32_t *connects, int32_t *el_color);
 // SELL-32 layout of s's block pattern; sorted: rows by length inside each
 // kRedBlock-node window (stable, longest first)
 std::string build_sell(const Setup &s, bool sorted, SellLayout &L);

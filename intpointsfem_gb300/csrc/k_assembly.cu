@@ -16,90 +16,100 @@
 //                    added colour by colour into the nodal 2x2 block matrix.
 //
 // Element blocks are stored compactly: dphi[e][q][d][n] = d(phi_n)/d(x_d) at
-// point q (the reference's fStorage holds the same numbers in a (27 x 18)
+// point q (the reference's fStorage holds the same numbers in a (3 nq x 2 nn)
 // block with structural zeros).  Products use fma in the order of the
 // reference's row-major block traversal; skipped terms are exact zeros.
+// Every kernel is instantiated for the element orders P = 1, 2, 3 (the
+// reference builds one order per binary, KernelsMatrixAssemble.h:3-12):
+// nn = nq = (P+1)^2 connects and Gauss points, nd = 2 nn dofs per element.
 #include "ipfem_internal.h"
 #include "tma.cuh"
 
 namespace ipfem {
 
-constexpr int kGatherTile = 32;     // elements per CTA (288 threads)
-constexpr int kResTile = 16;        // elements per CTA (288 threads)
-constexpr int kElBytes = 162 * 8;   // compact block bytes per element (multiple of 16)
+template <int P>
+struct Elem {
+    static constexpr int N1 = P + 1, NN = N1 * N1, NQ = N1 * N1, ND = 2 * NN;
+    static constexpr int NB = NQ * 2 * NN;                    // compact block values per element
+    static constexpr int kGatherTile = P == 1 ? 64 : (P == 2 ? 32 : 8);   // elements per CTA
+    static constexpr int kResTile = P == 1 ? 32 : (P == 2 ? 16 : 8);      // elements per CTA
+};
+static_assert(Elem<1>::NB * 8 % 16 == 0 && Elem<2>::NB * 8 % 16 == 0 && Elem<3>::NB * 8 % 16 == 0,
+              "bulk copies of whole element blocks need 16-byte multiples");
 
-__global__ void __launch_bounds__(kGatherTile * 9) k_gather_strain(int32_t n_el, int64_t n_ip,
-                                                                   const double *__restrict__ dphi,
-                                                                   const int32_t *__restrict__ dofs,
-                                                                   const double *__restrict__ u,
-                                                                   double *__restrict__ strain,
-                                                                   int *__restrict__ err)
+template <int P>
+__global__ void __launch_bounds__(Elem<P>::kGatherTile * Elem<P>::NQ)
+k_gather_strain(int32_t n_el, int64_t n_ip, const double *__restrict__ dphi, const int32_t *__restrict__ dofs,
+                const double *__restrict__ u, double *__restrict__ strain, int *__restrict__ err)
 {
+    typedef Elem<P> E;
     extern __shared__ __align__(128) unsigned char smem[];
     uint64_t *bar = reinterpret_cast<uint64_t *>(smem);
     double *s_dn = reinterpret_cast<double *>(smem + 128);
-    double *s_u = s_dn + kGatherTile * 162;
-    const int32_t e0 = blockIdx.x * kGatherTile;
-    const int ne = min(kGatherTile, n_el - e0);
+    double *s_u = s_dn + E::kGatherTile * E::NB;
+    const int32_t e0 = blockIdx.x * E::kGatherTile;
+    const int ne = min(E::kGatherTile, n_el - e0);
     if (threadIdx.x == 0) mbar_init(bar, 1);
     __syncthreads();
     if (threadIdx.x == 0) {
-        const uint32_t bytes = (uint32_t)ne * kElBytes;
+        const uint32_t bytes = (uint32_t)ne * E::NB * 8;
         mbar_expect_tx(bar, bytes);
-        bulk_g2s(s_dn, dphi + (size_t)e0 * 162, bytes, bar);
+        bulk_g2s(s_dn, dphi + (size_t)e0 * E::NB, bytes, bar);
     }
-    for (int k = threadIdx.x; k < ne * 18; k += blockDim.x) s_u[k] = __ldg(&u[__ldg(&dofs[(size_t)e0 * 18 + k])]);
+    for (int k = threadIdx.x; k < ne * E::ND; k += blockDim.x)
+        s_u[k] = __ldg(&u[__ldg(&dofs[(size_t)e0 * E::ND + k])]);
     const bool ok = mbar_wait_bounded(bar, 0);
     __syncthreads();
     if (!ok) {
         if (threadIdx.x == 0) atomicExch(err, 1);
         return;
     }
-    const int el = threadIdx.x / 9, q = threadIdx.x % 9;
+    const int el = threadIdx.x / E::NQ, q = threadIdx.x % E::NQ;
     if (el >= ne) return;
-    const double *dx = s_dn + el * 162 + q * 18;
-    const double *dy = dx + 9;
-    const double *ue = s_u + el * 18;
+    const double *dx = s_dn + el * E::NB + q * 2 * E::NN;
+    const double *dy = dx + E::NN;
+    const double *ue = s_u + el * E::ND;
     double exx = 0.0, gxy = 0.0, eyy = 0.0;
 #pragma unroll
-    for (int n = 0; n < 9; n++) exx = fma(dx[n], ue[2 * n], exx);
+    for (int n = 0; n < E::NN; n++) exx = fma(dx[n], ue[2 * n], exx);
 #pragma unroll
-    for (int n = 0; n < 9; n++) {
+    for (int n = 0; n < E::NN; n++) {
         gxy = fma(dy[n], ue[2 * n], gxy);
         gxy = fma(dx[n], ue[2 * n + 1], gxy);
     }
 #pragma unroll
-    for (int n = 0; n < 9; n++) eyy = fma(dy[n], ue[2 * n + 1], eyy);
-    const int64_t ip = (int64_t)(e0 + el) * 9 + q;
+    for (int n = 0; n < E::NN; n++) eyy = fma(dy[n], ue[2 * n + 1], eyy);
+    const int64_t ip = (int64_t)(e0 + el) * E::NQ + q;
     strain[ip] = exx;
     strain[n_ip + ip] = gxy;
     strain[2 * n_ip + ip] = eyy;
 }
 
-__global__ void __launch_bounds__(kResTile * 18) k_stress_residual(int32_t n_el, int64_t n_ip,
-                                                                   const double *__restrict__ dphi,
-                                                                   const double *__restrict__ sigma_w,
-                                                                   double *__restrict__ fe,
-                                                                   int *__restrict__ err)
+template <int P>
+__global__ void __launch_bounds__(Elem<P>::kResTile * Elem<P>::ND)
+k_stress_residual(int32_t n_el, int64_t n_ip, const double *__restrict__ dphi, const double *__restrict__ sigma_w,
+                  double *__restrict__ fe, int *__restrict__ err)
 {
+    typedef Elem<P> E;
+    constexpr int T = E::kResTile;
     extern __shared__ __align__(128) unsigned char smem[];
     uint64_t *bar = reinterpret_cast<uint64_t *>(smem);
     double *s_dn = reinterpret_cast<double *>(smem + 128);
-    double *s_sig = s_dn + kResTile * 162;            // [3][kResTile*9]
-    const int32_t e0 = blockIdx.x * kResTile;
-    const int ne = min(kResTile, n_el - e0);
+    double *s_sig = s_dn + T * E::NB;                  // [3][T*nq]
+    const int32_t e0 = blockIdx.x * T;
+    const int ne = min(T, n_el - e0);
     if (threadIdx.x == 0) mbar_init(bar, 1);
     __syncthreads();
     if (threadIdx.x == 0) {
-        const uint32_t bytes = (uint32_t)ne * kElBytes;
+        const uint32_t bytes = (uint32_t)ne * E::NB * 8;
         mbar_expect_tx(bar, bytes);
-        bulk_g2s(s_dn, dphi + (size_t)e0 * 162, bytes, bar);
+        bulk_g2s(s_dn, dphi + (size_t)e0 * E::NB, bytes, bar);
     }
-    const int npt = ne * 9;
-    const int64_t ip0 = (int64_t)e0 * 9;
+    const int npt = ne * E::NQ;
+    const int64_t ip0 = (int64_t)e0 * E::NQ;
     for (int k = threadIdx.x; k < 3 * npt; k += blockDim.x) {
         const int cmp = k / npt, i = k - cmp * npt;
-        s_sig[cmp * kResTile * 9 + i] = sigma_w[cmp * n_ip + ip0 + i];
+        s_sig[cmp * T * E::NQ + i] = sigma_w[cmp * n_ip + ip0 + i];
     }
     const bool ok = mbar_wait_bounded(bar, 0);
     __syncthreads();
@@ -107,21 +117,21 @@ __global__ void __launch_bounds__(kResTile * 18) k_stress_residual(int32_t n_el,
         if (threadIdx.x == 0) atomicExch(err, 1);
         return;
     }
-    const int el = threadIdx.x / 18, j = threadIdx.x % 18;
+    const int el = threadIdx.x / E::ND, j = threadIdx.x % E::ND;
     if (el >= ne) return;
     const int n = j >> 1;
-    const double *dn = s_dn + el * 162;
+    const double *dn = s_dn + el * E::NB;
     // x-dof: dNx*sxx + dNy*sxy per point; y-dof: dNx*sxy + dNy*syy.  The two
     // stress rows are selected by pointer so the warp does not diverge.
-    const double *s1 = s_sig + (j & 1) * kResTile * 9 + el * 9;
-    const double *s2 = s1 + kResTile * 9;
+    const double *s1 = s_sig + (j & 1) * T * E::NQ + el * E::NQ;
+    const double *s2 = s1 + T * E::NQ;
     double acc = 0.0;
 #pragma unroll
-    for (int q = 0; q < 9; q++) {
-        acc = fma(dn[q * 18 + n], s1[q], acc);
-        acc = fma(dn[q * 18 + 9 + n], s2[q], acc);
+    for (int q = 0; q < E::NQ; q++) {
+        acc = fma(dn[q * 2 * E::NN + n], s1[q], acc);
+        acc = fma(dn[q * 2 * E::NN + E::NN + n], s2[q], acc);
     }
-    fe[(size_t)(e0 + el) * 18 + j] = -acc;
+    fe[(size_t)(e0 + el) * E::ND + j] = -acc;
 }
 
 // Per node: contributions of the incident element of each colour (0 if none),
@@ -179,49 +189,54 @@ constexpr int kStiffWarps = 4;
 // T = double: the plain tangent (bit-exact with the oracle); T = float: the
 // FP32 tangent of the mixed-precision solve (blocks and w*Dep rounded to FP32,
 // FP32 fma accumulation).
-template <class T>
+template <class T, int P>
 __global__ void __launch_bounds__(kStiffWarps * 32) k_stiffness(int32_t n_in_color, const int32_t *__restrict__ els,
                                                                  int64_t n_ip, const T *__restrict__ dphi,
                                                                  const double *__restrict__ dep,
                                                                  const int32_t *__restrict__ el_blk,
                                                                  T *__restrict__ K)
 {
-    __shared__ __align__(16) T s_dn[kStiffWarps][162];
-    __shared__ T s_D[kStiffWarps][81];        // [q][9]
-    __shared__ T s_DB[kStiffWarps][54];       // [3][18]
+    typedef Elem<P> E;
+    constexpr int NE = E::ND * (E::ND + 1) / 2;   // upper-triangle entries
+    constexpr int MM = (NE + 31) / 32;            // entries per lane
+    __shared__ __align__(16) T s_dn[kStiffWarps][E::NB];
+    __shared__ T s_D[kStiffWarps][E::NQ * 9];    // [q][9]
+    __shared__ T s_DB[kStiffWarps][3 * E::ND];   // [3][nd]
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int32_t k = blockIdx.x * kStiffWarps + w;
     if (k >= n_in_color) return;              // warp-uniform
     const int32_t e = __ldg(&els[k]);
-    const T *dn_g = dphi + (size_t)e * 162;
-    for (int t = lane; t < 162; t += 32) s_dn[w][t] = __ldg(&dn_g[t]);
-    for (int t = lane; t < 81; t += 32) {
-        const int cmp = t / 9, q = t - cmp * 9;
-        s_D[w][q * 9 + cmp] = (T)__ldg(&dep[cmp * n_ip + (int64_t)e * 9 + q]);
+    const T *dn_g = dphi + (size_t)e * E::NB;
+    for (int t = lane; t < E::NB; t += 32) s_dn[w][t] = __ldg(&dn_g[t]);
+    for (int t = lane; t < 9 * E::NQ; t += 32) {
+        const int cmp = t / E::NQ, q = t - cmp * E::NQ;
+        s_D[w][q * 9 + cmp] = (T)__ldg(&dep[cmp * n_ip + (int64_t)e * E::NQ + q]);
     }
     __syncwarp();
     const T *dn = s_dn[w];
     // upper-triangle entries (a <= b, row-major order) owned by this lane
-    int pa[6], pb[6];
+    int pa[MM], pb[MM];
 #pragma unroll
-    for (int m = 0; m < 6; m++) {
+    for (int m = 0; m < MM; m++) {
         int r = lane + 32 * m, a = 0;
-        if (r < 171)
-            while (r >= 18 - a) {
-                r -= 18 - a;
+        if (r < NE)
+            while (r >= E::ND - a) {
+                r -= E::ND - a;
                 a++;
             }
         pa[m] = a;
         pb[m] = a + r;
     }
-    T acc[6] = {T(0), T(0), T(0), T(0), T(0), T(0)};
+    T acc[MM];
+#pragma unroll
+    for (int m = 0; m < MM; m++) acc[m] = T(0);
 #pragma unroll 1
-    for (int q = 0; q < 9; q++) {
+    for (int q = 0; q < E::NQ; q++) {
         const T *D = &s_D[w][q * 9];
-        const T *dx = dn + q * 18, *dy = dx + 9;
-        for (int t = lane; t < 54; t += 32) {
+        const T *dx = dn + q * 2 * E::NN, *dy = dx + E::NN;
+        for (int t = lane; t < 3 * E::ND; t += 32) {
             // x-dof column j: D[i][0] dNx + D[i][1] dNy; y-dof: D[i][1] dNx + D[i][2] dNy
-            const int i = t / 18, j = t - i * 18, n = j >> 1, c0 = 3 * i + (j & 1);
+            const int i = t / E::ND, j = t - i * E::ND, n = j >> 1, c0 = 3 * i + (j & 1);
             T sv = D[c0] * dx[n];
             sv = fma(D[c0 + 1], dy[n], sv);
             s_DB[w][t] = sv;
@@ -229,34 +244,34 @@ __global__ void __launch_bounds__(kStiffWarps * 32) k_stiffness(int32_t n_in_col
         __syncwarp();
         const T *DB = s_DB[w];
 #pragma unroll
-        for (int m = 0; m < 6; m++) {
+        for (int m = 0; m < MM; m++) {
             const int p = lane + 32 * m;
-            if (p < 171) {
+            if (p < NE) {
                 // x-dof row a: dNx DB[0][b] + dNy DB[1][b]; y-dof: dNx DB[1][b] + dNy DB[2][b]
-                const int a = pa[m], b = pb[m], na = a >> 1, o = (a & 1) * 18 + b;
+                const int a = pa[m], b = pb[m], na = a >> 1, o = (a & 1) * E::ND + b;
                 T t = acc[m];
                 t = fma(dx[na], DB[o], t);
-                t = fma(dy[na], DB[o + 18], t);
+                t = fma(dy[na], DB[o + E::ND], t);
                 acc[m] = t;
             }
         }
         __syncwarp();
     }
-    const int32_t *eb = el_blk + (size_t)e * 81;
+    const int32_t *eb = el_blk + (size_t)e * E::NN * E::NN;
 #pragma unroll
-    for (int m = 0; m < 6; m++) {
+    for (int m = 0; m < MM; m++) {
         const int p = lane + 32 * m;
-        if (p < 171) {
+        if (p < NE) {
             const int a = pa[m], b = pb[m];
             const int ma = a >> 1, ca = a & 1, nb = b >> 1, cb = b & 1;
             const T v = acc[m];
             if (ma == nb) {
-                T *blk = K + 4 * (size_t)__ldg(&eb[ma * 9 + ma]);
+                T *blk = K + 4 * (size_t)__ldg(&eb[ma * E::NN + ma]);
                 blk[2 * ca + cb] = blk[2 * ca + cb] + v;
                 if (ca != cb) blk[2 * cb + ca] = blk[2 * cb + ca] + v;
             } else {
-                T *b1 = K + 4 * (size_t)__ldg(&eb[ma * 9 + nb]);
-                T *b2 = K + 4 * (size_t)__ldg(&eb[nb * 9 + ma]);
+                T *b1 = K + 4 * (size_t)__ldg(&eb[ma * E::NN + nb]);
+                T *b2 = K + 4 * (size_t)__ldg(&eb[nb * E::NN + ma]);
                 b1[2 * ca + cb] = b1[2 * ca + cb] + v;
                 b2[2 * cb + ca] = b2[2 * cb + ca] + v;
             }
@@ -275,22 +290,44 @@ __global__ void k_jacobi(int32_t n_nodes, const int64_t *__restrict__ diag, cons
     dinv[2 * (size_t)i + 1] = fixed[2 * (size_t)i + 1] ? T(0) : T(1) / blk[3];
 }
 
+template <int P>
+static void gather_strain_p(ipfem_ctx *c, const double *d_u, double *d_strain)
+{
+    typedef Elem<P> E;
+    const Setup &s = c->s;
+    const unsigned grid = (unsigned)((s.n_el + E::kGatherTile - 1) / E::kGatherTile);
+    const size_t smem = 128 + (size_t)E::kGatherTile * (E::NB + E::ND) * 8;
+    k_gather_strain<P><<<grid, E::kGatherTile * E::NQ, smem, c->stream>>>(s.n_el, s.n_ip, c->d_dphi, c->d_dofs,
+                                                                           d_u, d_strain, c->d_err);
+}
+
 void launch_gather_strain(ipfem_ctx *c, const double *d_u, double *d_strain)
 {
+    switch (c->s.order) {
+    case 1: gather_strain_p<1>(c, d_u, d_strain); break;
+    case 3: gather_strain_p<3>(c, d_u, d_strain); break;
+    default: gather_strain_p<2>(c, d_u, d_strain); break;
+    }
+}
+
+template <int P>
+static void stress_residual_p(ipfem_ctx *c, const double *d_sigma_w, double *d_fe)
+{
+    typedef Elem<P> E;
     const Setup &s = c->s;
-    const unsigned grid = (unsigned)((s.n_el + kGatherTile - 1) / kGatherTile);
-    const size_t smem = 128 + kGatherTile * 162 * 8 + kGatherTile * 18 * 8;
-    k_gather_strain<<<grid, kGatherTile * 9, smem, c->stream>>>(s.n_el, s.n_ip, c->d_dphi, c->d_dofs, d_u,
-                                                                d_strain, c->d_err);
+    const unsigned grid = (unsigned)((s.n_el + E::kResTile - 1) / E::kResTile);
+    const size_t smem = 128 + (size_t)E::kResTile * (E::NB + 3 * E::NQ) * 8;
+    k_stress_residual<P><<<grid, E::kResTile * E::ND, smem, c->stream>>>(s.n_el, s.n_ip, c->d_dphi, d_sigma_w,
+                                                                          d_fe, c->d_err);
 }
 
 void launch_stress_residual(ipfem_ctx *c, const double *d_sigma_w, double *d_fe)
 {
-    const Setup &s = c->s;
-    const unsigned grid = (unsigned)((s.n_el + kResTile - 1) / kResTile);
-    const size_t smem = 128 + kResTile * 162 * 8 + 3 * kResTile * 9 * 8;
-    k_stress_residual<<<grid, kResTile * 18, smem, c->stream>>>(s.n_el, s.n_ip, c->d_dphi, d_sigma_w, d_fe,
-                                                                c->d_err);
+    switch (c->s.order) {
+    case 1: stress_residual_p<1>(c, d_sigma_w, d_fe); break;
+    case 3: stress_residual_p<3>(c, d_sigma_w, d_fe); break;
+    default: stress_residual_p<2>(c, d_sigma_w, d_fe); break;
+    }
 }
 
 void launch_color_reduce(ipfem_ctx *c, const double *d_fe, double lambda, int with_load, double *d_res)
@@ -309,8 +346,10 @@ void launch_stiffness(ipfem_ctx *c)
         const int32_t first = s.color_ptr[col], n = s.color_ptr[col + 1] - first;
         if (n == 0) continue;
         const unsigned grid = (unsigned)((n + kStiffWarps - 1) / kStiffWarps);
-        k_stiffness<double><<<grid, kStiffWarps * 32, 0, c->stream>>>(n, c->d_color_els + first, s.n_ip, c->d_dphi,
-                                                                      c->d_dep, c->dsell.el_blk, c->d_K);
+        auto kern = s.order == 1 ? k_stiffness<double, 1> : (s.order == 3 ? k_stiffness<double, 3> :
+                                                                            k_stiffness<double, 2>);
+        kern<<<grid, kStiffWarps * 32, 0, c->stream>>>(n, c->d_color_els + first, s.n_ip, c->d_dphi, c->d_dep,
+                                                       c->dsell.el_blk, c->d_K);
     }
     const unsigned g2 = (unsigned)((s.n_nodes + 255) / 256);
     k_jacobi<double><<<g2, 256, 0, c->stream>>>(s.n_nodes, c->dsell.diag_blk, c->d_K, c->d_fixed, c->d_dinv);
@@ -325,8 +364,10 @@ void launch_stiffness32(ipfem_ctx *c)
         const int32_t first = s.color_ptr[col], n = s.color_ptr[col + 1] - first;
         if (n == 0) continue;
         const unsigned grid = (unsigned)((n + kStiffWarps - 1) / kStiffWarps);
-        k_stiffness<float><<<grid, kStiffWarps * 32, 0, c->stream>>>(n, c->d_color_els + first, s.n_ip, m.dphi,
-                                                                     c->d_dep, m.dsell.el_blk, m.K);
+        auto kern = s.order == 1 ? k_stiffness<float, 1> : (s.order == 3 ? k_stiffness<float, 3> :
+                                                                           k_stiffness<float, 2>);
+        kern<<<grid, kStiffWarps * 32, 0, c->stream>>>(n, c->d_color_els + first, s.n_ip, m.dphi, c->d_dep,
+                                                       m.dsell.el_blk, m.K);
     }
     const unsigned g2 = (unsigned)((s.n_nodes + 255) / 256);
     k_jacobi<float><<<g2, 256, 0, c->stream>>>(s.n_nodes, m.dsell.diag_blk, m.K, c->d_fixed, m.dinv);

@@ -8,7 +8,7 @@
 namespace ipfem {
 
 template <bool DEP, bool UPD>
-__global__ void __launch_bounds__(128) k_compute_sigma(int64_t n_ip, int32_t n_el, ElasticConst E,
+__global__ void __launch_bounds__(128) k_compute_sigma(int64_t n_ip, int32_t n_el, int32_t npts, ElasticConst E,
                                                        const double *__restrict__ strain,
                                                        const double *__restrict__ weight,
                                                        const double *__restrict__ mat,
@@ -21,7 +21,7 @@ __global__ void __launch_bounds__(128) k_compute_sigma(int64_t n_ip, int32_t n_e
 {
     const int64_t ip = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (ip >= n_ip) return;
-    const int64_t e = ip / IPFEM_NPTS;
+    const int64_t e = ip / npts;
     MCConst m;
     m.c = __ldg(&mat[e]);
     m.sinphi = __ldg(&mat[n_el + e]);
@@ -61,7 +61,7 @@ void launch_compute_sigma(ipfem_ctx *c, int update_mem, const double *d_strain, 
     const int tpb = 128;
     const unsigned grid = (unsigned)((s.n_ip + tpb - 1) / tpb);
     if (grid == 0) return;
-#define ARGS s.n_ip, s.n_el, E, d_strain, c->d_weight, c->d_mat, c->d_eps_p, d_sigma_w, d_dep, c->d_sigma, \
+#define ARGS s.n_ip, s.n_el, s.nq, E, d_strain, c->d_weight, c->d_mat, c->d_eps_p, d_sigma_w, d_dep, c->d_sigma, \
              c->d_mtype, c->d_alpha
     if (d_dep) {
         if (update_mem) k_compute_sigma<true, true><<<grid, tpb, 0, c->stream>>>(ARGS);

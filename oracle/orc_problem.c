@@ -101,7 +101,7 @@ void orc_vertex_coords(const orc_params *prm, double *vxy)
     free(r);
 }
 
-/* reference coordinates of the 9 connects (PZ quad order) */
+/* reference coordinates of the 9 connects of order 2 (PZ quad order) */
 static const int ref_a[9] = {-1, 1, 1, -1, 0, 1, 0, -1, 0};
 static const int ref_b[9] = {-1, -1, 1, 1, -1, 0, 1, 0, 0};
 
@@ -119,23 +119,95 @@ static double dlag(int a, double x)
     return x + 0.5;
 }
 
-void orc_element_blocks(int32_t n_el, const int32_t *connects, const double *node_xy,
+/* 1-D Lagrange function a of order p on the equispaced nodes t_m = -1 + 2m/p
+ * and its derivative (orders 1 and 3; order 2 uses lag/dlag above) */
+static double lagp(int p, int a, double x)
+{
+    const double ta = -1.0 + 2.0 * a / p;
+    double num = 1.0, den = 1.0;
+    for (int m = 0; m <= p; m++) {
+        if (m == a) continue;
+        const double tm = -1.0 + 2.0 * m / p;
+        num = num * (x - tm);
+        den = den * (ta - tm);
+    }
+    return num / den;
+}
+
+static double dlagp(int p, int a, double x)
+{
+    const double ta = -1.0 + 2.0 * a / p;
+    double s = 0.0;
+    for (int k = 0; k <= p; k++) {
+        if (k == a) continue;
+        const double tk = -1.0 + 2.0 * k / p;
+        double prod = 1.0 / (ta - tk);
+        for (int m = 0; m <= p; m++) {
+            if (m == a || m == k) continue;
+            const double tm = -1.0 + 2.0 * m / p;
+            prod = prod * ((x - tm) / (ta - tm));
+        }
+        s = s + prod;
+    }
+    return s;
+}
+
+/* index-space position (a, b) in [0, p]^2 of connect n of an order-p element */
+static void ref_node(int p, int n, int *a, int *b)
+{
+    const int vx[4] = {0, p, p, 0}, vy[4] = {0, 0, p, p};
+    if (n < 4) { *a = vx[n]; *b = vy[n]; return; }
+    n -= 4;
+    if (n < 4 * (p - 1)) {
+        const int e = n / (p - 1), k = n % (p - 1) + 1;
+        if (e == 0) { *a = k; *b = 0; }
+        else if (e == 1) { *a = p; *b = k; }
+        else if (e == 2) { *a = p - k; *b = p; }
+        else { *a = 0; *b = p - k; }
+        return;
+    }
+    n -= 4 * (p - 1);
+    *a = n % (p - 1) + 1;
+    *b = n / (p - 1) + 1;
+}
+
+/* Gauss points and weights, p + 1 per direction */
+static void gauss(int p, double *gp, double *gw)
+{
+    if (p == 1) {
+        const double g = 1.0 / sqrt(3.0);
+        gp[0] = -g; gp[1] = g;
+        gw[0] = 1.0; gw[1] = 1.0;
+    } else if (p == 2) {
+        const double g = sqrt(0.6);
+        gp[0] = -g; gp[1] = 0.0; gp[2] = g;
+        gw[0] = 5.0 / 9.0; gw[1] = 8.0 / 9.0; gw[2] = 5.0 / 9.0;
+    } else {
+        const double a = sqrt(3.0 / 7.0 - 2.0 / 7.0 * sqrt(6.0 / 5.0));
+        const double b = sqrt(3.0 / 7.0 + 2.0 / 7.0 * sqrt(6.0 / 5.0));
+        const double wa = (18.0 + sqrt(30.0)) / 36.0, wb = (18.0 - sqrt(30.0)) / 36.0;
+        gp[0] = -b; gp[1] = -a; gp[2] = a; gp[3] = b;
+        gw[0] = wb; gw[1] = wa; gw[2] = wa; gw[3] = wb;
+    }
+}
+
+void orc_element_blocks(int32_t order, int32_t n_el, const int32_t *connects, const double *node_xy,
                         double *B, double *weight)
 {
-    const double g = sqrt(0.6);
-    const double gp[3] = {-g, 0.0, g};
-    const double gw[3] = {5.0 / 9.0, 8.0 / 9.0, 5.0 / 9.0};
+    const int p = order, n1 = p + 1, nn = n1 * n1, nq = n1 * n1, nd = 2 * nn, nb = 3 * nq * nd;
+    double gp[4], gw[4];
+    gauss(p, gp, gw);
 #pragma omp parallel for schedule(static)
     for (int32_t e = 0; e < n_el; e++) {
         double X[4], Y[4];
         for (int v = 0; v < 4; v++) {
-            X[v] = node_xy[2 * (size_t)connects[9 * (size_t)e + v]];
-            Y[v] = node_xy[2 * (size_t)connects[9 * (size_t)e + v] + 1];
+            X[v] = node_xy[2 * (size_t)connects[(size_t)nn * e + v]];
+            Y[v] = node_xy[2 * (size_t)connects[(size_t)nn * e + v] + 1];
         }
-        double *Be = &B[(size_t)e * 486];
-        memset(Be, 0, 486 * sizeof(double));
-        for (int iq = 0; iq < 9; iq++) {
-            const int ix = iq % 3, iy = iq / 3;
+        double *Be = &B[(size_t)e * nb];
+        memset(Be, 0, (size_t)nb * sizeof(double));
+        for (int iq = 0; iq < nq; iq++) {
+            const int ix = iq % n1, iy = iq / n1;
             const double xi = gp[ix], eta = gp[iy];
             const double dpx[4] = {-(1.0 - eta) / 4.0, (1.0 - eta) / 4.0, (1.0 + eta) / 4.0, -(1.0 + eta) / 4.0};
             const double dpe[4] = {-(1.0 - xi) / 4.0, -(1.0 + xi) / 4.0, (1.0 + xi) / 4.0, (1.0 - xi) / 4.0};
@@ -150,13 +222,21 @@ void orc_element_blocks(int32_t n_el, const int32_t *connects, const double *nod
             const double det = x_xi * y_eta - x_eta * y_xi;
             const double xi_x = y_eta / det, xi_y = -x_eta / det;
             const double eta_x = -y_xi / det, eta_y = x_xi / det;
-            weight[(size_t)e * 9 + iq] = (gw[ix] * gw[iy]) * fabs(det);
-            double *r0 = &Be[(3 * iq + 0) * 18];
-            double *r1 = &Be[(3 * iq + 1) * 18];
-            double *r2 = &Be[(3 * iq + 2) * 18];
-            for (int n = 0; n < 9; n++) {
-                const double Nxi = dlag(ref_a[n], xi) * lag(ref_b[n], eta);
-                const double Neta = lag(ref_a[n], xi) * dlag(ref_b[n], eta);
+            weight[(size_t)e * nq + iq] = (gw[ix] * gw[iy]) * fabs(det);
+            double *r0 = &Be[(3 * iq + 0) * nd];
+            double *r1 = &Be[(3 * iq + 1) * nd];
+            double *r2 = &Be[(3 * iq + 2) * nd];
+            for (int n = 0; n < nn; n++) {
+                double Nxi, Neta;
+                if (p == 2) {
+                    Nxi = dlag(ref_a[n], xi) * lag(ref_b[n], eta);
+                    Neta = lag(ref_a[n], xi) * dlag(ref_b[n], eta);
+                } else {
+                    int a, b;
+                    ref_node(p, n, &a, &b);
+                    Nxi = dlagp(p, a, xi) * lagp(p, b, eta);
+                    Neta = lagp(p, a, xi) * dlagp(p, b, eta);
+                }
                 const double dNx = Nxi * xi_x + Neta * eta_x;
                 const double dNy = Nxi * xi_y + Neta * eta_y;
                 r0[2 * n] = dNx;
@@ -168,7 +248,8 @@ void orc_element_blocks(int32_t n_el, const int32_t *connects, const double *nod
     }
 }
 
-int32_t orc_greedy_coloring(int32_t n_el, int32_t n_nodes, const int32_t *connects, int32_t *el_color)
+int32_t orc_greedy_coloring_n(int32_t n_el, int32_t n_nodes, int32_t nn, const int32_t *connects,
+                              int32_t *el_color)
 {
     uint8_t *mark = (uint8_t *)xcalloc((size_t)n_nodes, 1);
     for (int32_t e = 0; e < n_el; e++) el_color[e] = -1;
@@ -178,19 +259,24 @@ int32_t orc_greedy_coloring(int32_t n_el, int32_t n_nodes, const int32_t *connec
         again = 0;
         for (int32_t e = 0; e < n_el; e++) {
             if (el_color[e] != -1) continue;
-            const int32_t *c = &connects[9 * (size_t)e];
+            const int32_t *c = &connects[(size_t)nn * e];
             int k;
-            for (k = 0; k < 9; k++)
+            for (k = 0; k < nn; k++)
                 if (mark[c[k]]) break;
-            if (k != 9) { again = 1; continue; }
+            if (k != nn) { again = 1; continue; }
             el_color[e] = color;
-            for (k = 0; k < 9; k++) mark[c[k]] = 1;
+            for (k = 0; k < nn; k++) mark[c[k]] = 1;
         }
         color++;
         memset(mark, 0, (size_t)n_nodes);
     }
     free(mark);
     return color;
+}
+
+int32_t orc_greedy_coloring(int32_t n_el, int32_t n_nodes, const int32_t *connects, int32_t *el_color)
+{
+    return orc_greedy_coloring_n(n_el, n_nodes, 9, connects, el_color);
 }
 
 static int cmp_i32(const void *a, const void *b)
@@ -233,7 +319,10 @@ orc_problem *orc_problem_create(const orc_params *prm, int nthreads)
     p->n_el = nr * nt;
     p->n_nodes = gr * gt;
     p->neq = 2 * p->n_nodes;
-    p->n_ip = (int64_t)p->n_el * ORC_NPTS;
+    p->order = 2;
+    p->nn = p->nq = 9;
+    p->nd = 18;
+    p->n_ip = (int64_t)p->n_el * p->nq;
 
     /* nodes: vertex grid, then edge / centre nodes on the bilinear map */
     double *vxy = (double *)xcalloc((size_t)(nr + 1) * (nt + 1) * 2, sizeof(double));
@@ -302,9 +391,9 @@ orc_problem *orc_problem_create(const orc_params *prm, int nthreads)
     return p;
 }
 
-/* The same problem on a caller's order-2 quadrilateral mesh (connect order of
- * each element: 4 vertices, 4 edge midpoints, centre; bilinear geometry from
- * the vertices): material, in-situ seed, setup and state as above. */
+/* The same problem on a caller's quadrilateral mesh of order 1, 2 or 3
+ * (connect order as in orc_problem.h; bilinear geometry from the vertices):
+ * material, in-situ seed, setup and state as above. */
 orc_problem *orc_problem_from_mesh(const orc_mesh_in *m, const orc_params *prm, int nthreads)
 {
     if (nthreads > 0) omp_set_num_threads(nthreads);
@@ -314,11 +403,14 @@ orc_problem *orc_problem_from_mesh(const orc_mesh_in *m, const orc_params *prm, 
     p->n_el = m->n_el;
     p->n_nodes = m->n_nodes;
     p->neq = 2 * m->n_nodes;
-    p->n_ip = (int64_t)p->n_el * ORC_NPTS;
+    p->order = m->order > 0 ? m->order : 2;
+    p->nn = p->nq = (p->order + 1) * (p->order + 1);
+    p->nd = 2 * p->nn;
+    p->n_ip = (int64_t)p->n_el * p->nq;
     p->node_xy = (double *)xcalloc((size_t)p->n_nodes * 2, sizeof(double));
     memcpy(p->node_xy, m->node_xy, (size_t)p->n_nodes * 2 * sizeof(double));
-    p->connects = (int32_t *)xcalloc((size_t)p->n_el * 9, sizeof(int32_t));
-    memcpy(p->connects, m->connects, (size_t)p->n_el * 9 * sizeof(int32_t));
+    p->connects = (int32_t *)xcalloc((size_t)p->n_el * p->nn, sizeof(int32_t));
+    memcpy(p->connects, m->connects, (size_t)p->n_el * p->nn * sizeof(int32_t));
     p->fixed = (uint8_t *)xcalloc((size_t)p->neq, 1);
     if (m->fixed) memcpy(p->fixed, m->fixed, (size_t)p->neq);
     p->f0 = (double *)xcalloc((size_t)p->neq, sizeof(double));
@@ -371,16 +463,17 @@ static void problem_setup(orc_problem *p, const orc_params *prm)
         for (int k = 0; k < 6; k++) p->eps_p0[k] = -e6[k];
     }
     /* setup: B blocks, weights, dof map, colouring */
-    p->B = (double *)xcalloc((size_t)p->n_el * 486, sizeof(double));
+    const int nn = p->nn, nd = p->nd;
+    p->B = (double *)xcalloc((size_t)p->n_el * 3 * p->nq * nd, sizeof(double));
     p->weight = (double *)xcalloc((size_t)p->n_ip, sizeof(double));
-    orc_element_blocks(p->n_el, p->connects, p->node_xy, p->B, p->weight);
-    p->dofs = (int32_t *)xcalloc((size_t)p->n_el * 18, sizeof(int32_t));
-    for (size_t k = 0; k < (size_t)p->n_el * 9; k++) {
+    orc_element_blocks(p->order, p->n_el, p->connects, p->node_xy, p->B, p->weight);
+    p->dofs = (int32_t *)xcalloc((size_t)p->n_el * nd, sizeof(int32_t));
+    for (size_t k = 0; k < (size_t)p->n_el * nn; k++) {
         p->dofs[2 * k] = 2 * p->connects[k];
         p->dofs[2 * k + 1] = 2 * p->connects[k] + 1;
     }
     p->el_color = (int32_t *)xcalloc((size_t)p->n_el, sizeof(int32_t));
-    p->n_colors = orc_greedy_coloring(p->n_el, p->n_nodes, p->connects, p->el_color);
+    p->n_colors = orc_greedy_coloring_n(p->n_el, p->n_nodes, nn, p->connects, p->el_color);
     p->color_ptr = (int32_t *)xcalloc((size_t)p->n_colors + 1, sizeof(int32_t));
     p->color_els = (int32_t *)xcalloc((size_t)p->n_el, sizeof(int32_t));
     for (int32_t e = 0; e < p->n_el; e++) p->color_ptr[p->el_color[e] + 1]++;
@@ -398,14 +491,14 @@ static void problem_setup(orc_problem *p, const orc_params *prm)
         int32_t *deg = (int32_t *)xcalloc((size_t)p->n_nodes, sizeof(int32_t));
         int32_t *cnt = (int32_t *)xcalloc((size_t)p->n_nodes, sizeof(int32_t));
         for (int32_t e = 0; e < p->n_el; e++)
-            for (int m = 0; m < 9; m++) cnt[p->connects[9 * (size_t)e + m]] += 9;
+            for (int m = 0; m < nn; m++) cnt[p->connects[(size_t)nn * e + m]] += nn;
         int64_t *cap = (int64_t *)xcalloc((size_t)p->n_nodes + 1, sizeof(int64_t));
         for (int32_t i = 0; i < p->n_nodes; i++) cap[i + 1] = cap[i] + cnt[i];
         int32_t *tmp = (int32_t *)xcalloc((size_t)cap[p->n_nodes], sizeof(int32_t));
         for (int32_t e = 0; e < p->n_el; e++)
-            for (int m = 0; m < 9; m++) {
-                int32_t r = p->connects[9 * (size_t)e + m];
-                for (int n = 0; n < 9; n++) tmp[cap[r] + deg[r]++] = p->connects[9 * (size_t)e + n];
+            for (int m = 0; m < nn; m++) {
+                int32_t r = p->connects[(size_t)nn * e + m];
+                for (int n = 0; n < nn; n++) tmp[cap[r] + deg[r]++] = p->connects[(size_t)nn * e + n];
             }
         p->row_ptr = (int64_t *)xcalloc((size_t)p->n_nodes + 1, sizeof(int64_t));
         for (int32_t i = 0; i < p->n_nodes; i++) {
@@ -422,19 +515,19 @@ static void problem_setup(orc_problem *p, const orc_params *prm)
         for (int32_t i = 0; i < p->n_nodes; i++)
             memcpy(&p->col[p->row_ptr[i]], &tmp[cap[i]], (size_t)deg[i] * sizeof(int32_t));
         free(tmp); free(cap); free(cnt); free(deg);
-        p->el_blk = (int64_t *)xcalloc((size_t)p->n_el * 81, sizeof(int64_t));
+        p->el_blk = (int64_t *)xcalloc((size_t)p->n_el * nn * nn, sizeof(int64_t));
 #pragma omp parallel for schedule(static)
         for (int32_t e = 0; e < p->n_el; e++)
-            for (int m = 0; m < 9; m++) {
-                int32_t r = p->connects[9 * (size_t)e + m];
-                for (int n = 0; n < 9; n++) {
-                    int32_t c = p->connects[9 * (size_t)e + n];
+            for (int m = 0; m < nn; m++) {
+                int32_t r = p->connects[(size_t)nn * e + m];
+                for (int n = 0; n < nn; n++) {
+                    int32_t c = p->connects[(size_t)nn * e + n];
                     int64_t lo = p->row_ptr[r], hi = p->row_ptr[r + 1] - 1;
                     while (lo < hi) {
                         int64_t mid = (lo + hi) / 2;
                         if (p->col[mid] < c) lo = mid + 1; else hi = mid;
                     }
-                    p->el_blk[(size_t)e * 81 + m * 9 + n] = lo;
+                    p->el_blk[((size_t)e * nn + m) * nn + n] = lo;
                 }
             }
     }
@@ -534,13 +627,14 @@ void orc_gather_strain(const orc_problem *p, const double *u, double *strain)
 {
 #pragma omp parallel for schedule(static)
     for (int32_t e = 0; e < p->n_el; e++) {
-        double ue[18];
-        for (int j = 0; j < 18; j++) ue[j] = u[p->dofs[18 * (size_t)e + j]];
-        const double *Be = &p->B[(size_t)e * 486];
-        for (int r = 0; r < 27; r++) {
+        const int nd = p->nd, nr = 3 * p->nq;
+        double ue[32];
+        for (int j = 0; j < nd; j++) ue[j] = u[p->dofs[(size_t)nd * e + j]];
+        const double *Be = &p->B[(size_t)e * nr * nd];
+        for (int r = 0; r < nr; r++) {
             double acc = 0.0;
-            for (int j = 0; j < 18; j++) acc = fma(Be[r * 18 + j], ue[j], acc);
-            strain[(size_t)e * 27 + r] = acc;
+            for (int j = 0; j < nd; j++) acc = fma(Be[r * nd + j], ue[j], acc);
+            strain[(size_t)e * nr + r] = acc;
         }
     }
 }
@@ -552,13 +646,14 @@ void orc_scatter_residual(const orc_problem *p, const double *sigma_w, double *r
     double *slab = (double *)xcalloc((size_t)nc * neq, sizeof(double));
 #pragma omp parallel for schedule(static)
     for (int32_t e = 0; e < p->n_el; e++) {
-        const double *Be = &p->B[(size_t)e * 486];
-        const double *s = &sigma_w[(size_t)e * 27];
+        const int nd = p->nd, nr = 3 * p->nq;
+        const double *Be = &p->B[(size_t)e * nr * nd];
+        const double *s = &sigma_w[(size_t)e * nr];
         double *sl = &slab[(size_t)p->el_color[e] * neq];
-        for (int j = 0; j < 18; j++) {
+        for (int j = 0; j < nd; j++) {
             double acc = 0.0;
-            for (int r = 0; r < 27; r++) acc = fma(Be[r * 18 + j], s[r], acc);
-            sl[p->dofs[18 * (size_t)e + j]] = -acc;
+            for (int r = 0; r < nr; r++) acc = fma(Be[r * nd + j], s[r], acc);
+            sl[p->dofs[(size_t)nd * e + j]] = -acc;
         }
     }
     int64_t ncol = nc, ca = nc / 2;
@@ -586,7 +681,7 @@ static void finish_rhs(const orc_problem *p, double lambda, double *rhs)
 void orc_assemble_residual(orc_problem *p, const double *u, double lambda, int update_mem, double *rhs)
 {
     orc_gather_strain(p, u, p->strain);
-    orc_compute_sigma_batch(p->n_ip, ORC_NPTS, &p->el, p->mats, p->strain, p->eps_p, p->weight,
+    orc_compute_sigma_batch(p->n_ip, p->nq, &p->el, p->mats, p->strain, p->eps_p, p->weight,
                             update_mem, p->sigma_w, 0, p->sigma, p->mtype, p->alpha);
     orc_scatter_residual(p, p->sigma_w, rhs);
     finish_rhs(p, lambda, rhs);
@@ -595,7 +690,7 @@ void orc_assemble_residual(orc_problem *p, const double *u, double lambda, int u
 void orc_assemble(orc_problem *p, const double *u, double lambda, double *rhs)
 {
     orc_gather_strain(p, u, p->strain);
-    orc_compute_sigma_batch(p->n_ip, ORC_NPTS, &p->el, p->mats, p->strain, p->eps_p, p->weight,
+    orc_compute_sigma_batch(p->n_ip, p->nq, &p->el, p->mats, p->strain, p->eps_p, p->weight,
                             0, p->sigma_w, p->dep, 0, 0, 0);
     orc_scatter_residual(p, p->sigma_w, rhs);
     finish_rhs(p, lambda, rhs);
@@ -604,41 +699,42 @@ void orc_assemble(orc_problem *p, const double *u, double lambda, double *rhs)
 #pragma omp parallel for schedule(static)
         for (int32_t k = p->color_ptr[c]; k < p->color_ptr[c + 1]; k++) {
             const int32_t e = p->color_els[k];
-            const double *Be = &p->B[(size_t)e * 486];
-            double Kl[18][18];
+            const int nn = p->nn, nq = p->nq, nd = p->nd;
+            const double *Be = &p->B[(size_t)e * 3 * nq * nd];
+            double Kl[32][32];
             memset(Kl, 0, sizeof Kl);
-            for (int q = 0; q < 9; q++) {
-                const double *Bq = &Be[q * 54];
-                const double *D = &p->dep[((size_t)e * 9 + q) * 9];
-                double DB[3][18];
+            for (int q = 0; q < nq; q++) {
+                const double *Bq = &Be[q * 3 * nd];
+                const double *D = &p->dep[((size_t)e * nq + q) * 9];
+                double DB[3][32];
                 for (int i = 0; i < 3; i++)
-                    for (int j = 0; j < 18; j++) {
-                        double s = D[3 * i + 0] * Bq[0 * 18 + j];
-                        s = fma(D[3 * i + 1], Bq[1 * 18 + j], s);
-                        s = fma(D[3 * i + 2], Bq[2 * 18 + j], s);
+                    for (int j = 0; j < nd; j++) {
+                        double s = D[3 * i + 0] * Bq[0 * nd + j];
+                        s = fma(D[3 * i + 1], Bq[1 * nd + j], s);
+                        s = fma(D[3 * i + 2], Bq[2 * nd + j], s);
                         DB[i][j] = s;
                     }
-                for (int a = 0; a < 18; a++)
-                    for (int b = a; b < 18; b++) {
+                for (int a = 0; a < nd; a++)
+                    for (int b = a; b < nd; b++) {
                         double t = Kl[a][b];
-                        t = fma(Bq[0 * 18 + a], DB[0][b], t);
-                        t = fma(Bq[1 * 18 + a], DB[1][b], t);
-                        t = fma(Bq[2 * 18 + a], DB[2][b], t);
+                        t = fma(Bq[0 * nd + a], DB[0][b], t);
+                        t = fma(Bq[1 * nd + a], DB[1][b], t);
+                        t = fma(Bq[2 * nd + a], DB[2][b], t);
                         Kl[a][b] = t;
                     }
             }
-            const int64_t *eb = &p->el_blk[(size_t)e * 81];
-            for (int a = 0; a < 18; a++)
-                for (int b = a; b < 18; b++) {
+            const int64_t *eb = &p->el_blk[(size_t)e * nn * nn];
+            for (int a = 0; a < nd; a++)
+                for (int b = a; b < nd; b++) {
                     const int m = a / 2, ca = a % 2, n = b / 2, cb = b % 2;
                     const double v = Kl[a][b];
                     if (m == n) {
-                        double *blk = &p->K[4 * eb[m * 9 + m]];
+                        double *blk = &p->K[4 * eb[m * nn + m]];
                         blk[2 * ca + cb] = blk[2 * ca + cb] + v;
                         if (ca != cb) blk[2 * cb + ca] = blk[2 * cb + ca] + v;
                     } else {
-                        double *b1 = &p->K[4 * eb[m * 9 + n]];
-                        double *b2 = &p->K[4 * eb[n * 9 + m]];
+                        double *b1 = &p->K[4 * eb[m * nn + n]];
+                        double *b2 = &p->K[4 * eb[n * nn + m]];
                         b1[2 * ca + cb] = b1[2 * ca + cb] + v;
                         b2[2 * cb + ca] = b2[2 * cb + ca] + v;
                     }

@@ -13,9 +13,14 @@
 extern "C" {
 #endif
 
-#define ORC_NPTS 9      /* 3x3 Gauss points per quadratic quad */
-#define ORC_NNODE 9     /* Q2 nodes (connects) per element */
-#define ORC_NDOF 18     /* element dofs */
+/* Element order p (1, 2, 3): (p+1)^2 connects and (p+1)^2 Gauss points per
+ * quadrilateral, 2 (p+1)^2 dofs; the wellbore provider builds order 2.
+ * Connect order of an element: 4 vertices, the p-1 nodes of each edge in the
+ * element's traversal direction (edges v0v1, v1v2, v2v3, v3v0), interior
+ * nodes row by row. */
+#define ORC_NPTS 9      /* order 2: 3x3 Gauss points */
+#define ORC_NNODE 9     /* order 2: connects per element */
+#define ORC_NDOF 18     /* order 2: element dofs */
 
 typedef struct {
     int32_t nr, nt;            /* elements in radial / angular direction */
@@ -37,16 +42,16 @@ typedef struct {
     int64_t n_ip;
     /* mesh provider (stand-in for the NeoPZ geometric/computational mesh) */
     double *node_xy;           /* [n_nodes*2] */
-    int32_t *connects;         /* [n_el*9] connect order: 4 vertices, 4 edges, centre */
+    int32_t *connects;         /* [n_el*nn] connect order: vertices, edge nodes, interior */
     uint8_t *fixed;            /* [neq] strong Dirichlet dofs */
     double *f0, *df;           /* [neq] external load = f0 + lambda*df */
     orc_elastic el;
     orc_mc *mats;              /* [n_el] */
     double *eps_p0;            /* [6] in-situ plastic-strain seed -C^{-1} sigma0 */
     /* setup (TPZNumericalIntegrator::SetUp*) */
-    double *B;                 /* [n_el*27*18] row-major element blocks (fStorage) */
+    double *B;                 /* [n_el*(3 nq)*nd] row-major element blocks (fStorage) */
     double *weight;            /* [n_ip] */
-    int32_t *dofs;             /* [n_el*18] fDoFIndexes */
+    int32_t *dofs;             /* [n_el*nd] fDoFIndexes */
     int32_t n_colors;
     int32_t *el_color;         /* [n_el] */
     int32_t *color_ptr;        /* [n_colors+1] */
@@ -55,7 +60,7 @@ typedef struct {
     int64_t n_blocks;
     int64_t *row_ptr;          /* [n_nodes+1] */
     int32_t *col;              /* [n_blocks] ascending per row */
-    int64_t *el_blk;           /* [n_el*81] block index of local node pair (m,n) */
+    int64_t *el_blk;           /* [n_el*nn*nn] block index of local node pair (m,n) */
     /* state at integration points (committed) */
     double *eps_p;             /* [n_ip*6] */
     double *sigma;             /* [n_ip*6] */
@@ -68,6 +73,7 @@ typedef struct {
     double *K;                 /* [n_blocks*4] */
     double *dinv;              /* [neq] */
     int nthreads;
+    int32_t order, nn, nq, nd; /* element order; connects, points, dofs per element */
 } orc_problem;
 
 orc_problem *orc_problem_create(const orc_params *prm, int nthreads);
@@ -79,6 +85,7 @@ typedef struct {
     const int32_t *connects;   /* [n_el*9] */
     const uint8_t *fixed;      /* [2*n_nodes] or NULL */
     const double *f0, *df;     /* [2*n_nodes] or NULL */
+    int32_t order;             /* 1, 2 or 3 (0 = 2) */
 } orc_mesh_in;
 orc_problem *orc_problem_from_mesh(const orc_mesh_in *m, const orc_params *prm, int nthreads);
 void orc_problem_destroy(orc_problem *p);
@@ -86,7 +93,7 @@ void orc_default_params(orc_params *prm, int n);
 
 /* setup pieces (exposed for tests) */
 void orc_vertex_coords(const orc_params *prm, double *vxy);
-void orc_element_blocks(int32_t n_el, const int32_t *connects, const double *node_xy,
+void orc_element_blocks(int32_t order, int32_t n_el, const int32_t *connects, const double *node_xy,
                         double *B, double *weight);
 int32_t orc_greedy_coloring(int32_t n_el, int32_t n_nodes, const int32_t *connects, int32_t *el_color);
 

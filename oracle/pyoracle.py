@@ -42,7 +42,8 @@ class Problem(C.Structure):
                 ("el_color", _ip), ("color_ptr", _ip), ("color_els", _ip), ("n_blocks", C.c_int64),
                 ("row_ptr", _lp), ("col", _ip), ("el_blk", _lp), ("eps_p", _dp), ("sigma", _dp),
                 ("mtype", C.POINTER(C.c_int8)), ("alpha", _dp), ("strain", _dp), ("sigma_w", _dp),
-                ("dep", _dp), ("K", _dp), ("dinv", _dp), ("nthreads", C.c_int)]
+                ("dep", _dp), ("K", _dp), ("dinv", _dp), ("nthreads", C.c_int), ("order", C.c_int32),
+                ("nn", C.c_int32), ("nq", C.c_int32), ("nd", C.c_int32)]
 
 
 class SolveOpts(C.Structure):
@@ -53,7 +54,7 @@ class SolveOpts(C.Structure):
 
 class MeshIn(C.Structure):
     _fields_ = [("n_el", C.c_int32), ("n_nodes", C.c_int32), ("node_xy", _dp), ("connects", _ip),
-                ("fixed", _bp), ("f0", _dp), ("df", _dp)]
+                ("fixed", _bp), ("f0", _dp), ("df", _dp), ("order", C.c_int32)]
 
 
 class SolveStats(C.Structure):
@@ -130,8 +131,8 @@ class OracleProblem:
 
     def __init__(self, params, nthreads=0, mesh=None):
         """the structured quarter annulus of `params`, or with mesh = dict(node_xy,
-        connects, fixed, f0, df) a caller's order-2 mesh (params then give the
-        material and in-situ stress only)"""
+        connects, fixed, f0, df[, order]) a caller's mesh of order 1, 2 or 3
+        (params then give the material and in-situ stress only)"""
         self.params = params
         if mesh is None:
             self._p = lib().orc_problem_create(C.byref(params), int(nthreads))
@@ -139,12 +140,14 @@ class OracleProblem:
             a = {k: np.ascontiguousarray(mesh[k], dtype=t) for k, t in
                  (("node_xy", np.float64), ("connects", np.int32), ("fixed", np.uint8), ("f0", np.float64),
                   ("df", np.float64))}
-            m = MeshIn(a["connects"].size // 9, a["node_xy"].size // 2, ptr(a["node_xy"]), ptr(a["connects"]),
-                       ptr(a["fixed"]), ptr(a["f0"]), ptr(a["df"]))
+            order = int(mesh.get("order", 2))
+            m = MeshIn(a["connects"].size // (order + 1) ** 2, a["node_xy"].size // 2, ptr(a["node_xy"]),
+                       ptr(a["connects"]), ptr(a["fixed"]), ptr(a["f0"]), ptr(a["df"]), order)
             self._p = lib().orc_problem_from_mesh(C.byref(m), C.byref(params), int(nthreads))
         P = self._p.contents
         self.P = P
         self.n_el, self.n_nodes, self.neq, self.n_ip = P.n_el, P.n_nodes, P.neq, P.n_ip
+        self.order, self.nn, self.nq, self.nd = P.order, P.nn, P.nq, P.nd
         self.n_colors = P.n_colors
         self.n_blocks = P.n_blocks
 
@@ -162,13 +165,14 @@ class OracleProblem:
     # array views
     def arr(self, name):
         P = self.P
-        sizes = {"node_xy": (2 * self.n_nodes, np.float64), "connects": (9 * self.n_el, np.int32),
+        nn, nq, nd = self.nn, self.nq, self.nd
+        sizes = {"node_xy": (2 * self.n_nodes, np.float64), "connects": (nn * self.n_el, np.int32),
                  "fixed": (self.neq, np.uint8), "f0": (self.neq, np.float64), "df": (self.neq, np.float64),
-                 "B": (486 * self.n_el, np.float64), "weight": (self.n_ip, np.float64),
-                 "dofs": (18 * self.n_el, np.int32), "el_color": (self.n_el, np.int32),
+                 "B": (3 * nq * nd * self.n_el, np.float64), "weight": (self.n_ip, np.float64),
+                 "dofs": (nd * self.n_el, np.int32), "el_color": (self.n_el, np.int32),
                  "color_ptr": (self.n_colors + 1, np.int32), "color_els": (self.n_el, np.int32),
                  "row_ptr": (self.n_nodes + 1, np.int64), "col": (self.n_blocks, np.int32),
-                 "el_blk": (81 * self.n_el, np.int64), "eps_p": (6 * self.n_ip, np.float64),
+                 "el_blk": (nn * nn * self.n_el, np.int64), "eps_p": (6 * self.n_ip, np.float64),
                  "sigma": (6 * self.n_ip, np.float64), "mtype": (self.n_ip, np.int8),
                  "alpha": (self.n_ip, np.float64), "strain": (3 * self.n_ip, np.float64),
                  "sigma_w": (3 * self.n_ip, np.float64), "dep": (9 * self.n_ip, np.float64),

@@ -39,8 +39,8 @@ def main():
             f = os.path.join(d, case, "out-1.txt")
             if os.path.exists(f):
                 run = parse(f)
-                if not case.startswith("order2-"):
-                    # orders 1 and 3: counts only (the histories are for order 2)
+                if not case.endswith(("-mesh1", "-mesh2")):
+                    # meshes 3-5: counts only (the histories replayed are those of meshes 1 and 2)
                     del run["delta_du"], run["residue"]
                 out["runs"]["%s/%s" % (arm, case)] = run
     with open(OUT, "w") as f:

@@ -24,23 +24,51 @@ def _mesh(tmp_path, k):
     return ip.GmshMesh(path)
 
 
-def _problem(g, cohesion=5.0):
+def _problem(g, cohesion=5.0, order=2):
     bcs, mat = gw.reference_bcs(cohesion)
-    return ip.GmshProblem(g, bcs, **mat)
+    return ip.GmshProblem(g, bcs, order=order, **mat)
 
 
 @pytest.mark.parametrize("k", [1, 2, 3])
 def test_equation_and_colour_counts_match_the_logs(tmp_path, k):
-    """order-2 equations and greedy colours of meshes 1-3 equal the
-    reference's logged "DOF" and "Number of colors" for them"""
+    """equations and greedy colours of meshes 1-3 at orders 1, 2 and 3 equal
+    the reference's logged "DOF" and "Number of colors" for them"""
     g = _mesh(tmp_path, k)
-    pb = _problem(g)
-    run = rh.reference_run("CPU_NOT_MODIFIED/order2-mesh%d" % k)
-    nc, _ = ip.color_elements(pb.array("connects"), pb.n_nodes)
-    assert pb.neq == run["dof"]
-    assert nc == run["colors"] == 4
     n = gw.REFERENCE_MESHES[k][0]
     assert len(g.quads) == 4 * (n - 1) ** 2 and len(g.lines) == 8 * (n - 1) and len(g.points) == 4
+    for order in (1, 2, 3):
+        pb = _problem(g, order=order)
+        run = rh.reference_run("CPU_NOT_MODIFIED/order%d-mesh%d" % (order, k))
+        nc, _ = ip.color_elements(pb.array("connects"), pb.n_nodes, (order + 1) ** 2)
+        assert pb.neq == run["dof"], (order, pb.neq, run["dof"])
+        assert nc == run["colors"] == 4
+
+
+@pytest.mark.parametrize("order", [1, 2, 3])
+def test_element_geometry(tmp_path, order):
+    """shape-function derivatives of every element sum to zero, a linear
+    displacement field gives its constant strain at every point, the
+    quadrature weights add up to the area of the polygonal annulus, and edge
+    connects of neighbouring elements coincide"""
+    g = _mesh(tmp_path, 1)
+    pb = _problem(g, order=order)
+    nn = (order + 1) ** 2
+    dphi = pb.array("dphi").reshape(-1, nn, 2, nn)
+    con = pb.array("connects").reshape(-1, nn)
+    xy = pb.array("node_xy").reshape(-1, 2)
+    assert np.abs(dphi.sum(-1)).max() < 1e-11
+    ux, uy = 1e-3 * xy[:, 0] + 2e-3 * xy[:, 1], -0.5e-3 * xy[:, 0] + 3e-3 * xy[:, 1]
+    exx = np.einsum("eqn,en->eq", dphi[:, :, 0, :], ux[con])
+    gxy = np.einsum("eqn,en->eq", dphi[:, :, 1, :], ux[con]) + np.einsum("eqn,en->eq", dphi[:, :, 0, :], uy[con])
+    eyy = np.einsum("eqn,en->eq", dphi[:, :, 1, :], uy[con])
+    assert np.abs(exx - 1e-3).max() < 1e-12 and np.abs(gxy - 1.5e-3).max() < 1e-12
+    assert np.abs(eyy - 3e-3).max() < 1e-12
+    r, th = gw.wellbore_nodes(*gw.REFERENCE_MESHES[1])
+    area = 0.5 * len(th) * np.sin(2 * np.pi / len(th)) * (r[-1] ** 2 - r[0] ** 2)
+    assert abs(pb.array("weight").sum() - area) < 1e-10 * area
+    # every connect is used, and no two connects share a position
+    assert np.unique(con).size == pb.n_nodes
+    assert np.unique(np.round(xy, 12), axis=0).shape[0] == pb.n_nodes
 
 
 @pytest.mark.skipif(not os.path.isdir(REF_GMSH), reason="reference meshes not present")
@@ -114,7 +142,46 @@ def test_reader_and_problem_reject_what_they_do_not_support(tmp_path):
 def _oracle(pb, cohesion=5.0):
     prm = po.default_params(4, E=2000.0, nu=0.2, cohesion=cohesion, phi_deg=20.0, psi_deg=20.0, sxx0=0.0,
                             syy0=0.0, szz0=0.0, sxy0=0.0)
-    return po.OracleProblem(prm, mesh={k: pb.array(k) for k in ("node_xy", "connects", "fixed", "f0", "df")})
+    mesh = {k: pb.array(k) for k in ("node_xy", "connects", "fixed", "f0", "df")}
+    mesh["order"] = pb.order
+    return po.OracleProblem(prm, mesh=mesh)
+
+
+@pytest.mark.parametrize("order", [1, 3])
+def test_oracle_element_blocks_equal_the_library_blocks(tmp_path, order):
+    """the oracle's own element blocks (recomputed from the coordinates) hold
+    the library's dphi and weights bit for bit"""
+    pb = _problem(_mesh(tmp_path, 1), order=order)
+    P = _oracle(pb)
+    nn = nq = (order + 1) ** 2
+    nd = 2 * nn
+    B = P.arr("B").reshape(-1, nq, 3, nd)
+    d = pb.array("dphi").reshape(-1, nq, 2, nn)
+    assert np.array_equal(B[:, :, 0, 0::2], d[:, :, 0, :]) and np.array_equal(B[:, :, 1, 0::2], d[:, :, 1, :])
+    assert np.array_equal(B[:, :, 1, 1::2], d[:, :, 0, :]) and np.array_equal(B[:, :, 2, 1::2], d[:, :, 1, :])
+    assert np.array_equal(P.arr("weight"), pb.array("weight"))
+
+
+def test_oracle_replays_the_order_1_logs(tmp_path):
+    """order 1 (NeoPZ's order-1 basis is the bilinear Lagrange basis, so the
+    residual norms themselves are comparable): initial stiffness on mesh 1,
+    ratios within 0.003 of the logged ones (limit 0.5282 to 1e-4) and norms
+    within 1 %; modified Thomas within 0.01 per ratio"""
+    pb = _problem(_mesh(tmp_path, 1), order=1)
+    for accel, variant in ((0, "CPU_NOT_MODIFIED"), (1, "CPU_MODIFIED")):
+        P = _oracle(pb)
+        ref = rh.reference_run(variant + "/order1-mesh1")
+        n_run = len(ref["residue"])
+        st, log = P.solve_steps(np.zeros(P.neq), 1, newton_rtol=1e-14, newton_max_it=n_run, cg_rtol=1e-11,
+                                tangent_mode=1, accel=accel)
+        ours, refr = log[:, 2], np.asarray(ref["residue"])
+        diff = np.abs(rh.ratios(ours) - rh.ratios(refr)).max()
+        print("order 1 %s: max ratio difference %.4f, first norms %.6f / %.6f" % (variant, diff, ours[0], refr[0]))
+        if accel == 0:
+            assert diff < 0.003 and abs(rh.ratios(ours)[-1] - rh.ratios(refr)[-1]) < 1e-4
+            assert np.abs(ours / refr - 1).max() < 0.01
+        else:
+            assert diff < 0.01
 
 
 @pytest.mark.parametrize("accel,variant,iters,tol_early,tol_late", [

@@ -21,22 +21,25 @@ from oracle import pyoracle as po  # noqa: E402
 import replay_helpers as rh  # noqa: E402
 
 
-def _problem(tmp_path, n, q, cohesion=5.0):
+def _problem(tmp_path, n, q, cohesion=5.0, order=2):
     path = str(tmp_path / ("wb_%d.msh" % n))
     gw.write_wellbore_msh(path, n, q)
     bcs, mat = gw.reference_bcs(cohesion)
-    return ip.GmshProblem(ip.GmshMesh(path), bcs, **mat)
+    return ip.GmshProblem(ip.GmshMesh(path), bcs, order=order, **mat)
 
 
 def _oracle(pb, cohesion=5.0):
     prm = po.default_params(4, E=2000.0, nu=0.2, cohesion=cohesion, phi_deg=20.0, psi_deg=20.0, sxx0=0.0,
                             syy0=0.0, szz0=0.0, sxy0=0.0)
-    return po.OracleProblem(prm, mesh={k: pb.array(k) for k in ("node_xy", "connects", "fixed", "f0", "df")})
+    mesh = {k: pb.array(k) for k in ("node_xy", "connects", "fixed", "f0", "df")}
+    mesh["order"] = pb.order
+    return po.OracleProblem(prm, mesh=mesh)
 
 
-@pytest.mark.parametrize("tangent,accel", [(0, 0), (1, 0), (1, 1)])
-def test_gmsh_problem_bit_exact_with_oracle(tmp_path, tangent, accel):
-    pb = _problem(tmp_path, 9, 1.3)
+@pytest.mark.parametrize("order,tangent,accel", [(2, 0, 0), (2, 1, 0), (2, 1, 1), (1, 0, 0), (1, 1, 1), (3, 0, 0),
+                                                 (3, 1, 1)])
+def test_gmsh_problem_bit_exact_with_oracle(tmp_path, order, tangent, accel):
+    pb = _problem(tmp_path, 9, 1.3, order=order)
     sm = ip.ElastoPlasticIntPointsStructMatrix(pb)
     P = _oracle(pb)
     assert sm.n_colors == P.n_colors == 4
@@ -50,6 +53,12 @@ def test_gmsh_problem_bit_exact_with_oracle(tmp_path, tangent, accel):
     assert np.array_equal(lg, lo)
     assert np.array_equal(ug, uo)
     assert np.abs(ug).max() > 1e-4
+    # the state committed at the accepted step
+    n_ip = P.n_ip
+    sg_state = sm.get_state(1).reshape(4, n_ip)
+    so_state = P.arr("sigma").reshape(n_ip, 6)
+    assert np.array_equal(sg_state[0], so_state[:, 0]) and np.array_equal(sg_state[2], so_state[:, 3])
+    assert np.array_equal(sm.get_state(3), P.arr("mtype").astype(np.float64))
 
 
 @pytest.mark.parametrize("k", [1, 2])
@@ -84,3 +93,68 @@ def test_replay_of_the_logged_runs(tmp_path, k, accel):
     else:
         assert early < 0.02 and late < 0.03
         assert it_ours is not None and abs(it_ours - it_ref) <= 1
+
+
+@pytest.mark.parametrize("order,k", [(1, 1), (1, 2), (3, 1), (3, 2)])
+def test_replay_of_the_logged_runs_orders_1_and_3(tmp_path, order, k):
+    """orders 1 and 3 on meshes 1 and 2, initial stiffness: the whole logged
+    run (order 3 converges slowly, 251 and 179 iterations, with the limit
+    ratio 0.9632 / 0.9547) and its limit ratio to 2e-3; for order 1 (NeoPZ's
+    order-1 basis is the bilinear Lagrange basis) also the ratio sequence, the
+    norms themselves and the iteration count.  For order 3 the transient
+    ratios depend on the basis (NeoPZ's hierarchical cubic functions against
+    Lagrange ones), the limit does not.  Then the modified-Thomas run's
+    iteration count to the logged reduction."""
+    n, q = gw.REFERENCE_MESHES[k]
+    pb = _problem(tmp_path, n, q, order=order)
+    ref = rh.reference_run("CPU_NOT_MODIFIED/order%d-mesh%d" % (order, k))
+    sm = ip.ElastoPlasticIntPointsStructMatrix(pb)
+    assert sm.neq == ref["dof"] and sm.n_colors == ref["colors"]
+    sm.set_newton_tangent(1)
+    n_run = len(ref["residue"])
+    st, log = sm.newton(np.zeros(sm.neq), 1, newton_rtol=1e-14, newton_max_it=n_run, cg_rtol=1e-11,
+                        log_cap=n_run + 8)
+    ours, refr = log[:, 2], np.asarray(ref["residue"])
+    ro, rr = rh.ratios(ours), rh.ratios(refr)
+    early, late, it_ours, it_ref = rh.compare(ours, refr, n_run - 1)
+    print("order %d mesh %d: %d equations, ratio differences %.4f / %.4f, limit %.4f vs %.4f, iterations to the "
+          "reference's reduction %s vs %s, first norms %.5g / %.5g"
+          % (order, k, sm.neq, early, late, ro[-1], rr[-1], it_ours, it_ref, ours[0], refr[0]))
+    assert abs(ro[-1] - rr[-1]) < 2e-3
+    if order == 1:
+        assert it_ours is not None and abs(it_ours - it_ref) <= 1
+        assert late < 0.006 and np.abs(ours / refr - 1).max() < 0.02
+    refm = rh.reference_run("CPU_MODIFIED/order%d-mesh%d" % (order, k))
+    sm2 = ip.ElastoPlasticIntPointsStructMatrix(pb)
+    sm2.set_newton_tangent(1)
+    sm2.set_newton_accel(1)
+    n_m = 2 * len(refm["residue"]) if order == 3 else len(refm["residue"]) + 4
+    st2, log2 = sm2.newton(np.zeros(sm2.neq), 1, newton_rtol=1e-14, newton_max_it=n_m, cg_rtol=1e-11,
+                           log_cap=n_m + 8)
+    _, _, itm_ours, itm_ref = rh.compare(log2[:, 2], refm["residue"], len(refm["residue"]) - 1)
+    print("  modified Thomas: iterations to the reference's reduction %s vs %s" % (itm_ours, itm_ref))
+    assert itm_ours is not None
+    if order == 1:
+        assert abs(itm_ours - itm_ref) <= 1
+    else:
+        # the residual norms of the cubic bases weight the slow modes differently,
+        # so only the scale of the count compares
+        assert itm_ours <= 1.5 * itm_ref
+
+
+@pytest.mark.parametrize("order", [1, 3])
+def test_mixed_precision_orders_1_and_3(tmp_path, order):
+    """the FP32 tangent and FP32 CG of the mixed solve at orders 1 and 3:
+    the same Newton solution as plain FP64 to the Newton tolerance"""
+    pb = _problem(tmp_path, 16, 1.3, order=order)
+    u = {}
+    for prec in (ip.PLAIN_FP64, ip.MIXED):
+        sm = ip.ElastoPlasticIntPointsStructMatrix(pb)
+        sm.set_precision(prec)
+        uu = np.zeros(sm.neq)
+        st, _ = sm.newton(uu, 1, newton_rtol=1e-10, newton_max_it=40,
+                          cg_rtol=1e-4 if prec == ip.MIXED else 1e-10)
+        assert st.converged
+        u[prec] = uu
+    err = np.abs(u[ip.MIXED] - u[ip.PLAIN_FP64]).max() / np.abs(u[ip.PLAIN_FP64]).max()
+    assert err < 1e-7, err
