@@ -158,3 +158,43 @@ def test_mixed_precision_orders_1_and_3(tmp_path, order):
         u[prec] = uu
     err = np.abs(u[ip.MIXED] - u[ip.PLAIN_FP64]).max() / np.abs(u[ip.PLAIN_FP64]).max()
     assert err < 1e-7, err
+
+
+def test_line_probe_of_the_solution_matches_the_reference_fem(tmp_path):
+    """The reference's verification configuration on mesh 2 (order 2, the
+    logged initial-stiffness iteration to convergence), post-processed like
+    the reference's data: a 1001-point probe along y = 0 written with the
+    columns of its CSVs.  Against its finite-element profile
+    (ElastoPlasticFEMdata.csv, made on a coarser mesh that is not shipped:
+    about 20 radial nodes with progression 1.25): radial displacement within
+    2 % (measured 1.4 %), stresses beyond the first element layer within 5 %
+    (3.1 %), and the plastic radius (FailureType) at the RK solution's 0.162
+    (0.1624)."""
+    from intpointsfem_gb300 import postprocess as pp
+    import verification_helpers as vh
+
+    n, q = gw.REFERENCE_MESHES[2]
+    pb = _problem(tmp_path, n, q)
+    sm = ip.ElastoPlasticIntPointsStructMatrix(pb)
+    sm.set_newton_tangent(1)
+    u = np.zeros(sm.neq)
+    st, _ = sm.newton(u, 1, newton_rtol=1e-10, newton_max_it=80, cg_rtol=1e-11)
+    assert st.converged
+    S = pp.Solution.from_struct_matrix(pb, sm, u)
+    rows = S.write_line_probe_csv(str(tmp_path / "probe.csv"), (0.1, 0.0), (4.0, 0.0), 1001)
+    with open(tmp_path / "probe.csv") as f:
+        assert [h.strip('"') for h in f.readline().strip().split(",")] == pp.COLUMNS
+    c = {k: i for i, k in enumerate(pp.COLUMNS)}
+    fem = vh.fixture()["ep_fem"]                   # x, u_x, s_xx, s_yy, s_zz, ep_xx, ep_yy
+    x = rows[:, c["Points:0"]]
+    assert rows[:, c["vtkValidPointMask"]].min() == 1.0
+    eu = np.abs(rows[:, c["Displacement:0"]] - np.interp(x, fem[:, 0], fem[:, 1])).max() / np.abs(fem[:, 1]).max()
+    beyond = x > 0.12
+    sc = np.abs(fem[:, 2]).max()
+    es = max(np.abs(rows[beyond, c[col]] - np.interp(x[beyond], fem[:, 0], fem[:, k])).max() / sc
+             for col, k in (("Stress:0", 2), ("Stress:4", 3), ("Stress:8", 4)))
+    plastic = x[rows[:, c["FailureType"]] > 0.5]
+    print("line probe vs reference FEM: u %.2e, stresses %.2e, plastic to r = %.4f" % (eu, es, plastic.max()))
+    assert eu < 2e-2 and es < 5e-2
+    assert abs(plastic.max() - 0.162) < 0.01
+    S.write_vtk(str(tmp_path / "solution.vtk"))
