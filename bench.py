@@ -1,7 +1,7 @@
 """Benchmark: ms per Newton iteration (and residual IP/s) of the plain FP64
 wellbore solve, 400 x 400 order-2 quads (1.44 M integration points,
-1 283 202 dofs), Jacobi-CG to 1e-8 and Newton to 1e-8 relative residual, on
-one GB300.
+1 283 202 dofs), block-Jacobi CG to 1e-8 and Newton to 1e-8 relative
+residual, on one GB300 (--jacobi: scalar Jacobi).
 
 A step is one Newton iteration of the load-stepped solve (CG on the current
 tangent, u += du, Assemble(K, rhs), convergence test; load-step acceptance
@@ -14,9 +14,10 @@ occur).  W warm-up iterations run untimed, then exactly K are timed.
   roofline : the CG block SpMV (dominant kernel), algorithmic bytes / launch
              over its CUDA-event duration, against the measured HBM copy peak
   cpu_baseline : the C oracle on the host cores, bounded sample (one tangent
-             assembly + S CG iterations), scaled to a Newton iteration with the
-             CG iteration count of the timed GPU iterations (the oracle performs
-             bit-identical arithmetic, so the counts are the same)
+             assembly + S CG iterations with the same preconditioner), scaled to
+             a Newton iteration with the CG iteration count of the timed GPU
+             iterations (the oracle performs bit-identical arithmetic, so the
+             counts are the same)
 
 --impl reference times the oracle alone (the reference's own CPU path cannot
 be built: it needs NeoPZ, Intel MKL and TBB).
@@ -46,9 +47,10 @@ CONFIGS = {
                                          "pw_final": -5.0}},
 }
 # CG iterations of the first Newton iterations of the 400 x 400 solve, as run on
-# the GPU (identical on the CPU oracle); used by --impl reference to scale its
-# bounded CG sample to whole Newton iterations.
-CFG2_CG_ITERS = [10119, 9495]
+# the GPU (identical on the CPU oracle), with block Jacobi and with Jacobi; used
+# by --impl reference to scale its bounded CG sample to whole Newton iterations.
+CFG2_CG_ITERS = [7001, 7822, 7021, 7695, 7021, 7913, 7021, 7895]
+CFG2_CG_ITERS_JACOBI = [10119, 9495]
 # DRAM bytes (read + write) of one SpMV launch at 400 x 400 (rows sorted by
 # length), from the ncu capture summarised in profiles/k_cg_spmv_400x400.md
 SPMV_DRAM_BYTES = 388.405504e6 + 9.274112e6
@@ -121,7 +123,7 @@ class ClockSampler:
 class CpuArm:
     """The C oracle on the host cores (bounded samples of the same workload)."""
 
-    def __init__(self, n, threads, n_steps=N_STEPS, wb=None):
+    def __init__(self, n, threads, n_steps=N_STEPS, wb=None, block=True):
         import numpy as np
 
         from oracle import pyoracle as po
@@ -130,6 +132,7 @@ class CpuArm:
         self.threads = threads
         t0 = time.perf_counter()
         self.P = po.OracleProblem(po.default_params(n, **(wb or {})), nthreads=threads)
+        self.P.set_block_jacobi(block)
         self.n_steps = n_steps
         self.t_setup = time.perf_counter() - t0
         self.u = np.zeros(self.P.neq)
@@ -180,7 +183,7 @@ def run_reference(args):
         return 0
     threads = args.cpu_threads or os.cpu_count()
     n = args.n
-    arm = CpuArm(n, threads, args.n_steps, args.wb)
+    arm = CpuArm(n, threads, args.n_steps, args.wb, block=not args.jacobi)
     if n <= 100:
         # small meshes: the oracle's own CG iteration count to 1e-8 on the first tangent
         R = arm.P.assemble(arm.u, 1.0 / args.n_steps)
@@ -188,7 +191,7 @@ def run_reference(args):
         cg_iters, cg_note = [abs(k)], "the oracle's CG iterations to 1e-8 on the first tangent"
     else:
         # the measured 400 x 400 counts, scaled by n / 400 (CG iterations grow linearly with n here)
-        cg_iters = [c * n / 400.0 for c in CFG2_CG_ITERS]
+        cg_iters = [c * n / 400.0 for c in (CFG2_CG_ITERS_JACOBI if args.jacobi else CFG2_CG_ITERS)]
         cg_note = "the GPU's CG iterations per Newton iteration at 400x400 scaled by n/400"
     mean_cg = sum(cg_iters) / len(cg_iters)
     samples = []
@@ -203,11 +206,13 @@ def run_reference(args):
         "impl": "reference", "metric": METRIC, "value": ms, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": False, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": "wellbore %dx%d order-2 quads, %d IPs, plain FP64, Jacobi-CG 1e-8, Newton 1e-8, "
-                               "%d load steps (configuration %d)" % (n, n, 9 * n * n, args.n_steps, args.config)},
+        "config": {"workload": "wellbore %dx%d order-2 quads, %d IPs, plain FP64, %s 1e-8, Newton 1e-8, "
+                               "%d load steps (configuration %d)"
+                               % (n, n, 9 * n * n, "Jacobi-CG" if args.jacobi else "block-Jacobi CG", args.n_steps,
+                                  args.config)},
         "ip_per_s": statistics.mean(s["ip_per_s"] for s in samples),
         "cpu_baseline": {"value": ms, "unit": UNIT, "cores": threads, "kind": "port",
-                         "sample": "per step: one tangent assembly + %d Jacobi-CG iterations of the C oracle, "
+                         "sample": "per step: one tangent assembly + %d CG iterations of the C oracle, "
                                    "scaled to %.0f CG iterations per Newton iteration (%s)"
                                    % (samples[0]["cg_sample"], mean_cg, cg_note)},
         "e2e": {"value": ms, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -246,6 +251,10 @@ def run_gpu(args):
         A.set_precision(ip.MIXED)
         if B:
             B.set_precision(ip.MIXED)
+    if not args.jacobi:
+        A.set_preconditioner(ip.PREC_BLOCK_JACOBI)
+        if B:
+            B.set_preconditioner(ip.PREC_BLOCK_JACOBI)
     stream = torch.cuda.ExternalStream(A.stream, device=dev)
     fp64_tflops = A.measure_fp64_peak()
 
@@ -310,6 +319,8 @@ def run_gpu(args):
                 C_.mlp_init(0)
                 C_.set_mlp_params(tp.load_weights())
                 C_.set_preconditioner(ip.PREC_MLP)
+            elif not args.jacobi:
+                C_.set_preconditioner(ip.PREC_BLOCK_JACOBI)
             uc = torch.zeros(C_.neq, dtype=torch.float64, device=dev)
             C_.newton_begin(N_STEPS, newton_max_it=40, cg_rtol=args.mixed_cg_rtol)
             C_.newton_advance(uc, args.warmup, ip.DEVICE)
@@ -334,8 +345,8 @@ def run_gpu(args):
                             "triangular factor (weights shipped in intpointsfem_gb300/weights), FP64 residual/"
                             "return mapping/Newton refinement" % args.mixed_cg_rtol)
         chosen["mixed_jacobi"] = mixed_arm(False)
-        chosen["mixed_jacobi"]["method"] = "mixed: FP32 tangent + FP32 Jacobi-CG to %g, FP64 Newton refinement" % (
-            args.mixed_cg_rtol)
+        chosen["mixed_jacobi"]["method"] = "mixed: FP32 tangent + FP32 %s to %g, FP64 Newton refinement" % (
+            "Jacobi-CG" if args.jacobi else "block-Jacobi CG", args.mixed_cg_rtol)
         chosen["speedup_vs_plain"] = ms_dev / chosen["ms_per_newton_iter"]
 
     # roofline of the dominant kernel (CG block SpMV), CUDA events on the library stream
@@ -349,7 +360,7 @@ def run_gpu(args):
 
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
-        arm = CpuArm(n, args.cpu_threads or os.cpu_count(), args.n_steps, args.wb)
+        arm = CpuArm(n, args.cpu_threads or os.cpu_count(), args.n_steps, args.wb, block=not args.jacobi)
         cpu = arm.sample(cg_per_iter, args.cpu_cg_sample)
         arm.close()
 
@@ -361,10 +372,11 @@ def run_gpu(args):
         "metric": METRIC, "value": ms_dev, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms_dev, "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64" if not mixed else "f32+f64",
         "data": "synthetic",
-        "config": {"workload": "wellbore %dx%d order-2 quads, %d IPs, %d dofs, %s, Jacobi-CG %g, "
+        "config": {"workload": "wellbore %dx%d order-2 quads, %d IPs, %d dofs, %s, %s %g, "
                                "Newton 1e-8, %d load steps%s; first %d Newton iterations (warm-up %d); "
                                "configuration %d"
-                               % (n, n, A.n_ip, A.neq, "plain FP64" if not mixed else "mixed FP32/FP64", cg_rtol,
+                               % (n, n, A.n_ip, A.neq, "plain FP64" if not mixed else "mixed FP32/FP64",
+                                  "Jacobi-CG" if args.jacobi else "block-Jacobi CG", cg_rtol,
                                   N_STEPS, (", material %s" % json.dumps(args.wb)) if args.wb else "",
                                   args.warmup + args.steps, args.warmup, args.config),
                    "l2": "inputs larger than L2 (tangent %.0f MB, element blocks %.0f MB)"
@@ -396,7 +408,7 @@ def run_gpu(args):
         line["cpu_baseline"] = {"value": cpu["ms_per_newton"], "unit": UNIT, "cores": args.cpu_threads or os.cpu_count(),
                                 "kind": "port",
                                 "sample": "C oracle (bit-identical arithmetic): one tangent assembly (%.0f ms) + %d "
-                                          "Jacobi-CG iterations (%.2f ms each), scaled by %.0f CG iterations per "
+                                          "CG iterations (%.2f ms each), scaled by %.0f CG iterations per "
                                           "Newton iteration; residual %.1f ms = %.3g IP/s"
                                           % (cpu["t_asm_ms"], cpu["cg_sample"], cpu["t_cg_iter_ms"], cg_per_iter,
                                              cpu["t_res_ms"], cpu["ip_per_s"])}
@@ -422,6 +434,7 @@ def main():
     ap.add_argument("--mixed-cg-rtol", type=float, default=1e-4)
     ap.add_argument("--no-chosen", dest="chosen", action="store_false")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--jacobi", action="store_true", help="scalar Jacobi instead of block Jacobi in the CG")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

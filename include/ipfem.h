@@ -40,7 +40,7 @@ typedef enum {
 
 enum { IPFEM_HOST = 0, IPFEM_DEVICE = 1 };
 enum { IPFEM_PLAIN_FP64 = 0, IPFEM_MIXED = 1 };
-enum { IPFEM_PREC_JACOBI = 0, IPFEM_PREC_MLP = 1 };
+enum { IPFEM_PREC_JACOBI = 0, IPFEM_PREC_MLP = 1, IPFEM_PREC_BLOCK_JACOBI = 2 };
 
 /* Element order p = 1, 2 or 3 (the reference's O_LINEAR, O_QUADRATIC and
  * O_CUBIC builds, KernelsMatrixAssemble.h:3-12): (p+1)^2 connects and
@@ -265,6 +265,11 @@ int32_t ipfem_color_elements_nn(int32_t n_elements, int32_t n_nodes, int32_t nn,
 ipfem_status ipfem_set_node_grid(ipfem_ctx *ctx, int32_t gr, int32_t gt);
 /* allocates the network (He-uniform W1, W2; W3 = 0, zero biases) */
 ipfem_status ipfem_mlp_init(ipfem_ctx *ctx, uint64_t seed);
+/* Preconditioner of the CG solves: IPFEM_PREC_JACOBI (default; z_i = r_i / K_ii
+ * on free dofs), IPFEM_PREC_BLOCK_JACOBI (z = B_i^-1 r at every node, B_i the
+ * 2x2 diagonal block of the tangent restricted to the node's free dofs; plain
+ * and mixed precision), IPFEM_PREC_MLP (the learned factor above, IPFEM_MIXED
+ * only).  No counterpart in the reference, which factorises K (Pardiso). */
 ipfem_status ipfem_set_preconditioner(ipfem_ctx *ctx, int kind);
 ipfem_status ipfem_mlp_get_params(ipfem_ctx *ctx, float *out);
 ipfem_status ipfem_mlp_set_params(ipfem_ctx *ctx, const float *in);

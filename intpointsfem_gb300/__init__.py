@@ -17,7 +17,7 @@ LIB_PATH = os.path.join(HERE, "libipfem.so")
 
 HOST, DEVICE = 0, 1
 PLAIN_FP64, MIXED = 0, 1
-PREC_JACOBI, PREC_MLP = 0, 1
+PREC_JACOBI, PREC_MLP, PREC_BLOCK_JACOBI = 0, 1, 2
 MLP_PARAMS = 23316
 STATUS = {0: "ok", 1: "not converged", 2: "non-finite value", 3: "CG breakdown", 4: "out of device memory",
           5: "invalid argument", 6: "CUDA error", 7: "no sm_103 device"}

@@ -76,12 +76,12 @@ void free_all(ipfem_ctx *c)
                     c->d_fixed, c->d_K,
                     c->d_dinv, c->d_eps_p, c->d_sigma, c->d_alpha, c->d_mtype, c->d_u, c->d_rhs, c->d_strain,
                     c->d_sigma_w, c->d_dep, c->d_fe, c->d_x, c->d_r, c->d_z, c->d_p, c->d_q, c->d_b, c->d_part,
-                    c->d_sc, c->d_counters, c->d_dotres, c->d_err, c->d_acc};
+                    c->d_sc, c->d_counters, c->d_dotres, c->d_err, c->d_acc, c->d_binv};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     {
         MixedBuffers &m = c->mx;
-        void *mp[] = {m.dphi, m.K, m.dinv, m.x, m.r, m.z, m.p, m.q, m.part, m.sc};
+        void *mp[] = {m.dphi, m.K, m.dinv, m.binv, m.x, m.r, m.z, m.p, m.q, m.part, m.sc};
         for (void *p : mp)
             if (p) cudaFree(p);
         if (m.h_sc) cudaFreeHost(m.h_sc);
@@ -457,6 +457,7 @@ ipfem_status ipfem_set_precision(ipfem_ctx *c, int mode)
         ck(upload_sell(m.sell, false, m.dsell, c->stream));
         ck(dalloc(&m.K, (size_t)m.sell.n_sell * 4));
         ck(dalloc(&m.dinv, (size_t)s.neq));
+        ck(dalloc(&m.binv, (size_t)s.n_nodes * 4));
         ck(dalloc(&m.x, (size_t)s.neq));
         ck(dalloc(&m.r, (size_t)s.neq));
         ck(dalloc(&m.z, (size_t)s.neq));

@@ -213,12 +213,32 @@ ipfem_status ipfem_mlp_init(ipfem_ctx *c, uint64_t seed)
 
 ipfem_status ipfem_set_preconditioner(ipfem_ctx *c, int kind)
 {
-    if (!c || (kind != IPFEM_PREC_JACOBI && kind != IPFEM_PREC_MLP)) return mfail(c, IPFEM_INVALID, "bad preconditioner");
+    if (!c || (kind != IPFEM_PREC_JACOBI && kind != IPFEM_PREC_MLP && kind != IPFEM_PREC_BLOCK_JACOBI))
+        return mfail(c, IPFEM_INVALID, "bad preconditioner");
     if (kind == IPFEM_PREC_MLP) {
         if (c->precision != IPFEM_MIXED) return mfail(c, IPFEM_INVALID, "the learned preconditioner needs IPFEM_MIXED");
         if (!c->mlp.ready) return mfail(c, IPFEM_INVALID, "ipfem_mlp_init not called");
     }
+    if (kind == IPFEM_PREC_BLOCK_JACOBI && !c->d_binv) {
+        if (cudaMalloc((void **)&c->d_binv, (size_t)c->s.n_nodes * 4 * sizeof(double)) != cudaSuccess)
+            return mfail(c, IPFEM_OOM, "allocation of the block-Jacobi inverses failed");
+    }
+    if (kind != c->preconditioner) {
+        // the captured CG iterations launch the kernels of the previous preconditioner
+        if (c->cg_exec) {
+            cudaGraphExecDestroy(c->cg_exec);
+            c->cg_exec = nullptr;
+        }
+        if (c->mx.exec) {
+            cudaGraphExecDestroy(c->mx.exec);
+            c->mx.exec = nullptr;
+        }
+    }
     c->preconditioner = kind;
+    if (kind == IPFEM_PREC_BLOCK_JACOBI && c->tangent_valid) {
+        launch_jacobi(c);
+        MK(cudaStreamSynchronize(c->stream));
+    }
     return IPFEM_OK;
 }
 

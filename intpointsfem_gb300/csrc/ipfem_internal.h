@@ -59,6 +59,7 @@ struct MixedBuffers {
     SellLayout sell;              // node-ordered rows (the FP32 SpMV is gather-bound)
     SellDev dsell;
     float *dinv = nullptr;        // [neq]
+    float *binv = nullptr;        // [n_nodes*4] block-Jacobi inverses
     float *x = nullptr, *r = nullptr, *z = nullptr, *p = nullptr, *q = nullptr;
     float *part = nullptr;        // 2 partial arrays
     CGScalarsT<float> *sc = nullptr;
@@ -165,6 +166,7 @@ struct ipfem_ctx {
     ipfem::SellDev dsell;                // FP64 tangent layout
     // device: tangent
     double *d_K = nullptr, *d_dinv = nullptr;
+    double *d_binv = nullptr;             // [n_nodes*4] block-Jacobi inverses (IPFEM_PREC_BLOCK_JACOBI)
     // device: integration-point state {xx, xy, yy, zz} SoA
     double *d_eps_p = nullptr, *d_sigma = nullptr, *d_alpha = nullptr;
     int8_t *d_mtype = nullptr;
@@ -192,7 +194,7 @@ struct ipfem_ctx {
     uint64_t launches = 0;               // kernels launched through this context
     int precision = 0;                   // IPFEM_PLAIN_FP64 or IPFEM_MIXED
     ipfem::MixedBuffers mx;
-    int preconditioner = 0;              // IPFEM_PREC_JACOBI or IPFEM_PREC_MLP
+    int preconditioner = 0;              // IPFEM_PREC_JACOBI, IPFEM_PREC_MLP or IPFEM_PREC_BLOCK_JACOBI
     ipfem::MlpBuffers mlp;
     cudaGraphExec_t fcg_exec = nullptr;
     int64_t fcg_fallbacks = 0;
@@ -214,6 +216,8 @@ void launch_axpy_u(ipfem_ctx *c, double *d_u, const double *d_du);
 void launch_scale_add(ipfem_ctx *c, double *d_u, const double *d_x, double alpha, double *d_t);
 void launch_fp64_probe(ipfem_ctx *c, double *d_out, int grid, int iters);
 void launch_stiffness32(ipfem_ctx *c);
+// recomputes the Jacobi (and, when allocated, block-Jacobi) inverses of the current tangent
+void launch_jacobi(ipfem_ctx *c);
 void launch_cg32_init(ipfem_ctx *c, const double *d_b, double scale, float rtol, int max_it);
 void launch_cg32_iteration(ipfem_ctx *c);
 void launch_cg32_spmv_only(ipfem_ctx *c);

@@ -279,15 +279,38 @@ __global__ void __launch_bounds__(kStiffWarps * 32) k_stiffness(int32_t n_in_col
     }
 }
 
+// Jacobi inverses of the free diagonal entries and, when binv is given, the
+// inverse of every nodal 2x2 diagonal block restricted to its free dofs
+// (block Jacobi; det = a d - b c, entries d/det, -b/det, -c/det, a/det).
 template <class T>
 __global__ void k_jacobi(int32_t n_nodes, const int64_t *__restrict__ diag, const T *__restrict__ K,
-                         const uint8_t *__restrict__ fixed, T *__restrict__ dinv)
+                         const uint8_t *__restrict__ fixed, T *__restrict__ dinv, T *__restrict__ binv)
 {
     const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n_nodes) return;
     const T *blk = K + 4 * (size_t)diag[i];
-    dinv[2 * (size_t)i] = fixed[2 * (size_t)i] ? T(0) : T(1) / blk[0];
-    dinv[2 * (size_t)i + 1] = fixed[2 * (size_t)i + 1] ? T(0) : T(1) / blk[3];
+    const bool fx = fixed[2 * (size_t)i], fy = fixed[2 * (size_t)i + 1];
+    dinv[2 * (size_t)i] = fx ? T(0) : T(1) / blk[0];
+    dinv[2 * (size_t)i + 1] = fy ? T(0) : T(1) / blk[3];
+    if (binv) {
+        T m0 = T(0), m1 = T(0), m2 = T(0), m3 = T(0);
+        if (!fx && !fy) {
+            const T det = blk[0] * blk[3] - blk[1] * blk[2];
+            m0 = blk[3] / det;
+            m1 = -blk[1] / det;
+            m2 = -blk[2] / det;
+            m3 = blk[0] / det;
+        } else if (!fx) {
+            m0 = T(1) / blk[0];
+        } else if (!fy) {
+            m3 = T(1) / blk[3];
+        }
+        T *m = binv + 4 * (size_t)i;
+        m[0] = m0;
+        m[1] = m1;
+        m[2] = m2;
+        m[3] = m3;
+    }
 }
 
 template <int P>
@@ -351,8 +374,20 @@ void launch_stiffness(ipfem_ctx *c)
         kern<<<grid, kStiffWarps * 32, 0, c->stream>>>(n, c->d_color_els + first, s.n_ip, c->d_dphi, c->d_dep,
                                                        c->dsell.el_blk, c->d_K);
     }
+    launch_jacobi(c);
+}
+
+void launch_jacobi(ipfem_ctx *c)
+{
+    const Setup &s = c->s;
     const unsigned g2 = (unsigned)((s.n_nodes + 255) / 256);
-    k_jacobi<double><<<g2, 256, 0, c->stream>>>(s.n_nodes, c->dsell.diag_blk, c->d_K, c->d_fixed, c->d_dinv);
+    if (c->precision == 1) {
+        MixedBuffers &m = c->mx;
+        k_jacobi<float><<<g2, 256, 0, c->stream>>>(s.n_nodes, m.dsell.diag_blk, m.K, c->d_fixed, m.dinv, m.binv);
+    } else {
+        k_jacobi<double><<<g2, 256, 0, c->stream>>>(s.n_nodes, c->dsell.diag_blk, c->d_K, c->d_fixed, c->d_dinv,
+                                                    c->d_binv);
+    }
 }
 
 void launch_stiffness32(ipfem_ctx *c)
@@ -369,8 +404,7 @@ void launch_stiffness32(ipfem_ctx *c)
         kern<<<grid, kStiffWarps * 32, 0, c->stream>>>(n, c->d_color_els + first, s.n_ip, m.dphi, c->d_dep,
                                                        m.dsell.el_blk, m.K);
     }
-    const unsigned g2 = (unsigned)((s.n_nodes + 255) / 256);
-    k_jacobi<float><<<g2, 256, 0, c->stream>>>(s.n_nodes, m.dsell.diag_blk, m.K, c->d_fixed, m.dinv);
+    launch_jacobi(c);
 }
 
 }  // namespace ipfem

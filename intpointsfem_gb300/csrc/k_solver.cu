@@ -193,8 +193,23 @@ __device__ __forceinline__ void load_block(const float *K, int64_t s, float &a, 
     a = u.x; b = u.y; c = u.z; d = u.w;
 }
 
-// x = 0, r = b*scale (converted to T), z = D^-1 r, p = z; b.b and r.z
-template <class T>
+// z = M r at node i: Jacobi (minv = dinv[2 n]) or block Jacobi (minv = binv[4 n]:
+// z0 = fma(m01, r1, m00 r0), z1 = fma(m11, r1, m10 r0))
+template <class T, bool BLOCK>
+__device__ __forceinline__ typename Vec2<T>::type precondition(const T *__restrict__ minv, int32_t i,
+                                                               typename Vec2<T>::type rr)
+{
+    typedef typename Vec2<T>::type V;
+    if (BLOCK) {
+        const V m01 = reinterpret_cast<const V *>(minv)[2 * i], m23 = reinterpret_cast<const V *>(minv)[2 * i + 1];
+        return mk2(fma(m01.y, rr.y, m01.x * rr.x), fma(m23.y, rr.y, m23.x * rr.x));
+    }
+    const V di = reinterpret_cast<const V *>(minv)[i];
+    return mk2(rr.x * di.x, rr.y * di.y);
+}
+
+// x = 0, r = b*scale (converted to T), z = M r, p = z; b.b and r.z
+template <class T, bool BLOCK>
 __global__ void __launch_bounds__(kRedBlock) k_cg_init(int32_t n_nodes, const double *__restrict__ b, double scale,
                                                        const T *__restrict__ dinv, T *__restrict__ x,
                                                        T *__restrict__ r, T *__restrict__ z, T *__restrict__ p,
@@ -207,8 +222,7 @@ __global__ void __launch_bounds__(kRedBlock) k_cg_init(int32_t n_nodes, const do
     if (i < n_nodes) {
         const double2 b64 = reinterpret_cast<const double2 *>(b)[i];
         const V bb = mk2((T)(b64.x * scale), (T)(b64.y * scale));
-        const V di = reinterpret_cast<const V *>(dinv)[i];
-        const V zz = mk2(bb.x * di.x, bb.y * di.y);
+        const V zz = precondition<T, BLOCK>(dinv, i, bb);
         reinterpret_cast<V *>(x)[i] = mk2(T(0), T(0));
         reinterpret_cast<V *>(r)[i] = bb;
         reinterpret_cast<V *>(z)[i] = zz;
@@ -303,9 +317,9 @@ __global__ void __launch_bounds__(kRedBlock) k_cg_spmv(int32_t n_nodes, const in
     }
 }
 
-// x += alpha p, r -= alpha q, z = D^-1 r; partials of r.r and r.z;
+// x += alpha p, r -= alpha q, z = M r; partials of r.r and r.z;
 // last CTA: convergence test, beta
-template <class T>
+template <class T, bool BLOCK>
 __global__ void __launch_bounds__(kRedBlock) k_cg_update(int32_t n_nodes, const T *__restrict__ p,
                                                          const T *__restrict__ q, const T *__restrict__ dinv,
                                                          T *__restrict__ x, T *__restrict__ r, T *__restrict__ z,
@@ -313,11 +327,10 @@ __global__ void __launch_bounds__(kRedBlock) k_cg_update(int32_t n_nodes, const 
 {
     typedef typename Vec2<T>::type V;
     const int32_t i = blockIdx.x * kRedBlock + threadIdx.x;
-    // p, dinv, x and r (not written by the SpMV) before the wait, q after it
-    V pp, qq, di, xx, rr;
+    // p, x and r (not written by the SpMV) before the wait, q after it
+    V pp, qq, xx, rr;
     if (i < n_nodes) {
         pp = reinterpret_cast<const V *>(p)[i];
-        di = reinterpret_cast<const V *>(dinv)[i];
         xx = reinterpret_cast<V *>(x)[i];
         rr = reinterpret_cast<V *>(r)[i];
     }
@@ -332,7 +345,7 @@ __global__ void __launch_bounds__(kRedBlock) k_cg_update(int32_t n_nodes, const 
         xx.y = fma(alpha, pp.y, xx.y);
         rr.x = fma(-alpha, qq.x, rr.x);
         rr.y = fma(-alpha, qq.y, rr.y);
-        const V zz = mk2(rr.x * di.x, rr.y * di.y);
+        const V zz = precondition<T, BLOCK>(dinv, i, rr);
         reinterpret_cast<V *>(x)[i] = xx;
         reinterpret_cast<V *>(r)[i] = rr;
         reinterpret_cast<V *>(z)[i] = zz;
@@ -460,7 +473,9 @@ static unsigned grid_nodes(const ipfem_ctx *c)
 
 void launch_cg_init(ipfem_ctx *c, const double *d_b, double rtol, int max_it)
 {
-    k_cg_init<double><<<grid_nodes(c), kRedBlock, 0, c->stream>>>(c->s.n_nodes, d_b, 1.0, c->d_dinv, c->d_x, c->d_r,
+    const bool blk = c->preconditioner == IPFEM_PREC_BLOCK_JACOBI;
+    (blk ? k_cg_init<double, true> : k_cg_init<double, false>)<<<grid_nodes(c), kRedBlock, 0, c->stream>>>(
+        c->s.n_nodes, d_b, 1.0, blk ? c->d_binv : c->d_dinv, c->d_x, c->d_r,
                                                                   c->d_z, c->d_p, c->d_part, c->n_red,
                                                                   c->d_counters + 0, c->d_sc, rtol, max_it);
 }
@@ -484,9 +499,10 @@ void launch_cg_iteration(ipfem_ctx *c)
 {
     const unsigned g = grid_nodes(c);
     launch_spmv<double>(c, c->dsell, c->d_K, c->d_p, c->d_q, c->d_part, c->d_counters + 1, c->d_sc);
-    launch_pdl(k_cg_update<double>, g, kRedBlock, c->stream, c->s.n_nodes, (const double *)c->d_p,
-               (const double *)c->d_q, (const double *)c->d_dinv, c->d_x, c->d_r, c->d_z, c->d_part, c->n_red,
-               c->d_counters + 2, c->d_sc);
+    const bool blk = c->preconditioner == IPFEM_PREC_BLOCK_JACOBI;
+    launch_pdl(blk ? k_cg_update<double, true> : k_cg_update<double, false>, g, kRedBlock, c->stream, c->s.n_nodes,
+               (const double *)c->d_p, (const double *)c->d_q, (const double *)(blk ? c->d_binv : c->d_dinv), c->d_x,
+               c->d_r, c->d_z, c->d_part, c->n_red, c->d_counters + 2, c->d_sc);
     launch_pdl(k_cg_pupdate<double>, grid_pupdate(c), kRedBlock, c->stream, c->s.n_nodes,
                (const double *)c->d_z, c->d_p, (const CGScalarsT<double> *)c->d_sc);
 }
@@ -499,7 +515,9 @@ void launch_cg_spmv_only(ipfem_ctx *c)
 void launch_cg32_init(ipfem_ctx *c, const double *d_b, double scale, float rtol, int max_it)
 {
     MixedBuffers &m = c->mx;
-    k_cg_init<float><<<grid_nodes(c), kRedBlock, 0, c->stream>>>(c->s.n_nodes, d_b, scale, m.dinv, m.x, m.r, m.z,
+    const bool blk = c->preconditioner == IPFEM_PREC_BLOCK_JACOBI;
+    (blk ? k_cg_init<float, true> : k_cg_init<float, false>)<<<grid_nodes(c), kRedBlock, 0, c->stream>>>(
+        c->s.n_nodes, d_b, scale, blk ? m.binv : m.dinv, m.x, m.r, m.z,
                                                                  m.p, m.part, c->n_red, c->d_counters + 4, m.sc,
                                                                  rtol, max_it);
 }
@@ -509,9 +527,10 @@ void launch_cg32_iteration(ipfem_ctx *c)
     MixedBuffers &m = c->mx;
     const unsigned g = grid_nodes(c);
     launch_spmv<float>(c, m.dsell, m.K, m.p, m.q, m.part, c->d_counters + 5, m.sc);
-    launch_pdl(k_cg_update<float>, g, kRedBlock, c->stream, c->s.n_nodes, (const float *)m.p,
-               (const float *)m.q, (const float *)m.dinv, m.x, m.r, m.z, m.part, c->n_red, c->d_counters + 6,
-               m.sc);
+    const bool blk = c->preconditioner == IPFEM_PREC_BLOCK_JACOBI;
+    launch_pdl(blk ? k_cg_update<float, true> : k_cg_update<float, false>, g, kRedBlock, c->stream, c->s.n_nodes,
+               (const float *)m.p, (const float *)m.q, (const float *)(blk ? m.binv : m.dinv), m.x, m.r, m.z, m.part,
+               c->n_red, c->d_counters + 6, m.sc);
     launch_pdl(k_cg_pupdate<float>, grid_pupdate(c), kRedBlock, c->stream, c->s.n_nodes, (const float *)m.z,
                m.p, (const CGScalarsT<float> *)m.sc);
 }

@@ -548,11 +548,13 @@ static void problem_setup(orc_problem *p, const orc_params *prm)
     p->dep = (double *)xcalloc((size_t)p->n_ip * 9, sizeof(double));
     p->K = (double *)xcalloc((size_t)p->n_blocks * 4, sizeof(double));
     p->dinv = (double *)xcalloc((size_t)p->neq, sizeof(double));
+    p->binv = (double *)xcalloc((size_t)p->n_nodes * 4, sizeof(double));
 }
 
 void orc_problem_destroy(orc_problem *p)
 {
     if (!p) return;
+    free(p->binv);
     free(p->node_xy); free(p->connects); free(p->fixed); free(p->f0); free(p->df);
     free(p->mats); free(p->eps_p0); free(p->B); free(p->weight); free(p->dofs);
     free(p->el_color); free(p->color_ptr); free(p->color_els); free(p->row_ptr);
@@ -752,6 +754,21 @@ void orc_assemble(orc_problem *p, const double *u, double lambda, double *rhs)
         const double *blk = &p->K[4 * lo];
         p->dinv[2 * i] = p->fixed[2 * i] ? 0.0 : 1.0 / blk[0];
         p->dinv[2 * i + 1] = p->fixed[2 * i + 1] ? 0.0 : 1.0 / blk[3];
+        /* block Jacobi: the inverse of the 2x2 diagonal block on the free dofs */
+        const int fx = p->fixed[2 * i], fy = p->fixed[2 * i + 1];
+        double *m = &p->binv[4 * (size_t)i];
+        m[0] = m[1] = m[2] = m[3] = 0.0;
+        if (!fx && !fy) {
+            const double det = blk[0] * blk[3] - blk[1] * blk[2];
+            m[0] = blk[3] / det;
+            m[1] = -blk[1] / det;
+            m[2] = -blk[2] / det;
+            m[3] = blk[0] / det;
+        } else if (!fx) {
+            m[0] = 1.0 / blk[0];
+        } else if (!fy) {
+            m[3] = 1.0 / blk[3];
+        }
     }
 }
 
@@ -773,6 +790,24 @@ void orc_spmv(const orc_problem *p, const double *x, double *y)
     }
 }
 
+/* z = M r: Jacobi (z_i = r_i / K_ii on free dofs) or block Jacobi
+ * (z = B_i^-1 r at node i, z0 = fma(m01, r1, m00 r0), z1 = fma(m11, r1, m10 r0)) */
+static void precondition(const orc_problem *p, const double *r, double *z)
+{
+    if (p->cg_block) {
+#pragma omp parallel for schedule(static)
+        for (int32_t i = 0; i < p->n_nodes; i++) {
+            const double *m = &p->binv[4 * (size_t)i];
+            const double r0 = r[2 * i], r1 = r[2 * i + 1];
+            z[2 * i] = fma(m[1], r1, m[0] * r0);
+            z[2 * i + 1] = fma(m[3], r1, m[2] * r0);
+        }
+    } else {
+#pragma omp parallel for schedule(static)
+        for (int32_t i = 0; i < p->neq; i++) z[i] = r[i] * p->dinv[i];
+    }
+}
+
 int orc_pcg(const orc_problem *p, const double *b, double *x, double rtol, int max_it, double *work)
 {
     const int32_t n = p->neq;
@@ -782,9 +817,10 @@ int orc_pcg(const orc_problem *p, const double *b, double *x, double rtol, int m
     for (int32_t i = 0; i < n; i++) {
         x[i] = 0.0;
         r[i] = b[i];
-        z[i] = r[i] * p->dinv[i];
-        pv[i] = z[i];
     }
+    precondition(p, r, z);
+#pragma omp parallel for schedule(static)
+    for (int32_t i = 0; i < n; i++) pv[i] = z[i];
     const double bb = orc_dot(nn, b, b);
     if (bb == 0.0) return 0;
     const double thr = (rtol * rtol) * bb;
@@ -798,8 +834,8 @@ int orc_pcg(const orc_problem *p, const double *b, double *x, double rtol, int m
         for (int32_t i = 0; i < n; i++) {
             x[i] = fma(alpha, pv[i], x[i]);
             r[i] = fma(-alpha, q[i], r[i]);
-            z[i] = r[i] * p->dinv[i];
         }
+        precondition(p, r, z);
         const double rr = orc_dot(nn, r, r);
         if (rr <= thr) return k;
         const double rzn = orc_dot(nn, r, z);

@@ -74,6 +74,8 @@ typedef struct {
     double *dinv;              /* [neq] */
     int nthreads;
     int32_t order, nn, nq, nd; /* element order; connects, points, dofs per element */
+    double *binv;              /* [n_nodes*4] inverse of each nodal diagonal block on its free dofs */
+    int32_t cg_block;          /* 1: orc_pcg preconditions with binv (block Jacobi), 0: dinv */
 } orc_problem;
 
 orc_problem *orc_problem_create(const orc_params *prm, int nthreads);

@@ -43,7 +43,7 @@ class Problem(C.Structure):
                 ("row_ptr", _lp), ("col", _ip), ("el_blk", _lp), ("eps_p", _dp), ("sigma", _dp),
                 ("mtype", C.POINTER(C.c_int8)), ("alpha", _dp), ("strain", _dp), ("sigma_w", _dp),
                 ("dep", _dp), ("K", _dp), ("dinv", _dp), ("nthreads", C.c_int), ("order", C.c_int32),
-                ("nn", C.c_int32), ("nq", C.c_int32), ("nd", C.c_int32)]
+                ("nn", C.c_int32), ("nq", C.c_int32), ("nd", C.c_int32), ("binv", _dp), ("cg_block", C.c_int32)]
 
 
 class SolveOpts(C.Structure):
@@ -177,7 +177,7 @@ class OracleProblem:
                  "alpha": (self.n_ip, np.float64), "strain": (3 * self.n_ip, np.float64),
                  "sigma_w": (3 * self.n_ip, np.float64), "dep": (9 * self.n_ip, np.float64),
                  "K": (4 * self.n_blocks, np.float64), "dinv": (self.neq, np.float64),
-                 "eps_p0": (6, np.float64)}
+                 "eps_p0": (6, np.float64), "binv": (4 * self.n_nodes, np.float64)}
         n, dt = sizes[name]
         return np.ctypeslib.as_array(getattr(P, name), shape=(int(n),))
 
@@ -200,6 +200,10 @@ class OracleProblem:
         y = np.zeros(self.neq)
         lib().orc_spmv(self._p, ptr(x), ptr(y))
         return y
+
+    def set_block_jacobi(self, on=True):
+        """precondition orc_pcg (and the Newton solve) with the nodal block-Jacobi inverse"""
+        self.P.cg_block = 1 if on else 0
 
     def pcg(self, b, rtol=1e-8, max_it=100000):
         x = np.zeros(self.neq)

@@ -87,3 +87,21 @@ def test_mixed_learned_newton_cfg1_against_fp64_oracle():
                             sg.fcg_fallbacks))
     assert eu < 1e-6 and es < 1e-6 and eep < 1e-6
     assert flips <= 2
+
+
+def test_mixed_block_jacobi():
+    """FP32 block-Jacobi CG inside the FP64 Newton: the same solution as the
+    scalar-Jacobi mixed solve to the Newton tolerance, fewer CG iterations"""
+    res = {}
+    for prec in (ip.PREC_JACOBI, ip.PREC_BLOCK_JACOBI):
+        w = ip.WellboreMesh(ip.wellbore_params(40))
+        sm = ip.ElastoPlasticIntPointsStructMatrix(w)
+        sm.set_precision(ip.MIXED)
+        sm.set_preconditioner(prec)
+        u = np.zeros(sm.neq)
+        st, _ = sm.newton(u, 10, newton_max_it=40, cg_rtol=1e-4)
+        assert st.converged
+        res[prec] = (u, st.cg_iters)
+    (u0, k0), (u1, k1) = res[ip.PREC_JACOBI], res[ip.PREC_BLOCK_JACOBI]
+    assert np.abs(u1 - u0).max() < 1e-6 * np.abs(u0).max()
+    assert k1 < 0.9 * k0, (k1, k0)
