@@ -331,6 +331,8 @@ typedef struct {
     int32_t *connects;
     double *dphi, *weight, *f0, *df, *el_cohesion, *el_phi;
     uint8_t *fixed;
+    uint8_t *el_shape;        /* [n_elements] 0 quadrilateral, 1 triangle (NULL: all quadrilaterals) */
+    int32_t n_ghost;          /* ghost connects of the triangles (fixed, zero shape functions) */
 } ipfem_wellbore;
 
 void ipfem_wellbore_default(ipfem_wellbore_params *p, int32_t n);
@@ -341,6 +343,7 @@ void ipfem_wellbore_free(ipfem_wellbore *w);
 /* The reference reads its geometry with NeoPZ's TPZGmshReader
  * (ReadGeometry, main.cpp:447-464; gmsh/wellbore_*.msh).  This reads the
  * same files: Gmsh 4.1 ASCII with 4-node quadrilaterals (element type 3),
+ * 3-node triangles (type 2; the reference's wellbore_mix.msh mixes both),
  * 2-node lines (type 1) and points (type 15); every element carries the first
  * physical tag of its entity (0 when it has none).  Node indices are 0-based
  * in file order.  Other element types, binary files and other format versions
@@ -357,6 +360,8 @@ typedef struct {
     int32_t n_phys;
     int32_t *phys_dim, *phys_tag;     /* [n_phys] $PhysicalNames */
     char **phys_name;                 /* [n_phys] */
+    int32_t n_tris;
+    int32_t *tris, *tri_phys;         /* [3*n_tris] 3-node triangles (element type 2), [n_tris] */
 } ipfem_gmsh;
 
 ipfem_status ipfem_gmsh_read(const char *path, ipfem_gmsh **out);
@@ -383,7 +388,12 @@ typedef struct {
  * of (order+1)^2 connects, its edge connects equally spaced on the straight
  * edges and its interior connects on the bilinear map (the geometric elements
  * are linear); a shared edge's connects are numbered from its lower-numbered
- * vertex, so that both elements use the same ones.  Connects are numbered
+ * vertex, so that both elements use the same ones.  Triangles of the domain tag
+ * (the reference's mixed mesh wellbore_mix.msh) become order-p Lagrange
+ * triangles carried in the block shape of the order-p quadrilateral: their
+ * (p+1)(p+2)/2 connects, then ghost connects with zero shape functions and
+ * fixed dofs up to (p+1)^2, and (p+1)^2 collapsed-Gauss points; el_shape
+ * marks them and n_ghost counts the ghosts.  Connects are numbered
  * in order of first use by the elements, so that elements close in file
  * order share nearby rows.  Loads go into df (f0 = 0): load factor 1 applies
  * them in full.  mat supplies E, nu, cohesion, phi, psi and sigma0

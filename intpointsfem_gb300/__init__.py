@@ -68,14 +68,15 @@ class WellboreParams(C.Structure):
 class Wellbore(C.Structure):
     _fields_ = [("mesh", Mesh), ("material", Material), ("node_xy", _dp), ("connects", _ip), ("dphi", _dp),
                 ("weight", _dp), ("f0", _dp), ("df", _dp), ("el_cohesion", _dp), ("el_phi", _dp),
-                ("fixed", _bp)]
+                ("fixed", _bp), ("el_shape", _bp), ("n_ghost", C.c_int32)]
 
 
 class GmshData(C.Structure):
     _fields_ = [("n_nodes", C.c_int32), ("xy", _dp), ("n_quads", C.c_int32), ("quads", _ip), ("quad_phys", _ip),
                 ("n_lines", C.c_int32), ("lines", _ip), ("line_phys", _ip), ("n_points", C.c_int32),
                 ("points", _ip), ("point_phys", _ip), ("n_phys", C.c_int32), ("phys_dim", _ip),
-                ("phys_tag", _ip), ("phys_name", C.POINTER(C.c_char_p))]
+                ("phys_tag", _ip), ("phys_name", C.POINTER(C.c_char_p)), ("n_tris", C.c_int32), ("tris", _ip),
+                ("tri_phys", _ip)]
 
 
 class BC(C.Structure):
@@ -188,6 +189,13 @@ def wellbore_params(n, **kw):
     return p
 
 
+class _OwnedArray(np.ndarray):
+    """an ndarray view of library memory that holds a reference to its owner"""
+
+    def __array_finalize__(self, obj):
+        self.owner = getattr(obj, "owner", None)
+
+
 class WellboreMesh:
     """Quarter-annulus wellbore mesh provider (stand-in for the NeoPZ mesh)."""
 
@@ -212,15 +220,19 @@ class WellboreMesh:
         return self._w.contents.material
 
     def array(self, name):
+        """numpy view of one of the problem's arrays; the view (and every view
+        derived from it) keeps the problem alive"""
         w = self._w.contents
         nn = (self.order + 1) ** 2
         n = {"node_xy": 2 * self.n_nodes, "connects": nn * self.n_el, "dphi": 2 * nn * nn * self.n_el,
              "weight": nn * self.n_el, "f0": self.neq, "df": self.neq, "fixed": self.neq,
-             "el_cohesion": self.n_el, "el_phi": self.n_el}[name]
+             "el_cohesion": self.n_el, "el_phi": self.n_el, "el_shape": self.n_el}[name]
         p = getattr(w, name)
         if not p:
             return None
-        return np.ctypeslib.as_array(p, shape=(n,))
+        a = np.ctypeslib.as_array(p, shape=(n,)).view(_OwnedArray)
+        a.owner = self
+        return a
 
     def close(self):
         if self._w:
@@ -252,6 +264,8 @@ class GmshMesh:
         self.xy = arr(g.xy, 2 * g.n_nodes).reshape(-1, 2) if g.n_nodes else np.zeros((0, 2))
         self.quads = arr(g.quads, 4 * g.n_quads).reshape(-1, 4)
         self.quad_phys = arr(g.quad_phys, g.n_quads)
+        self.tris = arr(g.tris, 3 * g.n_tris).reshape(-1, 3)
+        self.tri_phys = arr(g.tri_phys, g.n_tris)
         self.lines = arr(g.lines, 2 * g.n_lines).reshape(-1, 2)
         self.line_phys = arr(g.line_phys, g.n_lines)
         self.points = arr(g.points, g.n_points)
@@ -304,6 +318,8 @@ class GmshProblem(WellboreMesh):
         self.n_nodes = w.mesh.n_nodes
         self.neq = 2 * self.n_nodes
         self.order = int(w.mesh.order)
+        self.n_ghost = int(w.n_ghost)
+        self.n_equations = self.neq - 2 * self.n_ghost     # without the fixed ghost connects of triangles
 
 
 class ElastoPlasticIntPointsStructMatrix:

@@ -121,6 +121,8 @@ extern "C" void ipfem_gmsh_free(ipfem_gmsh *g)
     std::free(g->point_phys);
     std::free(g->phys_dim);
     std::free(g->phys_tag);
+    std::free(g->tris);
+    std::free(g->tri_phys);
     if (g->phys_name)
         for (int32_t i = 0; i < g->n_phys; i++) std::free(g->phys_name[i]);
     std::free(g->phys_name);
@@ -146,7 +148,7 @@ extern "C" ipfem_status ipfem_gmsh_read(const char *path, ipfem_gmsh **out)
     auto ent_key = [](long long dim, long long tag) { return ((uint64_t)dim << 40) ^ (uint64_t)tag; };
     std::unordered_map<long long, int32_t> node_index;
     std::vector<double> xy;
-    std::vector<int32_t> quads, quad_phys, lines, line_phys, points, point_phys, pdim, ptag;
+    std::vector<int32_t> quads, quad_phys, lines, line_phys, points, point_phys, tris, tri_phys, pdim, ptag;
     std::vector<std::string> pname;
     while (true) {
         t.skip_ws();
@@ -228,9 +230,11 @@ extern "C" ipfem_status ipfem_gmsh_read(const char *path, ipfem_gmsh **out)
                 if (type == 15) { nn = 1; conn = &points; phys = &point_phys; }
                 else if (type == 1) { nn = 2; conn = &lines; phys = &line_phys; }
                 else if (type == 3) { nn = 4; conn = &quads; phys = &quad_phys; }
+                else if (type == 2) { nn = 3; conn = &tris; phys = &tri_phys; }
                 else
                     return gmsh_fail("element type " + std::to_string(type) +
-                                     " is not supported (4-node quadrilaterals, 2-node lines and points)");
+                                     " is not supported (4-node quadrilaterals, 3-node triangles, 2-node lines "
+                                     "and points)");
                 auto it = ent_phys.find(ent_key(edim, etag));
                 const int32_t ph = it == ent_phys.end() ? 0 : it->second;
                 for (long long i = 0; i < n && !t.bad; i++) {
@@ -272,12 +276,15 @@ extern "C" ipfem_status ipfem_gmsh_read(const char *path, ipfem_gmsh **out)
     g->n_points = (int32_t)point_phys.size();
     g->points = dup_i32(points);
     g->point_phys = dup_i32(point_phys);
+    g->n_tris = (int32_t)tri_phys.size();
+    g->tris = dup_i32(tris);
+    g->tri_phys = dup_i32(tri_phys);
     g->n_phys = (int32_t)pname.size();
     g->phys_dim = dup_i32(pdim);
     g->phys_tag = dup_i32(ptag);
     g->phys_name = (char **)std::calloc(pname.size() ? pname.size() : 1, sizeof(char *));
     bool ok = g->xy && g->quads && g->quad_phys && g->lines && g->line_phys && g->points && g->point_phys &&
-              g->phys_dim && g->phys_tag && g->phys_name;
+              g->phys_dim && g->phys_tag && g->phys_name && g->tris && g->tri_phys;
     for (size_t i = 0; ok && i < pname.size(); i++) {
         g->phys_name[i] = (char *)std::malloc(pname[i].size() + 1);
         if (!g->phys_name[i]) ok = false;
@@ -308,58 +315,72 @@ extern "C" ipfem_status ipfem_gmsh_problem(const ipfem_gmsh *g, int32_t order, i
         if (ty == 0 && (bcs[b].val[0] != 0.0 || bcs[b].val[1] != 0.0))
             return gmsh_fail("non-zero Dirichlet values are not supported");
     }
-    // the domain's quadrilaterals, in file order
-    std::vector<int32_t> els;
+    // the domain's quadrilaterals, then its triangles, in file order
+    struct El {
+        const int32_t *v;
+        int nv;
+    };
+    std::vector<El> els;
     for (int32_t q = 0; q < g->n_quads; q++)
-        if (domain_phys < 0 || g->quad_phys[q] == domain_phys) els.push_back(q);
-    if (els.empty()) return gmsh_fail("no quadrilateral carries physical tag " + std::to_string(domain_phys));
+        if (domain_phys < 0 || g->quad_phys[q] == domain_phys) els.push_back({&g->quads[4 * (size_t)q], 4});
+    for (int32_t q = 0; q < g->n_tris; q++)
+        if (domain_phys < 0 || g->tri_phys[q] == domain_phys) els.push_back({&g->tris[3 * (size_t)q], 3});
+    if (els.empty()) return gmsh_fail("no element carries physical tag " + std::to_string(domain_phys));
     const int64_t n_el = (int64_t)els.size();
+    const int nt = (p + 1) * (p + 2) / 2;                // connects of a triangle
     // edges: key -> edge index; first element and number of elements per edge
     std::unordered_map<uint64_t, int32_t> edge_of;
     edge_of.reserve((size_t)n_el * 2);
     std::vector<int32_t> edge_el, edge_uses;
-    std::vector<int32_t> el_edge((size_t)n_el * 4);
+    std::vector<int32_t> el_edge((size_t)n_el * 4, -1);
     for (int64_t e = 0; e < n_el; e++) {
-        const int32_t *v = &g->quads[4 * (size_t)els[(size_t)e]];
-        for (int k = 0; k < 4; k++) {
-            const int32_t a = v[k], b = v[(k + 1) & 3];
-            if (a == b) return gmsh_fail("degenerate quadrilateral");
+        const El &E = els[(size_t)e];
+        for (int k = 0; k < E.nv; k++) {
+            const int32_t a = E.v[k], b = E.v[(k + 1) % E.nv];
+            if (a == b) return gmsh_fail("degenerate element");
             auto ins = edge_of.emplace(edge_key(a, b), (int32_t)edge_el.size());
             if (ins.second) {
                 edge_el.push_back((int32_t)e);
                 edge_uses.push_back(0);
             }
             if (++edge_uses[(size_t)ins.first->second] > 2)
-                return gmsh_fail("an edge is shared by more than two quadrilaterals");
+                return gmsh_fail("an edge is shared by more than two elements");
             el_edge[4 * (size_t)e + k] = ins.first->second;
         }
     }
     const int64_t n_edges = (int64_t)edge_el.size();
-    const int64_t n_nodes_max = (int64_t)g->n_nodes + n_edges * ne1 + n_el * ne1 * ne1;
+    const int64_t n_nodes_max = (int64_t)g->n_nodes + n_edges * ne1 + n_el * nn;
     if (2 * n_nodes_max > INT32_MAX || n_el * nn * nn > INT32_MAX) return gmsh_fail("mesh too large");
     // connects numbered in order of first use by the elements; the interior
     // connects of a shared edge are numbered from its lower-numbered vertex
     std::vector<int32_t> vnew((size_t)g->n_nodes, -1), enew((size_t)(n_edges * ne1), -1);
     std::vector<int32_t> conn((size_t)n_el * nn);
+    std::vector<uint8_t> ghost;                          // per connect: 1 = ghost of a triangle
     int32_t next = 0;
+    auto fresh = [&](uint8_t is_ghost) {
+        ghost.push_back(is_ghost);
+        return next++;
+    };
     for (int64_t e = 0; e < n_el; e++) {
-        const int32_t *v = &g->quads[4 * (size_t)els[(size_t)e]];
+        const El &E = els[(size_t)e];
         int32_t *c = &conn[(size_t)nn * e];
-        for (int k = 0; k < 4; k++) {
-            if (vnew[(size_t)v[k]] < 0) vnew[(size_t)v[k]] = next++;
-            c[k] = vnew[(size_t)v[k]];
+        for (int k = 0; k < E.nv; k++) {
+            if (vnew[(size_t)E.v[k]] < 0) vnew[(size_t)E.v[k]] = fresh(0);
+            c[k] = vnew[(size_t)E.v[k]];
         }
-        for (int k = 0; k < 4; k++) {
+        for (int k = 0; k < E.nv; k++) {
             const int32_t ed = el_edge[4 * (size_t)e + k];
-            const bool fwd = v[k] < v[(k + 1) & 3];
+            const bool fwd = E.v[k] < E.v[(k + 1) % E.nv];
             for (int i = 1; i <= ne1; i++) {
                 const int j = fwd ? i : p - i;          // position from the lower vertex
                 int32_t &en = enew[(size_t)ed * ne1 + (j - 1)];
-                if (en < 0) en = next++;
-                c[4 + k * ne1 + (i - 1)] = en;
+                if (en < 0) en = fresh(0);
+                c[E.nv + k * ne1 + (i - 1)] = en;
             }
         }
-        for (int k = 4 + 4 * ne1; k < nn; k++) c[k] = next++;
+        const int first_inner = E.nv + E.nv * ne1, n_real = E.nv == 4 ? nn : nt;
+        for (int k = first_inner; k < n_real; k++) c[k] = fresh(0);
+        for (int k = n_real; k < nn; k++) c[k] = fresh(1);
     }
     const int64_t n_nodes = next, neq = 2 * n_nodes;
     ipfem_wellbore *w = new (std::nothrow) ipfem_wellbore();
@@ -372,24 +393,28 @@ extern "C" ipfem_status ipfem_gmsh_problem(const ipfem_gmsh *g, int32_t order, i
     w->f0 = (double *)std::calloc((size_t)neq, sizeof(double));
     w->df = (double *)std::calloc((size_t)neq, sizeof(double));
     w->fixed = (uint8_t *)std::calloc((size_t)neq, 1);
-    if (!w->node_xy || !w->connects || !w->dphi || !w->weight || !w->f0 || !w->df || !w->fixed) {
+    w->el_shape = (uint8_t *)std::calloc((size_t)n_el, 1);
+    if (!w->node_xy || !w->connects || !w->dphi || !w->weight || !w->f0 || !w->df || !w->fixed || !w->el_shape) {
         ipfem_wellbore_free(w);
         return IPFEM_OOM;
     }
     std::memcpy(w->connects, conn.data(), conn.size() * sizeof(int32_t));
+    for (int64_t e = 0; e < n_el; e++) w->el_shape[e] = els[(size_t)e].nv == 3;
     // coordinates: vertices, equally spaced edge connects, interior connects on
-    // the bilinear map (order 2: the straight-edge midpoints and the centre)
+    // the bilinear (quadrilateral) or affine (triangle) map; ghosts at the
+    // triangle's centre (order 2 quadrilaterals: the straight-edge midpoints
+    // and the centre)
     for (int64_t e = 0; e < n_el; e++) {
-        const int32_t *v = &g->quads[4 * (size_t)els[(size_t)e]];
+        const El &E = els[(size_t)e];
         const int32_t *c = &conn[(size_t)nn * e];
         const double *pv[4];
-        for (int k = 0; k < 4; k++) {
-            pv[k] = &g->xy[2 * (size_t)v[k]];
+        for (int k = 0; k < E.nv; k++) {
+            pv[k] = &g->xy[2 * (size_t)E.v[k]];
             w->node_xy[2 * (size_t)c[k]] = pv[k][0];
             w->node_xy[2 * (size_t)c[k] + 1] = pv[k][1];
         }
-        for (int k = 0; k < 4; k++) {
-            const int32_t va = v[k], vb = v[(k + 1) & 3];
+        for (int k = 0; k < E.nv; k++) {
+            const int32_t va = E.v[k], vb = E.v[(k + 1) % E.nv];
             const double *lo = &g->xy[2 * (size_t)std::min(va, vb)], *hi = &g->xy[2 * (size_t)std::max(va, vb)];
             const int32_t ed = el_edge[4 * (size_t)e + k];
             for (int j = 1; j <= ne1; j++) {
@@ -399,13 +424,16 @@ extern "C" ipfem_status ipfem_gmsh_problem(const ipfem_gmsh *g, int32_t order, i
                                                               : (lo[d] * (p - j) + hi[d] * j) / p;
             }
         }
-        for (int k = 4 + 4 * ne1; k < nn; k++) {
-            const int m = k - 4 - 4 * ne1, ia = m % ne1 + 1, ib = m / ne1 + 1;
+        const int first_inner = E.nv + E.nv * ne1;
+        for (int k = first_inner; k < nn; k++) {
             for (int d = 0; d < 2; d++) {
                 double x;
-                if (p == 2) {
+                if (E.nv == 3) {
+                    x = (pv[0][d] + pv[1][d] + pv[2][d]) / 3.0;     // interior node (order 3) and ghosts
+                } else if (p == 2) {
                     x = 0.25 * (((pv[0][d] + pv[1][d]) + pv[2][d]) + pv[3][d]);
                 } else {
+                    const int m = k - first_inner, ia = m % ne1 + 1, ib = m / ne1 + 1;
                     const double u = (double)ia / p, t = (double)ib / p;
                     x = (1.0 - u) * (1.0 - t) * pv[0][d] + u * (1.0 - t) * pv[1][d] + u * t * pv[2][d] +
                         (1.0 - u) * t * pv[3][d];
@@ -414,7 +442,12 @@ extern "C" ipfem_status ipfem_gmsh_problem(const ipfem_gmsh *g, int32_t order, i
             }
         }
     }
-    element_blocks_dphi(p, n_el, w->connects, w->node_xy, w->dphi, w->weight);
+    element_blocks_dphi(p, n_el, w->connects, w->node_xy, w->dphi, w->weight, w->el_shape);
+    for (int64_t i = 0; i < n_nodes; i++)
+        if (ghost[(size_t)i]) {
+            w->fixed[2 * (size_t)i] = w->fixed[2 * (size_t)i + 1] = 1;
+            w->n_ghost++;
+        }
     // boundary conditions
     for (int32_t b = 0; b < n_bc; b++) {
         const ipfem_bc &bc = bcs[b];
@@ -455,11 +488,11 @@ extern "C" ipfem_status ipfem_gmsh_problem(const ipfem_gmsh *g, int32_t order, i
                 const double dx = pb[0] - pa[0], dy = pb[1] - pa[1];
                 const double L = std::sqrt(dx * dx + dy * dy);
                 double nx = dy / L, ny = -dx / L;
-                const int32_t *ce = &conn[(size_t)nn * edge_el[(size_t)ed]];
+                const El &Ea = els[(size_t)edge_el[(size_t)ed]];
                 double cx = 0.0, cy = 0.0;
-                for (int k = 0; k < 4; k++) {
-                    cx += 0.25 * w->node_xy[2 * (size_t)ce[k]];
-                    cy += 0.25 * w->node_xy[2 * (size_t)ce[k] + 1];
+                for (int k = 0; k < Ea.nv; k++) {
+                    cx += g->xy[2 * (size_t)Ea.v[k]] / Ea.nv;
+                    cy += g->xy[2 * (size_t)Ea.v[k] + 1] / Ea.nv;
                 }
                 if ((cx - 0.5 * (pa[0] + pb[0])) * nx + (cy - 0.5 * (pa[1] + pb[1])) * ny > 0.0) {
                     nx = -nx;

@@ -429,17 +429,88 @@ static void element_dphi(int p, const double *X, const double *Y, double *dphi, 
     }
 }
 
+// barycentric index (i, j, k), i + j + k = p, of connect n of an order-p
+// triangle: vertices, the p-1 nodes of each edge in traversal order (edges
+// v0v1, v1v2, v2v0), the interior node (p = 3)
+static void tri_node(int p, int n, int &i, int &j, int &k)
+{
+    if (n < 3) {
+        i = n == 0 ? p : 0;
+        j = n == 1 ? p : 0;
+        k = n == 2 ? p : 0;
+        return;
+    }
+    n -= 3;
+    if (n < 3 * (p - 1)) {
+        const int e = n / (p - 1), m = n % (p - 1) + 1;
+        if (e == 0) { i = p - m; j = m; k = 0; }
+        else if (e == 1) { i = 0; j = p - m; k = m; }
+        else { i = m; j = 0; k = p - m; }
+        return;
+    }
+    i = j = k = 1;
+}
+
+// l_m(L) = prod_{s<m} (p L - s)/(s + 1) and its derivative in L
+static void bary_factor(int p, int m, double L, double &v, double &d)
+{
+    v = 1.0;
+    d = 0.0;
+    for (int s = 0; s < m; s++) {
+        const double f = (p * L - s) / (s + 1), df = (double)p / (s + 1);
+        d = d * f + v * df;
+        v = v * f;
+    }
+}
+
+// An order-p triangle (Lagrange functions on the equispaced barycentric
+// lattice, affine geometry from its 3 vertex connects) in the block shape of
+// the order-p quadrilateral: its (p+1)(p+2)/2 connects fill the first
+// columns, the remaining columns (ghost connects) are zero; the (p+1)^2
+// points are the collapsed Gauss rule xi = u, eta = v (1 - u) on the unit
+// triangle (u, v on the Gauss points of [0, 1]), weight w_u w_v (1 - u)|det|,
+// exact for the degree-2p integrands of the tangent.
+void tri_element_dphi(int p, const double *X, const double *Y, double *dphi, double *w)
+{
+    const int n1 = p + 1, nn = n1 * n1, nq = n1 * n1, nt = (p + 1) * (p + 2) / 2;
+    double gp[4], gw[4];
+    gauss(p, gp, gw);
+    const double x1 = X[1] - X[0], x2 = X[2] - X[0], y1 = Y[1] - Y[0], y2 = Y[2] - Y[0];
+    const double det = x1 * y2 - x2 * y1;
+    const double xi_x = y2 / det, xi_y = -x2 / det, eta_x = -y1 / det, eta_y = x1 / det;
+    for (int t = 0; t < nq * 2 * nn; t++) dphi[t] = 0.0;
+    for (int iq = 0; iq < nq; iq++) {
+        const int iu = iq % n1, iv = iq / n1;
+        const double u = 0.5 * (1.0 + gp[iu]), v = 0.5 * (1.0 + gp[iv]);
+        const double xi = u, eta = v * (1.0 - u);
+        w[iq] = ((0.5 * gw[iu]) * (0.5 * gw[iv])) * (1.0 - u) * std::fabs(det);
+        const double L[3] = {1.0 - xi - eta, xi, eta};
+        for (int n = 0; n < nt; n++) {
+            int b[3];
+            tri_node(p, n, b[0], b[1], b[2]);
+            double f[3], df[3];
+            for (int c = 0; c < 3; c++) bary_factor(p, b[c], L[c], f[c], df[c]);
+            const double dL0 = df[0] * f[1] * f[2], dL1 = f[0] * df[1] * f[2], dL2 = f[0] * f[1] * df[2];
+            const double Nxi = dL1 - dL0, Neta = dL2 - dL0;
+            dphi[iq * 2 * nn + n] = Nxi * xi_x + Neta * eta_x;
+            dphi[iq * 2 * nn + nn + n] = Nxi * xi_y + Neta * eta_y;
+        }
+    }
+}
+
 void element_blocks_dphi(int order, int64_t n_el, const int32_t *connects, const double *node_xy, double *dphi,
-                         double *weight)
+                         double *weight, const uint8_t *shape)
 {
     const int nn = (order + 1) * (order + 1), nq = nn;
     parallel_for(n_el, [&](int64_t e) {
         double X[4], Y[4];
-        for (int v = 0; v < 4; v++) {
+        const int nv = (shape && shape[e]) ? 3 : 4;
+        for (int v = 0; v < nv; v++) {
             X[v] = node_xy[2 * (size_t)connects[(size_t)nn * e + v]];
             Y[v] = node_xy[2 * (size_t)connects[(size_t)nn * e + v] + 1];
         }
-        element_dphi(order, X, Y, dphi + e * nq * 2 * nn, weight + e * nq);
+        if (nv == 3) tri_element_dphi(order, X, Y, dphi + e * nq * 2 * nn, weight + e * nq);
+        else element_dphi(order, X, Y, dphi + e * nq * 2 * nn, weight + e * nq);
     });
 }
 
@@ -517,6 +588,7 @@ extern "C" void ipfem_wellbore_free(ipfem_wellbore *w)
     std::free(w->el_cohesion);
     std::free(w->el_phi);
     std::free(w->fixed);
+    std::free(w->el_shape);
     delete w;
 }
 

@@ -98,10 +98,12 @@ struct Setup {
 // builds the setup; returns an empty string or an error message
 std::string build_setup(const ipfem_mesh *mesh, const ipfem_material *mat, Setup &s);
 // d(phi)/dx, d(phi)/dy and w|detJ| at the (p+1)^2 Gauss points of order-p
-// Lagrange elements with bilinear geometry from their 4 vertex connects
-// (host, threaded)
+// Lagrange elements with bilinear geometry from their 4 vertex connects, or,
+// where shape[e] = 1, of triangles from their 3 (host, threaded)
 void element_blocks_dphi(int order, int64_t n_el, const int32_t *connects, const double *node_xy, double *dphi,
-                         double *weight);
+                         double *weight, const uint8_t *shape = nullptr);
+// an order-p triangle in the block shape of the order-p quadrilateral (ghost columns zero)
+void tri_element_dphi(int p, const double *X, const double *Y, double *dphi, double *w);
 int32_t greedy_coloring_nn(int32_t n_el, int32_t n_nodes, int32_t nn, const int32_t *connects, int32_t *el_color);
 // SELL-32 layout of s's block pattern; sorted: rows by length inside each
 // kRedBlock-node window (stable, longest first)

@@ -39,9 +39,12 @@ def wellbore_nodes(n, q, r_in=0.1, r_out=4.0):
     return r, th
 
 
-def write_wellbore_msh(path, n, q, r_in=0.1, r_out=4.0):
+def write_wellbore_msh(path, n, q, r_in=0.1, r_out=4.0, tri_quadrants=()):
     """Write the wellbore mesh with n nodes per quarter arc and radial line and
-    radial progression q as a Gmsh 4.1 ASCII file; returns (n_nodes, n_quads)."""
+    radial progression q as a Gmsh 4.1 ASCII file; returns (n_nodes, n_elements).
+    The quadrants listed in tri_quadrants (0-3) are split into triangles (each
+    quadrilateral along its diagonal from its first vertex), as wellbore.geo
+    leaves the surfaces it does not recombine."""
     if n < 2:
         raise ValueError("n must be at least 2")
     r, th = wellbore_nodes(n, q, r_in, r_out)
@@ -100,12 +103,19 @@ def write_wellbore_msh(path, n, q, r_in=0.1, r_out=4.0):
     nq = 0
     for quad in range(4):
         rows = []
+        tri = quad in tri_quadrants
         for j in range(n - 1):                       # radial layer
             for k in range(quad * (n - 1), (quad + 1) * (n - 1)):
-                rows.append("%d %d %d %d %d" % (eid, tag(j, k), tag(j + 1, k), tag(j + 1, k + 1), tag(j, k + 1)))
-                eid += 1
+                v = (tag(j, k), tag(j + 1, k), tag(j + 1, k + 1), tag(j, k + 1))
+                if tri:
+                    rows.append("%d %d %d %d" % (eid, v[0], v[1], v[2]))
+                    rows.append("%d %d %d %d" % (eid + 1, v[0], v[2], v[3]))
+                    eid += 2
+                else:
+                    rows.append("%d %d %d %d %d" % (eid, v[0], v[1], v[2], v[3]))
+                    eid += 1
         nq += len(rows)
-        blocks.append(("2 %d 3 %d" % (quad + 1, len(rows)), rows))
+        blocks.append(("2 %d %d %d" % (quad + 1, 2 if tri else 3, len(rows)), rows))
     lines += ["$Elements", "%d %d 1 %d" % (len(blocks), eid - 1, eid - 1)]
     for head, rows in blocks:
         lines.append(head)

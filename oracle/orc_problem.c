@@ -417,7 +417,11 @@ orc_problem *orc_problem_from_mesh(const orc_mesh_in *m, const orc_params *prm, 
     p->df = (double *)xcalloc((size_t)p->neq, sizeof(double));
     if (m->f0) memcpy(p->f0, m->f0, (size_t)p->neq * sizeof(double));
     if (m->df) memcpy(p->df, m->df, (size_t)p->neq * sizeof(double));
+    p->ext_dphi = m->dphi;
+    p->ext_weight = m->weight;
     problem_setup(p, prm);
+    p->ext_dphi = NULL;
+    p->ext_weight = NULL;
     return p;
 }
 
@@ -466,7 +470,27 @@ static void problem_setup(orc_problem *p, const orc_params *prm)
     const int nn = p->nn, nd = p->nd;
     p->B = (double *)xcalloc((size_t)p->n_el * 3 * p->nq * nd, sizeof(double));
     p->weight = (double *)xcalloc((size_t)p->n_ip, sizeof(double));
-    orc_element_blocks(p->order, p->n_el, p->connects, p->node_xy, p->B, p->weight);
+    if (p->ext_dphi && p->ext_weight) {
+        /* the caller's compact blocks into the fStorage layout */
+        const int nq = p->nq, nb = 3 * nq * nd;
+        for (int32_t e = 0; e < p->n_el; e++)
+            for (int q = 0; q < nq; q++) {
+                const double *dx = &p->ext_dphi[(((size_t)e * nq + q) * 2 + 0) * nn];
+                const double *dy = &p->ext_dphi[(((size_t)e * nq + q) * 2 + 1) * nn];
+                double *r0 = &p->B[(size_t)e * nb + (3 * q + 0) * nd];
+                double *r1 = &p->B[(size_t)e * nb + (3 * q + 1) * nd];
+                double *r2 = &p->B[(size_t)e * nb + (3 * q + 2) * nd];
+                for (int n = 0; n < nn; n++) {
+                    r0[2 * n] = dx[n];
+                    r1[2 * n] = dy[n];
+                    r1[2 * n + 1] = dx[n];
+                    r2[2 * n + 1] = dy[n];
+                }
+            }
+        memcpy(p->weight, p->ext_weight, (size_t)p->n_ip * sizeof(double));
+    } else {
+        orc_element_blocks(p->order, p->n_el, p->connects, p->node_xy, p->B, p->weight);
+    }
     p->dofs = (int32_t *)xcalloc((size_t)p->n_el * nd, sizeof(int32_t));
     for (size_t k = 0; k < (size_t)p->n_el * nn; k++) {
         p->dofs[2 * k] = 2 * p->connects[k];

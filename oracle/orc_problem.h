@@ -76,6 +76,7 @@ typedef struct {
     int32_t order, nn, nq, nd; /* element order; connects, points, dofs per element */
     double *binv;              /* [n_nodes*4] inverse of each nodal diagonal block on its free dofs */
     int32_t cg_block;          /* 1: orc_pcg preconditions with binv (block Jacobi), 0: dinv */
+    const double *ext_dphi, *ext_weight;   /* caller's element blocks during construction only */
 } orc_problem;
 
 orc_problem *orc_problem_create(const orc_params *prm, int nthreads);
@@ -88,6 +89,10 @@ typedef struct {
     const uint8_t *fixed;      /* [2*n_nodes] or NULL */
     const double *f0, *df;     /* [2*n_nodes] or NULL */
     int32_t order;             /* 1, 2 or 3 (0 = 2) */
+    /* element blocks given by the caller (elements that are not bilinear
+     * quadrilaterals, e.g. padded triangles), or NULL: computed from node_xy */
+    const double *dphi;        /* [n_el*nq*2*nn] d(phi_n)/d(x_d) at point q, ((e*nq+q)*2+d)*nn+n */
+    const double *weight;      /* [n_el*nq] */
 } orc_mesh_in;
 orc_problem *orc_problem_from_mesh(const orc_mesh_in *m, const orc_params *prm, int nthreads);
 void orc_problem_destroy(orc_problem *p);

@@ -43,7 +43,8 @@ class Problem(C.Structure):
                 ("row_ptr", _lp), ("col", _ip), ("el_blk", _lp), ("eps_p", _dp), ("sigma", _dp),
                 ("mtype", C.POINTER(C.c_int8)), ("alpha", _dp), ("strain", _dp), ("sigma_w", _dp),
                 ("dep", _dp), ("K", _dp), ("dinv", _dp), ("nthreads", C.c_int), ("order", C.c_int32),
-                ("nn", C.c_int32), ("nq", C.c_int32), ("nd", C.c_int32), ("binv", _dp), ("cg_block", C.c_int32)]
+                ("nn", C.c_int32), ("nq", C.c_int32), ("nd", C.c_int32), ("binv", _dp), ("cg_block", C.c_int32),
+                ("ext_dphi", _dp), ("ext_weight", _dp)]
 
 
 class SolveOpts(C.Structure):
@@ -54,7 +55,7 @@ class SolveOpts(C.Structure):
 
 class MeshIn(C.Structure):
     _fields_ = [("n_el", C.c_int32), ("n_nodes", C.c_int32), ("node_xy", _dp), ("connects", _ip),
-                ("fixed", _bp), ("f0", _dp), ("df", _dp), ("order", C.c_int32)]
+                ("fixed", _bp), ("f0", _dp), ("df", _dp), ("order", C.c_int32), ("dphi", _dp), ("weight", _dp)]
 
 
 class SolveStats(C.Structure):
@@ -131,7 +132,8 @@ class OracleProblem:
 
     def __init__(self, params, nthreads=0, mesh=None):
         """the structured quarter annulus of `params`, or with mesh = dict(node_xy,
-        connects, fixed, f0, df[, order]) a caller's mesh of order 1, 2 or 3
+        connects, fixed, f0, df[, order][, dphi, weight]) a caller's mesh of order
+        1, 2 or 3, its element blocks computed from the coordinates or given
         (params then give the material and in-situ stress only)"""
         self.params = params
         if mesh is None:
@@ -141,8 +143,10 @@ class OracleProblem:
                  (("node_xy", np.float64), ("connects", np.int32), ("fixed", np.uint8), ("f0", np.float64),
                   ("df", np.float64))}
             order = int(mesh.get("order", 2))
+            ext = {k: np.ascontiguousarray(mesh[k], dtype=np.float64) for k in ("dphi", "weight") if k in mesh}
             m = MeshIn(a["connects"].size // (order + 1) ** 2, a["node_xy"].size // 2, ptr(a["node_xy"]),
-                       ptr(a["connects"]), ptr(a["fixed"]), ptr(a["f0"]), ptr(a["df"]), order)
+                       ptr(a["connects"]), ptr(a["fixed"]), ptr(a["f0"]), ptr(a["df"]), order,
+                       ptr(ext.get("dphi")), ptr(ext.get("weight")))
             self._p = lib().orc_problem_from_mesh(C.byref(m), C.byref(params), int(nthreads))
         P = self._p.contents
         self.P = P

@@ -209,3 +209,49 @@ def test_oracle_replays_the_logged_runs(tmp_path, accel, variant, iters, tol_ear
         assert abs(rh.ratios(ours)[-1] - rh.ratios(ref["residue"])[-1]) < 1e-3
     else:
         assert it_ours == it_ref == ref["iterations"]
+
+
+@pytest.mark.parametrize("order", [1, 2, 3])
+def test_mixed_mesh_triangles(tmp_path, order):
+    """triangles (two quadrants split, as wellbore.geo leaves the surfaces it
+    does not recombine) of order p in the order-p block shape: ghost columns
+    zero and ghost dofs fixed, Lagrange connects shared with the neighbouring
+    quadrilaterals, a linear field's strain exact, the quadrature area equal to
+    the all-quadrilateral mesh's, and the equations without ghosts as counted
+    from the mesh's vertices, edges and faces"""
+    path = str(tmp_path / "mix.msh")
+    gw.write_wellbore_msh(path, 9, 1.3, tri_quadrants=(1, 3))
+    g = ip.GmshMesh(path)
+    assert len(g.tris) == 2 * 2 * 8 * 8 and len(g.quads) == 2 * 8 * 8
+    pb = _problem(g, order=order)
+    nn, nt = (order + 1) ** 2, (order + 1) * (order + 2) // 2
+    shape = pb.array("el_shape").astype(bool)
+    assert shape.sum() == len(g.tris)
+    dphi = pb.array("dphi").reshape(-1, nn, 2, nn)
+    con = pb.array("connects").reshape(-1, nn)
+    xy = pb.array("node_xy").reshape(-1, 2)
+    fixed = pb.array("fixed").reshape(-1, 2)
+    assert not dphi[shape][:, :, :, nt:].any()
+    ghosts = np.unique(con[shape][:, nt:])
+    assert ghosts.size == pb.n_ghost == shape.sum() * (nn - nt) and fixed[ghosts].all()
+    ux = 1e-3 * xy[:, 0] + 2e-3 * xy[:, 1]
+    assert np.abs(np.einsum("eqn,en->eq", dphi[:, :, 0, :], ux[con]) - 1e-3).max() < 1e-12
+    assert np.abs(np.einsum("eqn,en->eq", dphi[:, :, 1, :], ux[con]) - 2e-3).max() < 1e-12
+    gw.write_wellbore_msh(str(tmp_path / "q.msh"), 9, 1.3)
+    area_q = _problem(ip.GmshMesh(str(tmp_path / "q.msh")), order=order).array("weight").sum()
+    assert abs(pb.array("weight").sum() - area_q) < 1e-12 * area_q
+    V = len(g.xy)
+    E = (4 * len(g.quads) + 3 * len(g.tris) + 8 * 8) // 2
+    real = V + (order - 1) * E + (order - 1) ** 2 * len(g.quads) + (1 if order == 3 else 0) * len(g.tris)
+    assert pb.n_equations == 2 * real
+    nc, _ = ip.color_elements(con, pb.n_nodes, nn)
+    assert nc <= 16
+
+
+@pytest.mark.skipif(not os.path.isdir(REF_GMSH), reason="reference meshes not present")
+def test_reference_mixed_mesh_reads(tmp_path):
+    g = ip.GmshMesh(os.path.join(REF_GMSH, "wellbore_mix.msh"))
+    assert len(g.quads) == 64 and len(g.tris) == 208 and len(g.lines) == 48 and len(g.points) == 4
+    for order in (1, 2, 3):
+        pb = _problem(g, order=order)
+        assert pb.n_el == 272 and pb.array("el_shape").sum() == 208

@@ -198,3 +198,56 @@ def test_line_probe_of_the_solution_matches_the_reference_fem(tmp_path):
     assert eu < 2e-2 and es < 5e-2
     assert abs(plastic.max() - 0.162) < 0.01
     S.write_vtk(str(tmp_path / "solution.vtk"))
+
+
+def _mixed(tmp_path, n, q, order):
+    path = str(tmp_path / ("mix_%d.msh" % n))
+    gw.write_wellbore_msh(path, n, q, tri_quadrants=(1, 3))
+    bcs, mat = gw.reference_bcs()
+    return ip.GmshProblem(ip.GmshMesh(path), bcs, order=order, **mat)
+
+
+@pytest.mark.parametrize("order", [1, 2, 3])
+def test_mixed_mesh_bit_exact_with_oracle(tmp_path, order):
+    """a mixed triangle/quadrilateral mesh (triangles in the padded block shape)
+    through the full-tangent and the initial-stiffness Newton iterations:
+    bit-identical to the oracle run on the same element blocks"""
+    pb = _mixed(tmp_path, 9, 1.3, order)
+    mesh = {k: pb.array(k) for k in ("node_xy", "connects", "fixed", "f0", "df", "dphi", "weight")}
+    mesh["order"] = order
+    for tangent in (0, 1):
+        sm = ip.ElastoPlasticIntPointsStructMatrix(pb)
+        prm = po.default_params(4, E=2000.0, nu=0.2, cohesion=5.0, phi_deg=20.0, psi_deg=20.0, sxx0=0.0,
+                                syy0=0.0, szz0=0.0, sxy0=0.0)
+        P = po.OracleProblem(prm, mesh=mesh)
+        assert sm.n_colors == P.n_colors
+        sm.set_newton_tangent(tangent)
+        ug, uo = np.zeros(sm.neq), np.zeros(sm.neq)
+        sg, lg = sm.newton(ug, 1, newton_rtol=1e-12, newton_max_it=5, cg_rtol=1e-10)
+        so, lo = P.solve_steps(uo, 1, newton_rtol=1e-12, newton_max_it=5, cg_rtol=1e-10, tangent_mode=tangent)
+        assert sg.newton_iters == so.newton_iters and sg.cg_iters == so.cg_iters
+        assert np.array_equal(lg, lo) and np.array_equal(ug, uo)
+        ghosts = pb.array("fixed").reshape(-1, 2).all(1)
+        assert not ug.reshape(-1, 2)[ghosts].any()
+
+
+def test_mixed_mesh_solution_matches_the_quadrilateral_one(tmp_path):
+    """the verification configuration on mesh 1 with two quadrants split into
+    triangles (order 2): the wellbore displacement and the plastic radius agree
+    with the all-quadrilateral solution of the same mesh"""
+    n, q = gw.REFERENCE_MESHES[1]
+    res = {}
+    for mixed in (False, True):
+        pb = _mixed(tmp_path, n, q, 2) if mixed else _problem(tmp_path, n, q)
+        sm = ip.ElastoPlasticIntPointsStructMatrix(pb)
+        sm.set_preconditioner(ip.PREC_BLOCK_JACOBI)
+        u = np.zeros(sm.neq)
+        st, _ = sm.newton(u, 1, newton_rtol=1e-9, newton_max_it=60, cg_rtol=1e-10)
+        assert st.converged
+        xy = pb.array("node_xy").reshape(-1, 2)
+        well = np.isclose(np.hypot(xy[:, 0], xy[:, 1]), 0.1, atol=1e-9)
+        ur = (u.reshape(-1, 2)[well] * xy[well]).sum(1) / 0.1
+        res[mixed] = (ur.mean(), ur.min(), ur.max())
+    print("wellbore radial displacement, quadrilaterals %.6e, mixed %.6e (min %.6e max %.6e)"
+          % (res[False][0], res[True][0], res[True][1], res[True][2]))
+    assert abs(res[True][0] / res[False][0] - 1) < 5e-3
