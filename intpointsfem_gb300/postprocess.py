@@ -10,12 +10,14 @@ Here, on the host with numpy (post-processing is not on the solver's path):
   - integration-point fields from the solution: total strain B u (tensor
     components, epsilon_xy = gamma_xy / 2, epsilon_zz = 0 in plane strain),
     the committed stress and plastic strain, m_type as the failure type;
-  - a lumped L2 projection of every field onto the nodes (connects):
-    f_n = sum_e sum_q N_n(x_q) w_q f_q / sum_e sum_q N_n(x_q) w_q;
+  - an L2 projection of every field onto each element's Lagrange space,
+    averaged at the shared connects weighted by element area;
   - point evaluation on the finite-element space (the displacement itself,
     the projected fields), with the bilinear geometry inverted by Newton;
   - line probes as CSV with the reference's columns, and a legacy VTK file
-    (VTK_QUAD, VTK_BIQUADRATIC_QUAD or VTK_LAGRANGE_QUADRILATERAL by order).
+    (VTK_QUAD, VTK_BIQUADRATIC_QUAD or VTK_LAGRANGE_QUADRILATERAL by order;
+    triangles of mixed meshes as VTK_TRIANGLE, VTK_QUADRATIC_TRIANGLE or
+    VTK_LAGRANGE_TRIANGLE, their ghost connects left out).
 Tensors are written as 3x3 row-major (xx, xy, xz, yx, yy, yz, zx, zy, zz).
 """
 import numpy as np
@@ -62,6 +64,42 @@ def gauss(p):
     return x, w
 
 
+def tri_nodes(p):
+    """barycentric indices (i, j, k) of the connects of an order-p triangle, in the
+    library's order: vertices, the p-1 nodes of each edge in traversal order
+    (v0v1, v1v2, v2v0), the interior node (p = 3)"""
+    out = [(p, 0, 0), (0, p, 0), (0, 0, p)]
+    for e in range(3):
+        for m in range(1, p):
+            out.append([(p - m, m, 0), (0, p - m, m), (m, 0, p - m)][e])
+    if p == 3:
+        out.append((1, 1, 1))
+    return out
+
+
+def tri_shape(p, xi, eta, nn):
+    """[nn, len(xi)] Lagrange functions of an order-p triangle at (xi, eta) of the
+    unit triangle, zero rows for the ghost connects up to nn"""
+    xi, eta = np.asarray(xi, dtype=np.float64), np.asarray(eta, dtype=np.float64)
+    L = (1.0 - xi - eta, xi, eta)
+    out = np.zeros((nn,) + xi.shape)
+    for n, b in enumerate(tri_nodes(p)):
+        v = np.ones_like(xi)
+        for c in range(3):
+            for s_ in range(b[c]):
+                v = v * (p * L[c] - s_) / (s_ + 1)
+        out[n] = v
+    return out
+
+
+def tri_points(p):
+    """the collapsed Gauss points (xi, eta) of the library's order-p triangles"""
+    gp, _ = gauss(p)
+    n1 = p + 1
+    u, v = 0.5 * (1 + np.tile(gp, n1)), 0.5 * (1 + np.repeat(gp, n1))
+    return u, v * (1 - u)
+
+
 class Solution:
     """A solution on a problem (WellboreMesh or GmshProblem): u [neq] and the
     committed state sigma [4][n_ip], eps_p [4][n_ip] (xx, xy, yy, zz), m_type [n_ip]."""
@@ -70,6 +108,9 @@ class Solution:
         self.order = problem.order
         self.nn = (self.order + 1) ** 2
         self.con = problem.array("connects").reshape(-1, self.nn).astype(np.int64)
+        sh = problem.array("el_shape")
+        self.tri = np.zeros(len(self.con), bool) if sh is None else np.asarray(sh).astype(bool)
+        self.nt = (self.order + 1) * (self.order + 2) // 2
         self.xy = problem.array("node_xy").reshape(-1, 2).copy()
         self.dphi = problem.array("dphi").reshape(-1, self.nn, 2, self.nn)
         self.weight = problem.array("weight").reshape(-1, self.nn)
@@ -97,31 +138,52 @@ class Solution:
         return cls(problem, u, sm.get_state(1), sm.get_state(0), sm.get_state(3))
 
     def nodal(self):
-        """lumped L2 projection of the integration-point fields onto the connects"""
+        """L2 projection of the integration-point fields onto each element's
+        Lagrange space (M_e c = b_e with M_e = sum_q w_q N N^T), averaged at the
+        shared connects weighted by element area"""
         if self._nodal is None:
             gp, _ = gauss(self.order)
             n1 = self.order + 1
-            N = shape(self.order, np.tile(gp, n1), np.repeat(gp, n1))      # [n, q]
-            wN = np.einsum("nq,eq->enq", N, self.weight)                   # [e, n, q]
+            Nq = shape(self.order, np.tile(gp, n1), np.repeat(gp, n1))     # [nn, q]
+            Nt = tri_shape(self.order, *tri_points(self.order), self.nt)   # [nt, q]
             den = np.zeros(len(self.xy))
-            np.add.at(den, self.con, wN.sum(2))
-            self._nodal = {}
-            for k, f in self.ip.items():
-                fq = f.reshape(self.weight.shape[0], self.nn, -1)          # [e, q, c]
-                num = np.zeros((len(self.xy), fq.shape[2]))
-                np.add.at(num, self.con, np.einsum("enq,eqc->enc", wN, fq))
-                self._nodal[k] = num / den[:, None]
+            num = {k: np.zeros((len(self.xy), f.shape[1])) for k, f in self.ip.items()}
+            n_el = self.weight.shape[0]
+            for mask, N in ((~self.tri, Nq), (self.tri, Nt)):
+                if not mask.any():
+                    continue
+                n = N.shape[0]
+                w = self.weight[mask]                                       # [E, q]
+                M = np.einsum("nq,mq,eq->enm", N, N, w)
+                area = w.sum(1)
+                con = self.con[mask][:, :n]
+                np.add.at(den, con, np.repeat(area[:, None], n, 1))
+                for k, f in self.ip.items():
+                    fq = f.reshape(n_el, self.nn, -1)[mask]                 # [E, q, c]
+                    c = np.linalg.solve(M, np.einsum("nq,eq,eqc->enc", N, w, fq))
+                    np.add.at(num[k], con, c * area[:, None, None])
+            # ghost connects of triangles belong to no element's space: 0 there
+            self._nodal = {k: np.divide(v, den[:, None], out=np.zeros_like(v), where=den[:, None] != 0)
+                           for k, v in num.items()}
         return self._nodal
 
     def locate(self, pts, tol=1e-10):
         """element and reference coordinates of each point (element -1 outside)"""
         V = self.xy[self.con[:, :4]]                                       # [e, 4, 2]
+        V[self.tri, 3] = V[self.tri, 2]                                    # triangles: 3 vertices
         lo, hi = V.min(1) - 1e-12, V.max(1) + 1e-12
         el = np.full(len(pts), -1)
         ref = np.zeros((len(pts), 2))
         for i, x in enumerate(np.asarray(pts, dtype=np.float64)):
             for e in np.nonzero(np.all((x >= lo) & (x <= hi), 1))[0]:
                 v = V[e]
+                if self.tri[e]:
+                    J = np.stack([v[1] - v[0], v[2] - v[0]], 1)
+                    s = np.linalg.solve(J, x - v[0])
+                    if s.min() >= -tol and s.sum() <= 1 + tol:
+                        el[i], ref[i] = e, s
+                        break
+                    continue
                 s = np.zeros(2)
                 for _ in range(30):
                     xi, et = s
@@ -146,6 +208,9 @@ class Solution:
         el, ref = self.locate(pts)
         ok = el >= 0
         N = shape(self.order, ref[:, 0], ref[:, 1]).T                      # [pts, n]
+        on_tri = ok & self.tri[np.maximum(el, 0)]
+        if on_tri.any():
+            N[on_tri] = tri_shape(self.order, ref[on_tri, 0], ref[on_tri, 1], self.nn).T
         nodes = self.con[np.maximum(el, 0)]                                # [pts, n]
         out = {"Displacement": np.einsum("pn,pnc->pc", N, self.u[nodes])}
         for k, f in self.nodal().items():
@@ -178,6 +243,7 @@ class Solution:
         """legacy ASCII VTK unstructured grid of the connects with the projected fields"""
         p = self.order
         cell_type = {1: 9, 2: 28, 3: 70}[p]
+        tri_type = {1: 5, 2: 22, 3: 69}[p]                                 # triangles: ghosts left out
         perm = list(range(self.nn))
         if p == 3:
             # VTK runs edge 2 from v3 to v2 and edge 3 from v0 to v3
@@ -186,15 +252,18 @@ class Solution:
             perm[e3:e3 + p - 1] = perm[e3:e3 + p - 1][::-1]
         nodal = self.nodal()
         n_el, n_pt = self.con.shape[0], len(self.xy)
+        cells = [self.con[e, :self.nt] if self.tri[e] else self.con[e, perm] for e in range(n_el)]
+        n_ent = sum(len(c) + 1 for c in cells)
         with open(path, "w") as f:
             f.write("# vtk DataFile Version 3.0\nelastoplastic solution, order %d\nASCII\n"
                     "DATASET UNSTRUCTURED_GRID\n" % p)
             f.write("POINTS %d double\n" % n_pt)
             np.savetxt(f, np.concatenate([self.xy, np.zeros((n_pt, 1))], 1), fmt="%.15g")
-            f.write("CELLS %d %d\n" % (n_el, n_el * (self.nn + 1)))
-            np.savetxt(f, np.concatenate([np.full((n_el, 1), self.nn), self.con[:, perm]], 1), fmt="%d")
+            f.write("CELLS %d %d\n" % (n_el, n_ent))
+            for c in cells:
+                f.write("%d %s\n" % (len(c), " ".join(str(int(v)) for v in c)))
             f.write("CELL_TYPES %d\n" % n_el)
-            np.savetxt(f, np.full(n_el, cell_type), fmt="%d")
+            np.savetxt(f, np.where(self.tri, tri_type, cell_type), fmt="%d")
             f.write("POINT_DATA %d\n" % n_pt)
             f.write("SCALARS FailureType double 1\nLOOKUP_TABLE default\n")
             np.savetxt(f, nodal["FailureType"][:, 0], fmt="%.10g")

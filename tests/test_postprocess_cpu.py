@@ -75,3 +75,31 @@ def test_vtk_file(tmp_path, order):
     for name in ("SCALARS FailureType double 1", "VECTORS Displacement double", "TENSORS Stress double",
                  "TENSORS Strain double", "TENSORS StrainPlastic double"):
         assert name in lines
+
+
+@pytest.mark.parametrize("order", [1, 2, 3])
+def test_mixed_mesh_probe_and_vtk(tmp_path, order):
+    """the same checks on a mixed triangle/quadrilateral mesh: a linear field
+    and constant state reproduced along a probe that crosses both kinds of
+    element, triangle cells in the VTK file without their ghost connects"""
+    path = str(tmp_path / "mix.msh")
+    gw.write_wellbore_msh(path, 9, 1.3, tri_quadrants=(1, 3))
+    bcs, mat = gw.reference_bcs()
+    pb = ip.GmshProblem(ip.GmshMesh(path), bcs, order=order, **mat)
+    xy = pb.array("node_xy").reshape(-1, 2)
+    u = np.stack([1e-3 * xy[:, 0] + 2e-3 * xy[:, 1], -0.5e-3 * xy[:, 0] + 3e-3 * xy[:, 1]], 1).ravel()
+    n_ip = pb.array("weight").size
+    sig = np.tile(np.array([-1.0, 0.5, -2.0, -0.6])[:, None], (1, n_ip))
+    S = pp.Solution(pb, u, sig, np.zeros((4, n_ip)), np.ones(n_ip))
+    rows = S.line_probe((2.0, 0.5), (-2.0, 1.0), 81)                  # quadrant 0 -> quadrant 1 (triangles)
+    c = {k: i for i, k in enumerate(pp.COLUMNS)}
+    X, Y = rows[:, c["Points:0"]], rows[:, c["Points:1"]]
+    assert rows[:, c["vtkValidPointMask"]].min() == 1.0
+    assert np.abs(rows[:, c["Displacement:0"]] - (1e-3 * X + 2e-3 * Y)).max() < 1e-15
+    assert np.abs(rows[:, c["Strain:1"]] - 0.75e-3).max() < 1e-12
+    assert np.abs(rows[:, c["Stress:4"]] + 2.0).max() < 1e-12
+    S.write_vtk(str(tmp_path / "m.vtk"))
+    lines = open(tmp_path / "m.vtk").read().split("\n")
+    k = lines.index("CELL_TYPES %d" % pb.n_el)
+    types = np.array(lines[k + 1:k + 1 + pb.n_el], dtype=int)
+    assert (types == {1: 5, 2: 22, 3: 69}[order]).sum() == pb.array("el_shape").sum()
