@@ -14,7 +14,9 @@ from oracle import pyoracle as po  # noqa: E402
 
 import replay_helpers as rh  # noqa: E402
 
-REF_GMSH = "/root/reference/gmsh"
+from oracle.build import reference_dir  # noqa: E402
+
+REF_GMSH = os.path.join(reference_dir(), "gmsh")
 
 
 def _mesh(tmp_path, k):

@@ -11,7 +11,9 @@ ip = pytest.importorskip("intpointsfem_gb300")
 from intpointsfem_gb300 import gmsh_wellbore as gw  # noqa: E402
 from intpointsfem_gb300 import postprocess as pp  # noqa: E402
 
-REF_CSV = "/root/reference/mathematica_notebooks/RK_Verification/ElastoPlasticFEMdata.csv"
+from oracle.build import reference_dir  # noqa: E402
+
+REF_CSV = os.path.join(reference_dir(), "mathematica_notebooks", "RK_Verification", "ElastoPlasticFEMdata.csv")
 
 
 def _problem(tmp_path, order, n=12, q=1.3):
