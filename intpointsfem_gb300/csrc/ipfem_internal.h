@@ -239,6 +239,9 @@ void launch_patch_features(ipfem_ctx *c, float *d_X);
 void launch_patch_net(ipfem_ctx *c, int64_t rows, const float *d_X, float *d_O);
 // tcgen05 network kernel (k_net_tc.cu)
 cudaError_t net_tc_configure();
+// C = op(A) op(B) on tcgen05 (BF16 operands, FP32 accumulation), split K over gridDim.z
+void launch_gemm_tc(ipfem_ctx *c, int M, int N, int K, const float *A, int lda, int transA, const float *B, int ldb,
+                    int transB, float *C, int ldc, int kchunk, int splits);
 void launch_patch_net_tc(ipfem_ctx *c, int64_t rows, const float *d_X, float *d_O);
 void launch_patch_operator(ipfem_ctx *c);
 void launch_fcg_init(ipfem_ctx *c, const double *d_b, double scale, float rtol, int max_it);

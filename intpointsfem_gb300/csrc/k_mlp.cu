@@ -43,102 +43,8 @@ __device__ __forceinline__ uint32_t pack_bf16(float lo, float hi)
     return *reinterpret_cast<uint32_t *>(&v);
 }
 
-__device__ __forceinline__ float bf16r(float x)
-{
-    return __bfloat162float(__float2bfloat16_rn(x));
-}
-
-__device__ __forceinline__ void mma_bf16(float (&d)[4], const uint32_t (&a)[4], const uint32_t (&b)[2])
-{
-    asm volatile(
-        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
-        "{%0,%1,%2,%3};\n"
-        : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
-        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
-}
-
-// ------------------------------------------------------------------ GEMM
-// C[M][N] = op(A)[M][K] op(B)[K][N].  A and B are FP32 in global memory and
-// rounded to BF16 when staged; FP32 accumulation.
-//   transA = 0: A[m][k] = A[m*lda + k];   transA = 1: A[m][k] = A[k*lda + m]
-//   transB = 0: B[k][n] = B[k*ldb + n];   transB = 1: B[k][n] = B[n*ldb + k]
-// 64x64 tile per CTA, K step 32, 4 warps as 2 x 2, each warp 32 x 32.
-// Split K: CTA z covers k in [z*kchunk, (z+1)*kchunk) and writes its partial
-// product to C + z*M*ldc (kchunk a multiple of 32; one split writes C itself).
-constexpr int GT = 64, GK = 32, GPAD = 8;
-
-__global__ void __launch_bounds__(128) k_gemm_bf16(int M, int N, int K, const float *__restrict__ A, int lda, int transA,
-                                                   const float *__restrict__ B, int ldb, int transB,
-                                                   float *__restrict__ C, int ldc, int kchunk)
-{
-    __shared__ __align__(16) __nv_bfloat16 sA[GT][GK + GPAD];   // [m][k]
-    __shared__ __align__(16) __nv_bfloat16 sB[GT][GK + GPAD];   // [n][k]
-    const int m0 = blockIdx.y * GT, n0 = blockIdx.x * GT;
-    const int kb = blockIdx.z * kchunk, ke = min(K, kb + kchunk);
-    C += (size_t)blockIdx.z * M * ldc;
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int wm = (warp >> 1) * 32, wn = (warp & 1) * 32;
-    const int g = lane >> 2, t = lane & 3;
-    float acc[2][4][4];
-#pragma unroll
-    for (int i = 0; i < 2; i++)
-#pragma unroll
-        for (int j = 0; j < 4; j++)
-#pragma unroll
-            for (int r = 0; r < 4; r++) acc[i][j][r] = 0.f;
-    for (int k0 = kb; k0 < ke; k0 += GK) {
-        for (int e = threadIdx.x; e < GT * GK; e += 128) {
-            int mm, kk;
-            if (transA) { kk = e / GT; mm = e % GT; } else { mm = e / GK; kk = e % GK; }
-            const int gm = m0 + mm, gk = k0 + kk;
-            float v = 0.f;
-            if (gm < M && gk < ke) v = transA ? A[(size_t)gk * lda + gm] : A[(size_t)gm * lda + gk];
-            sA[mm][kk] = __float2bfloat16_rn(v);
-        }
-        for (int e = threadIdx.x; e < GT * GK; e += 128) {
-            int nn, kk;
-            if (transB) { nn = e / GK; kk = e % GK; } else { kk = e / GT; nn = e % GT; }
-            const int gn = n0 + nn, gk = k0 + kk;
-            float v = 0.f;
-            if (gn < N && gk < ke) v = transB ? B[(size_t)gn * ldb + gk] : B[(size_t)gk * ldb + gn];
-            sB[nn][kk] = __float2bfloat16_rn(v);
-        }
-        __syncthreads();
-#pragma unroll
-        for (int ks = 0; ks < GK; ks += 16) {
-            uint32_t af[2][4], bf[4][2];
-#pragma unroll
-            for (int i = 0; i < 2; i++) {
-                const int r0 = wm + 16 * i + g;
-                af[i][0] = *reinterpret_cast<const uint32_t *>(&sA[r0][ks + 2 * t]);
-                af[i][1] = *reinterpret_cast<const uint32_t *>(&sA[r0 + 8][ks + 2 * t]);
-                af[i][2] = *reinterpret_cast<const uint32_t *>(&sA[r0][ks + 8 + 2 * t]);
-                af[i][3] = *reinterpret_cast<const uint32_t *>(&sA[r0 + 8][ks + 8 + 2 * t]);
-            }
-#pragma unroll
-            for (int j = 0; j < 4; j++) {
-                const int c0 = wn + 8 * j + g;
-                bf[j][0] = *reinterpret_cast<const uint32_t *>(&sB[c0][ks + 2 * t]);
-                bf[j][1] = *reinterpret_cast<const uint32_t *>(&sB[c0][ks + 8 + 2 * t]);
-            }
-#pragma unroll
-            for (int i = 0; i < 2; i++)
-#pragma unroll
-                for (int j = 0; j < 4; j++) mma_bf16(acc[i][j], af[i], bf[j]);
-        }
-        __syncthreads();
-    }
-#pragma unroll
-    for (int i = 0; i < 2; i++)
-#pragma unroll
-        for (int j = 0; j < 4; j++)
-#pragma unroll
-            for (int r = 0; r < 4; r++) {
-                const int gm = m0 + wm + 16 * i + g + ((r >> 1) << 3);
-                const int gn = n0 + wn + 8 * j + 2 * t + (r & 1);
-                if (gm < M && gn < N) C[(size_t)gm * ldc + gn] = acc[i][j][r];
-            }
-}
+// The training GEMMs (C = op(A) op(B), BF16 operands, FP32 accumulation,
+// split K) run on tcgen05: launch_gemm_tc (k_net_tc.cu).
 
 // out[i] = sum_z part[z*n + i] (split-K partials, in z order)
 __global__ void k_sum_splits(int64_t n, int splits, const float *__restrict__ part, float *__restrict__ out)
@@ -1054,8 +960,7 @@ constexpr int kSplitK = 4096;    // rows per split of the weight-gradient GEMMs
 static void gemm(ipfem_ctx *c, int M, int N, int K, const float *A, int lda, int tA, const float *B, int ldb, int tB,
                  float *C, int ldc)
 {
-    dim3 grid((N + GT - 1) / GT, (M + GT - 1) / GT, 1);
-    k_gemm_bf16<<<grid, 128, 0, c->stream>>>(M, N, K, A, lda, tA, B, ldb, tB, C, ldc, ((K + GK - 1) / GK) * GK);
+    launch_gemm_tc(c, M, N, K, A, lda, tA, B, ldb, tB, C, ldc, ((K + 31) / 32) * 32, 1);
 }
 
 // C[M][N] = A^T B over K = rows (both row-major with rows as the K index), split K
@@ -1064,8 +969,7 @@ static void gemm_tn_split(ipfem_ctx *c, int M, int N, int64_t rows, const float 
 {
     MlpBuffers &m = c->mlp;
     const int splits = (int)((rows + kSplitK - 1) / kSplitK);
-    dim3 grid((N + GT - 1) / GT, (M + GT - 1) / GT, splits);
-    k_gemm_bf16<<<grid, 128, 0, c->stream>>>(M, N, (int)rows, A, lda, 1, B, ldb, 0, m.part, N, kSplitK);
+    launch_gemm_tc(c, M, N, (int)rows, A, lda, 1, B, ldb, 0, m.part, N, kSplitK, splits);
     const int64_t n = (int64_t)M * N;
     k_sum_splits<<<(unsigned)((n + 255) / 256), 256, 0, c->stream>>>(n, splits, m.part, C);
 }

@@ -279,9 +279,128 @@ __global__ void __launch_bounds__(128) k_patch_net_tc(int64_t rows, const float 
                      : "memory");
 }
 
+// ------------------------------------------------ general GEMM on tcgen05
+// C[M][N] = op(A)[M][K] op(B)[K][N] for the training passes: A and B FP32 in
+// global memory, rounded to BF16 while they are staged into the canonical
+// K-major layouts, FP32 accumulators in tensor memory.
+//   transA = 0: A[m][k] = A[m*lda + k];   transA = 1: A[m][k] = A[k*lda + m]
+//   transB = 0: B[k][n] = B[k*ldb + n];   transB = 1: B[k][n] = B[n*ldb + k]
+// One CTA of 128 threads per 128 x 128 tile of C (thread t owns row m0 + t,
+// TMEM lane t); K in chunks of 32 (two MMAs of K = 16).  Split K: CTA z
+// covers k in [z*kchunk, (z+1)*kchunk) and writes C + z*M*ldc.  The dynamic
+// shared-memory request keeps at most 4 CTAs on an SM, so that their 128
+// TMEM columns each always fit and tcgen05.alloc never waits.
+namespace {
+constexpr uint32_t G_OFF_A = 0;                  // 128 x 32 BF16: 8 KB
+constexpr uint32_t G_OFF_B = 128 * 32 * 2;       // 128 x 32 BF16: 8 KB
+constexpr uint32_t G_OFF_BAR = G_OFF_B + 128 * 32 * 2;
+constexpr uint32_t G_OFF_TMEM = G_OFF_BAR + 8;
+constexpr uint32_t G_SMEM = 56 * 1024;           // residency cap, not the footprint
+constexpr uint32_t G_TMEM_COLS = 128;
+}  // namespace
+
+__global__ void __launch_bounds__(128) k_gemm_tc(int M, int N, int K, const float *__restrict__ A, int lda, int transA,
+                                                 const float *__restrict__ B, int ldb, int transB, float *__restrict__ C,
+                                                 int ldc, int kchunk, int *err)
+{
+    extern __shared__ __align__(1024) unsigned char smem[];
+    const uint32_t tid = threadIdx.x, warp = tid >> 5;
+    const uint32_t sbase = smem_u32(smem);
+    uint64_t *bar = reinterpret_cast<uint64_t *>(smem + G_OFF_BAR);
+    const int m0 = blockIdx.y * 128, n0 = blockIdx.x * 128;
+    const int kb = blockIdx.z * kchunk, ke = min(K, kb + kchunk);
+    C += (size_t)blockIdx.z * M * ldc;
+    if (tid == 0) mbar_init(bar, 1);
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(sbase + G_OFF_TMEM),
+                     "r"(G_TMEM_COLS)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    fence_async_smem();
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *reinterpret_cast<volatile uint32_t *>(smem + G_OFF_TMEM);
+    const uint32_t lane_t = tmem + ((warp * 32u) << 16);
+    constexpr uint32_t ID = idesc_bf16(128, 128);
+    uint32_t phase = 0;
+    bool ok = true, first = true;
+    for (int k0 = kb; k0 < ke && ok; k0 += 32) {
+        // A tile (128 x 32) and B tile (128 columns of C x 32), reads along the contiguous index
+        for (int e = tid; e < 128 * 32; e += 128) {
+            int mm, kk;
+            if (transA) { kk = e >> 7; mm = e & 127; } else { mm = e >> 5; kk = e & 31; }
+            const int gm = m0 + mm, gk = k0 + kk;
+            float v = 0.f;
+            if (gm < M && gk < ke) v = transA ? A[(size_t)gk * lda + gm] : A[(size_t)gm * lda + gk];
+            *reinterpret_cast<__nv_bfloat16 *>(smem + G_OFF_A + cano(mm, kk, 128)) = __float2bfloat16_rn(v);
+        }
+        for (int e = tid; e < 128 * 32; e += 128) {
+            int nn, kk;
+            if (transB) { nn = e >> 5; kk = e & 31; } else { kk = e >> 7; nn = e & 127; }
+            const int gn = n0 + nn, gk = k0 + kk;
+            float v = 0.f;
+            if (gn < N && gk < ke) v = transB ? B[(size_t)gn * ldb + gk] : B[(size_t)gk * ldb + gn];
+            *reinterpret_cast<__nv_bfloat16 *>(smem + G_OFF_B + cano(nn, kk, 128)) = __float2bfloat16_rn(v);
+        }
+        fence_async_smem();
+        tc_fence_before();
+        __syncthreads();
+        if (tid == 0) {
+            tc_fence_after();
+#pragma unroll
+            for (uint32_t kk = 0; kk < 2; kk++)
+                tc_mma(tmem, sdesc(sbase + G_OFF_A + kk * 2 * 2048, 2048, 128),
+                       sdesc(sbase + G_OFF_B + kk * 2 * 2048, 2048, 128), ID, (first && kk == 0) ? 0u : 1u);
+            tc_commit(sbase + G_OFF_BAR);
+        }
+        ok = wait_all(bar, phase);
+        phase ^= 1u;
+        first = false;
+        tc_fence_after();
+    }
+    if (ok) {
+        const int row = m0 + (int)tid;
+#pragma unroll 1
+        for (uint32_t c = 0; c < 4; c++) {
+            float v[32];
+            if (first) {
+#pragma unroll
+                for (int j = 0; j < 32; j++) v[j] = 0.f;          // empty K range
+            } else {
+                tc_ld32(lane_t + 32 * c, v);
+            }
+            if (row < M)
+#pragma unroll
+                for (int j = 0; j < 32; j++) {
+                    const int col = n0 + 32 * (int)c + j;
+                    if (col < N) C[(size_t)row * ldc + col] = v[j];
+                }
+        }
+    }
+    if (!ok && tid == 0) atomicExch(err, 3);
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(G_TMEM_COLS)
+                     : "memory");
+}
+
+void launch_gemm_tc(ipfem_ctx *c, int M, int N, int K, const float *A, int lda, int transA, const float *B, int ldb,
+                    int transB, float *C, int ldc, int kchunk, int splits)
+{
+    dim3 grid((N + 127) / 128, (M + 127) / 128, splits);
+    k_gemm_tc<<<grid, 128, G_SMEM, c->stream>>>(M, N, K, A, lda, transA, B, ldb, transB, C, ldc, kchunk, c->d_err);
+}
+
 cudaError_t net_tc_configure()
 {
-    return cudaFuncSetAttribute(k_patch_net_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TC_SMEM);
+    cudaError_t e = cudaFuncSetAttribute(k_patch_net_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TC_SMEM);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_gemm_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)G_SMEM);
+    return e;
 }
 
 void launch_patch_net_tc(ipfem_ctx *c, int64_t rows, const float *d_X, float *d_O)
