@@ -241,8 +241,11 @@ void launch_patch_net(ipfem_ctx *c, int64_t rows, const float *d_X, float *d_O);
 cudaError_t net_tc_configure();
 // C = op(A) op(B) on tcgen05 (BF16 operands, FP32 accumulation), split K over gridDim.z
 void launch_gemm_tc(ipfem_ctx *c, int M, int N, int K, const float *A, int lda, int transA, const float *B, int ldb,
-                    int transB, float *C, int ldc, int kchunk, int splits);
-void launch_patch_net_tc(ipfem_ctx *c, int64_t rows, const float *d_X, float *d_O);
+                    int transB, float *C, int ldc, int kchunk, int splits, float *colsum = nullptr);
+void launch_patch_net_tc(ipfem_ctx *c, int64_t rows, const float *d_X, float *d_O, float *d_H1 = nullptr,
+                         float *d_H2 = nullptr);
+void launch_patch_net_bwd_tc(ipfem_ctx *c, int64_t rows, const float *d_dO, const float *d_H1, const float *d_H2,
+                             float *d_dH2, float *d_dH1);
 void launch_patch_operator(ipfem_ctx *c);
 void launch_fcg_init(ipfem_ctx *c, const double *d_b, double scale, float rtol, int max_it);
 void launch_fcg_iteration(ipfem_ctx *c, int par);

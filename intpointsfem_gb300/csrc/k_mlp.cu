@@ -21,10 +21,10 @@
 // condition number of M K plus the residual of the plain solver's
 // (residual, increment) pairs.
 //
-// The inference network runs on the 5th-generation tensor cores (tcgen05.mma,
-// TMEM accumulators; k_net_tc.cu).  The training GEMMs below run on the tensor
-// cores in BF16 (operands rounded to BF16 in shared memory) with FP32
-// accumulation (mma.m16n8k16).
+// The network runs on the 5th-generation tensor cores (tcgen05.mma, TMEM
+// accumulators, BF16 operands, FP32 accumulation; k_net_tc.cu): inference and
+// the training forward in k_patch_net_tc, the backward of the hidden layers in
+// k_patch_net_bwd_tc, the split-K weight gradients in k_gemm_tc.
 #include <cuda_bf16.h>
 
 #include <algorithm>
@@ -43,54 +43,24 @@ __device__ __forceinline__ uint32_t pack_bf16(float lo, float hi)
     return *reinterpret_cast<uint32_t *>(&v);
 }
 
-// The training GEMMs (C = op(A) op(B), BF16 operands, FP32 accumulation,
-// split K) run on tcgen05: launch_gemm_tc (k_net_tc.cu).
-
-// out[i] = sum_z part[z*n + i] (split-K partials, in z order)
-__global__ void k_sum_splits(int64_t n, int splits, const float *__restrict__ part, float *__restrict__ out)
-{
-    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    float s = 0.f;
-    for (int z = 0; z < splits; z++) s += part[(size_t)z * n + i];
-    out[i] = s;
-}
-
-// ---------------------------------------------------- elementwise helpers
-// H = act(H + b) (b broadcast over rows of width n)
-__global__ void k_bias_act(int64_t rows, int n, float *__restrict__ H, const float *__restrict__ b, int relu)
-{
-    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (i >= rows * n) return;
-    const float v = H[i] + b[i % n];
-    H[i] = relu ? fmaxf(v, 0.f) : v;
-}
-
-// D = D * (H > 0)
-__global__ void k_relu_mask(int64_t count, float *__restrict__ D, const float *__restrict__ H)
-{
-    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (i < count && !(H[i] > 0.f)) D[i] = 0.f;
-}
-
-// column sums of D[rows][n], level 1: CTA (x, y) sums columns 32x..32x+31 over
-// rows y*chunk .. (y+1)*chunk-1 into part[y][n]
-constexpr int kColChunk = 4096;
-__global__ void __launch_bounds__(256) k_colsum_part(int64_t rows, int n, const float *__restrict__ D,
-                                                     float *__restrict__ part)
+// out[i] = sum_z part[z*n + i] (split-K partials): CTA x sums columns
+// 32x .. 32x+31, its 8 warps split z = w, w+8, ... and are added in warp order
+__global__ void __launch_bounds__(256) k_sum_splits(int64_t n, int splits, const float *__restrict__ part,
+                                                    float *__restrict__ out)
 {
     __shared__ float s[8][33];
-    const int c = blockIdx.x * 32 + (threadIdx.x & 31), w = threadIdx.x >> 5;
-    const int64_t r0 = (int64_t)blockIdx.y * kColChunk, r1 = min(rows, r0 + kColChunk);
+    const int64_t i = blockIdx.x * (int64_t)32 + (threadIdx.x & 31);
+    const int w = threadIdx.x >> 5;
     float a = 0.f;
-    if (c < n)
-        for (int64_t r = r0 + w; r < r1; r += 8) a += D[r * n + c];
+    if (i < n)
+        for (int z = w; z < splits; z += 8) a += part[(size_t)z * n + i];
     s[w][threadIdx.x & 31] = a;
     __syncthreads();
-    if (w == 0 && c < n) {
+    if (w == 0 && i < n) {
         float t = 0.f;
+#pragma unroll
         for (int k = 0; k < 8; k++) t += s[k][threadIdx.x];
-        part[(size_t)blockIdx.y * n + c] = t;
+        out[i] = t;
     }
 }
 
@@ -955,38 +925,36 @@ void launch_fcg_iteration(ipfem_ctx *c, int par)
 }
 
 // ------------------------------------------------------------ training pass
-constexpr int kSplitK = 4096;    // rows per split of the weight-gradient GEMMs
+// The weight-gradient GEMMs split their K (= rows) into at most kMaxSplits
+// ranges of a multiple of 32 rows: 4 CTAs on each of 152 SMs, one wave.
+constexpr int kMaxSplits = 608;
 
-static void gemm(ipfem_ctx *c, int M, int N, int K, const float *A, int lda, int tA, const float *B, int ldb, int tB,
-                 float *C, int ldc)
+static int split_rows(int64_t rows)
 {
-    launch_gemm_tc(c, M, N, K, A, lda, tA, B, ldb, tB, C, ldc, ((K + 31) / 32) * 32, 1);
+    const int64_t per = (rows + kMaxSplits - 1) / kMaxSplits;
+    return (int)std::max<int64_t>(32, (per + 31) / 32 * 32);
 }
 
-// C[M][N] = A^T B over K = rows (both row-major with rows as the K index), split K
+// C[M][N] = A^T B over K = rows (both row-major with rows as the K index),
+// split K; colsum[N] = the column sums of B (1^T B) from the same pass
 static void gemm_tn_split(ipfem_ctx *c, int M, int N, int64_t rows, const float *A, int lda, const float *B, int ldb,
-                          float *C)
+                          float *C, float *colsum)
 {
     MlpBuffers &m = c->mlp;
-    const int splits = (int)((rows + kSplitK - 1) / kSplitK);
-    launch_gemm_tc(c, M, N, (int)rows, A, lda, 1, B, ldb, 0, m.part, N, kSplitK, splits);
+    const int kchunk = split_rows(rows);
+    const int splits = (int)((rows + kchunk - 1) / kchunk);
+    float *cpart = m.part + (size_t)kMaxSplits * 128 * 128;
+    launch_gemm_tc(c, M, N, (int)rows, A, lda, 1, B, ldb, 0, m.part, N, kchunk, splits, cpart);
     const int64_t n = (int64_t)M * N;
-    k_sum_splits<<<(unsigned)((n + 255) / 256), 256, 0, c->stream>>>(n, splits, m.part, C);
+    k_sum_splits<<<(unsigned)((n + 31) / 32), 256, 0, c->stream>>>(n, splits, m.part, C);
+    k_sum_splits<<<(unsigned)((N + 31) / 32), 256, 0, c->stream>>>(N, splits, cpart, colsum);
 }
 
-static void colsum(ipfem_ctx *c, int64_t rows, int n, const float *D, float *out)
+// floats of mlp.part: the split-K partials of a 128 x 128 weight gradient and
+// of its column sums
+size_t patch_part_floats(int64_t)
 {
-    MlpBuffers &m = c->mlp;
-    const int chunks = (int)((rows + kColChunk - 1) / kColChunk);
-    k_colsum_part<<<dim3((n + 31) / 32, chunks), 256, 0, c->stream>>>(rows, n, D, m.part);
-    k_sum_splits<<<(n + 255) / 256, 256, 0, c->stream>>>(n, chunks, m.part, out);
-}
-
-size_t patch_part_floats(int64_t n_nodes)
-{
-    const int64_t splits = (n_nodes + kSplitK - 1) / kSplitK;
-    const int64_t chunks = (n_nodes + kColChunk - 1) / kColChunk;
-    return (size_t)std::max<int64_t>(splits * 128 * 128, chunks * 128);
+    return (size_t)kMaxSplits * (128 * 128 + 128);
 }
 
 // Gradient of
@@ -1007,17 +975,11 @@ void patch_learn_grad(ipfem_ctx *c, const float *d_r, const float *d_e, int P, f
     GridInfo G{m.gr, m.gt};
     const unsigned gn = (unsigned)((n + 255) / 256);
     const unsigned ge = (unsigned)((neq + 255) / 256);
-    const unsigned eh = (unsigned)(((int64_t)n * 128 + 255) / 256);
     const float2 *d2 = reinterpret_cast<const float2 *>(x.dinv);
     float4 *Gm = reinterpret_cast<float4 *>(m.M);
-    // forward through the GEMM path (keeps the hidden layers for the backward)
+    // forward through the fused network kernel, which also writes the hidden layers for the backward
     launch_patch_features(c, m.X);
-    gemm(c, n, 128, 32, m.X, 32, 0, W + kOffW1, 128, 0, m.H1, 128);
-    k_bias_act<<<eh, 256, 0, st>>>(n, 128, m.H1, W + kOffB1, 1);
-    gemm(c, n, 128, 128, m.H1, 128, 0, W + kOffW2, 128, 0, m.H2, 128);
-    k_bias_act<<<eh, 256, 0, st>>>(n, 128, m.H2, W + kOffB2, 1);
-    gemm(c, n, NOUT, 128, m.H2, 128, 0, W + kOffW3, NOUT, 0, m.O, NOUT);
-    k_bias_act<<<(unsigned)(((int64_t)n * NOUT + 255) / 256), 256, 0, st>>>(n, NOUT, m.O, W + kOffB3, 0);
+    launch_patch_net_tc(c, n, m.X, m.O, m.H1, m.H2);
     k_tri_build<<<gn, 256, 0, st>>>(n, G, m.O, d2, Gm, nullptr);
     m.op_valid = false;
     cudaMemsetAsync(m.dN, 0, (size_t)n * NOUT * sizeof(float), st);
@@ -1057,17 +1019,11 @@ void patch_learn_grad(ipfem_ctx *c, const float *d_r, const float *d_e, int P, f
     cudaMemcpyAsync(m.dN, dO, (size_t)n * NOUT * sizeof(float), cudaMemcpyDeviceToDevice, st);
     // backward
     float *gr = m.grads;
-    gemm_tn_split(c, 128, NOUT, n, m.H2, 128, m.dN, NOUT, gr + kOffW3);              // dW3 = H2^T dO
-    colsum(c, n, NOUT, m.dN, gr + kOffB3);
-    gemm(c, n, 128, NOUT, m.dN, NOUT, 0, W + kOffW3, NOUT, 1, m.dH2, 128);           // dH2 = dO W3^T
-    k_relu_mask<<<eh, 256, 0, st>>>((int64_t)n * 128, m.dH2, m.H2);
-    gemm_tn_split(c, 128, 128, n, m.H1, 128, m.dH2, 128, gr + kOffW2);              // dW2 = H1^T dH2
-    colsum(c, n, 128, m.dH2, gr + kOffB2);
-    gemm(c, n, 128, 128, m.dH2, 128, 0, W + kOffW2, 128, 1, m.dH1, 128);             // dH1 = dH2 W2^T
-    k_relu_mask<<<eh, 256, 0, st>>>((int64_t)n * 128, m.dH1, m.H1);
-    gemm_tn_split(c, 32, 128, n, m.X, 32, m.dH1, 128, gr + kOffW1);                  // dW1 = X^T dH1
-    colsum(c, n, 128, m.dH1, gr + kOffB1);
-    c->launches += 10 + 9 * (uint64_t)(wp > 0.f ? P : 0) + 14;
+    gemm_tn_split(c, 128, NOUT, n, m.H2, 128, m.dN, NOUT, gr + kOffW3, gr + kOffB3);  // dW3 = H2^T dO
+    launch_patch_net_bwd_tc(c, n, m.dN, m.H1, m.H2, m.dH2, m.dH1);                    // dH2, dH1
+    gemm_tn_split(c, 128, 128, n, m.H1, 128, m.dH2, 128, gr + kOffW2, gr + kOffB2);  // dW2 = H1^T dH2
+    gemm_tn_split(c, 32, 128, n, m.X, 32, m.dH1, 128, gr + kOffW1, gr + kOffB1);      // dW1 = X^T dH1
+    c->launches += 3 + 9 * (uint64_t)(wp > 0.f ? P : 0) + 3 + 10;
 }
 
 // one Adam step on the parameters with the gradient in mlp.grads

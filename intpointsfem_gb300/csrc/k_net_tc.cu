@@ -125,16 +125,31 @@ __device__ __forceinline__ void store_hidden(unsigned char *smem, uint32_t r, ui
     }
 }
 
+// the same 32 hidden values in FP32 to row r of a [rows][128] array
+__device__ __forceinline__ void store_hidden_f32(float *__restrict__ Hrow, uint32_t c0, const float (&v)[32],
+                                                 const float *b)
+{
+#pragma unroll
+    for (int q = 0; q < 8; q++)
+        reinterpret_cast<float4 *>(Hrow + c0)[q] =
+            make_float4(fmaxf(v[4 * q + 0] + b[c0 + 4 * q + 0], 0.f), fmaxf(v[4 * q + 1] + b[c0 + 4 * q + 1], 0.f),
+                        fmaxf(v[4 * q + 2] + b[c0 + 4 * q + 2], 0.f), fmaxf(v[4 * q + 3] + b[c0 + 4 * q + 3], 0.f));
+}
+
 }  // namespace
 
 // O[rows][20] = network(X[rows][32]); persistent CTAs of 128 threads over
-// 128-row tiles.  A barrier wait that runs out sets *err = 3 and the CTA stops.
+// 128-row tiles.  With H1 and H2 given, the hidden layers relu(X W1 + b1) and
+// relu(H1 W2 + b2) are also written out in FP32 ([rows][128] each; the BF16
+// operand of the next layer is the same value rounded), for the training
+// backward.  A barrier wait that runs out sets *err = 3 and the CTA stops.
 __global__ void __launch_bounds__(128) k_patch_net_tc(int64_t rows, const float *__restrict__ X,
                                                       const __nv_bfloat16 *__restrict__ w1t,
                                                       const __nv_bfloat16 *__restrict__ w2t,
                                                       const __nv_bfloat16 *__restrict__ w3t,
                                                       const float *__restrict__ b1, const float *__restrict__ b2,
-                                                      const float *__restrict__ b3, float *__restrict__ O, int *err)
+                                                      const float *__restrict__ b3, float *__restrict__ O,
+                                                      float *__restrict__ H1, float *__restrict__ H2, int *err)
 {
     extern __shared__ __align__(1024) unsigned char smem[];
     const uint32_t tid = threadIdx.x, warp = tid >> 5;
@@ -217,6 +232,7 @@ __global__ void __launch_bounds__(128) k_patch_net_tc(int64_t rows, const float 
             float v[32];
             tc_ld32(lane_t + 32 * c, v);
             store_hidden(smem, tid, 32 * c, v, sb1);
+            if (H1 && row < rows) store_hidden_f32(H1 + row * 128, 32 * c, v, sb1);
         }
         fence_async_smem();
         tc_fence_before();
@@ -239,6 +255,7 @@ __global__ void __launch_bounds__(128) k_patch_net_tc(int64_t rows, const float 
             float v[32];
             tc_ld32(lane_t + 128 + 32 * c, v);
             store_hidden(smem, tid, 32 * c, v, sb2);
+            if (H2 && row < rows) store_hidden_f32(H2 + row * 128, 32 * c, v, sb2);
         }
         fence_async_smem();
         tc_fence_before();
@@ -279,17 +296,180 @@ __global__ void __launch_bounds__(128) k_patch_net_tc(int64_t rows, const float 
                      : "memory");
 }
 
+// Backward of the two hidden layers for the training pass, per 128-row tile:
+//   dH2 = (dO W3^T) * (H2 > 0)     (K = 20, padded to 32)
+//   dH1 = (dH2 W2^T) * (H1 > 0)    (K = 128)
+// dO [rows][20], H1, H2, dH1, dH2 [rows][128], all FP32; W = the FP32
+// parameter vector (W2 [128][128] at kOffW2, W3 [128][20] at kOffW3,
+// row-major), rounded to BF16 once per CTA into the B operands.  dH2 is kept
+// on chip as the BF16 A operand of the second product.  Persistent CTAs of
+// 128 threads (thread t = row t = TMEM lane t), one 128-column accumulator
+// used by both products; the mask rows of H2 and H1 are loaded while the MMAs
+// run.  Shared-memory regions: OFF_X = dO tile (128 x 32), OFF_W1 = W3 as
+// N = 128 x K = 32, OFF_H = dH2 tile, OFF_W2 = W2 as N = 128 x K = 128.
+__global__ void __launch_bounds__(128) k_patch_net_bwd_tc(int64_t rows, const float *__restrict__ dO,
+                                                          const float *__restrict__ H1,
+                                                          const float *__restrict__ H2,
+                                                          const float *__restrict__ W, float *__restrict__ dH2,
+                                                          float *__restrict__ dH1, int *err)
+{
+    extern __shared__ __align__(1024) unsigned char smem[];
+    const uint32_t tid = threadIdx.x, warp = tid >> 5;
+    const uint32_t sbase = smem_u32(smem);
+    uint64_t *bar = reinterpret_cast<uint64_t *>(smem + OFF_BAR);
+    // B(n = j, k = o) = W3[j][o] (o < 20), 8 K values per 16-byte store
+    for (uint32_t e = tid; e < 128 * 4; e += blockDim.x) {
+        const uint32_t n = e >> 2, q = e & 3;
+        float f[8];
+#pragma unroll
+        for (int j = 0; j < 8; j++) f[j] = (8 * q + j < 20) ? W[kOffW3 + n * 20 + 8 * q + j] : 0.f;
+        *reinterpret_cast<uint4 *>(smem + OFF_W1 + cano(n, 8 * q, 128)) =
+            make_uint4(pk_bf16(f[0], f[1]), pk_bf16(f[2], f[3]), pk_bf16(f[4], f[5]), pk_bf16(f[6], f[7]));
+    }
+    // B(n = i, k = j) = W2[i][j]
+    for (uint32_t e = tid; e < 128 * 16; e += blockDim.x) {
+        const uint32_t n = e >> 4, q = e & 15;
+        const float4 f0 = *reinterpret_cast<const float4 *>(W + kOffW2 + n * 128 + 8 * q);
+        const float4 f1 = *reinterpret_cast<const float4 *>(W + kOffW2 + n * 128 + 8 * q + 4);
+        *reinterpret_cast<uint4 *>(smem + OFF_W2 + cano(n, 8 * q, 128)) =
+            make_uint4(pk_bf16(f0.x, f0.y), pk_bf16(f0.z, f0.w), pk_bf16(f1.x, f1.y), pk_bf16(f1.z, f1.w));
+    }
+    if (tid == 0) mbar_init(bar, 1);
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(sbase + OFF_TMEM),
+                     "r"(128u)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    fence_async_smem();
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *reinterpret_cast<volatile uint32_t *>(smem + OFF_TMEM);
+    const uint32_t lane_t = tmem + ((warp * 32u) << 16);
+    constexpr uint32_t ID128 = idesc_bf16(128, 128);
+    uint32_t phase = 0;
+    bool ok = true;
+    const int64_t n_tiles = (rows + TC_ROWS - 1) / TC_ROWS;
+    for (int64_t tile = blockIdx.x; tile < n_tiles && ok; tile += gridDim.x) {
+        const int64_t row = tile * TC_ROWS + tid;
+        const bool live = row < rows;
+        {
+            float f[32];
+#pragma unroll
+            for (int j = 0; j < 5; j++) {
+                const float4 t = live ? reinterpret_cast<const float4 *>(dO + row * 20)[j] : make_float4(0.f, 0.f, 0.f, 0.f);
+                f[4 * j] = t.x; f[4 * j + 1] = t.y; f[4 * j + 2] = t.z; f[4 * j + 3] = t.w;
+            }
+#pragma unroll
+            for (int j = 20; j < 32; j++) f[j] = 0.f;
+#pragma unroll
+            for (int q = 0; q < 4; q++)
+                *reinterpret_cast<uint4 *>(smem + OFF_X + cano(tid, 8 * q, 128)) =
+                    make_uint4(pk_bf16(f[8 * q], f[8 * q + 1]), pk_bf16(f[8 * q + 2], f[8 * q + 3]),
+                               pk_bf16(f[8 * q + 4], f[8 * q + 5]), pk_bf16(f[8 * q + 6], f[8 * q + 7]));
+        }
+        fence_async_smem();
+        tc_fence_before();
+        __syncthreads();
+        if (tid == 0) {
+            tc_fence_after();
+#pragma unroll
+            for (uint32_t kk = 0; kk < 2; kk++)
+                tc_mma(tmem, sdesc(sbase + OFF_X + kk * 2 * 2048, 2048, 128),
+                       sdesc(sbase + OFF_W1 + kk * 2 * 2048, 2048, 128), ID128, kk);
+            tc_commit(sbase + OFF_BAR);
+        }
+        float4 hm[32];                               // mask row, loaded while the MMAs run
+#pragma unroll
+        for (int j = 0; j < 32; j++)
+            hm[j] = live ? reinterpret_cast<const float4 *>(H2 + row * 128)[j] : make_float4(0.f, 0.f, 0.f, 0.f);
+        ok = wait_all(bar, phase);
+        phase ^= 1u;
+        if (!ok) break;
+        tc_fence_after();
+#pragma unroll
+        for (uint32_t c = 0; c < 4; c++) {
+            float v[32];
+            tc_ld32(lane_t + 32 * c, v);
+#pragma unroll
+            for (int q = 0; q < 8; q++) {
+                const float4 m = hm[8 * c + q];
+                if (!(m.x > 0.f)) v[4 * q] = 0.f;
+                if (!(m.y > 0.f)) v[4 * q + 1] = 0.f;
+                if (!(m.z > 0.f)) v[4 * q + 2] = 0.f;
+                if (!(m.w > 0.f)) v[4 * q + 3] = 0.f;
+                if (live)
+                    reinterpret_cast<float4 *>(dH2 + row * 128 + 32 * c)[q] =
+                        make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
+            }
+#pragma unroll
+            for (int q = 0; q < 4; q++)
+                *reinterpret_cast<uint4 *>(smem + OFF_H + cano(tid, 32 * c + 8 * q, 128)) =
+                    make_uint4(pk_bf16(v[8 * q], v[8 * q + 1]), pk_bf16(v[8 * q + 2], v[8 * q + 3]),
+                               pk_bf16(v[8 * q + 4], v[8 * q + 5]), pk_bf16(v[8 * q + 6], v[8 * q + 7]));
+        }
+        fence_async_smem();
+        tc_fence_before();
+        __syncthreads();
+        if (tid == 0) {
+            tc_fence_after();
+#pragma unroll
+            for (uint32_t kk = 0; kk < 8; kk++)
+                tc_mma(tmem, sdesc(sbase + OFF_H + kk * 2 * 2048, 2048, 128),
+                       sdesc(sbase + OFF_W2 + kk * 2 * 2048, 2048, 128), ID128, kk);
+            tc_commit(sbase + OFF_BAR);
+        }
+#pragma unroll
+        for (int j = 0; j < 32; j++)
+            hm[j] = live ? reinterpret_cast<const float4 *>(H1 + row * 128)[j] : make_float4(0.f, 0.f, 0.f, 0.f);
+        ok = wait_all(bar, phase);
+        phase ^= 1u;
+        if (!ok) break;
+        tc_fence_after();
+#pragma unroll
+        for (uint32_t c = 0; c < 4; c++) {
+            float v[32];
+            tc_ld32(lane_t + 32 * c, v);
+#pragma unroll
+            for (int q = 0; q < 8; q++) {
+                const float4 m = hm[8 * c + q];
+                if (live)
+                    reinterpret_cast<float4 *>(dH1 + row * 128 + 32 * c)[q] =
+                        make_float4(m.x > 0.f ? v[4 * q] : 0.f, m.y > 0.f ? v[4 * q + 1] : 0.f,
+                                    m.z > 0.f ? v[4 * q + 2] : 0.f, m.w > 0.f ? v[4 * q + 3] : 0.f);
+            }
+        }
+        tc_fence_before();
+        __syncthreads();
+    }
+    if (!ok && tid == 0) atomicExch(err, 3);
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(128u) : "memory");
+}
+
 // ------------------------------------------------ general GEMM on tcgen05
-// C[M][N] = op(A)[M][K] op(B)[K][N] for the training passes: A and B FP32 in
-// global memory, rounded to BF16 while they are staged into the canonical
-// K-major layouts, FP32 accumulators in tensor memory.
+// C[M][N] = op(A)[M][K] op(B)[K][N] for the weight gradients of the training
+// pass: A and B FP32 in global memory, rounded to BF16 while they are staged
+// into the canonical K-major layouts, FP32 accumulators in tensor memory.
 //   transA = 0: A[m][k] = A[m*lda + k];   transA = 1: A[m][k] = A[k*lda + m]
 //   transB = 0: B[k][n] = B[k*ldb + n];   transB = 1: B[k][n] = B[n*ldb + k]
-// One CTA of 128 threads per 128 x 128 tile of C (thread t owns row m0 + t,
-// TMEM lane t); K in chunks of 32 (two MMAs of K = 16).  Split K: CTA z
-// covers k in [z*kchunk, (z+1)*kchunk) and writes C + z*M*ldc.  The dynamic
-// shared-memory request keeps at most 4 CTAs on an SM, so that their 128
-// TMEM columns each always fit and tcgen05.alloc never waits.
+// With colsum given (B read with transB = 0, N <= 128), the CTAs of the first
+// M tile also write the FP32 column sums of B over their K range to
+// colsum[z*N + n] (the bias gradient of a weight-gradient GEMM).
+// One CTA of 128 threads per 128 x 128 tile of C (TMEM lane t = row m0 + t);
+// K in chunks of 32 (two MMAs of K = 16).  Thread t stages row t of both
+// operand tiles: 32 FP32 loads into registers (float4 along a contiguous K,
+// else one coalesced load per K across the warp), then four 16-byte stores
+// of 8 BF16 each, which fall on consecutive 16-byte slots across the warp.
+// The loads of chunk i+1 are issued while the MMAs of chunk i run.  Split K:
+// CTA z covers k in [z*kchunk, (z+1)*kchunk) (kchunk a multiple of 32) and
+// writes C + z*M*ldc.  The dynamic shared-memory request keeps at most 4 CTAs
+// on an SM, so that their 128 TMEM columns each always fit and tcgen05.alloc
+// never waits.
 namespace {
 constexpr uint32_t G_OFF_A = 0;                  // 128 x 32 BF16: 8 KB
 constexpr uint32_t G_OFF_B = 128 * 32 * 2;       // 128 x 32 BF16: 8 KB
@@ -297,11 +477,54 @@ constexpr uint32_t G_OFF_BAR = G_OFF_B + 128 * 32 * 2;
 constexpr uint32_t G_OFF_TMEM = G_OFF_BAR + 8;
 constexpr uint32_t G_SMEM = 56 * 1024;           // residency cap, not the footprint
 constexpr uint32_t G_TMEM_COLS = 128;
+
+// row r (of R) of an operand tile, K values k0 .. k0+31 (those >= ke read as 0):
+// element (r, k) at P[r*ld + k] when kcontig, else at P[k*ld + r]; vec: P and
+// ld allow 16-byte loads along K (k0 is a multiple of 32)
+__device__ __forceinline__ void g_load(float (&v)[32], const float *__restrict__ P, int ld, bool kcontig, bool vec,
+                                       int r, int R, int k0, int ke)
+{
+    if (r >= R) {
+#pragma unroll
+        for (int j = 0; j < 32; j++) v[j] = 0.f;
+        return;
+    }
+    if (kcontig) {
+        const float *row = P + (size_t)r * ld + k0;
+#pragma unroll
+        for (int q = 0; q < 8; q++) {
+            if (vec && k0 + 4 * q + 4 <= ke) {
+                const float4 t = __ldg(reinterpret_cast<const float4 *>(row + 4 * q));
+                v[4 * q] = t.x; v[4 * q + 1] = t.y; v[4 * q + 2] = t.z; v[4 * q + 3] = t.w;
+            } else {
+#pragma unroll
+                for (int j = 0; j < 4; j++) v[4 * q + j] = (k0 + 4 * q + j < ke) ? __ldg(row + 4 * q + j) : 0.f;
+            }
+        }
+    } else {
+#pragma unroll
+        for (int j = 0; j < 32; j++) v[j] = (k0 + j < ke) ? __ldg(P + (size_t)(k0 + j) * ld + r) : 0.f;
+    }
+}
+
+// row r of a 128 x 32 BF16 tile in the canonical layout: cano(r, 8o, 128) = o*2048 + r*16
+__device__ __forceinline__ void g_store(unsigned char *tile, const float (&v)[32], uint32_t r)
+{
+#pragma unroll
+    for (int o = 0; o < 4; o++) {
+        uint4 w;
+        w.x = pk_bf16(v[8 * o + 0], v[8 * o + 1]);
+        w.y = pk_bf16(v[8 * o + 2], v[8 * o + 3]);
+        w.z = pk_bf16(v[8 * o + 4], v[8 * o + 5]);
+        w.w = pk_bf16(v[8 * o + 6], v[8 * o + 7]);
+        *reinterpret_cast<uint4 *>(tile + cano(r, 8 * o, 128)) = w;
+    }
+}
 }  // namespace
 
 __global__ void __launch_bounds__(128) k_gemm_tc(int M, int N, int K, const float *__restrict__ A, int lda, int transA,
                                                  const float *__restrict__ B, int ldb, int transB, float *__restrict__ C,
-                                                 int ldc, int kchunk, int *err)
+                                                 int ldc, int kchunk, float *__restrict__ colsum, int *err)
 {
     extern __shared__ __align__(1024) unsigned char smem[];
     const uint32_t tid = threadIdx.x, warp = tid >> 5;
@@ -324,25 +547,28 @@ __global__ void __launch_bounds__(128) k_gemm_tc(int M, int N, int K, const floa
     const uint32_t tmem = *reinterpret_cast<volatile uint32_t *>(smem + G_OFF_TMEM);
     const uint32_t lane_t = tmem + ((warp * 32u) << 16);
     constexpr uint32_t ID = idesc_bf16(128, 128);
+    const bool kcA = !transA, kcB = transB != 0;
+    const bool vecA = kcA && (lda & 3) == 0 && (reinterpret_cast<uintptr_t>(A) & 15) == 0;
+    const bool vecB = kcB && (ldb & 3) == 0 && (reinterpret_cast<uintptr_t>(B) & 15) == 0;
     uint32_t phase = 0;
     bool ok = true, first = true;
-    for (int k0 = kb; k0 < ke && ok; k0 += 32) {
-        // A tile (128 x 32) and B tile (128 columns of C x 32), reads along the contiguous index
-        for (int e = tid; e < 128 * 32; e += 128) {
-            int mm, kk;
-            if (transA) { kk = e >> 7; mm = e & 127; } else { mm = e >> 5; kk = e & 31; }
-            const int gm = m0 + mm, gk = k0 + kk;
-            float v = 0.f;
-            if (gm < M && gk < ke) v = transA ? A[(size_t)gk * lda + gm] : A[(size_t)gm * lda + gk];
-            *reinterpret_cast<__nv_bfloat16 *>(smem + G_OFF_A + cano(mm, kk, 128)) = __float2bfloat16_rn(v);
+    float a[32], b[32], bsum = 0.f;
+    if (kb < ke) {
+        g_load(a, A, lda, kcA, vecA, m0 + (int)tid, M, kb, ke);
+        g_load(b, B, ldb, kcB, vecB, n0 + (int)tid, N, kb, ke);
+    }
+    for (int k0 = kb; k0 < ke; k0 += 32) {
+        if (!first) {                          // the MMAs of the previous chunk have read the tiles
+            ok = wait_all(bar, phase);
+            phase ^= 1u;
+            tc_fence_after();
+            if (!ok) break;
         }
-        for (int e = tid; e < 128 * 32; e += 128) {
-            int nn, kk;
-            if (transB) { nn = e >> 5; kk = e & 31; } else { kk = e >> 7; nn = e & 127; }
-            const int gn = n0 + nn, gk = k0 + kk;
-            float v = 0.f;
-            if (gn < N && gk < ke) v = transB ? B[(size_t)gn * ldb + gk] : B[(size_t)gk * ldb + gn];
-            *reinterpret_cast<__nv_bfloat16 *>(smem + G_OFF_B + cano(nn, kk, 128)) = __float2bfloat16_rn(v);
+        g_store(smem + G_OFF_A, a, tid);
+        g_store(smem + G_OFF_B, b, tid);
+        if (colsum) {
+#pragma unroll
+            for (int j = 0; j < 32; j++) bsum += b[j];
         }
         fence_async_smem();
         tc_fence_before();
@@ -355,15 +581,21 @@ __global__ void __launch_bounds__(128) k_gemm_tc(int M, int N, int K, const floa
                        sdesc(sbase + G_OFF_B + kk * 2 * 2048, 2048, 128), ID, (first && kk == 0) ? 0u : 1u);
             tc_commit(sbase + G_OFF_BAR);
         }
-        ok = wait_all(bar, phase);
-        phase ^= 1u;
         first = false;
+        if (k0 + 32 < ke) {
+            g_load(a, A, lda, kcA, vecA, m0 + (int)tid, M, k0 + 32, ke);
+            g_load(b, B, ldb, kcB, vecB, n0 + (int)tid, N, k0 + 32, ke);
+        }
+    }
+    if (ok && !first) {
+        ok = wait_all(bar, phase);
         tc_fence_after();
     }
     if (ok) {
         const int row = m0 + (int)tid;
+        const bool vecC = (ldc & 3) == 0 && (reinterpret_cast<uintptr_t>(C) & 15) == 0;
 #pragma unroll 1
-        for (uint32_t c = 0; c < 4; c++) {
+        for (uint32_t c = 0; c < 4 && n0 + 32 * (int)c < N; c++) {
             float v[32];
             if (first) {
 #pragma unroll
@@ -371,14 +603,23 @@ __global__ void __launch_bounds__(128) k_gemm_tc(int M, int N, int K, const floa
             } else {
                 tc_ld32(lane_t + 32 * c, v);
             }
-            if (row < M)
+            if (row >= M) continue;
+            float *crow = C + (size_t)row * ldc;
 #pragma unroll
-                for (int j = 0; j < 32; j++) {
-                    const int col = n0 + 32 * (int)c + j;
-                    if (col < N) C[(size_t)row * ldc + col] = v[j];
+            for (int q = 0; q < 8; q++) {
+                const int col = n0 + 32 * (int)c + 4 * q;
+                if (vecC && col + 4 <= N) {
+                    *reinterpret_cast<float4 *>(crow + col) =
+                        make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
+                } else {
+#pragma unroll
+                    for (int j = 0; j < 4; j++)
+                        if (col + j < N) crow[col + j] = v[4 * q + j];
                 }
+            }
         }
     }
+    if (ok && colsum && blockIdx.y == 0 && n0 + (int)tid < N) colsum[(size_t)blockIdx.z * N + n0 + tid] = bsum;
     if (!ok && tid == 0) atomicExch(err, 3);
     tc_fence_before();
     __syncthreads();
@@ -389,21 +630,24 @@ __global__ void __launch_bounds__(128) k_gemm_tc(int M, int N, int K, const floa
 }
 
 void launch_gemm_tc(ipfem_ctx *c, int M, int N, int K, const float *A, int lda, int transA, const float *B, int ldb,
-                    int transB, float *C, int ldc, int kchunk, int splits)
+                    int transB, float *C, int ldc, int kchunk, int splits, float *colsum)
 {
     dim3 grid((N + 127) / 128, (M + 127) / 128, splits);
-    k_gemm_tc<<<grid, 128, G_SMEM, c->stream>>>(M, N, K, A, lda, transA, B, ldb, transB, C, ldc, kchunk, c->d_err);
+    k_gemm_tc<<<grid, 128, G_SMEM, c->stream>>>(M, N, K, A, lda, transA, B, ldb, transB, C, ldc, kchunk, colsum,
+                                                c->d_err);
 }
 
 cudaError_t net_tc_configure()
 {
     cudaError_t e = cudaFuncSetAttribute(k_patch_net_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TC_SMEM);
     if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_patch_net_bwd_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TC_SMEM);
+    if (e == cudaSuccess)
         e = cudaFuncSetAttribute(k_gemm_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)G_SMEM);
     return e;
 }
 
-void launch_patch_net_tc(ipfem_ctx *c, int64_t rows, const float *d_X, float *d_O)
+void launch_patch_net_tc(ipfem_ctx *c, int64_t rows, const float *d_X, float *d_O, float *d_H1, float *d_H2)
 {
     int sms = 152;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device);
@@ -413,7 +657,18 @@ void launch_patch_net_tc(ipfem_ctx *c, int64_t rows, const float *d_X, float *d_
     k_patch_net_tc<<<grid, 128, TC_SMEM, c->stream>>>(
         rows, d_X, static_cast<const __nv_bfloat16 *>(m.w1t), static_cast<const __nv_bfloat16 *>(m.w2t),
         static_cast<const __nv_bfloat16 *>(m.w3t), m.params + kOffB1, m.params + kOffB2, m.params + kOffB3, d_O,
-        c->d_err);
+        d_H1, d_H2, c->d_err);
+}
+
+void launch_patch_net_bwd_tc(ipfem_ctx *c, int64_t rows, const float *d_dO, const float *d_H1, const float *d_H2,
+                             float *d_dH2, float *d_dH1)
+{
+    int sms = 152;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device);
+    const int64_t tiles = (rows + TC_ROWS - 1) / TC_ROWS;
+    const unsigned grid = (unsigned)std::max<int64_t>(1, std::min<int64_t>(tiles, 2 * (int64_t)sms));
+    k_patch_net_bwd_tc<<<grid, 128, TC_SMEM, c->stream>>>(rows, d_dO, d_H1, d_H2, c->mlp.params, d_dH2, d_dH1,
+                                                          c->d_err);
 }
 
 }  // namespace ipfem

@@ -45,6 +45,38 @@ def evaluate(params, n, newton_iters, cases=((-12.0, 28.0), (-25.0, 33.0)), **kw
     return out
 
 
+def time_step(n, pairs, steps, warmup=2):
+    """ms per training step (gradient pass + Adam on the device gradient) on an
+    n x n problem, pairs of random FP32 vectors; CUDA events on the library's
+    stream after `warmup` untimed gradient passes"""
+    import torch
+    import intpointsfem_gb300 as ip
+    wb, sm = learned.make_solver(n, -10.0, 30.0, seed=3)
+    try:
+        u = torch.zeros(sm.neq, dtype=torch.float64, device="cuda")
+        sm.SetLoadFactor(0.5)
+        R = torch.zeros_like(u)
+        sm.assemble(u, R, ip.DEVICE)
+        g = torch.Generator(device="cuda").manual_seed(5)
+        r = torch.randn(pairs, sm.neq, device="cuda", dtype=torch.float32, generator=g)
+        e = torch.randn(pairs, sm.neq, device="cuda", dtype=torch.float32, generator=g)
+        for _ in range(warmup):
+            sm.learn_grad(r, e, pairs, 1.0, 1.0)
+        torch.cuda.synchronize()
+        st = torch.cuda.ExternalStream(sm.stream, device=u.device)
+        t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        t0.record(st)
+        for _ in range(steps):
+            sm.learn_grad(r, e, pairs, 1.0, 1.0)
+            sm.mlp_adam(None, 1e-5)
+        t1.record(st)
+        torch.cuda.synchronize()
+        return t0.elapsed_time(t1) / steps
+    finally:
+        sm.close()
+        wb.close()
+
+
 def main(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--n", type=int, default=400)
@@ -62,7 +94,14 @@ def main(argv=None):
     ap.add_argument("--n-steps", type=int, default=10)
     ap.add_argument("--learned-only", action="store_true",
                     help="with --eval-only: run only the learned arm of the first case (profiling)")
+    ap.add_argument("--time-step", type=int, default=0,
+                    help="time this many gradient + Adam steps on one --n problem with random pairs and exit")
     a = ap.parse_args(argv)
+    if a.time_step:
+        print("ms per Adam step (%dx%d, %d pairs): %.2f" % (a.n, a.n, a.pairs_per_step,
+                                                            time_step(a.n, a.pairs_per_step, a.time_step)),
+              flush=True)
+        return
     mat = {"material_mode": a.material_mode, "c_cv": a.c_cv} if a.material_mode else {}
     if a.eval_only and a.learned_only:
         res = learned.compare(load_weights(a.eval_only), n=a.eval_n or a.n, newton_iters=a.eval_newton,
