@@ -255,6 +255,10 @@ def run_gpu(args):
         A.set_preconditioner(ip.PREC_BLOCK_JACOBI)
         if B:
             B.set_preconditioner(ip.PREC_BLOCK_JACOBI)
+    if args.no_row_stencils:
+        A.set_row_stencils(0)
+        if B:
+            B.set_row_stencils(0)
     stream = torch.cuda.ExternalStream(A.stream, device=dev)
     fp64_tflops = A.measure_fp64_peak()
 
@@ -313,6 +317,8 @@ def run_gpu(args):
 
         def mixed_arm(learned_prec):
             C_ = ip.ElastoPlasticIntPointsStructMatrix(wb)
+            if args.no_row_stencils:
+                C_.set_row_stencils(0)
             C_.set_precision(ip.MIXED)
             if learned_prec:
                 C_.set_node_grid(2 * n + 1, 2 * n + 1)
@@ -353,7 +359,9 @@ def run_gpu(args):
     ms_spmv = A.profile_spmv(reps=20)
     nb, nn = A.n_blocks, A.n_nodes
     vb = 16 if mixed else 32                                   # bytes of one 2x2 block
-    spmv_bytes = nb * (vb + 4) + nn * (2 * vb // 2 + 4 + 2)    # blocks + col; p read, q write, rowlen, fixed
+    stencils = A.row_stencil_count()[1 if mixed else 0] > 0 and not args.no_row_stencils
+    idx_bytes = nn if stencils else 4 * nb                     # 8-bit stencil id per row, or a column per block
+    spmv_bytes = nb * vb + idx_bytes + nn * (vb + 4 + 2)       # blocks, indices; p read, q write, rowlen, fixed
     hbm_peak, peak_kind = measured_peaks()
     achieved = spmv_bytes / (ms_spmv * 1e-3) / 1e9
     spmv_fp64_tflops = 2.0 * (4 * nb + 2 * nn) / (ms_spmv * 1e-3) / 1e12
@@ -381,7 +389,7 @@ def run_gpu(args):
                                   args.warmup + args.steps, args.warmup, args.config),
                    "l2": "inputs larger than L2 (tangent %.0f MB, element blocks %.0f MB)"
                          % (nb * 32 / 1e6, A.n_el * 1296 / 1e6),
-                   "replicas": ws},
+                   "replicas": ws, "row_stencils": bool(stencils)},
         "ip_per_s": A.n_ip / (ms_res * 1e-3),
         "ms_residual": ms_res,
         "cg_iters_per_newton": cg_per_iter,
@@ -435,6 +443,8 @@ def main():
     ap.add_argument("--no-chosen", dest="chosen", action="store_false")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--jacobi", action="store_true", help="scalar Jacobi instead of block Jacobi in the CG")
+    ap.add_argument("--no-row-stencils", action="store_true",
+                    help="SpMVs read the stored column indices instead of the row stencils (same results)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -179,6 +179,19 @@ ipfem_status ipfem_set_newton_accel(ipfem_ctx *ctx, int mode);
  * later linear solve, and later assemblies compute the residual only. */
 ipfem_status ipfem_set_newton_tangent(ipfem_ctx *ctx, int mode);
 
+/* Row stencils of the SpMVs.  On a structured node grid every row of the
+ * block tangent has one of a few dozen column-offset patterns (interior
+ * vertex, edge and centre nodes and their boundary variants); the SpMVs then
+ * form each block's column as node + offset from an 8-bit pattern id instead
+ * of loading the column index stored with the block.  Same blocks in the
+ * same order: the results are equal bit for bit.  on = 1 (default) uses the
+ * stencils wherever the layout has them, 0 the stored indices.  No
+ * counterpart in the reference (its solve is Pardiso). */
+ipfem_status ipfem_set_row_stencils(ipfem_ctx *ctx, int on);
+/* stencils of the FP64 and FP32 (IPFEM_MIXED, else 0) layouts; 0 = explicit
+ * columns only (rows longer than 32 blocks or more than 255 patterns) */
+ipfem_status ipfem_row_stencil_count(ipfem_ctx *ctx, int32_t *n_fp64, int32_t *n_fp32);
+
 /* Resumable form of the same loop: begin sets the options and the step range;
  * each advance performs n_iters Newton iterations (0 = until the last step is
  * accepted).  An iteration is: CG on the current tangent, u += du,

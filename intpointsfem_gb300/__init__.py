@@ -143,6 +143,8 @@ def lib():
             "ipfem_wellbore_build": (S, [C.POINTER(WellboreParams), C.POINTER(C.POINTER(Wellbore))]),
             "ipfem_wellbore_free": (None, [C.POINTER(Wellbore)]),
             "ipfem_set_newton_tangent": (S, [P, S]),
+            "ipfem_set_row_stencils": (S, [P, S]),
+            "ipfem_row_stencil_count": (S, [P, _ip, _ip]),
             "ipfem_gmsh_read": (S, [C.c_char_p, C.POINTER(C.POINTER(GmshData))]),
             "ipfem_gmsh_free": (None, [C.POINTER(GmshData)]),
             "ipfem_gmsh_problem": (S, [C.POINTER(GmshData), C.c_int32, C.c_int32, C.POINTER(BC), C.c_int32,
@@ -394,6 +396,17 @@ class ElastoPlasticIntPointsStructMatrix:
         first assembly kept (the reference's logged runs: main.cpp:218-222 with
         AssembleResidual in place of the Assemble of main.cpp:229-233)"""
         self._check(lib().ipfem_set_newton_tangent(self._ctx, int(mode)))
+
+    def set_row_stencils(self, on):
+        """1 (default): SpMVs form block columns from row stencils where the
+        layout has them; 0: from the stored column indices (same result)"""
+        self._check(lib().ipfem_set_row_stencils(self._ctx, int(bool(on))))
+
+    def row_stencil_count(self):
+        """(stencils of the FP64 layout, of the FP32 layout); 0 = explicit columns"""
+        a, b = C.c_int32(0), C.c_int32(0)
+        self._check(lib().ipfem_row_stencil_count(self._ctx, C.byref(a), C.byref(b)))
+        return a.value, b.value
 
     def set_precision(self, mode):
         self._check(lib().ipfem_set_precision(self._ctx, int(mode)))

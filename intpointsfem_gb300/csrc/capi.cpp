@@ -55,6 +55,11 @@ cudaError_t upload_sell(const SellLayout &L, bool sorted, SellDev &D, cudaStream
     ck(upload(&D.rowlen, L.rowlen, t));
     ck(upload(&D.sell_node, L.sell_node, t));
     ck(upload(&D.el_blk, L.el_blk, t));
+    if (L.n_pat > 0) {
+        ck(upload(&D.pat_id, L.pat_id, t));
+        ck(upload(&D.pat_off, L.pat_off, t));
+        D.n_pat = L.n_pat;
+    }
     D.n_sell = L.n_sell;
     D.sorted = sorted;
     return e;
@@ -62,7 +67,7 @@ cudaError_t upload_sell(const SellLayout &L, bool sorted, SellDev &D, cudaStream
 
 void free_sell(SellDev &D)
 {
-    void *ptrs[] = {D.slice_base, D.diag_blk, D.sell_col, D.rowlen, D.sell_node, D.el_blk};
+    void *ptrs[] = {D.slice_base, D.diag_blk, D.sell_col, D.rowlen, D.sell_node, D.el_blk, D.pat_id, D.pat_off};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     D = SellDev();
@@ -454,6 +459,7 @@ ipfem_status ipfem_set_precision(ipfem_ctx *c, int mode)
         ck(upload(&m.dphi, d32, c->stream));
         const std::string e = build_sell(s, false, m.sell);
         if (!e.empty()) return fail(c, IPFEM_INVALID, e);
+        build_row_stencils(m.sell);
         ck(upload_sell(m.sell, false, m.dsell, c->stream));
         ck(dalloc(&m.K, (size_t)m.sell.n_sell * 4));
         ck(dalloc(&m.dinv, (size_t)s.neq));
@@ -519,6 +525,30 @@ ipfem_status ipfem_set_newton_tangent(ipfem_ctx *c, int mode)
 {
     if (!c || (mode != 0 && mode != 1)) return fail(c, IPFEM_INVALID, "bad Newton tangent mode");
     c->newton_tangent = mode;
+    return IPFEM_OK;
+}
+
+ipfem_status ipfem_set_row_stencils(ipfem_ctx *c, int on)
+{
+    if (!c || (on != 0 && on != 1)) return fail(c, IPFEM_INVALID, "bad row-stencil mode");
+    if (on != c->row_stencils) {
+        // captured CG iterations launch the SpMV of the previous mode
+        cudaGraphExec_t *g[] = {&c->cg_exec, &c->fcg_exec, &c->mx.exec};
+        for (cudaGraphExec_t *e : g)
+            if (*e) {
+                cudaGraphExecDestroy(*e);
+                *e = nullptr;
+            }
+    }
+    c->row_stencils = on;
+    return IPFEM_OK;
+}
+
+ipfem_status ipfem_row_stencil_count(ipfem_ctx *c, int32_t *n_fp64, int32_t *n_fp32)
+{
+    if (!c) return IPFEM_INVALID;
+    if (n_fp64) *n_fp64 = c->dsell.n_pat;
+    if (n_fp32) *n_fp32 = c->mx.dsell.n_pat;
     return IPFEM_OK;
 }
 

@@ -11,6 +11,7 @@
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
+#include <map>
 #include <new>
 #include <thread>
 
@@ -143,6 +144,55 @@ std::string build_sell(const Setup &s, bool sorted, SellLayout &L)
     return "";
 }
 
+// Row stencils: the column offsets (column - node) of a row in slot order.
+// On a structured node grid a few dozen distinct stencils cover every row
+// (interior vertex, edge and centre nodes of the quadrilaterals plus their
+// boundary variants), so an SpMV can form a row's columns from its node and
+// an 8-bit stencil id instead of loading one index per block.  With a row
+// longer than kPatLen or more than kPatMax stencils (unstructured numbering)
+// the layout keeps only its explicit columns (n_pat = 0).
+void build_row_stencils(SellLayout &L)
+{
+    L.n_pat = 0;
+    L.pat_id.clear();
+    L.pat_off.clear();
+    const int32_t n = (int32_t)L.rowlen.size();
+    std::map<std::vector<int32_t>, int> index;
+    std::vector<uint8_t> id((size_t)n);
+    std::vector<int32_t> off, key;
+    for (int32_t t = 0; t < n; t++) {
+        const int32_t i = L.sell_node[t];
+        const int len = L.rowlen[t];
+        if (len > kPatLen) return;
+        key.resize((size_t)len);
+        const int64_t base = L.slice_base[t / 32] + (t % 32);
+        for (int k = 0; k < len; k++) key[k] = L.sell_col[(size_t)(base + (int64_t)k * 32)] - i;
+        // rows of a grid line repeat the stencils of the rows two and four before
+        int p = -1;
+        for (int back = 2; back <= 4 && p < 0; back += 2) {
+            if (t < back || L.rowlen[t - back] != len) continue;
+            const int q = id[(size_t)(t - back)];
+            if (std::equal(key.begin(), key.end(), off.begin() + (size_t)q * kPatLen)) p = q;
+        }
+        if (p < 0) {
+            auto it = index.find(key);
+            if (it != index.end()) {
+                p = it->second;
+            } else {
+                if ((int)index.size() == kPatMax) return;
+                p = (int)index.size();
+                index.emplace(key, p);
+                off.resize((size_t)(p + 1) * kPatLen, 0);
+                std::copy(key.begin(), key.end(), off.begin() + (size_t)p * kPatLen);
+            }
+        }
+        id[(size_t)t] = (uint8_t)p;
+    }
+    L.pat_id = std::move(id);
+    L.pat_off = std::move(off);
+    L.n_pat = (int)index.size();
+}
+
 std::string build_setup(const ipfem_mesh *m, const ipfem_material *mat, Setup &s)
 {
     if (!m || !mat) return "null mesh or material";
@@ -239,6 +289,7 @@ std::string build_setup(const ipfem_mesh *m, const ipfem_material *mat, Setup &s
     {
         const std::string e = build_sell(s, true, s.sell);
         if (!e.empty()) return e;
+        build_row_stencils(s.sell);
     }
     // boundary conditions and loads
     s.fixed.assign((size_t)s.neq, 0);

@@ -14,6 +14,8 @@ namespace ipfem {
 
 constexpr int kMaxColors = 16;
 constexpr int kRedBlock = 256;       // nodes per level-1 reduction block (= CTA size)
+constexpr int kPatLen = 32;          // offsets per row stencil (longest row that can use one)
+constexpr int kPatMax = 255;         // row stencils per layout (ids are 8-bit)
 
 struct ElasticConstH {               // mirrors ElasticConst of constitutive.cuh
     double lambda, mu, K, G, l2m, c1, c2, inv_mu;
@@ -42,6 +44,11 @@ struct SellLayout {
     std::vector<int64_t> bsr_to_sell;    // [n_blocks]
     std::vector<int32_t> el_blk;         // [n_el*nn*nn] slot of local node pair (m, n)
     std::vector<int64_t> diag_blk;       // [n_nodes] slot of the diagonal block
+    // row stencils (build_row_stencils): row position t has columns
+    // sell_node[t] + pat_off[pat_id[t] * kPatLen + k], k < rowlen[t]
+    std::vector<uint8_t> pat_id;         // [n_nodes], empty without stencils
+    std::vector<int32_t> pat_off;        // [n_pat * kPatLen]
+    int n_pat = 0;
 };
 
 // the same on the device
@@ -49,6 +56,9 @@ struct SellDev {
     int64_t n_sell = 0;
     int64_t *slice_base = nullptr, *diag_blk = nullptr;
     int32_t *sell_col = nullptr, *rowlen = nullptr, *sell_node = nullptr, *el_blk = nullptr;
+    uint8_t *pat_id = nullptr;           // row stencils, null without
+    int32_t *pat_off = nullptr;
+    int n_pat = 0;
     bool sorted = false;
 };
 
@@ -108,6 +118,7 @@ int32_t greedy_coloring_nn(int32_t n_el, int32_t n_nodes, int32_t nn, const int3
 // SELL-32 layout of s's block pattern; sorted: rows by length inside each
 // kRedBlock-node window (stable, longest first)
 std::string build_sell(const Setup &s, bool sorted, SellLayout &L);
+void build_row_stencils(SellLayout &L);
 int32_t greedy_coloring(int32_t n_el, int32_t n_nodes, const int32_t *connects, int32_t *el_color);
 void elastic_constants(double E, double nu, ElasticConstH &el);
 // message returned by ipfem_last_error(NULL) on the calling thread
@@ -197,6 +208,7 @@ struct ipfem_ctx {
     int precision = 0;                   // IPFEM_PLAIN_FP64 or IPFEM_MIXED
     ipfem::MixedBuffers mx;
     int preconditioner = 0;              // IPFEM_PREC_JACOBI, IPFEM_PREC_MLP or IPFEM_PREC_BLOCK_JACOBI
+    int row_stencils = 1;                // SpMVs read row stencils where the layout has them
     ipfem::MlpBuffers mlp;
     cudaGraphExec_t fcg_exec = nullptr;
     int64_t fcg_fallbacks = 0;
@@ -204,6 +216,12 @@ struct ipfem_ctx {
 
 // ---- kernel launchers (implemented in the .cu files) ----
 namespace ipfem {
+// whether the SpMVs over layout L read its row stencils
+inline bool use_row_stencils(const ipfem_ctx *c, const SellDev &L)
+{
+    return c->row_stencils != 0 && L.n_pat > 0 && L.pat_id != nullptr;
+}
+
 cudaError_t upload_constants(const ElasticConstH &el);
 void launch_gather_strain(ipfem_ctx *c, const double *d_u, double *d_strain);
 void launch_compute_sigma(ipfem_ctx *c, int update_mem, const double *d_strain, double *d_sigma_w, double *d_dep);

@@ -409,8 +409,11 @@ __global__ void __launch_bounds__(256) k_tri_precond(int32_t n, GridInfo G, cons
 // columns), q = K p_new, partials of p_new.q; last CTA: alpha = rz / pq.
 // Node-ordered SELL rows; the tangent and its column indices are streamed
 // (evict-first) so that z and p_old stay in L2.
+template <bool PAT>
 __global__ void __launch_bounds__(256) k_fcg_spmv(int32_t n, const int64_t *__restrict__ slice_base,
                                                   const int32_t *__restrict__ rowlen, const int32_t *__restrict__ scol,
+                                                  const uint8_t *__restrict__ pat_id,
+                                                  const int32_t *__restrict__ pat_off,
                                                   const float4 *__restrict__ K, const uint8_t *__restrict__ fixed,
                                                   const float2 *__restrict__ z, const float2 *__restrict__ p_old,
                                                   float2 *__restrict__ p_new, float2 *__restrict__ q, float *part,
@@ -421,9 +424,11 @@ __global__ void __launch_bounds__(256) k_fcg_spmv(int32_t n, const int64_t *__re
     // preconditioner pass) after it
     int64_t base = 0;
     int len = 0;
+    const int32_t *po = pat_off;
     if (i < n) {
         base = __ldg(&slice_base[i >> 5]) + (i & 31);
         len = __ldg(&rowlen[i]);
+        if (PAT) po = pat_off + (int)__ldg(&pat_id[i]) * kPatLen;
     }
     pdl_wait();
     pdl_launch_dependents();
@@ -435,7 +440,7 @@ __global__ void __launch_bounds__(256) k_fcg_spmv(int32_t n, const int64_t *__re
 #pragma unroll 4
         for (int k = 0; k < len; k++) {
             const int64_t s = base + (int64_t)k * 32;
-            const int32_t c = __ldcs(&scol[s]);
+            const int32_t c = PAT ? i + __ldg(&po[k]) : __ldcs(&scol[s]);
             const float4 a = __ldcs(&K[s]);
             const float2 zz = __ldg(&z[c]), pp = __ldg(&p_old[c]);
             const float px = fmaf(beta, pp.x, zz.x), py = fmaf(beta, pp.y, zz.y);
@@ -546,10 +551,12 @@ __global__ void __launch_bounds__(256, 8) k_fcg_update_first(int32_t n, GridInfo
 
 // ------------------------------------------------------------- training
 // y = K x on an FP32 SELL tangent (Dirichlet rows 0), no reductions
+template <bool PAT>
 __global__ void __launch_bounds__(256) k_spmv32(int32_t n, const int64_t *__restrict__ slice_base,
                                                 const int32_t *__restrict__ rowlen,
                                                 const int32_t *__restrict__ sell_node,
-                                                const int32_t *__restrict__ scol, const float4 *__restrict__ K,
+                                                const int32_t *__restrict__ scol, const uint8_t *__restrict__ pat_id,
+                                                const int32_t *__restrict__ pat_off, const float4 *__restrict__ K,
                                                 const uint8_t *__restrict__ fixed, const float2 *__restrict__ x,
                                                 float2 *__restrict__ y)
 {
@@ -558,11 +565,13 @@ __global__ void __launch_bounds__(256) k_spmv32(int32_t n, const int64_t *__rest
     const int32_t i = sell_node[t];
     const int64_t base = slice_base[t >> 5] + (t & 31);
     const int len = rowlen[t];
+    const int32_t *po = PAT ? pat_off + (int)__ldg(&pat_id[t]) * kPatLen : pat_off;
     float y0 = 0.f, y1 = 0.f;
+#pragma unroll 4
     for (int k = 0; k < len; k++) {
         const int64_t s = base + (int64_t)k * 32;
         const float4 a = __ldg(&K[s]);
-        const float2 v = __ldg(&x[scol[s]]);
+        const float2 v = __ldg(&x[PAT ? i + __ldg(&po[k]) : __ldg(&scol[s])]);
         y0 = fmaf(a.x, v.x, fmaf(a.y, v.y, y0));
         y1 = fmaf(a.z, v.x, fmaf(a.w, v.y, y1));
     }
@@ -910,8 +919,9 @@ void launch_fcg_iteration(ipfem_ctx *c, int par)
     float2 *R[2] = {reinterpret_cast<float2 *>(m.r), reinterpret_cast<float2 *>(l.r_old)};
     const float2 *d2 = reinterpret_cast<const float2 *>(m.dinv);
     float *part = m.part;
-    launch_pdl(k_fcg_spmv, fcg_grid(c), 256, c->stream, n, (const int64_t *)L.slice_base,
-               (const int32_t *)L.rowlen, (const int32_t *)L.sell_col, reinterpret_cast<const float4 *>(m.K),
+    launch_pdl(use_row_stencils(c, L) ? k_fcg_spmv<true> : k_fcg_spmv<false>, fcg_grid(c), 256, c->stream, n,
+               (const int64_t *)L.slice_base, (const int32_t *)L.rowlen, (const int32_t *)L.sell_col,
+               (const uint8_t *)L.pat_id, (const int32_t *)L.pat_off, reinterpret_cast<const float4 *>(m.K),
                (const uint8_t *)c->d_fixed, reinterpret_cast<const float2 *>(m.z), (const float2 *)P[par],
                P[1 - par], reinterpret_cast<float2 *>(m.q), part, (int64_t)fcg_grid(c), c->d_counters + 5, m.sc);
     launch_pdl(k_fcg_update_first, fcg_grid(c), 256, c->stream, n, G, reinterpret_cast<const uint2 *>(l.Gh), d2,
@@ -990,20 +1000,21 @@ void patch_learn_grad(ipfem_ctx *c, const float *d_r, const float *d_e, int P, f
     const SellDev &L = x.dsell;
     const float4 *K4 = reinterpret_cast<const float4 *>(x.K);
     const float w = P > 0 ? wp / (float)P : 0.f;
+    auto spmv32 = [&](const float2 *xin, float2 *yout) {
+        (use_row_stencils(c, L) ? k_spmv32<true> : k_spmv32<false>)<<<gn, 256, 0, st>>>(
+            n, L.slice_base, L.rowlen, L.sell_node, L.sell_col, L.pat_id, L.pat_off, K4, c->d_fixed, xin, yout);
+    };
     for (int p = 0; p < P && wp > 0.f; p++) {
         const float2 *r2 = reinterpret_cast<const float2 *>(d_r + (size_t)p * neq);
         const float2 *e2 = reinterpret_cast<const float2 *>(d_e + (size_t)p * neq);
         k_tri_first<<<gn, 256, 0, st>>>(n, G, Gm, d2, r2, reinterpret_cast<float2 *>(y), nullptr);
         k_tri_second<<<gn, 256, 0, st>>>(n, G, Gm, d2, reinterpret_cast<const float2 *>(y),
                                          reinterpret_cast<float2 *>(z));
-        k_spmv32<<<gn, 256, 0, st>>>(n, L.slice_base, L.rowlen, L.sell_node, L.sell_col, K4, c->d_fixed, e2,
-                                     reinterpret_cast<float2 *>(ae));
-        k_spmv32<<<gn, 256, 0, st>>>(n, L.slice_base, L.rowlen, L.sell_node, L.sell_col, K4, c->d_fixed,
-                                     reinterpret_cast<const float2 *>(z), reinterpret_cast<float2 *>(az));
+        spmv32(e2, reinterpret_cast<float2 *>(ae));
+        spmv32(reinterpret_cast<const float2 *>(z), reinterpret_cast<float2 *>(az));
         k_res_part<<<ge, 256, 0, st>>>(neq, ae, az, res, m.part);
         k_res_final<<<1, 256, 0, st>>>((int)ge, m.part, m.scal, m.loss, w);
-        k_spmv32<<<gn, 256, 0, st>>>(n, L.slice_base, L.rowlen, L.sell_node, L.sell_col, K4, c->d_fixed,
-                                     reinterpret_cast<const float2 *>(res), reinterpret_cast<float2 *>(g));
+        spmv32(reinterpret_cast<const float2 *>(res), reinterpret_cast<float2 *>(g));
         k_tri_first<<<gn, 256, 0, st>>>(n, G, Gm, d2, reinterpret_cast<const float2 *>(g),
                                         reinterpret_cast<float2 *>(v), nullptr);
         k_tri_grad_pairs<<<gn, 256, 0, st>>>(n, G, d2, r2, reinterpret_cast<const float2 *>(g),

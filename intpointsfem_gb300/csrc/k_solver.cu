@@ -251,11 +251,16 @@ __global__ void __launch_bounds__(kRedBlock) k_cg_init(int32_t n_nodes, const do
 // SORTED: thread t runs SELL row position t, i.e. node sell_node[t] of the
 // same kRedBlock window, and its p.q term goes through shared memory back to
 // the node's own slot, so the block tree adds in node order either way.
-template <class T, bool SORTED>
+// PAT: block k of the row has column i + pat_off[pat_id[t] * kPatLen + k]
+// (row stencils, L1-resident) instead of the column index stored with it;
+// same blocks in the same order, so the result is the same bit for bit.
+template <class T, bool SORTED, bool PAT>
 __global__ void __launch_bounds__(kRedBlock) k_cg_spmv(int32_t n_nodes, const int64_t *__restrict__ slice_base,
                                                        const int32_t *__restrict__ rowlen,
                                                        const int32_t *__restrict__ sell_node,
-                                                       const int32_t *__restrict__ scol, const T *__restrict__ K,
+                                                       const int32_t *__restrict__ scol,
+                                                       const uint8_t *__restrict__ pat_id,
+                                                       const int32_t *__restrict__ pat_off, const T *__restrict__ K,
                                                        const uint8_t *__restrict__ fixed, const T *__restrict__ p,
                                                        T *__restrict__ q, T *part, int64_t n_red, unsigned *ticket,
                                                        CGScalarsT<T> *sc)
@@ -266,10 +271,12 @@ __global__ void __launch_bounds__(kRedBlock) k_cg_spmv(int32_t n_nodes, const in
     // row metadata is loaded before the flag so that the two latencies overlap
     int32_t i = t, len = 0;
     int64_t base = 0;
+    const int32_t *po = pat_off;
     if (t < n_nodes) {
         if (SORTED) i = __ldg(&sell_node[t]);
         base = __ldg(&slice_base[t >> 5]) + (t & 31);
         len = __ldg(&rowlen[t]);
+        if (PAT) po = pat_off + (int)__ldg(&pat_id[t]) * kPatLen;
     }
     pdl_wait();
     pdl_launch_dependents();
@@ -281,7 +288,7 @@ __global__ void __launch_bounds__(kRedBlock) k_cg_spmv(int32_t n_nodes, const in
 #pragma unroll 4
         for (int k = 0; k < len; k++) {
             const int64_t s = base + (int64_t)k * 32;
-            const int32_t c = __ldg(&scol[s]);
+            const int32_t c = PAT ? i + __ldg(&po[k]) : __ldg(&scol[s]);
             T a00, a01, a10, a11;
             load_block(K, s, a00, a01, a10, a11);
             const V xx = __ldg(&pv[c]);
@@ -489,10 +496,13 @@ template <class T>
 void launch_spmv(ipfem_ctx *c, const SellDev &L, const T *K, const T *p, T *q, T *part, unsigned *ticket,
                  CGScalarsT<T> *sc)
 {
-    launch_pdl(L.sorted ? k_cg_spmv<T, true> : k_cg_spmv<T, false>, grid_nodes(c), kRedBlock, c->stream,
-               c->s.n_nodes, (const int64_t *)L.slice_base, (const int32_t *)L.rowlen, (const int32_t *)L.sell_node,
-               (const int32_t *)L.sell_col, (const T *)K, (const uint8_t *)c->d_fixed, (const T *)p, q, part,
-               c->n_red, ticket, sc);
+    const bool pat = use_row_stencils(c, L);
+    auto kern = L.sorted ? (pat ? k_cg_spmv<T, true, true> : k_cg_spmv<T, true, false>)
+                         : (pat ? k_cg_spmv<T, false, true> : k_cg_spmv<T, false, false>);
+    launch_pdl(kern, grid_nodes(c), kRedBlock, c->stream, c->s.n_nodes, (const int64_t *)L.slice_base,
+               (const int32_t *)L.rowlen, (const int32_t *)L.sell_node, (const int32_t *)L.sell_col,
+               (const uint8_t *)L.pat_id, (const int32_t *)L.pat_off, (const T *)K, (const uint8_t *)c->d_fixed,
+               (const T *)p, q, part, c->n_red, ticket, sc);
 }
 
 void launch_cg_iteration(ipfem_ctx *c)
