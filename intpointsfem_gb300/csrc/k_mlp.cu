@@ -31,6 +31,7 @@
 #include <cmath>
 
 #include "ipfem_internal.h"
+#include "ldhint.cuh"
 #include "pdl.cuh"
 
 namespace ipfem {
@@ -410,7 +411,7 @@ __global__ void __launch_bounds__(256) k_tri_precond(int32_t n, GridInfo G, cons
 // Node-ordered SELL rows; the tangent and its column indices are streamed
 // (evict-first) so that z and p_old stay in L2.
 template <bool PAT>
-__global__ void __launch_bounds__(256) k_fcg_spmv(int32_t n, const int64_t *__restrict__ slice_base,
+__global__ void __launch_bounds__(256, 8) k_fcg_spmv(int32_t n, const int64_t *__restrict__ slice_base,
                                                   const int32_t *__restrict__ rowlen, const int32_t *__restrict__ scol,
                                                   const uint8_t *__restrict__ pat_id,
                                                   const int32_t *__restrict__ pat_off,
@@ -423,12 +424,11 @@ __global__ void __launch_bounds__(256) k_fcg_spmv(int32_t n, const int64_t *__re
     // row metadata before the wait; z, beta and the flag (written by the
     // preconditioner pass) after it
     int64_t base = 0;
-    int len = 0;
-    const int32_t *po = pat_off;
+    int len = 0, pb = 0;
     if (i < n) {
         base = __ldg(&slice_base[i >> 5]) + (i & 31);
         len = __ldg(&rowlen[i]);
-        if (PAT) po = pat_off + (int)__ldg(&pat_id[i]) * kPatLen;
+        if (PAT) pb = (int)__ldg(&pat_id[i]) * kPatLen;
     }
     pdl_wait();
     pdl_launch_dependents();
@@ -436,13 +436,14 @@ __global__ void __launch_bounds__(256) k_fcg_spmv(int32_t n, const int64_t *__re
     const float beta = *reinterpret_cast<volatile float *>(&sc->beta);
     float v[1] = {0.f};
     if (i < n) {
+        const uint64_t keep = l2_policy_keep();
         float y0 = 0.f, y1 = 0.f;
 #pragma unroll 4
         for (int k = 0; k < len; k++) {
             const int64_t s = base + (int64_t)k * 32;
-            const int32_t c = PAT ? i + __ldg(&po[k]) : __ldcs(&scol[s]);
+            const int32_t c = PAT ? i + __ldg(&pat_off[pb + k]) : __ldcs(&scol[s]);
             const float4 a = __ldcs(&K[s]);
-            const float2 zz = __ldg(&z[c]), pp = __ldg(&p_old[c]);
+            const float2 zz = ld_keep(&z[c], keep), pp = ld_keep(&p_old[c], keep);
             const float px = fmaf(beta, pp.x, zz.x), py = fmaf(beta, pp.y, zz.y);
             y0 = fmaf(a.y, py, fmaf(a.x, px, y0));
             y1 = fmaf(a.w, py, fmaf(a.z, px, y1));
@@ -565,13 +566,14 @@ __global__ void __launch_bounds__(256) k_spmv32(int32_t n, const int64_t *__rest
     const int32_t i = sell_node[t];
     const int64_t base = slice_base[t >> 5] + (t & 31);
     const int len = rowlen[t];
-    const int32_t *po = PAT ? pat_off + (int)__ldg(&pat_id[t]) * kPatLen : pat_off;
+    const int pb = PAT ? (int)__ldg(&pat_id[t]) * kPatLen : 0;
+    const uint64_t keep = l2_policy_keep();
     float y0 = 0.f, y1 = 0.f;
 #pragma unroll 4
     for (int k = 0; k < len; k++) {
         const int64_t s = base + (int64_t)k * 32;
-        const float4 a = __ldg(&K[s]);
-        const float2 v = __ldg(&x[PAT ? i + __ldg(&po[k]) : __ldg(&scol[s])]);
+        const float4 a = __ldcs(&K[s]);
+        const float2 v = ld_keep(&x[PAT ? i + __ldg(&pat_off[pb + k]) : __ldg(&scol[s])], keep);
         y0 = fmaf(a.x, v.x, fmaf(a.y, v.y, y0));
         y1 = fmaf(a.z, v.x, fmaf(a.w, v.y, y1));
     }

@@ -19,6 +19,7 @@
 #include <mutex>
 
 #include "ipfem_internal.h"
+#include "ldhint.cuh"
 #include "pdl.cuh"
 
 namespace ipfem {
@@ -180,16 +181,17 @@ template <> struct Vec2<float> { typedef float2 type; };
 __device__ __forceinline__ double2 mk2(double a, double b) { return make_double2(a, b); }
 __device__ __forceinline__ float2 mk2(float a, float b) { return make_float2(a, b); }
 
-// 2x2 block s of a SELL matrix: FP64 as two 16-byte loads, FP32 as one
+// 2x2 block s of a SELL matrix: FP64 as two 16-byte loads, FP32 as one;
+// streamed (evict-first: each block is read once per SpMV)
 __device__ __forceinline__ void load_block(const double *K, int64_t s, double &a, double &b, double &c, double &d)
 {
     const double2 *Kv = reinterpret_cast<const double2 *>(K);
-    const double2 u = __ldg(&Kv[2 * s]), v = __ldg(&Kv[2 * s + 1]);
+    const double2 u = __ldcs(&Kv[2 * s]), v = __ldcs(&Kv[2 * s + 1]);
     a = u.x; b = u.y; c = v.x; d = v.y;
 }
 __device__ __forceinline__ void load_block(const float *K, int64_t s, float &a, float &b, float &c, float &d)
 {
-    const float4 u = __ldg(&reinterpret_cast<const float4 *>(K)[s]);
+    const float4 u = __ldcs(&reinterpret_cast<const float4 *>(K)[s]);
     a = u.x; b = u.y; c = u.z; d = u.w;
 }
 
@@ -269,14 +271,13 @@ __global__ void __launch_bounds__(kRedBlock) k_cg_spmv(int32_t n_nodes, const in
     __shared__ T s_pq[1][kRedStage];
     const int32_t t = blockIdx.x * kRedBlock + threadIdx.x;
     // row metadata is loaded before the flag so that the two latencies overlap
-    int32_t i = t, len = 0;
+    int32_t i = t, len = 0, pb = 0;
     int64_t base = 0;
-    const int32_t *po = pat_off;
     if (t < n_nodes) {
         if (SORTED) i = __ldg(&sell_node[t]);
         base = __ldg(&slice_base[t >> 5]) + (t & 31);
         len = __ldg(&rowlen[t]);
-        if (PAT) po = pat_off + (int)__ldg(&pat_id[t]) * kPatLen;
+        if (PAT) pb = (int)__ldg(&pat_id[t]) * kPatLen;
     }
     pdl_wait();
     pdl_launch_dependents();
@@ -284,14 +285,15 @@ __global__ void __launch_bounds__(kRedBlock) k_cg_spmv(int32_t n_nodes, const in
     T v = T(0);
     if (t < n_nodes) {
         const V *pv = reinterpret_cast<const V *>(p);
+        const uint64_t keep = l2_policy_keep();
         T y0 = T(0), y1 = T(0);
 #pragma unroll 4
         for (int k = 0; k < len; k++) {
             const int64_t s = base + (int64_t)k * 32;
-            const int32_t c = PAT ? i + __ldg(&po[k]) : __ldg(&scol[s]);
+            const int32_t c = PAT ? i + __ldg(&pat_off[pb + k]) : __ldg(&scol[s]);
             T a00, a01, a10, a11;
             load_block(K, s, a00, a01, a10, a11);
-            const V xx = __ldg(&pv[c]);
+            const V xx = ld_keep(&pv[c], keep);
             y0 = fma(a00, xx.x, y0);
             y0 = fma(a01, xx.y, y0);
             y1 = fma(a10, xx.x, y1);
