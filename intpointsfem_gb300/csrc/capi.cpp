@@ -62,6 +62,7 @@ cudaError_t upload_sell(const SellLayout &L, bool sorted, SellDev &D, cudaStream
     }
     D.n_sell = L.n_sell;
     D.sorted = sorted;
+    D.pair = L.pair;
     return e;
 }
 
@@ -457,7 +458,7 @@ ipfem_status ipfem_set_precision(ipfem_ctx *c, int mode)
         };
         std::vector<float> d32(s.dphi.begin(), s.dphi.end());
         ck(upload(&m.dphi, d32, c->stream));
-        const std::string e = build_sell(s, false, m.sell);
+        const std::string e = build_sell(s, false, true, m.sell);
         if (!e.empty()) return fail(c, IPFEM_INVALID, e);
         build_row_stencils(m.sell);
         ck(upload_sell(m.sell, false, m.dsell, c->stream));

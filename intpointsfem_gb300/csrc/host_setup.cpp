@@ -89,8 +89,9 @@ static void parallel_for(int64_t n, F f)
 // SELL-32 layout of the block pattern.  With sorted rows the warps of a
 // slice run rows of one length, while every row keeps its own block order
 // and stays inside the reduction block that owns it in node order.
-std::string build_sell(const Setup &s, bool sorted, SellLayout &L)
+std::string build_sell(const Setup &s, bool sorted, bool pair, SellLayout &L)
 {
+    L.pair = pair;
     const int64_t ns = (s.n_nodes + 31) / 32;
     std::vector<int32_t> deg(s.n_nodes);
     for (int32_t i = 0; i < s.n_nodes; i++) deg[i] = (int32_t)(s.row_ptr[i + 1] - s.row_ptr[i]);
@@ -108,6 +109,7 @@ std::string build_sell(const Setup &s, bool sorted, SellLayout &L)
     for (int64_t sl = 0; sl < ns; sl++) {
         int32_t w = 0;
         for (int64_t t = sl * 32; t < std::min<int64_t>(s.n_nodes, sl * 32 + 32); t++) w = std::max(w, L.rowlen[t]);
+        if (pair) w += w & 1;
         L.slice_base[sl + 1] = L.slice_base[sl] + 32 * (int64_t)w;
     }
     L.n_sell = L.slice_base[ns];
@@ -117,16 +119,15 @@ std::string build_sell(const Setup &s, bool sorted, SellLayout &L)
     L.diag_blk.resize(s.n_nodes);
     for (int32_t t = 0; t < s.n_nodes; t++) {
         const int32_t i = L.sell_node[t];
-        const int64_t base = L.slice_base[t / 32] + (t % 32);
         for (int64_t j = 0; j < L.rowlen[t]; j++) {
-            const int64_t slot = base + j * 32;
+            const int64_t slot = sell_slot(L, t, j);
             const int32_t c = s.col[s.row_ptr[i] + j];
             L.sell_col[slot] = c;
             L.bsr_to_sell[s.row_ptr[i] + j] = slot;
             if (c == i) L.diag_blk[i] = slot;
         }
         for (int64_t j = L.rowlen[t]; j < (int64_t)(L.slice_base[t / 32 + 1] - L.slice_base[t / 32]) / 32; j++)
-            L.sell_col[base + j * 32] = i;
+            L.sell_col[sell_slot(L, t, j)] = i;
     }
     const int nn = s.nn, nd = s.nd;
     L.el_blk.resize((size_t)s.n_el * nn * nn);
@@ -165,8 +166,7 @@ void build_row_stencils(SellLayout &L)
         const int len = L.rowlen[t];
         if (len > kPatLen) return;
         key.resize((size_t)len);
-        const int64_t base = L.slice_base[t / 32] + (t % 32);
-        for (int k = 0; k < len; k++) key[k] = L.sell_col[(size_t)(base + (int64_t)k * 32)] - i;
+        for (int k = 0; k < len; k++) key[k] = L.sell_col[(size_t)sell_slot(L, t, k)] - i;
         // rows of a grid line repeat the stencils of the rows two and four before
         int p = -1;
         for (int back = 2; back <= 4 && p < 0; back += 2) {
@@ -287,7 +287,7 @@ std::string build_setup(const ipfem_mesh *m, const ipfem_material *mat, Setup &s
             std::memcpy(s.col.data() + s.row_ptr[i], tmp.data() + cap[i], (size_t)deg[i] * sizeof(int32_t));
     }
     {
-        const std::string e = build_sell(s, true, s.sell);
+        const std::string e = build_sell(s, true, false, s.sell);
         if (!e.empty()) return e;
         build_row_stencils(s.sell);
     }

@@ -33,9 +33,14 @@ constexpr int kStatusFallback = 9;   // flexible CG stagnated: the caller falls 
 typedef CGScalarsT<double> CGScalars;
 
 // SELL-32 layout of the nodal 2x2 block pattern: row position t of slice
-// t/32 holds node sell_node[t] (identity when the rows keep node order), its
-// block k sits in slot slice_base[t/32] + 32*k + t%32.
+// t/32 holds node sell_node[t] (identity when the rows keep node order).
+// Its block k sits in slot slice_base[t/32] + 32*k + t%32, or, with slot
+// pairs, in slot slice_base[t/32] + 64*(k/2) + 2*(t%32) + k%2: two blocks of
+// one row side by side, so that a 32-byte sector of FP32 blocks never holds
+// a block of a shorter neighbouring row's padding (slices are then padded to
+// an even width).
 struct SellLayout {
+    bool pair = false;                   // slot pairs (the FP32 layout)
     int64_t n_sell = 0;                  // padded block slots
     std::vector<int64_t> slice_base;     // [n_slices+1], in blocks
     std::vector<int32_t> sell_node;      // [n_nodes] node at each row position
@@ -59,7 +64,7 @@ struct SellDev {
     uint8_t *pat_id = nullptr;           // row stencils, null without
     int32_t *pat_off = nullptr;
     int n_pat = 0;
-    bool sorted = false;
+    bool sorted = false, pair = false;
 };
 
 // buffers of the mixed-precision solve (FP32 tangent and CG)
@@ -117,7 +122,29 @@ void tri_element_dphi(int p, const double *X, const double *Y, double *dphi, dou
 int32_t greedy_coloring_nn(int32_t n_el, int32_t n_nodes, int32_t nn, const int32_t *connects, int32_t *el_color);
 // SELL-32 layout of s's block pattern; sorted: rows by length inside each
 // kRedBlock-node window (stable, longest first)
-std::string build_sell(const Setup &s, bool sorted, SellLayout &L);
+std::string build_sell(const Setup &s, bool sorted, bool pair, SellLayout &L);
+
+// slot of block k of row position t
+inline int64_t sell_slot(const SellLayout &L, int64_t t, int64_t k)
+{
+    return L.pair ? L.slice_base[t / 32] + 64 * (k >> 1) + 2 * (t % 32) + (k & 1)
+                  : L.slice_base[t / 32] + 32 * k + t % 32;
+}
+
+#ifdef __CUDACC__
+// the same on the device, split into the row's first slot (slice start
+// slice0, lane = t % 32) and the offset of its block k
+template <bool PAIR>
+__device__ __forceinline__ int64_t sell_row0(int64_t slice0, int lane)
+{
+    return slice0 + (PAIR ? 2 * lane : lane);
+}
+template <bool PAIR>
+__device__ __forceinline__ int64_t sell_koff(int k)
+{
+    return PAIR ? 64 * (int64_t)(k >> 1) + (k & 1) : 32 * (int64_t)k;
+}
+#endif
 void build_row_stencils(SellLayout &L);
 int32_t greedy_coloring(int32_t n_el, int32_t n_nodes, const int32_t *connects, int32_t *el_color);
 void elastic_constants(double E, double nu, ElasticConstH &el);

@@ -426,7 +426,7 @@ __global__ void __launch_bounds__(256, 8) k_fcg_spmv(int32_t n, const int64_t *_
     int64_t base = 0;
     int len = 0, pb = 0;
     if (i < n) {
-        base = __ldg(&slice_base[i >> 5]) + (i & 31);
+        base = sell_row0<true>(__ldg(&slice_base[i >> 5]), i & 31);
         len = __ldg(&rowlen[i]);
         if (PAT) pb = (int)__ldg(&pat_id[i]) * kPatLen;
     }
@@ -440,7 +440,7 @@ __global__ void __launch_bounds__(256, 8) k_fcg_spmv(int32_t n, const int64_t *_
         float y0 = 0.f, y1 = 0.f;
 #pragma unroll 4
         for (int k = 0; k < len; k++) {
-            const int64_t s = base + (int64_t)k * 32;
+            const int64_t s = base + sell_koff<true>(k);
             const int32_t c = PAT ? i + __ldg(&pat_off[pb + k]) : __ldcs(&scol[s]);
             const float4 a = __ldcs(&K[s]);
             const float2 zz = ld_keep(&z[c], keep), pp = ld_keep(&p_old[c], keep);
@@ -564,14 +564,14 @@ __global__ void __launch_bounds__(256) k_spmv32(int32_t n, const int64_t *__rest
     const int32_t t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= n) return;
     const int32_t i = sell_node[t];
-    const int64_t base = slice_base[t >> 5] + (t & 31);
+    const int64_t base = sell_row0<true>(slice_base[t >> 5], t & 31);
     const int len = rowlen[t];
     const int pb = PAT ? (int)__ldg(&pat_id[t]) * kPatLen : 0;
     const uint64_t keep = l2_policy_keep();
     float y0 = 0.f, y1 = 0.f;
 #pragma unroll 4
     for (int k = 0; k < len; k++) {
-        const int64_t s = base + (int64_t)k * 32;
+        const int64_t s = base + sell_koff<true>(k);
         const float4 a = __ldcs(&K[s]);
         const float2 v = ld_keep(&x[PAT ? i + __ldg(&pat_off[pb + k]) : __ldg(&scol[s])], keep);
         y0 = fmaf(a.x, v.x, fmaf(a.y, v.y, y0));

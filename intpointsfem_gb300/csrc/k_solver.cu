@@ -256,6 +256,7 @@ __global__ void __launch_bounds__(kRedBlock) k_cg_init(int32_t n_nodes, const do
 // PAT: block k of the row has column i + pat_off[pat_id[t] * kPatLen + k]
 // (row stencils, L1-resident) instead of the column index stored with it;
 // same blocks in the same order, so the result is the same bit for bit.
+// FP32 layouts use slot pairs, FP64 layouts one slot per lane and block.
 template <class T, bool SORTED, bool PAT>
 __global__ void __launch_bounds__(kRedBlock) k_cg_spmv(int32_t n_nodes, const int64_t *__restrict__ slice_base,
                                                        const int32_t *__restrict__ rowlen,
@@ -268,6 +269,7 @@ __global__ void __launch_bounds__(kRedBlock) k_cg_spmv(int32_t n_nodes, const in
                                                        CGScalarsT<T> *sc)
 {
     typedef typename Vec2<T>::type V;
+    constexpr bool PAIR = sizeof(T) == 4;
     __shared__ T s_pq[1][kRedStage];
     const int32_t t = blockIdx.x * kRedBlock + threadIdx.x;
     // row metadata is loaded before the flag so that the two latencies overlap
@@ -275,7 +277,7 @@ __global__ void __launch_bounds__(kRedBlock) k_cg_spmv(int32_t n_nodes, const in
     int64_t base = 0;
     if (t < n_nodes) {
         if (SORTED) i = __ldg(&sell_node[t]);
-        base = __ldg(&slice_base[t >> 5]) + (t & 31);
+        base = sell_row0<PAIR>(__ldg(&slice_base[t >> 5]), t & 31);
         len = __ldg(&rowlen[t]);
         if (PAT) pb = (int)__ldg(&pat_id[t]) * kPatLen;
     }
@@ -289,7 +291,7 @@ __global__ void __launch_bounds__(kRedBlock) k_cg_spmv(int32_t n_nodes, const in
         T y0 = T(0), y1 = T(0);
 #pragma unroll 4
         for (int k = 0; k < len; k++) {
-            const int64_t s = base + (int64_t)k * 32;
+            const int64_t s = base + sell_koff<PAIR>(k);
             const int32_t c = PAT ? i + __ldg(&pat_off[pb + k]) : __ldg(&scol[s]);
             T a00, a01, a10, a11;
             load_block(K, s, a00, a01, a10, a11);
