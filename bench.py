@@ -51,9 +51,10 @@ CONFIGS = {
 # by --impl reference to scale its bounded CG sample to whole Newton iterations.
 CFG2_CG_ITERS = [7001, 7822, 7021, 7695, 7021, 7913, 7021, 7895]
 CFG2_CG_ITERS_JACOBI = [10119, 9495]
-# DRAM bytes (read + write) of one SpMV launch at 400 x 400 (rows sorted by
-# length), from the ncu capture summarised in profiles/k_cg_spmv_400x400.md
-SPMV_DRAM_BYTES = 388.405504e6 + 9.274112e6
+# DRAM bytes (read + write) of one FP64 SpMV launch at 400 x 400 (rows sorted
+# by length), from the ncu captures summarised in profiles/k_cg_spmv_400x400.md:
+# with row stencils, and with the stored column indices
+SPMV_DRAM_BYTES = {True: 346.375424e6 + 4.631552e6, False: 388.405504e6 + 9.274112e6}
 FALLBACK_HBM_GBS = 6800.0
 
 
@@ -401,7 +402,7 @@ def run_gpu(args):
         "precision": args.precision,
         "roofline": {"kernel": "k_cg_spmv", "bound": "hbm", "achieved": achieved, "peak": hbm_peak,
                      "unit": "GB/s", "frac": achieved / hbm_peak, "peak_kind": peak_kind,
-                     "traffic": SPMV_DRAM_BYTES if (n == 400 and not mixed) else None,
+                     "traffic": SPMV_DRAM_BYTES[bool(stencils)] if (n == 400 and not mixed) else None,
                      "algorithmic_bytes": spmv_bytes,
                      "ms_per_launch": ms_spmv,
                      "fp64": {"achieved_tflops": spmv_fp64_tflops, "peak_tflops": fp64_tflops,
