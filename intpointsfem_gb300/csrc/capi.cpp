@@ -62,7 +62,6 @@ cudaError_t upload_sell(const SellLayout &L, bool sorted, SellDev &D, cudaStream
     }
     D.n_sell = L.n_sell;
     D.sorted = sorted;
-    D.pair = L.pair;
     return e;
 }
 

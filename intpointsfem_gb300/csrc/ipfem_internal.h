@@ -64,7 +64,7 @@ struct SellDev {
     uint8_t *pat_id = nullptr;           // row stencils, null without
     int32_t *pat_off = nullptr;
     int n_pat = 0;
-    bool sorted = false, pair = false;
+    bool sorted = false;                 // the FP32 layouts use slot pairs, the FP64 layouts do not
 };
 
 // buffers of the mixed-precision solve (FP32 tangent and CG)
