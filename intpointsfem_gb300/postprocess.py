@@ -167,39 +167,68 @@ class Solution:
                            for k, v in num.items()}
         return self._nodal
 
-    def locate(self, pts, tol=1e-10):
-        """element and reference coordinates of each point (element -1 outside)"""
-        V = self.xy[self.con[:, :4]]                                       # [e, 4, 2]
-        V[self.tri, 3] = V[self.tri, 2]                                    # triangles: 3 vertices
-        lo, hi = V.min(1) - 1e-12, V.max(1) + 1e-12
+    def _inside(self, e, x, tol):
+        """reference coordinates of x in element e, or None outside it"""
+        v = self._V[e]
+        if self.tri[e]:
+            J = np.stack([v[1] - v[0], v[2] - v[0]], 1)
+            s = np.linalg.solve(J, x - v[0])
+            return s if (s.min() >= -tol and s.sum() <= 1 + tol) else None
+        s = np.zeros(2)
+        for _ in range(30):
+            xi, et = s
+            Nv = 0.25 * np.array([(1 - xi) * (1 - et), (1 + xi) * (1 - et), (1 + xi) * (1 + et),
+                                  (1 - xi) * (1 + et)])
+            dN = 0.25 * np.array([[-(1 - et), (1 - et), (1 + et), -(1 + et)],
+                                  [-(1 - xi), -(1 + xi), (1 + xi), (1 - xi)]])
+            r = Nv @ v - x
+            J = dN @ v                                                     # [2 (xi, eta), 2 (x, y)]
+            step = np.linalg.solve(J.T, r)
+            s = s - step
+            if np.abs(step).max() < 1e-14:
+                break
+        return np.clip(s, -1, 1) if np.all(np.abs(s) <= 1 + tol) else None
+
+    def locate(self, pts, tol=1e-10, k_near=16):
+        """element and reference coordinates of each point (element -1 outside).
+        The candidates are the k_near elements with the nearest centres (a k-d
+        tree) whose bounding box contains the point; the lowest-numbered
+        candidate that contains it is taken.  A point that none of them
+        contains is tested against every element in order.  On a conforming
+        mesh every element that contains a point is among its nearest, so the
+        choice equals the lowest-numbered containing element."""
+        if getattr(self, "_V", None) is None:
+            V = self.xy[self.con[:, :4]]                                   # [e, 4, 2]
+            V[self.tri, 3] = V[self.tri, 2]                                # triangles: 3 vertices
+            self._V = V
+            self._lo, self._hi = V.min(1) - 1e-12, V.max(1) + 1e-12
+            self._tree = None
+            try:
+                from scipy.spatial import cKDTree
+                self._tree = cKDTree(V.mean(1))
+            except ImportError:
+                pass
+        lo, hi = self._lo, self._hi
+        pts = np.asarray(pts, dtype=np.float64).reshape(-1, 2)
         el = np.full(len(pts), -1)
         ref = np.zeros((len(pts), 2))
-        for i, x in enumerate(np.asarray(pts, dtype=np.float64)):
-            for e in np.nonzero(np.all((x >= lo) & (x <= hi), 1))[0]:
-                v = V[e]
-                if self.tri[e]:
-                    J = np.stack([v[1] - v[0], v[2] - v[0]], 1)
-                    s = np.linalg.solve(J, x - v[0])
-                    if s.min() >= -tol and s.sum() <= 1 + tol:
+        k = min(k_near, len(lo))
+        near = self._tree.query(pts, k=k)[1].reshape(len(pts), -1) if self._tree is not None else None
+        for i, x in enumerate(pts):
+            found = False
+            if near is not None:
+                cand = np.sort(near[i][np.all((x >= lo[near[i]]) & (x <= hi[near[i]]), 1)])
+                for e in cand:
+                    s = self._inside(e, x, tol)
+                    if s is not None:
+                        el[i], ref[i], found = e, s, True
+                        break
+            if not found:
+                for e in np.nonzero(np.all((x >= lo) & (x <= hi), 1))[0]:
+                    s = self._inside(e, x, tol)
+                    if s is not None:
                         el[i], ref[i] = e, s
                         break
-                    continue
-                s = np.zeros(2)
-                for _ in range(30):
-                    xi, et = s
-                    Nv = 0.25 * np.array([(1 - xi) * (1 - et), (1 + xi) * (1 - et), (1 + xi) * (1 + et),
-                                          (1 - xi) * (1 + et)])
-                    dN = 0.25 * np.array([[-(1 - et), (1 - et), (1 + et), -(1 + et)],
-                                          [-(1 - xi), -(1 + xi), (1 + xi), (1 - xi)]])
-                    r = Nv @ v - x
-                    J = dN @ v                                             # [2 (xi, eta), 2 (x, y)]
-                    step = np.linalg.solve(J.T, r)
-                    s = s - step
-                    if np.abs(step).max() < 1e-14:
-                        break
-                if np.all(np.abs(s) <= 1 + tol):
-                    el[i], ref[i] = e, np.clip(s, -1, 1)
-                    break
         return el, ref
 
     def evaluate(self, pts):
