@@ -56,7 +56,7 @@ typedef struct ipfem_ctx ipfem_ctx;
 /* ------------------------------------------------------------------ mesh */
 /* Host description of the integration-point data that the reference builds
  * in TPZElastoPlasticIntPointsStructMatrix::SetUpDataStructure
- * (TPZElastoPlasticIntPointsStructMatrix.cpp:156-173).  All arrays are read
+ * (TPZElastoPlasticIntPointsStructMatrix.cpp:80-97).  All arrays are read
  * during ipfem_create only.  nn = nq = (order+1)^2 connects and points per
  * element. */
 typedef struct {
@@ -103,7 +103,9 @@ void *ipfem_stream(ipfem_ctx *ctx);
 
 /* ----------------------------------- TPZElastoPlasticIntPointsStructMatrix */
 /* External load factor: rhs_linear = f0 + lambda*df (the reference's
- * fRhsLinear, TPZElastoPlasticIntPointsStructMatrix.cpp:232-243). */
+ * fRhsLinear, built by AssembleBoundaryData,
+ * TPZElastoPlasticIntPointsStructMatrix.cpp:156-167, and added to the
+ * residual at :118 and :147). */
 ipfem_status ipfem_set_load_factor(ipfem_ctx *ctx, double lambda);
 /* Precision of the tangent and the linear solve (no counterpart in the
  * reference, whose tangent and solve are FP64):
@@ -118,10 +120,10 @@ ipfem_status ipfem_set_precision(ipfem_ctx *ctx, int mode);
 /* TPZMatWithMem::SetUpdateMem: when set, the next residual commits the
  * integration-point state (main.cpp:487-522). */
 ipfem_status ipfem_set_update_mem(ipfem_ctx *ctx, int update);
-/* Assemble(rhs) (TPZElastoPlasticIntPointsStructMatrix.cpp:213-230):
+/* Assemble(rhs) (TPZElastoPlasticIntPointsStructMatrix.cpp:137-154):
  * rhs = -B^T sigma(u) + rhs_linear, Dirichlet rows zeroed. */
 ipfem_status ipfem_assemble_residual(ipfem_ctx *ctx, const double *u, double *rhs, int where);
-/* Assemble(K, rhs) (TPZElastoPlasticIntPointsStructMatrix.cpp:175-211):
+/* Assemble(K, rhs) (TPZElastoPlasticIntPointsStructMatrix.cpp:99-135):
  * rhs as above; the tangent K stays on the device for ipfem_solve. */
 ipfem_status ipfem_assemble(ipfem_ctx *ctx, const double *u, double *rhs, int where);
 /* K as nodal 2x2 blocks, rows ascending, columns ascending per row:
@@ -206,7 +208,10 @@ ipfem_status ipfem_newton_advance(ipfem_ctx *ctx, int32_t n_iters, double *u, in
 /* ------------------------------------------------ TPZCudaCalls replacements */
 /* Canonical deterministic dot product of two device vectors of length neq
  * (the reduction order of the CG; replaces cublasDdot in
- * TPZCudaCalls::SolveCG, TPZCudaCalls.cu:245-286).  *out is a host double. */
+ * TPZCudaCalls::SolveCG, TPZCudaCalls.cu:245-286).  *out is a host double.
+ * d_a and d_b must be 16-byte aligned (cudaMalloc'd memory is; a slice at an
+ * odd double offset is not): misaligned vectors are rejected with
+ * IPFEM_INVALID before anything is launched. */
 ipfem_status ipfem_dot(ipfem_ctx *ctx, const double *d_a, const double *d_b, double *out);
 /* TPZNumericalIntegrator::Multiply (TPZNumericalIntegrator.cpp:25-37):
  * gather + B*u.  d_strain: device, SoA [3][n_ip] (eps_xx, gamma_xy, eps_yy). */
@@ -224,16 +229,19 @@ ipfem_status ipfem_scatter_residual(ipfem_ctx *ctx, const double *d_sigma_w, dou
  * memory (an application that serves all device memory from its own
  * preallocated pool, or a latency-critical pipeline that must not call
  * cudaMalloc, which synchronises the device).  No counterpart in the
- * reference.  Needs no context: d_a and
- * d_b are device vectors of n doubles (n even, n <= 33,554,432), the result is
- * written to the device double *d_out, asynchronously on `stream`
- * (cudaStream_t, NULL = legacy default stream).  The scratch lives in a
- * 512 KiB array inside the library that every device keeps until process
- * exit; it allocates nothing and calls no allocating routine.  The first call
- * on a device also looks up that array's device address (make it before any
- * stream capture).  Calls share the array: calls that overlap on the GPU (on
- * different streams without ordering) race and give wrong results.  Larger n
- * is rejected with IPFEM_INVALID; the message is in ipfem_last_error(NULL). */
+ * reference.  Needs no context: d_a and d_b are device vectors of n doubles
+ * (n even, n <= 33,554,432), both 16-byte aligned; the result is written to
+ * the device double *d_out (8-byte aligned), asynchronously on `stream`
+ * (cudaStream_t, NULL = legacy default stream).  Bad arguments (null,
+ * misaligned, odd or too large n) are rejected with IPFEM_INVALID before
+ * anything touches the device; the message is in ipfem_last_error(NULL).
+ * The scratch lives in a 512 KiB array inside the library that every device
+ * keeps until process exit; the call allocates nothing and calls no
+ * allocating routine.  Every call looks up that array's device address in
+ * the current device's context (a lookup, not an allocation); the first call
+ * on a device may also load the library's device code, so make it before any
+ * stream capture.  Calls share the array: calls that overlap on the GPU (on
+ * different streams without ordering) race and give wrong results. */
 ipfem_status ipfem_dot_noalloc(const double *d_a, const double *d_b, int64_t n, double *d_out, void *stream);
 
 /* Integration-point state (TPZConstitutiveLawProcessor members), host copies.

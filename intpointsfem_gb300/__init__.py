@@ -329,7 +329,7 @@ class ElastoPlasticIntPointsStructMatrix:
 
     Create()/CreateAssemble(rhs) build the integration-point data once;
     Assemble(K, rhs) computes tangent + residual, Assemble(rhs) the residual
-    (TPZElastoPlasticIntPointsStructMatrix.cpp:110-230).  The solution vector
+    (TPZElastoPlasticIntPointsStructMatrix.cpp:34-78, 99-154).  The solution vector
     that the reference reads from the PZ mesh is passed explicitly.
     """
 

@@ -787,6 +787,9 @@ uint64_t ipfem_launch_count(const ipfem_ctx *c)
 ipfem_status ipfem_dot(ipfem_ctx *c, const double *d_a, const double *d_b, double *out)
 {
     if (!c || !d_a || !d_b || !out) return fail(c, IPFEM_INVALID, "bad args");
+    // the dot kernel reads node pairs as 16-byte loads
+    if ((reinterpret_cast<uintptr_t>(d_a) | reinterpret_cast<uintptr_t>(d_b)) & 15u)
+        return fail(c, IPFEM_INVALID, "ipfem_dot: d_a and d_b must be 16-byte aligned");
     return dot_host(c, d_a, d_b, out);
 }
 

@@ -9,7 +9,7 @@
 //                    reduction of the reference, evaluated per node as a
 //                    gather over the (at most one per colour) incident elements,
 //                    in the reference's pairing order; + f0 + lambda*df and
-//                    Dirichlet masking (TPZElastoPlasticIntPointsStructMatrix.cpp:213-230).
+//                    Dirichlet masking (TPZElastoPlasticIntPointsStructMatrix.cpp:137-154).
 //  k_stiffness       TPZNumericalIntegrator::KAssembly (…cpp:131-214) and
 //                    MatrixAssembleKernel (KernelsMatrixAssemble.h:24-57): one warp
 //                    per element, K_e = sum_q B_q^T (w Dep_q) B_q (upper triangle),

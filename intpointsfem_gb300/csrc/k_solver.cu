@@ -16,8 +16,6 @@
 // Scalars (alpha, beta, convergence) live in device memory, so an iteration
 // is three kernels with no host round trip; the host replays a captured CUDA
 // graph of several iterations and checks the `done` word between replays.
-#include <mutex>
-
 #include "ipfem_internal.h"
 #include "ldhint.cuh"
 #include "pdl.cuh"
@@ -608,19 +606,25 @@ struct NoAllocScratch {
 
 static __device__ __align__(256) NoAllocScratch g_noalloc_scratch;
 
-namespace {
-std::mutex g_noalloc_mu;
-NoAllocScratch *g_noalloc_ptr[256] = {nullptr};   // device address of the array, per device
-}  // namespace
-
 }  // namespace ipfem
 
 extern "C" ipfem_status ipfem_dot_noalloc(const double *d_a, const double *d_b, int64_t n, double *d_out,
                                           void *stream)
 {
     using namespace ipfem;
+    // every argument is checked before the first CUDA call: a rejected call
+    // touches neither the device nor the stream
     if (!d_a || !d_b || !d_out || n < 0 || (n & 1)) {
         set_thread_error("ipfem_dot_noalloc: null pointer, negative or odd length");
+        return IPFEM_INVALID;
+    }
+    // the kernel reads the vectors as pairs of doubles (16-byte loads)
+    if ((reinterpret_cast<uintptr_t>(d_a) | reinterpret_cast<uintptr_t>(d_b)) & 15u) {
+        set_thread_error("ipfem_dot_noalloc: d_a and d_b must be 16-byte aligned");
+        return IPFEM_INVALID;
+    }
+    if (reinterpret_cast<uintptr_t>(d_out) & 7u) {
+        set_thread_error("ipfem_dot_noalloc: d_out must be 8-byte aligned");
         return IPFEM_INVALID;
     }
     const int64_t n_nodes = n / 2;
@@ -630,29 +634,18 @@ extern "C" ipfem_status ipfem_dot_noalloc(const double *d_a, const double *d_b, 
                          std::to_string(2 * kRedBlock * kNoAllocMaxPartials) + " doubles");
         return IPFEM_INVALID;
     }
-    int dev = -1;
-    cudaError_t e = cudaGetDevice(&dev);
-    if (e != cudaSuccess || dev < 0 || dev >= 256) {
-        set_thread_error(std::string("ipfem_dot_noalloc: no current device: ") + cudaGetErrorString(e));
-        return IPFEM_NO_DEVICE;
+    // The host-side name of the array is not a device address: ask the
+    // runtime for the address in the current device's context.  The lookup
+    // allocates nothing; it is repeated on every call so that a context
+    // created anew (after cudaDeviceReset, or on another device) is never
+    // given a stale address.
+    void *p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess || !p) {
+        set_thread_error(std::string("ipfem_dot_noalloc: cudaGetSymbolAddress failed: ") + cudaGetErrorString(e));
+        return e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver ? IPFEM_NO_DEVICE : IPFEM_CUDA;
     }
-    NoAllocScratch *scr = nullptr;
-    {
-        // one-time set-up on this device: the host-side name of the array is
-        // not a device address, so ask the runtime for the device address
-        std::lock_guard<std::mutex> lk(g_noalloc_mu);
-        if (!g_noalloc_ptr[dev]) {
-            void *p = nullptr;
-            e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-            if (e != cudaSuccess || !p) {
-                set_thread_error(std::string("ipfem_dot_noalloc: cudaGetSymbolAddress failed: ") +
-                                 cudaGetErrorString(e));
-                return IPFEM_CUDA;
-            }
-            g_noalloc_ptr[dev] = static_cast<NoAllocScratch *>(p);
-        }
-        scr = g_noalloc_ptr[dev];
-    }
+    NoAllocScratch *scr = static_cast<NoAllocScratch *>(p);
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     if (n_nodes == 0) {
         e = cudaMemsetAsync(d_out, 0, sizeof(double), st);

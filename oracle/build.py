@@ -3,7 +3,8 @@
 * ``oracle/liboracle.so``   -- the C restatement (orc_constitutive.c, orc_problem.c)
 * ``oracle/_ref/libipfem_ref.so`` -- the reference's own constitutive headers
   (FunctionsStressStrain.h, FunctionsTangentOperator.h, compiled unmodified from
-  the reference tree named by IPFEM_REFERENCE_DIR, default /root/reference)
+  the reference tree named by IPFEM_REFERENCE_DIR, by default the directory
+  `reference` beside the repository root)
   behind oracle/ref_driver.cpp and the two-header shim in oracle/ref_shim/.
   Built only where the reference tree exists; outputs go to oracle/_ref/ only.
 
@@ -43,7 +44,12 @@ def build_oracle(force=False):
 
 
 def reference_dir():
-    return os.environ.get("IPFEM_REFERENCE_DIR", "/root/reference")
+    """the reference tree: IPFEM_REFERENCE_DIR, else `reference` beside the
+    repository root (absent on machines that only run the prebuilt files)"""
+    d = os.environ.get("IPFEM_REFERENCE_DIR")
+    if d:
+        return d
+    return os.path.normpath(os.path.join(HERE, "..", "..", "reference"))
 
 
 def build_ref(force=False):

@@ -75,7 +75,7 @@ void orc_ip_tangent6(const orc_elastic *el, const orc_mc *mc, const double strai
                      double sigma6[6], double eps_p6_out[6], double T36[36], int *mtype);
 
 /* Same, but with the argument aliasing of the reference GPU residual kernel
- * (KernelsComputeSigma.h:171: ProjectSigma(sigma_projected, sigma_projected, ...)).
+ * (KernelsComputeSigma.h:48: ProjectSigma(sigma_projected, sigma_projected, ...)).
  * Only used to document the CPU/GPU discrepancy of the reference. */
 void orc_ip_update_gpu_alias(const orc_elastic *el, const orc_mc *mc,
                              const double strain3[3], const double eps_p6[6], double weight,
@@ -87,7 +87,7 @@ void orc_ip_update_gpu_alias(const orc_elastic *el, const orc_mc *mc,
  * (3 for strain/sigma_w, 6 for plastic strain, 9 for dep).  dep may be NULL.
  * If update_mem != 0, eps_p6 is overwritten with the updated plastic strain
  * and sigma6_state / mtype / alpha receive the committed values (the GPU
- * assignment semantics of KernelsComputeSigma.h:184-194). */
+ * assignment semantics of KernelsComputeSigma.h:59-68). */
 void orc_compute_sigma_batch(int64_t npts, int pts_per_mat,
                              const orc_elastic *el, const orc_mc *mats,
                              const double *strain3, double *eps_p6,

@@ -11,8 +11,8 @@
  *   orc_gather_strain    TPZNumericalIntegrator.cpp:40-51 + TPZIrregularBlocksMatrix.cpp:97-140 (opt 0)
  *   orc_scatter_residual TPZNumericalIntegrator.cpp:81-105 (alpha = -1, colour slabs,
  *                        pairwise slab reduction)
- *   orc_assemble_residual TPZElastoPlasticIntPointsStructMatrix.cpp:213-230
- *   orc_assemble         TPZElastoPlasticIntPointsStructMatrix.cpp:175-211 and
+ *   orc_assemble_residual TPZElastoPlasticIntPointsStructMatrix.cpp:137-154
+ *   orc_assemble         TPZElastoPlasticIntPointsStructMatrix.cpp:99-135 and
  *                        TPZNumericalIntegrator.cpp:131-182, 236-270 (element
  *                        tangent, upper triangle, colour-ordered accumulation)
  *   orc_solve_steps      main.cpp:160-262 (Newton) and main.cpp:487-522 (accept)

@@ -6,7 +6,7 @@
  *
  *  ref_ip_sigma      : TPZConstitutiveLawProcessor.cpp:163-195 (CPU ComputeSigma)
  *  ref_ip_sigma_dep  : TPZConstitutiveLawProcessor.cpp:377-423 (CPU ComputeSigmaDep)
- *  ref_ip_sigma_gpu  : KernelsComputeSigma.h:154-182 (GPU ComputeSigmaKernel,
+ *  ref_ip_sigma_gpu  : KernelsComputeSigma.h:7-74 (GPU ComputeSigmaKernel,
  *                      whose ProjectSigma call aliases input and output)
  *
  * Built by oracle/build.py into oracle/_ref/ only; never part of the product.

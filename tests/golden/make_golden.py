@@ -7,7 +7,7 @@ through three per-point sequences of the reference:
 
   cpu      TPZConstitutiveLawProcessor.cpp:163-195  (ComputeSigma, CPU)
   cpu_dep  TPZConstitutiveLawProcessor.cpp:377-423  (ComputeSigmaDep, CPU)
-  gpu      KernelsComputeSigma.h:154-182            (ComputeSigmaKernel)
+  gpu      KernelsComputeSigma.h:7-74               (ComputeSigmaKernel)
 
 Inputs are seeded synthetic (strain, committed plastic strain, material)
 triples chosen to visit every branch: elastic, main plane, right and left

@@ -13,7 +13,9 @@ import os
 import re
 import sys
 
-REF = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+# the reference tree: argument, IPFEM_REFERENCE_DIR, or `reference` beside the repository root
+REF = sys.argv[1] if len(sys.argv) > 1 else (os.environ.get("IPFEM_REFERENCE_DIR") or os.path.normpath(
+     os.path.join(os.path.dirname(os.path.abspath(__file__)), "..", "..", "..", "reference")))
 OUT = os.path.join(os.path.dirname(os.path.abspath(__file__)), "reference_logs.json")
 
 

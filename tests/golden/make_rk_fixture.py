@@ -39,8 +39,13 @@ def load_fem(path):
     return np.array([[float(r[i]) for i in idx] for r in rows[1:]])
 
 
+# the reference tree: argument, IPFEM_REFERENCE_DIR, or `reference` beside the repository root
+DEFAULT_REF = os.environ.get("IPFEM_REFERENCE_DIR") or os.path.normpath(
+    os.path.join(os.path.dirname(os.path.abspath(__file__)), "..", "..", "..", "reference"))
+
+
 def main():
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    ref = sys.argv[1] if len(sys.argv) > 1 else DEFAULT_REF
     d = os.path.join(ref, "mathematica_notebooks", "RK_Verification")
     ep = load(os.path.join(d, "ElastoPlasticRKdata.txt"))
     el = load(os.path.join(d, "ElasticRKdata.txt"))

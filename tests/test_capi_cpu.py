@@ -98,3 +98,27 @@ def test_coloring_rejects_bad_connects():
 def test_wellbore_rejects_bad_params():
     with pytest.raises(ip.IpfemError):
         ip.WellboreMesh(ip.wellbore_params(0))
+
+
+def test_dot_noalloc_rejects_bad_arguments_before_any_device_call():
+    """ipfem_dot_noalloc validates every argument before its first CUDA call,
+    so these rejections need no GPU: the addresses are never dereferenced.
+    A slice at an odd double offset (8 bytes past a 16-byte boundary) is
+    refused, as are null pointers, odd lengths and lengths past the
+    maximum."""
+    import ctypes as C
+
+    L = ip.lib()
+    a, b, out = 0x10000, 0x20000, 0x30000          # 16-byte aligned, never dereferenced
+    cases = [
+        (a + 8, b, 16, out, b"16-byte"),           # d_a at an odd double offset
+        (a, b + 8, 16, out, b"16-byte"),
+        (a, b, 16, out + 4, b"8-byte"),            # d_out not a double address
+        (0, b, 16, out, b"null"),
+        (a, b, 3, out, b"odd"),
+        (a, b, 2 * 256 * 65536 + 2, out, b"maximum"),
+    ]
+    for pa, pb, n, po_, msg in cases:
+        st = L.ipfem_dot_noalloc(C.c_void_p(pa), C.c_void_p(pb), n, C.c_void_p(po_), None)
+        assert st == 5, (pa, pb, n, po_)
+        assert msg in L.ipfem_last_error(None), L.ipfem_last_error(None)

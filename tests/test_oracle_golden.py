@@ -75,7 +75,7 @@ def test_oracle_bit_exact_vs_reference(gold, tag, dep):
 
 def test_reference_gpu_kernel_aliasing_is_reproduced(gold):
     """The reference's residual kernel aliases ProjectSigma's input and output
-    (KernelsComputeSigma.h:171); the oracle's aliased variant reproduces it,
+    (KernelsComputeSigma.h:48); the oracle's aliased variant reproduces it,
     and it differs from the CPU path on some edge/apex points."""
     n = len(gold["lam"])
     for i in range(n):

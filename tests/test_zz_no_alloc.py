@@ -53,3 +53,18 @@ def test_dot_noalloc_rejects_oversize_and_odd():
     st = L.ipfem_dot_noalloc(C.c_void_p(a.data_ptr()), C.c_void_p(a.data_ptr()), 3, C.c_void_p(out.data_ptr()),
                              None)
     assert st == 5
+
+
+def test_dot_noalloc_rejects_offset_slice_and_launches_nothing():
+    """a vector that starts at an odd double offset of an allocation is
+    refused with IPFEM_INVALID; the output is left untouched"""
+    torch = pytest.importorskip("torch")
+    L = ip.lib()
+    base = torch.ones(66, dtype=torch.float64, device="cuda")
+    out = torch.full((1,), 7.0, dtype=torch.float64, device="cuda")
+    torch.cuda.synchronize()
+    st = L.ipfem_dot_noalloc(C.c_void_p(base[1:].data_ptr()), C.c_void_p(base.data_ptr()), 64,
+                             C.c_void_p(out.data_ptr()), None)
+    torch.cuda.synchronize()
+    assert st == 5 and b"16-byte" in L.ipfem_last_error(None)
+    assert out.item() == 7.0
