@@ -9,18 +9,24 @@ and the next step's first assembly fall inside the iteration where they
 occur).  W warm-up iterations run untimed, then exactly K are timed.
 
   value    : device-timed (CUDA events on the library's stream), inputs resident
-  e2e      : the same iterations through the C-ABI with pinned host buffers
-             (u copied H2D and D2H every iteration), host-timed
+  e2e      : the same iterations through the C-ABI with a pinned host u: each
+             timed step is one ipfem_newton_advance(u, 1, IPFEM_HOST) call,
+             which copies u H2D on entry and D2H on exit; host-timed
+  solve    : time to solution: the whole load-stepped solve (the warm-up,
+             timed and remaining iterations of the same run), with its Newton
+             and CG iteration counts, for the plain and the chosen method
   roofline : the CG block SpMV (dominant kernel), algorithmic bytes / launch
              over its CUDA-event duration, against the measured HBM copy peak
   cpu_baseline : the C oracle on the host cores, bounded sample (one tangent
              assembly + S CG iterations with the same preconditioner), scaled to
-             a Newton iteration with the CG iteration count of the timed GPU
-             iterations (the oracle performs bit-identical arithmetic, so the
+             a Newton iteration with the CG iteration count this run measured on
+             the GPU (the oracle performs bit-identical arithmetic, so the
              counts are the same)
 
---impl reference times the oracle alone (the reference's own CPU path cannot
-be built: it needs NeoPZ, Intel MKL and TBB).
+--impl reference runs the oracle's own Newton iterations on all host cores:
+the same W warm-up and K timed iterations of the same solve, measured, not
+scaled (the reference's own CPU path cannot be built: it needs NeoPZ, Intel
+MKL and TBB).
 """
 import argparse
 import json
@@ -46,14 +52,9 @@ CONFIGS = {
     5: {"n": 2000, "n_steps": 30, "wb": {"material_mode": 2, "c_cv": 0.3, "phi_lo_deg": 25.0, "phi_hi_deg": 35.0,
                                          "pw_final": -5.0}},
 }
-# CG iterations of the first Newton iterations of the 400 x 400 solve, as run on
-# the GPU (identical on the CPU oracle), with block Jacobi and with Jacobi; used
-# by --impl reference to scale its bounded CG sample to whole Newton iterations.
-CFG2_CG_ITERS = [7001, 7822, 7021, 7695, 7021, 7913, 7021, 7895]
-CFG2_CG_ITERS_JACOBI = [10119, 9495]
 # DRAM bytes (read + write) of one FP64 SpMV launch at 400 x 400 (rows sorted
-# by length), from the ncu captures summarised in profiles/k_cg_spmv_400x400.md:
-# with row stencils, and with the stored column indices
+# by length), from the ncu capture of that launch (dram__bytes_read.sum +
+# dram__bytes_write.sum): with row stencils, and with the stored column indices
 SPMV_DRAM_BYTES = {True: 346.375424e6 + 4.631552e6, False: 388.405504e6 + 9.274112e6}
 FALLBACK_HBM_GBS = 6800.0
 
@@ -178,48 +179,97 @@ def ddp_env():
     return ws, rank, local
 
 
+def workload_config(args):
+    """the workload both arms run, named by what it is (identical dicts)"""
+    n = args.n
+    n_ip, neq = 9 * n * n, 2 * (2 * n + 1) ** 2
+    n_blocks = (8 * n + 1) ** 2
+    prec = "Jacobi-CG" if args.jacobi else "block-Jacobi CG"
+    return {"workload": "wellbore %dx%d order-2 quads, %d IPs, %d dofs, plain FP64, %s 1e-8, Newton 1e-8, "
+                        "%d load steps%s; Newton iterations %d-%d of the solve timed (warm-up %d)"
+                        % (n, n, n_ip, neq, prec, args.n_steps,
+                           (", material %s" % json.dumps(args.wb)) if args.wb else "",
+                           args.warmup + 1, args.warmup + args.steps, args.warmup),
+            "mesh": "%dx%d" % (n, n), "load_steps": args.n_steps, "ips": n_ip, "dofs": neq,
+            "linear_solver": prec, "cg_rtol": 1e-8, "newton_rtol": 1e-8,
+            "l2": ("inputs larger than L2 (tangent %.0f MB, element blocks %.0f MB)" if n_blocks * 32 > 129e6
+                   else "inputs fit in L2 (tangent %.0f MB, element blocks %.0f MB); no flush")
+                  % (n_blocks * 32 / 1e6, n * n * 1296 / 1e6)}
+
+
 def run_reference(args):
+    """The oracle's Newton iterations on all host cores: W untimed, K timed.
+    The oracle's arithmetic is the library's bit for bit, so these are the
+    same iterations (same CG counts) as the GPU arm's."""
     ws, rank, _ = ddp_env()
     if rank != 0:
         return 0
+    import numpy as np
+
+    from oracle import pyoracle as po
+
     threads = args.cpu_threads or os.cpu_count()
-    n = args.n
-    arm = CpuArm(n, threads, args.n_steps, args.wb, block=not args.jacobi)
-    if n <= 100:
-        # small meshes: the oracle's own CG iteration count to 1e-8 on the first tangent
-        R = arm.P.assemble(arm.u, 1.0 / args.n_steps)
-        _, k = arm.P.pcg(R, rtol=1e-8, max_it=200000)
-        cg_iters, cg_note = [abs(k)], "the oracle's CG iterations to 1e-8 on the first tangent"
-    else:
-        # the measured 400 x 400 counts, scaled by n / 400 (CG iterations grow linearly with n here)
-        cg_iters = [c * n / 400.0 for c in (CFG2_CG_ITERS_JACOBI if args.jacobi else CFG2_CG_ITERS)]
-        cg_note = "the GPU's CG iterations per Newton iteration at 400x400 scaled by n/400"
-    mean_cg = sum(cg_iters) / len(cg_iters)
-    samples = []
-    for i in range(args.warmup + args.steps):
-        cg = cg_iters[i] if i < len(cg_iters) else mean_cg
-        r = arm.sample(cg, args.cpu_cg_sample if i >= args.warmup else 5)
-        if i >= args.warmup:
-            samples.append(r)
-    arm.close()
-    ms = statistics.mean(s["ms_per_newton"] for s in samples)
+    P = po.OracleProblem(po.default_params(args.n, **args.wb), nthreads=threads)
+    P.set_block_jacobi(not args.jacobi)
+    u = np.zeros(P.neq)
+    newton = po.OracleNewton(P, args.n_steps, newton_max_it=40, cg_rtol=1e-8)
+    _, cg_w = newton.advance(u, args.warmup)
+    t0 = time.perf_counter()
+    k, cg = newton.advance(u, args.steps)
+    t_run = time.perf_counter() - t0
+    ms = 1e3 * t_run / max(1, k)
+    # residual evaluation (Assemble(rhs)) at the reached state, for IP/s
+    t0 = time.perf_counter()
+    nres = 3
+    for _ in range(nres):
+        P.assemble_residual(u, newton._lam())
+    t_res = (time.perf_counter() - t0) / nres
+    P.close()
     line = {
         "impl": "reference", "metric": METRIC, "value": ms, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": False, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": "wellbore %dx%d order-2 quads, %d IPs, plain FP64, %s 1e-8, Newton 1e-8, "
-                               "%d load steps (configuration %d)"
-                               % (n, n, 9 * n * n, "Jacobi-CG" if args.jacobi else "block-Jacobi CG", args.n_steps,
-                                  args.config)},
-        "ip_per_s": statistics.mean(s["ip_per_s"] for s in samples),
+        "config": workload_config(args),
+        "ip_per_s": P.n_ip / t_res,
+        "newton_iters_timed": k,
+        "cg_iters_per_newton": cg / max(1, k),
         "cpu_baseline": {"value": ms, "unit": UNIT, "cores": threads, "kind": "port",
-                         "sample": "per step: one tangent assembly + %d CG iterations of the C oracle, "
-                                   "scaled to %.0f CG iterations per Newton iteration (%s)"
-                                   % (samples[0]["cg_sample"], mean_cg, cg_note)},
+                         "sample": "the C oracle's own Newton iterations %d-%d of the solve (tangent assembly, "
+                                   "%s to 1e-8: %d CG iterations, residual norm and load-step commit), "
+                                   "measured on %d host threads; residual evaluation %.1f ms"
+                                   % (args.warmup + 1, args.warmup + k,
+                                      "Jacobi-CG" if args.jacobi else "block-Jacobi CG", cg, threads,
+                                      1e3 * t_res)},
         "e2e": {"value": ms, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
     return 0
+
+
+def timed_advance(S, stream, u, n_iters, e0, e1):
+    """n_iters Newton iterations (0 = to the end of the solve) of context S,
+    CUDA-event timed on its stream; returns (stats, ms)"""
+    import torch
+
+    import intpointsfem_gb300 as ip
+
+    torch.cuda.synchronize()
+    e0.record(stream)
+    st, _ = S.newton_advance(u, n_iters, ip.DEVICE)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    return st, e0.elapsed_time(e1)
+
+
+def solve_record(parts, n_steps):
+    """time to solution from the (stats, ms) of consecutive advances that
+    together cover the whole load-stepped solve"""
+    ms = sum(p[1] for p in parts)
+    nit = sum(p[0].newton_iters for p in parts)
+    cg = sum(p[0].cg_iters for p in parts)
+    return {"ms": ms, "load_steps": n_steps, "newton_iters": nit, "cg_iters": cg,
+            "ms_per_newton_iter": ms / max(1, nit), "converged": bool(parts[-1][0].converged),
+            "fcg_fallbacks": sum(p[0].fcg_fallbacks for p in parts)}
 
 
 def run_gpu(args):
@@ -247,21 +297,15 @@ def run_gpu(args):
     mixed = args.precision == "mixed"
     cg_rtol = args.mixed_cg_rtol if mixed else 1e-8
     A = ip.ElastoPlasticIntPointsStructMatrix(wb)         # device-resident arm
-    B = None if args.no_e2e else ip.ElastoPlasticIntPointsStructMatrix(wb)   # host-buffer (e2e) arm
     if mixed:
         A.set_precision(ip.MIXED)
-        if B:
-            B.set_precision(ip.MIXED)
     if not args.jacobi:
         A.set_preconditioner(ip.PREC_BLOCK_JACOBI)
-        if B:
-            B.set_preconditioner(ip.PREC_BLOCK_JACOBI)
     if args.no_row_stencils:
         A.set_row_stencils(0)
-        if B:
-            B.set_row_stencils(0)
     stream = torch.cuda.ExternalStream(A.stream, device=dev)
     fp64_tflops = A.measure_fp64_peak()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
 
     # residual evaluation throughput (Assemble(rhs)), inputs resident
     du = torch.zeros(A.neq, dtype=torch.float64, device=dev)
@@ -269,8 +313,8 @@ def run_gpu(args):
     A.SetLoadFactor(1.0 / N_STEPS)
     for _ in range(3):
         A.assemble_residual(du, dr, ip.DEVICE)
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     nres = 20
+    torch.cuda.synchronize()
     e0.record(stream)
     for _ in range(nres):
         A.assemble_residual(du, dr, ip.DEVICE)
@@ -278,9 +322,10 @@ def run_gpu(args):
     torch.cuda.synchronize()
     ms_res = e0.elapsed_time(e1) / nres
 
-    # Newton iterations, device-resident
+    # Newton iterations, device-resident: W warm-up, K timed, then (for the
+    # time to solution) the rest of the same solve
     A.newton_begin(N_STEPS, newton_max_it=40, cg_rtol=cg_rtol)
-    st_w, _ = A.newton_advance(du, args.warmup, ip.DEVICE)
+    part_w = timed_advance(A, stream, du, args.warmup, e0, e1)
     clocks = ClockSampler(dev.index)
     if dist:
         dist.barrier()
@@ -292,31 +337,47 @@ def run_gpu(args):
     e1.record(stream)
     torch.cuda.synchronize()
     clk = clocks.stop()
-    ms_dev = e0.elapsed_time(e1) / args.steps
+    ms_timed = e0.elapsed_time(e1)
     launches = A.launch_count - l0
-    ms_dev = reduce_max(ms_dev, dist)
+    ms_dev = reduce_max(ms_timed / args.steps, dist)
     cg_per_iter = st.cg_iters / max(1, st.newton_iters)
+    solve_plain = None
+    if args.solve:
+        part_r = timed_advance(A, stream, du, 0, e0, e1)
+        solve_plain = solve_record([part_w, (st, ms_timed), part_r], N_STEPS)
 
-    # e2e through the C-ABI with pinned host buffers
+    # e2e through the C-ABI with a pinned host u: one call per Newton
+    # iteration, u copied H2D on entry and D2H on exit of every call
     ms_e2e = None
-    if B:
+    if not args.no_e2e:
+        B = ip.ElastoPlasticIntPointsStructMatrix(wb)
+        if mixed:
+            B.set_precision(ip.MIXED)
+        if not args.jacobi:
+            B.set_preconditioner(ip.PREC_BLOCK_JACOBI)
+        if args.no_row_stencils:
+            B.set_row_stencils(0)
         hu = torch.zeros(B.neq, dtype=torch.float64, pin_memory=True)
         B.newton_begin(N_STEPS, newton_max_it=40, cg_rtol=cg_rtol)
-        B.newton_advance(hu, args.warmup, ip.HOST)
+        for _ in range(args.warmup):
+            B.newton_advance(hu, 1, ip.HOST)
         if dist:
             dist.barrier()
+        torch.cuda.synchronize()
         t0 = time.perf_counter()
-        B.newton_advance(hu, args.steps, ip.HOST)
+        for _ in range(args.steps):
+            B.newton_advance(hu, 1, ip.HOST)
         ms_e2e = 1e3 * (time.perf_counter() - t0) / args.steps
         B.close()
 
     # the chosen method (mixed precision + learned preconditioner) and mixed
-    # precision with Jacobi beside the plain one, same Newton iterations
+    # precision with block Jacobi beside the plain one, same Newton iterations;
+    # the chosen method also runs to the end of the solve (time to solution)
     chosen = None
     if not mixed and args.chosen:
         from intpointsfem_gb300 import train_preconditioner as tp
 
-        def mixed_arm(learned_prec):
+        def mixed_arm(learned_prec, to_end):
             C_ = ip.ElastoPlasticIntPointsStructMatrix(wb)
             if args.no_row_stencils:
                 C_.set_row_stencils(0)
@@ -329,32 +390,33 @@ def run_gpu(args):
             elif not args.jacobi:
                 C_.set_preconditioner(ip.PREC_BLOCK_JACOBI)
             uc = torch.zeros(C_.neq, dtype=torch.float64, device=dev)
-            C_.newton_begin(N_STEPS, newton_max_it=40, cg_rtol=args.mixed_cg_rtol)
-            C_.newton_advance(uc, args.warmup, ip.DEVICE)
             sc_ = torch.cuda.ExternalStream(C_.stream, device=dev)
-            torch.cuda.synchronize()
+            C_.newton_begin(N_STEPS, newton_max_it=40, cg_rtol=args.mixed_cg_rtol)
+            pw = timed_advance(C_, sc_, uc, args.warmup, e0, e1)
             l0c = C_.launch_count
-            e0.record(sc_)
-            stc, _ = C_.newton_advance(uc, args.steps, ip.DEVICE)
-            e1.record(sc_)
-            torch.cuda.synchronize()
-            out = {"ms_per_newton_iter": e0.elapsed_time(e1) / args.steps,
+            stc, msc = timed_advance(C_, sc_, uc, args.steps, e0, e1)
+            out = {"ms_per_newton_iter": msc / args.steps,
                    "cg_iters_per_newton": stc.cg_iters / max(1, stc.newton_iters),
                    "newton_iters_timed": stc.newton_iters, "fcg_fallbacks": stc.fcg_fallbacks,
                    "ms_cg_per_newton": stc.ms_solve / args.steps, "gpu_launches": C_.launch_count - l0c}
+            if to_end:
+                pr = timed_advance(C_, sc_, uc, 0, e0, e1)
+                out["solve"] = solve_record([pw, (stc, msc), pr], N_STEPS)
             if not learned_prec:
                 out["ms_spmv_fp32"] = C_.profile_spmv(reps=20)
             C_.close()
             return out
 
-        chosen = mixed_arm(True)
+        chosen = mixed_arm(True, args.solve)
         chosen["method"] = ("mixed + learned: FP32 tangent, flexible CG to %g preconditioned by the learned "
                             "triangular factor (weights shipped in intpointsfem_gb300/weights), FP64 residual/"
                             "return mapping/Newton refinement" % args.mixed_cg_rtol)
-        chosen["mixed_jacobi"] = mixed_arm(False)
+        chosen["mixed_jacobi"] = mixed_arm(False, False)
         chosen["mixed_jacobi"]["method"] = "mixed: FP32 tangent + FP32 %s to %g, FP64 Newton refinement" % (
             "Jacobi-CG" if args.jacobi else "block-Jacobi CG", args.mixed_cg_rtol)
         chosen["speedup_vs_plain"] = ms_dev / chosen["ms_per_newton_iter"]
+        if solve_plain and "solve" in chosen:
+            chosen["solve_speedup_vs_plain"] = solve_plain["ms"] / chosen["solve"]["ms"]
 
     # roofline of the dominant kernel (CG block SpMV), CUDA events on the library stream
     ms_spmv = A.profile_spmv(reps=20)
@@ -377,27 +439,27 @@ def run_gpu(args):
         if dist:
             dist.destroy_process_group()
         return 0
+    cfg = workload_config(args)
+    if mixed:
+        cfg["workload"] = cfg["workload"].replace("plain FP64", "mixed FP32/FP64").replace(
+            "CG 1e-8", "CG %g" % cg_rtol)
+        cfg["cg_rtol"] = cg_rtol
+    cfg["replicas"] = ws
     line = {
         "metric": METRIC, "value": ms_dev, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": ms_dev, "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64" if not mixed else "f32+f64",
-        "data": "synthetic",
-        "config": {"workload": "wellbore %dx%d order-2 quads, %d IPs, %d dofs, %s, %s %g, "
-                               "Newton 1e-8, %d load steps%s; first %d Newton iterations (warm-up %d); "
-                               "configuration %d"
-                               % (n, n, A.n_ip, A.neq, "plain FP64" if not mixed else "mixed FP32/FP64",
-                                  "Jacobi-CG" if args.jacobi else "block-Jacobi CG", cg_rtol,
-                                  N_STEPS, (", material %s" % json.dumps(args.wb)) if args.wb else "",
-                                  args.warmup + args.steps, args.warmup, args.config),
-                   "l2": "inputs larger than L2 (tangent %.0f MB, element blocks %.0f MB)"
-                         % (nb * 32 / 1e6, A.n_el * 1296 / 1e6),
-                   "replicas": ws, "row_stencils": bool(stencils)},
+        "ms_per_step": ms_dev, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64" if not mixed else "f32+f64", "data": "synthetic",
+        "config": cfg,
+        "row_stencils": bool(stencils),
         "ip_per_s": A.n_ip / (ms_res * 1e-3),
         "ms_residual": ms_res,
         "cg_iters_per_newton": cg_per_iter,
         "newton_iters_timed": st.newton_iters,
         "ms_breakdown": {"assemble": st.ms_assemble / args.steps, "cg": st.ms_solve / args.steps,
                          "commit": st.ms_commit / args.steps},
-        "e2e": ({"value": ms_e2e, "unit": UNIT, "h2d_bytes_per_step": 8 * A.neq, "d2h_bytes_per_step": 8 * A.neq}
+        "e2e": ({"value": ms_e2e, "unit": UNIT, "h2d_bytes_per_step": 8 * A.neq, "d2h_bytes_per_step": 8 * A.neq,
+                 "how": "one ipfem_newton_advance(u, 1, IPFEM_HOST) call per step: u (8 B x neq) copied H2D "
+                        "and D2H inside every timed step"}
                 if ms_e2e is not None else None),
         "precision": args.precision,
         "roofline": {"kernel": "k_cg_spmv", "bound": "hbm", "achieved": achieved, "peak": hbm_peak,
@@ -409,6 +471,8 @@ def run_gpu(args):
                               "frac": spmv_fp64_tflops / fp64_tflops, "peak_kind": "measured live (fma probe)"}},
         "gpu_launches": launches,
     }
+    if solve_plain:
+        line["solve"] = solve_plain
     if chosen:
         line["chosen"] = chosen
     if clk:
@@ -417,8 +481,8 @@ def run_gpu(args):
         line["cpu_baseline"] = {"value": cpu["ms_per_newton"], "unit": UNIT, "cores": args.cpu_threads or os.cpu_count(),
                                 "kind": "port",
                                 "sample": "C oracle (bit-identical arithmetic): one tangent assembly (%.0f ms) + %d "
-                                          "CG iterations (%.2f ms each), scaled by %.0f CG iterations per "
-                                          "Newton iteration; residual %.1f ms = %.3g IP/s"
+                                          "CG iterations (%.2f ms each), scaled by the %.0f CG iterations per "
+                                          "Newton iteration measured here on the GPU; residual %.1f ms = %.3g IP/s"
                                           % (cpu["t_asm_ms"], cpu["cg_sample"], cpu["t_cg_iter_ms"], cg_per_iter,
                                              cpu["t_res_ms"], cpu["ip_per_s"])}
     print(json.dumps(line))
@@ -443,6 +507,8 @@ def main():
     ap.add_argument("--mixed-cg-rtol", type=float, default=1e-4)
     ap.add_argument("--no-chosen", dest="chosen", action="store_false")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-solve", dest="solve", action="store_false",
+                    help="skip the time to solution (the rest of the solve after the timed iterations)")
     ap.add_argument("--jacobi", action="store_true", help="scalar Jacobi instead of block Jacobi in the CG")
     ap.add_argument("--no-row-stencils", action="store_true",
                     help="SpMVs read the stored column indices instead of the row stencils (same results)")

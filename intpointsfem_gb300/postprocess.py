@@ -189,46 +189,64 @@ class Solution:
                 break
         return np.clip(s, -1, 1) if np.all(np.abs(s) <= 1 + tol) else None
 
-    def locate(self, pts, tol=1e-10, k_near=16):
-        """element and reference coordinates of each point (element -1 outside).
-        The candidates are the k_near elements with the nearest centres (a k-d
-        tree) whose bounding box contains the point; the lowest-numbered
-        candidate that contains it is taken.  A point that none of them
-        contains is tested against every element in order.  On a conforming
-        mesh every element that contains a point is among its nearest, so the
-        choice equals the lowest-numbered containing element."""
-        if getattr(self, "_V", None) is None:
-            V = self.xy[self.con[:, :4]]                                   # [e, 4, 2]
-            V[self.tri, 3] = V[self.tri, 2]                                # triangles: 3 vertices
-            self._V = V
-            self._lo, self._hi = V.min(1) - 1e-12, V.max(1) + 1e-12
-            self._tree = None
-            try:
-                from scipy.spatial import cKDTree
-                self._tree = cKDTree(V.mean(1))
-            except ImportError:
-                pass
+    def _index(self):
+        """element vertices, bounding boxes and a uniform grid of cells, each
+        listing (in ascending order) the elements whose bounding box overlaps it"""
+        if getattr(self, "_V", None) is not None:
+            return
+        V = self.xy[self.con[:, :4]]                                       # [e, 4, 2]
+        V[self.tri, 3] = V[self.tri, 2]                                    # triangles: 3 vertices
+        self._V = V
+        lo, hi = V.min(1) - 1e-12, V.max(1) + 1e-12
+        self._lo, self._hi = lo, hi
+        g = max(1, int(np.sqrt(len(V))))
+        x0, x1 = lo.min(0), hi.max(0)
+        h = np.where(x1 > x0, (x1 - x0) / g, 1.0)
+        self._grid = (g, x0, h)
+        i0 = np.clip(np.floor((lo - x0) / h).astype(np.int64), 0, g - 1)
+        i1 = np.clip(np.floor((hi - x0) / h).astype(np.int64), 0, g - 1)
+        nx, ny = i1[:, 0] - i0[:, 0] + 1, i1[:, 1] - i0[:, 1] + 1
+        cnt = nx * ny
+        el = np.repeat(np.arange(len(V)), cnt)                             # ascending element order
+        k = np.arange(cnt.sum()) - np.repeat(np.cumsum(cnt) - cnt, cnt)    # index inside each element's block
+        cx = i0[el, 0] + k % nx[el]
+        cy = i0[el, 1] + k // nx[el]
+        cell = cy * g + cx
+        order = np.argsort(cell, kind="stable")                            # stable: elements stay ascending
+        self._cell_el = el[order]
+        self._cell_ptr = np.searchsorted(cell[order], np.arange(g * g + 1))
+
+    def _candidates(self, x):
+        """ascending elements whose bounding box contains x"""
+        g, x0, h = self._grid
+        c = np.floor((x - x0) / h).astype(np.int64)
+        if np.any(c < 0) or np.any(c >= g):
+            # outside the grid: only elements whose box reaches past it
+            # (none, as the grid spans every box), so nothing contains x
+            return np.zeros(0, np.int64)
+        cid = c[1] * g + c[0]
+        cand = self._cell_el[self._cell_ptr[cid]:self._cell_ptr[cid + 1]]
+        return cand[np.all((x >= self._lo[cand]) & (x <= self._hi[cand]), 1)]
+
+    def locate(self, pts, tol=1e-10, scan=False):
+        """element and reference coordinates of each point (element -1 outside):
+        the lowest-numbered element that contains it.  Every element whose
+        bounding box contains the point is listed, in ascending order, in the
+        grid cell of the point (the cells an element is filed under cover its
+        box), so the grid path tests exactly the elements, in the same order,
+        that the full scan (scan=True) tests, and picks the same element."""
+        self._index()
         lo, hi = self._lo, self._hi
         pts = np.asarray(pts, dtype=np.float64).reshape(-1, 2)
         el = np.full(len(pts), -1)
         ref = np.zeros((len(pts), 2))
-        k = min(k_near, len(lo))
-        near = self._tree.query(pts, k=k)[1].reshape(len(pts), -1) if self._tree is not None else None
         for i, x in enumerate(pts):
-            found = False
-            if near is not None:
-                cand = np.sort(near[i][np.all((x >= lo[near[i]]) & (x <= hi[near[i]]), 1)])
-                for e in cand:
-                    s = self._inside(e, x, tol)
-                    if s is not None:
-                        el[i], ref[i], found = e, s, True
-                        break
-            if not found:
-                for e in np.nonzero(np.all((x >= lo) & (x <= hi), 1))[0]:
-                    s = self._inside(e, x, tol)
-                    if s is not None:
-                        el[i], ref[i] = e, s
-                        break
+            cand = np.nonzero(np.all((x >= lo) & (x <= hi), 1))[0] if scan else self._candidates(x)
+            for e in cand:
+                s = self._inside(e, x, tol)
+                if s is not None:
+                    el[i], ref[i] = e, s
+                    break
         return el, ref
 
     def evaluate(self, pts):

@@ -233,3 +233,61 @@ def dot(a, b):
     a = np.ascontiguousarray(a, dtype=np.float64)
     b = np.ascontiguousarray(b, dtype=np.float64)
     return lib().orc_dot(a.size // 2, ptr(a), ptr(b))
+
+
+class OracleNewton:
+    """Resumable form of orc_solve_steps (plain Newton, full tangent), cut into
+    Newton iterations exactly as the library's ipfem_newton_advance cuts them:
+    an iteration is CG on the current tangent, u += du, Assemble(K, rhs) and
+    the convergence test; a load step that converges (or reaches
+    newton_max_it) is accepted inside the iteration that ends it (state
+    commit, main.cpp:487-522), and the next step's first assembly opens the
+    following iteration (main.cpp:160-262).  Same calls in the same order as
+    orc_solve_steps, so the iterates are identical."""
+
+    def __init__(self, prob, n_steps, step_begin=0, step_end=None, newton_rtol=1e-8, newton_max_it=20,
+                 cg_rtol=1e-8, cg_max_it=200000):
+        self.p = prob
+        self.n_steps = int(n_steps)
+        self.step = int(step_begin)
+        self.step_end = self.n_steps if step_end is None else int(step_end)
+        self.newton_rtol, self.newton_max_it = float(newton_rtol), int(newton_max_it)
+        self.cg_rtol, self.cg_max_it = float(cg_rtol), int(cg_max_it)
+        self.open = False
+        self.R = None
+        self.r0 = self.rn = 0.0
+        self.it = 0
+        self.all_converged = True
+
+    def _lam(self):
+        return (self.step + 1) / self.n_steps
+
+    def advance(self, u, n_iters=0):
+        """n_iters Newton iterations on u (in place; 0 = to the end of the last
+        step); returns (iterations, CG iterations) performed"""
+        done, cg = 0, 0
+        n_iters = n_iters or (1 << 30)
+        while done < n_iters and self.step < self.step_end:
+            lam = self._lam()
+            if not self.open:
+                self.R = self.p.assemble(u, lam)
+                self.r0 = self.rn = float(np.sqrt(dot(self.R, self.R)))
+                self.it = 0
+                self.open = True
+            conv = self.r0 == 0.0
+            if not conv:
+                du, k = self.p.pcg(self.R, rtol=self.cg_rtol, max_it=self.cg_max_it)
+                cg += abs(k)
+                u += du
+                self.it += 1
+                done += 1
+                self.R = self.p.assemble(u, lam)
+                self.rn = float(np.sqrt(dot(self.R, self.R)))
+                conv = self.rn <= self.newton_rtol * self.r0
+            if conv or self.it >= self.newton_max_it:
+                if not conv:
+                    self.all_converged = False
+                self.p.assemble_residual(u, lam, update_mem=True)
+                self.step += 1
+                self.open = False
+        return done, cg

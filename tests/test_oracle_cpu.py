@@ -165,3 +165,26 @@ def test_block_jacobi_preconditioner():
     x1, k1 = P.pcg(R)
     assert 0 < k1 < 0.85 * k0, (k1, k0)
     assert np.abs(x1 - x0).max() < 1e-6 * np.abs(x0).max()
+
+
+def test_resumable_newton_equals_solve_steps():
+    """OracleNewton (the reference arm's timed Newton iterations) cut into
+    chunks of 3 iterations gives the iterates, counts and committed state of
+    orc_solve_steps bit for bit"""
+    n, steps = 10, 6
+    P1 = po.OracleProblem(po.default_params(n), nthreads=2)
+    P2 = po.OracleProblem(po.default_params(n), nthreads=2)
+    for P in (P1, P2):
+        P.set_block_jacobi(True)
+    u1, u2 = np.zeros(P1.neq), np.zeros(P2.neq)
+    st, _ = P1.solve_steps(u1, steps, newton_max_it=40)
+    N = po.OracleNewton(P2, steps, newton_max_it=40)
+    its = cgs = 0
+    while N.step < steps:
+        d, c = N.advance(u2, 3)
+        its += d
+        cgs += c
+    assert its == st.newton_iters and cgs == st.cg_iters
+    assert np.array_equal(u1, u2)
+    for f in ("eps_p", "sigma", "mtype", "alpha"):
+        assert np.array_equal(P1.arr(f), P2.arr(f)), f

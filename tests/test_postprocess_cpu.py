@@ -105,3 +105,33 @@ def test_mixed_mesh_probe_and_vtk(tmp_path, order):
     k = lines.index("CELL_TYPES %d" % pb.n_el)
     types = np.array(lines[k + 1:k + 1 + pb.n_el], dtype=int)
     assert (types == {1: 5, 2: 22, 3: 69}[order]).sum() == pb.array("el_shape").sum()
+
+
+@pytest.mark.parametrize("tri", [(), (1, 3)])
+@pytest.mark.parametrize("order", [1, 2])
+def test_locate_grid_equals_full_scan(tmp_path, tri, order):
+    """point location through the grid of element boxes picks the same element
+    as the full scan over all elements, also for points exactly on element
+    vertices and edges (several elements contain them: the lowest-numbered
+    one is taken), on a graded quadrilateral mesh and on a mixed
+    triangle/quadrilateral mesh, plus random points inside and outside"""
+    path = str(tmp_path / "m.msh")
+    gw.write_wellbore_msh(path, 9, 1.3, tri_quadrants=tri)
+    bcs, mat = gw.reference_bcs()
+    pb = ip.GmshProblem(ip.GmshMesh(path), bcs, order=order, **mat)
+    n_ip = pb.array("weight").size
+    z4 = np.zeros((4, n_ip))
+    S = pp.Solution(pb, np.zeros(pb.neq), z4, z4, np.zeros(n_ip))
+    S._index()
+    V = S._V
+    rng = np.random.default_rng(3)
+    verts = V.reshape(-1, 2)
+    mids = 0.5 * (V + np.roll(V, -1, axis=1)).reshape(-1, 2)               # edge midpoints
+    lo, hi = verts.min(0), verts.max(0)
+    rnd = lo + (hi - lo) * rng.random((400, 2))                            # the hole and beyond: some outside
+    pts = np.concatenate([verts[rng.choice(len(verts), 300)], mids[rng.choice(len(mids), 300)], rnd])
+    e_grid, r_grid = S.locate(pts)
+    e_scan, r_scan = S.locate(pts, scan=True)
+    assert np.array_equal(e_grid, e_scan)
+    assert np.array_equal(r_grid, r_scan)
+    assert (e_grid >= 0).sum() > 600 and (e_grid < 0).any()
