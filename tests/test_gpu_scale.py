@@ -1,0 +1,252 @@
+"""GPU parity at the configuration sizes the measurements are quoted on.
+
+Configuration 2 (400 x 400, 1.44 M points, 1 283 202 dofs), configuration 3
+(1000 x 1000, per-element cohesion lognormal with cv 0.2) and configuration 5
+(2000 x 2000, friction angle per element uniform in [25, 35] degrees,
+cohesion lognormal with cv 0.3: 256 M nodal blocks, 8.2 GB of FP64 tangent,
+index ranges past 2^30 values) against the CPU oracle, through the C-ABI.
+The plain FP64 method follows the oracle's operation order, so every
+comparison is exact (==).  The displacement is a wellbore-like field (radial
+inward displacement A / r, plastic near the well) plus small seeded noise.
+
+The last tests state the errors of the chosen method (mixed precision +
+learned preconditioner) and of mixed precision with block Jacobi against the
+plain FP64 GPU solve, which is itself bit-exact with the oracle: over the
+whole 20-step configuration-2 solve and over the first load steps of
+configuration 3.  Tolerance: 1e-6 relative (max norm) on u, sigma and the
+plastic strain.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+ip = pytest.importorskip("intpointsfem_gb300")
+from oracle import pyoracle as po  # noqa: E402
+
+CFG3 = dict(material_mode=1, c_cv=0.2)
+CFG5 = dict(material_mode=2, c_cv=0.3, phi_lo_deg=25.0, phi_hi_deg=35.0, pw_final=-5.0)
+
+
+def _soa4(p6, n_ip):
+    p = p6.reshape(n_ip, 6)
+    return np.ascontiguousarray(np.stack([p[:, 0], p[:, 1], p[:, 3], p[:, 5]]).ravel())
+
+
+def _eq(a, b):
+    return np.array_equal(np.asarray(a), np.asarray(b), equal_nan=True)
+
+
+def _wellbore_u(w, fixed, amp=5e-5, noise=1e-7, seed=0):
+    """radial inward displacement amp / r (strains ~amp / r^2: plastic for
+    r below about 0.2 m) plus seeded noise; zero on the Dirichlet dofs"""
+    xy = np.asarray(w.array("node_xy")).reshape(-1, 2)
+    r2 = (xy ** 2).sum(1)
+    u = (-amp * xy / r2[:, None]).ravel()
+    u += np.random.default_rng(seed).normal(size=u.size) * noise
+    u[fixed] = 0.0
+    return u
+
+
+def _state_equal(sm, P):
+    mt = sm.get_state(3)
+    assert np.array_equal(mt, P.arr("mtype").astype(np.float64))
+    assert _eq(sm.get_state(0), _soa4(P.arr("eps_p"), P.n_ip))
+    assert _eq(sm.get_state(1), _soa4(P.arr("sigma"), P.n_ip))
+    assert _eq(sm.get_state(2), P.arr("alpha"))
+    return int((mt != 0).sum())
+
+
+def _need_memory(host_gb, device_gb):
+    """skip (do not fail) where the machine cannot hold the case: the oracle
+    and the host copies at 2000 x 2000 take about 60 GB of host memory"""
+    avail = 0.0
+    with open("/proc/meminfo") as f:
+        for line in f:
+            if line.startswith("MemAvailable:"):
+                avail = int(line.split()[1]) / 1e6
+    if avail < host_gb:
+        pytest.skip("needs %.0f GB of free host memory, %.0f GB available" % (host_gb, avail))
+    import torch
+    free, _ = torch.cuda.mem_get_info()
+    if free / 1e9 < device_gb:
+        pytest.skip("needs %.0f GB of free device memory, %.0f GB free" % (device_gb, free / 1e9))
+
+
+def _rel(a, b):
+    return float(np.abs(a - b).max() / np.abs(b).max())
+
+
+@pytest.fixture(scope="module")
+def cfg2():
+    w = ip.WellboreMesh(ip.wellbore_params(400))
+    P = po.OracleProblem(po.default_params(400), nthreads=0)
+    P.set_block_jacobi(True)
+    yield w, P
+    P.close()
+
+
+def test_cfg2_residual_commit_tangent_cg_bit_exact(cfg2):
+    """400 x 400: residual with state commit, the tangent (block pattern and
+    values), and 300 iterations of block-Jacobi CG: every value equal"""
+    w, P = cfg2
+    sm = ip.ElastoPlasticIntPointsStructMatrix(w)
+    sm.set_preconditioner(ip.PREC_BLOCK_JACOBI)
+    assert sm.n_colors == P.n_colors == 4
+    assert np.array_equal(sm.get_setup(0), P.arr("el_color"))
+    fixed = P.arr("fixed").astype(bool)
+    u = _wellbore_u(w, fixed)
+    lam = 0.75
+    sm.SetLoadFactor(lam)
+    r = sm.assemble_residual(u, np.zeros(sm.neq))
+    ro = P.assemble_residual(u.copy(), lam)
+    assert _eq(r, ro), np.abs(r - ro).max()
+    sm.SetUpdateMem(True)
+    sm.assemble_residual(u, np.zeros(sm.neq))
+    sm.SetUpdateMem(False)
+    P.assemble_residual(u.copy(), lam, update_mem=True)
+    n_pl = _state_equal(sm, P)
+    assert n_pl > 1000, n_pl
+    # tangent at the same u (from the committed state)
+    r = sm.assemble(u, np.zeros(sm.neq))
+    ro = P.assemble(u.copy(), lam)
+    assert _eq(r, ro)
+    rp, col, K = sm.stiffness()
+    assert np.array_equal(rp, P.arr("row_ptr")) and np.array_equal(col, P.arr("col"))
+    assert _eq(K, P.arr("K"))
+    del K
+    x, it = sm.solve(r, rtol=1e-12, max_it=300, allow_nonconverged=True)
+    xo, ito = P.pcg(ro, rtol=1e-12, max_it=300)
+    assert it == abs(ito) == 300
+    assert _eq(x, xo)
+    print("400x400: %d plastic points, residual/tangent/300 CG iterations bit-exact" % n_pl)
+    sm.close()
+
+
+def test_cfg2_first_load_step_newton_bit_exact(cfg2):
+    """400 x 400: the first load step of the 20-step solve (Newton with
+    block-Jacobi CG to 1e-8), iterates, logs, CG counts and committed state"""
+    w, _ = cfg2
+    P = po.OracleProblem(po.default_params(400), nthreads=0)
+    P.set_block_jacobi(True)
+    sm = ip.ElastoPlasticIntPointsStructMatrix(w)
+    sm.set_preconditioner(ip.PREC_BLOCK_JACOBI)
+    ug, uo = np.zeros(sm.neq), np.zeros(sm.neq)
+    sg, lg = sm.newton(ug, 20, 0, 1, newton_max_it=40)
+    so, lo = P.solve_steps(uo, 20, 0, 1, newton_max_it=40)
+    assert sg.converged and so.converged
+    assert sg.newton_iters == so.newton_iters and sg.cg_iters == so.cg_iters
+    assert _eq(lg, lo) and _eq(ug, uo)
+    _state_equal(sm, P)
+    print("400x400 load step 1: %d Newton / %d CG iterations, bit-exact" % (sg.newton_iters, sg.cg_iters))
+    sm.close()
+    P.close()
+
+
+def test_cfg3_residual_and_commit_bit_exact():
+    """1000 x 1000 with per-element lognormal cohesion (cv 0.2): residual and
+    the committed state (sigma, plastic strain, m_type, alpha)"""
+    _need_memory(40, 16)
+    w = ip.WellboreMesh(ip.wellbore_params(1000, **CFG3))
+    P = po.OracleProblem(po.default_params(1000, **CFG3), nthreads=0)
+    sm = ip.ElastoPlasticIntPointsStructMatrix(w)
+    assert np.array_equal(w.array("el_cohesion"), P.mats()[:, 0])
+    fixed = P.arr("fixed").astype(bool)
+    u = _wellbore_u(w, fixed, seed=1)
+    lam = 0.5
+    sm.SetLoadFactor(lam)
+    sm.SetUpdateMem(True)
+    r = sm.assemble_residual(u, np.zeros(sm.neq))
+    sm.SetUpdateMem(False)
+    ro = P.assemble_residual(u.copy(), lam, update_mem=True)
+    assert _eq(r, ro), np.abs(r - ro).max()
+    n_pl = _state_equal(sm, P)
+    assert n_pl > 1000
+    # a second evaluation from the committed state
+    u2 = u * 1.01
+    r = sm.assemble_residual(u2, np.zeros(sm.neq))
+    ro = P.assemble_residual(u2.copy(), lam)
+    assert _eq(r, ro)
+    print("1000x1000 lognormal cohesion: %d plastic points, residual and commit bit-exact" % n_pl)
+    sm.close()
+    P.close()
+
+
+def test_cfg5_residual_and_tangent_bit_exact():
+    """2000 x 2000 with per-element friction angle and cohesion: residual and
+    the 8.2 GB FP64 tangent (1.02 G values, byte offsets past 2^32), compared
+    block by block"""
+    _need_memory(120, 48)
+    w = ip.WellboreMesh(ip.wellbore_params(2000, **CFG5))
+    P = po.OracleProblem(po.default_params(2000, **CFG5), nthreads=0)
+    sm = ip.ElastoPlasticIntPointsStructMatrix(w)
+    assert sm.n_blocks == P.n_blocks == (8 * 2000 + 1) ** 2
+    fixed = P.arr("fixed").astype(bool)
+    u = _wellbore_u(w, fixed, seed=2)
+    lam = 1.0
+    sm.SetLoadFactor(lam)
+    r = sm.assemble(u, np.zeros(sm.neq))
+    ro = P.assemble(u.copy(), lam)
+    assert _eq(r, ro), np.abs(r - ro).max()
+    rp, col, K = sm.stiffness()
+    assert np.array_equal(rp, P.arr("row_ptr"))
+    assert np.array_equal(col, P.arr("col"))
+    del rp, col
+    Ko = P.arr("K")
+    step = 1 << 26
+    for i in range(0, K.size, step):
+        assert _eq(K[i:i + step], Ko[i:i + step]), i
+    print("2000x2000 heterogeneous: residual and %d tangent values bit-exact" % K.size)
+    sm.close()
+    P.close()
+
+
+def _solve(w, n, mode, n_steps, step_end, learned=False):
+    sm = ip.ElastoPlasticIntPointsStructMatrix(w)
+    if mode == "plain":
+        sm.set_preconditioner(ip.PREC_BLOCK_JACOBI)
+        rtol = 1e-8
+    else:
+        sm.set_precision(ip.MIXED)
+        rtol = 1e-4
+        if learned:
+            from intpointsfem_gb300 import train_preconditioner as tp
+            sm.set_node_grid(2 * n + 1, 2 * n + 1)
+            sm.mlp_init(0)
+            sm.set_mlp_params(tp.load_weights())
+            sm.set_preconditioner(ip.PREC_MLP)
+        else:
+            sm.set_preconditioner(ip.PREC_BLOCK_JACOBI)
+    u = np.zeros(sm.neq)
+    st, _ = sm.newton(u, n_steps, 0, step_end, newton_max_it=40, cg_rtol=rtol)
+    out = {"u": u, "sigma": sm.get_state(1), "eps_p": sm.get_state(0), "mtype": sm.get_state(3),
+           "newton": st.newton_iters, "cg": st.cg_iters, "converged": st.converged,
+           "fallbacks": st.fcg_fallbacks}
+    sm.close()
+    return out
+
+
+def _errors(a, ref):
+    return {"u": _rel(a["u"], ref["u"]), "sigma": _rel(a["sigma"], ref["sigma"]),
+            "eps_p": _rel(a["eps_p"], ref["eps_p"]), "flips": int((a["mtype"] != ref["mtype"]).sum()),
+            "plastic": int((ref["mtype"] != 0).sum())}
+
+
+@pytest.mark.parametrize("n,cfg,n_steps,step_end", [(400, {}, 20, 20), (1000, CFG3, 20, 2)],
+                         ids=["cfg2-full-solve", "cfg3-first-2-steps"])
+def test_chosen_and_mixed_against_plain_fp64(n, cfg, n_steps, step_end):
+    """errors of the mixed methods against the plain FP64 solve (bit-exact
+    with the oracle by the tests above) after the same load steps"""
+    w = ip.WellboreMesh(ip.wellbore_params(n, **cfg))
+    ref = _solve(w, n, "plain", n_steps, step_end)
+    assert ref["converged"]
+    for name, learned in (("mixed + learned", True), ("mixed + block Jacobi", False)):
+        a = _solve(w, n, "mixed", n_steps, step_end, learned)
+        e = _errors(a, ref)
+        print("%dx%d steps 1-%d %-21s u %.2e sigma %.2e eps_p %.2e flips %d of %d plastic; Newton %d (plain %d), "
+              "CG %d (plain %d), fallbacks %d"
+              % (n, n, step_end, name, e["u"], e["sigma"], e["eps_p"], e["flips"], e["plastic"], a["newton"],
+                 ref["newton"], a["cg"], ref["cg"], a["fallbacks"]))
+        assert a["converged"]
+        assert e["u"] < 1e-6 and e["sigma"] < 1e-6 and e["eps_p"] < 1e-6, e
+        assert e["flips"] <= max(2, e["plastic"] // 100000)
