@@ -130,6 +130,18 @@ ipfem_status ipfem_assemble(ipfem_ctx *ctx, const double *u, double *rhs, int wh
  * row_ptr[n_nodes+1], col[n_blocks], vals[4*n_blocks] (row-major blocks);
  * in IPFEM_MIXED mode the FP32 tangent, widened to double. */
 ipfem_status ipfem_get_stiffness(ipfem_ctx *ctx, int64_t *row_ptr, int32_t *col, double *vals);
+/* K in the reference's matrix form: the upper triangle (column >= row) of
+ * the scalar dof matrix in CSR, rows ascending, columns ascending per row,
+ * 0-based, int64 indices -- TPZSYsmpMatrix's IA, JA and A, the positions the
+ * reference's colour-ordered assembly writes (TPZNumericalIntegrator.cpp:
+ * 538-606, FillLIndexes / me), which Assemble(K, rhs) copies back
+ * (TPZElastoPlasticIntPointsStructMatrix.cpp:122).  With ia, ja and a all
+ * NULL, *nnz receives the number of entries; otherwise *nnz gives the
+ * capacity of ja and a (ia holds 2*n_nodes+1) and receives the count; with a
+ * NULL only the pattern (ia, ja) is written, which needs no assembled
+ * tangent.  Dirichlet rows and columns are stored as assembled (the solves
+ * mask them). */
+ipfem_status ipfem_get_stiffness_sym_csr(ipfem_ctx *ctx, int64_t *nnz, int64_t *ia, int64_t *ja, double *a);
 /* Jacobi-preconditioned CG on the current K (replaces the reference's
  * TPZCudaCalls::SolveCG, TPZCudaCalls.cu:213-290, and the Pardiso solve):
  * stops when |r|^2 <= rtol^2 |b|^2.  *iters receives the iteration count. */

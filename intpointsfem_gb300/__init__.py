@@ -108,6 +108,7 @@ def lib():
             "ipfem_assemble_residual": (S, [P, P, P, S]),
             "ipfem_assemble": (S, [P, P, P, S]),
             "ipfem_get_stiffness": (S, [P, _lp, _ip, _dp]),
+            "ipfem_get_stiffness_sym_csr": (S, [P, _lp, _lp, _lp, _dp]),
             "ipfem_solve": (S, [P, P, P, C.c_double, S, S, C.POINTER(C.c_int)]),
             "ipfem_newton_solve": (S, [P, C.POINTER(SolveOpts), C.c_int32, C.c_int32, P, S,
                                        C.POINTER(SolveStats), _dp, C.c_int32]),
@@ -429,6 +430,17 @@ class ElastoPlasticIntPointsStructMatrix:
         val = np.zeros(4 * self.n_blocks)
         self._check(lib().ipfem_get_stiffness(self._ctx, _np_ptr(rp, _lp), _np_ptr(col, _ip), _np_ptr(val, _dp)))
         return rp, col, val
+
+    def stiffness_sym_csr(self):
+        """K as TPZSYsmpMatrix stores it: upper-triangle CSR (IA, JA, A) over dofs"""
+        nnz = np.zeros(1, np.int64)
+        self._check(lib().ipfem_get_stiffness_sym_csr(self._ctx, _np_ptr(nnz, _lp), None, None, None))
+        ia = np.zeros(self.neq + 1, np.int64)
+        ja = np.zeros(int(nnz[0]), np.int64)
+        a = np.zeros(int(nnz[0]))
+        self._check(lib().ipfem_get_stiffness_sym_csr(self._ctx, _np_ptr(nnz, _lp), _np_ptr(ia, _lp),
+                                                       _np_ptr(ja, _lp), _np_ptr(a, _dp)))
+        return ia, ja, a
 
     def solve(self, b, x=None, rtol=1e-8, max_it=200000, where=HOST, allow_nonconverged=False):
         if x is None:

@@ -440,7 +440,8 @@ ipfem_status ipfem_sizes(const ipfem_ctx *c, int64_t out[6])
 
 ipfem_status ipfem_set_load_factor(ipfem_ctx *c, double lambda)
 {
-    if (!c || !std::isfinite(lambda)) return IPFEM_INVALID;
+    if (!c) return IPFEM_INVALID;
+    if (!std::isfinite(lambda)) return fail(c, IPFEM_INVALID, "load factor is not finite");
     c->load_factor = lambda;
     return IPFEM_OK;
 }
@@ -577,6 +578,53 @@ ipfem_status ipfem_get_stiffness(ipfem_ctx *c, int64_t *row_ptr, int32_t *col, d
         for (int64_t k = 0; k < s.n_blocks; k++)
             std::memcpy(vals + 4 * k, h.data() + 4 * s.sell.bsr_to_sell[k], 4 * sizeof(double));
     }
+    return IPFEM_OK;
+}
+
+ipfem_status ipfem_get_stiffness_sym_csr(ipfem_ctx *c, int64_t *nnz, int64_t *ia, int64_t *ja, double *a)
+{
+    if (!c || !nnz) return fail(c, IPFEM_INVALID, "bad args");
+    const Setup &s = c->s;
+    // entries of the upper triangle: 4 per off-diagonal block (j > i) of a
+    // block row, 3 per diagonal block ((2i, 2i), (2i, 2i+1), (2i+1, 2i+1))
+    int64_t n_up = 0;
+    for (int32_t i = 0; i < s.n_nodes; i++)
+        for (int64_t k = s.row_ptr[i]; k < s.row_ptr[i + 1]; k++) n_up += s.col[k] > i ? 4 : (s.col[k] == i ? 3 : 0);
+    if (!ia && !ja && !a) {
+        *nnz = n_up;
+        return IPFEM_OK;
+    }
+    if (*nnz < n_up) return fail(c, IPFEM_INVALID, "ipfem_get_stiffness_sym_csr: arrays hold fewer than nnz entries");
+    if (!ia || !ja) return fail(c, IPFEM_INVALID, "ipfem_get_stiffness_sym_csr: ia and ja are needed");
+    std::vector<double> v;
+    if (a) {
+        if (!c->tangent_valid) return fail(c, IPFEM_INVALID, "no tangent assembled");
+        v.resize((size_t)s.n_blocks * 4);
+        ipfem_status st = ipfem_get_stiffness(c, nullptr, nullptr, v.data());
+        if (st != IPFEM_OK) return st;
+    }
+    // dof row 2i+p holds, for the blocks (i, j >= i) in ascending j, the
+    // columns 2j and 2j+1 at or right of the diagonal: columns ascend
+    int64_t e = 0;
+    ia[0] = 0;
+    for (int32_t i = 0; i < s.n_nodes; i++) {
+        for (int p = 0; p < 2; p++) {
+            const int64_t row = 2 * (int64_t)i + p;
+            for (int64_t k = s.row_ptr[i]; k < s.row_ptr[i + 1]; k++) {
+                const int32_t j = s.col[k];
+                if (j < i) continue;
+                for (int q = 0; q < 2; q++) {
+                    const int64_t col = 2 * (int64_t)j + q;
+                    if (col < row) continue;
+                    ja[e] = col;
+                    if (a) a[e] = v[4 * k + 2 * p + q];
+                    e++;
+                }
+            }
+            ia[row + 1] = e;
+        }
+    }
+    *nnz = e;
     return IPFEM_OK;
 }
 

@@ -122,3 +122,24 @@ def test_dot_noalloc_rejects_bad_arguments_before_any_device_call():
         st = L.ipfem_dot_noalloc(C.c_void_p(pa), C.c_void_p(pb), n, C.c_void_p(po_), None)
         assert st == 5, (pa, pb, n, po_)
         assert msg in L.ipfem_last_error(None), L.ipfem_last_error(None)
+
+
+def test_struct_matrix_class_compiles_links_and_throws_without_device(tmp_path):
+    """the C++ class of include/ipfem_pz.hpp compiles with g++ -Wall -Werror,
+    links against libipfem.so, refuses a bad element order, and (without a
+    GPU) throws std::runtime_error from its constructor with the library's
+    message, as the reference's struct matrix throws on CUDA failures"""
+    import subprocess
+
+    try:
+        import torch
+        if torch.cuda.is_available():
+            pytest.skip("a GPU is present (the GPU test drives the class)")
+    except ImportError:
+        pass
+    from struct_matrix_build import build_driver
+
+    exe = build_driver(tmp_path)
+    r = subprocess.run([exe, "6", "0.5", str(tmp_path)], capture_output=True, text=True)
+    assert r.returncode == 3, (r.stdout, r.stderr)
+    assert "runtime_error: ipfem: no sm_103 device" in r.stdout, r.stdout
