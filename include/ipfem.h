@@ -331,6 +331,15 @@ ipfem_status ipfem_cg_snapshots(ipfem_ctx *ctx, const double *d_b, double rtol, 
                                 const int32_t *snap_iters, float *d_xs, float *d_rs, float *d_xfinal, int *iters);
 
 /* ------------------------------------------------------------ diagnostics */
+/* JSON-lines record of the Newton iterations of ipfem_newton_solve /
+ * ipfem_newton_advance, appended to the file at `path` (NULL or "" closes
+ * it): per iteration {"step", "iter", "cg_iters", "res" (|R|), "res_rel"
+ * (|R| / |R0| of the load step), "ms_solve", "ms_assemble", "ips_assemble"
+ * (integration points per second of the iteration's assembly),
+ * "fcg_fallback"}, and per accepted load step {"step", "accepted",
+ * "newton_iters", "converged", "res_rel", "ms_commit", "ms_step_total"}.
+ * The reference prints its residual norms to stdout (main.cpp:239-252). */
+ipfem_status ipfem_set_iteration_log(ipfem_ctx *ctx, const char *path);
 /* number of kernels this context has launched (graph nodes included) */
 uint64_t ipfem_launch_count(const ipfem_ctx *ctx);
 /* average duration of the CG block SpMV on the current tangent, timed with

@@ -119,6 +119,7 @@ def lib():
             "ipfem_dot": (S, [P, P, P, _dp]),
             "ipfem_dot_noalloc": (S, [P, P, C.c_int64, P, P]),
             "ipfem_launch_count": (C.c_uint64, [P]),
+            "ipfem_set_iteration_log": (S, [P, C.c_char_p]),
             "ipfem_profile_spmv": (S, [P, S, _dp]),
             "ipfem_measure_fp64_peak": (S, [P, _dp]),
             "ipfem_set_node_grid": (S, [P, C.c_int32, C.c_int32]),
@@ -483,6 +484,11 @@ class ElastoPlasticIntPointsStructMatrix:
         out = np.zeros(1)
         self._check(lib().ipfem_dot(self._ctx, _ptr(d_a), _ptr(d_b), _np_ptr(out, _dp)))
         return float(out[0])
+
+    def set_iteration_log(self, path):
+        """append a JSON-lines record per Newton iteration and per accepted
+        load step to `path` (None closes the log)"""
+        self._check(lib().ipfem_set_iteration_log(self._ctx, os.fsencode(path) if path else None))
 
     @property
     def launch_count(self):

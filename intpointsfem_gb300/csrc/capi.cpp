@@ -2,12 +2,24 @@
 // calls (Assemble(rhs), Assemble(K, rhs)), the CG solve, the Newton driver of
 // main.cpp, and the kernel-level replacements of TPZCudaCalls.
 #include <cmath>
+#include <cstdio>
 #include <cstring>
 #include <new>
+
+#include <nvtx3/nvToolsExt.h>
 
 #include "ipfem_internal.h"
 
 using namespace ipfem;
+
+// NVTX range around a phase of the path (assemble, solve, commit): visible
+// in Nsight timelines, free when no tool is attached
+struct Range {
+    explicit Range(const char *name) { nvtxRangePushA(name); }
+    ~Range() { nvtxRangePop(); }
+    Range(const Range &) = delete;
+    Range &operator=(const Range &) = delete;
+};
 
 namespace {
 
@@ -108,6 +120,7 @@ void free_all(ipfem_ctx *c)
         cudaEventDestroy(c->ev[1]);
     }
     if (c->stream) cudaStreamDestroy(c->stream);
+    if (c->iter_log) std::fclose(c->iter_log);
 }
 
 }  // namespace
@@ -679,7 +692,9 @@ static ipfem_status newton_advance(ipfem_ctx *c, int32_t n_iters, double *du, ip
     };
     int32_t done = 0;
     while (done < n_iters && ns.step < ns.step_end) {
+        const double ma0 = st->ms_assemble, ms0 = st->ms_solve, mc0 = st->ms_commit;
         if (!ns.open) {
+            Range rg("ipfem:newton:first_assembly");
             c->load_factor = (double)(ns.step + 1) / (double)o.n_steps;
             cudaEventRecord(ev[0], c->stream);
             newton_assemble(c, du);
@@ -699,8 +714,13 @@ static ipfem_status newton_advance(ipfem_ctx *c, int32_t n_iters, double *du, ip
         if (!conv) {
             int k = 0;
             const int64_t fb0 = c->fcg_fallbacks;
+            Range rg("ipfem:newton:iteration");
             cudaEventRecord(ev[0], c->stream);
-            ipfem_status e = solve_device(c, c->d_rhs, o.cg_rtol, o.cg_max_it, &k, du, c->newton_accel ? 0 : 1);
+            ipfem_status e;
+            {
+                Range rs("ipfem:solve");
+                e = solve_device(c, c->d_rhs, o.cg_rtol, o.cg_max_it, &k, du, c->newton_accel ? 0 : 1);
+            }
             st->fcg_fallbacks += c->fcg_fallbacks - fb0;
             cudaEventRecord(ev[1], c->stream);
             st->ms_solve += elapsed();
@@ -736,6 +756,7 @@ static ipfem_status newton_advance(ipfem_ctx *c, int32_t n_iters, double *du, ip
             ns.it++;
             done++;
             st->newton_iters++;
+            Range ra("ipfem:assemble");
             cudaEventRecord(ev[0], c->stream);
             newton_assemble(c, du);
             cudaEventRecord(ev[1], c->stream);
@@ -752,17 +773,40 @@ static ipfem_status newton_advance(ipfem_ctx *c, int32_t n_iters, double *du, ip
                 (*nlog)++;
             }
             conv = ns.rn <= o.newton_rtol * ns.r0;
+            if (c->iter_log) {
+                const double ma = st->ms_assemble - ma0, ms = st->ms_solve - ms0;
+                std::fprintf(c->iter_log,
+                             "{\"step\": %d, \"iter\": %d, \"cg_iters\": %d, \"res\": %.17g, \"res_rel\": %.17g, "
+                             "\"ms_solve\": %.6f, \"ms_assemble\": %.6f, \"ips_assemble\": %.6g, "
+                             "\"fcg_fallback\": %d}\n",
+                             ns.step, ns.it, k, ns.rn, ns.r0 > 0.0 ? ns.rn / ns.r0 : 0.0, ms, ma,
+                             ma > 0.0 ? (double)c->s.n_ip / (1e-3 * ma) : 0.0,
+                             (int)(c->fcg_fallbacks - fb0));
+                std::fflush(c->iter_log);
+            }
         }
         if (conv || ns.it >= o.newton_max_it) {
             st->last_step_iters = ns.it;
             st->final_res = ns.r0 > 0.0 ? ns.rn / ns.r0 : 0.0;
             if (!conv) ns.all_converged = 0;
-            cudaEventRecord(ev[0], c->stream);
-            residual_device(c, du, c->d_b, 1);
-            cudaEventRecord(ev[1], c->stream);
-            st->ms_commit += elapsed();
+            {
+                Range rc("ipfem:commit");
+                cudaEventRecord(ev[0], c->stream);
+                residual_device(c, du, c->d_b, 1);
+                cudaEventRecord(ev[1], c->stream);
+                st->ms_commit += elapsed();
+            }
             ipfem_status e = sync_check(c);
             if (e != IPFEM_OK) return e;
+            if (c->iter_log) {
+                std::fprintf(c->iter_log,
+                             "{\"step\": %d, \"accepted\": true, \"newton_iters\": %d, \"converged\": %s, "
+                             "\"res_rel\": %.17g, \"ms_commit\": %.6f, \"ms_step_total\": %.6f}\n",
+                             ns.step, ns.it, conv ? "true" : "false", ns.r0 > 0.0 ? ns.rn / ns.r0 : 0.0,
+                             st->ms_commit - mc0,
+                             (st->ms_assemble - ma0) + (st->ms_solve - ms0) + (st->ms_commit - mc0));
+                std::fflush(c->iter_log);
+            }
             ns.step++;
             ns.open = 0;
         }
@@ -830,6 +874,19 @@ ipfem_status ipfem_newton_solve(ipfem_ctx *c, const ipfem_solve_opts *o, int32_t
 uint64_t ipfem_launch_count(const ipfem_ctx *c)
 {
     return c ? c->launches : 0;
+}
+
+ipfem_status ipfem_set_iteration_log(ipfem_ctx *c, const char *path)
+{
+    if (!c) return IPFEM_INVALID;
+    if (c->iter_log) {
+        std::fclose(c->iter_log);
+        c->iter_log = nullptr;
+    }
+    if (!path || !*path) return IPFEM_OK;
+    c->iter_log = std::fopen(path, "a");
+    if (!c->iter_log) return fail(c, IPFEM_INVALID, std::string("cannot open the iteration log ") + path);
+    return IPFEM_OK;
 }
 
 ipfem_status ipfem_dot(ipfem_ctx *c, const double *d_a, const double *d_b, double *out)

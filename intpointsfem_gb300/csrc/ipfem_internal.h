@@ -4,6 +4,7 @@
 
 #include <cuda_runtime.h>
 #include <stdint.h>
+#include <stdio.h>
 
 #include <string>
 #include <vector>
@@ -239,6 +240,7 @@ struct ipfem_ctx {
     ipfem::MlpBuffers mlp;
     cudaGraphExec_t fcg_exec = nullptr;
     int64_t fcg_fallbacks = 0;
+    FILE *iter_log = nullptr;            // JSON-lines record of the Newton iterations (ipfem_set_iteration_log)
 };
 
 // ---- kernel launchers (implemented in the .cu files) ----

@@ -141,3 +141,27 @@ def test_device_pointer_kernels_match_oracle():
     scat = np.zeros(P.neq)
     po.lib().orc_scatter_residual(P._p, po.ptr(P.arr("sigma_w")), po.ptr(scat))
     assert _eq(res.cpu().numpy(), scat)
+
+
+def test_iteration_log_records_every_newton_iteration(tmp_path):
+    """ipfem_set_iteration_log: one JSON line per Newton iteration (its CG
+    count and |R| equal the solve's own log) and one per accepted load step"""
+    import json
+
+    sm, _ = (ip.ElastoPlasticIntPointsStructMatrix(ip.WellboreMesh(ip.wellbore_params(8))), None)
+    path = str(tmp_path / "newton.jsonl")
+    sm.set_iteration_log(path)
+    u = np.zeros(sm.neq)
+    st, log = sm.newton(u, 10, 0, 3, newton_max_it=30)
+    sm.set_iteration_log(None)
+    recs = [json.loads(line) for line in open(path)]
+    its = [r for r in recs if "iter" in r]
+    acc = [r for r in recs if r.get("accepted")]
+    assert len(its) == st.newton_iters and len(acc) == 3
+    assert [r["cg_iters"] for r in its] == log[:, 1].astype(int).tolist()
+    assert [r["res"] for r in its] == log[:, 2].tolist()
+    assert all(r["converged"] and r["res_rel"] <= 1e-8 for r in acc)
+    assert all(r["ms_solve"] > 0 and r["ips_assemble"] > 0 for r in its)
+    # closing the log stops the records
+    sm.newton(np.zeros(sm.neq), 10, 0, 1, newton_max_it=30)
+    assert len(open(path).readlines()) == len(recs)
