@@ -117,6 +117,19 @@ ipfem_status ipfem_set_load_factor(ipfem_ctx *ctx, double lambda);
  *                    iterative refinement.  cg_rtol is then the inner FP32
  *                    tolerance (1e-4 is a good choice). */
 ipfem_status ipfem_set_precision(ipfem_ctx *ctx, int mode);
+/* Precision of the residual evaluations in IPFEM_MIXED (no counterpart in
+ * the reference): bits = 64 (default) or 32.  With 32 the strain gather
+ * (FP32 element blocks, u rounded to FP32 as it is gathered), the weighted
+ * stresses and the residual scatter with its colour sums run in FP32 with
+ * FP32 accumulation; the return mapping and tangent operator stay FP64 (on
+ * the widened FP32 strain), the external load is added in FP64 and the
+ * residual norm is FP64.  In the Newton iteration a load step evaluates
+ * FP32 residuals until |R| <= switch_rtol |R0| or |R| stops halving, then
+ * refines with FP64 residuals (the first at the same u, the tangent kept);
+ * the convergence test and the state commit only ever use FP64 residuals.
+ * Direct ipfem_assemble / ipfem_assemble_residual calls return the FP32
+ * residual (widened) while 32 is set, except when committing. */
+ipfem_status ipfem_set_residual_precision(ipfem_ctx *ctx, int bits, double switch_rtol);
 /* TPZMatWithMem::SetUpdateMem: when set, the next residual commits the
  * integration-point state (main.cpp:487-522). */
 ipfem_status ipfem_set_update_mem(ipfem_ctx *ctx, int update);

@@ -105,6 +105,7 @@ def lib():
             "ipfem_set_load_factor": (S, [P, C.c_double]),
             "ipfem_set_update_mem": (S, [P, S]),
             "ipfem_set_precision": (S, [P, S]),
+            "ipfem_set_residual_precision": (S, [P, S, C.c_double]),
             "ipfem_assemble_residual": (S, [P, P, P, S]),
             "ipfem_assemble": (S, [P, P, P, S]),
             "ipfem_get_stiffness": (S, [P, _lp, _ip, _dp]),
@@ -412,6 +413,11 @@ class ElastoPlasticIntPointsStructMatrix:
 
     def set_precision(self, mode):
         self._check(lib().ipfem_set_precision(self._ctx, int(mode)))
+
+    def set_residual_precision(self, bits, switch_rtol=1e-5):
+        """32: FP32 strain gather / residual scatter in IPFEM_MIXED, with FP64
+        refinement once |R| <= switch_rtol |R0| or |R| stops halving; 64: FP64"""
+        self._check(lib().ipfem_set_residual_precision(self._ctx, int(bits), float(switch_rtol)))
 
     def SetLoadFactor(self, lam):
         self._check(lib().ipfem_set_load_factor(self._ctx, float(lam)))

@@ -98,7 +98,7 @@ void free_all(ipfem_ctx *c)
         if (p) cudaFree(p);
     {
         MixedBuffers &m = c->mx;
-        void *mp[] = {m.dphi, m.K, m.dinv, m.binv, m.x, m.r, m.z, m.p, m.q, m.part, m.sc};
+        void *mp[] = {m.dphi, m.K, m.dinv, m.binv, m.x, m.r, m.z, m.p, m.q, m.part, m.sc, m.strain32, m.sigw32, m.fe32};
         for (void *p : mp)
             if (p) cudaFree(p);
         if (m.h_sc) cudaFreeHost(m.h_sc);
@@ -150,6 +150,14 @@ ipfem_status sync_check(ipfem_ctx *c)
 void residual_device(ipfem_ctx *c, const double *d_u, double *d_out, int update_mem)
 {
     c->launches += 4;
+    if (c->res32_active && !update_mem) {
+        MixedBuffers &m = c->mx;
+        launch_gather_strain32(c, d_u, m.strain32);
+        launch_compute_sigma32(c, 0, m.strain32, m.sigw32, nullptr);
+        launch_stress_residual32(c, m.sigw32, m.fe32);
+        launch_color_reduce32(c, m.fe32, c->load_factor, 1, d_out);
+        return;
+    }
     launch_gather_strain(c, d_u, c->d_strain);
     launch_compute_sigma(c, update_mem, c->d_strain, c->d_sigma_w, nullptr);
     launch_stress_residual(c, c->d_sigma_w, c->d_fe);
@@ -159,10 +167,18 @@ void residual_device(ipfem_ctx *c, const double *d_u, double *d_out, int update_
 void tangent_device(ipfem_ctx *c, const double *d_u, double *d_out, int update_mem)
 {
     c->launches += 6 + c->s.n_colors;
-    launch_gather_strain(c, d_u, c->d_strain);
-    launch_compute_sigma(c, update_mem, c->d_strain, c->d_sigma_w, c->d_dep);
-    launch_stress_residual(c, c->d_sigma_w, c->d_fe);
-    launch_color_reduce(c, c->d_fe, c->load_factor, 1, d_out);
+    if (c->res32_active && !update_mem) {
+        MixedBuffers &m = c->mx;
+        launch_gather_strain32(c, d_u, m.strain32);
+        launch_compute_sigma32(c, 0, m.strain32, m.sigw32, c->d_dep);
+        launch_stress_residual32(c, m.sigw32, m.fe32);
+        launch_color_reduce32(c, m.fe32, c->load_factor, 1, d_out);
+    } else {
+        launch_gather_strain(c, d_u, c->d_strain);
+        launch_compute_sigma(c, update_mem, c->d_strain, c->d_sigma_w, c->d_dep);
+        launch_stress_residual(c, c->d_sigma_w, c->d_fe);
+        launch_color_reduce(c, c->d_fe, c->load_factor, 1, d_out);
+    }
     if (c->precision == 1) launch_stiffness32(c);
     else launch_stiffness(c);
     c->mlp.op_valid = false;     // the learned operator belongs to the previous tangent
@@ -470,6 +486,7 @@ ipfem_status ipfem_set_precision(ipfem_ctx *c, int mode)
             if (e != cudaSuccess && st == IPFEM_OK) st = (e == cudaErrorMemoryAllocation) ? IPFEM_OOM : IPFEM_CUDA;
         };
         std::vector<float> d32(s.dphi.begin(), s.dphi.end());
+        d32.resize(d32.size() + 4, 0.f);   // the FP32 gather's last bulk copy may read 8 bytes past the blocks
         ck(upload(&m.dphi, d32, c->stream));
         const std::string e = build_sell(s, false, true, m.sell);
         if (!e.empty()) return fail(c, IPFEM_INVALID, e);
@@ -492,6 +509,7 @@ ipfem_status ipfem_set_precision(ipfem_ctx *c, int mode)
     }
     if (mode != c->precision) c->tangent_valid = false;
     c->precision = mode;
+    if (mode != IPFEM_MIXED) c->res32 = 0;
     return IPFEM_OK;
 }
 
@@ -513,10 +531,37 @@ static ipfem_status assemble_common(ipfem_ctx *c, const double *u, double *rhs, 
         du = c->d_u;
         dr = c->d_rhs;
     }
+    // direct calls evaluate FP32 residuals whenever they are switched on (a
+    // committing call stays FP64)
+    c->res32_active = c->res32 && c->precision == IPFEM_MIXED;
     if (tangent) tangent_device(c, du, dr, c->update_mem);
     else residual_device(c, du, dr, c->update_mem);
+    c->res32_active = 0;
     if (where == IPFEM_HOST) CK(cudaMemcpyAsync(rhs, dr, nb, cudaMemcpyDeviceToHost, c->stream));
     return sync_check(c);
+}
+
+ipfem_status ipfem_set_residual_precision(ipfem_ctx *c, int bits, double switch_rtol)
+{
+    if (!c) return IPFEM_INVALID;
+    if (bits != 32 && bits != 64) return fail(c, IPFEM_INVALID, "residual precision must be 32 or 64 bits");
+    if (!(switch_rtol >= 0.0 && switch_rtol < 1.0))
+        return fail(c, IPFEM_INVALID, "switch_rtol must be in [0, 1)");
+    if (bits == 32 && c->precision != IPFEM_MIXED)
+        return fail(c, IPFEM_INVALID, "FP32 residuals need IPFEM_MIXED (its FP32 element blocks)");
+    if (bits == 32 && !c->mx.strain32) {
+        MixedBuffers &m = c->mx;
+        const Setup &s = c->s;
+        cudaError_t e = dalloc(&m.strain32, (size_t)3 * s.n_ip);
+        if (e == cudaSuccess) e = dalloc(&m.sigw32, (size_t)3 * s.n_ip);
+        if (e == cudaSuccess) e = dalloc(&m.fe32, (size_t)s.n_el * s.nd);
+        if (e != cudaSuccess)
+            return fail(c, e == cudaErrorMemoryAllocation ? IPFEM_OOM : IPFEM_CUDA,
+                        "allocation of the FP32 residual buffers failed");
+    }
+    c->res32 = bits == 32;
+    c->res32_switch = switch_rtol;
+    return IPFEM_OK;
 }
 
 ipfem_status ipfem_assemble_residual(ipfem_ctx *c, const double *u, double *rhs, int where)
@@ -696,6 +741,7 @@ static ipfem_status newton_advance(ipfem_ctx *c, int32_t n_iters, double *du, ip
         if (!ns.open) {
             Range rg("ipfem:newton:first_assembly");
             c->load_factor = (double)(ns.step + 1) / (double)o.n_steps;
+            c->res32_active = c->res32 && c->precision == IPFEM_MIXED;
             cudaEventRecord(ev[0], c->stream);
             newton_assemble(c, du);
             cudaEventRecord(ev[1], c->stream);
@@ -764,24 +810,43 @@ static ipfem_status newton_advance(ipfem_ctx *c, int32_t n_iters, double *du, ip
             e = dot_host(c, c->d_rhs, c->d_rhs, &rsq);
             st->ms_assemble += elapsed();
             if (e != IPFEM_OK) return e;
+            const double rn_prev = ns.rn;
             ns.rn = std::sqrt(rsq);
             if (!std::isfinite(ns.rn)) return fail(c, IPFEM_NAN, "residual is not finite");
+            const int was32 = c->res32_active;
+            const double rsq32 = rsq;
+            if (c->res32_active && (ns.rn <= c->res32_switch * ns.r0 || ns.rn > 0.5 * rn_prev)) {
+                // FP64 refinement: from here on this load step evaluates FP64
+                // residuals, starting with the one at the current u (the
+                // tangent just assembled is kept); the convergence test only
+                // ever sees FP64 residuals
+                c->res32_active = 0;
+                cudaEventRecord(ev[0], c->stream);
+                residual_device(c, du, c->d_rhs, 0);
+                cudaEventRecord(ev[1], c->stream);
+                e = dot_host(c, c->d_rhs, c->d_rhs, &rsq);
+                st->ms_assemble += elapsed();
+                if (e != IPFEM_OK) return e;
+                ns.rn = std::sqrt(rsq);
+                if (!std::isfinite(ns.rn)) return fail(c, IPFEM_NAN, "residual is not finite");
+            }
             if (log && *nlog < log_cap) {
                 log[3 * *nlog + 0] = (double)ns.step;
                 log[3 * *nlog + 1] = (double)k;
                 log[3 * *nlog + 2] = ns.rn;
                 (*nlog)++;
             }
-            conv = ns.rn <= o.newton_rtol * ns.r0;
+            conv = !c->res32_active && ns.rn <= o.newton_rtol * ns.r0;
             if (c->iter_log) {
                 const double ma = st->ms_assemble - ma0, ms = st->ms_solve - ms0;
                 std::fprintf(c->iter_log,
                              "{\"step\": %d, \"iter\": %d, \"cg_iters\": %d, \"res\": %.17g, \"res_rel\": %.17g, "
                              "\"ms_solve\": %.6f, \"ms_assemble\": %.6f, \"ips_assemble\": %.6g, "
-                             "\"fcg_fallback\": %d}\n",
+                             "\"fcg_fallback\": %d, \"res32\": %d, \"res32_rel\": %.17g}\n",
                              ns.step, ns.it, k, ns.rn, ns.r0 > 0.0 ? ns.rn / ns.r0 : 0.0, ms, ma,
                              ma > 0.0 ? (double)c->s.n_ip / (1e-3 * ma) : 0.0,
-                             (int)(c->fcg_fallbacks - fb0));
+                             (int)(c->fcg_fallbacks - fb0), c->res32_active,
+                             was32 && ns.r0 > 0.0 ? std::sqrt(rsq32) / ns.r0 : 0.0);
                 std::fflush(c->iter_log);
             }
         }

@@ -78,6 +78,8 @@ struct MixedBuffers {
     float *binv = nullptr;        // [n_nodes*4] block-Jacobi inverses
     float *x = nullptr, *r = nullptr, *z = nullptr, *p = nullptr, *q = nullptr;
     float *part = nullptr;        // 2 partial arrays
+    float *strain32 = nullptr, *sigw32 = nullptr;   // [3][n_ip] FP32 residual (ipfem_set_residual_precision)
+    float *fe32 = nullptr;                          // [n_el][nd]
     CGScalarsT<float> *sc = nullptr;
     CGScalarsT<float> *h_sc = nullptr;   // pinned
     cudaGraphExec_t exec = nullptr;
@@ -241,6 +243,9 @@ struct ipfem_ctx {
     cudaGraphExec_t fcg_exec = nullptr;
     int64_t fcg_fallbacks = 0;
     FILE *iter_log = nullptr;            // JSON-lines record of the Newton iterations (ipfem_set_iteration_log)
+    int res32 = 0;                       // FP32 residual evaluations in IPFEM_MIXED (ipfem_set_residual_precision)
+    int res32_active = 0;                // the residuals being evaluated now are FP32
+    double res32_switch = 1e-5;          // |R| / |R0| below which a load step refines with FP64 residuals
 };
 
 // ---- kernel launchers (implemented in the .cu files) ----
@@ -256,6 +261,12 @@ void launch_gather_strain(ipfem_ctx *c, const double *d_u, double *d_strain);
 void launch_compute_sigma(ipfem_ctx *c, int update_mem, const double *d_strain, double *d_sigma_w, double *d_dep);
 void launch_stress_residual(ipfem_ctx *c, const double *d_sigma_w, double *d_fe);
 void launch_color_reduce(ipfem_ctx *c, const double *d_fe, double lambda, int with_load, double *d_res);
+// the FP32 residual of IPFEM_MIXED_RES32: FP32 gather, FP64 point update on
+// FP32 strains, FP32 scatter and colour sums (the load added in FP64)
+void launch_gather_strain32(ipfem_ctx *c, const double *d_u, float *d_strain);
+void launch_compute_sigma32(ipfem_ctx *c, int update_mem, const float *d_strain, float *d_sigma_w, double *d_dep);
+void launch_stress_residual32(ipfem_ctx *c, const float *d_sigma_w, float *d_fe);
+void launch_color_reduce32(ipfem_ctx *c, const float *d_fe, double lambda, int with_load, double *d_res);
 void launch_stiffness(ipfem_ctx *c);
 void launch_cg_init(ipfem_ctx *c, const double *d_b, double rtol, int max_it);
 void launch_cg_iteration(ipfem_ctx *c);

@@ -35,29 +35,41 @@ struct Elem {
     static constexpr int kResTile = P == 1 ? 32 : (P == 2 ? 16 : 8);      // elements per CTA
 };
 static_assert(Elem<1>::NB * 8 % 16 == 0 && Elem<2>::NB * 8 % 16 == 0 && Elem<3>::NB * 8 % 16 == 0,
-              "bulk copies of whole element blocks need 16-byte multiples");
+              "bulk copies of whole FP64 element blocks need 16-byte multiples");
+// FP32 tiles start at 16-byte boundaries (full tiles are 16-byte multiples)
+static_assert(Elem<1>::kGatherTile * Elem<1>::NB * 4 % 16 == 0 && Elem<2>::kGatherTile * Elem<2>::NB * 4 % 16 == 0 &&
+                  Elem<3>::kGatherTile * Elem<3>::NB * 4 % 16 == 0 && Elem<1>::kResTile * Elem<1>::NB * 4 % 16 == 0 &&
+                  Elem<2>::kResTile * Elem<2>::NB * 4 % 16 == 0 && Elem<3>::kResTile * Elem<3>::NB * 4 % 16 == 0,
+              "FP32 element tiles must start on 16-byte boundaries");
 
-template <int P>
+// T = double: the plain path (bit-exact with the oracle); T = float: the
+// FP32 strain gather of the mixed-precision residual (FP32 element blocks, u
+// rounded to FP32 as it is gathered, FP32 fma, FP32 strain).
+template <class T, int P>
 __global__ void __launch_bounds__(Elem<P>::kGatherTile * Elem<P>::NQ)
-k_gather_strain(int32_t n_el, int64_t n_ip, const double *__restrict__ dphi, const int32_t *__restrict__ dofs,
-                const double *__restrict__ u, double *__restrict__ strain, int *__restrict__ err)
+k_gather_strain(int32_t n_el, int64_t n_ip, const T *__restrict__ dphi, const int32_t *__restrict__ dofs,
+                const double *__restrict__ u, T *__restrict__ strain, int *__restrict__ err)
 {
     typedef Elem<P> E;
     extern __shared__ __align__(128) unsigned char smem[];
     uint64_t *bar = reinterpret_cast<uint64_t *>(smem);
-    double *s_dn = reinterpret_cast<double *>(smem + 128);
-    double *s_u = s_dn + E::kGatherTile * E::NB;
+    T *s_dn = reinterpret_cast<T *>(smem + 128);
+    T *s_u = s_dn + E::kGatherTile * E::NB;
     const int32_t e0 = blockIdx.x * E::kGatherTile;
     const int ne = min(E::kGatherTile, n_el - e0);
     if (threadIdx.x == 0) mbar_init(bar, 1);
     __syncthreads();
     if (threadIdx.x == 0) {
-        const uint32_t bytes = (uint32_t)ne * E::NB * 8;
+        // a bulk copy moves a multiple of 16 bytes: an FP32 order-2 block is
+        // 648 bytes, so a partial tile of an odd number of elements copies 8
+        // bytes more, which stay inside the tile's staging area (the FP32
+        // block array is allocated with 16 bytes of padding for them)
+        const uint32_t bytes = ((uint32_t)ne * E::NB * (uint32_t)sizeof(T) + 15u) & ~15u;
         mbar_expect_tx(bar, bytes);
         bulk_g2s(s_dn, dphi + (size_t)e0 * E::NB, bytes, bar);
     }
     for (int k = threadIdx.x; k < ne * E::ND; k += blockDim.x)
-        s_u[k] = __ldg(&u[__ldg(&dofs[(size_t)e0 * E::ND + k])]);
+        s_u[k] = (T)__ldg(&u[__ldg(&dofs[(size_t)e0 * E::ND + k])]);
     const bool ok = mbar_wait_bounded(bar, 0);
     __syncthreads();
     if (!ok) {
@@ -66,10 +78,10 @@ k_gather_strain(int32_t n_el, int64_t n_ip, const double *__restrict__ dphi, con
     }
     const int el = threadIdx.x / E::NQ, q = threadIdx.x % E::NQ;
     if (el >= ne) return;
-    const double *dx = s_dn + el * E::NB + q * 2 * E::NN;
-    const double *dy = dx + E::NN;
-    const double *ue = s_u + el * E::ND;
-    double exx = 0.0, gxy = 0.0, eyy = 0.0;
+    const T *dx = s_dn + el * E::NB + q * 2 * E::NN;
+    const T *dy = dx + E::NN;
+    const T *ue = s_u + el * E::ND;
+    T exx = T(0), gxy = T(0), eyy = T(0);
 #pragma unroll
     for (int n = 0; n < E::NN; n++) exx = fma(dx[n], ue[2 * n], exx);
 #pragma unroll
@@ -85,23 +97,25 @@ k_gather_strain(int32_t n_el, int64_t n_ip, const double *__restrict__ dphi, con
     strain[2 * n_ip + ip] = eyy;
 }
 
-template <int P>
+// V = double: the plain path; V = float: the FP32 residual scatter of the
+// mixed-precision residual (FP32 blocks, stresses and fma accumulation).
+template <class V, int P>
 __global__ void __launch_bounds__(Elem<P>::kResTile * Elem<P>::ND)
-k_stress_residual(int32_t n_el, int64_t n_ip, const double *__restrict__ dphi, const double *__restrict__ sigma_w,
-                  double *__restrict__ fe, int *__restrict__ err)
+k_stress_residual(int32_t n_el, int64_t n_ip, const V *__restrict__ dphi, const V *__restrict__ sigma_w,
+                  V *__restrict__ fe, int *__restrict__ err)
 {
     typedef Elem<P> E;
     constexpr int T = E::kResTile;
     extern __shared__ __align__(128) unsigned char smem[];
     uint64_t *bar = reinterpret_cast<uint64_t *>(smem);
-    double *s_dn = reinterpret_cast<double *>(smem + 128);
-    double *s_sig = s_dn + T * E::NB;                  // [3][T*nq]
+    V *s_dn = reinterpret_cast<V *>(smem + 128);
+    V *s_sig = s_dn + T * E::NB;                       // [3][T*nq]
     const int32_t e0 = blockIdx.x * T;
     const int ne = min(T, n_el - e0);
     if (threadIdx.x == 0) mbar_init(bar, 1);
     __syncthreads();
     if (threadIdx.x == 0) {
-        const uint32_t bytes = (uint32_t)ne * E::NB * 8;
+        const uint32_t bytes = ((uint32_t)ne * E::NB * (uint32_t)sizeof(V) + 15u) & ~15u;   // see k_gather_strain
         mbar_expect_tx(bar, bytes);
         bulk_g2s(s_dn, dphi + (size_t)e0 * E::NB, bytes, bar);
     }
@@ -120,12 +134,12 @@ k_stress_residual(int32_t n_el, int64_t n_ip, const double *__restrict__ dphi, c
     const int el = threadIdx.x / E::ND, j = threadIdx.x % E::ND;
     if (el >= ne) return;
     const int n = j >> 1;
-    const double *dn = s_dn + el * E::NB;
+    const V *dn = s_dn + el * E::NB;
     // x-dof: dNx*sxx + dNy*sxy per point; y-dof: dNx*sxy + dNy*syy.  The two
     // stress rows are selected by pointer so the warp does not diverge.
-    const double *s1 = s_sig + (j & 1) * T * E::NQ + el * E::NQ;
-    const double *s2 = s1 + T * E::NQ;
-    double acc = 0.0;
+    const V *s1 = s_sig + (j & 1) * T * E::NQ + el * E::NQ;
+    const V *s2 = s1 + T * E::NQ;
+    V acc = V(0);
 #pragma unroll
     for (int q = 0; q < E::NQ; q++) {
         acc = fma(dn[q * 2 * E::NN + n], s1[q], acc);
@@ -137,9 +151,16 @@ k_stress_residual(int32_t n_el, int64_t n_ip, const double *__restrict__ dphi, c
 // Per node: contributions of the incident element of each colour (0 if none),
 // summed in the reference's pairwise slab order
 // (TPZNumericalIntegrator.cpp:69-77: slab k += slab (nc-ca)+k, nc -= ca).
+template <class V> struct Pair;
+template <> struct Pair<double> { typedef double2 type; };
+template <> struct Pair<float> { typedef float2 type; };
+
+// V = float: the element forces of the FP32 residual, summed in FP32; the
+// external load (FP64) is added to the FP32 sum in FP64.
+template <class V>
 __global__ void __launch_bounds__(256) k_color_reduce(int32_t n_nodes, int n_colors,
                                                       const int32_t *__restrict__ inc,
-                                                      const double *__restrict__ fe, double lambda,
+                                                      const V *__restrict__ fe, double lambda,
                                                       int with_load, const double *__restrict__ f0,
                                                       const double *__restrict__ df,
                                                       const uint8_t *__restrict__ fixed,
@@ -147,15 +168,15 @@ __global__ void __launch_bounds__(256) k_color_reduce(int32_t n_nodes, int n_col
 {
     const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n_nodes) return;
-    double sx[kMaxColors], sy[kMaxColors];
+    V sx[kMaxColors], sy[kMaxColors];
 #pragma unroll
     for (int c = 0; c < kMaxColors; c++) {
-        sx[c] = 0.0;
-        sy[c] = 0.0;
+        sx[c] = V(0);
+        sy[c] = V(0);
         if (c < n_colors) {
             const int32_t k = __ldg(&inc[(size_t)c * n_nodes + i]);
             if (k >= 0) {
-                const double2 v = *reinterpret_cast<const double2 *>(&fe[2 * (size_t)k]);
+                const typename Pair<V>::type v = *reinterpret_cast<const typename Pair<V>::type *>(&fe[2 * (size_t)k]);
                 sx[c] = v.x;
                 sy[c] = v.y;
             }
@@ -173,7 +194,7 @@ __global__ void __launch_bounds__(256) k_color_reduce(int32_t n_nodes, int n_col
         nc -= ca;
         ca = nc / 2;
     }
-    double rx = sx[0], ry = sy[0];
+    double rx = (double)sx[0], ry = (double)sy[0];
     if (with_load) {
         const double lx = fma(lambda, df[2 * (size_t)i], f0[2 * (size_t)i]);
         const double ly = fma(lambda, df[2 * (size_t)i + 1], f0[2 * (size_t)i + 1]);
@@ -313,43 +334,61 @@ __global__ void k_jacobi(int32_t n_nodes, const int64_t *__restrict__ diag, cons
     }
 }
 
-template <int P>
-static void gather_strain_p(ipfem_ctx *c, const double *d_u, double *d_strain)
+template <class T, int P>
+static void gather_strain_p(ipfem_ctx *c, const T *dphi, const double *d_u, T *d_strain)
 {
     typedef Elem<P> E;
     const Setup &s = c->s;
     const unsigned grid = (unsigned)((s.n_el + E::kGatherTile - 1) / E::kGatherTile);
-    const size_t smem = 128 + (size_t)E::kGatherTile * (E::NB + E::ND) * 8;
-    k_gather_strain<P><<<grid, E::kGatherTile * E::NQ, smem, c->stream>>>(s.n_el, s.n_ip, c->d_dphi, c->d_dofs,
-                                                                           d_u, d_strain, c->d_err);
+    const size_t smem = 128 + (size_t)E::kGatherTile * (E::NB + E::ND) * sizeof(T);
+    k_gather_strain<T, P><<<grid, E::kGatherTile * E::NQ, smem, c->stream>>>(s.n_el, s.n_ip, dphi, c->d_dofs, d_u,
+                                                                              d_strain, c->d_err);
 }
 
 void launch_gather_strain(ipfem_ctx *c, const double *d_u, double *d_strain)
 {
     switch (c->s.order) {
-    case 1: gather_strain_p<1>(c, d_u, d_strain); break;
-    case 3: gather_strain_p<3>(c, d_u, d_strain); break;
-    default: gather_strain_p<2>(c, d_u, d_strain); break;
+    case 1: gather_strain_p<double, 1>(c, c->d_dphi, d_u, d_strain); break;
+    case 3: gather_strain_p<double, 3>(c, c->d_dphi, d_u, d_strain); break;
+    default: gather_strain_p<double, 2>(c, c->d_dphi, d_u, d_strain); break;
     }
 }
 
-template <int P>
-static void stress_residual_p(ipfem_ctx *c, const double *d_sigma_w, double *d_fe)
+void launch_gather_strain32(ipfem_ctx *c, const double *d_u, float *d_strain)
+{
+    switch (c->s.order) {
+    case 1: gather_strain_p<float, 1>(c, c->mx.dphi, d_u, d_strain); break;
+    case 3: gather_strain_p<float, 3>(c, c->mx.dphi, d_u, d_strain); break;
+    default: gather_strain_p<float, 2>(c, c->mx.dphi, d_u, d_strain); break;
+    }
+}
+
+template <class V, int P>
+static void stress_residual_p(ipfem_ctx *c, const V *dphi, const V *d_sigma_w, V *d_fe)
 {
     typedef Elem<P> E;
     const Setup &s = c->s;
     const unsigned grid = (unsigned)((s.n_el + E::kResTile - 1) / E::kResTile);
-    const size_t smem = 128 + (size_t)E::kResTile * (E::NB + 3 * E::NQ) * 8;
-    k_stress_residual<P><<<grid, E::kResTile * E::ND, smem, c->stream>>>(s.n_el, s.n_ip, c->d_dphi, d_sigma_w,
-                                                                          d_fe, c->d_err);
+    const size_t smem = 128 + (size_t)E::kResTile * (E::NB + 3 * E::NQ) * sizeof(V);
+    k_stress_residual<V, P><<<grid, E::kResTile * E::ND, smem, c->stream>>>(s.n_el, s.n_ip, dphi, d_sigma_w, d_fe,
+                                                                             c->d_err);
 }
 
 void launch_stress_residual(ipfem_ctx *c, const double *d_sigma_w, double *d_fe)
 {
     switch (c->s.order) {
-    case 1: stress_residual_p<1>(c, d_sigma_w, d_fe); break;
-    case 3: stress_residual_p<3>(c, d_sigma_w, d_fe); break;
-    default: stress_residual_p<2>(c, d_sigma_w, d_fe); break;
+    case 1: stress_residual_p<double, 1>(c, c->d_dphi, d_sigma_w, d_fe); break;
+    case 3: stress_residual_p<double, 3>(c, c->d_dphi, d_sigma_w, d_fe); break;
+    default: stress_residual_p<double, 2>(c, c->d_dphi, d_sigma_w, d_fe); break;
+    }
+}
+
+void launch_stress_residual32(ipfem_ctx *c, const float *d_sigma_w, float *d_fe)
+{
+    switch (c->s.order) {
+    case 1: stress_residual_p<float, 1>(c, c->mx.dphi, d_sigma_w, d_fe); break;
+    case 3: stress_residual_p<float, 3>(c, c->mx.dphi, d_sigma_w, d_fe); break;
+    default: stress_residual_p<float, 2>(c, c->mx.dphi, d_sigma_w, d_fe); break;
     }
 }
 
@@ -357,8 +396,16 @@ void launch_color_reduce(ipfem_ctx *c, const double *d_fe, double lambda, int wi
 {
     const Setup &s = c->s;
     const unsigned grid = (unsigned)((s.n_nodes + 255) / 256);
-    k_color_reduce<<<grid, 256, 0, c->stream>>>(s.n_nodes, s.n_colors, c->d_inc, d_fe, lambda, with_load, c->d_f0,
-                                                 c->d_df, c->d_fixed, d_res);
+    k_color_reduce<double><<<grid, 256, 0, c->stream>>>(s.n_nodes, s.n_colors, c->d_inc, d_fe, lambda, with_load,
+                                                         c->d_f0, c->d_df, c->d_fixed, d_res);
+}
+
+void launch_color_reduce32(ipfem_ctx *c, const float *d_fe, double lambda, int with_load, double *d_res)
+{
+    const Setup &s = c->s;
+    const unsigned grid = (unsigned)((s.n_nodes + 255) / 256);
+    k_color_reduce<float><<<grid, 256, 0, c->stream>>>(s.n_nodes, s.n_colors, c->d_inc, d_fe, lambda, with_load,
+                                                        c->d_f0, c->d_df, c->d_fixed, d_res);
 }
 
 void launch_stiffness(ipfem_ctx *c)

@@ -7,13 +7,16 @@
 
 namespace ipfem {
 
-template <bool DEP, bool UPD>
+// TS = double: the plain path; TS = float: the FP32 strain and weighted
+// stress arrays of the mixed-precision residual (the point update itself
+// stays FP64: the strain is widened, the weighted stress rounded at the end).
+template <bool DEP, bool UPD, class TS>
 __global__ void __launch_bounds__(128) k_compute_sigma(int64_t n_ip, int32_t n_el, int32_t npts, ElasticConst E,
-                                                       const double *__restrict__ strain,
+                                                       const TS *__restrict__ strain,
                                                        const double *__restrict__ weight,
                                                        const double *__restrict__ mat,
                                                        double *__restrict__ eps_p,
-                                                       double *__restrict__ sigma_w,
+                                                       TS *__restrict__ sigma_w,
                                                        double *__restrict__ dep,
                                                        double *__restrict__ sig_state,
                                                        int8_t *__restrict__ mtype,
@@ -28,14 +31,14 @@ __global__ void __launch_bounds__(128) k_compute_sigma(int64_t n_ip, int32_t n_e
     m.cosphi = __ldg(&mat[2 * (int64_t)n_el + e]);
     m.tanphi = __ldg(&mat[3 * (int64_t)n_el + e]);
     m.sinpsi = __ldg(&mat[4 * (int64_t)n_el + e]);
-    const double eps[3] = {strain[ip], strain[n_ip + ip], strain[2 * n_ip + ip]};
+    const double eps[3] = {(double)strain[ip], (double)strain[n_ip + ip], (double)strain[2 * n_ip + ip]};
     const double pl[4] = {eps_p[ip], eps_p[n_ip + ip], eps_p[2 * n_ip + ip], eps_p[3 * n_ip + ip]};
     double sig[4], plo[4], a, d[9];
     const int mt = ip_update<DEP>(eps, pl, E, m, sig, plo, a, d);
     const double w = weight[ip];
-    sigma_w[ip] = sig[0] * w;
-    sigma_w[n_ip + ip] = sig[1] * w;
-    sigma_w[2 * n_ip + ip] = sig[2] * w;
+    sigma_w[ip] = (TS)(sig[0] * w);
+    sigma_w[n_ip + ip] = (TS)(sig[1] * w);
+    sigma_w[2 * n_ip + ip] = (TS)(sig[2] * w);
     if (DEP) {
 #pragma unroll
         for (int k = 0; k < 9; k++) dep[k * n_ip + ip] = d[k] * w;
@@ -51,8 +54,8 @@ __global__ void __launch_bounds__(128) k_compute_sigma(int64_t n_ip, int32_t n_e
     }
 }
 
-void launch_compute_sigma(ipfem_ctx *c, int update_mem, const double *d_strain, double *d_sigma_w,
-                          double *d_dep)
+template <class TS>
+static void compute_sigma_t(ipfem_ctx *c, int update_mem, const TS *d_strain, TS *d_sigma_w, double *d_dep)
 {
     const Setup &s = c->s;
     ElasticConst E;
@@ -64,13 +67,23 @@ void launch_compute_sigma(ipfem_ctx *c, int update_mem, const double *d_strain, 
 #define ARGS s.n_ip, s.n_el, s.nq, E, d_strain, c->d_weight, c->d_mat, c->d_eps_p, d_sigma_w, d_dep, c->d_sigma, \
              c->d_mtype, c->d_alpha
     if (d_dep) {
-        if (update_mem) k_compute_sigma<true, true><<<grid, tpb, 0, c->stream>>>(ARGS);
-        else k_compute_sigma<true, false><<<grid, tpb, 0, c->stream>>>(ARGS);
+        if (update_mem) k_compute_sigma<true, true, TS><<<grid, tpb, 0, c->stream>>>(ARGS);
+        else k_compute_sigma<true, false, TS><<<grid, tpb, 0, c->stream>>>(ARGS);
     } else {
-        if (update_mem) k_compute_sigma<false, true><<<grid, tpb, 0, c->stream>>>(ARGS);
-        else k_compute_sigma<false, false><<<grid, tpb, 0, c->stream>>>(ARGS);
+        if (update_mem) k_compute_sigma<false, true, TS><<<grid, tpb, 0, c->stream>>>(ARGS);
+        else k_compute_sigma<false, false, TS><<<grid, tpb, 0, c->stream>>>(ARGS);
     }
 #undef ARGS
+}
+
+void launch_compute_sigma(ipfem_ctx *c, int update_mem, const double *d_strain, double *d_sigma_w, double *d_dep)
+{
+    compute_sigma_t<double>(c, update_mem, d_strain, d_sigma_w, d_dep);
+}
+
+void launch_compute_sigma32(ipfem_ctx *c, int update_mem, const float *d_strain, float *d_sigma_w, double *d_dep)
+{
+    compute_sigma_t<float>(c, update_mem, d_strain, d_sigma_w, d_dep);
 }
 
 }  // namespace ipfem

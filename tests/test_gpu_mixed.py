@@ -105,3 +105,52 @@ def test_mixed_block_jacobi():
     (u0, k0), (u1, k1) = res[ip.PREC_JACOBI], res[ip.PREC_BLOCK_JACOBI]
     assert np.abs(u1 - u0).max() < 1e-6 * np.abs(u0).max()
     assert k1 < 0.9 * k0, (k1, k0)
+
+
+def test_fp32_residual_against_fp64():
+    """FP32 strain gather / residual scatter (IPFEM_MIXED with 32-bit
+    residuals): within FP32 rounding of the FP64 oracle residual; a
+    committing call stays FP64 and bit-exact"""
+    sm, P = _pair(24, material_mode=2)
+    sm.set_precision(ip.MIXED)
+    sm.set_residual_precision(32)
+    rng = np.random.default_rng(8)
+    u = rng.normal(size=sm.neq) * 2e-3
+    u[P.arr("fixed").astype(bool)] = 0.0
+    sm.SetLoadFactor(0.9)
+    r32 = sm.assemble_residual(u, np.zeros(sm.neq))
+    r64 = P.assemble_residual(u.copy(), 0.9)
+    err = np.abs(r32 - r64).max() / np.abs(r64).max()
+    print("FP32 residual vs FP64: %.2e relative (max norm)" % err)
+    assert 1e-9 < err < 1e-5
+    sm.SetUpdateMem(True)
+    rc = sm.assemble_residual(u, np.zeros(sm.neq))
+    sm.SetUpdateMem(False)
+    assert np.array_equal(rc, r64)
+
+
+def test_fp32_residual_newton_refines_to_fp64_accuracy(tmp_path):
+    """Newton with FP32 residuals and FP64 refinement on 40 x 40, 10 load
+    steps: converges to 1e-8 like the FP64 residual, the solution within
+    1e-6 of the FP64 oracle; the FP32 residual's own floor is stated"""
+    import json
+
+    sm, P = _pair(40)
+    sm.set_precision(ip.MIXED)
+    sm.set_residual_precision(32, 0.0)           # FP32 until it stops halving: shows its floor
+    log = str(tmp_path / "it.jsonl")
+    sm.set_iteration_log(log)
+    ug, uo = np.zeros(sm.neq), np.zeros(sm.neq)
+    sg, _ = sm.newton(ug, 10, newton_max_it=40, cg_rtol=1e-4)
+    so, _ = P.solve_steps(uo, 10, newton_max_it=40)
+    assert sg.converged
+    recs = [json.loads(line) for line in open(log)]
+    floor = min(r["res32_rel"] for r in recs if r.get("res32_rel", 0) > 0)
+    n32 = sum(1 for r in recs if "iter" in r and r["res32_rel"] > 0)
+    eu = np.abs(ug - uo).max() / np.abs(uo).max()
+    sig, sigo = sm.get_state(1), _soa4(P.arr("sigma"), P.n_ip)
+    es = np.abs(sig - sigo).max() / np.abs(sigo).max()
+    print("FP32 residual: floor |R32|/|R0| %.2e; %d of %d Newton iterations on FP32 residuals (FP64 oracle %d); "
+          "u %.2e sigma %.2e" % (floor, n32, sg.newton_iters, so.newton_iters, eu, es))
+    assert eu < 1e-6 and es < 1e-6
+    assert floor > 1e-9                      # the FP32 residual cannot reach the 1e-8 target on its own
