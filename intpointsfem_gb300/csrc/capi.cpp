@@ -135,7 +135,9 @@ ipfem_status check_device(ipfem_ctx *c)
     CK(cudaMemcpyAsync(&c->h_pin[7], c->d_err, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
     CK(cudaStreamSynchronize(c->stream));
     std::memcpy(&err, &c->h_pin[7], sizeof(int));
-    if (err) return fail(c, IPFEM_CUDA, "device wait timed out (bulk copy did not complete)");
+    if (err)
+        return fail(c, IPFEM_CUDA, err == kErrGridWait ? "device wait timed out (grid barrier of a solver kernel)"
+                                                      : "device wait timed out (bulk copy did not complete)");
     return IPFEM_OK;
 }
 
@@ -209,7 +211,7 @@ ipfem_status cg_device(ipfem_ctx *c, const double *d_b, double rtol, int max_it,
     for (;;) {
         CK(cudaGraphLaunch(c->cg_exec, c->stream));
         launched += batch;
-        c->launches += 3 * batch;
+        c->launches += 2 * batch;
         CK(cudaMemcpyAsync(c->h_sc, c->d_sc, sizeof(CGScalars), cudaMemcpyDeviceToHost, c->stream));
         CK(cudaStreamSynchronize(c->stream));
         if (c->h_sc->done || launched >= max_it + batch) break;
@@ -245,7 +247,7 @@ ipfem_status cg32_device(ipfem_ctx *c, const double *d_b, double scale, double r
     for (;;) {
         CK(cudaGraphLaunch(m.exec, c->stream));
         launched += batch;
-        c->launches += 3 * batch;
+        c->launches += 2 * batch;
         CK(cudaMemcpyAsync(m.h_sc, m.sc, sizeof(CGScalarsT<float>), cudaMemcpyDeviceToHost, c->stream));
         CK(cudaStreamSynchronize(c->stream));
         if (m.h_sc->done || launched >= max_it + batch) break;
@@ -412,7 +414,7 @@ ipfem_status ipfem_create(const ipfem_mesh *mesh, const ipfem_material *mat, ipf
     c->n_red = (s.n_nodes + kRedBlock - 1) / kRedBlock;
     ck(dalloc(&c->d_part, (size_t)c->n_red * 3));
     ck(dalloc(&c->d_sc, 1));
-    ck(dalloc(&c->d_counters, 8));
+    ck(dalloc(&c->d_counters, 16));
     ck(dalloc(&c->d_dotres, 8));
     ck(dalloc(&c->d_err, 1));
     ck(cudaMallocHost((void **)&c->h_sc, sizeof(CGScalars)));
@@ -421,7 +423,12 @@ ipfem_status ipfem_create(const ipfem_mesh *mesh, const ipfem_material *mat, ipf
         c->err = "device allocation failed";
         return bail(st);
     }
-    ck(cudaMemsetAsync(c->d_counters, 0, 8 * sizeof(unsigned), t));
+    ck(cudaMemsetAsync(c->d_counters, 0, 16 * sizeof(unsigned), t));
+    solver_configure(c);
+    if (c->coop_cap_cg64 <= 0 || c->coop_cap_cg32 <= 0 || c->coop_cap_fcg <= 0) {
+        c->err = "occupancy query of the solver kernels failed";
+        return bail(IPFEM_CUDA);
+    }
     ck(cudaMemsetAsync(c->d_err, 0, sizeof(int), t));
     ck(cudaMemsetAsync(c->d_sc, 0, sizeof(CGScalars), t));
     ck(cudaMemsetAsync(c->d_u, 0, (size_t)s.neq * sizeof(double), t));

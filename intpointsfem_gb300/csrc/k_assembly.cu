@@ -73,7 +73,7 @@ k_gather_strain(int32_t n_el, int64_t n_ip, const T *__restrict__ dphi, const in
     const bool ok = mbar_wait_bounded(bar, 0);
     __syncthreads();
     if (!ok) {
-        if (threadIdx.x == 0) atomicExch(err, 1);
+        if (threadIdx.x == 0) atomicExch(err, kErrBulkWait);
         return;
     }
     const int el = threadIdx.x / E::NQ, q = threadIdx.x % E::NQ;
@@ -128,7 +128,7 @@ k_stress_residual(int32_t n_el, int64_t n_ip, const V *__restrict__ dphi, const 
     const bool ok = mbar_wait_bounded(bar, 0);
     __syncthreads();
     if (!ok) {
-        if (threadIdx.x == 0) atomicExch(err, 1);
+        if (threadIdx.x == 0) atomicExch(err, kErrBulkWait);
         return;
     }
     const int el = threadIdx.x / E::ND, j = threadIdx.x % E::ND;

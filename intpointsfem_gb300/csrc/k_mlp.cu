@@ -30,6 +30,7 @@
 #include <algorithm>
 #include <cmath>
 
+#include "grid_sync.cuh"
 #include "ipfem_internal.h"
 #include "ldhint.cuh"
 #include "pdl.cuh"
@@ -221,7 +222,9 @@ __device__ __forceinline__ float2 tri_mul(int32_t i, int32_t n, GridInfo G, cons
 
 // z_j = sigma_j * sum_k G_{i,k}^T y_i over the nodes i = nbr(j, 8-k) that
 // hold j at position k (gather form of G^T)
-template <class GT>
+// (COHERENT: y was written earlier in the same kernel, so it is read through
+// L2 instead of the read-only path)
+template <class GT, bool COHERENT = false>
 __device__ __forceinline__ float2 trit_mul(int32_t j, int32_t n, GridInfo G, const GT *__restrict__ Gm,
                                            const float2 *__restrict__ dinv, const float2 *__restrict__ y)
 {
@@ -231,7 +234,7 @@ __device__ __forceinline__ float2 trit_mul(int32_t j, int32_t n, GridInfo G, con
         const int32_t i = patch_nbr(j, 8 - k, G);
         if (i < 0) continue;
         const float4 m = load_g(Gm, (int64_t)k * n + i);
-        const float2 v = __ldg(&y[i]);
+        const float2 v = COHERENT ? __ldcg(&y[i]) : __ldg(&y[i]);
         z.x = fmaf(m.x, v.x, fmaf(m.z, v.y, z.x));
         z.y = fmaf(m.y, v.x, fmaf(m.w, v.y, z.y));
     }
@@ -546,6 +549,141 @@ __global__ void __launch_bounds__(256, 8) k_fcg_update_first(int32_t n, GridInfo
                 sc->status = IPFEM_NONCONVERGED;
             }
             *ticket = 0u;
+        }
+    }
+}
+
+// Partials of one 256-node window w, the sums of fcg_partials (warp trees,
+// then the CTA's warp sums in order) written to part[k * n_part + w], no ticket.
+template <int NV>
+__device__ __forceinline__ void fcg_window_partials(const float (&v)[NV], float *part, int64_t n_part, int64_t w)
+{
+    __shared__ float ws[NV][32];
+    const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+    for (int k = 0; k < NV; k++) {
+        const float t = wsum(v[k]);
+        if (lane == 0) ws[k][wp] = t;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int k = 0; k < NV; k++) {
+            float a = 0.f;
+            for (int q = 0; q < nw; q++) a = a + ws[k][q];
+            part[k * n_part + w] = a;
+        }
+    }
+    __syncthreads();
+}
+
+// The two vector passes of a flexible-CG iteration in one cooperative
+// launch: phase 1 is k_fcg_update_first (x += alpha p, r_new, y = G (sigma
+// r_new), r_new.r_new per window), a grid barrier whose last CTA runs its
+// epilogue (convergence, stagnation, iteration limit), phase 2 is
+// k_tri_precond (z = sigma G^T y, r.z and r_old.z per window) and a last-CTA
+// epilogue (beta).  The same operations on the same values, and the same
+// per-window partials in the same order, as the two kernels: equal results
+// bit for bit.  Windows w = blockIdx.x + j gridDim.x.
+__global__ void __launch_bounds__(256, 8) k_fcg_update_precond(int32_t n, int64_t n_win, GridInfo G,
+                                                            const uint2 *__restrict__ Gm, const float2 *__restrict__ dinv,
+                                                            const float2 *__restrict__ p, const float2 *__restrict__ q,
+                                                            float2 *__restrict__ x, const float2 *__restrict__ r_old,
+                                                            float2 *__restrict__ r_new, float2 *__restrict__ y,
+                                                            float *__restrict__ z, float *part, float *part2,
+                                                            int64_t n_part, unsigned *count, unsigned *gen,
+                                                            unsigned *count2, CGScalarsT<float> *sc, int stall_window,
+                                                            int *err)
+{
+    const unsigned gen0 = ld_acquire_gpu(gen);     // before this CTA arrives
+    pdl_wait();
+    pdl_launch_dependents();
+    if (*reinterpret_cast<volatile int *>(&sc->done)) return;
+    const float alpha = *reinterpret_cast<volatile float *>(&sc->alpha);
+    for (int64_t w = blockIdx.x; w < n_win; w += gridDim.x) {
+        const int32_t i = (int32_t)(w * 256) + (int32_t)threadIdx.x;
+        float v[1] = {0.f};
+        if (i < n) {
+            float2 xx = x[i];
+            const float2 pp = p[i];
+            xx.x = fmaf(alpha, pp.x, xx.x);
+            xx.y = fmaf(alpha, pp.y, xx.y);
+            x[i] = xx;
+            float2 acc = make_float2(0.f, 0.f);
+#pragma unroll
+            for (int k = 0; k < NTRI; k++) {
+                const int32_t jn = patch_nbr(i, k, G);
+                if (jn < 0) continue;
+                const float2 ro = __ldg(&r_old[jn]);
+                const float2 qq = __ldg(&q[jn]);
+                const float2 rn = make_float2(fmaf(-alpha, qq.x, ro.x), fmaf(-alpha, qq.y, ro.y));
+                if (k == 4) {
+                    r_new[i] = rn;
+                    v[0] = fmaf(rn.y, rn.y, rn.x * rn.x);
+                }
+                const float4 m = load_g(Gm, (int64_t)k * n + i);
+                const float2 sg = sqrt2(__ldg(&dinv[jn]));
+                const float vx = sg.x * rn.x, vy = sg.y * rn.y;
+                acc.x = fmaf(m.x, vx, fmaf(m.y, vy, acc.x));
+                acc.y = fmaf(m.z, vx, fmaf(m.w, vy, acc.y));
+            }
+            y[i] = acc;
+        }
+        fcg_window_partials<1>(v, part, n_part, w);
+    }
+    if (grid_arrive(count)) {
+        float o[1];
+        fcg_final<1>(part, n_part, o);
+        if (threadIdx.x == 0) {
+            const float rr = o[0];
+            sc->rr = rr;
+            sc->iters += 1;
+            if (rr < 0.98f * sc->rr_best) {
+                sc->rr_best = rr;
+                sc->it_best = sc->iters;
+            }
+            if (rr <= sc->thr) {
+                sc->done = 1;
+            } else if (!(rr == rr) || sc->iters - sc->it_best > max(stall_window, sc->it_best)) {
+                sc->done = 1;
+                sc->status = kStatusFallback;
+            } else if (sc->iters >= sc->max_it) {
+                sc->done = 1;
+                sc->status = IPFEM_NONCONVERGED;
+            }
+        }
+        grid_release(count, gen, gen0);
+    } else if (!grid_wait(gen, gen0, err)) {
+        if (threadIdx.x == 0) atomicExch(&sc->done, 1);
+        return;
+    }
+    if (*reinterpret_cast<volatile int *>(&sc->done)) return;
+    for (int64_t w = blockIdx.x; w < n_win; w += gridDim.x) {
+        const int32_t i = (int32_t)(w * 256) + (int32_t)threadIdx.x;
+        float v[2] = {0.f, 0.f};
+        if (i < n) {
+            const float2 zz = trit_mul<uint2, true>(i, n, G, Gm, dinv, y);
+            reinterpret_cast<float2 *>(z)[i] = zz;
+            const float2 rr = r_new[i], ro = r_old[i];
+            v[0] = fmaf(rr.y, zz.y, rr.x * zz.x);
+            v[1] = fmaf(ro.y, zz.y, ro.x * zz.x);
+        }
+        fcg_window_partials<2>(v, part2, n_part, w);
+    }
+    if (grid_arrive(count2)) {
+        float out[2];
+        fcg_final<2>(part2, n_part, out);
+        if (threadIdx.x == 0) {
+            const float rz = out[0], cross = out[1];
+            float beta = (sc->rz > 0.f) ? (rz - cross) / sc->rz : 0.f;
+            if (!(beta > 0.f)) beta = 0.f;
+            sc->beta = beta;
+            sc->rz = rz;
+            if (!(rz > 0.f)) {          // M r is not a descent direction
+                sc->done = 1;
+                sc->status = kStatusFallback;
+            }
+            *count2 = 0u;
         }
     }
 }
@@ -926,14 +1064,18 @@ void launch_fcg_iteration(ipfem_ctx *c, int par)
                (const uint8_t *)L.pat_id, (const int32_t *)L.pat_off, reinterpret_cast<const float4 *>(m.K),
                (const uint8_t *)c->d_fixed, reinterpret_cast<const float2 *>(m.z), (const float2 *)P[par],
                P[1 - par], reinterpret_cast<float2 *>(m.q), part, (int64_t)fcg_grid(c), c->d_counters + 5, m.sc);
-    launch_pdl(k_fcg_update_first, fcg_grid(c), 256, c->stream, n, G, reinterpret_cast<const uint2 *>(l.Gh), d2,
-               (const float2 *)P[1 - par], reinterpret_cast<const float2 *>(m.q), reinterpret_cast<float2 *>(m.x),
-               (const float2 *)R[par], R[1 - par], reinterpret_cast<float2 *>(l.y), part, (int64_t)fcg_grid(c),
-               c->d_counters + 6, m.sc, stall_window(c));
     float *part2 = reinterpret_cast<float *>(c->d_part);
-    launch_pdl(k_tri_precond, fcg_grid(c), 256, c->stream, n, G, reinterpret_cast<const uint2 *>(l.Gh), d2,
-               reinterpret_cast<const float2 *>(l.y), reinterpret_cast<const float *>(R[1 - par]),
-               reinterpret_cast<const float *>(R[par]), m.z, part2, (int64_t)fcg_grid(c), c->d_counters + 7, m.sc);
+    const int64_t n_win = fcg_grid(c);
+    launch_coop(k_fcg_update_precond, (unsigned)std::max<int64_t>(1, std::min<int64_t>(n_win, c->coop_cap_fcg)), 256,
+                c->stream, true, n, n_win, G, reinterpret_cast<const uint2 *>(l.Gh), d2, (const float2 *)P[1 - par],
+                reinterpret_cast<const float2 *>(m.q), reinterpret_cast<float2 *>(m.x), (const float2 *)R[par],
+                R[1 - par], reinterpret_cast<float2 *>(l.y), m.z, part, part2, n_win, c->d_counters + 12,
+                c->d_counters + 13, c->d_counters + 7, m.sc, stall_window(c), c->d_err);
+}
+
+int fcg_grid_capacity()
+{
+    return grid_capacity(k_fcg_update_precond, 256, 0);
 }
 
 // ------------------------------------------------------------ training pass

@@ -16,6 +16,9 @@
 // Scalars (alpha, beta, convergence) live in device memory, so an iteration
 // is three kernels with no host round trip; the host replays a captured CUDA
 // graph of several iterations and checks the `done` word between replays.
+#include <algorithm>
+
+#include "grid_sync.cuh"
 #include "ipfem_internal.h"
 #include "ldhint.cuh"
 #include "pdl.cuh"
@@ -382,6 +385,109 @@ __global__ void __launch_bounds__(kRedBlock) k_cg_update(int32_t n_nodes, const 
     }
 }
 
+// Partial sums of one 256-node window w (the same canonical tree as
+// block_partials) written to part[k * n_red + w], without a ticket; s is the
+// caller's staging area, free again on return.
+template <class T, int NV>
+__device__ __forceinline__ void window_partials(const T (&v)[NV], T *part, int64_t n_red, int64_t w,
+                                                T (*s)[kRedStage])
+{
+#pragma unroll
+    for (int k = 0; k < NV; k++) s[k][red_stage(threadIdx.x)] = v[k];
+    __syncthreads();
+    const int wp = threadIdx.x >> 5, w0 = (int)(w & 3);
+#pragma unroll
+    for (int k = 0; k < NV; k++)
+        if (wp == ((w0 + 2 * k) & 3)) {
+            const T o = tree256_warp<T>(s[k]);
+            if ((threadIdx.x & 31) == 0) part[k * n_red + w] = o;
+        }
+    __syncthreads();
+}
+
+// One CG iteration's vector work in one cooperative launch: phase 1 is
+// k_cg_update (x += alpha p, r -= alpha q, z = M r, partials of r.r and r.z
+// per 256-node window), a grid barrier whose last CTA runs k_cg_update's
+// epilogue (convergence test, beta), then phase 2 is k_cg_pupdate (p = z +
+// beta p) on the same windows, z kept in shared memory (the first kFuseWin
+// windows of the CTA) or in global memory.  Same operations on the same
+// values as the two kernels: the results are equal bit for bit.  Windows
+// w = blockIdx.x + j gridDim.x; the grid is at most the resident capacity.
+constexpr int kFuseWin = 4;
+
+template <class T, bool BLOCK>
+__global__ void __launch_bounds__(kRedBlock) k_cg_update_p(int32_t n_nodes, int64_t n_win, const T *__restrict__ q,
+                                                           const T *__restrict__ minv, T *__restrict__ x,
+                                                           T *__restrict__ r, T *__restrict__ z, T *p, T *part,
+                                                           int64_t n_red, unsigned *count, unsigned *gen,
+                                                           CGScalarsT<T> *sc, int *err)
+{
+    typedef typename Vec2<T>::type V;
+    __shared__ T s_red[2][kRedStage];
+    __shared__ V s_z[kFuseWin][kRedBlock];
+    const unsigned gen0 = ld_acquire_gpu(gen);     // before this CTA arrives
+    pdl_wait();
+    pdl_launch_dependents();
+    if (*reinterpret_cast<volatile int *>(&sc->done)) return;
+    const T alpha = *reinterpret_cast<volatile T *>(&sc->alpha);
+    int j = 0;
+    for (int64_t w = blockIdx.x; w < n_win; w += gridDim.x, j++) {
+        const int32_t i = (int32_t)(w * kRedBlock) + (int32_t)threadIdx.x;
+        T v[2] = {T(0), T(0)};
+        if (i < n_nodes) {
+            const V pp = reinterpret_cast<const V *>(p)[i], qq = reinterpret_cast<const V *>(q)[i];
+            V xx = reinterpret_cast<V *>(x)[i], rr = reinterpret_cast<V *>(r)[i];
+            xx.x = fma(alpha, pp.x, xx.x);
+            xx.y = fma(alpha, pp.y, xx.y);
+            rr.x = fma(-alpha, qq.x, rr.x);
+            rr.y = fma(-alpha, qq.y, rr.y);
+            const V zz = precondition<T, BLOCK>(minv, i, rr);
+            reinterpret_cast<V *>(x)[i] = xx;
+            reinterpret_cast<V *>(r)[i] = rr;
+            if (j < kFuseWin) s_z[j][threadIdx.x] = zz;
+            else reinterpret_cast<V *>(z)[i] = zz;
+            v[0] = fma(rr.y, rr.y, fma(rr.x, rr.x, T(0)));
+            v[1] = fma(rr.y, zz.y, fma(rr.x, zz.x, T(0)));
+        }
+        window_partials<T, 2>(v, part, n_red, w, s_red);
+    }
+    if (grid_arrive(count)) {
+        T o[2];
+        final_reduce<T, 2>(part, n_red, o);
+        if (threadIdx.x == 0) {
+            const T rr = o[0], rzn = o[1];
+            sc->rr = rr;
+            sc->iters += 1;
+            if (rr <= sc->thr) {
+                sc->done = 1;
+            } else if (sc->iters >= sc->max_it) {
+                sc->done = 1;
+                sc->status = IPFEM_NONCONVERGED;
+            } else {
+                sc->beta = rzn / sc->rz;
+                sc->rz = rzn;
+            }
+        }
+        grid_release(count, gen, gen0);
+    } else if (!grid_wait(gen, gen0, err)) {
+        if (threadIdx.x == 0) atomicExch(&sc->done, 1);
+        return;
+    }
+    if (*reinterpret_cast<volatile int *>(&sc->done)) return;
+    const T beta = *reinterpret_cast<volatile T *>(&sc->beta);
+    j = 0;
+    for (int64_t w = blockIdx.x; w < n_win; w += gridDim.x, j++) {
+        const int32_t i = (int32_t)(w * kRedBlock) + (int32_t)threadIdx.x;
+        if (i < n_nodes) {
+            const V zz = j < kFuseWin ? s_z[j][threadIdx.x] : reinterpret_cast<const V *>(z)[i];
+            V pp = reinterpret_cast<const V *>(p)[i];
+            pp.x = fma(beta, pp.x, zz.x);
+            pp.y = fma(beta, pp.y, zz.y);
+            reinterpret_cast<V *>(p)[i] = pp;
+        }
+    }
+}
+
 // p = z + beta p, kPupNodes nodes per thread (strided by the CTA size) so that
 // each thread has several loads in flight: the kernel moves 48 bytes per node
 // and is bound by memory latency, not bandwidth, at one node per thread
@@ -507,16 +613,21 @@ void launch_spmv(ipfem_ctx *c, const SellDev &L, const T *K, const T *p, T *q, T
                (const T *)p, q, part, c->n_red, ticket, sc);
 }
 
+// cooperative grid of k_cg_update_p: every window once, at most the resident capacity
+static unsigned grid_fused(const ipfem_ctx *c, bool fp64)
+{
+    const int cap = fp64 ? c->coop_cap_cg64 : c->coop_cap_cg32;
+    return (unsigned)std::max<int64_t>(1, std::min<int64_t>(c->n_red, cap));
+}
+
 void launch_cg_iteration(ipfem_ctx *c)
 {
-    const unsigned g = grid_nodes(c);
     launch_spmv<double>(c, c->dsell, c->d_K, c->d_p, c->d_q, c->d_part, c->d_counters + 1, c->d_sc);
     const bool blk = c->preconditioner == IPFEM_PREC_BLOCK_JACOBI;
-    launch_pdl(blk ? k_cg_update<double, true> : k_cg_update<double, false>, g, kRedBlock, c->stream, c->s.n_nodes,
-               (const double *)c->d_p, (const double *)c->d_q, (const double *)(blk ? c->d_binv : c->d_dinv), c->d_x,
-               c->d_r, c->d_z, c->d_part, c->n_red, c->d_counters + 2, c->d_sc);
-    launch_pdl(k_cg_pupdate<double>, grid_pupdate(c), kRedBlock, c->stream, c->s.n_nodes,
-               (const double *)c->d_z, c->d_p, (const CGScalarsT<double> *)c->d_sc);
+    launch_coop(blk ? k_cg_update_p<double, true> : k_cg_update_p<double, false>, grid_fused(c, true), kRedBlock,
+                c->stream, true, c->s.n_nodes, c->n_red, (const double *)c->d_q,
+                (const double *)(blk ? c->d_binv : c->d_dinv), c->d_x, c->d_r, c->d_z, c->d_p, c->d_part, c->n_red,
+                c->d_counters + 8, c->d_counters + 9, c->d_sc, c->d_err);
 }
 
 void launch_cg_spmv_only(ipfem_ctx *c)
@@ -537,14 +648,20 @@ void launch_cg32_init(ipfem_ctx *c, const double *d_b, double scale, float rtol,
 void launch_cg32_iteration(ipfem_ctx *c)
 {
     MixedBuffers &m = c->mx;
-    const unsigned g = grid_nodes(c);
     launch_spmv<float>(c, m.dsell, m.K, m.p, m.q, m.part, c->d_counters + 5, m.sc);
     const bool blk = c->preconditioner == IPFEM_PREC_BLOCK_JACOBI;
-    launch_pdl(blk ? k_cg_update<float, true> : k_cg_update<float, false>, g, kRedBlock, c->stream, c->s.n_nodes,
-               (const float *)m.p, (const float *)m.q, (const float *)(blk ? m.binv : m.dinv), m.x, m.r, m.z, m.part,
-               c->n_red, c->d_counters + 6, m.sc);
-    launch_pdl(k_cg_pupdate<float>, grid_pupdate(c), kRedBlock, c->stream, c->s.n_nodes, (const float *)m.z,
-               m.p, (const CGScalarsT<float> *)m.sc);
+    launch_coop(blk ? k_cg_update_p<float, true> : k_cg_update_p<float, false>, grid_fused(c, false), kRedBlock,
+                c->stream, true, c->s.n_nodes, c->n_red, (const float *)m.q, (const float *)(blk ? m.binv : m.dinv),
+                m.x, m.r, m.z, m.p, m.part, c->n_red, c->d_counters + 10, c->d_counters + 11, m.sc, c->d_err);
+}
+
+void solver_configure(ipfem_ctx *c)
+{
+    c->coop_cap_cg64 = std::min(grid_capacity(k_cg_update_p<double, true>, kRedBlock, 0),
+                                grid_capacity(k_cg_update_p<double, false>, kRedBlock, 0));
+    c->coop_cap_cg32 = std::min(grid_capacity(k_cg_update_p<float, true>, kRedBlock, 0),
+                                grid_capacity(k_cg_update_p<float, false>, kRedBlock, 0));
+    c->coop_cap_fcg = fcg_grid_capacity();
 }
 
 void launch_cg32_spmv_only(ipfem_ctx *c)
