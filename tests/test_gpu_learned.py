@@ -135,10 +135,13 @@ def test_learn_grad_matches_oracle():
         g, loss = sm.learn_grad(rs, E, npair, wk, wp)
         loss_ref, g_ref = orc_mlp.loss_and_grads(sm.mlp_params(), X.cpu().numpy(), matvec, matvec.blocks, gr, gr,
                                                  dinv, rs.cpu().numpy()[:npair], E.cpu().numpy()[:npair], wk, wp)
+        print("loss (wk %g, wp %g): %.6g vs oracle %.6g, rel %.2e" % (wk, wp, loss, loss_ref,
+                                                                     abs(loss - loss_ref) / max(abs(loss_ref), 1e-30)))
         assert loss == pytest.approx(loss_ref, rel=2e-3, abs=1e-5), (wk, wp)
         gd, rd = orc_mlp.unpack(g), orc_mlp.unpack(g_ref)
         for name, _ in orc_mlp.SIZES:
             e = np.linalg.norm(gd[name] - rd[name]) / np.linalg.norm(rd[name])
+            print("  grad %-3s rel %.2e" % (name, e))
             assert e < 2e-2, (wk, wp, name, e)
     # a small Adam step along the gradient lowers the loss
     g, loss = sm.learn_grad(rs, E, len(snaps))
