@@ -970,6 +970,32 @@ ipfem_status ipfem_dot(ipfem_ctx *c, const double *d_a, const double *d_b, doubl
     return dot_host(c, d_a, d_b, out);
 }
 
+ipfem_status ipfem_probe_wait_timeout(ipfem_ctx *c, double *ms)
+{
+    if (!c || !ms) return fail(c, IPFEM_INVALID, "bad args");
+    ipfem_status st = check_device(c);
+    if (st != IPFEM_OK) return st;
+    if (!c->ev_ready) {
+        CK(cudaEventCreate(&c->ev[0]));
+        CK(cudaEventCreate(&c->ev[1]));
+        c->ev_ready = true;
+    }
+    CK(cudaEventRecord(c->ev[0], c->stream));
+    launch_wait_probe(c);
+    CK(cudaGetLastError());
+    CK(cudaEventRecord(c->ev[1], c->stream));
+    CK(cudaEventSynchronize(c->ev[1]));
+    float t = 0.f;
+    CK(cudaEventElapsedTime(&t, c->ev[0], c->ev[1]));
+    *ms = t;
+    int err = 0;
+    CK(cudaMemcpy(&err, c->d_err, sizeof(int), cudaMemcpyDeviceToHost));
+    CK(cudaMemsetAsync(c->d_err, 0, sizeof(int), c->stream));   // the context stays usable
+    CK(cudaStreamSynchronize(c->stream));
+    if (err != kErrGridWait) return fail(c, IPFEM_CUDA, "the bounded grid wait did not report its timeout");
+    return IPFEM_OK;
+}
+
 ipfem_status ipfem_measure_fp64_peak(ipfem_ctx *c, double *tflops)
 {
     if (!c || !tflops) return fail(c, IPFEM_INVALID, "bad args");

@@ -279,6 +279,7 @@ void launch_dot(ipfem_ctx *c, const double *a, const double *b, double *d_out);
 void launch_axpy_u(ipfem_ctx *c, double *d_u, const double *d_du);
 void launch_scale_add(ipfem_ctx *c, double *d_u, const double *d_x, double alpha, double *d_t);
 void launch_fp64_probe(ipfem_ctx *c, double *d_out, int grid, int iters);
+void launch_wait_probe(ipfem_ctx *c);
 void launch_stiffness32(ipfem_ctx *c);
 // recomputes the Jacobi (and, when allocated, block-Jacobi) inverses of the current tangent
 void launch_jacobi(ipfem_ctx *c);

@@ -559,6 +559,19 @@ __global__ void __launch_bounds__(256) k_fp64_probe(double *out, int iters, doub
     out[blockIdx.x * blockDim.x + threadIdx.x] = ((x0 + x1) + (x2 + x3)) + ((x4 + x5) + (x6 + x7));
 }
 
+// One CTA waits at a grid barrier that no CTA releases (the generation word
+// is never written): the bounded wait must give up and record kErrGridWait.
+__global__ void k_wait_probe(const unsigned *gen, int *err)
+{
+    const unsigned g0 = ld_acquire_gpu(gen);
+    grid_wait(gen, g0, err);
+}
+
+void launch_wait_probe(ipfem_ctx *c)
+{
+    k_wait_probe<<<1, 32, 0, c->stream>>>(c->d_counters + 14, c->d_err);
+}
+
 void launch_fp64_probe(ipfem_ctx *c, double *d_out, int grid, int iters)
 {
     k_fp64_probe<<<grid, 256, 0, c->stream>>>(d_out, iters, 0.999, 0.001);
