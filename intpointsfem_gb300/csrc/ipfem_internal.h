@@ -286,7 +286,6 @@ void launch_jacobi(ipfem_ctx *c);
 void launch_cg32_init(ipfem_ctx *c, const double *d_b, double scale, float rtol, int max_it);
 void launch_cg32_iteration(ipfem_ctx *c);
 void launch_cg32_spmv_only(ipfem_ctx *c);
-void launch_cg32_pupdate_only(ipfem_ctx *c);
 // resident capacity of the cooperative solver kernels on the context's device
 void solver_configure(ipfem_ctx *c);
 int fcg_grid_capacity();

@@ -402,30 +402,26 @@ __global__ void __launch_bounds__(256) k_tri_precond(int32_t n, GridInfo G, cons
     }
 }
 
-// ----------------------------------------- fused flexible-CG iteration (FP32)
-// One iteration = k_fcg_spmv, k_fcg_update_first, k_tri_precond (factor in
-// BF16), with the
-// search direction and the residual double-buffered (the caller alternates
-// the buffers): the p-update of the previous iteration is formed on the fly
-// inside the SpMV, the x/r update inside the first factor pass.
+// ----------------------------------------- flexible-CG iteration (FP32)
+// One iteration = two launches: k_fcg_spmv_p (q = K p, p.q, alpha) and the
+// cooperative k_fcg_update_precond (x/r update and first factor pass, grid
+// barrier, second factor pass with r.z and r_old.z, grid barrier for beta,
+// p = z + beta p).  The residual is double-buffered (the caller alternates
+// the buffers: the first factor pass reads r_old at the lower neighbours).
 
-// p_new = z + beta p_old (the owner stores it, gatherers form it for their
-// columns), q = K p_new, partials of p_new.q; last CTA: alpha = rz / pq.
-// Node-ordered SELL rows; the tangent and its column indices are streamed
-// (evict-first) so that z and p_old stay in L2.
+// q = K p, partials of p.q; last CTA: alpha = rz / pq.  Each block column
+// gathers p alone (the tangent and the column indices are streamed
+// evict-first so that p stays in L2).
 template <bool PAT>
-__global__ void __launch_bounds__(256, 8) k_fcg_spmv(int32_t n, const int64_t *__restrict__ slice_base,
-                                                  const int32_t *__restrict__ rowlen, const int32_t *__restrict__ scol,
-                                                  const uint8_t *__restrict__ pat_id,
-                                                  const int32_t *__restrict__ pat_off,
-                                                  const float4 *__restrict__ K, const uint8_t *__restrict__ fixed,
-                                                  const float2 *__restrict__ z, const float2 *__restrict__ p_old,
-                                                  float2 *__restrict__ p_new, float2 *__restrict__ q, float *part,
-                                                  int64_t n_part, unsigned *ticket, CGScalarsT<float> *sc)
+__global__ void __launch_bounds__(256, 8) k_fcg_spmv_p(int32_t n, const int64_t *__restrict__ slice_base,
+                                                    const int32_t *__restrict__ rowlen,
+                                                    const int32_t *__restrict__ scol, const uint8_t *__restrict__ pat_id,
+                                                    const int32_t *__restrict__ pat_off,
+                                                    const float4 *__restrict__ K, const uint8_t *__restrict__ fixed,
+                                                    const float2 *__restrict__ p, float2 *__restrict__ q, float *part,
+                                                    int64_t n_part, unsigned *ticket, CGScalarsT<float> *sc)
 {
     const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    // row metadata before the wait; z, beta and the flag (written by the
-    // preconditioner pass) after it
     int64_t base = 0;
     int len = 0, pb = 0;
     if (i < n) {
@@ -436,7 +432,6 @@ __global__ void __launch_bounds__(256, 8) k_fcg_spmv(int32_t n, const int64_t *_
     pdl_wait();
     pdl_launch_dependents();
     if (*reinterpret_cast<volatile int *>(&sc->done)) return;
-    const float beta = *reinterpret_cast<volatile float *>(&sc->beta);
     float v[1] = {0.f};
     if (i < n) {
         const uint64_t keep = l2_policy_keep();
@@ -446,17 +441,14 @@ __global__ void __launch_bounds__(256, 8) k_fcg_spmv(int32_t n, const int64_t *_
             const int64_t s = base + sell_koff<true>(k);
             const int32_t c = PAT ? i + __ldg(&pat_off[pb + k]) : __ldcs(&scol[s]);
             const float4 a = __ldcs(&K[s]);
-            const float2 zz = ld_keep(&z[c], keep), pp = ld_keep(&p_old[c], keep);
-            const float px = fmaf(beta, pp.x, zz.x), py = fmaf(beta, pp.y, zz.y);
-            y0 = fmaf(a.y, py, fmaf(a.x, px, y0));
-            y1 = fmaf(a.w, py, fmaf(a.z, px, y1));
+            const float2 pp = ld_keep(&p[c], keep);
+            y0 = fmaf(a.y, pp.y, fmaf(a.x, pp.x, y0));
+            y1 = fmaf(a.w, pp.y, fmaf(a.z, pp.x, y1));
         }
         if (fixed[2 * (int64_t)i]) y0 = 0.f;
         if (fixed[2 * (int64_t)i + 1]) y1 = 0.f;
         q[i] = make_float2(y0, y1);
-        const float2 zi = z[i], pi = p_old[i];
-        const float2 pn = make_float2(fmaf(beta, pi.x, zi.x), fmaf(beta, pi.y, zi.y));
-        p_new[i] = pn;
+        const float2 pn = p[i];
         v[0] = fmaf(pn.y, y1, pn.x * y0);
     }
     if (fcg_partials<1>(v, part, n_part, ticket)) {
@@ -476,81 +468,15 @@ __global__ void __launch_bounds__(256, 8) k_fcg_spmv(int32_t n, const int64_t *_
     }
 }
 
-// x += alpha p, r_new = r_old - alpha q (the owner stores it, the factor
-// pass forms it for its neighbours), y = G (sigma * r_new); partials of
-// r_new.r_new; last CTA: convergence, stagnation and iteration limit
-__global__ void __launch_bounds__(256, 8) k_fcg_update_first(int32_t n, GridInfo G, const uint2 *__restrict__ Gm,
-                                                          const float2 *__restrict__ dinv,
-                                                          const float2 *__restrict__ p, const float2 *__restrict__ q,
-                                                          float2 *__restrict__ x, const float2 *__restrict__ r_old,
-                                                          float2 *__restrict__ r_new, float2 *__restrict__ y,
-                                                          float *part, int64_t n_part, unsigned *ticket,
-                                                          CGScalarsT<float> *sc, int stall_window)
+// p = z + beta p (the first search direction of a solve: beta = 0, p = 0)
+__global__ void __launch_bounds__(256) k_fcg_pinit(int32_t n, const float2 *__restrict__ z, float2 *__restrict__ p,
+                                                   const CGScalarsT<float> *sc)
 {
     const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    // x and r_old (not written by the SpMV) before the wait; p, q, alpha and
-    // the flag after it
-    float2 xx = make_float2(0.f, 0.f), ro[NTRI];
-    int32_t jn[NTRI];
-    if (i < n) {
-        xx = x[i];
-#pragma unroll
-        for (int k = 0; k < NTRI; k++) {
-            jn[k] = patch_nbr(i, k, G);
-            if (jn[k] >= 0) ro[k] = __ldg(&r_old[jn[k]]);
-        }
-    }
-    pdl_wait();
-    pdl_launch_dependents();
-    if (*reinterpret_cast<volatile int *>(&sc->done)) return;
-    const float alpha = *reinterpret_cast<volatile float *>(&sc->alpha);
-    float v[1] = {0.f};
-    if (i < n) {
-        const float2 pp = p[i];
-        xx.x = fmaf(alpha, pp.x, xx.x);
-        xx.y = fmaf(alpha, pp.y, xx.y);
-        x[i] = xx;
-        float2 acc = make_float2(0.f, 0.f);
-#pragma unroll
-        for (int k = 0; k < NTRI; k++) {
-            if (jn[k] < 0) continue;
-            const float2 qq = __ldg(&q[jn[k]]);
-            const float2 rn = make_float2(fmaf(-alpha, qq.x, ro[k].x), fmaf(-alpha, qq.y, ro[k].y));
-            if (k == 4) {
-                r_new[i] = rn;
-                v[0] = fmaf(rn.y, rn.y, rn.x * rn.x);
-            }
-            const float4 m = load_g(Gm, (int64_t)k * n + i);
-            const float2 sg = sqrt2(__ldg(&dinv[jn[k]]));
-            const float vx = sg.x * rn.x, vy = sg.y * rn.y;
-            acc.x = fmaf(m.x, vx, fmaf(m.y, vy, acc.x));
-            acc.y = fmaf(m.z, vx, fmaf(m.w, vy, acc.y));
-        }
-        y[i] = acc;
-    }
-    if (fcg_partials<1>(v, part, n_part, ticket)) {
-        float o[1];
-        fcg_final<1>(part, n_part, o);
-        if (threadIdx.x == 0) {
-            const float rr = o[0];
-            sc->rr = rr;
-            sc->iters += 1;
-            if (rr < 0.98f * sc->rr_best) {
-                sc->rr_best = rr;
-                sc->it_best = sc->iters;
-            }
-            if (rr <= sc->thr) {
-                sc->done = 1;
-            } else if (!(rr == rr) || sc->iters - sc->it_best > max(stall_window, sc->it_best)) {
-                sc->done = 1;
-                sc->status = kStatusFallback;
-            } else if (sc->iters >= sc->max_it) {
-                sc->done = 1;
-                sc->status = IPFEM_NONCONVERGED;
-            }
-            *ticket = 0u;
-        }
-    }
+    if (i >= n || *reinterpret_cast<const volatile int *>(&sc->done)) return;
+    const float beta = sc->beta;
+    const float2 zz = z[i], pp = p[i];
+    p[i] = make_float2(fmaf(beta, pp.x, zz.x), fmaf(beta, pp.y, zz.y));
 }
 
 // Partials of one 256-node window w, the sums of fcg_partials (warp trees,
@@ -577,25 +503,29 @@ __device__ __forceinline__ void fcg_window_partials(const float (&v)[NV], float 
     __syncthreads();
 }
 
-// The two vector passes of a flexible-CG iteration in one cooperative
-// launch: phase 1 is k_fcg_update_first (x += alpha p, r_new, y = G (sigma
-// r_new), r_new.r_new per window), a grid barrier whose last CTA runs its
-// epilogue (convergence, stagnation, iteration limit), phase 2 is
-// k_tri_precond (z = sigma G^T y, r.z and r_old.z per window) and a last-CTA
-// epilogue (beta).  The same operations on the same values, and the same
-// per-window partials in the same order, as the two kernels: equal results
-// bit for bit.  Windows w = blockIdx.x + j gridDim.x.
+// The vector work of a flexible-CG iteration in one cooperative launch:
+// phase 1: x += alpha p, r_new = r_old - alpha q at the node and its lower
+// neighbours, y = G (sigma r_new), r_new.r_new per 256-node window; a grid
+// barrier whose last CTA tests convergence, stagnation and the iteration
+// limit; phase 2: z = sigma G^T y (y of the upper neighbours, read through
+// L2), r.z and r_old.z per window; a grid barrier whose last CTA forms the
+// Polak-Ribiere beta; phase 3: p = z + beta p.  Windows w = blockIdx.x +
+// j gridDim.x; z of the CTA's first windows stays in shared memory.
+constexpr int kFcgFuseWin = 4;   // windows per CTA whose z stays in shared memory for phase 3
+
 __global__ void __launch_bounds__(256, 8) k_fcg_update_precond(int32_t n, int64_t n_win, GridInfo G,
                                                             const uint2 *__restrict__ Gm, const float2 *__restrict__ dinv,
-                                                            const float2 *__restrict__ p, const float2 *__restrict__ q,
+                                                            float2 *p, const float2 *__restrict__ q,
                                                             float2 *__restrict__ x, const float2 *__restrict__ r_old,
                                                             float2 *__restrict__ r_new, float2 *__restrict__ y,
                                                             float *__restrict__ z, float *part, float *part2,
                                                             int64_t n_part, unsigned *count, unsigned *gen,
-                                                            unsigned *count2, CGScalarsT<float> *sc, int stall_window,
-                                                            int *err)
+                                                            unsigned *count2, unsigned *gen2, CGScalarsT<float> *sc,
+                                                            int stall_window, int *err)
 {
+    __shared__ float2 s_z[kFcgFuseWin][256];
     const unsigned gen0 = ld_acquire_gpu(gen);     // before this CTA arrives
+    const unsigned gen20 = ld_acquire_gpu(gen2);
     pdl_wait();
     pdl_launch_dependents();
     if (*reinterpret_cast<volatile int *>(&sc->done)) return;
@@ -658,12 +588,14 @@ __global__ void __launch_bounds__(256, 8) k_fcg_update_precond(int32_t n, int64_
         return;
     }
     if (*reinterpret_cast<volatile int *>(&sc->done)) return;
-    for (int64_t w = blockIdx.x; w < n_win; w += gridDim.x) {
+    int j = 0;
+    for (int64_t w = blockIdx.x; w < n_win; w += gridDim.x, j++) {
         const int32_t i = (int32_t)(w * 256) + (int32_t)threadIdx.x;
         float v[2] = {0.f, 0.f};
         if (i < n) {
             const float2 zz = trit_mul<uint2, true>(i, n, G, Gm, dinv, y);
-            reinterpret_cast<float2 *>(z)[i] = zz;
+            if (j < kFcgFuseWin) s_z[j][threadIdx.x] = zz;
+            else reinterpret_cast<float2 *>(z)[i] = zz;
             const float2 rr = r_new[i], ro = r_old[i];
             v[0] = fmaf(rr.y, zz.y, rr.x * zz.x);
             v[1] = fmaf(ro.y, zz.y, ro.x * zz.x);
@@ -683,7 +615,22 @@ __global__ void __launch_bounds__(256, 8) k_fcg_update_precond(int32_t n, int64_
                 sc->done = 1;
                 sc->status = kStatusFallback;
             }
-            *count2 = 0u;
+        }
+        grid_release(count2, gen2, gen20);
+    } else if (!grid_wait(gen2, gen20, err)) {
+        if (threadIdx.x == 0) atomicExch(&sc->done, 1);
+        return;
+    }
+    // phase 3: the next search direction p = z + beta p (the next SpMV gathers p alone)
+    if (*reinterpret_cast<volatile int *>(&sc->done)) return;
+    const float beta = *reinterpret_cast<volatile float *>(&sc->beta);
+    j = 0;
+    for (int64_t w = blockIdx.x; w < n_win; w += gridDim.x, j++) {
+        const int32_t i = (int32_t)(w * 256) + (int32_t)threadIdx.x;
+        if (i < n) {
+            const float2 zz = j < kFcgFuseWin ? s_z[j][threadIdx.x] : reinterpret_cast<const float2 *>(z)[i];
+            const float2 pp = p[i];
+            p[i] = make_float2(fmaf(beta, pp.x, zz.x), fmaf(beta, pp.y, zz.y));
         }
     }
 }
@@ -1044,10 +991,12 @@ void launch_fcg_init(ipfem_ctx *c, const double *d_b, double scale, float rtol, 
     k_fcg_init<<<fcg_grid(c), 256, 0, c->stream>>>(c->s.n_nodes, d_b, scale, m.x, m.r, m.p, c->mlp.r_old, m.part,
                                                    (int64_t)fcg_grid(c), c->d_counters + 4, m.sc, rtol, max_it);
     launch_precond(c, 0);
+    k_fcg_pinit<<<fcg_grid(c), 256, 0, c->stream>>>(c->s.n_nodes, reinterpret_cast<const float2 *>(m.z),
+                                                    reinterpret_cast<float2 *>(m.p), m.sc);
 }
 
-// iteration k (par = k % 2): P[par] -> P[1-par] in the SpMV, R[par] -> R[1-par]
-// in the update, z from R[1-par]
+// iteration k (par = k % 2): R[par] -> R[1-par] in the vector kernel; p is
+// updated in place at its end (z from R[1-par])
 void launch_fcg_iteration(ipfem_ctx *c, int par)
 {
     MixedBuffers &m = c->mx;
@@ -1055,22 +1004,22 @@ void launch_fcg_iteration(ipfem_ctx *c, int par)
     const SellDev &L = m.dsell;
     GridInfo G{l.gr, l.gt};
     const int32_t n = c->s.n_nodes;
-    float2 *P[2] = {reinterpret_cast<float2 *>(m.p), reinterpret_cast<float2 *>(l.p2)};
     float2 *R[2] = {reinterpret_cast<float2 *>(m.r), reinterpret_cast<float2 *>(l.r_old)};
     const float2 *d2 = reinterpret_cast<const float2 *>(m.dinv);
     float *part = m.part;
-    launch_pdl(use_row_stencils(c, L) ? k_fcg_spmv<true> : k_fcg_spmv<false>, fcg_grid(c), 256, c->stream, n,
+    float2 *p = reinterpret_cast<float2 *>(m.p);
+    launch_pdl(use_row_stencils(c, L) ? k_fcg_spmv_p<true> : k_fcg_spmv_p<false>, fcg_grid(c), 256, c->stream, n,
                (const int64_t *)L.slice_base, (const int32_t *)L.rowlen, (const int32_t *)L.sell_col,
                (const uint8_t *)L.pat_id, (const int32_t *)L.pat_off, reinterpret_cast<const float4 *>(m.K),
-               (const uint8_t *)c->d_fixed, reinterpret_cast<const float2 *>(m.z), (const float2 *)P[par],
-               P[1 - par], reinterpret_cast<float2 *>(m.q), part, (int64_t)fcg_grid(c), c->d_counters + 5, m.sc);
+               (const uint8_t *)c->d_fixed, (const float2 *)p, reinterpret_cast<float2 *>(m.q), part,
+               (int64_t)fcg_grid(c), c->d_counters + 5, m.sc);
     float *part2 = reinterpret_cast<float *>(c->d_part);
     const int64_t n_win = fcg_grid(c);
     launch_coop(k_fcg_update_precond, (unsigned)std::max<int64_t>(1, std::min<int64_t>(n_win, c->coop_cap_fcg)), 256,
-                c->stream, true, n, n_win, G, reinterpret_cast<const uint2 *>(l.Gh), d2, (const float2 *)P[1 - par],
+                c->stream, true, n, n_win, G, reinterpret_cast<const uint2 *>(l.Gh), d2, p,
                 reinterpret_cast<const float2 *>(m.q), reinterpret_cast<float2 *>(m.x), (const float2 *)R[par],
                 R[1 - par], reinterpret_cast<float2 *>(l.y), m.z, part, part2, n_win, c->d_counters + 12,
-                c->d_counters + 13, c->d_counters + 7, m.sc, stall_window(c), c->d_err);
+                c->d_counters + 13, c->d_counters + 7, c->d_counters + 15, m.sc, stall_window(c), c->d_err);
 }
 
 int fcg_grid_capacity()

@@ -329,62 +329,6 @@ __global__ void __launch_bounds__(kRedBlock) k_cg_spmv(int32_t n_nodes, const in
     }
 }
 
-// x += alpha p, r -= alpha q, z = M r; partials of r.r and r.z;
-// last CTA: convergence test, beta
-template <class T, bool BLOCK>
-__global__ void __launch_bounds__(kRedBlock) k_cg_update(int32_t n_nodes, const T *__restrict__ p,
-                                                         const T *__restrict__ q, const T *__restrict__ dinv,
-                                                         T *__restrict__ x, T *__restrict__ r, T *__restrict__ z,
-                                                         T *part, int64_t n_red, unsigned *ticket, CGScalarsT<T> *sc)
-{
-    typedef typename Vec2<T>::type V;
-    const int32_t i = blockIdx.x * kRedBlock + threadIdx.x;
-    // p, x and r (not written by the SpMV) before the wait, q after it
-    V pp, qq, xx, rr;
-    if (i < n_nodes) {
-        pp = reinterpret_cast<const V *>(p)[i];
-        xx = reinterpret_cast<V *>(x)[i];
-        rr = reinterpret_cast<V *>(r)[i];
-    }
-    pdl_wait();
-    pdl_launch_dependents();
-    if (i < n_nodes) qq = reinterpret_cast<const V *>(q)[i];
-    if (*reinterpret_cast<volatile int *>(&sc->done)) return;
-    const T alpha = *reinterpret_cast<volatile T *>(&sc->alpha);
-    T v[2] = {T(0), T(0)};
-    if (i < n_nodes) {
-        xx.x = fma(alpha, pp.x, xx.x);
-        xx.y = fma(alpha, pp.y, xx.y);
-        rr.x = fma(-alpha, qq.x, rr.x);
-        rr.y = fma(-alpha, qq.y, rr.y);
-        const V zz = precondition<T, BLOCK>(dinv, i, rr);
-        reinterpret_cast<V *>(x)[i] = xx;
-        reinterpret_cast<V *>(r)[i] = rr;
-        reinterpret_cast<V *>(z)[i] = zz;
-        v[0] = fma(rr.y, rr.y, fma(rr.x, rr.x, T(0)));
-        v[1] = fma(rr.y, zz.y, fma(rr.x, zz.x, T(0)));
-    }
-    if (block_partials<T, 2>(v, part, n_red, ticket)) {
-        T o[2];
-        final_reduce<T, 2>(part, n_red, o);
-        if (threadIdx.x == 0) {
-            const T rr = o[0], rzn = o[1];
-            sc->rr = rr;
-            sc->iters += 1;
-            if (rr <= sc->thr) {
-                sc->done = 1;
-            } else if (sc->iters >= sc->max_it) {
-                sc->done = 1;
-                sc->status = IPFEM_NONCONVERGED;
-            } else {
-                sc->beta = rzn / sc->rz;
-                sc->rz = rzn;
-            }
-            *ticket = 0u;
-        }
-    }
-}
-
 // Partial sums of one 256-node window w (the same canonical tree as
 // block_partials) written to part[k * n_red + w], without a ticket; s is the
 // caller's staging area, free again on return.
@@ -488,38 +432,6 @@ __global__ void __launch_bounds__(kRedBlock) k_cg_update_p(int32_t n_nodes, int6
     }
 }
 
-// p = z + beta p, kPupNodes nodes per thread (strided by the CTA size) so that
-// each thread has several loads in flight: the kernel moves 48 bytes per node
-// and is bound by memory latency, not bandwidth, at one node per thread
-constexpr int kPupNodes = 4;
-
-template <class T>
-__global__ void __launch_bounds__(kRedBlock) k_cg_pupdate(int32_t n_nodes, const T *__restrict__ z,
-                                                          T *__restrict__ p, const CGScalarsT<T> *sc)
-{
-    typedef typename Vec2<T>::type V;
-    const int32_t i0 = blockIdx.x * (kRedBlock * kPupNodes) + threadIdx.x;
-    // p (not written by the update) before the wait, z after it
-    V pp[kPupNodes], zz[kPupNodes];
-#pragma unroll
-    for (int j = 0; j < kPupNodes; j++)
-        if (i0 + j * kRedBlock < n_nodes) pp[j] = reinterpret_cast<V *>(p)[i0 + j * kRedBlock];
-    pdl_wait();
-    pdl_launch_dependents();
-#pragma unroll
-    for (int j = 0; j < kPupNodes; j++)
-        if (i0 + j * kRedBlock < n_nodes) zz[j] = reinterpret_cast<const V *>(z)[i0 + j * kRedBlock];
-    if (*reinterpret_cast<const volatile int *>(&sc->done)) return;
-    const T beta = *reinterpret_cast<const volatile T *>(&sc->beta);
-#pragma unroll
-    for (int j = 0; j < kPupNodes; j++)
-        if (i0 + j * kRedBlock < n_nodes) {
-            pp[j].x = fma(beta, pp[j].x, zz[j].x);
-            pp[j].y = fma(beta, pp[j].y, zz[j].y);
-            reinterpret_cast<V *>(p)[i0 + j * kRedBlock] = pp[j];
-        }
-}
-
 __global__ void __launch_bounds__(kRedBlock) k_dot(int32_t n_nodes, const double *__restrict__ a,
                                                    const double *__restrict__ b, double *part, int64_t n_red,
                                                    unsigned *ticket, double *out)
@@ -608,11 +520,6 @@ void launch_cg_init(ipfem_ctx *c, const double *d_b, double rtol, int max_it)
                                                                   c->d_counters + 0, c->d_sc, rtol, max_it);
 }
 
-static unsigned grid_pupdate(const ipfem_ctx *c)
-{
-    return (unsigned)((c->s.n_nodes + kRedBlock * kPupNodes - 1) / (kRedBlock * kPupNodes));
-}
-
 template <class T>
 void launch_spmv(ipfem_ctx *c, const SellDev &L, const T *K, const T *p, T *q, T *part, unsigned *ticket,
                  CGScalarsT<T> *sc)
@@ -681,12 +588,6 @@ void launch_cg32_spmv_only(ipfem_ctx *c)
 {
     MixedBuffers &m = c->mx;
     launch_spmv<float>(c, m.dsell, m.K, m.p, m.q, m.part, c->d_counters + 5, m.sc);
-}
-
-void launch_cg32_pupdate_only(ipfem_ctx *c)
-{
-    MixedBuffers &m = c->mx;
-    k_cg_pupdate<float><<<grid_pupdate(c), kRedBlock, 0, c->stream>>>(c->s.n_nodes, m.z, m.p, m.sc);
 }
 
 void launch_add_scaled32(ipfem_ctx *c, double *d_u, const float *x, double scale)
