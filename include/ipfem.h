@@ -358,12 +358,6 @@ uint64_t ipfem_launch_count(const ipfem_ctx *ctx);
 /* average duration of the CG block SpMV on the current tangent, timed with
  * CUDA events on the context's stream over `reps` back-to-back launches */
 ipfem_status ipfem_profile_spmv(ipfem_ctx *ctx, int reps, double *ms_per_launch);
-/* Self-test of the bounded device waits: one CTA waits at a grid barrier
- * that nothing releases; the wait must give up after its limit (about a
- * second) and record the timeout, which this call reads and clears, so the
- * context stays usable.  *ms receives the time until the wait gave up.
- * IPFEM_OK when the timeout was reported as designed. */
-ipfem_status ipfem_probe_wait_timeout(ipfem_ctx *ctx, double *ms);
 /* FP64 fma issue rate of this device (TFLOP/s, 2 flops per fma), measured with
  * a dependent-chain probe kernel timed by CUDA events */
 ipfem_status ipfem_measure_fp64_peak(ipfem_ctx *ctx, double *tflops);

@@ -123,7 +123,6 @@ def lib():
             "ipfem_set_iteration_log": (S, [P, C.c_char_p]),
             "ipfem_profile_spmv": (S, [P, S, _dp]),
             "ipfem_measure_fp64_peak": (S, [P, _dp]),
-            "ipfem_probe_wait_timeout": (S, [P, _dp]),
             "ipfem_set_node_grid": (S, [P, C.c_int32, C.c_int32]),
             "ipfem_mlp_init": (S, [P, C.c_uint64]),
             "ipfem_set_preconditioner": (S, [P, S]),
@@ -566,13 +565,6 @@ class ElastoPlasticIntPointsStructMatrix:
                                              si.ctypes.data_as(_ip), _ptr(d_xs), _ptr(d_rs), _ptr(d_xfinal),
                                              C.byref(it)))
         return it.value
-
-    def probe_wait_timeout(self):
-        """ms until a grid wait that nothing releases gave up (its timeout is
-        read and cleared; raises if it was not reported)"""
-        out = np.zeros(1)
-        self._check(lib().ipfem_probe_wait_timeout(self._ctx, _np_ptr(out, _dp)))
-        return float(out[0])
 
     def measure_fp64_peak(self):
         out = np.zeros(1)

@@ -19,7 +19,7 @@ INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 
 CU = ["k_constitutive.cu", "k_assembly.cu", "k_solver.cu", "k_mlp.cu", "k_net_tc.cu", "capi_mlp.cu"]
 CPP = ["capi.cpp", "host_setup.cpp", "host_gmsh.cpp"]
-HEADERS = ["ipfem_internal.h", "constitutive.cuh", "tma.cuh", "pdl.cuh", "ldhint.cuh", "grid_sync.cuh"]
+HEADERS = ["ipfem_internal.h", "constitutive.cuh", "tma.cuh", "pdl.cuh", "ldhint.cuh"]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 

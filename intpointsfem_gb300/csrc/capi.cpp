@@ -136,8 +136,8 @@ ipfem_status check_device(ipfem_ctx *c)
     CK(cudaStreamSynchronize(c->stream));
     std::memcpy(&err, &c->h_pin[7], sizeof(int));
     if (err)
-        return fail(c, IPFEM_CUDA, err == kErrGridWait ? "device wait timed out (grid barrier of a solver kernel)"
-                                                      : "device wait timed out (bulk copy did not complete)");
+        return fail(c, IPFEM_CUDA, err == kErrBulkWait ? "device wait timed out (bulk copy did not complete)"
+                                                      : "device wait timed out (tensor-core pipeline)");
     return IPFEM_OK;
 }
 
@@ -211,7 +211,7 @@ ipfem_status cg_device(ipfem_ctx *c, const double *d_b, double rtol, int max_it,
     for (;;) {
         CK(cudaGraphLaunch(c->cg_exec, c->stream));
         launched += batch;
-        c->launches += 2 * batch;
+        c->launches += 3 * batch;
         CK(cudaMemcpyAsync(c->h_sc, c->d_sc, sizeof(CGScalars), cudaMemcpyDeviceToHost, c->stream));
         CK(cudaStreamSynchronize(c->stream));
         if (c->h_sc->done || launched >= max_it + batch) break;
@@ -247,7 +247,7 @@ ipfem_status cg32_device(ipfem_ctx *c, const double *d_b, double scale, double r
     for (;;) {
         CK(cudaGraphLaunch(m.exec, c->stream));
         launched += batch;
-        c->launches += 2 * batch;
+        c->launches += 3 * batch;
         CK(cudaMemcpyAsync(m.h_sc, m.sc, sizeof(CGScalarsT<float>), cudaMemcpyDeviceToHost, c->stream));
         CK(cudaStreamSynchronize(c->stream));
         if (m.h_sc->done || launched >= max_it + batch) break;
@@ -424,11 +424,6 @@ ipfem_status ipfem_create(const ipfem_mesh *mesh, const ipfem_material *mat, ipf
         return bail(st);
     }
     ck(cudaMemsetAsync(c->d_counters, 0, 16 * sizeof(unsigned), t));
-    solver_configure(c);
-    if (c->coop_cap_cg64 <= 0 || c->coop_cap_cg32 <= 0 || c->coop_cap_fcg <= 0) {
-        c->err = "occupancy query of the solver kernels failed";
-        return bail(IPFEM_CUDA);
-    }
     ck(cudaMemsetAsync(c->d_err, 0, sizeof(int), t));
     ck(cudaMemsetAsync(c->d_sc, 0, sizeof(CGScalars), t));
     ck(cudaMemsetAsync(c->d_u, 0, (size_t)s.neq * sizeof(double), t));
@@ -968,32 +963,6 @@ ipfem_status ipfem_dot(ipfem_ctx *c, const double *d_a, const double *d_b, doubl
     if ((reinterpret_cast<uintptr_t>(d_a) | reinterpret_cast<uintptr_t>(d_b)) & 15u)
         return fail(c, IPFEM_INVALID, "ipfem_dot: d_a and d_b must be 16-byte aligned");
     return dot_host(c, d_a, d_b, out);
-}
-
-ipfem_status ipfem_probe_wait_timeout(ipfem_ctx *c, double *ms)
-{
-    if (!c || !ms) return fail(c, IPFEM_INVALID, "bad args");
-    ipfem_status st = check_device(c);
-    if (st != IPFEM_OK) return st;
-    if (!c->ev_ready) {
-        CK(cudaEventCreate(&c->ev[0]));
-        CK(cudaEventCreate(&c->ev[1]));
-        c->ev_ready = true;
-    }
-    CK(cudaEventRecord(c->ev[0], c->stream));
-    launch_wait_probe(c);
-    CK(cudaGetLastError());
-    CK(cudaEventRecord(c->ev[1], c->stream));
-    CK(cudaEventSynchronize(c->ev[1]));
-    float t = 0.f;
-    CK(cudaEventElapsedTime(&t, c->ev[0], c->ev[1]));
-    *ms = t;
-    int err = 0;
-    CK(cudaMemcpy(&err, c->d_err, sizeof(int), cudaMemcpyDeviceToHost));
-    CK(cudaMemsetAsync(c->d_err, 0, sizeof(int), c->stream));   // the context stays usable
-    CK(cudaStreamSynchronize(c->stream));
-    if (err != kErrGridWait) return fail(c, IPFEM_CUDA, "the bounded grid wait did not report its timeout");
-    return IPFEM_OK;
 }
 
 ipfem_status ipfem_measure_fp64_peak(ipfem_ctx *c, double *tflops)

@@ -120,14 +120,14 @@ ipfem_status fcg_device(ipfem_ctx *c, const double *d_b, double scale, double rt
     for (;;) {
         MK(cudaGraphLaunch(c->fcg_exec, c->stream));
         launched += batch;
-        c->launches += 2 * batch;
+        c->launches += 3 * batch;
         MK(cudaMemcpyAsync(m.h_sc, m.sc, sizeof(CGScalarsT<float>), cudaMemcpyDeviceToHost, c->stream));
         MK(cudaStreamSynchronize(c->stream));
         if (m.h_sc->done || launched >= max_it + batch) break;
     }
     MK(cudaGetLastError());
     {
-        // a bounded device wait that gave up (grid barrier) is an error, not a result
+        // a bounded device wait that gave up is an error, not a result
         const ipfem_status e = check_device(c);
         if (e != IPFEM_OK) return e;
     }

@@ -32,8 +32,7 @@ struct CGScalarsT {
 };
 constexpr int kStatusFallback = 9;   // flexible CG stagnated: the caller falls back to Jacobi-PCG
 // codes of the device error word (bounded waits that gave up)
-constexpr int kErrBulkWait = 1;      // a bulk (TMA) copy did not complete
-constexpr int kErrGridWait = 2;      // a grid barrier of a cooperative solver kernel
+constexpr int kErrBulkWait = 1;      // a bulk (TMA) copy did not complete (3: a tensor-core pipeline wait)
 typedef CGScalarsT<double> CGScalars;
 
 // SELL-32 layout of the nodal 2x2 block pattern: row position t of slice
@@ -246,7 +245,6 @@ struct ipfem_ctx {
     cudaGraphExec_t fcg_exec = nullptr;
     int64_t fcg_fallbacks = 0;
     FILE *iter_log = nullptr;            // JSON-lines record of the Newton iterations (ipfem_set_iteration_log)
-    int coop_cap_cg64 = 0, coop_cap_cg32 = 0, coop_cap_fcg = 0;   // resident capacity of the cooperative solver kernels
     int res32 = 0;                       // FP32 residual evaluations in IPFEM_MIXED (ipfem_set_residual_precision)
     int res32_active = 0;                // the residuals being evaluated now are FP32
     double res32_switch = 1e-5;          // |R| / |R0| below which a load step refines with FP64 residuals
@@ -279,16 +277,13 @@ void launch_dot(ipfem_ctx *c, const double *a, const double *b, double *d_out);
 void launch_axpy_u(ipfem_ctx *c, double *d_u, const double *d_du);
 void launch_scale_add(ipfem_ctx *c, double *d_u, const double *d_x, double alpha, double *d_t);
 void launch_fp64_probe(ipfem_ctx *c, double *d_out, int grid, int iters);
-void launch_wait_probe(ipfem_ctx *c);
 void launch_stiffness32(ipfem_ctx *c);
 // recomputes the Jacobi (and, when allocated, block-Jacobi) inverses of the current tangent
 void launch_jacobi(ipfem_ctx *c);
 void launch_cg32_init(ipfem_ctx *c, const double *d_b, double scale, float rtol, int max_it);
 void launch_cg32_iteration(ipfem_ctx *c);
 void launch_cg32_spmv_only(ipfem_ctx *c);
-// resident capacity of the cooperative solver kernels on the context's device
-void solver_configure(ipfem_ctx *c);
-int fcg_grid_capacity();
+
 void launch_add_scaled32(ipfem_ctx *c, double *d_u, const float *x, double scale);
 // solver drivers (capi.cpp, capi_mlp.cu)
 ipfem_status check_device(ipfem_ctx *c);

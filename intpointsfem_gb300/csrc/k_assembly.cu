@@ -68,8 +68,21 @@ k_gather_strain(int32_t n_el, int64_t n_ip, const T *__restrict__ dphi, const in
         mbar_expect_tx(bar, bytes);
         bulk_g2s(s_dn, dphi + (size_t)e0 * E::NB, bytes, bar);
     }
-    for (int k = threadIdx.x; k < ne * E::ND; k += blockDim.x)
-        s_u[k] = (T)__ldg(&u[__ldg(&dofs[(size_t)e0 * E::ND + k])]);
+    for (int k = threadIdx.x; k < ne * E::ND; k += blockDim.x) {
+        const double uk = __ldg(&u[__ldg(&dofs[(size_t)e0 * E::ND + k])]);
+        if constexpr (sizeof(T) == 8) {
+            s_u[k] = uk;
+        } else {
+            // FP32: the displacement relative to the element's first connect
+            // (same component), formed in FP64 before rounding.  The strain of
+            // a rigid translation is zero, so the strain is unchanged, but the
+            // rounded values now carry the variation across the element
+            // instead of the far-field displacement, which is orders of
+            // magnitude larger than that variation
+            const size_t comp = (size_t)e0 * E::ND + (size_t)(k / E::ND) * E::ND + (k & 1);
+            s_u[k] = (T)(uk - __ldg(&u[__ldg(&dofs[comp])]));
+        }
+    }
     const bool ok = mbar_wait_bounded(bar, 0);
     __syncthreads();
     if (!ok) {

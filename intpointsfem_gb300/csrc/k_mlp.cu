@@ -30,7 +30,6 @@
 #include <algorithm>
 #include <cmath>
 
-#include "grid_sync.cuh"
 #include "ipfem_internal.h"
 #include "ldhint.cuh"
 #include "pdl.cuh"
@@ -222,9 +221,7 @@ __device__ __forceinline__ float2 tri_mul(int32_t i, int32_t n, GridInfo G, cons
 
 // z_j = sigma_j * sum_k G_{i,k}^T y_i over the nodes i = nbr(j, 8-k) that
 // hold j at position k (gather form of G^T)
-// (COHERENT: y was written earlier in the same kernel, so it is read through
-// L2 instead of the read-only path)
-template <class GT, bool COHERENT = false>
+template <class GT>
 __device__ __forceinline__ float2 trit_mul(int32_t j, int32_t n, GridInfo G, const GT *__restrict__ Gm,
                                            const float2 *__restrict__ dinv, const float2 *__restrict__ y)
 {
@@ -234,7 +231,7 @@ __device__ __forceinline__ float2 trit_mul(int32_t j, int32_t n, GridInfo G, con
         const int32_t i = patch_nbr(j, 8 - k, G);
         if (i < 0) continue;
         const float4 m = load_g(Gm, (int64_t)k * n + i);
-        const float2 v = COHERENT ? __ldcg(&y[i]) : __ldg(&y[i]);
+        const float2 v = __ldg(&y[i]);
         z.x = fmaf(m.x, v.x, fmaf(m.z, v.y, z.x));
         z.y = fmaf(m.y, v.x, fmaf(m.w, v.y, z.y));
     }
@@ -402,26 +399,30 @@ __global__ void __launch_bounds__(256) k_tri_precond(int32_t n, GridInfo G, cons
     }
 }
 
-// ----------------------------------------- flexible-CG iteration (FP32)
-// One iteration = two launches: k_fcg_spmv_p (q = K p, p.q, alpha) and the
-// cooperative k_fcg_update_precond (x/r update and first factor pass, grid
-// barrier, second factor pass with r.z and r_old.z, grid barrier for beta,
-// p = z + beta p).  The residual is double-buffered (the caller alternates
-// the buffers: the first factor pass reads r_old at the lower neighbours).
+// ----------------------------------------- fused flexible-CG iteration (FP32)
+// One iteration = k_fcg_spmv, k_fcg_update_first, k_tri_precond (factor in
+// BF16), with the
+// search direction and the residual double-buffered (the caller alternates
+// the buffers): the p-update of the previous iteration is formed on the fly
+// inside the SpMV, the x/r update inside the first factor pass.
 
-// q = K p, partials of p.q; last CTA: alpha = rz / pq.  Each block column
-// gathers p alone (the tangent and the column indices are streamed
-// evict-first so that p stays in L2).
+// p_new = z + beta p_old (the owner stores it, gatherers form it for their
+// columns), q = K p_new, partials of p_new.q; last CTA: alpha = rz / pq.
+// Node-ordered SELL rows; the tangent and its column indices are streamed
+// (evict-first) so that z and p_old stay in L2.
 template <bool PAT>
-__global__ void __launch_bounds__(256, 8) k_fcg_spmv_p(int32_t n, const int64_t *__restrict__ slice_base,
-                                                    const int32_t *__restrict__ rowlen,
-                                                    const int32_t *__restrict__ scol, const uint8_t *__restrict__ pat_id,
-                                                    const int32_t *__restrict__ pat_off,
-                                                    const float4 *__restrict__ K, const uint8_t *__restrict__ fixed,
-                                                    const float2 *__restrict__ p, float2 *__restrict__ q, float *part,
-                                                    int64_t n_part, unsigned *ticket, CGScalarsT<float> *sc)
+__global__ void __launch_bounds__(256, 8) k_fcg_spmv(int32_t n, const int64_t *__restrict__ slice_base,
+                                                  const int32_t *__restrict__ rowlen, const int32_t *__restrict__ scol,
+                                                  const uint8_t *__restrict__ pat_id,
+                                                  const int32_t *__restrict__ pat_off,
+                                                  const float4 *__restrict__ K, const uint8_t *__restrict__ fixed,
+                                                  const float2 *__restrict__ z, const float2 *__restrict__ p_old,
+                                                  float2 *__restrict__ p_new, float2 *__restrict__ q, float *part,
+                                                  int64_t n_part, unsigned *ticket, CGScalarsT<float> *sc)
 {
     const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    // row metadata before the wait; z, beta and the flag (written by the
+    // preconditioner pass) after it
     int64_t base = 0;
     int len = 0, pb = 0;
     if (i < n) {
@@ -432,6 +433,7 @@ __global__ void __launch_bounds__(256, 8) k_fcg_spmv_p(int32_t n, const int64_t 
     pdl_wait();
     pdl_launch_dependents();
     if (*reinterpret_cast<volatile int *>(&sc->done)) return;
+    const float beta = *reinterpret_cast<volatile float *>(&sc->beta);
     float v[1] = {0.f};
     if (i < n) {
         const uint64_t keep = l2_policy_keep();
@@ -441,14 +443,17 @@ __global__ void __launch_bounds__(256, 8) k_fcg_spmv_p(int32_t n, const int64_t 
             const int64_t s = base + sell_koff<true>(k);
             const int32_t c = PAT ? i + __ldg(&pat_off[pb + k]) : __ldcs(&scol[s]);
             const float4 a = __ldcs(&K[s]);
-            const float2 pp = ld_keep(&p[c], keep);
-            y0 = fmaf(a.y, pp.y, fmaf(a.x, pp.x, y0));
-            y1 = fmaf(a.w, pp.y, fmaf(a.z, pp.x, y1));
+            const float2 zz = ld_keep(&z[c], keep), pp = ld_keep(&p_old[c], keep);
+            const float px = fmaf(beta, pp.x, zz.x), py = fmaf(beta, pp.y, zz.y);
+            y0 = fmaf(a.y, py, fmaf(a.x, px, y0));
+            y1 = fmaf(a.w, py, fmaf(a.z, px, y1));
         }
         if (fixed[2 * (int64_t)i]) y0 = 0.f;
         if (fixed[2 * (int64_t)i + 1]) y1 = 0.f;
         q[i] = make_float2(y0, y1);
-        const float2 pn = p[i];
+        const float2 zi = z[i], pi = p_old[i];
+        const float2 pn = make_float2(fmaf(beta, pi.x, zi.x), fmaf(beta, pi.y, zi.y));
+        p_new[i] = pn;
         v[0] = fmaf(pn.y, y1, pn.x * y0);
     }
     if (fcg_partials<1>(v, part, n_part, ticket)) {
@@ -468,100 +473,59 @@ __global__ void __launch_bounds__(256, 8) k_fcg_spmv_p(int32_t n, const int64_t 
     }
 }
 
-// p = z + beta p (the first search direction of a solve: beta = 0, p = 0)
-__global__ void __launch_bounds__(256) k_fcg_pinit(int32_t n, const float2 *__restrict__ z, float2 *__restrict__ p,
-                                                   const CGScalarsT<float> *sc)
+// x += alpha p, r_new = r_old - alpha q (the owner stores it, the factor
+// pass forms it for its neighbours), y = G (sigma * r_new); partials of
+// r_new.r_new; last CTA: convergence, stagnation and iteration limit
+__global__ void __launch_bounds__(256, 8) k_fcg_update_first(int32_t n, GridInfo G, const uint2 *__restrict__ Gm,
+                                                          const float2 *__restrict__ dinv,
+                                                          const float2 *__restrict__ p, const float2 *__restrict__ q,
+                                                          float2 *__restrict__ x, const float2 *__restrict__ r_old,
+                                                          float2 *__restrict__ r_new, float2 *__restrict__ y,
+                                                          float *part, int64_t n_part, unsigned *ticket,
+                                                          CGScalarsT<float> *sc, int stall_window)
 {
     const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n || *reinterpret_cast<const volatile int *>(&sc->done)) return;
-    const float beta = sc->beta;
-    const float2 zz = z[i], pp = p[i];
-    p[i] = make_float2(fmaf(beta, pp.x, zz.x), fmaf(beta, pp.y, zz.y));
-}
-
-// Partials of one 256-node window w, the sums of fcg_partials (warp trees,
-// then the CTA's warp sums in order) written to part[k * n_part + w], no ticket.
-template <int NV>
-__device__ __forceinline__ void fcg_window_partials(const float (&v)[NV], float *part, int64_t n_part, int64_t w)
-{
-    __shared__ float ws[NV][32];
-    const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    // x and r_old (not written by the SpMV) before the wait; p, q, alpha and
+    // the flag after it
+    float2 xx = make_float2(0.f, 0.f), ro[NTRI];
+    int32_t jn[NTRI];
+    if (i < n) {
+        xx = x[i];
 #pragma unroll
-    for (int k = 0; k < NV; k++) {
-        const float t = wsum(v[k]);
-        if (lane == 0) ws[k][wp] = t;
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-#pragma unroll
-        for (int k = 0; k < NV; k++) {
-            float a = 0.f;
-            for (int q = 0; q < nw; q++) a = a + ws[k][q];
-            part[k * n_part + w] = a;
+        for (int k = 0; k < NTRI; k++) {
+            jn[k] = patch_nbr(i, k, G);
+            if (jn[k] >= 0) ro[k] = __ldg(&r_old[jn[k]]);
         }
     }
-    __syncthreads();
-}
-
-// The vector work of a flexible-CG iteration in one cooperative launch:
-// phase 1: x += alpha p, r_new = r_old - alpha q at the node and its lower
-// neighbours, y = G (sigma r_new), r_new.r_new per 256-node window; a grid
-// barrier whose last CTA tests convergence, stagnation and the iteration
-// limit; phase 2: z = sigma G^T y (y of the upper neighbours, read through
-// L2), r.z and r_old.z per window; a grid barrier whose last CTA forms the
-// Polak-Ribiere beta; phase 3: p = z + beta p.  Windows w = blockIdx.x +
-// j gridDim.x; z of the CTA's first windows stays in shared memory.
-constexpr int kFcgFuseWin = 4;   // windows per CTA whose z stays in shared memory for phase 3
-
-__global__ void __launch_bounds__(256, 8) k_fcg_update_precond(int32_t n, int64_t n_win, GridInfo G,
-                                                            const uint2 *__restrict__ Gm, const float2 *__restrict__ dinv,
-                                                            float2 *p, const float2 *__restrict__ q,
-                                                            float2 *__restrict__ x, const float2 *__restrict__ r_old,
-                                                            float2 *__restrict__ r_new, float2 *__restrict__ y,
-                                                            float *__restrict__ z, float *part, float *part2,
-                                                            int64_t n_part, unsigned *count, unsigned *gen,
-                                                            unsigned *count2, unsigned *gen2, CGScalarsT<float> *sc,
-                                                            int stall_window, int *err)
-{
-    __shared__ float2 s_z[kFcgFuseWin][256];
-    const unsigned gen0 = ld_acquire_gpu(gen);     // before this CTA arrives
-    const unsigned gen20 = ld_acquire_gpu(gen2);
     pdl_wait();
     pdl_launch_dependents();
     if (*reinterpret_cast<volatile int *>(&sc->done)) return;
     const float alpha = *reinterpret_cast<volatile float *>(&sc->alpha);
-    for (int64_t w = blockIdx.x; w < n_win; w += gridDim.x) {
-        const int32_t i = (int32_t)(w * 256) + (int32_t)threadIdx.x;
-        float v[1] = {0.f};
-        if (i < n) {
-            float2 xx = x[i];
-            const float2 pp = p[i];
-            xx.x = fmaf(alpha, pp.x, xx.x);
-            xx.y = fmaf(alpha, pp.y, xx.y);
-            x[i] = xx;
-            float2 acc = make_float2(0.f, 0.f);
+    float v[1] = {0.f};
+    if (i < n) {
+        const float2 pp = p[i];
+        xx.x = fmaf(alpha, pp.x, xx.x);
+        xx.y = fmaf(alpha, pp.y, xx.y);
+        x[i] = xx;
+        float2 acc = make_float2(0.f, 0.f);
 #pragma unroll
-            for (int k = 0; k < NTRI; k++) {
-                const int32_t jn = patch_nbr(i, k, G);
-                if (jn < 0) continue;
-                const float2 ro = __ldg(&r_old[jn]);
-                const float2 qq = __ldg(&q[jn]);
-                const float2 rn = make_float2(fmaf(-alpha, qq.x, ro.x), fmaf(-alpha, qq.y, ro.y));
-                if (k == 4) {
-                    r_new[i] = rn;
-                    v[0] = fmaf(rn.y, rn.y, rn.x * rn.x);
-                }
-                const float4 m = load_g(Gm, (int64_t)k * n + i);
-                const float2 sg = sqrt2(__ldg(&dinv[jn]));
-                const float vx = sg.x * rn.x, vy = sg.y * rn.y;
-                acc.x = fmaf(m.x, vx, fmaf(m.y, vy, acc.x));
-                acc.y = fmaf(m.z, vx, fmaf(m.w, vy, acc.y));
+        for (int k = 0; k < NTRI; k++) {
+            if (jn[k] < 0) continue;
+            const float2 qq = __ldg(&q[jn[k]]);
+            const float2 rn = make_float2(fmaf(-alpha, qq.x, ro[k].x), fmaf(-alpha, qq.y, ro[k].y));
+            if (k == 4) {
+                r_new[i] = rn;
+                v[0] = fmaf(rn.y, rn.y, rn.x * rn.x);
             }
-            y[i] = acc;
+            const float4 m = load_g(Gm, (int64_t)k * n + i);
+            const float2 sg = sqrt2(__ldg(&dinv[jn[k]]));
+            const float vx = sg.x * rn.x, vy = sg.y * rn.y;
+            acc.x = fmaf(m.x, vx, fmaf(m.y, vy, acc.x));
+            acc.y = fmaf(m.z, vx, fmaf(m.w, vy, acc.y));
         }
-        fcg_window_partials<1>(v, part, n_part, w);
+        y[i] = acc;
     }
-    if (grid_arrive(count)) {
+    if (fcg_partials<1>(v, part, n_part, ticket)) {
         float o[1];
         fcg_final<1>(part, n_part, o);
         if (threadIdx.x == 0) {
@@ -581,56 +545,7 @@ __global__ void __launch_bounds__(256, 8) k_fcg_update_precond(int32_t n, int64_
                 sc->done = 1;
                 sc->status = IPFEM_NONCONVERGED;
             }
-        }
-        grid_release(count, gen, gen0);
-    } else if (!grid_wait(gen, gen0, err)) {
-        if (threadIdx.x == 0) atomicExch(&sc->done, 1);
-        return;
-    }
-    if (*reinterpret_cast<volatile int *>(&sc->done)) return;
-    int j = 0;
-    for (int64_t w = blockIdx.x; w < n_win; w += gridDim.x, j++) {
-        const int32_t i = (int32_t)(w * 256) + (int32_t)threadIdx.x;
-        float v[2] = {0.f, 0.f};
-        if (i < n) {
-            const float2 zz = trit_mul<uint2, true>(i, n, G, Gm, dinv, y);
-            if (j < kFcgFuseWin) s_z[j][threadIdx.x] = zz;
-            else reinterpret_cast<float2 *>(z)[i] = zz;
-            const float2 rr = r_new[i], ro = r_old[i];
-            v[0] = fmaf(rr.y, zz.y, rr.x * zz.x);
-            v[1] = fmaf(ro.y, zz.y, ro.x * zz.x);
-        }
-        fcg_window_partials<2>(v, part2, n_part, w);
-    }
-    if (grid_arrive(count2)) {
-        float out[2];
-        fcg_final<2>(part2, n_part, out);
-        if (threadIdx.x == 0) {
-            const float rz = out[0], cross = out[1];
-            float beta = (sc->rz > 0.f) ? (rz - cross) / sc->rz : 0.f;
-            if (!(beta > 0.f)) beta = 0.f;
-            sc->beta = beta;
-            sc->rz = rz;
-            if (!(rz > 0.f)) {          // M r is not a descent direction
-                sc->done = 1;
-                sc->status = kStatusFallback;
-            }
-        }
-        grid_release(count2, gen2, gen20);
-    } else if (!grid_wait(gen2, gen20, err)) {
-        if (threadIdx.x == 0) atomicExch(&sc->done, 1);
-        return;
-    }
-    // phase 3: the next search direction p = z + beta p (the next SpMV gathers p alone)
-    if (*reinterpret_cast<volatile int *>(&sc->done)) return;
-    const float beta = *reinterpret_cast<volatile float *>(&sc->beta);
-    j = 0;
-    for (int64_t w = blockIdx.x; w < n_win; w += gridDim.x, j++) {
-        const int32_t i = (int32_t)(w * 256) + (int32_t)threadIdx.x;
-        if (i < n) {
-            const float2 zz = j < kFcgFuseWin ? s_z[j][threadIdx.x] : reinterpret_cast<const float2 *>(z)[i];
-            const float2 pp = p[i];
-            p[i] = make_float2(fmaf(beta, pp.x, zz.x), fmaf(beta, pp.y, zz.y));
+            *ticket = 0u;
         }
     }
 }
@@ -991,12 +906,10 @@ void launch_fcg_init(ipfem_ctx *c, const double *d_b, double scale, float rtol, 
     k_fcg_init<<<fcg_grid(c), 256, 0, c->stream>>>(c->s.n_nodes, d_b, scale, m.x, m.r, m.p, c->mlp.r_old, m.part,
                                                    (int64_t)fcg_grid(c), c->d_counters + 4, m.sc, rtol, max_it);
     launch_precond(c, 0);
-    k_fcg_pinit<<<fcg_grid(c), 256, 0, c->stream>>>(c->s.n_nodes, reinterpret_cast<const float2 *>(m.z),
-                                                    reinterpret_cast<float2 *>(m.p), m.sc);
 }
 
-// iteration k (par = k % 2): R[par] -> R[1-par] in the vector kernel; p is
-// updated in place at its end (z from R[1-par])
+// iteration k (par = k % 2): P[par] -> P[1-par] in the SpMV, R[par] -> R[1-par]
+// in the update, z from R[1-par]
 void launch_fcg_iteration(ipfem_ctx *c, int par)
 {
     MixedBuffers &m = c->mx;
@@ -1004,27 +917,23 @@ void launch_fcg_iteration(ipfem_ctx *c, int par)
     const SellDev &L = m.dsell;
     GridInfo G{l.gr, l.gt};
     const int32_t n = c->s.n_nodes;
+    float2 *P[2] = {reinterpret_cast<float2 *>(m.p), reinterpret_cast<float2 *>(l.p2)};
     float2 *R[2] = {reinterpret_cast<float2 *>(m.r), reinterpret_cast<float2 *>(l.r_old)};
     const float2 *d2 = reinterpret_cast<const float2 *>(m.dinv);
     float *part = m.part;
-    float2 *p = reinterpret_cast<float2 *>(m.p);
-    launch_pdl(use_row_stencils(c, L) ? k_fcg_spmv_p<true> : k_fcg_spmv_p<false>, fcg_grid(c), 256, c->stream, n,
+    launch_pdl(use_row_stencils(c, L) ? k_fcg_spmv<true> : k_fcg_spmv<false>, fcg_grid(c), 256, c->stream, n,
                (const int64_t *)L.slice_base, (const int32_t *)L.rowlen, (const int32_t *)L.sell_col,
                (const uint8_t *)L.pat_id, (const int32_t *)L.pat_off, reinterpret_cast<const float4 *>(m.K),
-               (const uint8_t *)c->d_fixed, (const float2 *)p, reinterpret_cast<float2 *>(m.q), part,
-               (int64_t)fcg_grid(c), c->d_counters + 5, m.sc);
+               (const uint8_t *)c->d_fixed, reinterpret_cast<const float2 *>(m.z), (const float2 *)P[par],
+               P[1 - par], reinterpret_cast<float2 *>(m.q), part, (int64_t)fcg_grid(c), c->d_counters + 5, m.sc);
+    launch_pdl(k_fcg_update_first, fcg_grid(c), 256, c->stream, n, G, reinterpret_cast<const uint2 *>(l.Gh), d2,
+               (const float2 *)P[1 - par], reinterpret_cast<const float2 *>(m.q), reinterpret_cast<float2 *>(m.x),
+               (const float2 *)R[par], R[1 - par], reinterpret_cast<float2 *>(l.y), part, (int64_t)fcg_grid(c),
+               c->d_counters + 6, m.sc, stall_window(c));
     float *part2 = reinterpret_cast<float *>(c->d_part);
-    const int64_t n_win = fcg_grid(c);
-    launch_coop(k_fcg_update_precond, (unsigned)std::max<int64_t>(1, std::min<int64_t>(n_win, c->coop_cap_fcg)), 256,
-                c->stream, true, n, n_win, G, reinterpret_cast<const uint2 *>(l.Gh), d2, p,
-                reinterpret_cast<const float2 *>(m.q), reinterpret_cast<float2 *>(m.x), (const float2 *)R[par],
-                R[1 - par], reinterpret_cast<float2 *>(l.y), m.z, part, part2, n_win, c->d_counters + 12,
-                c->d_counters + 13, c->d_counters + 7, c->d_counters + 15, m.sc, stall_window(c), c->d_err);
-}
-
-int fcg_grid_capacity()
-{
-    return grid_capacity(k_fcg_update_precond, 256, 0);
+    launch_pdl(k_tri_precond, fcg_grid(c), 256, c->stream, n, G, reinterpret_cast<const uint2 *>(l.Gh), d2,
+               reinterpret_cast<const float2 *>(l.y), reinterpret_cast<const float *>(R[1 - par]),
+               reinterpret_cast<const float *>(R[par]), m.z, part2, (int64_t)fcg_grid(c), c->d_counters + 7, m.sc);
 }
 
 // ------------------------------------------------------------ training pass

@@ -16,9 +16,6 @@
 // Scalars (alpha, beta, convergence) live in device memory, so an iteration
 // is three kernels with no host round trip; the host replays a captured CUDA
 // graph of several iterations and checks the `done` word between replays.
-#include <algorithm>
-
-#include "grid_sync.cuh"
 #include "ipfem_internal.h"
 #include "ldhint.cuh"
 #include "pdl.cuh"
@@ -329,73 +326,42 @@ __global__ void __launch_bounds__(kRedBlock) k_cg_spmv(int32_t n_nodes, const in
     }
 }
 
-// Partial sums of one 256-node window w (the same canonical tree as
-// block_partials) written to part[k * n_red + w], without a ticket; s is the
-// caller's staging area, free again on return.
-template <class T, int NV>
-__device__ __forceinline__ void window_partials(const T (&v)[NV], T *part, int64_t n_red, int64_t w,
-                                                T (*s)[kRedStage])
-{
-#pragma unroll
-    for (int k = 0; k < NV; k++) s[k][red_stage(threadIdx.x)] = v[k];
-    __syncthreads();
-    const int wp = threadIdx.x >> 5, w0 = (int)(w & 3);
-#pragma unroll
-    for (int k = 0; k < NV; k++)
-        if (wp == ((w0 + 2 * k) & 3)) {
-            const T o = tree256_warp<T>(s[k]);
-            if ((threadIdx.x & 31) == 0) part[k * n_red + w] = o;
-        }
-    __syncthreads();
-}
-
-// One CG iteration's vector work in one cooperative launch: phase 1 is
-// k_cg_update (x += alpha p, r -= alpha q, z = M r, partials of r.r and r.z
-// per 256-node window), a grid barrier whose last CTA runs k_cg_update's
-// epilogue (convergence test, beta), then phase 2 is k_cg_pupdate (p = z +
-// beta p) on the same windows, z kept in shared memory (the first kFuseWin
-// windows of the CTA) or in global memory.  Same operations on the same
-// values as the two kernels: the results are equal bit for bit.  Windows
-// w = blockIdx.x + j gridDim.x; the grid is at most the resident capacity.
-constexpr int kFuseWin = 4;
-
+// x += alpha p, r -= alpha q, z = M r; partials of r.r and r.z;
+// last CTA: convergence test, beta
 template <class T, bool BLOCK>
-__global__ void __launch_bounds__(kRedBlock) k_cg_update_p(int32_t n_nodes, int64_t n_win, const T *__restrict__ q,
-                                                           const T *__restrict__ minv, T *__restrict__ x,
-                                                           T *__restrict__ r, T *__restrict__ z, T *p, T *part,
-                                                           int64_t n_red, unsigned *count, unsigned *gen,
-                                                           CGScalarsT<T> *sc, int *err)
+__global__ void __launch_bounds__(kRedBlock) k_cg_update(int32_t n_nodes, const T *__restrict__ p,
+                                                         const T *__restrict__ q, const T *__restrict__ dinv,
+                                                         T *__restrict__ x, T *__restrict__ r, T *__restrict__ z,
+                                                         T *part, int64_t n_red, unsigned *ticket, CGScalarsT<T> *sc)
 {
     typedef typename Vec2<T>::type V;
-    __shared__ T s_red[2][kRedStage];
-    __shared__ V s_z[kFuseWin][kRedBlock];
-    const unsigned gen0 = ld_acquire_gpu(gen);     // before this CTA arrives
+    const int32_t i = blockIdx.x * kRedBlock + threadIdx.x;
+    // p, x and r (not written by the SpMV) before the wait, q after it
+    V pp, qq, xx, rr;
+    if (i < n_nodes) {
+        pp = reinterpret_cast<const V *>(p)[i];
+        xx = reinterpret_cast<V *>(x)[i];
+        rr = reinterpret_cast<V *>(r)[i];
+    }
     pdl_wait();
     pdl_launch_dependents();
+    if (i < n_nodes) qq = reinterpret_cast<const V *>(q)[i];
     if (*reinterpret_cast<volatile int *>(&sc->done)) return;
     const T alpha = *reinterpret_cast<volatile T *>(&sc->alpha);
-    int j = 0;
-    for (int64_t w = blockIdx.x; w < n_win; w += gridDim.x, j++) {
-        const int32_t i = (int32_t)(w * kRedBlock) + (int32_t)threadIdx.x;
-        T v[2] = {T(0), T(0)};
-        if (i < n_nodes) {
-            const V pp = reinterpret_cast<const V *>(p)[i], qq = reinterpret_cast<const V *>(q)[i];
-            V xx = reinterpret_cast<V *>(x)[i], rr = reinterpret_cast<V *>(r)[i];
-            xx.x = fma(alpha, pp.x, xx.x);
-            xx.y = fma(alpha, pp.y, xx.y);
-            rr.x = fma(-alpha, qq.x, rr.x);
-            rr.y = fma(-alpha, qq.y, rr.y);
-            const V zz = precondition<T, BLOCK>(minv, i, rr);
-            reinterpret_cast<V *>(x)[i] = xx;
-            reinterpret_cast<V *>(r)[i] = rr;
-            if (j < kFuseWin) s_z[j][threadIdx.x] = zz;
-            else reinterpret_cast<V *>(z)[i] = zz;
-            v[0] = fma(rr.y, rr.y, fma(rr.x, rr.x, T(0)));
-            v[1] = fma(rr.y, zz.y, fma(rr.x, zz.x, T(0)));
-        }
-        window_partials<T, 2>(v, part, n_red, w, s_red);
+    T v[2] = {T(0), T(0)};
+    if (i < n_nodes) {
+        xx.x = fma(alpha, pp.x, xx.x);
+        xx.y = fma(alpha, pp.y, xx.y);
+        rr.x = fma(-alpha, qq.x, rr.x);
+        rr.y = fma(-alpha, qq.y, rr.y);
+        const V zz = precondition<T, BLOCK>(dinv, i, rr);
+        reinterpret_cast<V *>(x)[i] = xx;
+        reinterpret_cast<V *>(r)[i] = rr;
+        reinterpret_cast<V *>(z)[i] = zz;
+        v[0] = fma(rr.y, rr.y, fma(rr.x, rr.x, T(0)));
+        v[1] = fma(rr.y, zz.y, fma(rr.x, zz.x, T(0)));
     }
-    if (grid_arrive(count)) {
+    if (block_partials<T, 2>(v, part, n_red, ticket)) {
         T o[2];
         final_reduce<T, 2>(part, n_red, o);
         if (threadIdx.x == 0) {
@@ -411,25 +377,41 @@ __global__ void __launch_bounds__(kRedBlock) k_cg_update_p(int32_t n_nodes, int6
                 sc->beta = rzn / sc->rz;
                 sc->rz = rzn;
             }
-        }
-        grid_release(count, gen, gen0);
-    } else if (!grid_wait(gen, gen0, err)) {
-        if (threadIdx.x == 0) atomicExch(&sc->done, 1);
-        return;
-    }
-    if (*reinterpret_cast<volatile int *>(&sc->done)) return;
-    const T beta = *reinterpret_cast<volatile T *>(&sc->beta);
-    j = 0;
-    for (int64_t w = blockIdx.x; w < n_win; w += gridDim.x, j++) {
-        const int32_t i = (int32_t)(w * kRedBlock) + (int32_t)threadIdx.x;
-        if (i < n_nodes) {
-            const V zz = j < kFuseWin ? s_z[j][threadIdx.x] : reinterpret_cast<const V *>(z)[i];
-            V pp = reinterpret_cast<const V *>(p)[i];
-            pp.x = fma(beta, pp.x, zz.x);
-            pp.y = fma(beta, pp.y, zz.y);
-            reinterpret_cast<V *>(p)[i] = pp;
+            *ticket = 0u;
         }
     }
+}
+
+// p = z + beta p, kPupNodes nodes per thread (strided by the CTA size) so that
+// each thread has several loads in flight: the kernel moves 48 bytes per node
+// and is bound by memory latency, not bandwidth, at one node per thread
+constexpr int kPupNodes = 4;
+
+template <class T>
+__global__ void __launch_bounds__(kRedBlock) k_cg_pupdate(int32_t n_nodes, const T *__restrict__ z,
+                                                          T *__restrict__ p, const CGScalarsT<T> *sc)
+{
+    typedef typename Vec2<T>::type V;
+    const int32_t i0 = blockIdx.x * (kRedBlock * kPupNodes) + threadIdx.x;
+    // p (not written by the update) before the wait, z after it
+    V pp[kPupNodes], zz[kPupNodes];
+#pragma unroll
+    for (int j = 0; j < kPupNodes; j++)
+        if (i0 + j * kRedBlock < n_nodes) pp[j] = reinterpret_cast<V *>(p)[i0 + j * kRedBlock];
+    pdl_wait();
+    pdl_launch_dependents();
+#pragma unroll
+    for (int j = 0; j < kPupNodes; j++)
+        if (i0 + j * kRedBlock < n_nodes) zz[j] = reinterpret_cast<const V *>(z)[i0 + j * kRedBlock];
+    if (*reinterpret_cast<const volatile int *>(&sc->done)) return;
+    const T beta = *reinterpret_cast<const volatile T *>(&sc->beta);
+#pragma unroll
+    for (int j = 0; j < kPupNodes; j++)
+        if (i0 + j * kRedBlock < n_nodes) {
+            pp[j].x = fma(beta, pp[j].x, zz[j].x);
+            pp[j].y = fma(beta, pp[j].y, zz[j].y);
+            reinterpret_cast<V *>(p)[i0 + j * kRedBlock] = pp[j];
+        }
 }
 
 __global__ void __launch_bounds__(kRedBlock) k_dot(int32_t n_nodes, const double *__restrict__ a,
@@ -471,19 +453,6 @@ __global__ void __launch_bounds__(256) k_fp64_probe(double *out, int iters, doub
     out[blockIdx.x * blockDim.x + threadIdx.x] = ((x0 + x1) + (x2 + x3)) + ((x4 + x5) + (x6 + x7));
 }
 
-// One CTA waits at a grid barrier that no CTA releases (the generation word
-// is never written): the bounded wait must give up and record kErrGridWait.
-__global__ void k_wait_probe(const unsigned *gen, int *err)
-{
-    const unsigned g0 = ld_acquire_gpu(gen);
-    grid_wait(gen, g0, err);
-}
-
-void launch_wait_probe(ipfem_ctx *c)
-{
-    k_wait_probe<<<1, 32, 0, c->stream>>>(c->d_counters + 14, c->d_err);
-}
-
 void launch_fp64_probe(ipfem_ctx *c, double *d_out, int grid, int iters)
 {
     k_fp64_probe<<<grid, 256, 0, c->stream>>>(d_out, iters, 0.999, 0.001);
@@ -520,6 +489,11 @@ void launch_cg_init(ipfem_ctx *c, const double *d_b, double rtol, int max_it)
                                                                   c->d_counters + 0, c->d_sc, rtol, max_it);
 }
 
+static unsigned grid_pupdate(const ipfem_ctx *c)
+{
+    return (unsigned)((c->s.n_nodes + kRedBlock * kPupNodes - 1) / (kRedBlock * kPupNodes));
+}
+
 template <class T>
 void launch_spmv(ipfem_ctx *c, const SellDev &L, const T *K, const T *p, T *q, T *part, unsigned *ticket,
                  CGScalarsT<T> *sc)
@@ -533,21 +507,16 @@ void launch_spmv(ipfem_ctx *c, const SellDev &L, const T *K, const T *p, T *q, T
                (const T *)p, q, part, c->n_red, ticket, sc);
 }
 
-// cooperative grid of k_cg_update_p: every window once, at most the resident capacity
-static unsigned grid_fused(const ipfem_ctx *c, bool fp64)
-{
-    const int cap = fp64 ? c->coop_cap_cg64 : c->coop_cap_cg32;
-    return (unsigned)std::max<int64_t>(1, std::min<int64_t>(c->n_red, cap));
-}
-
 void launch_cg_iteration(ipfem_ctx *c)
 {
+    const unsigned g = grid_nodes(c);
     launch_spmv<double>(c, c->dsell, c->d_K, c->d_p, c->d_q, c->d_part, c->d_counters + 1, c->d_sc);
     const bool blk = c->preconditioner == IPFEM_PREC_BLOCK_JACOBI;
-    launch_coop(blk ? k_cg_update_p<double, true> : k_cg_update_p<double, false>, grid_fused(c, true), kRedBlock,
-                c->stream, true, c->s.n_nodes, c->n_red, (const double *)c->d_q,
-                (const double *)(blk ? c->d_binv : c->d_dinv), c->d_x, c->d_r, c->d_z, c->d_p, c->d_part, c->n_red,
-                c->d_counters + 8, c->d_counters + 9, c->d_sc, c->d_err);
+    launch_pdl(blk ? k_cg_update<double, true> : k_cg_update<double, false>, g, kRedBlock, c->stream, c->s.n_nodes,
+               (const double *)c->d_p, (const double *)c->d_q, (const double *)(blk ? c->d_binv : c->d_dinv), c->d_x,
+               c->d_r, c->d_z, c->d_part, c->n_red, c->d_counters + 2, c->d_sc);
+    launch_pdl(k_cg_pupdate<double>, grid_pupdate(c), kRedBlock, c->stream, c->s.n_nodes,
+               (const double *)c->d_z, c->d_p, (const CGScalarsT<double> *)c->d_sc);
 }
 
 void launch_cg_spmv_only(ipfem_ctx *c)
@@ -568,26 +537,26 @@ void launch_cg32_init(ipfem_ctx *c, const double *d_b, double scale, float rtol,
 void launch_cg32_iteration(ipfem_ctx *c)
 {
     MixedBuffers &m = c->mx;
+    const unsigned g = grid_nodes(c);
     launch_spmv<float>(c, m.dsell, m.K, m.p, m.q, m.part, c->d_counters + 5, m.sc);
     const bool blk = c->preconditioner == IPFEM_PREC_BLOCK_JACOBI;
-    launch_coop(blk ? k_cg_update_p<float, true> : k_cg_update_p<float, false>, grid_fused(c, false), kRedBlock,
-                c->stream, true, c->s.n_nodes, c->n_red, (const float *)m.q, (const float *)(blk ? m.binv : m.dinv),
-                m.x, m.r, m.z, m.p, m.part, c->n_red, c->d_counters + 10, c->d_counters + 11, m.sc, c->d_err);
-}
-
-void solver_configure(ipfem_ctx *c)
-{
-    c->coop_cap_cg64 = std::min(grid_capacity(k_cg_update_p<double, true>, kRedBlock, 0),
-                                grid_capacity(k_cg_update_p<double, false>, kRedBlock, 0));
-    c->coop_cap_cg32 = std::min(grid_capacity(k_cg_update_p<float, true>, kRedBlock, 0),
-                                grid_capacity(k_cg_update_p<float, false>, kRedBlock, 0));
-    c->coop_cap_fcg = fcg_grid_capacity();
+    launch_pdl(blk ? k_cg_update<float, true> : k_cg_update<float, false>, g, kRedBlock, c->stream, c->s.n_nodes,
+               (const float *)m.p, (const float *)m.q, (const float *)(blk ? m.binv : m.dinv), m.x, m.r, m.z, m.part,
+               c->n_red, c->d_counters + 6, m.sc);
+    launch_pdl(k_cg_pupdate<float>, grid_pupdate(c), kRedBlock, c->stream, c->s.n_nodes, (const float *)m.z,
+               m.p, (const CGScalarsT<float> *)m.sc);
 }
 
 void launch_cg32_spmv_only(ipfem_ctx *c)
 {
     MixedBuffers &m = c->mx;
     launch_spmv<float>(c, m.dsell, m.K, m.p, m.q, m.part, c->d_counters + 5, m.sc);
+}
+
+void launch_cg32_pupdate_only(ipfem_ctx *c)
+{
+    MixedBuffers &m = c->mx;
+    k_cg_pupdate<float><<<grid_pupdate(c), kRedBlock, 0, c->stream>>>(c->s.n_nodes, m.z, m.p, m.sc);
 }
 
 void launch_add_scaled32(ipfem_ctx *c, double *d_u, const float *x, double scale)

@@ -165,19 +165,3 @@ def test_iteration_log_records_every_newton_iteration(tmp_path):
     # closing the log stops the records
     sm.newton(np.zeros(sm.neq), 10, 0, 1, newton_max_it=30)
     assert len(open(path).readlines()) == len(recs)
-
-
-def test_bounded_grid_wait_gives_up_and_context_stays_usable():
-    """A grid barrier that nothing releases (the waits of the cooperative
-    solver kernels): the wait gives up after its limit, the host reads the
-    timeout as an error, and the same context then solves as before"""
-    sm, P = ip.ElastoPlasticIntPointsStructMatrix(ip.WellboreMesh(ip.wellbore_params(8))), \
-        po.OracleProblem(po.default_params(8), nthreads=0)
-    ms = sm.probe_wait_timeout()
-    print("grid wait gave up after %.0f ms" % ms)
-    assert 50.0 < ms < 10000.0
-    sm.SetLoadFactor(0.5)
-    r = sm.assemble(np.zeros(sm.neq), np.zeros(sm.neq))
-    x, it = sm.solve(r)
-    xo, ito = P.pcg(P.assemble(np.zeros(sm.neq), 0.5))
-    assert it == ito and _eq(x, xo)
