@@ -591,6 +591,27 @@ class ElastoPlasticIntPointsStructMatrix:
         arr = np.ascontiguousarray(arr, dtype=np.float64)
         self._check(lib().ipfem_set_state(self._ctx, int(field), _np_ptr(arr, _dp)))
 
+    def save_checkpoint(self, path, u, step):
+        """write u (host or device) and the committed integration-point state
+        (plastic strain, stress, alpha, m_type) after load step `step` to an
+        .npz file; load_checkpoint restores them into a context of the same
+        problem, from which the load-stepped solve continues with the same
+        iterates (the reference keeps this state only in memory,
+        TPZConstitutiveLawProcessor.cpp:86-121)"""
+        uh = u.detach().cpu().numpy() if hasattr(u, "detach") else np.asarray(u)
+        np.savez(path, u=np.asarray(uh, dtype=np.float64), step=np.int64(step), neq=np.int64(self.neq),
+                 **{"state%d" % f: self.get_state(f) for f in range(4)})
+
+    def load_checkpoint(self, path):
+        """restore a save_checkpoint file; returns (u as a host array, step)"""
+        d = np.load(path)
+        if int(d["neq"]) != self.neq:
+            raise IpfemError(5, "checkpoint of a problem with %d equations, this one has %d" % (int(d["neq"]),
+                                                                                               self.neq))
+        for f in range(4):
+            self.set_state(f, d["state%d" % f])
+        return np.array(d["u"]), int(d["step"])
+
     def get_setup(self, field):
         nn = self.n_ip // self.n_el
         spec = {0: (self.n_el, np.int32), 1: (1, np.int32), 2: (2 * nn * self.n_el, np.int32),

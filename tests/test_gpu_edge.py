@@ -165,3 +165,23 @@ def test_iteration_log_records_every_newton_iteration(tmp_path):
     # closing the log stops the records
     sm.newton(np.zeros(sm.neq), 10, 0, 1, newton_max_it=30)
     assert len(open(path).readlines()) == len(recs)
+
+
+def test_checkpoint_resume_is_bit_identical(tmp_path):
+    """save u and the integration-point state after load step 3, restore them
+    into a new context and continue: steps 4-6 give the iterates and state of
+    the uninterrupted solve bit for bit"""
+    w = ip.WellboreMesh(ip.wellbore_params(12, material_mode=2))
+    a = ip.ElastoPlasticIntPointsStructMatrix(w)
+    ua = np.zeros(a.neq)
+    a.newton(ua, 10, 0, 3, newton_max_it=30)
+    path = str(tmp_path / "step3.npz")
+    a.save_checkpoint(path, ua, 3)
+    a.newton(ua, 10, 3, 6, newton_max_it=30)
+    b = ip.ElastoPlasticIntPointsStructMatrix(w)
+    ub, step = b.load_checkpoint(path)
+    assert step == 3
+    b.newton(ub, 10, step, 6, newton_max_it=30)
+    assert _eq(ua, ub)
+    for f in range(4):
+        assert _eq(a.get_state(f), b.get_state(f)), f
