@@ -195,22 +195,27 @@ __global__ void __launch_bounds__(128) k_patch_net_tc(int64_t rows, const float 
     uint32_t phase = 0;
     bool ok = true;
     const int64_t n_tiles = (rows + TC_ROWS - 1) / TC_ROWS;
+    // features of this thread's node in the CTA's next tile, loaded one tile
+    // ahead so that the load latency overlaps the current tile's layers
+    float4 f[8];
+    auto load_features = [&](int64_t tile) {
+        const int64_t r = tile * TC_ROWS + tid;
+#pragma unroll
+        for (int j = 0; j < 8; j++)
+            f[j] = (tile < n_tiles && r < rows) ? __ldcs(reinterpret_cast<const float4 *>(X + r * 32) + j)
+                                                : make_float4(0.f, 0.f, 0.f, 0.f);
+    };
+    load_features(blockIdx.x);
     for (int64_t tile = blockIdx.x; tile < n_tiles && ok; tile += gridDim.x) {
         const int64_t row = tile * TC_ROWS + tid;
-        // features of this thread's node -> BF16 A operand
-        {
-            float4 f[8];
+        // features -> BF16 A operand, then the next tile's features in flight
 #pragma unroll
-            for (int j = 0; j < 8; j++)
-                f[j] = row < rows ? reinterpret_cast<const float4 *>(X + row * 32)[j] : make_float4(0.f, 0.f, 0.f, 0.f);
-#pragma unroll
-            for (int q = 0; q < 4; q++) {
-                const uint4 w = make_uint4(pk_bf16(f[2 * q].x, f[2 * q].y), pk_bf16(f[2 * q].z, f[2 * q].w),
-                                           pk_bf16(f[2 * q + 1].x, f[2 * q + 1].y),
-                                           pk_bf16(f[2 * q + 1].z, f[2 * q + 1].w));
-                *reinterpret_cast<uint4 *>(smem + OFF_X + cano(tid, 8 * q, 128)) = w;
-            }
+        for (int q = 0; q < 4; q++) {
+            const uint4 w = make_uint4(pk_bf16(f[2 * q].x, f[2 * q].y), pk_bf16(f[2 * q].z, f[2 * q].w),
+                                       pk_bf16(f[2 * q + 1].x, f[2 * q + 1].y), pk_bf16(f[2 * q + 1].z, f[2 * q + 1].w));
+            *reinterpret_cast<uint4 *>(smem + OFF_X + cano(tid, 8 * q, 128)) = w;
         }
+        load_features(tile + gridDim.x);
         fence_async_smem();
         tc_fence_before();
         __syncthreads();
