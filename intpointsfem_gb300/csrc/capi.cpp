@@ -110,7 +110,7 @@ void free_all(ipfem_ctx *c)
     if (c->fcg_exec) cudaGraphExecDestroy(c->fcg_exec);
     {
         MlpBuffers &l = c->mlp;
-        void *lp[] = {l.params, l.grads, l.m, l.v, l.w1t, l.w2t, l.w3t, l.slot, l.pslot, l.X, l.O, l.M, l.y, l.Gh, l.r_old, l.loss,
+        void *lp[] = {l.params, l.grads, l.m, l.v, l.w1t, l.w2t, l.w3t, l.slot, l.pslot, l.X, l.O, l.M, l.y, l.Gh, l.p2, l.r_old, l.loss,
                       l.scal, l.H1, l.H2, l.dH1, l.dH2, l.dN, l.part, l.vec};
         for (void *p : lp)
             if (p) cudaFree(p);

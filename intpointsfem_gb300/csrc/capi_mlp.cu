@@ -105,7 +105,7 @@ ipfem_status fcg_device(ipfem_ctx *c, const double *d_b, double scale, double rt
     *fell_back = 0;
     if (!c->mlp.op_valid) launch_patch_operator(c);
     launch_fcg_init(c, d_b, scale, (float)rtol, max_it);
-    c->launches += 4;
+    c->launches += 3;
     const int batch = 16;
     if (!c->fcg_exec) {
         cudaGraph_t g = nullptr;
@@ -120,7 +120,7 @@ ipfem_status fcg_device(ipfem_ctx *c, const double *d_b, double scale, double rt
     for (;;) {
         MK(cudaGraphLaunch(c->fcg_exec, c->stream));
         launched += batch;
-        c->launches += 4 * batch;
+        c->launches += 3 * batch;
         MK(cudaMemcpyAsync(m.h_sc, m.sc, sizeof(CGScalarsT<float>), cudaMemcpyDeviceToHost, c->stream));
         MK(cudaStreamSynchronize(c->stream));
         if (m.h_sc->done || launched >= max_it + batch) break;
@@ -180,6 +180,7 @@ ipfem_status ipfem_mlp_init(ipfem_ctx *c, uint64_t seed)
         MK(alloc(&m.M, (size_t)s.n_nodes * 20));
         MK(alloc(&m.r_old, (size_t)s.neq));
         MK(alloc(&m.y, (size_t)s.neq));
+        MK(alloc(&m.p2, (size_t)s.neq));
         MK(cudaMalloc(&m.Gh, (size_t)s.n_nodes * 5 * 8));
         MK(alloc(&m.loss, 1));
         MK(alloc(&m.scal, 2));

@@ -182,6 +182,7 @@ struct MlpBuffers {
     float *M = nullptr;           // [5][n_nodes][4] triangular factor G (M = sigma G^T G sigma)
     float *y = nullptr;           // [neq] first stencil pass of the preconditioner
     void *Gh = nullptr;           // [5][n_nodes] BF16 copy of G (4 values per block) for the solves
+    float *p2 = nullptr;          // [neq] second search-direction buffer of the fused flexible CG
     float *r_old = nullptr;       // flexible-CG previous residual
     float *loss = nullptr, *scal = nullptr;
     // training scratch (allocated by the first gradient pass)

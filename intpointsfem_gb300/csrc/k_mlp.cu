@@ -401,28 +401,28 @@ __global__ void __launch_bounds__(256) k_tri_precond(int32_t n, GridInfo G, cons
 
 // ----------------------------------------- fused flexible-CG iteration (FP32)
 // One iteration = k_fcg_spmv, k_fcg_update_first, k_tri_precond (factor in
-// BF16) and k_fcg_pupdate, chained by programmatic dependent launch, with
-// the residual double-buffered (the caller alternates the buffers: the first
-// factor pass reads r_old at the lower neighbours) and the x/r update inside
-// the first factor pass.  The p update has its own pass so that the SpMV
-// gathers p alone (forming p = z + beta p_old for every gathered column
-// instead doubles the gathers: 51.7 against 43 us per SpMV at 400 x 400).
+// BF16), with the
+// search direction and the residual double-buffered (the caller alternates
+// the buffers): the p-update of the previous iteration is formed on the fly
+// inside the SpMV, the x/r update inside the first factor pass.
 
-// q = K p, partials of p.q; last CTA: alpha = rz / pq.  Node-ordered SELL
-// rows; the tangent and its column indices are streamed (evict-first) so
-// that p stays in L2.
+// p_new = z + beta p_old (the owner stores it, gatherers form it for their
+// columns), q = K p_new, partials of p_new.q; last CTA: alpha = rz / pq.
+// Node-ordered SELL rows; the tangent and its column indices are streamed
+// (evict-first) so that z and p_old stay in L2.
 template <bool PAT>
 __global__ void __launch_bounds__(256, 8) k_fcg_spmv(int32_t n, const int64_t *__restrict__ slice_base,
                                                   const int32_t *__restrict__ rowlen, const int32_t *__restrict__ scol,
                                                   const uint8_t *__restrict__ pat_id,
                                                   const int32_t *__restrict__ pat_off,
                                                   const float4 *__restrict__ K, const uint8_t *__restrict__ fixed,
-                                                  const float2 *__restrict__ p, float2 *__restrict__ q, float *part,
+                                                  const float2 *__restrict__ z, const float2 *__restrict__ p_old,
+                                                  float2 *__restrict__ p_new, float2 *__restrict__ q, float *part,
                                                   int64_t n_part, unsigned *ticket, CGScalarsT<float> *sc)
 {
     const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    // row metadata before the wait; p and the flag (written by the p
-    // update) after it
+    // row metadata before the wait; z, beta and the flag (written by the
+    // preconditioner pass) after it
     int64_t base = 0;
     int len = 0, pb = 0;
     if (i < n) {
@@ -433,6 +433,7 @@ __global__ void __launch_bounds__(256, 8) k_fcg_spmv(int32_t n, const int64_t *_
     pdl_wait();
     pdl_launch_dependents();
     if (*reinterpret_cast<volatile int *>(&sc->done)) return;
+    const float beta = *reinterpret_cast<volatile float *>(&sc->beta);
     float v[1] = {0.f};
     if (i < n) {
         const uint64_t keep = l2_policy_keep();
@@ -442,14 +443,17 @@ __global__ void __launch_bounds__(256, 8) k_fcg_spmv(int32_t n, const int64_t *_
             const int64_t s = base + sell_koff<true>(k);
             const int32_t c = PAT ? i + __ldg(&pat_off[pb + k]) : __ldcs(&scol[s]);
             const float4 a = __ldcs(&K[s]);
-            const float2 pp = ld_keep(&p[c], keep);
-            y0 = fmaf(a.y, pp.y, fmaf(a.x, pp.x, y0));
-            y1 = fmaf(a.w, pp.y, fmaf(a.z, pp.x, y1));
+            const float2 zz = ld_keep(&z[c], keep), pp = ld_keep(&p_old[c], keep);
+            const float px = fmaf(beta, pp.x, zz.x), py = fmaf(beta, pp.y, zz.y);
+            y0 = fmaf(a.y, py, fmaf(a.x, px, y0));
+            y1 = fmaf(a.w, py, fmaf(a.z, px, y1));
         }
         if (fixed[2 * (int64_t)i]) y0 = 0.f;
         if (fixed[2 * (int64_t)i + 1]) y1 = 0.f;
         q[i] = make_float2(y0, y1);
-        const float2 pn = p[i];
+        const float2 zi = z[i], pi = p_old[i];
+        const float2 pn = make_float2(fmaf(beta, pi.x, zi.x), fmaf(beta, pi.y, zi.y));
+        p_new[i] = pn;
         v[0] = fmaf(pn.y, y1, pn.x * y0);
     }
     if (fcg_partials<1>(v, part, n_part, ticket)) {
@@ -467,23 +471,6 @@ __global__ void __launch_bounds__(256, 8) k_fcg_spmv(int32_t n, const int64_t *_
             *ticket = 0u;
         }
     }
-}
-
-// p = z + beta p (with beta = 0 and p = 0 the first direction of a solve);
-// skipped once the solve is done
-__global__ void __launch_bounds__(256) k_fcg_pupdate(int32_t n, const float2 *__restrict__ z, float2 *__restrict__ p,
-                                                     const CGScalarsT<float> *sc)
-{
-    const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    // p (not written by the factor pass) before the wait, z and beta after it
-    float2 pp = make_float2(0.f, 0.f);
-    if (i < n) pp = p[i];
-    pdl_wait();
-    pdl_launch_dependents();
-    if (i >= n || *reinterpret_cast<const volatile int *>(&sc->done)) return;
-    const float beta = *reinterpret_cast<const volatile float *>(&sc->beta);
-    const float2 zz = z[i];
-    p[i] = make_float2(fmaf(beta, pp.x, zz.x), fmaf(beta, pp.y, zz.y));
 }
 
 // x += alpha p, r_new = r_old - alpha q (the owner stores it, the factor
@@ -919,12 +906,10 @@ void launch_fcg_init(ipfem_ctx *c, const double *d_b, double scale, float rtol, 
     k_fcg_init<<<fcg_grid(c), 256, 0, c->stream>>>(c->s.n_nodes, d_b, scale, m.x, m.r, m.p, c->mlp.r_old, m.part,
                                                    (int64_t)fcg_grid(c), c->d_counters + 4, m.sc, rtol, max_it);
     launch_precond(c, 0);
-    k_fcg_pupdate<<<fcg_grid(c), 256, 0, c->stream>>>(c->s.n_nodes, reinterpret_cast<const float2 *>(m.z),
-                                                      reinterpret_cast<float2 *>(m.p), m.sc);
 }
 
-// iteration k (par = k % 2): R[par] -> R[1-par] in the update, z from
-// R[1-par], p updated in place at the end
+// iteration k (par = k % 2): P[par] -> P[1-par] in the SpMV, R[par] -> R[1-par]
+// in the update, z from R[1-par]
 void launch_fcg_iteration(ipfem_ctx *c, int par)
 {
     MixedBuffers &m = c->mx;
@@ -932,25 +917,23 @@ void launch_fcg_iteration(ipfem_ctx *c, int par)
     const SellDev &L = m.dsell;
     GridInfo G{l.gr, l.gt};
     const int32_t n = c->s.n_nodes;
-    float2 *p = reinterpret_cast<float2 *>(m.p);
+    float2 *P[2] = {reinterpret_cast<float2 *>(m.p), reinterpret_cast<float2 *>(l.p2)};
     float2 *R[2] = {reinterpret_cast<float2 *>(m.r), reinterpret_cast<float2 *>(l.r_old)};
     const float2 *d2 = reinterpret_cast<const float2 *>(m.dinv);
     float *part = m.part;
     launch_pdl(use_row_stencils(c, L) ? k_fcg_spmv<true> : k_fcg_spmv<false>, fcg_grid(c), 256, c->stream, n,
                (const int64_t *)L.slice_base, (const int32_t *)L.rowlen, (const int32_t *)L.sell_col,
                (const uint8_t *)L.pat_id, (const int32_t *)L.pat_off, reinterpret_cast<const float4 *>(m.K),
-               (const uint8_t *)c->d_fixed, (const float2 *)p, reinterpret_cast<float2 *>(m.q), part,
-               (int64_t)fcg_grid(c), c->d_counters + 5, m.sc);
+               (const uint8_t *)c->d_fixed, reinterpret_cast<const float2 *>(m.z), (const float2 *)P[par],
+               P[1 - par], reinterpret_cast<float2 *>(m.q), part, (int64_t)fcg_grid(c), c->d_counters + 5, m.sc);
     launch_pdl(k_fcg_update_first, fcg_grid(c), 256, c->stream, n, G, reinterpret_cast<const uint2 *>(l.Gh), d2,
-               (const float2 *)p, reinterpret_cast<const float2 *>(m.q), reinterpret_cast<float2 *>(m.x),
+               (const float2 *)P[1 - par], reinterpret_cast<const float2 *>(m.q), reinterpret_cast<float2 *>(m.x),
                (const float2 *)R[par], R[1 - par], reinterpret_cast<float2 *>(l.y), part, (int64_t)fcg_grid(c),
                c->d_counters + 6, m.sc, stall_window(c));
     float *part2 = reinterpret_cast<float *>(c->d_part);
     launch_pdl(k_tri_precond, fcg_grid(c), 256, c->stream, n, G, reinterpret_cast<const uint2 *>(l.Gh), d2,
                reinterpret_cast<const float2 *>(l.y), reinterpret_cast<const float *>(R[1 - par]),
                reinterpret_cast<const float *>(R[par]), m.z, part2, (int64_t)fcg_grid(c), c->d_counters + 7, m.sc);
-    launch_pdl(k_fcg_pupdate, fcg_grid(c), 256, c->stream, n, reinterpret_cast<const float2 *>(m.z), p,
-               (const CGScalarsT<float> *)m.sc);
 }
 
 // ------------------------------------------------------------ training pass
