@@ -1074,6 +1074,18 @@ ipfem_status ipfem_set_state(ipfem_ctx *c, int field, const double *in)
     case 0: CK(cudaMemcpyAsync(c->d_eps_p, in, 4 * n * sizeof(double), cudaMemcpyHostToDevice, c->stream)); break;
     case 1: CK(cudaMemcpyAsync(c->d_sigma, in, 4 * n * sizeof(double), cudaMemcpyHostToDevice, c->stream)); break;
     case 2: CK(cudaMemcpyAsync(c->d_alpha, in, n * sizeof(double), cudaMemcpyHostToDevice, c->stream)); break;
+    case 3: {
+        // m_type as double (0 elastic, 1 plane or edge, -1 apex) -> int8
+        std::vector<int8_t> h((size_t)n);
+        for (int64_t k = 0; k < n; k++) {
+            if (!(in[k] == 0.0 || in[k] == 1.0 || in[k] == -1.0))
+                return fail(c, IPFEM_INVALID, "m_type values must be 0, 1 or -1");
+            h[(size_t)k] = (int8_t)in[k];
+        }
+        CK(cudaMemcpyAsync(c->d_mtype, h.data(), (size_t)n, cudaMemcpyHostToDevice, c->stream));
+        CK(cudaStreamSynchronize(c->stream));
+        return IPFEM_OK;
+    }
     default: return fail(c, IPFEM_INVALID, "bad state field");
     }
     CK(cudaStreamSynchronize(c->stream));
