@@ -145,6 +145,101 @@ std::string build_sell(const Setup &s, bool sorted, bool pair, SellLayout &L)
     return "";
 }
 
+// Upper-only FP32 layout.  The FP32 tangent is symmetric block for block:
+// the assembly adds each element entry and its mirror with the same value, in
+// the same colour order, so the stored lower block (i, j) is exactly the
+// transpose of (j, i).  Row i keeps only (i, c >= i), diagonal first, in slot
+// pairs with rows in node order; an SpMV reads a lower block as the transpose
+// of row j's block at position q.  Summing the lower blocks first (ascending
+// j) and then the stored ones keeps the ascending-column order of the full
+// layout, so every SpMV gives the same bits at half the tangent bytes.
+std::string build_sell_sym(const Setup &s, SellLayout &L)
+{
+    L = SellLayout();
+    L.pair = true;
+    L.sym = true;
+    const int32_t n = s.n_nodes;
+    const int64_t ns = ((int64_t)n + 31) / 32;
+    std::vector<int64_t> first(n);   // index of the diagonal block in row i's nodal list
+    L.sell_node.resize(n);
+    L.rowlen.resize(n);
+    for (int32_t i = 0; i < n; i++) {
+        L.sell_node[i] = i;
+        const int32_t *c0 = s.col.data() + s.row_ptr[i], *c1 = s.col.data() + s.row_ptr[i + 1];
+        const int32_t *d = std::lower_bound(c0, c1, i);
+        if (d == c1 || *d != i) return "a row has no diagonal block";
+        first[i] = d - c0;
+        L.rowlen[i] = (int32_t)(c1 - d);
+    }
+    L.slice_base.assign((size_t)ns + 1, 0);
+    for (int64_t sl = 0; sl < ns; sl++) {
+        int32_t w = 0;
+        for (int64_t t = sl * 32; t < std::min<int64_t>(n, sl * 32 + 32); t++) w = std::max(w, L.rowlen[t]);
+        w += w & 1;
+        L.slice_base[sl + 1] = L.slice_base[sl] + 32 * (int64_t)w;
+    }
+    L.n_sell = L.slice_base[ns];
+    if (L.n_sell > INT32_MAX / 2) return "matrix too large for 32-bit block slots";
+    L.sell_col.assign((size_t)L.n_sell, 0);
+    L.bsr_to_sell.assign((size_t)s.n_blocks, -1);
+    L.diag_blk.resize(n);
+    for (int32_t i = 0; i < n; i++) {
+        for (int64_t k = 0; k < L.rowlen[i]; k++) {
+            const int64_t slot = sell_slot(L, i, k);
+            L.sell_col[slot] = s.col[s.row_ptr[i] + first[i] + k];
+            L.bsr_to_sell[s.row_ptr[i] + first[i] + k] = slot;
+        }
+        for (int64_t k = L.rowlen[i]; k < (L.slice_base[i / 32 + 1] - L.slice_base[i / 32]) / 32; k++)
+            L.sell_col[sell_slot(L, i, k)] = i;
+        L.diag_blk[i] = sell_slot(L, i, 0);
+    }
+    // lower blocks: -2 - slot of the stored twin; (position, stencil) lists
+    std::map<std::vector<int32_t>, int> index;
+    std::vector<int32_t> key;
+    L.tpat_id.resize(n);
+    for (int32_t i = 0; i < n; i++) {
+        key.clear();
+        for (int64_t k = 0; k < first[i]; k++) {
+            const int32_t j = s.col[s.row_ptr[i] + k];
+            const int32_t *c0 = s.col.data() + s.row_ptr[j] + first[j], *c1 = s.col.data() + s.row_ptr[j + 1];
+            const int32_t *f = std::lower_bound(c0, c1, i);
+            if (f == c1 || *f != i) return "the block pattern is not symmetric";
+            const int32_t q = (int32_t)(f - c0);
+            L.bsr_to_sell[s.row_ptr[i] + k] = -2 - sell_slot(L, j, q);
+            key.push_back(j - i);
+            key.push_back(q);
+        }
+        if ((int)key.size() > 2 * kPatLen) return "a row has more lower blocks than a stencil holds";
+        auto it = index.find(key);
+        if (it == index.end()) {
+            if ((int)index.size() == kPatMax) return "more transposed stencils than 8-bit ids";
+            it = index.emplace(key, (int)index.size()).first;
+            L.tpat.resize((size_t)index.size() * kPatLen * 2, 0);
+            L.tpat_len.push_back((int32_t)key.size() / 2);
+            std::copy(key.begin(), key.end(), L.tpat.begin() + (size_t)it->second * kPatLen * 2);
+        }
+        L.tpat_id[i] = (uint8_t)it->second;
+    }
+    L.n_tpat = (int)index.size();
+    const int nn = s.nn, nd = s.nd;
+    L.el_blk.resize((size_t)s.n_el * nn * nn);
+    parallel_for(s.n_el, [&](int64_t e) {
+        for (int a = 0; a < nn; a++) {
+            const int32_t r = s.dofs[(size_t)e * nd + 2 * a] >> 1;
+            const int32_t *b0 = s.col.data() + s.row_ptr[r], *b1 = s.col.data() + s.row_ptr[r + 1];
+            for (int b = 0; b < nn; b++) {
+                const int32_t c = s.dofs[(size_t)e * nd + 2 * b] >> 1;
+                const int64_t j = std::lower_bound(b0, b1, c) - b0;
+                const int64_t slot = L.bsr_to_sell[s.row_ptr[r] + j];
+                L.el_blk[((size_t)e * nn + a) * nn + b] = c >= r ? (int32_t)slot : -1;
+            }
+        }
+    });
+    build_row_stencils(L);
+    if (L.n_pat == 0) return "the upper lists have no row stencils";
+    return "";
+}
+
 // Row stencils: the column offsets (column - node) of a row in slot order.
 // On a structured node grid a few dozen distinct stencils cover every row
 // (interior vertex, edge and centre nodes of the quadrilaterals plus their

@@ -57,6 +57,16 @@ struct SellLayout {
     std::vector<uint8_t> pat_id;         // [n_nodes], empty without stencils
     std::vector<int32_t> pat_off;        // [n_pat * kPatLen]
     int n_pat = 0;
+    // upper-only layout (build_sell_sym, FP32): row i stores its blocks
+    // (i, c >= i); the lower block (i, j < i) is the transpose of the stored
+    // (j, i), at position q of row j.  Transposed stencils list, per row, the
+    // lower neighbours in ascending order as (offset j - i, q) pairs;
+    // bsr_to_sell holds -2 - slot for a lower block, el_blk -1.
+    bool sym = false;
+    std::vector<uint8_t> tpat_id;        // [n_nodes]
+    std::vector<int32_t> tpat;           // [n_tpat * kPatLen * 2] (offset, q)
+    std::vector<int32_t> tpat_len;       // [n_tpat]
+    int n_tpat = 0;
 };
 
 // the same on the device
@@ -68,6 +78,10 @@ struct SellDev {
     int32_t *pat_off = nullptr;
     int n_pat = 0;
     bool sorted = false;                 // the FP32 layouts use slot pairs, the FP64 layouts do not
+    bool sym = false;                    // upper-only layout (always with row and transposed stencils)
+    uint8_t *tpat_id = nullptr;
+    int2 *tpat = nullptr;                // [n_tpat * kPatLen] (offset, q)
+    int32_t *tpat_len = nullptr;
 };
 
 // buffers of the mixed-precision solve (FP32 tangent and CG)
@@ -76,6 +90,12 @@ struct MixedBuffers {
     float *K = nullptr;           // [sell.n_sell*4]
     SellLayout sell;              // node-ordered rows (the FP32 SpMV is gather-bound)
     SellDev dsell;
+    // the upper-only layout, used with row stencils where it can be built
+    // (structured grids): half the tangent bytes of `sell`
+    float *Ks = nullptr;          // [sym.n_sell*4]
+    SellLayout sym;
+    SellDev dsym;
+    bool have_sym = false;
     float *dinv = nullptr;        // [neq]
     float *binv = nullptr;        // [n_nodes*4] block-Jacobi inverses
     float *x = nullptr, *r = nullptr, *z = nullptr, *p = nullptr, *q = nullptr;
@@ -151,6 +171,9 @@ __device__ __forceinline__ int64_t sell_koff(int k)
 }
 #endif
 void build_row_stencils(SellLayout &L);
+// the upper-only FP32 layout with its row and transposed stencils; returns an
+// empty string, or why it cannot be built (the full layout is used then)
+std::string build_sell_sym(const Setup &s, SellLayout &L);
 int32_t greedy_coloring(int32_t n_el, int32_t n_nodes, const int32_t *connects, int32_t *el_color);
 void elastic_constants(double E, double nu, ElasticConstH &el);
 // message returned by ipfem_last_error(NULL) on the calling thread

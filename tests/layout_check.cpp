@@ -67,6 +67,53 @@ static int check(const Setup &s, const SellLayout &L, const char *name)
     return 0;
 }
 
+// the upper-only layout: every stored block, every lower block through its
+// stored twin (bsr_to_sell and the transposed stencils), the block map of the
+// assembly (-1 for lower pairs) and the diagonal map
+static int check_sym(const Setup &s, const SellLayout &L)
+{
+    std::vector<char> used((size_t)L.n_sell, 0);
+    int64_t stored = 0, lower = 0;
+    for (int32_t i = 0; i < s.n_nodes; i++) {
+        int64_t k_up = 0, k_lo = 0;
+        const int tp = L.tpat_id[(size_t)i];
+        for (int64_t b = s.row_ptr[i]; b < s.row_ptr[i + 1]; b++) {
+            const int32_t c = s.col[(size_t)b];
+            const int64_t code = L.bsr_to_sell[(size_t)b];
+            if (c >= i) {
+                const int64_t slot = sell_slot(L, i, k_up);
+                if (code != slot) return fail("sym block map", i, c);
+                if (L.sell_col[(size_t)slot] != c) return fail("sym column", i, c);
+                if (used[(size_t)slot]++) return fail("sym slot used twice", i, c);
+                if (i + L.pat_off[(size_t)L.pat_id[(size_t)i] * kPatLen + k_up] != c) return fail("sym stencil", i, c);
+                if (c == i && L.diag_blk[(size_t)i] != slot) return fail("sym diagonal", i, c);
+                k_up++;
+                stored++;
+            } else {
+                const int32_t off = L.tpat[((size_t)tp * kPatLen + k_lo) * 2];
+                const int32_t q = L.tpat[((size_t)tp * kPatLen + k_lo) * 2 + 1];
+                if (i + off != c) return fail("transposed stencil offset", i, c);
+                const int64_t twin = sell_slot(L, c, q);
+                if (code != -2 - twin) return fail("lower block code", i, c);
+                if (L.sell_col[(size_t)twin] != i) return fail("twin column", i, c);
+                k_lo++;
+                lower++;
+            }
+        }
+        if (k_up != L.rowlen[(size_t)i] || k_lo != L.tpat_len[(size_t)tp]) return fail("sym row length", i, k_up);
+    }
+    for (int64_t e = 0; e < s.n_el; e++)
+        for (int a = 0; a < s.nn; a++)
+            for (int b = 0; b < s.nn; b++) {
+                const int32_t r = s.dofs[(size_t)e * s.nd + 2 * a] >> 1, c = s.dofs[(size_t)e * s.nd + 2 * b] >> 1;
+                const int32_t eb = L.el_blk[((size_t)e * s.nn + a) * s.nn + b];
+                if (c < r ? eb != -1 : (eb < 0 || L.sell_col[(size_t)eb] != c)) return fail("sym element map", e, a);
+            }
+    std::printf("fp32-sym stencils %d slots %lld sectors %lld tstencils %d stored %lld lower %lld\n", L.n_pat,
+                (long long)L.n_sell, (long long)((L.n_sell + 1) / 2), L.n_tpat, (long long)stored, (long long)lower);
+    return 0;
+}
+
 int main(int argc, char **argv)
 {
     if (argc < 3) return 2;
@@ -120,6 +167,10 @@ int main(int argc, char **argv)
     build_row_stencils(pair);
     bad |= check(s, single, "fp32-single");
     bad |= check(s, pair, "fp32-pairs");
+    SellLayout sym;
+    const std::string es = build_sell_sym(s, sym);
+    if (es.empty()) bad |= check_sym(s, sym);
+    else std::printf("fp32-sym none: %s\n", es.c_str());
     ipfem_wellbore_free(w);
     if (g) ipfem_gmsh_free(g);
     return bad;

@@ -39,7 +39,11 @@ def _run(exe, *args):
         m = re.match(r"(\S+) stencils (\d+) slots (\d+) sectors (\d+)", line)
         if m:
             out[m.group(1)] = tuple(int(x) for x in m.groups()[1:])
-    assert set(out) == {"fp64", "fp32-single", "fp32-pairs"}, p.stdout
+        m = re.match(r"fp32-sym stencils (\d+) slots (\d+) sectors (\d+) tstencils (\d+) stored (\d+) lower (\d+)",
+                     line)
+        if m:
+            out["fp32-sym"] = tuple(int(x) for x in m.groups())
+    assert {"fp64", "fp32-single", "fp32-pairs"} <= set(out), p.stdout
     return out
 
 
@@ -54,6 +58,12 @@ def test_wellbore_layouts(checker, n):
         assert st["fp64"] == 16
         # slot pairs: fewer 32-byte sectors of FP32 blocks per SpMV than one slot per lane
         assert out["fp32-pairs"][2] < 0.9 * out["fp32-single"][2]
+        # the upper-only layout: 11 upper and 19 transposed stencils, the
+        # stored and lower blocks make up the nodal pattern, about half the slots
+        ns, slots, _, nt, stored, lower = out["fp32-sym"]
+        assert (ns, nt) == (11, 19)
+        assert stored + lower == (8 * n + 1) ** 2 and stored - lower == (2 * n + 1) ** 2
+        assert slots < 0.55 * out["fp32-pairs"][1]
 
 
 @pytest.mark.parametrize("order,tri", [(1, ()), (2, ()), (3, ()), (2, (1,))])
