@@ -72,14 +72,21 @@ cudaError_t upload_sell(const SellLayout &L, bool sorted, SellDev &D, cudaStream
         ck(upload(&D.pat_off, L.pat_off, t));
         D.n_pat = L.n_pat;
     }
+    if (L.sym) {
+        ck(upload(&D.tpat_id, L.tpat_id, t));
+        ck(upload(&D.tpat_len, L.tpat_len, t));
+        ck(upload(reinterpret_cast<int32_t **>(&D.tpat), L.tpat, t));
+    }
     D.n_sell = L.n_sell;
     D.sorted = sorted;
+    D.sym = L.sym;
     return e;
 }
 
 void free_sell(SellDev &D)
 {
-    void *ptrs[] = {D.slice_base, D.diag_blk, D.sell_col, D.rowlen, D.sell_node, D.el_blk, D.pat_id, D.pat_off};
+    void *ptrs[] = {D.slice_base, D.diag_blk, D.sell_col, D.rowlen, D.sell_node, D.el_blk, D.pat_id, D.pat_off,
+                    D.tpat_id, D.tpat_len, D.tpat};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     D = SellDev();
@@ -89,6 +96,7 @@ void free_all(ipfem_ctx *c)
 {
     free_sell(c->dsell);
     free_sell(c->mx.dsell);
+    free_sell(c->mx.dsym);
     void *ptrs[] = {c->d_dphi, c->d_weight, c->d_mat, c->d_f0, c->d_df, c->d_dofs, c->d_color_els, c->d_inc,
                     c->d_fixed, c->d_K,
                     c->d_dinv, c->d_eps_p, c->d_sigma, c->d_alpha, c->d_mtype, c->d_u, c->d_rhs, c->d_strain,
@@ -98,7 +106,8 @@ void free_all(ipfem_ctx *c)
         if (p) cudaFree(p);
     {
         MixedBuffers &m = c->mx;
-        void *mp[] = {m.dphi, m.K, m.dinv, m.binv, m.x, m.r, m.z, m.p, m.q, m.part, m.sc, m.strain32, m.sigw32, m.fe32};
+        void *mp[] = {m.dphi, m.K, m.Ks, m.dinv, m.binv, m.x, m.r, m.z, m.p, m.q, m.part, m.sc, m.strain32, m.sigw32,
+                      m.fe32};
         for (void *p : mp)
             if (p) cudaFree(p);
         if (m.h_sc) cudaFreeHost(m.h_sc);
@@ -110,7 +119,7 @@ void free_all(ipfem_ctx *c)
     if (c->fcg_exec) cudaGraphExecDestroy(c->fcg_exec);
     {
         MlpBuffers &l = c->mlp;
-        void *lp[] = {l.params, l.grads, l.m, l.v, l.w1t, l.w2t, l.w3t, l.slot, l.pslot, l.X, l.O, l.M, l.y, l.Gh, l.p2, l.r_old, l.loss,
+        void *lp[] = {l.params, l.grads, l.m, l.v, l.w1t, l.w2t, l.w3t, l.slot, l.pslot, l.slot_s, l.pslot_s, l.X, l.O, l.M, l.y, l.Gh, l.p2, l.r_old, l.loss,
                       l.scal, l.H1, l.H2, l.dH1, l.dH2, l.dN, l.part, l.vec};
         for (void *p : lp)
             if (p) cudaFree(p);
@@ -495,6 +504,12 @@ ipfem_status ipfem_set_precision(ipfem_ctx *c, int mode)
         build_row_stencils(m.sell);
         ck(upload_sell(m.sell, false, m.dsell, c->stream));
         ck(dalloc(&m.K, (size_t)m.sell.n_sell * 4));
+        // the upper-only layout where the grid has row and transposed stencils
+        m.have_sym = build_sell_sym(s, m.sym).empty();
+        if (m.have_sym) {
+            ck(upload_sell(m.sym, false, m.dsym, c->stream));
+            ck(dalloc(&m.Ks, (size_t)m.sym.n_sell * 4));
+        }
         ck(dalloc(&m.dinv, (size_t)s.neq));
         ck(dalloc(&m.binv, (size_t)s.n_nodes * 4));
         ck(dalloc(&m.x, (size_t)s.neq));
@@ -601,6 +616,9 @@ ipfem_status ipfem_set_row_stencils(ipfem_ctx *c, int on)
                 *e = nullptr;
             }
     }
+    // with the upper-only FP32 layout the switch also selects the layout the
+    // FP32 tangent lives in: it has to be assembled again
+    if (on != c->row_stencils && c->mx.have_sym) c->tangent_valid = false;
     c->row_stencils = on;
     return IPFEM_OK;
 }
@@ -625,12 +643,25 @@ ipfem_status ipfem_get_stiffness(ipfem_ctx *c, int64_t *row_ptr, int32_t *col, d
     if (row_ptr) std::memcpy(row_ptr, s.row_ptr.data(), s.row_ptr.size() * sizeof(int64_t));
     if (col) std::memcpy(col, s.col.data(), s.col.size() * sizeof(int32_t));
     if (vals && c->precision == 1) {
-        const SellLayout &L = c->mx.sell;
+        const bool sym = use_sym32(c);
+        const SellLayout &L = sym ? c->mx.sym : c->mx.sell;
         std::vector<float> h((size_t)L.n_sell * 4);
-        CK(cudaMemcpyAsync(h.data(), c->mx.K, h.size() * sizeof(float), cudaMemcpyDeviceToHost, c->stream));
+        CK(cudaMemcpyAsync(h.data(), sym ? c->mx.Ks : c->mx.K, h.size() * sizeof(float), cudaMemcpyDeviceToHost,
+                           c->stream));
         CK(cudaStreamSynchronize(c->stream));
-        for (int64_t k = 0; k < s.n_blocks; k++)
-            for (int j = 0; j < 4; j++) vals[4 * k + j] = h[4 * L.bsr_to_sell[k] + j];
+        for (int64_t k = 0; k < s.n_blocks; k++) {
+            const int64_t code = L.bsr_to_sell[k];
+            if (code >= 0) {
+                for (int j = 0; j < 4; j++) vals[4 * k + j] = h[4 * code + j];
+            } else {
+                // a lower block of the upper-only layout: the transpose of its stored twin
+                const float *t = &h[4 * (-2 - code)];
+                vals[4 * k + 0] = t[0];
+                vals[4 * k + 1] = t[2];
+                vals[4 * k + 2] = t[1];
+                vals[4 * k + 3] = t[3];
+            }
+        }
     } else if (vals) {
         std::vector<double> h((size_t)s.sell.n_sell * 4);
         CK(cudaMemcpyAsync(h.data(), c->d_K, h.size() * sizeof(double), cudaMemcpyDeviceToHost, c->stream));

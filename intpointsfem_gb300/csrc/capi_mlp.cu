@@ -191,6 +191,16 @@ ipfem_status ipfem_mlp_init(ipfem_ctx *c, uint64_t seed)
         MK(alloc(&m.pslot, pslot.size()));
         MK(cudaMemcpyAsync(m.pslot, pslot.data(), pslot.size() * sizeof(int32_t), cudaMemcpyHostToDevice,
                            c->stream));
+        if (c->mx.have_sym) {
+            // block codes of the upper-only layout: a lower block is -2 - slot of its stored twin
+            const std::vector<int32_t> ss = patch_slots(s, c->mx.sym, m.gr, m.gt);
+            MK(alloc(&m.slot_s, ss.size()));
+            MK(cudaMemcpyAsync(m.slot_s, ss.data(), ss.size() * sizeof(int32_t), cudaMemcpyHostToDevice, c->stream));
+            const std::vector<int32_t> ps = pair_slots(s, c->mx.sym, m.gr, m.gt);
+            MK(alloc(&m.pslot_s, ps.size()));
+            MK(cudaMemcpyAsync(m.pslot_s, ps.data(), ps.size() * sizeof(int32_t), cudaMemcpyHostToDevice,
+                               c->stream));
+        }
         MK(cudaStreamSynchronize(c->stream));
         int64_t nf = 0;
         for (uint8_t f : s.fixed) nf += f ? 0 : 1;

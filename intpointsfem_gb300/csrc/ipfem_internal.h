@@ -169,6 +169,17 @@ __device__ __forceinline__ int64_t sell_koff(int k)
 {
     return PAIR ? 64 * (int64_t)(k >> 1) + (k & 1) : 32 * (int64_t)k;
 }
+// upper-only FP32 layout (rows in node order, slot pairs): the slot of the
+// block at position q of row j, i.e. the stored twin of a lower block
+__device__ __forceinline__ int64_t sym_twin_slot(const int64_t *__restrict__ slice_base, int32_t j, int q)
+{
+    return sell_row0<true>(__ldg(&slice_base[j >> 5]), j & 31) + sell_koff<true>(q);
+}
+// a 2x2 block (row-major float4) transposed
+__device__ __forceinline__ float4 transpose4(float4 b)
+{
+    return make_float4(b.x, b.z, b.y, b.w);
+}
 #endif
 void build_row_stencils(SellLayout &L);
 // the upper-only FP32 layout with its row and transposed stencils; returns an
@@ -199,6 +210,7 @@ struct MlpBuffers {
     void *w1t = nullptr, *w2t = nullptr, *w3t = nullptr;   // BF16 [128][32], [128][128], [24][128] (n, k)
     int32_t *slot = nullptr;      // [9][n_nodes] FP32-tangent slot of block (i, nbr(i, k)) or -1
     int32_t *pslot = nullptr;     // [25][n_nodes] slot of block (nbr(i, k), nbr(i, l)), k, l < 5, or -1
+    int32_t *slot_s = nullptr, *pslot_s = nullptr;   // the same codes for the upper-only layout (-2 - slot: transposed)
     float nf = 0.f;               // number of free dofs
     float *X = nullptr;           // [n_nodes][32] features of the current tangent
     float *O = nullptr;           // [n_nodes][20] network output
@@ -279,6 +291,20 @@ namespace ipfem {
 inline bool use_row_stencils(const ipfem_ctx *c, const SellDev &L)
 {
     return c->row_stencils != 0 && L.n_pat > 0 && L.pat_id != nullptr;
+}
+// whether the FP32 tangent lives in the upper-only layout (with row stencils on)
+inline bool use_sym32(const ipfem_ctx *c)
+{
+    return c->mx.have_sym && c->row_stencils != 0;
+}
+// the FP32 tangent's active layout and values
+inline const SellDev &fp32_layout(const ipfem_ctx *c)
+{
+    return use_sym32(c) ? c->mx.dsym : c->mx.dsell;
+}
+inline float *fp32_values(const ipfem_ctx *c)
+{
+    return use_sym32(c) ? c->mx.Ks : c->mx.K;
 }
 
 cudaError_t upload_constants(const ElasticConstH &el);

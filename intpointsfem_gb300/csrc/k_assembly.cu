@@ -304,10 +304,17 @@ __global__ void __launch_bounds__(kStiffWarps * 32) k_stiffness(int32_t n_in_col
                 blk[2 * ca + cb] = blk[2 * ca + cb] + v;
                 if (ca != cb) blk[2 * cb + ca] = blk[2 * cb + ca] + v;
             } else {
-                T *b1 = K + 4 * (size_t)__ldg(&eb[ma * E::NN + nb]);
-                T *b2 = K + 4 * (size_t)__ldg(&eb[nb * E::NN + ma]);
-                b1[2 * ca + cb] = b1[2 * ca + cb] + v;
-                b2[2 * cb + ca] = b2[2 * cb + ca] + v;
+                // an entry and its mirror; the upper-only FP32 layout stores
+                // one of the two blocks (the other's map entry is -1)
+                const int32_t s1 = __ldg(&eb[ma * E::NN + nb]), s2 = __ldg(&eb[nb * E::NN + ma]);
+                if (s1 >= 0) {
+                    T *b1 = K + 4 * (size_t)s1;
+                    b1[2 * ca + cb] = b1[2 * ca + cb] + v;
+                }
+                if (s2 >= 0) {
+                    T *b2 = K + 4 * (size_t)s2;
+                    b2[2 * cb + ca] = b2[2 * cb + ca] + v;
+                }
             }
         }
     }
@@ -443,7 +450,8 @@ void launch_jacobi(ipfem_ctx *c)
     const unsigned g2 = (unsigned)((s.n_nodes + 255) / 256);
     if (c->precision == 1) {
         MixedBuffers &m = c->mx;
-        k_jacobi<float><<<g2, 256, 0, c->stream>>>(s.n_nodes, m.dsell.diag_blk, m.K, c->d_fixed, m.dinv, m.binv);
+        k_jacobi<float><<<g2, 256, 0, c->stream>>>(s.n_nodes, fp32_layout(c).diag_blk, fp32_values(c), c->d_fixed,
+                                                   m.dinv, m.binv);
     } else {
         k_jacobi<double><<<g2, 256, 0, c->stream>>>(s.n_nodes, c->dsell.diag_blk, c->d_K, c->d_fixed, c->d_dinv,
                                                     c->d_binv);
@@ -453,16 +461,17 @@ void launch_jacobi(ipfem_ctx *c)
 void launch_stiffness32(ipfem_ctx *c)
 {
     const Setup &s = c->s;
-    MixedBuffers &m = c->mx;
-    cudaMemsetAsync(m.K, 0, (size_t)m.dsell.n_sell * 4 * sizeof(float), c->stream);
+    const SellDev &L = fp32_layout(c);
+    float *K = fp32_values(c);
+    cudaMemsetAsync(K, 0, (size_t)L.n_sell * 4 * sizeof(float), c->stream);
     for (int col = 0; col < s.n_colors; col++) {
         const int32_t first = s.color_ptr[col], n = s.color_ptr[col + 1] - first;
         if (n == 0) continue;
         const unsigned grid = (unsigned)((n + kStiffWarps - 1) / kStiffWarps);
         auto kern = s.order == 1 ? k_stiffness<float, 1> : (s.order == 3 ? k_stiffness<float, 3> :
                                                                            k_stiffness<float, 2>);
-        kern<<<grid, kStiffWarps * 32, 0, c->stream>>>(n, c->d_color_els + first, s.n_ip, m.dphi, c->d_dep,
-                                                       m.dsell.el_blk, m.K);
+        kern<<<grid, kStiffWarps * 32, 0, c->stream>>>(n, c->d_color_els + first, s.n_ip, c->mx.dphi, c->d_dep,
+                                                       L.el_blk, K);
     }
     launch_jacobi(c);
 }

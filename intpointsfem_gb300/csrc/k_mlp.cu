@@ -104,8 +104,16 @@ __device__ __forceinline__ float2 sqrt2(float2 d)
     return make_float2(sqrtf(d.x), sqrtf(d.y));
 }
 
+// block (i, j) of the FP32 tangent from its slot code: s >= 0 the stored
+// block, s <= -2 the transpose of the stored twin -2 - s (the lower blocks of
+// the upper-only layout); -1 (no block) is the caller's case
+__device__ __forceinline__ float4 tangent_block(const float4 *__restrict__ K, int32_t s)
+{
+    return s >= 0 ? K[s] : transpose4(K[-2 - s]);
+}
+
 // features X[n][32] from the FP32 tangent: scaled couplings to the 8
-// neighbours (slot[k][n] = SELL slot of block (i, nbr(i, k)) or -1)
+// neighbours (slot[k][n] = slot code of block (i, nbr(i, k)), -1 for none)
 __global__ void __launch_bounds__(256) k_patch_features(int32_t n, GridInfo G, const float4 *__restrict__ K,
                                                         const int32_t *__restrict__ slot,
                                                         const float2 *__restrict__ dinv, float *__restrict__ X)
@@ -120,8 +128,8 @@ __global__ void __launch_bounds__(256) k_patch_features(int32_t n, GridInfo G, c
         if (k == 4) continue;
         const int32_t s = slot[(int64_t)k * n + i];
         float4 f = make_float4(0.f, 0.f, 0.f, 0.f);
-        if (s >= 0) {
-            const float4 blk = K[s];
+        if (s != -1) {
+            const float4 blk = tangent_block(K, s);
             const float2 sj = sqrt2(dinv[patch_nbr(i, k, G)]);
             f = make_float4(blk.x * si.x * sj.x, blk.y * si.x * sj.y, blk.z * si.y * sj.x, blk.w * si.y * sj.y);
         }
@@ -473,6 +481,85 @@ __global__ void __launch_bounds__(256, 8) k_fcg_spmv(int32_t n, const int64_t *_
     }
 }
 
+// The same over the upper-only FP32 layout: per row the lower blocks
+// (transposes of their stored twins, ascending), then the stored blocks:
+// the full layout's column order, so the same bits.  The stored blocks go
+// through L2 normally, as the rows of the next two grid lines read them again.
+__global__ void __launch_bounds__(256, 8) k_fcg_spmv_sym(int32_t n, const int64_t *__restrict__ slice_base,
+                                                      const int32_t *__restrict__ rowlen,
+                                                      const uint8_t *__restrict__ pat_id,
+                                                      const int32_t *__restrict__ pat_off,
+                                                      const uint8_t *__restrict__ tpat_id,
+                                                      const int2 *__restrict__ tpat,
+                                                      const int32_t *__restrict__ tpat_len,
+                                                      const float4 *__restrict__ K, const uint8_t *__restrict__ fixed,
+                                                      const float2 *__restrict__ z, const float2 *__restrict__ p_old,
+                                                      float2 *__restrict__ p_new, float2 *__restrict__ q, float *part,
+                                                      int64_t n_part, unsigned *ticket, CGScalarsT<float> *sc)
+{
+    const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    int64_t base = 0;
+    int len = 0, pb = 0, tl = 0, tb = 0;
+    if (i < n) {
+        base = sell_row0<true>(__ldg(&slice_base[i >> 5]), i & 31);
+        len = __ldg(&rowlen[i]);
+        pb = (int)__ldg(&pat_id[i]) * kPatLen;
+        const int tp = __ldg(&tpat_id[i]);
+        tl = __ldg(&tpat_len[tp]);
+        tb = tp * kPatLen;
+    }
+    pdl_wait();
+    pdl_launch_dependents();
+    if (*reinterpret_cast<volatile int *>(&sc->done)) return;
+    const float beta = *reinterpret_cast<volatile float *>(&sc->beta);
+    float v[1] = {0.f};
+    if (i < n) {
+        const uint64_t keep = l2_policy_keep();
+        float y0 = 0.f, y1 = 0.f;
+#pragma unroll 2
+        for (int k = 0; k < tl; k++) {
+            const int2 e = __ldg(&tpat[tb + k]);
+            const int32_t c = i + e.x;
+            const float4 a = transpose4(__ldcg(&K[sym_twin_slot(slice_base, c, e.y)]));
+            const float2 zz = ld_keep(&z[c], keep), pp = ld_keep(&p_old[c], keep);
+            const float px = fmaf(beta, pp.x, zz.x), py = fmaf(beta, pp.y, zz.y);
+            y0 = fmaf(a.y, py, fmaf(a.x, px, y0));
+            y1 = fmaf(a.w, py, fmaf(a.z, px, y1));
+        }
+#pragma unroll 4
+        for (int k = 0; k < len; k++) {
+            const int32_t c = i + __ldg(&pat_off[pb + k]);
+            const float4 a = __ldcg(&K[base + sell_koff<true>(k)]);
+            const float2 zz = ld_keep(&z[c], keep), pp = ld_keep(&p_old[c], keep);
+            const float px = fmaf(beta, pp.x, zz.x), py = fmaf(beta, pp.y, zz.y);
+            y0 = fmaf(a.y, py, fmaf(a.x, px, y0));
+            y1 = fmaf(a.w, py, fmaf(a.z, px, y1));
+        }
+        if (fixed[2 * (int64_t)i]) y0 = 0.f;
+        if (fixed[2 * (int64_t)i + 1]) y1 = 0.f;
+        q[i] = make_float2(y0, y1);
+        const float2 zi = z[i], pi = p_old[i];
+        const float2 pn = make_float2(fmaf(beta, pi.x, zi.x), fmaf(beta, pi.y, zi.y));
+        p_new[i] = pn;
+        v[0] = fmaf(pn.y, y1, pn.x * y0);
+    }
+    if (fcg_partials<1>(v, part, n_part, ticket)) {
+        float o[1];
+        fcg_final<1>(part, n_part, o);
+        if (threadIdx.x == 0) {
+            const float pq = o[0];
+            sc->pq = pq;
+            if (!(pq > 0.f)) {
+                sc->done = 1;
+                sc->status = kStatusFallback;
+            } else {
+                sc->alpha = sc->rz / pq;
+            }
+            *ticket = 0u;
+        }
+    }
+}
+
 // x += alpha p, r_new = r_old - alpha q (the owner stores it, the factor
 // pass forms it for its neighbours), y = G (sigma * r_new); partials of
 // r_new.r_new; last CTA: convergence, stagnation and iteration limit
@@ -574,6 +661,48 @@ __global__ void __launch_bounds__(256) k_spmv32(int32_t n, const int64_t *__rest
         const int64_t s = base + sell_koff<true>(k);
         const float4 a = __ldcs(&K[s]);
         const float2 v = ld_keep(&x[PAT ? i + __ldg(&pat_off[pb + k]) : __ldg(&scol[s])], keep);
+        y0 = fmaf(a.x, v.x, fmaf(a.y, v.y, y0));
+        y1 = fmaf(a.z, v.x, fmaf(a.w, v.y, y1));
+    }
+    if (fixed[2 * (int64_t)i]) y0 = 0.f;
+    if (fixed[2 * (int64_t)i + 1]) y1 = 0.f;
+    y[i] = make_float2(y0, y1);
+}
+
+// the same over the upper-only layout: the lower blocks (transposes of their
+// stored twins, ascending) first, then the stored ones: the full layout's
+// column order, so the same bits
+__global__ void __launch_bounds__(256) k_spmv32_sym(int32_t n, const int64_t *__restrict__ slice_base,
+                                                    const int32_t *__restrict__ rowlen,
+                                                    const uint8_t *__restrict__ pat_id,
+                                                    const int32_t *__restrict__ pat_off,
+                                                    const uint8_t *__restrict__ tpat_id, const int2 *__restrict__ tpat,
+                                                    const int32_t *__restrict__ tpat_len, const float4 *__restrict__ K,
+                                                    const uint8_t *__restrict__ fixed, const float2 *__restrict__ x,
+                                                    float2 *__restrict__ y)
+{
+    const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int64_t base = sell_row0<true>(slice_base[i >> 5], i & 31);
+    const int len = rowlen[i];
+    const int pb = (int)__ldg(&pat_id[i]) * kPatLen;
+    const int tp = __ldg(&tpat_id[i]);
+    const int tl = __ldg(&tpat_len[tp]), tb = tp * kPatLen;
+    const uint64_t keep = l2_policy_keep();
+    float y0 = 0.f, y1 = 0.f;
+#pragma unroll 4
+    for (int k = 0; k < tl; k++) {
+        const int2 e = __ldg(&tpat[tb + k]);
+        const int32_t j = i + e.x;
+        const float4 a = transpose4(__ldcg(&K[sym_twin_slot(slice_base, j, e.y)]));
+        const float2 v = ld_keep(&x[j], keep);
+        y0 = fmaf(a.x, v.x, fmaf(a.y, v.y, y0));
+        y1 = fmaf(a.z, v.x, fmaf(a.w, v.y, y1));
+    }
+#pragma unroll 4
+    for (int k = 0; k < len; k++) {
+        const float4 a = __ldcg(&K[base + sell_koff<true>(k)]);
+        const float2 v = ld_keep(&x[i + __ldg(&pat_off[pb + k])], keep);
         y0 = fmaf(a.x, v.x, fmaf(a.y, v.y, y0));
         y1 = fmaf(a.z, v.x, fmaf(a.w, v.y, y1));
     }
@@ -702,8 +831,8 @@ __global__ void __launch_bounds__(256) k_kap_H(int32_t n, GridInfo G, const floa
 #pragma unroll
             for (int l = 0; l < NTRI; l++) {
                 const int32_t s = pslot[(int64_t)(NTRI * k + l) * n + i];
-                if (s < 0) continue;
-                const float4 kb = K[s];
+                if (s == -1) continue;
+                const float4 kb = tangent_block(K, s);
                 // Ahat[q][t] for q (row, node j_k), t (column, node j_l)
                 const float a00 = sl[k].x * kb.x * sl[l].x, a01 = sl[k].x * kb.y * sl[l].y;
                 const float a10 = sl[k].y * kb.z * sl[l].x, a11 = sl[k].y * kb.w * sl[l].y;
@@ -846,9 +975,9 @@ void launch_patch_features(ipfem_ctx *c, float *d_X)
 {
     const int32_t n = c->s.n_nodes;
     GridInfo G{c->mlp.gr, c->mlp.gt};
-    k_patch_features<<<(n + 255) / 256, 256, 0, c->stream>>>(n, G, reinterpret_cast<const float4 *>(c->mx.K),
-                                                             c->mlp.slot, reinterpret_cast<const float2 *>(c->mx.dinv),
-                                                             d_X);
+    k_patch_features<<<(n + 255) / 256, 256, 0, c->stream>>>(n, G, reinterpret_cast<const float4 *>(fp32_values(c)),
+                                                             use_sym32(c) ? c->mlp.slot_s : c->mlp.slot,
+                                                             reinterpret_cast<const float2 *>(c->mx.dinv), d_X);
 }
 
 // features -> network -> triangular factor, for the current FP32 tangent
@@ -914,18 +1043,26 @@ void launch_fcg_iteration(ipfem_ctx *c, int par)
 {
     MixedBuffers &m = c->mx;
     MlpBuffers &l = c->mlp;
-    const SellDev &L = m.dsell;
+    const SellDev &L = fp32_layout(c);
     GridInfo G{l.gr, l.gt};
     const int32_t n = c->s.n_nodes;
     float2 *P[2] = {reinterpret_cast<float2 *>(m.p), reinterpret_cast<float2 *>(l.p2)};
     float2 *R[2] = {reinterpret_cast<float2 *>(m.r), reinterpret_cast<float2 *>(l.r_old)};
     const float2 *d2 = reinterpret_cast<const float2 *>(m.dinv);
     float *part = m.part;
-    launch_pdl(use_row_stencils(c, L) ? k_fcg_spmv<true> : k_fcg_spmv<false>, fcg_grid(c), 256, c->stream, n,
-               (const int64_t *)L.slice_base, (const int32_t *)L.rowlen, (const int32_t *)L.sell_col,
-               (const uint8_t *)L.pat_id, (const int32_t *)L.pat_off, reinterpret_cast<const float4 *>(m.K),
-               (const uint8_t *)c->d_fixed, reinterpret_cast<const float2 *>(m.z), (const float2 *)P[par],
-               P[1 - par], reinterpret_cast<float2 *>(m.q), part, (int64_t)fcg_grid(c), c->d_counters + 5, m.sc);
+    if (L.sym)
+        launch_pdl(k_fcg_spmv_sym, fcg_grid(c), 256, c->stream, n, (const int64_t *)L.slice_base,
+                   (const int32_t *)L.rowlen, (const uint8_t *)L.pat_id, (const int32_t *)L.pat_off,
+                   (const uint8_t *)L.tpat_id, (const int2 *)L.tpat, (const int32_t *)L.tpat_len,
+                   reinterpret_cast<const float4 *>(fp32_values(c)), (const uint8_t *)c->d_fixed,
+                   reinterpret_cast<const float2 *>(m.z), (const float2 *)P[par], P[1 - par],
+                   reinterpret_cast<float2 *>(m.q), part, (int64_t)fcg_grid(c), c->d_counters + 5, m.sc);
+    else
+        launch_pdl(use_row_stencils(c, L) ? k_fcg_spmv<true> : k_fcg_spmv<false>, fcg_grid(c), 256, c->stream, n,
+                   (const int64_t *)L.slice_base, (const int32_t *)L.rowlen, (const int32_t *)L.sell_col,
+                   (const uint8_t *)L.pat_id, (const int32_t *)L.pat_off, reinterpret_cast<const float4 *>(m.K),
+                   (const uint8_t *)c->d_fixed, reinterpret_cast<const float2 *>(m.z), (const float2 *)P[par],
+                   P[1 - par], reinterpret_cast<float2 *>(m.q), part, (int64_t)fcg_grid(c), c->d_counters + 5, m.sc);
     launch_pdl(k_fcg_update_first, fcg_grid(c), 256, c->stream, n, G, reinterpret_cast<const uint2 *>(l.Gh), d2,
                (const float2 *)P[1 - par], reinterpret_cast<const float2 *>(m.q), reinterpret_cast<float2 *>(m.x),
                (const float2 *)R[par], R[1 - par], reinterpret_cast<float2 *>(l.y), part, (int64_t)fcg_grid(c),
@@ -999,12 +1136,16 @@ void patch_learn_grad(ipfem_ctx *c, const float *d_r, const float *d_e, int P, f
     // pair term
     float *z = m.vec, *ae = m.vec + neq, *az = m.vec + 2 * neq, *res = m.vec + 3 * neq, *g = m.vec + 4 * neq;
     float *y = m.vec + 5 * neq, *v = m.vec + 6 * neq;
-    const SellDev &L = x.dsell;
-    const float4 *K4 = reinterpret_cast<const float4 *>(x.K);
+    const SellDev &L = fp32_layout(c);
+    const float4 *K4 = reinterpret_cast<const float4 *>(fp32_values(c));
     const float w = P > 0 ? wp / (float)P : 0.f;
     auto spmv32 = [&](const float2 *xin, float2 *yout) {
-        (use_row_stencils(c, L) ? k_spmv32<true> : k_spmv32<false>)<<<gn, 256, 0, st>>>(
-            n, L.slice_base, L.rowlen, L.sell_node, L.sell_col, L.pat_id, L.pat_off, K4, c->d_fixed, xin, yout);
+        if (L.sym)
+            k_spmv32_sym<<<gn, 256, 0, st>>>(n, L.slice_base, L.rowlen, L.pat_id, L.pat_off, L.tpat_id, L.tpat,
+                                              L.tpat_len, K4, c->d_fixed, xin, yout);
+        else
+            (use_row_stencils(c, L) ? k_spmv32<true> : k_spmv32<false>)<<<gn, 256, 0, st>>>(
+                n, L.slice_base, L.rowlen, L.sell_node, L.sell_col, L.pat_id, L.pat_off, K4, c->d_fixed, xin, yout);
     };
     for (int p = 0; p < P && wp > 0.f; p++) {
         const float2 *r2 = reinterpret_cast<const float2 *>(d_r + (size_t)p * neq);
@@ -1025,7 +1166,7 @@ void patch_learn_grad(ipfem_ctx *c, const float *d_r, const float *d_e, int P, f
     }
     // Kaporin term (H in the dH1 buffer, free before the backward)
     float *H = m.dH1;
-    k_kap_H<<<gn, 256, 0, st>>>(n, G, Gm, K4, m.pslot, d2, m.O, H, m.part);
+    k_kap_H<<<gn, 256, 0, st>>>(n, G, Gm, K4, use_sym32(c) ? m.pslot_s : m.pslot, d2, m.O, H, m.part);
     k_kap_final<<<1, 256, 0, st>>>((int)gn, m.part, m.scal, m.loss, wk, m.nf);
     float *dO = m.dH2;                      // [n][20], free until dH2 is formed
     k_tri_dO<<<gn, 256, 0, st>>>(n, G, m.O, d2, m.dN, H, m.scal, wk, m.nf, dO);

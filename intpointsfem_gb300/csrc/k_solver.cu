@@ -326,6 +326,92 @@ __global__ void __launch_bounds__(kRedBlock) k_cg_spmv(int32_t n_nodes, const in
     }
 }
 
+// The same SpMV over the upper-only FP32 layout (row and transposed
+// stencils): row i first adds its lower blocks (i, j < i), read as the
+// transposes of their stored twins (j, i) in ascending j, then its stored
+// blocks (i, c >= i) in ascending c, which is the full layout's column order,
+// so q and p.q are the same bits.  The stored blocks are loaded through L2
+// (not evict-first): the rows of the next two grid lines read them again as
+// twins.
+__global__ void __launch_bounds__(kRedBlock) k_cg_spmv_sym(int32_t n_nodes, const int64_t *__restrict__ slice_base,
+                                                           const int32_t *__restrict__ rowlen,
+                                                           const uint8_t *__restrict__ pat_id,
+                                                           const int32_t *__restrict__ pat_off,
+                                                           const uint8_t *__restrict__ tpat_id,
+                                                           const int2 *__restrict__ tpat,
+                                                           const int32_t *__restrict__ tpat_len,
+                                                           const float *__restrict__ K, const uint8_t *__restrict__ fixed,
+                                                           const float *__restrict__ p, float *__restrict__ q,
+                                                           float *part, int64_t n_red, unsigned *ticket,
+                                                           CGScalarsT<float> *sc)
+{
+    __shared__ float s_pq[1][kRedStage];
+    const int32_t i = blockIdx.x * kRedBlock + threadIdx.x;
+    int32_t len = 0, pb = 0, tl = 0, tb = 0;
+    int64_t base = 0;
+    if (i < n_nodes) {
+        base = sell_row0<true>(__ldg(&slice_base[i >> 5]), i & 31);
+        len = __ldg(&rowlen[i]);
+        pb = (int)__ldg(&pat_id[i]) * kPatLen;
+        const int t = __ldg(&tpat_id[i]);
+        tl = __ldg(&tpat_len[t]);
+        tb = t * kPatLen;
+    }
+    pdl_wait();
+    pdl_launch_dependents();
+    if (*reinterpret_cast<volatile int *>(&sc->done)) return;
+    float v = 0.f;
+    if (i < n_nodes) {
+        const float2 *pv = reinterpret_cast<const float2 *>(p);
+        const float4 *K4 = reinterpret_cast<const float4 *>(K);
+        const uint64_t keep = l2_policy_keep();
+        float y0 = 0.f, y1 = 0.f;
+#pragma unroll 4
+        for (int k = 0; k < tl; k++) {
+            const int2 e = __ldg(&tpat[tb + k]);
+            const int32_t j = i + e.x;
+            const float4 a = transpose4(__ldcg(&K4[sym_twin_slot(slice_base, j, e.y)]));
+            const float2 xx = ld_keep(&pv[j], keep);
+            y0 = fmaf(a.x, xx.x, y0);
+            y0 = fmaf(a.y, xx.y, y0);
+            y1 = fmaf(a.z, xx.x, y1);
+            y1 = fmaf(a.w, xx.y, y1);
+        }
+#pragma unroll 4
+        for (int k = 0; k < len; k++) {
+            const int32_t c = i + __ldg(&pat_off[pb + k]);
+            const float4 a = __ldcg(&K4[base + sell_koff<true>(k)]);
+            const float2 xx = ld_keep(&pv[c], keep);
+            y0 = fmaf(a.x, xx.x, y0);
+            y0 = fmaf(a.y, xx.y, y0);
+            y1 = fmaf(a.z, xx.x, y1);
+            y1 = fmaf(a.w, xx.y, y1);
+        }
+        if (fixed[2 * (size_t)i]) y0 = 0.f;
+        if (fixed[2 * (size_t)i + 1]) y1 = 0.f;
+        reinterpret_cast<float2 *>(q)[i] = make_float2(y0, y1);
+        const float2 pp = pv[i];
+        v = fmaf(pp.y, y1, fmaf(pp.x, y0, 0.f));
+    }
+    s_pq[0][red_stage(threadIdx.x)] = v;
+    __syncthreads();
+    if (block_partials_staged<float, 1>(s_pq, part, n_red, ticket)) {
+        float o[1];
+        final_reduce<float, 1>(part, n_red, o);
+        if (threadIdx.x == 0) {
+            const float pq = o[0];
+            sc->pq = pq;
+            if (!(pq > 0.f)) {
+                sc->done = 1;
+                sc->status = IPFEM_BREAKDOWN;
+            } else {
+                sc->alpha = sc->rz / pq;
+            }
+            *ticket = 0u;
+        }
+    }
+}
+
 // x += alpha p, r -= alpha q, z = M r; partials of r.r and r.z;
 // last CTA: convergence test, beta
 template <class T, bool BLOCK>
@@ -498,6 +584,16 @@ template <class T>
 void launch_spmv(ipfem_ctx *c, const SellDev &L, const T *K, const T *p, T *q, T *part, unsigned *ticket,
                  CGScalarsT<T> *sc)
 {
+    if constexpr (sizeof(T) == 4) {
+        if (L.sym) {
+            launch_pdl(k_cg_spmv_sym, grid_nodes(c), kRedBlock, c->stream, c->s.n_nodes,
+                       (const int64_t *)L.slice_base, (const int32_t *)L.rowlen, (const uint8_t *)L.pat_id,
+                       (const int32_t *)L.pat_off, (const uint8_t *)L.tpat_id, (const int2 *)L.tpat,
+                       (const int32_t *)L.tpat_len, (const float *)K, (const uint8_t *)c->d_fixed, (const float *)p,
+                       (float *)q, (float *)part, c->n_red, ticket, (CGScalarsT<float> *)sc);
+            return;
+        }
+    }
     const bool pat = use_row_stencils(c, L);
     auto kern = L.sorted ? (pat ? k_cg_spmv<T, true, true> : k_cg_spmv<T, true, false>)
                          : (pat ? k_cg_spmv<T, false, true> : k_cg_spmv<T, false, false>);
@@ -538,7 +634,7 @@ void launch_cg32_iteration(ipfem_ctx *c)
 {
     MixedBuffers &m = c->mx;
     const unsigned g = grid_nodes(c);
-    launch_spmv<float>(c, m.dsell, m.K, m.p, m.q, m.part, c->d_counters + 5, m.sc);
+    launch_spmv<float>(c, fp32_layout(c), fp32_values(c), m.p, m.q, m.part, c->d_counters + 5, m.sc);
     const bool blk = c->preconditioner == IPFEM_PREC_BLOCK_JACOBI;
     launch_pdl(blk ? k_cg_update<float, true> : k_cg_update<float, false>, g, kRedBlock, c->stream, c->s.n_nodes,
                (const float *)m.p, (const float *)m.q, (const float *)(blk ? m.binv : m.dinv), m.x, m.r, m.z, m.part,
@@ -550,7 +646,7 @@ void launch_cg32_iteration(ipfem_ctx *c)
 void launch_cg32_spmv_only(ipfem_ctx *c)
 {
     MixedBuffers &m = c->mx;
-    launch_spmv<float>(c, m.dsell, m.K, m.p, m.q, m.part, c->d_counters + 5, m.sc);
+    launch_spmv<float>(c, fp32_layout(c), fp32_values(c), m.p, m.q, m.part, c->d_counters + 5, m.sc);
 }
 
 void launch_cg32_pupdate_only(ipfem_ctx *c)
