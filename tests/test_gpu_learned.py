@@ -137,12 +137,15 @@ def test_learn_grad_matches_oracle():
                                                  dinv, rs.cpu().numpy()[:npair], E.cpu().numpy()[:npair], wk, wp)
         print("loss (wk %g, wp %g): %.6g vs oracle %.6g, rel %.2e" % (wk, wp, loss, loss_ref,
                                                                      abs(loss - loss_ref) / max(abs(loss_ref), 1e-30)))
-        assert loss == pytest.approx(loss_ref, rel=2e-3, abs=1e-5), (wk, wp)
+        # the oracle rounds the same operands to BF16; the remaining
+        # differences are FP32 summation orders (measured: <= 1e-5 on the
+        # loss, <= 1e-4 per parameter tensor)
+        assert loss == pytest.approx(loss_ref, rel=1e-4, abs=1e-6), (wk, wp)
         gd, rd = orc_mlp.unpack(g), orc_mlp.unpack(g_ref)
         for name, _ in orc_mlp.SIZES:
             e = np.linalg.norm(gd[name] - rd[name]) / np.linalg.norm(rd[name])
             print("  grad %-3s rel %.2e" % (name, e))
-            assert e < 2e-2, (wk, wp, name, e)
+            assert e < 1e-3, (wk, wp, name, e)
     # a small Adam step along the gradient lowers the loss
     g, loss = sm.learn_grad(rs, E, len(snaps))
     sm.mlp_adam(g, 1e-4)
