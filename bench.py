@@ -299,6 +299,8 @@ def run_gpu(args):
     A = ip.ElastoPlasticIntPointsStructMatrix(wb)         # device-resident arm
     if mixed:
         A.set_precision(ip.MIXED)
+        if args.residual32:
+            A.set_residual_precision(32)
     if not args.jacobi:
         A.set_preconditioner(ip.PREC_BLOCK_JACOBI)
     if args.no_row_stencils:
@@ -508,6 +510,8 @@ def main():
                     help="inner FP32 tolerance of the mixed methods (the chosen method's: 3e-3)")
     ap.add_argument("--no-chosen", dest="chosen", action="store_false")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--residual32", action="store_true",
+                    help="with --precision mixed: FP32 strain gather and residual scatter (FP64 refinement)")
     ap.add_argument("--no-solve", dest="solve", action="store_false",
                     help="skip the time to solution (the rest of the solve after the timed iterations)")
     ap.add_argument("--jacobi", action="store_true", help="scalar Jacobi instead of block Jacobi in the CG")
