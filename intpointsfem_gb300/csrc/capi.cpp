@@ -489,7 +489,7 @@ ipfem_status ipfem_set_load_factor(ipfem_ctx *c, double lambda)
 ipfem_status ipfem_set_precision(ipfem_ctx *c, int mode)
 {
     if (!c || (mode != IPFEM_PLAIN_FP64 && mode != IPFEM_MIXED)) return fail(c, IPFEM_INVALID, "bad precision mode");
-    if (mode == IPFEM_MIXED && !c->mx.K) {
+    if (mode == IPFEM_MIXED && !c->mx.dphi) {
         const Setup &s = c->s;
         MixedBuffers &m = c->mx;
         ipfem_status st = IPFEM_OK;
@@ -503,13 +503,14 @@ ipfem_status ipfem_set_precision(ipfem_ctx *c, int mode)
         if (!e.empty()) return fail(c, IPFEM_INVALID, e);
         build_row_stencils(m.sell);
         ck(upload_sell(m.sell, false, m.dsell, c->stream));
-        ck(dalloc(&m.K, (size_t)m.sell.n_sell * 4));
-        // the upper-only layout where the grid has row and transposed stencils
+        // the upper-only layout where the grid has row and transposed stencils;
+        // the values of the full layout are allocated when that layout is used
         m.have_sym = build_sell_sym(s, m.sym).empty();
         if (m.have_sym) {
             ck(upload_sell(m.sym, false, m.dsym, c->stream));
             ck(dalloc(&m.Ks, (size_t)m.sym.n_sell * 4));
         }
+        if (!use_sym32(c)) ck(dalloc(&m.K, (size_t)m.sell.n_sell * 4));
         ck(dalloc(&m.dinv, (size_t)s.neq));
         ck(dalloc(&m.binv, (size_t)s.n_nodes * 4));
         ck(dalloc(&m.x, (size_t)s.neq));
@@ -619,6 +620,12 @@ ipfem_status ipfem_set_row_stencils(ipfem_ctx *c, int on)
     // with the upper-only FP32 layout the switch also selects the layout the
     // FP32 tangent lives in: it has to be assembled again
     if (on != c->row_stencils && c->mx.have_sym) c->tangent_valid = false;
+    if (!on && c->mx.have_sym && !c->mx.K) {
+        const cudaError_t e = dalloc(&c->mx.K, (size_t)c->mx.sell.n_sell * 4);
+        if (e != cudaSuccess)
+            return fail(c, e == cudaErrorMemoryAllocation ? IPFEM_OOM : IPFEM_CUDA,
+                        "allocation of the full-layout FP32 tangent failed");
+    }
     c->row_stencils = on;
     return IPFEM_OK;
 }
