@@ -61,9 +61,15 @@ def test_struct_matrix_class_equals_oracle(tmp_path):
     assert np.array_equal(_read(d, "a.bin"), a)
     # the clone evaluates the same residual
     assert np.array_equal(_read(d, "clone_res.bin"), _read(d, "res.bin"))
-    # state commit through SetUpdateMem, then the next residual
+    # state commit through SetUpdateMem, then the next residual. This random u
+    # drives some points to the apex; evaluated again at the same strain, such a
+    # point has zero elastic strain, and the reference's spectral decomposition
+    # (FunctionsStressStrain.h, ComputeSigma) returns NaN there. The library and
+    # the oracle give NaN at the same entries and equal bits elsewhere.
     P.assemble_residual(u.copy(), lam, update_mem=True)
-    assert np.array_equal(_read(d, "res_after_commit.bin"), P.assemble_residual(u.copy(), lam))
+    after, want = _read(d, "res_after_commit.bin"), P.assemble_residual(u.copy(), lam)
+    assert np.array_equal(np.isnan(after), np.isnan(want))
+    assert np.array_equal(after, want, equal_nan=True)
 
 
 def test_sym_csr_export_matches_blocks():
