@@ -423,10 +423,12 @@ def run_gpu(args):
     # roofline of the dominant kernel (CG block SpMV), CUDA events on the library stream
     ms_spmv = A.profile_spmv(reps=20)
     nb, nn = A.n_blocks, A.n_nodes
+    nb_stored, _, upper_only = A.layout_info(fp32=mixed)      # the FP32 tangent may hold the upper blocks only
     vb = 16 if mixed else 32                                   # bytes of one 2x2 block
     stencils = A.row_stencil_count()[1 if mixed else 0] > 0 and not args.no_row_stencils
-    idx_bytes = nn if stencils else 4 * nb                     # 8-bit stencil id per row, or a column per block
-    spmv_bytes = nb * vb + idx_bytes + nn * (vb + 4 + 2)       # blocks, indices; p read, q write, rowlen, fixed
+    # 8-bit stencil id per row (and a transposed-stencil id with the upper-only layout), or a column per block
+    idx_bytes = nn * (2 if upper_only else 1) if stencils else 4 * nb_stored
+    spmv_bytes = nb_stored * vb + idx_bytes + nn * (vb + 4 + 2)  # blocks, indices; p read, q write, rowlen, fixed
     hbm_peak, peak_kind = measured_peaks()
     achieved = spmv_bytes / (ms_spmv * 1e-3) / 1e9
     spmv_fp64_tflops = 2.0 * (4 * nb + 2 * nn) / (ms_spmv * 1e-3) / 1e12
@@ -464,15 +466,19 @@ def run_gpu(args):
                         "and D2H inside every timed step"}
                 if ms_e2e is not None else None),
         "precision": args.precision,
-        "roofline": {"kernel": "k_cg_spmv", "bound": "hbm", "achieved": achieved, "peak": hbm_peak,
+        "roofline": {"kernel": "k_cg_spmv_sym" if upper_only else "k_cg_spmv", "bound": "hbm",
+                     "achieved": achieved, "peak": hbm_peak,
                      "unit": "GB/s", "frac": achieved / hbm_peak, "peak_kind": peak_kind,
                      "traffic": SPMV_DRAM_BYTES[bool(stencils)] if (n == 400 and not mixed) else None,
                      "algorithmic_bytes": spmv_bytes,
                      "ms_per_launch": ms_spmv,
-                     "fp64": {"achieved_tflops": spmv_fp64_tflops, "peak_tflops": fp64_tflops,
-                              "frac": spmv_fp64_tflops / fp64_tflops, "peak_kind": "measured live (fma probe)"}},
+                     "layout": {"stored_blocks": nb_stored, "upper_only": upper_only}},
         "gpu_launches": launches,
     }
+    if not mixed:                                              # the FP64 SpMV also meets the FP64 pipe's roofline
+        line["roofline"]["fp64"] = {"achieved_tflops": spmv_fp64_tflops, "peak_tflops": fp64_tflops,
+                                    "frac": spmv_fp64_tflops / fp64_tflops,
+                                    "peak_kind": "measured live (fma probe)"}
     if solve_plain:
         line["solve"] = solve_plain
     if chosen:

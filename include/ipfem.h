@@ -218,6 +218,14 @@ ipfem_status ipfem_set_row_stencils(ipfem_ctx *ctx, int on);
 /* stencils of the FP64 and FP32 (IPFEM_MIXED, else 0) layouts; 0 = explicit
  * columns only (rows longer than 32 blocks or more than 255 patterns) */
 ipfem_status ipfem_row_stencil_count(ipfem_ctx *ctx, int32_t *n_fp64, int32_t *n_fp32);
+/* The tangent layout the SpMVs read now: fp32 = 0 the FP64 tangent, 1 the
+ * FP32 one (IPFEM_MIXED only, else IPFEM_INVALID).  stored_blocks = 2x2
+ * blocks held, slots = padded SELL slots, upper_only = 1 when the FP32
+ * tangent holds only the blocks (i, j >= i) and reads the lower ones as
+ * transposes (structured grids with row stencils on).  Any output may be
+ * null.  No counterpart in the reference. */
+ipfem_status ipfem_layout_info(ipfem_ctx *ctx, int fp32, int64_t *stored_blocks, int64_t *slots,
+                               int32_t *upper_only);
 
 /* Resumable form of the same loop: begin sets the options and the step range;
  * each advance performs n_iters Newton iterations (0 = until the last step is

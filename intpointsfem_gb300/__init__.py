@@ -153,6 +153,7 @@ def lib():
             "ipfem_set_newton_tangent": (S, [P, S]),
             "ipfem_set_row_stencils": (S, [P, S]),
             "ipfem_row_stencil_count": (S, [P, _ip, _ip]),
+            "ipfem_layout_info": (S, [P, S, _lp, _lp, _ip]),
             "ipfem_gmsh_read": (S, [C.c_char_p, C.POINTER(C.POINTER(GmshData))]),
             "ipfem_gmsh_free": (None, [C.POINTER(GmshData)]),
             "ipfem_gmsh_problem": (S, [C.POINTER(GmshData), C.c_int32, C.c_int32, C.POINTER(BC), C.c_int32,
@@ -415,6 +416,13 @@ class ElastoPlasticIntPointsStructMatrix:
         a, b = C.c_int32(0), C.c_int32(0)
         self._check(lib().ipfem_row_stencil_count(self._ctx, C.byref(a), C.byref(b)))
         return a.value, b.value
+
+    def layout_info(self, fp32=False):
+        """(stored 2x2 blocks, padded SELL slots, upper_only) of the tangent
+        layout the SpMVs read now: the FP64 one, or with fp32 the FP32 one"""
+        nb, ns, up = C.c_int64(0), C.c_int64(0), C.c_int32(0)
+        self._check(lib().ipfem_layout_info(self._ctx, int(bool(fp32)), C.byref(nb), C.byref(ns), C.byref(up)))
+        return nb.value, ns.value, bool(up.value)
 
     def set_precision(self, mode):
         self._check(lib().ipfem_set_precision(self._ctx, int(mode)))

@@ -638,6 +638,21 @@ ipfem_status ipfem_row_stencil_count(ipfem_ctx *c, int32_t *n_fp64, int32_t *n_f
     return IPFEM_OK;
 }
 
+ipfem_status ipfem_layout_info(ipfem_ctx *c, int fp32, int64_t *stored_blocks, int64_t *slots,
+                               int32_t *upper_only)
+{
+    if (!c) return IPFEM_INVALID;
+    if (fp32 && c->precision != IPFEM_MIXED)
+        return fail(c, IPFEM_INVALID, "no FP32 tangent: the precision is not IPFEM_MIXED");
+    const int64_t nb = c->s.n_blocks, nn = c->s.n_nodes;
+    const bool sym = fp32 && use_sym32(c);
+    // the block pattern is symmetric: n_blocks = n_nodes + 2 * (off-diagonal upper blocks)
+    if (stored_blocks) *stored_blocks = sym ? (nb + nn) / 2 : nb;
+    if (slots) *slots = !fp32 ? c->s.sell.n_sell : (sym ? c->mx.sym.n_sell : c->mx.sell.n_sell);
+    if (upper_only) *upper_only = sym ? 1 : 0;
+    return IPFEM_OK;
+}
+
 ipfem_status ipfem_assemble(ipfem_ctx *c, const double *u, double *rhs, int where)
 {
     return assemble_common(c, u, rhs, where, true);

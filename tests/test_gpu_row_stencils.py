@@ -32,6 +32,23 @@ def test_stencil_counts():
     print("row stencils at 12 x 12: FP64 layout %d, FP32 layout %d" % (n64, n32))
 
 
+def test_layout_info():
+    """the FP64 layout holds every block; the FP32 one holds the diagonal and
+    the upper blocks while the stencils are on, and every block without them"""
+    sm = _matrix(12)
+    nb, nn = sm.n_blocks, sm.n_nodes
+    stored, slots, upper = sm.layout_info()
+    assert (stored, upper) == (nb, False) and slots >= nb
+    with pytest.raises(ip.IpfemError):
+        sm.layout_info(fp32=True)
+    sm.set_precision(ip.MIXED)
+    stored, slots, upper = sm.layout_info(fp32=True)
+    assert upper and stored == (nb + nn) // 2 and stored <= slots < nb
+    sm.set_row_stencils(0)
+    stored, slots, upper = sm.layout_info(fp32=True)
+    assert (stored, upper) == (nb, False) and slots >= nb
+
+
 def test_order3_rows_keep_explicit_columns(tmp_path):
     """order-3 vertex rows have 49 blocks: longer than a stencil, so the
     layout keeps its column indices and the solve is unchanged"""
