@@ -68,6 +68,27 @@ def measured_peaks():
         return FALLBACK_HBM_GBS, "fallback"
 
 
+def residual_kernel_roofline(M, ms, fp, hbm_peak):
+    """algorithmic bytes of the residual kernels of struct matrix M (fp = 8:
+    the FP64 kernels, 4: the FP32 gather and scatter) over their CUDA-event
+    durations ms, against the measured HBM copy bandwidth.  Gather: element
+    blocks, dof map, u once, strains; stress: blocks, weighted stresses,
+    element forces; reduce: incidence, element forces, load vector, fixed, rhs.
+    The return mapping is bound by the FP64 pipe and reported as a time."""
+    nn = (M.order + 1) ** 2
+    nb, nd = nn * 2 * nn, 2 * nn
+    e, q, neq = M.n_el, M.n_ip, M.neq
+    by = {"gather_strain": e * nb * fp + e * nd * 4 + neq * 8 + 3 * q * fp,
+          "stress_residual": e * nb * fp + 3 * q * fp + e * nd * fp,
+          "color_reduce": M.n_colors * M.n_nodes * 4 + e * nd * fp + neq * (8 + 1 + 8)}
+    out = {}
+    for k, b in by.items():
+        gbs = b / (ms[k] * 1e-3) / 1e9
+        out[k] = {"ms": ms[k], "algorithmic_bytes": b, "achieved_gbs": gbs, "frac": gbs / hbm_peak}
+    out["compute_sigma"] = {"ms": ms["compute_sigma"], "bound": "fp64 pipe"}
+    return out
+
+
 class ClockSampler:
     """nvidia-smi clocks and throttle reasons sampled every 200 ms"""
 
@@ -406,6 +427,10 @@ def run_gpu(args):
                 out["solve"] = solve_record([pw, (stc, msc), pr], N_STEPS)
             if not learned_prec:
                 out["ms_spmv_fp32"] = C_.profile_spmv(reps=20)
+                # the FP32 strain gather and residual scatter (the FP32 residual option)
+                C_.set_residual_precision(32)
+                out["residual_kernels_fp32"] = residual_kernel_roofline(
+                    C_, C_.profile_residual(uc, 32), 4, measured_peaks()[0])
             C_.close()
             return out
 
@@ -422,6 +447,9 @@ def run_gpu(args):
 
     # roofline of the dominant kernel (CG block SpMV), CUDA events on the library stream
     ms_spmv = A.profile_spmv(reps=20)
+    # the residual kernels at the last Newton iterate, CUDA events between them
+    res_bits = 32 if (mixed and args.residual32) else 64
+    res_kernels = residual_kernel_roofline(A, A.profile_residual(du, res_bits), res_bits // 8, measured_peaks()[0])
     nb, nn = A.n_blocks, A.n_nodes
     nb_stored, _, upper_only = A.layout_info(fp32=mixed)      # the FP32 tangent may hold the upper blocks only
     vb = 16 if mixed else 32                                   # bytes of one 2x2 block
@@ -457,6 +485,7 @@ def run_gpu(args):
         "row_stencils": bool(stencils),
         "ip_per_s": A.n_ip / (ms_res * 1e-3),
         "ms_residual": ms_res,
+        "residual_kernels": res_kernels,
         "cg_iters_per_newton": cg_per_iter,
         "newton_iters_timed": st.newton_iters,
         "ms_breakdown": {"assemble": st.ms_assemble / args.steps, "cg": st.ms_solve / args.steps,

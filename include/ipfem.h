@@ -257,6 +257,14 @@ ipfem_status ipfem_compute_sigma(ipfem_ctx *ctx, int update_mem, const double *d
 /* TPZNumericalIntegrator::MultiplyTranspose (TPZNumericalIntegrator.cpp:54-78):
  * -B^T sigma_w, scattered and reduced over colours (no load, no masking). */
 ipfem_status ipfem_scatter_residual(ipfem_ctx *ctx, const double *d_sigma_w, double *d_res);
+/* The FP32 kernels of the same two steps (IPFEM_MIXED after
+ * ipfem_set_residual_precision(ctx, 32, ...)): d_strain float SoA [3][n_ip],
+ * each displacement taken relative to its element's first connect (same
+ * component) in FP64 and rounded to FP32, FP32 fma; d_sigma_w float SoA
+ * [3][n_ip], FP32 element forces summed over colours in FP32, widened into
+ * the FP64 d_res (no load, no masking). */
+ipfem_status ipfem_gather_strain32(ipfem_ctx *ctx, const double *d_u, float *d_strain);
+ipfem_status ipfem_scatter_residual32(ipfem_ctx *ctx, const float *d_sigma_w, double *d_res);
 
 /* The same canonical dot product for callers that cannot allocate device
  * memory (an application that serves all device memory from its own
@@ -366,6 +374,16 @@ uint64_t ipfem_launch_count(const ipfem_ctx *ctx);
 /* average duration of the CG block SpMV on the current tangent, timed with
  * CUDA events on the context's stream over `reps` back-to-back launches */
 ipfem_status ipfem_profile_spmv(ipfem_ctx *ctx, int reps, double *ms_per_launch);
+/* average durations (ms) of the four kernels of one residual evaluation at
+ * the device displacement d_u, in the order they run: ms[0] strain
+ * gather, ms[1] return mapping (no tangent, no commit), ms[2] stress to
+ * element forces, ms[3] colour reduction + load.  bits = 64: the FP64
+ * kernels; 32: the FP32 gather and scatter (IPFEM_MIXED after
+ * ipfem_set_residual_precision(ctx, 32, ...)).  The chain runs `reps` times;
+ * CUDA events between the kernels on the context's stream time each one with
+ * the cache state the others leave.  The integration-point state is not
+ * changed. */
+ipfem_status ipfem_profile_residual(ipfem_ctx *ctx, const double *d_u, int bits, int reps, double *ms);
 /* FP64 fma issue rate of this device (TFLOP/s, 2 flops per fma), measured with
  * a dependent-chain probe kernel timed by CUDA events */
 ipfem_status ipfem_measure_fp64_peak(ipfem_ctx *ctx, double *tflops);

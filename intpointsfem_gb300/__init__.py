@@ -127,6 +127,7 @@ def lib():
             "ipfem_launch_count": (C.c_uint64, [P]),
             "ipfem_set_iteration_log": (S, [P, C.c_char_p]),
             "ipfem_profile_spmv": (S, [P, S, _dp]),
+            "ipfem_profile_residual": (S, [P, P, S, S, _dp]),
             "ipfem_measure_fp64_peak": (S, [P, _dp]),
             "ipfem_set_node_grid": (S, [P, C.c_int32, C.c_int32]),
             "ipfem_mlp_init": (S, [P, C.c_uint64]),
@@ -142,6 +143,8 @@ def lib():
             "ipfem_gather_strain": (S, [P, P, P]),
             "ipfem_compute_sigma": (S, [P, S, P, P, P]),
             "ipfem_scatter_residual": (S, [P, P, P]),
+            "ipfem_gather_strain32": (S, [P, P, P]),
+            "ipfem_scatter_residual32": (S, [P, P, P]),
             "ipfem_get_state": (S, [P, S, _dp]),
             "ipfem_set_state": (S, [P, S, _dp]),
             "ipfem_get_setup": (S, [P, S, P]),
@@ -355,6 +358,7 @@ class ElastoPlasticIntPointsStructMatrix:
         sz = np.zeros(6, np.int64)
         lib().ipfem_sizes(self._ctx, _np_ptr(sz, _lp))
         self.n_el, self.n_ip, self.n_nodes, self.neq, self.n_colors, self.n_blocks = map(int, sz)
+        self.order = int(mesh.order) or 2
         self.u = np.zeros(self.neq)   # the solution the reference reads from fMesh->Solution()
 
     def _check(self, st):
@@ -518,6 +522,14 @@ class ElastoPlasticIntPointsStructMatrix:
         self._check(lib().ipfem_profile_spmv(self._ctx, int(reps), _np_ptr(out, _dp)))
         return float(out[0])
 
+    def profile_residual(self, d_u, bits=64, reps=10):
+        """CUDA-event durations (ms) of the residual kernels at the device
+        displacement d_u: gather, return mapping, stress to element forces,
+        colour reduction; bits 32 times the FP32 gather and scatter"""
+        out = np.zeros(4)
+        self._check(lib().ipfem_profile_residual(self._ctx, _ptr(d_u), int(bits), int(reps), _np_ptr(out, _dp)))
+        return dict(zip(("gather_strain", "compute_sigma", "stress_residual", "color_reduce"), map(float, out)))
+
     # -- learned preconditioner --------------------------------------------
     def set_node_grid(self, gr, gt):
         self._check(lib().ipfem_set_node_grid(self._ctx, int(gr), int(gt)))
@@ -593,6 +605,14 @@ class ElastoPlasticIntPointsStructMatrix:
 
     def scatter_residual(self, d_sigma_w, d_res):
         self._check(lib().ipfem_scatter_residual(self._ctx, _ptr(d_sigma_w), _ptr(d_res)))
+
+    def gather_strain32(self, d_u, d_strain32):
+        """FP32 strain gather (MIXED with FP32 residuals): float32 [3][n_ip]"""
+        self._check(lib().ipfem_gather_strain32(self._ctx, _ptr(d_u), _ptr(d_strain32)))
+
+    def scatter_residual32(self, d_sigma_w32, d_res):
+        """FP32 element forces and colour sums from float32 [3][n_ip] into FP64 d_res"""
+        self._check(lib().ipfem_scatter_residual32(self._ctx, _ptr(d_sigma_w32), _ptr(d_res)))
 
     def get_state(self, field):
         n = {0: 4 * self.n_ip, 1: 4 * self.n_ip, 2: self.n_ip, 3: self.n_ip}[field]

@@ -97,7 +97,7 @@ void free_all(ipfem_ctx *c)
     free_sell(c->dsell);
     free_sell(c->mx.dsell);
     free_sell(c->mx.dsym);
-    void *ptrs[] = {c->d_dphi, c->d_weight, c->d_mat, c->d_f0, c->d_df, c->d_dofs, c->d_color_els, c->d_inc,
+    void *ptrs[] = {c->d_dphi, c->d_weight, c->d_mat, c->d_f0, c->d_df, c->d_lin, c->d_dofs, c->d_color_els, c->d_inc,
                     c->d_fixed, c->d_K,
                     c->d_dinv, c->d_eps_p, c->d_sigma, c->d_alpha, c->d_mtype, c->d_u, c->d_rhs, c->d_strain,
                     c->d_sigma_w, c->d_dep, c->d_fe, c->d_x, c->d_r, c->d_z, c->d_p, c->d_q, c->d_b, c->d_part,
@@ -107,7 +107,7 @@ void free_all(ipfem_ctx *c)
     {
         MixedBuffers &m = c->mx;
         void *mp[] = {m.dphi, m.K, m.Ks, m.dinv, m.binv, m.x, m.r, m.z, m.p, m.q, m.part, m.sc, m.strain32, m.sigw32,
-                      m.fe32};
+                      m.fe32, m.dphiT};
         for (void *p : mp)
             if (p) cudaFree(p);
         if (m.h_sc) cudaFreeHost(m.h_sc);
@@ -157,6 +157,14 @@ ipfem_status sync_check(ipfem_ctx *c)
     return check_device(c);
 }
 
+// the load factor and the load vector f0 + lambda df of the residuals that follow
+void set_load(ipfem_ctx *c, double lambda)
+{
+    c->load_factor = lambda;
+    launch_load_vector(c);
+    c->launches += 1;
+}
+
 // residual of the current load factor at d_u into d_out (device)
 void residual_device(ipfem_ctx *c, const double *d_u, double *d_out, int update_mem)
 {
@@ -166,13 +174,13 @@ void residual_device(ipfem_ctx *c, const double *d_u, double *d_out, int update_
         launch_gather_strain32(c, d_u, m.strain32);
         launch_compute_sigma32(c, 0, m.strain32, m.sigw32, nullptr);
         launch_stress_residual32(c, m.sigw32, m.fe32);
-        launch_color_reduce32(c, m.fe32, c->load_factor, 1, d_out);
+        launch_color_reduce32(c, m.fe32, 1, d_out);
         return;
     }
     launch_gather_strain(c, d_u, c->d_strain);
     launch_compute_sigma(c, update_mem, c->d_strain, c->d_sigma_w, nullptr);
     launch_stress_residual(c, c->d_sigma_w, c->d_fe);
-    launch_color_reduce(c, c->d_fe, c->load_factor, 1, d_out);
+    launch_color_reduce(c, c->d_fe, 1, d_out);
 }
 
 void tangent_device(ipfem_ctx *c, const double *d_u, double *d_out, int update_mem)
@@ -183,12 +191,12 @@ void tangent_device(ipfem_ctx *c, const double *d_u, double *d_out, int update_m
         launch_gather_strain32(c, d_u, m.strain32);
         launch_compute_sigma32(c, 0, m.strain32, m.sigw32, c->d_dep);
         launch_stress_residual32(c, m.sigw32, m.fe32);
-        launch_color_reduce32(c, m.fe32, c->load_factor, 1, d_out);
+        launch_color_reduce32(c, m.fe32, 1, d_out);
     } else {
         launch_gather_strain(c, d_u, c->d_strain);
         launch_compute_sigma(c, update_mem, c->d_strain, c->d_sigma_w, c->d_dep);
         launch_stress_residual(c, c->d_sigma_w, c->d_fe);
-        launch_color_reduce(c, c->d_fe, c->load_factor, 1, d_out);
+        launch_color_reduce(c, c->d_fe, 1, d_out);
     }
     if (c->precision == 1) launch_stiffness32(c);
     else launch_stiffness(c);
@@ -397,6 +405,7 @@ ipfem_status ipfem_create(const ipfem_mesh *mesh, const ipfem_material *mat, ipf
     ck(upload(&c->d_mat, s.mat, t));
     ck(upload(&c->d_f0, s.f0, t));
     ck(upload(&c->d_df, s.df, t));
+    ck(dalloc(&c->d_lin, (size_t)s.neq));
     ck(upload(&c->d_dofs, s.dofs, t));
     ck(upload(&c->d_color_els, s.color_els, t));
     ck(upload(&c->d_inc, s.inc, t));
@@ -438,6 +447,8 @@ ipfem_status ipfem_create(const ipfem_mesh *mesh, const ipfem_material *mat, ipf
     ck(cudaMemsetAsync(c->d_u, 0, (size_t)s.neq * sizeof(double), t));
     ck(cudaMemsetAsync(c->d_K, 0, (size_t)s.sell.n_sell * 4 * sizeof(double), t));
     ck(cudaMemsetAsync(c->d_dinv, 0, (size_t)s.neq * sizeof(double), t));
+    launch_load_vector(c);   // load factor 0
+    ck(cudaGetLastError());
     // initial state: in-situ seed
     {
         std::vector<double> h((size_t)s.n_ip * 4);
@@ -482,7 +493,8 @@ ipfem_status ipfem_set_load_factor(ipfem_ctx *c, double lambda)
 {
     if (!c) return IPFEM_INVALID;
     if (!std::isfinite(lambda)) return fail(c, IPFEM_INVALID, "load factor is not finite");
-    c->load_factor = lambda;
+    set_load(c, lambda);
+    CK(cudaGetLastError());
     return IPFEM_OK;
 }
 
@@ -570,12 +582,17 @@ ipfem_status ipfem_set_residual_precision(ipfem_ctx *c, int bits, double switch_
     if (bits == 32 && !c->mx.strain32) {
         MixedBuffers &m = c->mx;
         const Setup &s = c->s;
+        const size_t n_tiles = ((size_t)s.n_el + kTile32 - 1) / kTile32;
         cudaError_t e = dalloc(&m.strain32, (size_t)3 * s.n_ip);
         if (e == cudaSuccess) e = dalloc(&m.sigw32, (size_t)3 * s.n_ip);
         if (e == cudaSuccess) e = dalloc(&m.fe32, (size_t)s.n_el * s.nd);
+        if (e == cudaSuccess) e = dalloc(&m.dphiT, n_tiles * kTile32 * 2 * (size_t)s.nn * (size_t)(s.nq | 1));
         if (e != cudaSuccess)
             return fail(c, e == cudaErrorMemoryAllocation ? IPFEM_OOM : IPFEM_CUDA,
                         "allocation of the FP32 residual buffers failed");
+        launch_tile_blocks32(c);
+        c->launches += 1;
+        CK(cudaGetLastError());
     }
     c->res32 = bits == 32;
     c->res32_switch = switch_rtol;
@@ -795,7 +812,7 @@ static ipfem_status newton_advance(ipfem_ctx *c, int32_t n_iters, double *du, ip
         const double ma0 = st->ms_assemble, ms0 = st->ms_solve, mc0 = st->ms_commit;
         if (!ns.open) {
             Range rg("ipfem:newton:first_assembly");
-            c->load_factor = (double)(ns.step + 1) / (double)o.n_steps;
+            set_load(c, (double)(ns.step + 1) / (double)o.n_steps);
             c->res32_active = c->res32 && c->precision == IPFEM_MIXED;
             cudaEventRecord(ev[0], c->stream);
             newton_assemble(c, du);
@@ -1075,6 +1092,52 @@ ipfem_status ipfem_profile_spmv(ipfem_ctx *c, int reps, double *ms_per_launch)
     return sync_check(c);
 }
 
+ipfem_status ipfem_profile_residual(ipfem_ctx *c, const double *d_u, int bits, int reps, double *ms)
+{
+    if (!c || !d_u || reps < 1 || !ms || (bits != 32 && bits != 64)) return fail(c, IPFEM_INVALID, "bad args");
+    if (bits == 32 && (c->precision != IPFEM_MIXED || !c->mx.strain32))
+        return fail(c, IPFEM_INVALID, "the FP32 residual kernels need IPFEM_MIXED and "
+                                      "ipfem_set_residual_precision(ctx, 32, ...)");
+    cudaEvent_t ev[5] = {};
+    for (int k = 0; k < 5; k++) {
+        const cudaError_t e = cudaEventCreate(&ev[k]);
+        if (e != cudaSuccess) {
+            for (int j = 0; j < k; j++) cudaEventDestroy(ev[j]);
+            return fail(c, IPFEM_CUDA, cudaGetErrorString(e));
+        }
+    }
+    MixedBuffers &m = c->mx;
+    double acc[4] = {0, 0, 0, 0};
+    cudaError_t e = cudaSuccess;
+    for (int r = 0; r < reps && e == cudaSuccess; r++) {
+        cudaEventRecord(ev[0], c->stream);
+        if (bits == 32) launch_gather_strain32(c, d_u, m.strain32);
+        else launch_gather_strain(c, d_u, c->d_strain);
+        cudaEventRecord(ev[1], c->stream);
+        if (bits == 32) launch_compute_sigma32(c, 0, m.strain32, m.sigw32, nullptr);
+        else launch_compute_sigma(c, 0, c->d_strain, c->d_sigma_w, nullptr);
+        cudaEventRecord(ev[2], c->stream);
+        if (bits == 32) launch_stress_residual32(c, m.sigw32, m.fe32);
+        else launch_stress_residual(c, c->d_sigma_w, c->d_fe);
+        cudaEventRecord(ev[3], c->stream);
+        // into d_b, a scratch vector: d_rhs holds the Newton loop's residual
+        if (bits == 32) launch_color_reduce32(c, m.fe32, 1, c->d_b);
+        else launch_color_reduce(c, c->d_fe, 1, c->d_b);
+        cudaEventRecord(ev[4], c->stream);
+        c->launches += 4;
+        e = cudaEventSynchronize(ev[4]);
+        for (int k = 0; k < 4 && e == cudaSuccess; k++) {
+            float t = 0.0f;
+            e = cudaEventElapsedTime(&t, ev[k], ev[k + 1]);
+            acc[k] += t;
+        }
+    }
+    for (int k = 0; k < 5; k++) cudaEventDestroy(ev[k]);
+    if (e != cudaSuccess) return fail(c, IPFEM_CUDA, cudaGetErrorString(e));
+    for (int k = 0; k < 4; k++) ms[k] = acc[k] / reps;
+    return sync_check(c);
+}
+
 ipfem_status ipfem_gather_strain(ipfem_ctx *c, const double *d_u, double *d_strain)
 {
     if (!c || !d_u || !d_strain) return fail(c, IPFEM_INVALID, "bad args");
@@ -1094,7 +1157,24 @@ ipfem_status ipfem_scatter_residual(ipfem_ctx *c, const double *d_sigma_w, doubl
 {
     if (!c || !d_sigma_w || !d_res) return fail(c, IPFEM_INVALID, "bad args");
     launch_stress_residual(c, d_sigma_w, c->d_fe);
-    launch_color_reduce(c, c->d_fe, 0.0, 0, d_res);
+    launch_color_reduce(c, c->d_fe, 0, d_res);
+    return sync_check(c);
+}
+
+ipfem_status ipfem_gather_strain32(ipfem_ctx *c, const double *d_u, float *d_strain)
+{
+    if (!c || !d_u || !d_strain) return fail(c, IPFEM_INVALID, "bad args");
+    if (!c->mx.dphiT) return fail(c, IPFEM_INVALID, "the FP32 residual kernels need ipfem_set_residual_precision(ctx, 32, ...)");
+    launch_gather_strain32(c, d_u, d_strain);
+    return sync_check(c);
+}
+
+ipfem_status ipfem_scatter_residual32(ipfem_ctx *c, const float *d_sigma_w, double *d_res)
+{
+    if (!c || !d_sigma_w || !d_res) return fail(c, IPFEM_INVALID, "bad args");
+    if (!c->mx.dphiT) return fail(c, IPFEM_INVALID, "the FP32 residual kernels need ipfem_set_residual_precision(ctx, 32, ...)");
+    launch_stress_residual32(c, d_sigma_w, c->mx.fe32);
+    launch_color_reduce32(c, c->mx.fe32, 0, d_res);
     return sync_check(c);
 }
 

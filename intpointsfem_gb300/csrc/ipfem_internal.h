@@ -102,6 +102,10 @@ struct MixedBuffers {
     float *part = nullptr;        // 2 partial arrays
     float *strain32 = nullptr, *sigw32 = nullptr;   // [3][n_ip] FP32 residual (ipfem_set_residual_precision)
     float *fe32 = nullptr;                          // [n_el][nd]
+    // element blocks of the FP32 residual kernels in tiles of kTile32
+    // elements: [tile][d][n][element of the tile][q], the point index padded
+    // to the odd stride nq | 1, the last tile and the padding zero
+    float *dphiT = nullptr;
     CGScalarsT<float> *sc = nullptr;
     CGScalarsT<float> *h_sc = nullptr;   // pinned
     cudaGraphExec_t exec = nullptr;
@@ -241,6 +245,7 @@ struct ipfem_ctx {
     int update_mem = 0;
     // device: setup
     double *d_dphi = nullptr, *d_weight = nullptr, *d_mat = nullptr, *d_f0 = nullptr, *d_df = nullptr;
+    double *d_lin = nullptr;             // [neq] f0 + load_factor * df (the reference's fRhsLinear)
     int32_t *d_dofs = nullptr, *d_color_els = nullptr, *d_inc = nullptr;
     uint8_t *d_fixed = nullptr;
     ipfem::SellDev dsell;                // FP64 tangent layout
@@ -311,13 +316,19 @@ cudaError_t upload_constants(const ElasticConstH &el);
 void launch_gather_strain(ipfem_ctx *c, const double *d_u, double *d_strain);
 void launch_compute_sigma(ipfem_ctx *c, int update_mem, const double *d_strain, double *d_sigma_w, double *d_dep);
 void launch_stress_residual(ipfem_ctx *c, const double *d_sigma_w, double *d_fe);
-void launch_color_reduce(ipfem_ctx *c, const double *d_fe, double lambda, int with_load, double *d_res);
+// d_lin = f0 + c->load_factor * df, after every change of the load factor
+void launch_load_vector(ipfem_ctx *c);
+void launch_color_reduce(ipfem_ctx *c, const double *d_fe, int with_load, double *d_res);
 // the FP32 residual of IPFEM_MIXED_RES32: FP32 gather, FP64 point update on
 // FP32 strains, FP32 scatter and colour sums (the load added in FP64)
+// elements per tile of the FP32 residual's interleaved blocks (one per lane)
+constexpr int kTile32 = 32;
+// fills c->mx.dphiT (allocated: n_tiles * kTile32 * 2*nn * (nq | 1) floats) from the FP64 blocks
+void launch_tile_blocks32(ipfem_ctx *c);
 void launch_gather_strain32(ipfem_ctx *c, const double *d_u, float *d_strain);
 void launch_compute_sigma32(ipfem_ctx *c, int update_mem, const float *d_strain, float *d_sigma_w, double *d_dep);
 void launch_stress_residual32(ipfem_ctx *c, const float *d_sigma_w, float *d_fe);
-void launch_color_reduce32(ipfem_ctx *c, const float *d_fe, double lambda, int with_load, double *d_res);
+void launch_color_reduce32(ipfem_ctx *c, const float *d_fe, int with_load, double *d_res);
 void launch_stiffness(ipfem_ctx *c);
 void launch_cg_init(ipfem_ctx *c, const double *d_b, double rtol, int max_it);
 void launch_cg_iteration(ipfem_ctx *c);

@@ -8,8 +8,12 @@
 //  k_color_reduce    second half: the colour-slab scatter and pairwise slab
 //                    reduction of the reference, evaluated per node as a
 //                    gather over the (at most one per colour) incident elements,
-//                    in the reference's pairing order; + f0 + lambda*df and
+//                    in the reference's pairing order; + the load vector
+//                    f0 + lambda*df (k_load_vector, once per load factor) and
 //                    Dirichlet masking (TPZElastoPlasticIntPointsStructMatrix.cpp:137-154).
+//  k_gather_strain32, k_stress_residual32
+//                    the same two element kernels in FP32 for the mixed
+//                    precision's FP32 residuals, on tiles of 32 elements.
 //  k_stiffness       TPZNumericalIntegrator::KAssembly (…cpp:131-214) and
 //                    MatrixAssembleKernel (KernelsMatrixAssemble.h:24-57): one warp
 //                    per element, K_e = sum_q B_q^T (w Dep_q) B_q (upper triangle),
@@ -22,6 +26,8 @@
 // Every kernel is instantiated for the element orders P = 1, 2, 3 (the
 // reference builds one order per binary, KernelsMatrixAssemble.h:3-12):
 // nn = nq = (P+1)^2 connects and Gauss points, nd = 2 nn dofs per element.
+#include <algorithm>
+
 #include "ipfem_internal.h"
 #include "tma.cuh"
 
@@ -36,15 +42,8 @@ struct Elem {
 };
 static_assert(Elem<1>::NB * 8 % 16 == 0 && Elem<2>::NB * 8 % 16 == 0 && Elem<3>::NB * 8 % 16 == 0,
               "bulk copies of whole FP64 element blocks need 16-byte multiples");
-// FP32 tiles start at 16-byte boundaries (full tiles are 16-byte multiples)
-static_assert(Elem<1>::kGatherTile * Elem<1>::NB * 4 % 16 == 0 && Elem<2>::kGatherTile * Elem<2>::NB * 4 % 16 == 0 &&
-                  Elem<3>::kGatherTile * Elem<3>::NB * 4 % 16 == 0 && Elem<1>::kResTile * Elem<1>::NB * 4 % 16 == 0 &&
-                  Elem<2>::kResTile * Elem<2>::NB * 4 % 16 == 0 && Elem<3>::kResTile * Elem<3>::NB * 4 % 16 == 0,
-              "FP32 element tiles must start on 16-byte boundaries");
 
-// T = double: the plain path (bit-exact with the oracle); T = float: the
-// FP32 strain gather of the mixed-precision residual (FP32 element blocks, u
-// rounded to FP32 as it is gathered, FP32 fma, FP32 strain).
+// The plain path's strain gather (bit-exact with the oracle).
 template <class T, int P>
 __global__ void __launch_bounds__(Elem<P>::kGatherTile * Elem<P>::NQ)
 k_gather_strain(int32_t n_el, int64_t n_ip, const T *__restrict__ dphi, const int32_t *__restrict__ dofs,
@@ -60,29 +59,12 @@ k_gather_strain(int32_t n_el, int64_t n_ip, const T *__restrict__ dphi, const in
     if (threadIdx.x == 0) mbar_init(bar, 1);
     __syncthreads();
     if (threadIdx.x == 0) {
-        // a bulk copy moves a multiple of 16 bytes: an FP32 order-2 block is
-        // 648 bytes, so a partial tile of an odd number of elements copies 8
-        // bytes more, which stay inside the tile's staging area (the FP32
-        // block array is allocated with 16 bytes of padding for them)
-        const uint32_t bytes = ((uint32_t)ne * E::NB * (uint32_t)sizeof(T) + 15u) & ~15u;
+        const uint32_t bytes = (uint32_t)ne * E::NB * (uint32_t)sizeof(T);
         mbar_expect_tx(bar, bytes);
         bulk_g2s(s_dn, dphi + (size_t)e0 * E::NB, bytes, bar);
     }
-    for (int k = threadIdx.x; k < ne * E::ND; k += blockDim.x) {
-        const double uk = __ldg(&u[__ldg(&dofs[(size_t)e0 * E::ND + k])]);
-        if constexpr (sizeof(T) == 8) {
-            s_u[k] = uk;
-        } else {
-            // FP32: the displacement relative to the element's first connect
-            // (same component), formed in FP64 before rounding.  The strain of
-            // a rigid translation is zero, so the strain is unchanged, but the
-            // rounded values now carry the variation across the element
-            // instead of the far-field displacement, which is orders of
-            // magnitude larger than that variation
-            const size_t comp = (size_t)e0 * E::ND + (size_t)(k / E::ND) * E::ND + (k & 1);
-            s_u[k] = (T)(uk - __ldg(&u[__ldg(&dofs[comp])]));
-        }
-    }
+    for (int k = threadIdx.x; k < ne * E::ND; k += blockDim.x)
+        s_u[k] = __ldg(&u[__ldg(&dofs[(size_t)e0 * E::ND + k])]);
     const bool ok = mbar_wait_bounded(bar, 0);
     __syncthreads();
     if (!ok) {
@@ -110,8 +92,7 @@ k_gather_strain(int32_t n_el, int64_t n_ip, const T *__restrict__ dphi, const in
     strain[2 * n_ip + ip] = eyy;
 }
 
-// V = double: the plain path; V = float: the FP32 residual scatter of the
-// mixed-precision residual (FP32 blocks, stresses and fma accumulation).
+// The plain path's element forces (bit-exact with the oracle).
 template <class V, int P>
 __global__ void __launch_bounds__(Elem<P>::kResTile * Elem<P>::ND)
 k_stress_residual(int32_t n_el, int64_t n_ip, const V *__restrict__ dphi, const V *__restrict__ sigma_w,
@@ -128,7 +109,7 @@ k_stress_residual(int32_t n_el, int64_t n_ip, const V *__restrict__ dphi, const 
     if (threadIdx.x == 0) mbar_init(bar, 1);
     __syncthreads();
     if (threadIdx.x == 0) {
-        const uint32_t bytes = ((uint32_t)ne * E::NB * (uint32_t)sizeof(V) + 15u) & ~15u;   // see k_gather_strain
+        const uint32_t bytes = (uint32_t)ne * E::NB * (uint32_t)sizeof(V);
         mbar_expect_tx(bar, bytes);
         bulk_g2s(s_dn, dphi + (size_t)e0 * E::NB, bytes, bar);
     }
@@ -161,6 +142,184 @@ k_stress_residual(int32_t n_el, int64_t n_ip, const V *__restrict__ dphi, const 
     fe[(size_t)(e0 + el) * E::ND + j] = -acc;
 }
 
+// ---- FP32 residual kernels (IPFEM_MIXED with FP32 residuals) ----------------
+// One CTA per tile of kTile32 = 32 elements.  The tile's blocks arrive in one
+// bulk copy, laid out [d][n][element][q] with the point index padded to an odd
+// stride QS: the gather's threads (one per point, q fastest) and the stress
+// kernel's threads (one per node, element fastest) both read 32 different
+// banks per warp.  Every output keeps the fma order of the element-major
+// kernels above.
+
+// odd stride (in words) of the per-element point rows
+template <int N> struct OddStride { static constexpr int value = N | 1; };
+// float2 rows: 8-byte words at a stride that keeps the 16 lanes of each
+// half-warp phase on distinct bank pairs
+template <int N> struct PairStride { static constexpr int value = (N % 4 == 0) ? N + 2 : N; };
+// words of one tile of FP32 residual blocks
+template <int P> struct Tile32 {
+    static constexpr int QS = OddStride<Elem<P>::NQ>::value;
+    static constexpr int words = 2 * Elem<P>::NN * kTile32 * QS;
+    static_assert(words * 4 % 16 == 0, "tiles start on 16-byte boundaries and are bulk-copied whole");
+};
+
+template <int P>
+__global__ void k_tile_blocks32(int32_t n_el, int64_t total, const double *__restrict__ dphi,
+                                float *__restrict__ dphiT)
+{
+    typedef Elem<P> E;
+    constexpr int QS = Tile32<P>::QS, W = Tile32<P>::words;
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < total; k += (int64_t)gridDim.x * blockDim.x) {
+        const int o = (int)(k % W);
+        const int q = o % QS, el = (o / QS) % kTile32, dn = o / (QS * kTile32);
+        const int d = dn / E::NN, n = dn - d * E::NN;
+        const int64_t e = (k / W) * kTile32 + el;
+        dphiT[k] = (q < E::NQ && e < n_el) ? (float)dphi[((e * E::NQ + q) * 2 + d) * E::NN + n] : 0.0f;
+    }
+}
+
+// strain of every point of the tile: one thread per point (q fastest), so the
+// strains leave in coalesced rows.  Each displacement is taken relative to the
+// element's first connect (same component), formed in FP64 before rounding.
+// The strain of a rigid translation is zero, so the strain is unchanged, but
+// the rounded values carry the variation across the element instead of the
+// far-field displacement, which is orders of magnitude larger.
+template <int P>
+__global__ void __launch_bounds__(kTile32 * Elem<P>::NQ)
+k_gather_strain32(int32_t n_el, int64_t n_ip, const float *__restrict__ dphiT, const int32_t *__restrict__ dofs,
+                  const double *__restrict__ u, float *__restrict__ strain, int *__restrict__ err)
+{
+    typedef Elem<P> E;
+    constexpr int T = kTile32, QS = Tile32<P>::QS, W = Tile32<P>::words;
+    extern __shared__ __align__(128) unsigned char smem[];
+    uint64_t *bar = reinterpret_cast<uint64_t *>(smem);
+    float *s_dn = reinterpret_cast<float *>(smem + 128);   // [2][NN][T][QS]
+    float *s_u = s_dn + W;                                  // [T][ND]
+    const int32_t e0 = blockIdx.x * T;
+    const int ne = min(T, n_el - e0);
+    if (threadIdx.x == 0) mbar_init(bar, 1);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        mbar_expect_tx(bar, W * sizeof(float));
+        bulk_g2s(s_dn, dphiT + (size_t)blockIdx.x * W, W * sizeof(float), bar);
+    }
+    // the tile's 2 NN T displacements, two per thread (ND = 2 NQ), with both
+    // threads' index loads issued before their displacement loads
+    static_assert(E::ND == 2 * E::NQ, "two staged displacements per thread");
+    const int32_t *de = dofs + (size_t)e0 * E::ND;
+    const int lim = ne * E::ND;
+    const int k0 = threadIdx.x, k1 = threadIdx.x + T * E::NQ;
+    int32_t i0 = 0, j0 = 0, i1 = 0, j1 = 0;
+    if (k0 < lim) {
+        i0 = __ldg(&de[k0]);
+        j0 = __ldg(&de[k0 - k0 % E::ND + (k0 & 1)]);
+    }
+    if (k1 < lim) {
+        i1 = __ldg(&de[k1]);
+        j1 = __ldg(&de[k1 - k1 % E::ND + (k1 & 1)]);
+    }
+    double a0 = 0.0, b0 = 0.0, a1 = 0.0, b1 = 0.0;
+    if (k0 < lim) {
+        a0 = __ldg(&u[i0]);
+        b0 = __ldg(&u[j0]);
+    }
+    if (k1 < lim) {
+        a1 = __ldg(&u[i1]);
+        b1 = __ldg(&u[j1]);
+    }
+    if (k0 < lim) s_u[k0] = (float)(a0 - b0);
+    if (k1 < lim) s_u[k1] = (float)(a1 - b1);
+    const bool ok = mbar_wait_bounded(bar, 0);
+    __syncthreads();
+    if (!ok) {
+        if (threadIdx.x == 0) atomicExch(err, kErrBulkWait);
+        return;
+    }
+    const int el = threadIdx.x / E::NQ, q = threadIdx.x - el * E::NQ;
+    if (el >= ne) return;
+    const float *dx = s_dn + el * QS + q;                   // dx[n T QS]
+    const float *dy = dx + E::NN * T * QS;
+    const float *ue = s_u + el * E::ND;
+    float exx = 0.0f, gxy = 0.0f, eyy = 0.0f;
+#pragma unroll
+    for (int n = 0; n < E::NN; n++) exx = fmaf(dx[n * T * QS], ue[2 * n], exx);
+#pragma unroll
+    for (int n = 0; n < E::NN; n++) {
+        gxy = fmaf(dy[n * T * QS], ue[2 * n], gxy);
+        gxy = fmaf(dx[n * T * QS], ue[2 * n + 1], gxy);
+    }
+#pragma unroll
+    for (int n = 0; n < E::NN; n++) eyy = fmaf(dy[n * T * QS], ue[2 * n + 1], eyy);
+    const int64_t ip = (int64_t)e0 * E::NQ + threadIdx.x;
+    strain[ip] = exx;
+    strain[n_ip + ip] = gxy;
+    strain[2 * n_ip + ip] = eyy;
+}
+
+// element forces -B^T (w sigma) of the tile: thread (node, element), element
+// fastest, both components, each summed over the points in the element-major
+// kernel's order
+template <int P>
+__global__ void __launch_bounds__(kTile32 * Elem<P>::NN)
+k_stress_residual32(int32_t n_el, int64_t n_ip, const float *__restrict__ dphiT, const float *__restrict__ sigma_w,
+                    float *__restrict__ fe, int *__restrict__ err)
+{
+    typedef Elem<P> E;
+    constexpr int T = kTile32, QS = Tile32<P>::QS, W = Tile32<P>::words, FS = PairStride<E::ND>::value;
+    extern __shared__ __align__(128) unsigned char smem[];
+    uint64_t *bar = reinterpret_cast<uint64_t *>(smem);
+    float *s_dn = reinterpret_cast<float *>(smem + 128);   // [2][NN][T][QS]
+    float *s_sig = s_dn + W;                                // [3][T][QS]
+    float *s_fe = s_sig + 3 * T * QS;                       // [T][FS]
+    const int32_t e0 = blockIdx.x * T;
+    const int ne = min(T, n_el - e0);
+    if (threadIdx.x == 0) mbar_init(bar, 1);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        mbar_expect_tx(bar, W * sizeof(float));
+        bulk_g2s(s_dn, dphiT + (size_t)blockIdx.x * W, W * sizeof(float), bar);
+    }
+    // the tile's weighted stresses: one point per thread (NN = NQ), its three
+    // components loaded together
+    static_assert(E::NN == E::NQ, "one staged point per thread");
+    {
+        const int t = threadIdx.x;
+        if (t < ne * E::NQ) {
+            const int64_t ip = (int64_t)e0 * E::NQ + t;
+            const float a = sigma_w[ip], b = sigma_w[n_ip + ip], c = sigma_w[2 * n_ip + ip];
+            const int e = t / E::NQ, q = t - e * E::NQ;
+            s_sig[e * QS + q] = a;
+            s_sig[(T + e) * QS + q] = b;
+            s_sig[(2 * T + e) * QS + q] = c;
+        }
+    }
+    const bool ok = mbar_wait_bounded(bar, 0);
+    __syncthreads();
+    if (!ok) {
+        if (threadIdx.x == 0) atomicExch(err, kErrBulkWait);
+        return;
+    }
+    const int el = threadIdx.x % T, n = threadIdx.x / T;
+    const float *dnx = s_dn + (n * T + el) * QS;            // dNx at q: dnx[q], dNy: dnx[NN T QS + q]
+    const float *dny = dnx + E::NN * T * QS;
+    const float *sxx = s_sig + el * QS, *sxy = sxx + T * QS, *syy = sxy + T * QS;
+    float fx = 0.0f, fy = 0.0f;
+#pragma unroll
+    for (int q = 0; q < E::NQ; q++) {
+        const float nx = dnx[q], ny = dny[q], txy = sxy[q];
+        fx = fmaf(nx, sxx[q], fx);
+        fx = fmaf(ny, txy, fx);
+        fy = fmaf(nx, txy, fy);
+        fy = fmaf(ny, syy[q], fy);
+    }
+    *reinterpret_cast<float2 *>(&s_fe[el * FS + 2 * n]) = make_float2(-fx, -fy);
+    __syncthreads();
+    float2 *out = reinterpret_cast<float2 *>(fe + (size_t)e0 * E::ND);
+    for (int k = threadIdx.x; k < ne * E::NN; k += blockDim.x) {
+        const int e = k / E::NN, nn = k - e * E::NN;
+        out[k] = *reinterpret_cast<const float2 *>(&s_fe[e * FS + 2 * nn]);
+    }
+}
+
 // Per node: contributions of the incident element of each colour (0 if none),
 // summed in the reference's pairwise slab order
 // (TPZNumericalIntegrator.cpp:69-77: slab k += slab (nc-ca)+k, nc -= ca).
@@ -168,54 +327,81 @@ template <class V> struct Pair;
 template <> struct Pair<double> { typedef double2 type; };
 template <> struct Pair<float> { typedef float2 type; };
 
+// The reference's pairwise slab sum over NC colours, unrolled at compile time
+// so that the per-colour sums stay in registers: step with ca = nc / 2 adds
+// slab first + k (first = nc - ca) into slab k for k < ca, then nc -= ca.
+template <int NC> struct SlabPairs {
+    template <class V>
+    __device__ static void run(V *sx, V *sy)
+    {
+        constexpr int ca = NC / 2, first = NC - ca;
+#pragma unroll
+        for (int k = 0; k < ca; k++) {
+            sx[k] = sx[k] + sx[first + k];
+            sy[k] = sy[k] + sy[first + k];
+        }
+        SlabPairs<NC - ca>::run(sx, sy);
+    }
+};
+template <> struct SlabPairs<1> {
+    template <class V> __device__ static void run(V *, V *) {}
+};
+template <> struct SlabPairs<0> {
+    template <class V> __device__ static void run(V *, V *) {}
+};
+
 // V = float: the element forces of the FP32 residual, summed in FP32; the
-// external load (FP64) is added to the FP32 sum in FP64.
-template <class V>
-__global__ void __launch_bounds__(256) k_color_reduce(int32_t n_nodes, int n_colors,
-                                                      const int32_t *__restrict__ inc,
-                                                      const V *__restrict__ fe, double lambda,
-                                                      int with_load, const double *__restrict__ f0,
-                                                      const double *__restrict__ df,
+// external load (FP64) is added to the FP32 sum in FP64.  NC = the number of
+// colours.  The load vector and the Dirichlet flags are read before the
+// incidence so that their latency overlaps the dependent element-force loads.
+template <class V, int NC>
+__global__ void __launch_bounds__(256) k_color_reduce(int32_t n_nodes, const int32_t *__restrict__ inc,
+                                                      const V *__restrict__ fe, int with_load,
+                                                      const double *__restrict__ lin,
                                                       const uint8_t *__restrict__ fixed,
                                                       double *__restrict__ res)
 {
     const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n_nodes) return;
-    V sx[kMaxColors], sy[kMaxColors];
+    double2 lv = make_double2(0.0, 0.0);
+    uchar2 fx = make_uchar2(0, 0);
+    if (with_load) {
+        lv = __ldg(reinterpret_cast<const double2 *>(lin) + i);
+        fx = __ldg(reinterpret_cast<const uchar2 *>(fixed) + i);
+    }
+    constexpr int NS = NC > 0 ? NC : 1;
+    int32_t k[NS];
 #pragma unroll
-    for (int c = 0; c < kMaxColors; c++) {
+    for (int c = 0; c < NC; c++) k[c] = __ldg(&inc[(size_t)c * n_nodes + i]);
+    V sx[NS], sy[NS];
+    sx[0] = V(0);
+    sy[0] = V(0);
+#pragma unroll
+    for (int c = 0; c < NC; c++) {
         sx[c] = V(0);
         sy[c] = V(0);
-        if (c < n_colors) {
-            const int32_t k = __ldg(&inc[(size_t)c * n_nodes + i]);
-            if (k >= 0) {
-                const typename Pair<V>::type v = *reinterpret_cast<const typename Pair<V>::type *>(&fe[2 * (size_t)k]);
-                sx[c] = v.x;
-                sy[c] = v.y;
-            }
+        if (k[c] >= 0) {
+            const typename Pair<V>::type v = *reinterpret_cast<const typename Pair<V>::type *>(&fe[2 * (size_t)k[c]]);
+            sx[c] = v.x;
+            sy[c] = v.y;
         }
     }
-    int nc = n_colors, ca = n_colors / 2;
-    while (ca > 0) {
-        const int first = nc - ca;
-#pragma unroll
-        for (int k = 0; k < kMaxColors / 2; k++)
-            if (k < ca) {
-                sx[k] = sx[k] + sx[first + k];
-                sy[k] = sy[k] + sy[first + k];
-            }
-        nc -= ca;
-        ca = nc / 2;
-    }
+    SlabPairs<NC>::run(sx, sy);
     double rx = (double)sx[0], ry = (double)sy[0];
     if (with_load) {
-        const double lx = fma(lambda, df[2 * (size_t)i], f0[2 * (size_t)i]);
-        const double ly = fma(lambda, df[2 * (size_t)i + 1], f0[2 * (size_t)i + 1]);
-        rx = fixed[2 * (size_t)i] ? 0.0 : rx + lx;
-        ry = fixed[2 * (size_t)i + 1] ? 0.0 : ry + ly;
+        rx = fx.x ? 0.0 : rx + lv.x;
+        ry = fx.y ? 0.0 : ry + lv.y;
     }
-    res[2 * (size_t)i] = rx;
-    res[2 * (size_t)i + 1] = ry;
+    reinterpret_cast<double2 *>(res)[i] = make_double2(rx, ry);
+}
+
+// rhs_linear = f0 + lambda df (AssembleBoundaryData's fRhsLinear,
+// TPZElastoPlasticIntPointsStructMatrix.cpp:156-167), once per load factor
+__global__ void k_load_vector(int32_t neq, double lambda, const double *__restrict__ f0,
+                              const double *__restrict__ df, double *__restrict__ lin)
+{
+    for (int32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < neq; i += gridDim.x * blockDim.x)
+        lin[i] = fma(lambda, df[i], f0[i]);
 }
 
 constexpr int kStiffWarps = 4;
@@ -374,12 +560,49 @@ void launch_gather_strain(ipfem_ctx *c, const double *d_u, double *d_strain)
     }
 }
 
+template <int P>
+static void tile_blocks32_p(ipfem_ctx *c)
+{
+    const Setup &s = c->s;
+    const int64_t total = (int64_t)((s.n_el + kTile32 - 1) / kTile32) * Tile32<P>::words;
+    const unsigned grid = (unsigned)std::min<int64_t>((total + 255) / 256, 152 * 16);
+    k_tile_blocks32<P><<<grid, 256, 0, c->stream>>>(s.n_el, total, c->d_dphi, c->mx.dphiT);
+}
+
+void launch_tile_blocks32(ipfem_ctx *c)
+{
+    switch (c->s.order) {
+    case 1: tile_blocks32_p<1>(c); break;
+    case 3: tile_blocks32_p<3>(c); break;
+    default: tile_blocks32_p<2>(c); break;
+    }
+}
+
+// dynamic shared memory above the default 48 KB (order 3 tiles) is opted into per kernel
+template <class K>
+static void allow_smem(K kern, size_t bytes)
+{
+    if (bytes > 48 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+}
+
+template <int P>
+static void gather_strain32_p(ipfem_ctx *c, const double *d_u, float *d_strain)
+{
+    typedef Elem<P> E;
+    const Setup &s = c->s;
+    const unsigned grid = (unsigned)((s.n_el + kTile32 - 1) / kTile32);
+    const size_t smem = 128 + (size_t)(Tile32<P>::words + kTile32 * E::ND) * sizeof(float);
+    allow_smem(k_gather_strain32<P>, smem);
+    k_gather_strain32<P><<<grid, kTile32 * E::NQ, smem, c->stream>>>(s.n_el, s.n_ip, c->mx.dphiT, c->d_dofs, d_u,
+                                                                       d_strain, c->d_err);
+}
+
 void launch_gather_strain32(ipfem_ctx *c, const double *d_u, float *d_strain)
 {
     switch (c->s.order) {
-    case 1: gather_strain_p<float, 1>(c, c->mx.dphi, d_u, d_strain); break;
-    case 3: gather_strain_p<float, 3>(c, c->mx.dphi, d_u, d_strain); break;
-    default: gather_strain_p<float, 2>(c, c->mx.dphi, d_u, d_strain); break;
+    case 1: gather_strain32_p<1>(c, d_u, d_strain); break;
+    case 3: gather_strain32_p<3>(c, d_u, d_strain); break;
+    default: gather_strain32_p<2>(c, d_u, d_strain); break;
     }
 }
 
@@ -403,29 +626,59 @@ void launch_stress_residual(ipfem_ctx *c, const double *d_sigma_w, double *d_fe)
     }
 }
 
+template <int P>
+static void stress_residual32_p(ipfem_ctx *c, const float *d_sigma_w, float *d_fe)
+{
+    typedef Elem<P> E;
+    const Setup &s = c->s;
+    const unsigned grid = (unsigned)((s.n_el + kTile32 - 1) / kTile32);
+    const size_t smem = 128 + (size_t)(Tile32<P>::words + 3 * kTile32 * Tile32<P>::QS +
+                                       kTile32 * PairStride<E::ND>::value) * sizeof(float);
+    allow_smem(k_stress_residual32<P>, smem);
+    k_stress_residual32<P><<<grid, kTile32 * E::NN, smem, c->stream>>>(s.n_el, s.n_ip, c->mx.dphiT, d_sigma_w, d_fe,
+                                                                         c->d_err);
+}
+
 void launch_stress_residual32(ipfem_ctx *c, const float *d_sigma_w, float *d_fe)
 {
     switch (c->s.order) {
-    case 1: stress_residual_p<float, 1>(c, c->mx.dphi, d_sigma_w, d_fe); break;
-    case 3: stress_residual_p<float, 3>(c, c->mx.dphi, d_sigma_w, d_fe); break;
-    default: stress_residual_p<float, 2>(c, c->mx.dphi, d_sigma_w, d_fe); break;
+    case 1: stress_residual32_p<1>(c, d_sigma_w, d_fe); break;
+    case 3: stress_residual32_p<3>(c, d_sigma_w, d_fe); break;
+    default: stress_residual32_p<2>(c, d_sigma_w, d_fe); break;
     }
 }
 
-void launch_color_reduce(ipfem_ctx *c, const double *d_fe, double lambda, int with_load, double *d_res)
+void launch_load_vector(ipfem_ctx *c)
 {
-    const Setup &s = c->s;
-    const unsigned grid = (unsigned)((s.n_nodes + 255) / 256);
-    k_color_reduce<double><<<grid, 256, 0, c->stream>>>(s.n_nodes, s.n_colors, c->d_inc, d_fe, lambda, with_load,
-                                                         c->d_f0, c->d_df, c->d_fixed, d_res);
+    const int32_t neq = c->s.neq;
+    const unsigned grid = (unsigned)std::max(1, std::min((neq + 255) / 256, 152 * 8));
+    k_load_vector<<<grid, 256, 0, c->stream>>>(neq, c->load_factor, c->d_f0, c->d_df, c->d_lin);
 }
 
-void launch_color_reduce32(ipfem_ctx *c, const float *d_fe, double lambda, int with_load, double *d_res)
+// the instantiation for the mesh's colour count (at most kMaxColors, checked at setup)
+template <class V, int NC = 0>
+static void color_reduce_nc(ipfem_ctx *c, const V *d_fe, int with_load, double *d_res)
 {
-    const Setup &s = c->s;
-    const unsigned grid = (unsigned)((s.n_nodes + 255) / 256);
-    k_color_reduce<float><<<grid, 256, 0, c->stream>>>(s.n_nodes, s.n_colors, c->d_inc, d_fe, lambda, with_load,
-                                                        c->d_f0, c->d_df, c->d_fixed, d_res);
+    if constexpr (NC <= kMaxColors) {
+        const Setup &s = c->s;
+        if (s.n_colors != NC) {
+            color_reduce_nc<V, NC + 1>(c, d_fe, with_load, d_res);
+            return;
+        }
+        const unsigned grid = (unsigned)((s.n_nodes + 255) / 256);
+        k_color_reduce<V, NC><<<grid, 256, 0, c->stream>>>(s.n_nodes, c->d_inc, d_fe, with_load, c->d_lin,
+                                                             c->d_fixed, d_res);
+    }
+}
+
+void launch_color_reduce(ipfem_ctx *c, const double *d_fe, int with_load, double *d_res)
+{
+    color_reduce_nc<double>(c, d_fe, with_load, d_res);
+}
+
+void launch_color_reduce32(ipfem_ctx *c, const float *d_fe, int with_load, double *d_res)
+{
+    color_reduce_nc<float>(c, d_fe, with_load, d_res);
 }
 
 void launch_stiffness(ipfem_ctx *c)

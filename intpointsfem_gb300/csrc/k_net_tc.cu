@@ -1,9 +1,12 @@
 // Fused per-node network (32 -> 128 -> 128 -> 20) on the 5th-generation tensor
 // cores: tcgen05.mma (kind::f16, BF16 operands from shared memory, FP32
-// accumulators in tensor memory), tcgen05.ld for the epilogues.  One CTA of
-// 128 threads runs tiles of 128 nodes; thread t owns node row t, which is
-// TMEM lane t.  Layer 1 accumulates in TMEM columns 0..127, layer 2 in
-// 128..255, layer 3 (N padded to 32) reuses columns 0..31.
+// accumulators in tensor memory), tcgen05.ld for the epilogues.  Tiles of 128
+// nodes; node row r is TMEM lane r.  Layer 1 accumulates in TMEM columns
+// 0..127, layer 2 in 128..255, layer 3 (N padded to 32) reuses columns 0..31.
+// The inference kernel runs 8 warps per CTA: warps w and w + 4 read the
+// same lane quadrant (a warp may only access lanes 32 (w % 4) .. + 31) and
+// split the columns, so each epilogue takes half as long; the training
+// kernels run 4 warps, thread t = row t.
 //
 // Shared-memory operands use the canonical K-major layout without swizzle:
 // core matrices of 8 rows x 16 bytes (8 BF16 along K) stored as 128
@@ -138,21 +141,28 @@ __device__ __forceinline__ void store_hidden_f32(float *__restrict__ Hrow, uint3
 
 }  // namespace
 
-// O[rows][20] = network(X[rows][32]); persistent CTAs of 128 threads over
-// 128-row tiles.  With H1 and H2 given, the hidden layers relu(X W1 + b1) and
-// relu(H1 W2 + b2) are also written out in FP32 ([rows][128] each; the BF16
-// operand of the next layer is the same value rounded), for the training
-// backward.  A barrier wait that runs out sets *err = 3 and the CTA stops.
-__global__ void __launch_bounds__(128) k_patch_net_tc(int64_t rows, const float *__restrict__ X,
-                                                      const __nv_bfloat16 *__restrict__ w1t,
-                                                      const __nv_bfloat16 *__restrict__ w2t,
-                                                      const __nv_bfloat16 *__restrict__ w3t,
-                                                      const float *__restrict__ b1, const float *__restrict__ b2,
-                                                      const float *__restrict__ b3, float *__restrict__ O,
-                                                      float *__restrict__ H1, float *__restrict__ H2, int *err)
+// O[rows][20] = network(X[rows][32]); persistent CTAs of kNetThreads = 256
+// threads over 128-row tiles: thread t owns row t % 128 and, of every
+// 128-column epilogue, the columns 64 (t / 128) .. + 63.  With H1 and H2
+// given, the hidden layers relu(X W1 + b1) and relu(H1 W2 + b2) are also
+// written out in FP32 ([rows][128] each; the BF16 operand of the next layer is
+// the same value rounded), for the training backward.  A barrier wait that
+// runs out sets *err = 3 and the CTA stops.
+constexpr int kNetThreads = 256;
+
+__global__ void __launch_bounds__(kNetThreads) k_patch_net_tc(int64_t rows, const float *__restrict__ X,
+                                                              const __nv_bfloat16 *__restrict__ w1t,
+                                                              const __nv_bfloat16 *__restrict__ w2t,
+                                                              const __nv_bfloat16 *__restrict__ w3t,
+                                                              const float *__restrict__ b1,
+                                                              const float *__restrict__ b2,
+                                                              const float *__restrict__ b3, float *__restrict__ O,
+                                                              float *__restrict__ H1, float *__restrict__ H2,
+                                                              int *err)
 {
     extern __shared__ __align__(1024) unsigned char smem[];
     const uint32_t tid = threadIdx.x, warp = tid >> 5;
+    const uint32_t r = tid & 127u, half = tid >> 7;                 // row of the tile, column half
     const uint32_t sbase = smem_u32(smem);
     uint64_t *bar = reinterpret_cast<uint64_t *>(smem + OFF_BAR);
     // weights and biases into the canonical layouts (16 bytes = 8 BF16 along K per copy)
@@ -174,8 +184,10 @@ __global__ void __launch_bounds__(128) k_patch_net_tc(int64_t rows, const float 
     }
     float *sb1 = reinterpret_cast<float *>(smem + OFF_B1), *sb2 = reinterpret_cast<float *>(smem + OFF_B2);
     float *sb3 = reinterpret_cast<float *>(smem + OFF_B3);
-    sb1[tid] = b1[tid];
-    sb2[tid] = b2[tid];
+    if (tid < 128) {
+        sb1[tid] = b1[tid];
+        sb2[tid] = b2[tid];
+    }
     if (tid < TC_N3) sb3[tid] = tid < TC_NOUT ? b3[tid] : 0.f;
     if (tid == 0) mbar_init(bar, 1);
     // tensor memory: one warp allocates 256 columns
@@ -190,30 +202,32 @@ __global__ void __launch_bounds__(128) k_patch_net_tc(int64_t rows, const float 
     __syncthreads();
     tc_fence_after();
     const uint32_t tmem = *reinterpret_cast<volatile uint32_t *>(smem + OFF_TMEM);
-    const uint32_t lane_t = tmem + ((warp * 32u) << 16);             // this warp's TMEM lanes
+    const uint32_t lane_t = tmem + (((warp & 3u) * 32u) << 16);      // this warp's TMEM lanes
+    const uint32_t c_lo = 64u * half;                                 // this thread's first epilogue column
     constexpr uint32_t ID128 = idesc_bf16(128, 128), ID32 = idesc_bf16(128, TC_N3);
     uint32_t phase = 0;
     bool ok = true;
     const int64_t n_tiles = (rows + TC_ROWS - 1) / TC_ROWS;
-    // features of this thread's node in the CTA's next tile, loaded one tile
-    // ahead so that the load latency overlaps the current tile's layers
-    float4 f[8];
+    // this thread's 16 features of its row in the CTA's next tile, loaded one
+    // tile ahead so that the load latency overlaps the current tile's layers
+    float4 f[4];
     auto load_features = [&](int64_t tile) {
-        const int64_t r = tile * TC_ROWS + tid;
+        const int64_t row = tile * TC_ROWS + r;
 #pragma unroll
-        for (int j = 0; j < 8; j++)
-            f[j] = (tile < n_tiles && r < rows) ? __ldcs(reinterpret_cast<const float4 *>(X + r * 32) + j)
-                                                : make_float4(0.f, 0.f, 0.f, 0.f);
+        for (int j = 0; j < 4; j++)
+            f[j] = (tile < n_tiles && row < rows)
+                       ? __ldcs(reinterpret_cast<const float4 *>(X + row * 32 + 16 * half) + j)
+                       : make_float4(0.f, 0.f, 0.f, 0.f);
     };
     load_features(blockIdx.x);
     for (int64_t tile = blockIdx.x; tile < n_tiles && ok; tile += gridDim.x) {
-        const int64_t row = tile * TC_ROWS + tid;
+        const int64_t row = tile * TC_ROWS + r;
         // features -> BF16 A operand, then the next tile's features in flight
 #pragma unroll
-        for (int q = 0; q < 4; q++) {
+        for (int q = 0; q < 2; q++) {
             const uint4 w = make_uint4(pk_bf16(f[2 * q].x, f[2 * q].y), pk_bf16(f[2 * q].z, f[2 * q].w),
                                        pk_bf16(f[2 * q + 1].x, f[2 * q + 1].y), pk_bf16(f[2 * q + 1].z, f[2 * q + 1].w));
-            *reinterpret_cast<uint4 *>(smem + OFF_X + cano(tid, 8 * q, 128)) = w;
+            *reinterpret_cast<uint4 *>(smem + OFF_X + cano(r, 16 * half + 8 * q, 128)) = w;
         }
         load_features(tile + gridDim.x);
         fence_async_smem();
@@ -233,11 +247,11 @@ __global__ void __launch_bounds__(128) k_patch_net_tc(int64_t rows, const float 
         if (!ok) break;
         tc_fence_after();
 #pragma unroll 1
-        for (uint32_t c = 0; c < 4; c++) {
+        for (uint32_t c = c_lo; c < c_lo + 64; c += 32) {
             float v[32];
-            tc_ld32(lane_t + 32 * c, v);
-            store_hidden(smem, tid, 32 * c, v, sb1);
-            if (H1 && row < rows) store_hidden_f32(H1 + row * 128, 32 * c, v, sb1);
+            tc_ld32(lane_t + c, v);
+            store_hidden(smem, r, c, v, sb1);
+            if (H1 && row < rows) store_hidden_f32(H1 + row * 128, c, v, sb1);
         }
         fence_async_smem();
         tc_fence_before();
@@ -256,11 +270,11 @@ __global__ void __launch_bounds__(128) k_patch_net_tc(int64_t rows, const float 
         if (!ok) break;
         tc_fence_after();
 #pragma unroll 1
-        for (uint32_t c = 0; c < 4; c++) {
+        for (uint32_t c = c_lo; c < c_lo + 64; c += 32) {
             float v[32];
-            tc_ld32(lane_t + 128 + 32 * c, v);
-            store_hidden(smem, tid, 32 * c, v, sb2);
-            if (H2 && row < rows) store_hidden_f32(H2 + row * 128, 32 * c, v, sb2);
+            tc_ld32(lane_t + 128 + c, v);
+            store_hidden(smem, r, c, v, sb2);
+            if (H2 && row < rows) store_hidden_f32(H2 + row * 128, c, v, sb2);
         }
         fence_async_smem();
         tc_fence_before();
@@ -278,7 +292,7 @@ __global__ void __launch_bounds__(128) k_patch_net_tc(int64_t rows, const float 
         phase ^= 1u;
         if (!ok) break;
         tc_fence_after();
-        {
+        if (half == 0) {
             float v[32];
             tc_ld32(lane_t, v);
             if (row < rows) {
@@ -659,7 +673,7 @@ void launch_patch_net_tc(ipfem_ctx *c, int64_t rows, const float *d_X, float *d_
     const int64_t tiles = (rows + TC_ROWS - 1) / TC_ROWS;
     const unsigned grid = (unsigned)std::max<int64_t>(1, std::min<int64_t>(tiles, 2 * (int64_t)sms));
     const MlpBuffers &m = c->mlp;
-    k_patch_net_tc<<<grid, 128, TC_SMEM, c->stream>>>(
+    k_patch_net_tc<<<grid, kNetThreads, TC_SMEM, c->stream>>>(
         rows, d_X, static_cast<const __nv_bfloat16 *>(m.w1t), static_cast<const __nv_bfloat16 *>(m.w2t),
         static_cast<const __nv_bfloat16 *>(m.w3t), m.params + kOffB1, m.params + kOffB2, m.params + kOffB3, d_O,
         d_H1, d_H2, c->d_err);
