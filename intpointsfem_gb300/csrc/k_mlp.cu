@@ -1119,7 +1119,6 @@ void patch_learn_grad(ipfem_ctx *c, const float *d_r, const float *d_e, int P, f
     const Setup &s = c->s;
     const int32_t n = s.n_nodes;
     const int64_t neq = s.neq;
-    const float *W = m.params;
     cudaStream_t st = c->stream;
     GridInfo G{m.gr, m.gt};
     const unsigned gn = (unsigned)((n + 255) / 256);
