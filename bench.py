@@ -316,10 +316,19 @@ def run_gpu(args):
     wb = ip.WellboreMesh(ip.wellbore_params(n, **args.wb))
     N_STEPS = args.n_steps
     mixed = args.precision == "mixed"
+    if args.mixed_cg_rtol is None:
+        args.mixed_cg_rtol = ip.CHOSEN_CG_RTOL if args.inner == "adaptive" else ip.FIXED_CG_RTOL
     cg_rtol = args.mixed_cg_rtol if mixed else 1e-8
+
+    def set_inner(M):
+        # the mixed methods' inner tolerance: adaptive forcing term or fixed
+        if args.inner == "adaptive":
+            M.set_inner_tolerance(**ip.CHOSEN_INNER)
+
     A = ip.ElastoPlasticIntPointsStructMatrix(wb)         # device-resident arm
     if mixed:
         A.set_precision(ip.MIXED)
+        set_inner(A)
         if args.residual32:
             A.set_residual_precision(32)
     if not args.jacobi:
@@ -376,6 +385,7 @@ def run_gpu(args):
         B = ip.ElastoPlasticIntPointsStructMatrix(wb)
         if mixed:
             B.set_precision(ip.MIXED)
+            set_inner(B)
         if not args.jacobi:
             B.set_preconditioner(ip.PREC_BLOCK_JACOBI)
         if args.no_row_stencils:
@@ -405,6 +415,7 @@ def run_gpu(args):
             if args.no_row_stencils:
                 C_.set_row_stencils(0)
             C_.set_precision(ip.MIXED)
+            set_inner(C_)
             if learned_prec:
                 C_.set_node_grid(2 * n + 1, 2 * n + 1)
                 C_.mlp_init(0)
@@ -435,12 +446,14 @@ def run_gpu(args):
             return out
 
         chosen = mixed_arm(True, args.solve)
-        chosen["method"] = ("mixed + learned: FP32 tangent, flexible CG to %g preconditioned by the learned "
-                            "triangular factor (weights shipped in intpointsfem_gb300/weights), FP64 residual/"
-                            "return mapping/Newton refinement" % args.mixed_cg_rtol)
+        inner = (("adaptive inner tolerance (Eisenstat-Walker, first solve of a step to %g)" % args.mixed_cg_rtol)
+                 if args.inner == "adaptive" else "inner tolerance %g" % args.mixed_cg_rtol)
+        chosen["method"] = ("mixed + learned: FP32 tangent, flexible CG preconditioned by the learned "
+                            "triangular factor (weights shipped in intpointsfem_gb300/weights), %s, FP64 residual/"
+                            "return mapping/Newton refinement" % inner)
         chosen["mixed_jacobi"] = mixed_arm(False, False)
-        chosen["mixed_jacobi"]["method"] = "mixed: FP32 tangent + FP32 %s to %g, FP64 Newton refinement" % (
-            "Jacobi-CG" if args.jacobi else "block-Jacobi CG", args.mixed_cg_rtol)
+        chosen["mixed_jacobi"]["method"] = "mixed: FP32 tangent + FP32 %s, %s, FP64 Newton refinement" % (
+            "Jacobi-CG" if args.jacobi else "block-Jacobi CG", inner)
         chosen["speedup_vs_plain"] = ms_dev / chosen["ms_per_newton_iter"]
         if solve_plain and "solve" in chosen:
             chosen["solve_speedup_vs_plain"] = solve_plain["ms"] / chosen["solve"]["ms"]
@@ -474,8 +487,9 @@ def run_gpu(args):
     cfg = workload_config(args)
     if mixed:
         cfg["workload"] = cfg["workload"].replace("plain FP64", "mixed FP32/FP64").replace(
-            "CG 1e-8", "CG %g" % cg_rtol)
+            "CG 1e-8", ("CG adaptive (first solve %g)" if args.inner == "adaptive" else "CG %g") % cg_rtol)
         cfg["cg_rtol"] = cg_rtol
+        cfg["inner_tolerance"] = args.inner
     cfg["replicas"] = ws
     line = {
         "metric": METRIC, "value": ms_dev, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
@@ -541,8 +555,11 @@ def main():
     ap.add_argument("--cpu-cg-sample", type=int, default=100)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--precision", default="plain", choices=["plain", "mixed"])
-    ap.add_argument("--mixed-cg-rtol", type=float, default=3e-3,
-                    help="inner FP32 tolerance of the mixed methods (the chosen method's: 3e-3)")
+    ap.add_argument("--mixed-cg-rtol", type=float, default=None,
+                    help="inner FP32 tolerance of the mixed methods: of the first solve of a load step with the "
+                         "adaptive inner tolerance (default 3e-2), of every solve with --inner fixed (default 3e-3)")
+    ap.add_argument("--inner", default="adaptive", choices=["adaptive", "fixed"],
+                    help="inner tolerance of the mixed methods' Newton iterations")
     ap.add_argument("--no-chosen", dest="chosen", action="store_false")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--residual32", action="store_true",

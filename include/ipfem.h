@@ -205,6 +205,22 @@ ipfem_status ipfem_set_newton_accel(ipfem_ctx *ctx, int mode);
  * tangent of the first assembly after ipfem_newton_begin is kept for every
  * later linear solve, and later assemblies compute the residual only. */
 ipfem_status ipfem_set_newton_tangent(ipfem_ctx *ctx, int mode);
+/* Inner tolerance of the Newton iterations (no counterpart in the reference,
+ * whose solve is to a fixed tolerance).  mode 0 (default): every linear
+ * solve to opts.cg_rtol.  mode 1: an adaptive forcing term (Eisenstat and
+ * Walker's choice 2 with the safeguards of Kelley, "Iterative Methods for
+ * Linear and Nonlinear Equations", 1995, ch. 6): the first solve of a load
+ * step to opts.cg_rtol, then
+ *   eta_k = gamma (|R_k| / |R_k-1|)^alpha, at least gamma eta_k-1^alpha when
+ *   that is above 0.1, at least 0.5 newton_rtol |R0| / |R_k| (no solve
+ *   beyond what convergence needs), clamped to [eta_min, eta_max].
+ * The inner solves stop at relative residual eta_k, so no solve is tighter
+ * than the Newton contraction it serves (slow where the tangent is
+ * inconsistent).  Eisenstat and Walker suggest gamma 0.9, alpha 2 or
+ * (1 + sqrt 5) / 2; eta_min keeps FP32 inner solves above their precision
+ * floor. */
+ipfem_status ipfem_set_inner_tolerance(ipfem_ctx *ctx, int mode, double gamma, double alpha, double eta_min,
+                                       double eta_max);
 
 /* Row stencils of the SpMVs.  On a structured node grid every row of the
  * block tangent has one of a few dozen column-offset patterns (interior

@@ -20,10 +20,16 @@ PLAIN_FP64, MIXED = 0, 1
 PREC_JACOBI, PREC_MLP, PREC_BLOCK_JACOBI = 0, 1, 2
 MLP_PARAMS = 23316
 # Inner (FP32 flexible-CG) tolerance of the chosen method, mixed precision +
-# learned preconditioner, inside the FP64 Newton loop to 1e-8.  Measured over
-# the whole 20-step 400 x 400 solve on a GB300: 1e-2: 24.3 s (163 Newton
-# iterations), 3e-3: 20.6 s (148), 1e-3: 22.1 s (148), 1e-4: 30.2 s (148).
-CHOSEN_CG_RTOL = 3e-3
+# learned preconditioner, inside the FP64 Newton loop to 1e-8: the adaptive
+# forcing term (ipfem_set_inner_tolerance) with the first solve of each load
+# step to CHOSEN_CG_RTOL.  Measured over the whole 20-step 400 x 400 solve on a
+# GB300: fixed tolerances 1e-2: 24.3 s (163 Newton iterations), 3e-3: 18.9 s
+# (148), 1e-3: 22.1 s (148), 1e-4: 30.2 s (148); adaptive (gamma 0.9, alpha 2,
+# eta in [1e-4, 0.3], first solve 3e-2): 16.0 s (151 Newton iterations, 17 %
+# fewer CG iterations), u and sigma within 3e-10 of the fixed-3e-3 solve.
+CHOSEN_CG_RTOL = 3e-2
+CHOSEN_INNER = dict(mode=1, gamma=0.9, alpha=2.0, eta_min=1e-4, eta_max=0.3)
+FIXED_CG_RTOL = 3e-3       # the best fixed inner tolerance (mode 0)
 STATUS = {0: "ok", 1: "not converged", 2: "non-finite value", 3: "CG breakdown", 4: "out of device memory",
           5: "invalid argument", 6: "CUDA error", 7: "no sm_103 device"}
 
@@ -154,6 +160,7 @@ def lib():
             "ipfem_wellbore_build": (S, [C.POINTER(WellboreParams), C.POINTER(C.POINTER(Wellbore))]),
             "ipfem_wellbore_free": (None, [C.POINTER(Wellbore)]),
             "ipfem_set_newton_tangent": (S, [P, S]),
+            "ipfem_set_inner_tolerance": (S, [P, S, C.c_double, C.c_double, C.c_double, C.c_double]),
             "ipfem_set_row_stencils": (S, [P, S]),
             "ipfem_row_stencil_count": (S, [P, _ip, _ip]),
             "ipfem_layout_info": (S, [P, S, _lp, _lp, _ip]),
@@ -409,6 +416,12 @@ class ElastoPlasticIntPointsStructMatrix:
         first assembly kept (the reference's logged runs: main.cpp:218-222 with
         AssembleResidual in place of the Assemble of main.cpp:229-233)"""
         self._check(lib().ipfem_set_newton_tangent(self._ctx, int(mode)))
+
+    def set_inner_tolerance(self, mode, gamma=0.9, alpha=2.0, eta_min=1e-5, eta_max=0.1):
+        """0: every inner solve to cg_rtol; 1: adaptive forcing term (Eisenstat-Walker
+        choice 2 with Kelley's safeguards), the first solve of a step to cg_rtol"""
+        self._check(lib().ipfem_set_inner_tolerance(self._ctx, int(mode), float(gamma), float(alpha),
+                                                     float(eta_min), float(eta_max)))
 
     def set_row_stencils(self, on):
         """1 (default): SpMVs form block columns from row stencils where the

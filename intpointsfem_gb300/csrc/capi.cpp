@@ -830,6 +830,17 @@ static ipfem_status newton_advance(ipfem_ctx *c, int32_t n_iters, double *du, ip
         }
         bool conv = (ns.r0 == 0.0);
         if (!conv) {
+            // inner tolerance of this Newton iteration
+            double eta = o.cg_rtol;
+            if (c->inner.mode == 1 && ns.it > 0) {
+                const InnerTolerance &t = c->inner;
+                eta = t.gamma * std::pow(ns.rn / ns.rn_prev, t.alpha);
+                const double carry = t.gamma * std::pow(ns.eta, t.alpha);
+                if (carry > 0.1) eta = std::max(eta, carry);
+                eta = std::max(eta, 0.5 * o.newton_rtol * ns.r0 / ns.rn);
+                eta = std::min(std::max(eta, t.eta_min), t.eta_max);
+            }
+            ns.eta = eta;
             int k = 0;
             const int64_t fb0 = c->fcg_fallbacks;
             Range rg("ipfem:newton:iteration");
@@ -837,7 +848,7 @@ static ipfem_status newton_advance(ipfem_ctx *c, int32_t n_iters, double *du, ip
             ipfem_status e;
             {
                 Range rs("ipfem:solve");
-                e = solve_device(c, c->d_rhs, o.cg_rtol, o.cg_max_it, &k, du, c->newton_accel ? 0 : 1);
+                e = solve_device(c, c->d_rhs, eta, o.cg_max_it, &k, du, c->newton_accel ? 0 : 1);
             }
             st->fcg_fallbacks += c->fcg_fallbacks - fb0;
             cudaEventRecord(ev[1], c->stream);
@@ -856,7 +867,7 @@ static ipfem_status newton_advance(ipfem_ctx *c, int32_t n_iters, double *du, ip
                 int k2 = 0;
                 const int64_t fb1 = c->fcg_fallbacks;
                 cudaEventRecord(ev[0], c->stream);
-                e = solve_device(c, c->d_rhs, o.cg_rtol, o.cg_max_it, &k2, du, 0);
+                e = solve_device(c, c->d_rhs, eta, o.cg_max_it, &k2, du, 0);
                 st->fcg_fallbacks += c->fcg_fallbacks - fb1;
                 cudaEventRecord(ev[1], c->stream);
                 st->ms_solve += elapsed();
@@ -883,6 +894,7 @@ static ipfem_status newton_advance(ipfem_ctx *c, int32_t n_iters, double *du, ip
             st->ms_assemble += elapsed();
             if (e != IPFEM_OK) return e;
             const double rn_prev = ns.rn;
+            ns.rn_prev = rn_prev;
             ns.rn = std::sqrt(rsq);
             if (!std::isfinite(ns.rn)) return fail(c, IPFEM_NAN, "residual is not finite");
             const int was32 = c->res32_active;
@@ -914,11 +926,11 @@ static ipfem_status newton_advance(ipfem_ctx *c, int32_t n_iters, double *du, ip
                 std::fprintf(c->iter_log,
                              "{\"step\": %d, \"iter\": %d, \"cg_iters\": %d, \"res\": %.17g, \"res_rel\": %.17g, "
                              "\"ms_solve\": %.6f, \"ms_assemble\": %.6f, \"ips_assemble\": %.6g, "
-                             "\"fcg_fallback\": %d, \"res32\": %d, \"res32_rel\": %.17g}\n",
+                             "\"fcg_fallback\": %d, \"res32\": %d, \"res32_rel\": %.17g, \"cg_rtol\": %.6g}\n",
                              ns.step, ns.it, k, ns.rn, ns.r0 > 0.0 ? ns.rn / ns.r0 : 0.0, ms, ma,
                              ma > 0.0 ? (double)c->s.n_ip / (1e-3 * ma) : 0.0,
                              (int)(c->fcg_fallbacks - fb0), c->res32_active,
-                             was32 && ns.r0 > 0.0 ? std::sqrt(rsq32) / ns.r0 : 0.0);
+                             was32 && ns.r0 > 0.0 ? std::sqrt(rsq32) / ns.r0 : 0.0, eta);
                 std::fflush(c->iter_log);
             }
         }
@@ -949,6 +961,24 @@ static ipfem_status newton_advance(ipfem_ctx *c, int32_t n_iters, double *du, ip
         }
     }
     st->converged = ns.all_converged;
+    return IPFEM_OK;
+}
+
+ipfem_status ipfem_set_inner_tolerance(ipfem_ctx *c, int mode, double gamma, double alpha, double eta_min,
+                                       double eta_max)
+{
+    if (!c) return IPFEM_INVALID;
+    if (mode != 0 && mode != 1) return fail(c, IPFEM_INVALID, "inner tolerance mode must be 0 or 1");
+    if (mode == 1 && !(gamma > 0.0 && gamma <= 1.0 && alpha > 1.0 && alpha <= 2.0 && eta_min > 0.0 &&
+                       eta_min <= eta_max && eta_max < 1.0))
+        return fail(c, IPFEM_INVALID, "need 0 < gamma <= 1, 1 < alpha <= 2 and 0 < eta_min <= eta_max < 1");
+    c->inner.mode = mode;
+    if (mode == 1) {
+        c->inner.gamma = gamma;
+        c->inner.alpha = alpha;
+        c->inner.eta_min = eta_min;
+        c->inner.eta_max = eta_max;
+    }
     return IPFEM_OK;
 }
 

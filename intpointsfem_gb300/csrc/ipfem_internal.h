@@ -203,6 +203,13 @@ struct NewtonState {
     double r0 = 0.0, rn = 0.0;
     double alpha = 1.0;           // modified-Thomas acceleration factor of the open load step
     int have_k = 0;               // a tangent has been assembled since newton_begin
+    double eta = 0.0;             // inner tolerance of the last solve of the open load step
+    double rn_prev = 0.0;         // |R| before the last Newton iteration
+};
+// adaptive inner tolerance (ipfem_set_inner_tolerance)
+struct InnerTolerance {
+    int mode = 0;
+    double gamma = 0.9, alpha = 2.0, eta_min = 1e-5, eta_max = 0.1;
 };
 
 namespace ipfem {
@@ -288,6 +295,7 @@ struct ipfem_ctx {
     int res32 = 0;                       // FP32 residual evaluations in IPFEM_MIXED (ipfem_set_residual_precision)
     int res32_active = 0;                // the residuals being evaluated now are FP32
     double res32_switch = 1e-5;          // |R| / |R0| below which a load step refines with FP64 residuals
+    InnerTolerance inner;                // inner tolerance of the Newton iterations
 };
 
 // ---- kernel launchers (implemented in the .cu files) ----

@@ -159,3 +159,48 @@ def test_fp32_residual_newton_refines_to_fp64_accuracy(tmp_path):
           "u %.2e sigma %.2e" % (floor, n32, sg.newton_iters, so.newton_iters, eu, es))
     assert eu < 1e-6 and es < 1e-6
     assert floor > 1e-9                      # the FP32 residual cannot reach the 1e-8 target on its own
+
+
+def test_adaptive_inner_tolerance(tmp_path):
+    """ipfem_set_inner_tolerance: bad arguments are refused; on 40 x 40 with
+    the learned-free mixed solve, every Newton iteration's inner tolerance
+    (recorded in the iteration log) follows the forcing-term rule from the
+    residuals before it, and the solution stays within 1e-6 of the FP64 oracle"""
+    import json
+
+    sm, P = _pair(40)
+    sm.set_precision(ip.MIXED)
+    for bad in [dict(mode=2), dict(mode=1, gamma=0.0), dict(mode=1, alpha=2.5), dict(mode=1, eta_min=0.5, eta_max=0.1),
+                dict(mode=1, eta_max=1.0)]:
+        with pytest.raises(ip.IpfemError):
+            sm.set_inner_tolerance(**bad)
+    g, a, lo, hi, first, tol = 0.9, 2.0, 1e-4, 0.3, 3e-2, 1e-8
+    sm.set_inner_tolerance(1, g, a, lo, hi)
+    log = str(tmp_path / "it.jsonl")
+    sm.set_iteration_log(log)
+    ug, uo = np.zeros(sm.neq), np.zeros(sm.neq)
+    sg, _ = sm.newton(ug, 10, newton_max_it=40, newton_rtol=tol, cg_rtol=first)
+    so, _ = P.solve_steps(uo, 10, newton_max_it=40)
+    assert sg.converged
+    recs = [json.loads(line) for line in open(log) if '"iter"' in line]
+    checked = 0
+    for step in sorted({r["step"] for r in recs}):
+        rows = [r for r in recs if r["step"] == step]
+        r0 = rows[0]["res"] / rows[0]["res_rel"]
+        res = [r0] + [r["res"] for r in rows]          # |R| before iteration k is res[k - 1]
+        assert rows[0]["cg_rtol"] == pytest.approx(first, rel=1e-6)
+        for k in range(1, len(rows)):
+            eta = g * (res[k] / res[k - 1]) ** a
+            carry = g * rows[k - 1]["cg_rtol"] ** a
+            if carry > 0.1:
+                eta = max(eta, carry)
+            eta = min(max(eta, 0.5 * tol * r0 / res[k], lo), hi)
+            assert rows[k]["cg_rtol"] == pytest.approx(eta, rel=1e-5), (step, k)
+            checked += 1
+    assert checked > 10
+    eu = np.abs(ug - uo).max() / np.abs(uo).max()
+    sig, sigo = sm.get_state(1), _soa4(P.arr("sigma"), P.n_ip)
+    es = np.abs(sig - sigo).max() / np.abs(sigo).max()
+    print("adaptive inner tolerance: %d Newton / %d CG iterations (FP64 oracle %d Newton); u %.2e sigma %.2e"
+          % (sg.newton_iters, sg.cg_iters, so.newton_iters, eu, es))
+    assert eu < 1e-6 and es < 1e-6
