@@ -485,7 +485,10 @@ __global__ void __launch_bounds__(256, 8) k_fcg_spmv(int32_t n, const int64_t *_
 // (transposes of their stored twins, ascending), then the stored blocks:
 // the full layout's column order, so the same bits.  The stored blocks go
 // through L2 normally, as the rows of the next two grid lines read them again.
-__global__ void __launch_bounds__(256, 8) k_fcg_spmv_sym(int32_t n, const int64_t *__restrict__ slice_base,
+// 6 CTAs per SM: 40 registers and no spill.  Measured per flexible-CG
+// iteration at 400x400 (one box): 8 or 7 CTAs (32 registers, 40 B spilled)
+// 90.5-90.8 us, 6 CTAs 86.0 us, 5 CTAs 87.7 us, 4 CTAs 90.0 us.
+__global__ void __launch_bounds__(256, 6) k_fcg_spmv_sym(int32_t n, const int64_t *__restrict__ slice_base,
                                                       const int32_t *__restrict__ rowlen,
                                                       const uint8_t *__restrict__ pat_id,
                                                       const int32_t *__restrict__ pat_off,
