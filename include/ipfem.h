@@ -205,6 +205,16 @@ ipfem_status ipfem_set_newton_accel(ipfem_ctx *ctx, int mode);
  * tangent of the first assembly after ipfem_newton_begin is kept for every
  * later linear solve, and later assemblies compute the residual only. */
 ipfem_status ipfem_set_newton_tangent(ipfem_ctx *ctx, int mode);
+/* Secant predictor of the load steps (no counterpart in the reference, whose
+ * load steps start from the last accepted solution): with on = 1 each load
+ * step after the first of a newton_begin run starts from
+ *   u_s = u_{s-1} + (u_{s-1} - u_{s-2})
+ * (equal load increments), the solutions of the two previous accepted steps.
+ * The step's convergence target stays newton_rtol times |R| at u_{s-1} (one
+ * more residual evaluation per step), so the accepted solutions meet the
+ * same residual bound as without the predictor.  Off by default: the plain
+ * method then follows the reference's iterates bit for bit. */
+ipfem_status ipfem_set_newton_predictor(ipfem_ctx *ctx, int on);
 /* Inner tolerance of the Newton iterations (no counterpart in the reference,
  * whose solve is to a fixed tolerance).  mode 0 (default): every linear
  * solve to opts.cg_rtol.  mode 1: an adaptive forcing term (Eisenstat and

@@ -30,6 +30,21 @@ MLP_PARAMS = 23316
 CHOSEN_CG_RTOL = 3e-2
 CHOSEN_INNER = dict(mode=1, gamma=0.9, alpha=2.0, eta_min=1e-4, eta_max=0.3)
 FIXED_CG_RTOL = 3e-3       # the best fixed inner tolerance (mode 0)
+# The chosen method also starts each load step from the secant prediction
+# (ipfem_set_newton_predictor): the same 400 x 400 solve in 6.2 s (98 Newton,
+# 64 248 CG iterations) instead of 15.1 s, the elastic steps converging in one
+# Newton iteration from a start at ~1e-7 of their residual.
+CHOSEN_PREDICTOR = True
+
+
+def use_chosen_newton(sm):
+    """the chosen method's Newton settings on a struct matrix in IPFEM_MIXED:
+    adaptive inner tolerance (pass CHOSEN_CG_RTOL as cg_rtol) and the secant
+    predictor"""
+    sm.set_inner_tolerance(**CHOSEN_INNER)
+    sm.set_newton_predictor(CHOSEN_PREDICTOR)
+
+
 STATUS = {0: "ok", 1: "not converged", 2: "non-finite value", 3: "CG breakdown", 4: "out of device memory",
           5: "invalid argument", 6: "CUDA error", 7: "no sm_103 device"}
 
@@ -161,6 +176,7 @@ def lib():
             "ipfem_wellbore_free": (None, [C.POINTER(Wellbore)]),
             "ipfem_set_newton_tangent": (S, [P, S]),
             "ipfem_set_inner_tolerance": (S, [P, S, C.c_double, C.c_double, C.c_double, C.c_double]),
+            "ipfem_set_newton_predictor": (S, [P, S]),
             "ipfem_set_row_stencils": (S, [P, S]),
             "ipfem_row_stencil_count": (S, [P, _ip, _ip]),
             "ipfem_layout_info": (S, [P, S, _lp, _lp, _ip]),
@@ -422,6 +438,11 @@ class ElastoPlasticIntPointsStructMatrix:
         choice 2 with Kelley's safeguards), the first solve of a step to cg_rtol"""
         self._check(lib().ipfem_set_inner_tolerance(self._ctx, int(mode), float(gamma), float(alpha),
                                                      float(eta_min), float(eta_max)))
+
+    def set_newton_predictor(self, on):
+        """1: each load step after the first starts from the secant prediction
+        u + (u - u_prev); the convergence target stays |R| at the unpredicted start"""
+        self._check(lib().ipfem_set_newton_predictor(self._ctx, int(bool(on))))
 
     def set_row_stencils(self, on):
         """1 (default): SpMVs form block columns from row stencils where the

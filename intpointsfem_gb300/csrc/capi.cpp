@@ -101,7 +101,7 @@ void free_all(ipfem_ctx *c)
                     c->d_fixed, c->d_K,
                     c->d_dinv, c->d_eps_p, c->d_sigma, c->d_alpha, c->d_mtype, c->d_u, c->d_rhs, c->d_strain,
                     c->d_sigma_w, c->d_dep, c->d_fe, c->d_x, c->d_r, c->d_z, c->d_p, c->d_q, c->d_b, c->d_part,
-                    c->d_sc, c->d_counters, c->d_dotres, c->d_err, c->d_acc, c->d_binv};
+                    c->d_sc, c->d_counters, c->d_dotres, c->d_err, c->d_acc, c->d_binv, c->d_u_prev};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     {
@@ -815,20 +815,39 @@ static ipfem_status newton_advance(ipfem_ctx *c, int32_t n_iters, double *du, ip
             set_load(c, (double)(ns.step + 1) / (double)o.n_steps);
             c->res32_active = c->res32 && c->precision == IPFEM_MIXED;
             cudaEventRecord(ev[0], c->stream);
+            double r0sq = -1.0;
+            if (c->predictor) {
+                // the step's convergence target is |R| at the last accepted
+                // solution, as without the predictor; then the secant
+                // predictor (equal load increments) moves u by the last step's
+                // displacement increment before the first assembly
+                if (ns.have_prev) {
+                    residual_device(c, du, c->d_rhs, 0);
+                    ipfem_status e = dot_host(c, c->d_rhs, c->d_rhs, &r0sq);
+                    if (e != IPFEM_OK) return e;
+                    launch_predict(c, du, c->d_u_prev, 1.0);
+                } else {
+                    CK(cudaMemcpyAsync(c->d_u_prev, du, (size_t)c->s.neq * sizeof(double), cudaMemcpyDeviceToDevice,
+                                       c->stream));
+                }
+                c->launches += 1;
+            }
             newton_assemble(c, du);
             cudaEventRecord(ev[1], c->stream);
-            double r0sq = 0;
-            ipfem_status e = dot_host(c, c->d_rhs, c->d_rhs, &r0sq);
+            double rsq = 0;
+            ipfem_status e = dot_host(c, c->d_rhs, c->d_rhs, &rsq);
             st->ms_assemble += elapsed();
             if (e != IPFEM_OK) return e;
-            ns.r0 = std::sqrt(r0sq);
-            ns.rn = ns.r0;
+            ns.r0 = std::sqrt(r0sq >= 0.0 ? r0sq : rsq);
+            ns.rn = std::sqrt(rsq);
+            ns.r_pred = ns.rn;
             ns.it = 0;
             ns.alpha = 1.0;
             ns.open = 1;
-            if (!std::isfinite(ns.r0)) return fail(c, IPFEM_NAN, "residual is not finite");
+            if (!std::isfinite(ns.r0) || !std::isfinite(ns.rn)) return fail(c, IPFEM_NAN, "residual is not finite");
         }
-        bool conv = (ns.r0 == 0.0);
+        // a predicted start may already meet the step's target
+        bool conv = (ns.r0 == 0.0) || (!c->res32_active && ns.rn <= o.newton_rtol * ns.r0);
         if (!conv) {
             // inner tolerance of this Newton iteration
             double eta = o.cg_rtol;
@@ -950,17 +969,32 @@ static ipfem_status newton_advance(ipfem_ctx *c, int32_t n_iters, double *du, ip
             if (c->iter_log) {
                 std::fprintf(c->iter_log,
                              "{\"step\": %d, \"accepted\": true, \"newton_iters\": %d, \"converged\": %s, "
-                             "\"res_rel\": %.17g, \"ms_commit\": %.6f, \"ms_step_total\": %.6f}\n",
+                             "\"res_rel\": %.17g, \"res_start_rel\": %.17g, \"ms_commit\": %.6f, "
+                             "\"ms_step_total\": %.6f}\n",
                              ns.step, ns.it, conv ? "true" : "false", ns.r0 > 0.0 ? ns.rn / ns.r0 : 0.0,
+                             ns.r0 > 0.0 ? ns.r_pred / ns.r0 : 0.0,
                              st->ms_commit - mc0,
                              (st->ms_assemble - ma0) + (st->ms_solve - ms0) + (st->ms_commit - mc0));
                 std::fflush(c->iter_log);
             }
             ns.step++;
             ns.open = 0;
+            ns.have_prev = c->predictor;   // d_u_prev holds the start of the step just accepted
         }
     }
     st->converged = ns.all_converged;
+    return IPFEM_OK;
+}
+
+ipfem_status ipfem_set_newton_predictor(ipfem_ctx *c, int on)
+{
+    if (!c || (on != 0 && on != 1)) return fail(c, IPFEM_INVALID, "predictor must be 0 or 1");
+    if (on && !c->d_u_prev) {
+        const cudaError_t e = dalloc(&c->d_u_prev, (size_t)c->s.neq);
+        if (e != cudaSuccess) return fail(c, IPFEM_OOM, "allocation of the predictor vector failed");
+    }
+    c->predictor = on;
+    c->ns.have_prev = 0;   // the next load step starts unpredicted
     return IPFEM_OK;
 }
 

@@ -205,6 +205,8 @@ struct NewtonState {
     int have_k = 0;               // a tangent has been assembled since newton_begin
     double eta = 0.0;             // inner tolerance of the last solve of the open load step
     double rn_prev = 0.0;         // |R| before the last Newton iteration
+    int have_prev = 0;            // d_u_prev holds the solution of the previous accepted load step
+    double r_pred = 0.0;          // |R| at the predicted start of the open load step
 };
 // adaptive inner tolerance (ipfem_set_inner_tolerance)
 struct InnerTolerance {
@@ -296,6 +298,8 @@ struct ipfem_ctx {
     int res32_active = 0;                // the residuals being evaluated now are FP32
     double res32_switch = 1e-5;          // |R| / |R0| below which a load step refines with FP64 residuals
     InnerTolerance inner;                // inner tolerance of the Newton iterations
+    int predictor = 0;                   // secant predictor at the start of each load step
+    double *d_u_prev = nullptr;          // [neq] solution of the previous accepted load step (predictor)
 };
 
 // ---- kernel launchers (implemented in the .cu files) ----
@@ -343,6 +347,8 @@ void launch_cg_iteration(ipfem_ctx *c);
 void launch_cg_spmv_only(ipfem_ctx *c);
 void launch_dot(ipfem_ctx *c, const double *a, const double *b, double *d_out);
 void launch_axpy_u(ipfem_ctx *c, double *d_u, const double *d_du);
+// u <- u + ratio (u - u_prev), u_prev <- the old u
+void launch_predict(ipfem_ctx *c, double *d_u, double *d_u_prev, double ratio);
 void launch_scale_add(ipfem_ctx *c, double *d_u, const double *d_x, double alpha, double *d_t);
 void launch_fp64_probe(ipfem_ctx *c, double *d_out, int grid, int iters);
 void launch_stiffness32(ipfem_ctx *c);

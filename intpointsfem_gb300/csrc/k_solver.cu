@@ -527,6 +527,17 @@ __global__ void k_add(int64_t n, double *__restrict__ u, const double *__restric
     if (i < n) u[i] = u[i] + du[i];
 }
 
+// secant predictor of a load step: u <- u + ratio (u - u_prev), u_prev <- the old u
+__global__ void k_predict(int64_t n, double *__restrict__ u, double *__restrict__ u_prev, double ratio)
+{
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i < n) {
+        const double ui = u[i];
+        u[i] = fma(ratio, ui - u_prev[i], ui);
+        u_prev[i] = ui;
+    }
+}
+
 // FP64 FMA issue-rate probe: 8 independent fma chains per thread, bounded loop
 __global__ void __launch_bounds__(256) k_fp64_probe(double *out, int iters, double a, double b)
 {
@@ -677,6 +688,12 @@ void launch_axpy_u(ipfem_ctx *c, double *d_u, const double *d_du)
 {
     const int64_t n = c->s.neq;
     k_add<<<(unsigned)((n + 255) / 256), 256, 0, c->stream>>>(n, d_u, d_du);
+}
+
+void launch_predict(ipfem_ctx *c, double *d_u, double *d_u_prev, double ratio)
+{
+    const int64_t n = c->s.neq;
+    k_predict<<<(unsigned)((n + 255) / 256), 256, 0, c->stream>>>(n, d_u, d_u_prev, ratio);
 }
 
 // ---------------------------------------------------------------------------

@@ -204,3 +204,45 @@ def test_adaptive_inner_tolerance(tmp_path):
     print("adaptive inner tolerance: %d Newton / %d CG iterations (FP64 oracle %d Newton); u %.2e sigma %.2e"
           % (sg.newton_iters, sg.cg_iters, so.newton_iters, eu, es))
     assert eu < 1e-6 and es < 1e-6
+
+
+def test_secant_predictor(tmp_path):
+    """ipfem_set_newton_predictor on 40 x 40, mixed precision: every load step
+    after the first starts from u + (u - u_prev) (the log's res_start_rel is
+    |R| there relative to |R| at the unpredicted start: far below 1 where the
+    response is smooth, near 1 where the plastic zone grows), the steps
+    converge to the same target in fewer Newton iterations in all, and the
+    solution stays within 1e-6 of the FP64 oracle; bad arguments are refused"""
+    import json
+
+    sm, P = _pair(40)
+    sm.set_precision(ip.MIXED)
+    with pytest.raises(ip.IpfemError):
+        sm._check(ip.lib().ipfem_set_newton_predictor(sm._ctx, 2))
+    res = {}
+    for pred in (0, 1):
+        sm.set_newton_predictor(pred)
+        log = str(tmp_path / ("it%d.jsonl" % pred))
+        sm.set_iteration_log(log)
+        u = np.zeros(sm.neq)
+        st, _ = sm.newton(u, 10, newton_max_it=40, cg_rtol=1e-4)
+        sm.set_iteration_log(None)
+        steps = [json.loads(line) for line in open(log) if '"accepted"' in line]
+        assert st.converged and all(r["converged"] for r in steps) and len(steps) == 10
+        res[pred] = (u.copy(), st.newton_iters, steps, sm.get_state(1))
+        # a fresh state for the second run
+        sm = ip.ElastoPlasticIntPointsStructMatrix(ip.WellboreMesh(ip.wellbore_params(40)))
+        sm.set_precision(ip.MIXED)
+    uo = np.zeros(P.neq)
+    P.solve_steps(uo, 10, newton_max_it=40)
+    u1, n1, steps1, sig1 = res[1]
+    assert res[0][1] > n1
+    starts = [r["res_start_rel"] for r in steps1]
+    print("predicted start |R| / |R0| per load step:", " ".join("%.1e" % v for v in starts))
+    assert starts[0] == pytest.approx(1.0)                         # no prediction for the first step
+    assert min(starts[1:]) < 1e-2                                  # where the response is smooth
+    eu = np.abs(u1 - uo).max() / np.abs(uo).max()
+    sigo = _soa4(P.arr("sigma"), P.n_ip)
+    es = np.abs(sig1 - sigo).max() / np.abs(sigo).max()
+    print("secant predictor: %d Newton iterations (without: %d); u %.2e sigma %.2e" % (n1, res[0][1], eu, es))
+    assert eu < 1e-6 and es < 1e-6

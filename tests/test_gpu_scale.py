@@ -208,7 +208,7 @@ def _solve(w, n, mode, n_steps, step_end, learned=False):
         rtol = 1e-8
     else:
         sm.set_precision(ip.MIXED)
-        sm.set_inner_tolerance(**ip.CHOSEN_INNER)
+        ip.use_chosen_newton(sm)
         rtol = ip.CHOSEN_CG_RTOL
         if learned:
             from intpointsfem_gb300 import train_preconditioner as tp
