@@ -193,7 +193,10 @@ ipfem_status ipfem_newton_solve(ipfem_ctx *ctx, const ipfem_solve_opts *opts, in
  * at u, a second solve with the same tangent for du~, alpha += (alpha du .
  * du~) / (alpha du . alpha du), u += du~; alpha starts at 1 in every load
  * step.  Convergence is still judged on |R| / |R0| after the tangent
- * assembly at the new u. */
+ * assembly at the new u.  Refused while the adaptive inner tolerance is on
+ * (ipfem_set_inner_tolerance mode 1): with inner solves stopped at up to
+ * eta_max the step factor is wrong and the iteration diverged in a measured
+ * plastic step. */
 ipfem_status ipfem_set_newton_accel(ipfem_ctx *ctx, int mode);
 
 /* Tangent of the Newton iteration: 0 = Assemble(K, rhs) at every iteration

@@ -607,6 +607,9 @@ ipfem_status ipfem_assemble_residual(ipfem_ctx *c, const double *u, double *rhs,
 ipfem_status ipfem_set_newton_accel(ipfem_ctx *c, int mode)
 {
     if (!c || (mode != 0 && mode != 1)) return fail(c, IPFEM_INVALID, "bad Newton acceleration mode");
+    if (mode == 1 && c->inner.mode == 1)
+        return fail(c, IPFEM_INVALID, "the modified-Thomas acceleration needs a fixed inner tolerance (its step "
+                                      "factor assumes accurate inner solves)");
     if (mode == 1 && !c->d_acc) {
         cudaError_t e = dalloc(&c->d_acc, (size_t)c->s.neq);
         if (e != cudaSuccess) return fail(c, IPFEM_OOM, "allocation of the acceleration vector failed");
@@ -1003,6 +1006,9 @@ ipfem_status ipfem_set_inner_tolerance(ipfem_ctx *c, int mode, double gamma, dou
 {
     if (!c) return IPFEM_INVALID;
     if (mode != 0 && mode != 1) return fail(c, IPFEM_INVALID, "inner tolerance mode must be 0 or 1");
+    if (mode == 1 && c->newton_accel)
+        return fail(c, IPFEM_INVALID, "the adaptive inner tolerance cannot be combined with the modified-Thomas "
+                                      "acceleration (its step factor assumes accurate inner solves)");
     if (mode == 1 && !(gamma > 0.0 && gamma <= 1.0 && alpha > 1.0 && alpha <= 2.0 && eta_min > 0.0 &&
                        eta_min <= eta_max && eta_max < 1.0))
         return fail(c, IPFEM_INVALID, "need 0 < gamma <= 1, 1 < alpha <= 2 and 0 < eta_min <= eta_max < 1");

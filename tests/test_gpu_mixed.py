@@ -176,6 +176,8 @@ def test_adaptive_inner_tolerance(tmp_path):
             sm.set_inner_tolerance(**bad)
     g, a, lo, hi, first, tol = 0.9, 2.0, 1e-4, 0.3, 3e-2, 1e-8
     sm.set_inner_tolerance(1, g, a, lo, hi)
+    with pytest.raises(ip.IpfemError):                # the acceleration assumes accurate inner solves
+        sm.set_newton_accel(1)
     log = str(tmp_path / "it.jsonl")
     sm.set_iteration_log(log)
     ug, uo = np.zeros(sm.neq), np.zeros(sm.neq)
