@@ -226,7 +226,9 @@ ipfem_status ipfem_set_newton_predictor(ipfem_ctx *ctx, int on);
  * step to opts.cg_rtol, then
  *   eta_k = gamma (|R_k| / |R_k-1|)^alpha, at least gamma eta_k-1^alpha when
  *   that is above 0.1, at least 0.5 newton_rtol |R0| / |R_k| (no solve
- *   beyond what convergence needs), clamped to [eta_min, eta_max].
+ *   beyond what convergence needs), clamped to [eta_min, eta_max];
+ *   eta_k = eta_min after an iteration that reduced |R| by less than a
+ *   factor 0.9 (stagnation: the rule alone would loosen the solve there).
  * The inner solves stop at relative residual eta_k, so no solve is tighter
  * than the Newton contraction it serves (slow where the tangent is
  * inconsistent).  Eisenstat and Walker suggest gamma 0.9, alpha 2 or

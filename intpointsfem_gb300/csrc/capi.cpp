@@ -856,11 +856,18 @@ static ipfem_status newton_advance(ipfem_ctx *c, int32_t n_iters, double *du, ip
             double eta = o.cg_rtol;
             if (c->inner.mode == 1 && ns.it > 0) {
                 const InnerTolerance &t = c->inner;
-                eta = t.gamma * std::pow(ns.rn / ns.rn_prev, t.alpha);
-                const double carry = t.gamma * std::pow(ns.eta, t.alpha);
-                if (carry > 0.1) eta = std::max(eta, carry);
-                eta = std::max(eta, 0.5 * o.newton_rtol * ns.r0 / ns.rn);
-                eta = std::min(std::max(eta, t.eta_min), t.eta_max);
+                const double ratio = ns.rn / ns.rn_prev;
+                if (ratio > 0.9) {
+                    // stagnating or growing |R|: the forcing term would loosen
+                    // the solve just when the Newton step needs to be accurate
+                    eta = t.eta_min;
+                } else {
+                    eta = t.gamma * std::pow(ratio, t.alpha);
+                    const double carry = t.gamma * std::pow(ns.eta, t.alpha);
+                    if (carry > 0.1) eta = std::max(eta, carry);
+                    eta = std::max(eta, 0.5 * o.newton_rtol * ns.r0 / ns.rn);
+                    eta = std::min(std::max(eta, t.eta_min), t.eta_max);
+                }
             }
             ns.eta = eta;
             int k = 0;
