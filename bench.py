@@ -373,7 +373,9 @@ def run_gpu(args):
     clk = clocks.stop()
     ms_timed = e0.elapsed_time(e1)
     launches = A.launch_count - l0
-    ms_dev = reduce_max(ms_timed / args.steps, dist)
+    # per Newton iteration actually run (a short solve can end inside the window)
+    n_timed = max(1, st.newton_iters)
+    ms_dev = reduce_max(ms_timed / n_timed, dist)
     cg_per_iter = st.cg_iters / max(1, st.newton_iters)
     solve_plain = None
     if args.solve:
@@ -400,9 +402,10 @@ def run_gpu(args):
             dist.barrier()
         torch.cuda.synchronize()
         t0 = time.perf_counter()
+        n_e2e = 0
         for _ in range(args.steps):
-            B.newton_advance(hu, 1, ip.HOST)
-        ms_e2e = 1e3 * (time.perf_counter() - t0) / args.steps
+            n_e2e += B.newton_advance(hu, 1, ip.HOST)[0].newton_iters
+        ms_e2e = 1e3 * (time.perf_counter() - t0) / max(1, n_e2e)
         B.close()
 
     # the chosen method (mixed precision + learned preconditioner) and mixed
@@ -431,10 +434,11 @@ def run_gpu(args):
             pw = timed_advance(C_, sc_, uc, args.warmup, e0, e1)
             l0c = C_.launch_count
             stc, msc = timed_advance(C_, sc_, uc, args.steps, e0, e1)
-            out = {"ms_per_newton_iter": msc / args.steps,
+            nc = max(1, stc.newton_iters)
+            out = {"ms_per_newton_iter": msc / nc,
                    "cg_iters_per_newton": stc.cg_iters / max(1, stc.newton_iters),
                    "newton_iters_timed": stc.newton_iters, "fcg_fallbacks": stc.fcg_fallbacks,
-                   "ms_cg_per_newton": stc.ms_solve / args.steps, "gpu_launches": C_.launch_count - l0c}
+                   "ms_cg_per_newton": stc.ms_solve / nc, "gpu_launches": C_.launch_count - l0c}
             if to_end:
                 pr = timed_advance(C_, sc_, uc, 0, e0, e1)
                 out["solve"] = solve_record([pw, (stc, msc), pr], N_STEPS)
@@ -509,8 +513,8 @@ def run_gpu(args):
         "residual_kernels": res_kernels,
         "cg_iters_per_newton": cg_per_iter,
         "newton_iters_timed": st.newton_iters,
-        "ms_breakdown": {"assemble": st.ms_assemble / args.steps, "cg": st.ms_solve / args.steps,
-                         "commit": st.ms_commit / args.steps},
+        "ms_breakdown": {"assemble": st.ms_assemble / n_timed, "cg": st.ms_solve / n_timed,
+                         "commit": st.ms_commit / n_timed},
         "e2e": ({"value": ms_e2e, "unit": UNIT, "h2d_bytes_per_step": 8 * A.neq, "d2h_bytes_per_step": 8 * A.neq,
                  "how": "one ipfem_newton_advance(u, 1, IPFEM_HOST) call per step: u (8 B x neq) copied H2D "
                         "and D2H inside every timed step"}
