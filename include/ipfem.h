@@ -208,6 +208,19 @@ ipfem_status ipfem_set_newton_accel(ipfem_ctx *ctx, int mode);
  * tangent of the first assembly after ipfem_newton_begin is kept for every
  * later linear solve, and later assemblies compute the residual only. */
 ipfem_status ipfem_set_newton_tangent(ipfem_ctx *ctx, int mode);
+/* Tangent operator of the assemblies: 0 (default) the reference's
+ * TangentOperator (FunctionsTangentOperator.h:37-123), bit-identical to it;
+ * 1 the consistent spectral tangent, which differs in two places: the spin
+ * factor of each eigen-pair (s_i - s_j) / (e_i - e_j) takes the projected
+ * principal stresses instead of the trial ones, and each pair's ProdT terms
+ * start from zero instead of accumulating over the pairs.  It matches finite
+ * differences of the residual in plastic states (the reference's tangent is
+ * off by about 1e-2 there) and Newton then converges at its quadratic rate:
+ * on the oracle, 45 -> 27 Newton iterations for the 40 x 40 ramp and
+ * 108 -> 56 for 80 x 80, the same solution to 1e-10.  The residual and the
+ * accepted solutions are unchanged; only the iteration differs from the
+ * reference's. */
+ipfem_status ipfem_set_consistent_tangent(ipfem_ctx *ctx, int on);
 /* Secant predictor of the load steps (no counterpart in the reference, whose
  * load steps start from the last accepted solution): with on = 1 each load
  * step after the first of a newton_begin run starts from

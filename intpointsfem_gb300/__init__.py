@@ -177,6 +177,7 @@ def lib():
             "ipfem_set_newton_tangent": (S, [P, S]),
             "ipfem_set_inner_tolerance": (S, [P, S, C.c_double, C.c_double, C.c_double, C.c_double]),
             "ipfem_set_newton_predictor": (S, [P, S]),
+            "ipfem_set_consistent_tangent": (S, [P, S]),
             "ipfem_set_row_stencils": (S, [P, S]),
             "ipfem_row_stencil_count": (S, [P, _ip, _ip]),
             "ipfem_layout_info": (S, [P, S, _lp, _lp, _ip]),
@@ -438,6 +439,11 @@ class ElastoPlasticIntPointsStructMatrix:
         choice 2 with Kelley's safeguards), the first solve of a step to cg_rtol"""
         self._check(lib().ipfem_set_inner_tolerance(self._ctx, int(mode), float(gamma), float(alpha),
                                                      float(eta_min), float(eta_max)))
+
+    def set_consistent_tangent(self, on):
+        """1: the consistent spectral tangent (spin factors from the projected
+        principal stresses); 0 (default): the reference's TangentOperator"""
+        self._check(lib().ipfem_set_consistent_tangent(self._ctx, int(bool(on))))
 
     def set_newton_predictor(self, on):
         """1: each load step after the first starts from the secant prediction

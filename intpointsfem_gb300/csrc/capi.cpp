@@ -996,6 +996,14 @@ static ipfem_status newton_advance(ipfem_ctx *c, int32_t n_iters, double *du, ip
     return IPFEM_OK;
 }
 
+ipfem_status ipfem_set_consistent_tangent(ipfem_ctx *c, int on)
+{
+    if (!c || (on != 0 && on != 1)) return fail(c, IPFEM_INVALID, "consistent tangent must be 0 or 1");
+    c->consistent_tangent = on;
+    c->tangent_valid = false;   // the next solve needs a tangent of the chosen kind
+    return IPFEM_OK;
+}
+
 ipfem_status ipfem_set_newton_predictor(ipfem_ctx *c, int on)
 {
     if (!c || (on != 0 && on != 1)) return fail(c, IPFEM_INVALID, "predictor must be 0 or 1");

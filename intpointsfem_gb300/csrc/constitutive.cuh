@@ -24,6 +24,7 @@ struct ElasticConst {
     double K, G;            // lambda + 2 mu / 3, mu
     double l2m;             // lambda + 2 * mu
     double c1, c2, inv_mu;  // inverse elasticity coefficients of ComputeStrain
+    int consistent;         // 1: consistent spectral tangent (ipfem_set_consistent_tangent)
 };
 
 // ------------------------------------------------ spectral decomposition
@@ -379,9 +380,14 @@ __device__ __forceinline__ int project_sigma(const double ev[3], double sp[3], d
 // TangentOperator (FunctionsTangentOperator.h:37-123) restricted to the
 // entries that TranslateDep keeps (rows and columns XX, XY, YY = Voigt 0, 1, 3),
 // then TranslateDep (FunctionsStressStrain.h:103-119).  Each kept entry is
-// accumulated in the reference's order.
-__device__ __forceinline__ void tangent_dep(const double grad[9], const double sev[3], const double eev[3],
-                                            const double v[9], double G, double lambda, double dep[9])
+// accumulated in the reference's order.  With consistent = 1 the spin factor
+// of each eigen-pair takes the projected principal stresses sp instead of the
+// trial ones and the pair's ProdT terms start from zero: the consistent
+// spectral tangent (the reference's differs from finite differences of its
+// own residual by about 1e-2 in plastic states).
+__device__ __forceinline__ void tangent_dep(const double grad[9], const double sev[3], const double sp[3],
+                                            const double eev[3], const double v[9], double G, double lambda,
+                                            int consistent, double dep[9])
 {
     // Voigt k -> (ki, kj): 0 -> (0,0), 1 -> (0,1), 3 -> (1,1)
     double T[3][3];     // T[l][k] over l, k in {XX, XY, YY}
@@ -418,7 +424,12 @@ __device__ __forceinline__ void tangent_dep(const double grad[9], const double s
         const int i = (pr == 2) ? 1 : 0;
         const int j = (pr == 0) ? 1 : 2;
         const double deps = eev[i] - eev[j];
-        const double dsig = sev[i] - sev[j];
+        const double dsig = consistent ? sp[i] - sp[j] : sev[i] - sev[j];
+        if (consistent) {
+            tm00 = 0;
+            tm01 = 0;
+            tm11 = 0;
+        }
         double factor = 0.;
         if (!((fabs(deps) < 1.e-12) || (deps < 0.0)))
             factor = dsig / deps;
@@ -482,7 +493,7 @@ __device__ __forceinline__ int ip_update(const double eps[3], const double pl[4]
         ee[1] = ee[1] / 2;
         spectral(ee, eev, evec);
         mt = project_sigma<true>(sev, sp, alpha, m, E.K, E.G, grad);
-        tangent_dep(grad, sev, eev, evec, E.G, E.lambda, dep);
+        tangent_dep(grad, sev, sp, eev, evec, E.G, E.lambda, E.consistent, dep);
     } else {
         mt = project_sigma<false>(sev, sp, alpha, m, E.K, E.G, grad);
     }

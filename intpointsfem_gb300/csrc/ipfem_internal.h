@@ -299,6 +299,7 @@ struct ipfem_ctx {
     double res32_switch = 1e-5;          // |R| / |R0| below which a load step refines with FP64 residuals
     InnerTolerance inner;                // inner tolerance of the Newton iterations
     int predictor = 0;                   // secant predictor at the start of each load step
+    int consistent_tangent = 0;          // consistent spectral tangent (ipfem_set_consistent_tangent)
     double *d_u_prev = nullptr;          // [neq] solution of the previous accepted load step (predictor)
 };
 

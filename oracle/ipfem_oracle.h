@@ -68,6 +68,11 @@ void orc_ip_update(const orc_elastic *el, const orc_mc *mc,
                    double sigma6[6], double eps_p6_out[6], double strain6[6],
                    int *mtype, double *alpha);
 
+/* Tangent variant for Newton studies: 0 (default) the reference's
+ * TangentOperator; 1 the consistent spectral tangent (spin factors from the
+ * projected principal stresses, one ProdT pair per eigen-pair).  Global. */
+void orc_set_consistent_tangent(int on);
+
 /* Point update with the full 6x6 tangent (XX XY XZ YY YZ ZZ; row = stress,
  * column = strain), as TPZPlasticStepPV::ApplyStrainComputeSigma's Dep that
  * TRKSolution::RKProcess reads (TRKSolution.cpp:189-191). */

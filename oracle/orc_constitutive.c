@@ -528,8 +528,16 @@ static void project_sigma(const double *ev, double *sp, int *mtype, double *alph
 
 /* ------------------------------------------- FunctionsTangentOperator.h */
 
-/* TangentOperator, FunctionsTangentOperator.h:37-123 (6x6, row l, column k) */
-static void tangent_operator(const double *grad, const double *sev, const double *eev,
+/* Tangent variant for studies of the Newton iteration (the default, 0, is the
+ * reference's arithmetic, which every parity test pins): 1 = the consistent
+ * spectral tangent, with the spin factor of each eigen-pair from the
+ * projected principal stresses and one ProdT pair per eigen-pair. */
+static int g_consistent_tangent = 0;
+void orc_set_consistent_tangent(int on) { g_consistent_tangent = on; }
+
+/* TangentOperator, FunctionsTangentOperator.h:37-123 (6x6, row l, column k);
+ * sp: the projected principal stresses (read by the consistent variant only) */
+static void tangent_operator(const double *grad, const double *sev, const double *sp, const double *eev,
                              const double *evec, double *T, double G, double lambda)
 {
     static const int ki_[6] = {0, 0, 0, 1, 1, 2};
@@ -559,7 +567,9 @@ static void tangent_operator(const double *grad, const double *sev, const double
     for (int i = 0; i < 2; ++i) {
         for (int j = i + 1; j < 3; ++j) {
             double deps = eev[i] - eev[j];
-            double dsig = sev[i] - sev[j];
+            double dsig = g_consistent_tangent ? sp[i] - sp[j] : sev[i] - sev[j];
+            if (g_consistent_tangent)
+                for (int q = 0; q < 9; q++) tempMat[q] = 0;
             double factor = 0.;
             if (!((fabs(deps) < 1.e-12) || (deps < 0.0)))
                 factor = dsig / deps;
@@ -618,7 +628,7 @@ void orc_ip_tangent6(const orc_elastic *el, const orc_mc *mc, const double strai
     ee[1] = ee[1] / 2;
     spectral(ee, eev, evec);
     project_sigma(sev, sp, &mt, &a, mc, K, G, grad, 1);
-    tangent_operator(grad, sev, eev, evec, T36, G, lambda);
+    tangent_operator(grad, sev, sp, eev, evec, T36, G, lambda);
     reconstruct(sp, svec, sig);
     strain_from_stress(sig, ee, mu, lambda);
     plastic_strain(strain, ee, pl);
@@ -655,7 +665,7 @@ void orc_ip_update(const orc_elastic *el, const orc_mc *mc,
         ee[1] = ee[1] / 2;
         spectral(ee, eev, evec);
         project_sigma(sev, sp, &mt, &a, mc, K, G, grad, 1);
-        tangent_operator(grad, sev, eev, evec, T, G, lambda);
+        tangent_operator(grad, sev, sp, eev, evec, T, G, lambda);
         reconstruct(sp, svec, sig);
         strain_from_stress(sig, ee, mu, lambda);
         plastic_strain(strain, ee, pl);

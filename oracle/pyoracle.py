@@ -3,6 +3,7 @@
 Imported by tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg,
 never by the product package.
 """
+import contextlib
 import ctypes as C
 import os
 
@@ -100,6 +101,7 @@ def lib():
                                               _dp, _dp, _dp, C.POINTER(C.c_int), _dp]
         L.orc_compute_sigma_batch.argtypes = [C.c_int64, C.c_int, C.POINTER(Elastic), C.POINTER(MC), _dp,
                                               _dp, _dp, C.c_int, _dp, _dp, _dp, C.POINTER(C.c_int8), _dp]
+        L.orc_set_consistent_tangent.argtypes = [C.c_int]
         L.orc_greedy_coloring.restype = C.c_int32
         L.orc_greedy_coloring.argtypes = [C.c_int32, C.c_int32, _ip, _ip]
         _lib = L
@@ -227,6 +229,18 @@ class OracleProblem:
                               ptr(log), int(log_cap))
         nlog = st.newton_iters
         return st, log[:3 * min(nlog, log_cap)].reshape(-1, 3)
+
+
+@contextlib.contextmanager
+def consistent_tangent():
+    """The oracle's consistent spectral tangent (orc_set_consistent_tangent)
+    for the duration of the block.  The switch is global to the process; the
+    reference's tangent is restored on exit."""
+    lib().orc_set_consistent_tangent(1)
+    try:
+        yield
+    finally:
+        lib().orc_set_consistent_tangent(0)
 
 
 def dot(a, b):

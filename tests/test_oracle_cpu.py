@@ -1,5 +1,7 @@
 """CPU checks of the oracle's assembly and solver (the properties the GPU
 parity tests rely on)."""
+import contextlib
+
 import numpy as np
 import pytest
 
@@ -188,3 +190,36 @@ def test_resumable_newton_equals_solve_steps():
     assert np.array_equal(u1, u2)
     for f in ("eps_p", "sigma", "mtype", "alpha"):
         assert np.array_equal(P1.arr(f), P2.arr(f)), f
+
+
+def _plastic_tangent_fd_error(consistent):
+    """|K v - FD(v)| / |FD(v)| at the first Newton iterate of the last load
+    step of a 20 x 20 ten-step solve, where points have gone plastic"""
+    ctx = po.consistent_tangent() if consistent else contextlib.nullcontext()
+    with ctx:
+        P = po.OracleProblem(po.default_params(20), nthreads=2)
+        u = np.zeros(P.neq)
+        nw = po.OracleNewton(P, 10, newton_max_it=40, cg_rtol=1e-10)
+        while not (nw.step == 9 and nw.open and nw.it >= 1):
+            nw.advance(u, 1)
+        lam = nw._lam()
+        P.assemble(u, lam)
+        rng = np.random.default_rng(1)
+        v = rng.normal(size=P.neq)
+        v[P.arr("fixed").astype(bool)] = 0
+        Kv = P.spmv(v)
+        h = 1e-6 * np.abs(u).max() / np.abs(v).max()
+        fd = -(P.assemble_residual(u + h * v, lam) - P.assemble_residual(u - h * v, lam)) / (2 * h)
+        return np.linalg.norm(Kv - fd) / np.linalg.norm(fd)
+
+
+def test_consistent_tangent_matches_finite_differences_in_plastic_state():
+    """The consistent variant of the oracle's tangent (spin factors from the
+    projected principal stresses) is the derivative of the residual in a
+    plastic state; the reference's TangentOperator is not, and the default
+    switch gives the reference's tangent back."""
+    e_ref = _plastic_tangent_fd_error(False)
+    e_con = _plastic_tangent_fd_error(True)
+    print("tangent vs finite differences: reference %.2e, consistent %.2e" % (e_ref, e_con))
+    assert e_con < 5e-5 and e_ref > 1e-4
+    assert _plastic_tangent_fd_error(False) == e_ref
