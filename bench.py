@@ -322,10 +322,11 @@ def run_gpu(args):
 
     def set_inner(M):
         # the mixed methods' Newton settings: inner tolerance (adaptive forcing
-        # term or fixed) and the secant predictor of the load steps
+        # term or fixed), the secant predictor of the load steps and the tangent
         if args.inner == "adaptive":
             M.set_inner_tolerance(**ip.CHOSEN_INNER)
         M.set_newton_predictor(args.predictor == "on")
+        M.set_consistent_tangent(args.tangent == "consistent")
 
     A = ip.ElastoPlasticIntPointsStructMatrix(wb)         # device-resident arm
     if mixed:
@@ -456,6 +457,8 @@ def run_gpu(args):
                  if args.inner == "adaptive" else "inner tolerance %g" % args.mixed_cg_rtol)
         if args.predictor == "on":
             inner += ", secant predictor of the load steps"
+        if args.tangent == "consistent":
+            inner += ", consistent spectral tangent"
         chosen["method"] = ("mixed + learned: FP32 tangent, flexible CG preconditioned by the learned "
                             "triangular factor (weights shipped in intpointsfem_gb300/weights), %s, FP64 residual/"
                             "return mapping/Newton refinement" % inner)
@@ -464,8 +467,8 @@ def run_gpu(args):
             "Jacobi-CG" if args.jacobi else "block-Jacobi CG", inner)
         chosen["speedup_vs_plain"] = ms_dev / chosen["ms_per_newton_iter"]
         chosen["note"] = ("the chosen method's Newton iterations are not the plain method's (secant predictor, "
-                          "inexact inner solves): its per-iteration ratio compares different work; the time to "
-                          "solution (solve_speedup_vs_plain) is the like-for-like comparison")
+                          "inexact inner solves, consistent tangent): its per-iteration ratio compares different "
+                          "work; the time to solution (solve_speedup_vs_plain) is the like-for-like comparison")
         if solve_plain and "solve" in chosen:
             chosen["solve_speedup_vs_plain"] = solve_plain["ms"] / chosen["solve"]["ms"]
 
@@ -574,6 +577,9 @@ def main():
     ap.add_argument("--predictor", default="on", choices=["on", "off"],
                     help="secant predictor at the start of each load step of the mixed methods (the chosen "
                          "method's setting: on)")
+    ap.add_argument("--tangent", default="consistent", choices=["consistent", "reference"],
+                    help="tangent of the mixed methods: the consistent spectral tangent (the chosen method's "
+                         "setting) or the reference's TangentOperator; the plain method keeps the reference's")
     ap.add_argument("--no-chosen", dest="chosen", action="store_false")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--residual32", action="store_true",

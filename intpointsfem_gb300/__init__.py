@@ -35,14 +35,20 @@ FIXED_CG_RTOL = 3e-3       # the best fixed inner tolerance (mode 0)
 # 64 248 CG iterations) instead of 15.1 s, the elastic steps converging in one
 # Newton iteration from a start at ~1e-7 of their residual.
 CHOSEN_PREDICTOR = True
+# ... and assembles the consistent spectral tangent (ipfem_set_consistent_tangent):
+# 400 x 400 in 4.95 s (51 Newton, 52 816 CG iterations) instead of 6.41 s (95,
+# 67 547), u within 8e-11 and sigma within 1.5e-10 of the solve with the
+# reference's tangent.  The plain FP64 method keeps the reference's tangent.
+CHOSEN_CONSISTENT_TANGENT = True
 
 
 def use_chosen_newton(sm):
     """the chosen method's Newton settings on a struct matrix in IPFEM_MIXED:
-    adaptive inner tolerance (pass CHOSEN_CG_RTOL as cg_rtol) and the secant
-    predictor"""
+    adaptive inner tolerance (pass CHOSEN_CG_RTOL as cg_rtol), the secant
+    predictor and the consistent tangent"""
     sm.set_inner_tolerance(**CHOSEN_INNER)
     sm.set_newton_predictor(CHOSEN_PREDICTOR)
+    sm.set_consistent_tangent(CHOSEN_CONSISTENT_TANGENT)
 
 
 STATUS = {0: "ok", 1: "not converged", 2: "non-finite value", 3: "CG breakdown", 4: "out of device memory",

@@ -251,3 +251,40 @@ def test_secant_predictor(tmp_path):
     es = np.abs(sig1 - sigo).max() / np.abs(sigo).max()
     print("secant predictor: %d Newton iterations (without: %d); u %.2e sigma %.2e" % (n1, res[0][1], eu, es))
     assert eu < 1e-6 and es < 1e-6
+
+
+def test_chosen_settings_consistent_tangent():
+    """use_chosen_newton on 40 x 40 with the learned preconditioner: adaptive
+    inner tolerance, secant predictor and the consistent tangent.  With the
+    consistent tangent the ten load steps converge in fewer Newton iterations
+    than with the reference's tangent, and both solutions stay within 1e-6 of
+    the FP64 oracle (u, sigma), with at most two flipped return-mapping flags."""
+    from intpointsfem_gb300 import train_preconditioner as tp
+    n = 40
+    P = _pair(n)[1]
+    uo = np.zeros(P.neq)
+    P.solve_steps(uo, 10, newton_max_it=40)
+    sigo = _soa4(P.arr("sigma"), P.n_ip)
+    newton = {}
+    for consistent in (False, True):
+        sm = _pair(n)[0]
+        sm.set_precision(ip.MIXED)
+        sm.set_node_grid(2 * n + 1, 2 * n + 1)
+        sm.mlp_init(0)
+        sm.set_mlp_params(tp.load_weights())
+        sm.set_preconditioner(ip.PREC_MLP)
+        ip.use_chosen_newton(sm)
+        assert ip.CHOSEN_CONSISTENT_TANGENT
+        sm.set_consistent_tangent(consistent)
+        u = np.zeros(sm.neq)
+        st, _ = sm.newton(u, 10, newton_max_it=40, cg_rtol=ip.CHOSEN_CG_RTOL)
+        assert st.converged
+        eu = np.abs(u - uo).max() / np.abs(uo).max()
+        es = np.abs(sm.get_state(1) - sigo).max() / np.abs(sigo).max()
+        flips = int((sm.get_state(3) != P.arr("mtype")).sum())
+        print("chosen settings, %s tangent: Newton %d, CG %d; u %.2e sigma %.2e flips %d"
+              % ("consistent" if consistent else "reference", st.newton_iters, st.cg_iters, eu, es, flips))
+        assert eu < 1e-6 and es < 1e-6 and flips <= 2
+        newton[consistent] = st.newton_iters
+        sm.close()
+    assert newton[True] < newton[False]

@@ -192,5 +192,6 @@ def test_consistent_tangent_bit_exact():
     assert sg.newton_iters == so.newton_iters and sg.cg_iters == so.cg_iters
     assert _eq(lg, lo) and _eq(ug, uo)
     assert _eq(sm2.get_state(1), _soa4(P2.arr("sigma"), P2.n_ip))
-    print("consistent tangent: %d Newton iterations, %d CG iterations" % (sg.newton_iters, sg.cg_iters))
+    print("consistent tangent: %d Newton iterations, %d CG iterations"
+          % (sg.newton_iters, sg.cg_iters))
     assert sg.newton_iters < 45
