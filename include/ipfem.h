@@ -215,11 +215,12 @@ ipfem_status ipfem_set_newton_tangent(ipfem_ctx *ctx, int mode);
  * principal stresses instead of the trial ones, and each pair's ProdT terms
  * start from zero instead of accumulating over the pairs.  It matches finite
  * differences of the residual in plastic states (the reference's tangent is
- * off by about 1e-2 there) and Newton then converges at its quadratic rate:
- * on the oracle, 45 -> 27 Newton iterations for the 40 x 40 ramp and
- * 108 -> 56 for 80 x 80, the same solution to 1e-10.  The residual and the
- * accepted solutions are unchanged; only the iteration differs from the
- * reference's. */
+ * off by 1e-3 to 1e-2 there) and Newton then converges at its quadratic rate:
+ * 45 -> 27 Newton iterations for the plain 40 x 40 ramp and 108 -> 56 for
+ * 80 x 80, the same solution to 1e-10; 95 -> 51 for the whole 400 x 400
+ * solve of the mixed method with the learned preconditioner.  The residual
+ * and the accepted solutions are unchanged; only the iteration differs from
+ * the reference's. */
 ipfem_status ipfem_set_consistent_tangent(ipfem_ctx *ctx, int on);
 /* Secant predictor of the load steps (no counterpart in the reference, whose
  * load steps start from the last accepted solution): with on = 1 each load
