@@ -79,13 +79,6 @@ __global__ void k_adam(int n, float *__restrict__ p, const float *__restrict__ g
     p[i] -= lr * (mi / c1) / (sqrtf(vi / c2) + eps);
 }
 
-// grads *= s
-__global__ void k_scale(int n, float *__restrict__ g, float s)
-{
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) g[i] *= s;
-}
-
 // ------------------------------------------------------------ node grid
 struct GridInfo {
     int32_t gr, gt;
