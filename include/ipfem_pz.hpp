@@ -147,7 +147,9 @@ public:
     }
 
     // tangent and residual at Solution() (TPZElastoPlasticIntPointsStructMatrix.cpp:99-135):
-    // rhs = -B^T sigma(u) + rhs_linear, K the consistent tangent
+    // rhs = -B^T sigma(u) + rhs_linear, K the tangent: the reference's
+    // TangentOperator, or the consistent one after
+    // ipfem_set_consistent_tangent(Context(), 1)
     void Assemble(SymSparse &K, std::vector<double> &rhs)
     {
         rhs.assign((size_t)NEquations(), 0.0);
