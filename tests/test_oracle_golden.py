@@ -91,3 +91,53 @@ def test_sigma_and_sigma_dep_agree(gold):
     """ComputeSigma and ComputeSigmaDep give the same stress bit for bit."""
     assert _eq(gold["cpu_sigma6"], gold["cpu_dep_sigma6"])
     assert np.array_equal(gold["cpu_mtype"], gold["cpu_dep_mtype"])
+
+
+def _fd_tangent_errors(gold):
+    """per return type, max |Dep - dsigma_w/dstrain3| over a point's entries,
+    relative to its elastic stiffness w (lambda + 2 mu); central differences
+    that stay on the point's branch.  Returns {mtype: [errors]} and the Dep
+    matrices of the elastic points."""
+    errs, elastic = {0: [], 1: [], -1: []}, []
+    g = dict(gold, strain3=gold["strain3"].copy())
+    for i in range(len(gold["weight"])):
+        s3 = gold["strain3"][i]
+        _, d9, _, _, mt, _ = _run(gold, i, True)
+        if not np.all(np.isfinite(d9)):
+            continue            # repeated in-plane eigenvalue: NaN in the reference too
+        h = 1e-7 * max(np.abs(s3).max(), 1e-6)
+        F, same = np.zeros((3, 3)), True
+        for k in range(3):
+            g["strain3"][i] = s3 + h * np.eye(3)[k]
+            sp, _, _, _, mp, _ = _run(g, i, True)
+            g["strain3"][i] = s3 - h * np.eye(3)[k]
+            sm, _, _, _, mm, _ = _run(g, i, True)
+            g["strain3"][i] = s3
+            same = same and mp == mt and mm == mt
+            F[:, k] = (sp - sm) / (2 * h)
+        if not same:
+            continue
+        errs[mt].append(np.abs(d9.reshape(3, 3) - F).max() / (gold["weight"][i] * (gold["lam"][i] + 2 * gold["mu"][i])))
+        if mt == 0:
+            elastic.append(d9)
+    return {k: np.array(v) for k, v in errs.items()}, np.array(elastic)
+
+
+def test_tangents_against_finite_differences_per_return_type(gold):
+    """On the golden points, per return type: the consistent variant of the
+    oracle's tangent (orc_set_consistent_tangent) is the derivative of the
+    point's weighted stress; the reference's TangentOperator is off by a
+    sizeable fraction of the elastic stiffness wherever the point is plastic
+    (plane, edge and apex returns) and equal to the consistent one where it is
+    elastic."""
+    e_ref, d_ref = _fd_tangent_errors(gold)
+    with po.consistent_tangent():
+        e_con, d_con = _fd_tangent_errors(gold)
+    for mt, name in ((1, "plane/edge"), (-1, "apex"), (0, "elastic")):
+        print("%-10s n %4d  reference median %.2e max %.2e | consistent median %.2e p90 %.2e"
+              % (name, e_ref[mt].size, np.median(e_ref[mt]), e_ref[mt].max(), np.median(e_con[mt]),
+                 np.percentile(e_con[mt], 90)))
+    assert e_ref[1].size > 200 and e_ref[-1].size > 100 and e_ref[0].size > 700
+    assert e_con[1].max() < 1e-6 and np.percentile(e_con[-1], 90) < 1e-6
+    assert np.median(e_ref[1]) > 0.05 and np.median(e_ref[-1]) > 0.05
+    assert _eq(d_ref, d_con) and np.median(e_con[0]) < 1e-6
