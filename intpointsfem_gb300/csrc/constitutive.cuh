@@ -15,6 +15,17 @@
 // of the cubic residual is fabs().
 #pragma once
 
+// The same source compiles for the host (g++, -ffp-contract=off), where a CPU
+// test compares it with the oracle bit for bit.
+#if defined(__CUDACC__)
+#define IPFEM_HD __host__ __device__ __forceinline__
+#else
+#include <cmath>
+#define IPFEM_HD inline
+using std::fabs;
+using std::sqrt;
+#endif
+
 struct MCConst {            // per-element Mohr-Coulomb constants (libm trig from the host)
     double c, sinphi, cosphi, tanphi, sinpsi;
 };
@@ -30,7 +41,7 @@ struct ElasticConst {
 // ------------------------------------------------ spectral decomposition
 // Symmetric 3x3 with s_xz = s_yz = 0.  s = {xx, xy, yy, zz}.
 // FunctionsSpectralDecomp.h:61-111 (Newton on the normalised cubic)
-__device__ __forceinline__ void sd_newton(const double s[4], double ev[3], double maxel)
+IPFEM_HD void sd_newton(const double s[4], double ev[3], double maxel)
 {
     const double sxx = s[0], sxy = s[1], syy = s[2], szz = s[3];
     const double sxy2 = sxy * sxy;
@@ -84,7 +95,7 @@ __device__ __forceinline__ void sd_newton(const double s[4], double ev[3], doubl
 }
 
 // Multiplicity1, FunctionsSpectralDecomp.h:116-150
-__device__ __forceinline__ void sd_mult1(const double s[4], double lam, double *v_out)
+IPFEM_HD void sd_mult1(const double s[4], double lam, double *v_out)
 {
     const double sxx = s[0], sxy = s[1], syy = s[2], szz = s[3];
     const double det0 = (sxx - lam) * (syy - lam) - sxy * sxy;
@@ -117,7 +128,7 @@ __device__ __forceinline__ void sd_mult1(const double s[4], double lam, double *
 }
 
 // Multiplicity2, FunctionsSpectralDecomp.h:155-212 (second norm as in the reference)
-__device__ __forceinline__ void sd_mult2(const double s[4], double lam, double *a, double *b)
+IPFEM_HD void sd_mult2(const double s[4], double lam, double *a, double *b)
 {
     const double x0 = s[0] - lam, x1 = s[2] - lam, x2 = s[3] - lam;
     double maxx = fabs(x0);
@@ -142,7 +153,7 @@ __device__ __forceinline__ void sd_mult2(const double s[4], double lam, double *
 
 // SpectralDecomposition, FunctionsSpectralDecomp.h:261-268.  s is modified
 // (normalised and rescaled) exactly as the reference modifies its argument.
-__device__ __forceinline__ void spectral(double s[4], double ev[3], double vec[9])
+IPFEM_HD void spectral(double s[4], double ev[3], double vec[9])
 {
     // Normalize (…h:7-20); XZ and YZ are zero and never exceed |maxel|
     double m = s[0];
@@ -180,14 +191,14 @@ __device__ __forceinline__ void spectral(double s[4], double ev[3], double vec[9
 
 // ----------------------------------------------------- Mohr-Coulomb return
 // FunctionsSigmaProjection.h:6-20
-__device__ __forceinline__ bool phi_plane(const double ev[3], const MCConst &m)
+IPFEM_HD bool phi_plane(const double ev[3], const MCConst &m)
 {
     const double phi = ev[0] - ev[2] + (ev[0] + ev[2]) * m.sinphi - 2. * m.c * m.cosphi;
     return (fabs(phi) < 1.e-12) || (phi < 0.0);
 }
 
 // FunctionsSigmaProjection.h:25-63
-__device__ __forceinline__ bool rm_main_plane(const double st[3], double sp[3], double &hard,
+IPFEM_HD bool rm_main_plane(const double st[3], double sp[3], double &hard,
                                               const MCConst &m, double K, double G)
 {
     double e0 = st[0], e1 = st[1], e2 = st[2];
@@ -213,7 +224,7 @@ __device__ __forceinline__ bool rm_main_plane(const double st[3], double sp[3], 
 }
 
 // FunctionsSigmaProjection.h:68-88
-__device__ __forceinline__ void plane_tangent(double t[9], const MCConst &m, double K, double G)
+IPFEM_HD void plane_tangent(double t[9], const MCConst &m, double K, double G)
 {
     const double sin_phi = m.sinphi, sin_psi = m.sinpsi;
     const double den = 6.0 * G + 2.0 * (G + 3.0 * K) * sin_phi * sin_psi;
@@ -231,7 +242,7 @@ __device__ __forceinline__ void plane_tangent(double t[9], const MCConst &m, dou
 // Two-surface return on an edge (FunctionsSigmaProjection.h:93-158 right,
 // 193-257 left).  The Jacobian is loop-invariant with H = 0.
 template <bool RIGHT>
-__device__ __forceinline__ bool rm_edge(const double st[3], double sp[3], double &hard,
+IPFEM_HD bool rm_edge(const double st[3], double sp[3], double &hard,
                                         const MCConst &m, double K, double G)
 {
     double e0 = st[0], e1 = st[1], e2 = st[2];
@@ -273,7 +284,7 @@ __device__ __forceinline__ bool rm_edge(const double st[3], double sp[3], double
 }
 
 // FunctionsSigmaProjection.h:163-188
-__device__ __forceinline__ void right_edge_tangent(double t[9], const MCConst &m, double K, double G)
+IPFEM_HD void right_edge_tangent(double t[9], const MCConst &m, double K, double G)
 {
     const double sin_phi = m.sinphi, sin_psi = m.sinpsi;
     const double a = 4.0 * G * (1.0 + (1.0 / 3.0) * sin_phi * sin_psi) + 4.0 * K * sin_phi * sin_psi;
@@ -294,7 +305,7 @@ __device__ __forceinline__ void right_edge_tangent(double t[9], const MCConst &m
 }
 
 // FunctionsSigmaProjection.h:262-287
-__device__ __forceinline__ void left_edge_tangent(double t[9], const MCConst &m, double K, double G)
+IPFEM_HD void left_edge_tangent(double t[9], const MCConst &m, double K, double G)
 {
     const double sin_phi = m.sinphi, sin_psi = m.sinpsi;
     const double a = 4.0 * G * (1.0 + (1.0 / 3.0) * sin_phi * sin_psi) + 4.0 * K * sin_phi * sin_psi;
@@ -315,7 +326,7 @@ __device__ __forceinline__ void left_edge_tangent(double t[9], const MCConst &m,
 }
 
 // FunctionsSigmaProjection.h:292-323
-__device__ __forceinline__ void rm_apex(const double st[3], double sp[3], double &hard,
+IPFEM_HD void rm_apex(const double st[3], double sp[3], double &hard,
                                         const MCConst &m, double K)
 {
     const double cotphi = 1. / m.tanphi;
@@ -343,7 +354,7 @@ __device__ __forceinline__ void rm_apex(const double st[3], double sp[3], double
 // ProjectSigma, FunctionsSigmaProjection.h:337-379 (separate input/output
 // arrays as in the CPU path, TPZConstitutiveLawProcessor.cpp:184)
 template <bool GRAD>
-__device__ __forceinline__ int project_sigma(const double ev[3], double sp[3], double &alpha,
+IPFEM_HD int project_sigma(const double ev[3], double sp[3], double &alpha,
                                              const MCConst &m, double K, double G, double grad[9])
 {
     sp[0] = ev[0]; sp[1] = ev[1]; sp[2] = ev[2];
@@ -385,7 +396,7 @@ __device__ __forceinline__ int project_sigma(const double ev[3], double sp[3], d
 // trial ones and the pair's ProdT terms start from zero: the consistent
 // spectral tangent (the reference's differs from finite differences of its
 // own residual by about 1e-2 in plastic states).
-__device__ __forceinline__ void tangent_dep(const double grad[9], const double sev[3], const double sp[3],
+IPFEM_HD void tangent_dep(const double grad[9], const double sev[3], const double sp[3],
                                             const double eev[3], const double v[9], double G, double lambda,
                                             int consistent, double dep[9])
 {
@@ -468,7 +479,7 @@ __device__ __forceinline__ void tangent_dep(const double grad[9], const double s
 // plastic strain {xx, xy, yy, zz}.  Outputs the stress {xx, xy, yy, zz}, the
 // updated plastic strain, alpha, m_type and, if DEP, the unweighted 3x3 Dep.
 template <bool DEP>
-__device__ __forceinline__ int ip_update(const double eps[3], const double pl[4], const ElasticConst &E,
+IPFEM_HD int ip_update(const double eps[3], const double pl[4], const ElasticConst &E,
                                          const MCConst &m, double sig[4], double pl_out[4],
                                          double &alpha, double dep[9])
 {
