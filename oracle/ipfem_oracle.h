@@ -76,6 +76,15 @@ void orc_set_consistent_tangent(int on);
 /* Point update with the full 6x6 tangent (XX XY XZ YY YZ ZZ; row = stress,
  * column = strain), as TPZPlasticStepPV::ApplyStrainComputeSigma's Dep that
  * TRKSolution::RKProcess reads (TRKSolution.cpp:189-191). */
+/* Decomposition variant for studies: 0 (default) the reference's
+ * SpectralDecomposition; 1 the closed form of plane-strain tensors (XZ = YZ
+ * = 0): ZZ and the in-plane 2x2 eigen-pairs.  Global. */
+void orc_set_spectral_mode(int mode);
+
+/* SpectralDecomposition (FunctionsSpectralDecomp.h:261-268) of one symmetric
+ * tensor: eigenvalues in descending order, eigenvectors as rows of vec9. */
+void orc_spectral(const double s6[6], double ev[3], double vec9[9]);
+
 void orc_ip_tangent6(const orc_elastic *el, const orc_mc *mc, const double strain6[6], const double eps_p6[6],
                      double sigma6[6], double eps_p6_out[6], double T36[36], int *mtype);
 

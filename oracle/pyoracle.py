@@ -102,6 +102,8 @@ def lib():
         L.orc_compute_sigma_batch.argtypes = [C.c_int64, C.c_int, C.POINTER(Elastic), C.POINTER(MC), _dp,
                                               _dp, _dp, C.c_int, _dp, _dp, _dp, C.POINTER(C.c_int8), _dp]
         L.orc_set_consistent_tangent.argtypes = [C.c_int]
+        L.orc_spectral.argtypes = [_dp, _dp, _dp]
+        L.orc_set_spectral_mode.argtypes = [C.c_int]
         L.orc_greedy_coloring.restype = C.c_int32
         L.orc_greedy_coloring.argtypes = [C.c_int32, C.c_int32, _ip, _ip]
         _lib = L
@@ -229,6 +231,18 @@ class OracleProblem:
                               ptr(log), int(log_cap))
         nlog = st.newton_iters
         return st, log[:3 * min(nlog, log_cap)].reshape(-1, 3)
+
+
+@contextlib.contextmanager
+def plane_spectral():
+    """The oracle's closed-form plane-strain spectral decomposition
+    (orc_set_spectral_mode(1)) for the duration of the block; the reference's
+    decomposition is restored on exit."""
+    lib().orc_set_spectral_mode(1)
+    try:
+        yield
+    finally:
+        lib().orc_set_spectral_mode(0)
 
 
 @contextlib.contextmanager

@@ -141,3 +141,49 @@ def test_tangents_against_finite_differences_per_return_type(gold):
     assert e_con[1].max() < 1e-6 and np.percentile(e_con[-1], 90) < 1e-6
     assert np.median(e_ref[1]) > 0.05 and np.median(e_ref[-1]) > 0.05
     assert _eq(d_ref, d_con) and np.median(e_con[0]) < 1e-6
+
+
+# A state of golden point 914 (its material and plastic strain) moved along a
+# strain path until an in-plane principal trial stress lies within 7e-7
+# (relative) of sigma_zz: 84.97540 against 84.97561.  The point returns to the
+# apex, where the projected stress is hydrostatic, c cot(phi) in every
+# direction; the reference reconstructs it with eigenvectors that Multiplicity1
+# computed one at a time from a nearly singular system, which are far from
+# orthogonal here (FunctionsSpectralDecomp.h:116-150, 217-256).
+GLITCH = {"lam": 4166.666666666667, "mu": 6250.0, "c": 7.0, "phi": 0.4363323129985824,
+          "strain3": [0.010701258239680976, -0.01791932264000126, 0.010302795370944334],
+          "plastic6": [0.00036342429229277727, -0.0020668644577720397, 0.0, 0.003073056850626, 0.0,
+                       -0.000706630696552844]}
+
+
+def test_near_repeated_eigenvalue_gives_a_wrong_apex_stress_as_in_the_reference():
+    """The oracle keeps the reference's behaviour at a nearly repeated trial
+    eigenvalue bit for bit (and against the reference's compiled headers where
+    the reference tree is present): the apex stress keeps its trace but is not
+    hydrostatic.  (The states 5.4e-6 of strain away on either side along the
+    path are hydrostatic to 1e-7: the stress jumps there.)"""
+    g = GLITCH
+    el = po.Elastic(g["lam"], g["mu"])
+    mc = po.MC()
+    po.lib().orc_mc_from_angles(g["c"], g["phi"], g["phi"], C.byref(mc))
+    s3, p6 = np.array(g["strain3"]), np.array(g["plastic6"])
+    sw, s6, pout, st6, d9 = np.zeros(3), np.zeros(6), np.zeros(6), np.zeros(6), np.zeros(9)
+    mt, al = C.c_int(), C.c_double()
+    po.lib().orc_ip_update(C.byref(el), C.byref(mc), po.ptr(s3), po.ptr(p6), 1.0, po.ptr(sw), po.ptr(d9),
+                           po.ptr(s6), po.ptr(pout), po.ptr(st6), C.byref(mt), C.byref(al))
+    apex = g["c"] / np.tan(g["phi"])
+    assert mt.value == -1
+    assert abs((s6[0] + s6[3] + s6[5]) / 3 - apex) < 1e-12 * apex
+    assert np.abs(s6[[0, 3, 5]] - apex).max() > 5.0 and abs(s6[1]) > 5.0
+    from oracle.build import build_ref
+    so = build_ref()
+    if so is None:
+        pytest.skip("reference tree not present")
+    ref = C.CDLL(so)
+    P = lambda a: a.ctypes.data_as(C.POINTER(C.c_double))  # noqa: E731
+    rs6, rsw, rp = np.zeros(6), np.zeros(3), np.zeros(6)
+    rmt, ral = C.c_int(), C.c_double()
+    ref.ref_ip_sigma(C.c_double(g["lam"]), C.c_double(g["mu"]), C.c_double(g["phi"]), C.c_double(g["phi"]),
+                     C.c_double(g["c"]), P(s3), P(p6), C.c_double(1.0), P(rsw), P(rs6), P(rp), C.byref(rmt),
+                     C.byref(ral))
+    assert rmt.value == -1 and _eq(rs6, s6)
