@@ -222,6 +222,20 @@ ipfem_status ipfem_set_newton_tangent(ipfem_ctx *ctx, int mode);
  * and the accepted solutions are unchanged; only the iteration differs from
  * the reference's. */
 ipfem_status ipfem_set_consistent_tangent(ipfem_ctx *ctx, int on);
+/* Spectral decomposition of the trial stress and the elastic strain: 0
+ * (default) the reference's SpectralDecomposition
+ * (FunctionsSpectralDecomp.h:261-268), bit-identical to it; 1 the closed form
+ * of a plane-strain tensor, zz with (0, 0, 1) and the eigen-pairs of the
+ * in-plane 2x2 block.  Within about 1e-6 (relative) of a repeated eigenvalue
+ * the reference's cubic roots are about 3e-6 off and Multiplicity1 can return
+ * the same eigenvector twice; the reconstructed stress is then wrong by the
+ * size of the stress, and the residual jumps as a Newton iterate crosses such
+ * a state (an in-plane principal stress crossing sigma_zz).  Mode 1 has
+ * orthonormal vectors at any gap and no iteration; elsewhere it agrees with
+ * the reference to about 1e-7 (the reference's own accuracy there) and turns
+ * the reference's NaN at an exactly repeated in-plane eigenvalue into the
+ * right stress.  Invalidates the stored tangent. */
+ipfem_status ipfem_set_spectral_mode(ipfem_ctx *ctx, int mode);
 /* Secant predictor of the load steps (no counterpart in the reference, whose
  * load steps start from the last accepted solution): with on = 1 each load
  * step after the first of a newton_begin run starts from

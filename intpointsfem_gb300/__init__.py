@@ -184,6 +184,7 @@ def lib():
             "ipfem_set_inner_tolerance": (S, [P, S, C.c_double, C.c_double, C.c_double, C.c_double]),
             "ipfem_set_newton_predictor": (S, [P, S]),
             "ipfem_set_consistent_tangent": (S, [P, S]),
+            "ipfem_set_spectral_mode": (S, [P, S]),
             "ipfem_set_row_stencils": (S, [P, S]),
             "ipfem_row_stencil_count": (S, [P, _ip, _ip]),
             "ipfem_layout_info": (S, [P, S, _lp, _lp, _ip]),
@@ -450,6 +451,11 @@ class ElastoPlasticIntPointsStructMatrix:
         """1: the consistent spectral tangent (spin factors from the projected
         principal stresses); 0 (default): the reference's TangentOperator"""
         self._check(lib().ipfem_set_consistent_tangent(self._ctx, int(bool(on))))
+
+    def set_spectral_mode(self, mode):
+        """0 (default): the reference's spectral decomposition; 1: the closed
+        form of plane-strain tensors, orthonormal at any eigenvalue gap"""
+        self._check(lib().ipfem_set_spectral_mode(self._ctx, int(mode)))
 
     def set_newton_predictor(self, on):
         """1: each load step after the first starts from the secant prediction

@@ -1004,6 +1004,14 @@ ipfem_status ipfem_set_consistent_tangent(ipfem_ctx *c, int on)
     return IPFEM_OK;
 }
 
+ipfem_status ipfem_set_spectral_mode(ipfem_ctx *c, int mode)
+{
+    if (!c || (mode != 0 && mode != 1)) return fail(c, IPFEM_INVALID, "spectral mode must be 0 or 1");
+    c->spectral_mode = mode;
+    c->tangent_valid = false;   // the tangent depends on the decomposition
+    return IPFEM_OK;
+}
+
 ipfem_status ipfem_set_newton_predictor(ipfem_ctx *c, int on)
 {
     if (!c || (on != 0 && on != 1)) return fail(c, IPFEM_INVALID, "predictor must be 0 or 1");

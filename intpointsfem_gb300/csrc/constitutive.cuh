@@ -36,6 +36,7 @@ struct ElasticConst {
     double l2m;             // lambda + 2 * mu
     double c1, c2, inv_mu;  // inverse elasticity coefficients of ComputeStrain
     int consistent;         // 1: consistent spectral tangent (ipfem_set_consistent_tangent)
+    int spectral;           // 1: closed-form plane-strain decomposition (ipfem_set_spectral_mode)
 };
 
 // ------------------------------------------------ spectral decomposition
@@ -187,6 +188,46 @@ IPFEM_HD void spectral(double s[4], double ev[3], double vec[9])
             sd_mult1(s, ev[2], &vec[6]);
         }
     }
+}
+
+// Closed-form decomposition of a plane-strain tensor s = {xx, xy, yy, zz}:
+// zz with (0, 0, 1), and the eigen-pairs of the in-plane 2x2 block, so the
+// vectors are orthonormal at any eigenvalue gap (the decomposition above loses
+// that within about 1e-6, relative, of a repeated eigenvalue: its cubic roots
+// are about 3e-6 off there and Multiplicity1 can return the same vector
+// twice).  Same outputs as spectral(): eigenvalues descending, vectors as rows.
+IPFEM_HD void spectral_plane(const double s[4], double ev[3], double vec[9])
+{
+    const double d = 0.5 * (s[0] - s[2]), m = 0.5 * (s[0] + s[2]);
+    const double r = sqrt(d * d + s[1] * s[1]);
+    double c = 1.0, sn = 0.0;       // unit eigenvector of m + r
+    if (r > 0.0) {
+        // (A - (m + r) I) x = 0 for x = (d + r, b) and for x = (b, r - d):
+        // take the one with an entry of at least r
+        const double x = d >= 0.0 ? d + r : s[1];
+        const double y = d >= 0.0 ? s[1] : r - d;
+        const double n = sqrt(x * x + y * y);
+        c = x / n;
+        sn = y / n;
+    }
+    const double l0 = m + r, l1 = m - r, l2 = s[3];
+    // descending; m + r >= m - r, and zz goes after an equal in-plane value
+    double e0 = l0, e1 = l1, e2 = l2;
+    double v0[3] = {c, sn, 0.0}, v1[3] = {-sn, c, 0.0}, v2[3] = {0.0, 0.0, 1.0};
+    if (l2 > l0) {
+        e0 = l2; e1 = l0; e2 = l1;
+        v0[0] = 0.0; v0[1] = 0.0; v0[2] = 1.0;
+        v1[0] = c; v1[1] = sn; v1[2] = 0.0;
+        v2[0] = -sn; v2[1] = c; v2[2] = 0.0;
+    } else if (l2 > l1) {
+        e1 = l2; e2 = l1;
+        v1[0] = 0.0; v1[1] = 0.0; v1[2] = 1.0;
+        v2[0] = -sn; v2[1] = c; v2[2] = 0.0;
+    }
+    ev[0] = e0; ev[1] = e1; ev[2] = e2;
+    vec[0] = v0[0]; vec[1] = v0[1]; vec[2] = v0[2];
+    vec[3] = v1[0]; vec[4] = v1[1]; vec[5] = v1[2];
+    vec[6] = v2[0]; vec[7] = v2[1]; vec[8] = v2[2];
 }
 
 // ----------------------------------------------------- Mohr-Coulomb return
@@ -496,13 +537,19 @@ IPFEM_HD int ip_update(const double eps[3], const double pl[4], const ElasticCon
     s[3] = E.lambda * ee[0] + E.lambda * ee[2] + E.l2m * ee[3];
     s[1] = E.mu * ee[1];
     double sev[3], svec[9], sp[3], grad[9];
-    spectral(s, sev, svec);
+    if (E.spectral == 1)
+        spectral_plane(s, sev, svec);
+    else
+        spectral(s, sev, svec);
     alpha = 0.0;
     int mt;
     if (DEP) {
         double eev[3], evec[9];
         ee[1] = ee[1] / 2;
-        spectral(ee, eev, evec);
+        if (E.spectral == 1)
+            spectral_plane(ee, eev, evec);
+        else
+            spectral(ee, eev, evec);
         mt = project_sigma<true>(sev, sp, alpha, m, E.K, E.G, grad);
         tangent_dep(grad, sev, sp, eev, evec, E.G, E.lambda, E.consistent, dep);
     } else {

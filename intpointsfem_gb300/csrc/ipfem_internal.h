@@ -300,6 +300,7 @@ struct ipfem_ctx {
     InnerTolerance inner;                // inner tolerance of the Newton iterations
     int predictor = 0;                   // secant predictor at the start of each load step
     int consistent_tangent = 0;          // consistent spectral tangent (ipfem_set_consistent_tangent)
+    int spectral_mode = 0;               // 1: closed-form plane-strain decomposition (ipfem_set_spectral_mode)
     double *d_u_prev = nullptr;          // [neq] solution of the previous accepted load step (predictor)
 };
 

@@ -62,6 +62,7 @@ static void compute_sigma_t(ipfem_ctx *c, int update_mem, const TS *d_strain, TS
     E.lambda = s.el.lambda; E.mu = s.el.mu; E.K = s.el.K; E.G = s.el.G; E.l2m = s.el.l2m;
     E.c1 = s.el.c1; E.c2 = s.el.c2; E.inv_mu = s.el.inv_mu;
     E.consistent = c->consistent_tangent;
+    E.spectral = c->spectral_mode;
     const int tpb = 128;
     const unsigned grid = (unsigned)((s.n_ip + tpb - 1) / tpb);
     if (grid == 0) return;

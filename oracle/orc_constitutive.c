@@ -301,13 +301,13 @@ static void spectral_plane(const double *s, double *ev, double *vec)
     }
     const double lam[3] = {m + r, m - r, s[ZZ]};
     const double v[3][3] = {{c, sn, 0.0}, {-sn, c, 0.0}, {0.0, 0.0, 1.0}};
+    /* descending; m + r >= m - r, and ZZ goes after an equal in-plane value */
     int o[3] = {0, 1, 2};
-    for (int i = 1; i < 3; i++)         /* descending, ties keep the order above */
-        for (int j = i; j > 0 && lam[o[j]] > lam[o[j - 1]]; j--) {
-            const int t = o[j];
-            o[j] = o[j - 1];
-            o[j - 1] = t;
-        }
+    if (lam[2] > lam[0]) {
+        o[0] = 2; o[1] = 0; o[2] = 1;
+    } else if (lam[2] > lam[1]) {
+        o[1] = 2; o[2] = 1;
+    }
     for (int k = 0; k < 3; k++) {
         ev[k] = lam[o[k]];
         for (int q = 0; q < 3; q++) vec[3 * k + q] = v[o[k]][q];

@@ -4,7 +4,7 @@
 // with g++ -ffp-contract=off, the host counterpart of the device's --fmad=false.
 #include "../intpointsfem_gb300/csrc/constitutive.cuh"
 
-extern "C" int host_ip_update(int dep, int consistent, double lambda, double mu, const double mc5[5],
+extern "C" int host_ip_update(int dep, int consistent, int spectral, double lambda, double mu, const double mc5[5],
                               const double eps[3], const double pl[4], double weight, double sigma_w3[3],
                               double sig4[4], double pl_out4[4], double *alpha, double dep9[9])
 {
@@ -19,6 +19,7 @@ extern "C" int host_ip_update(int dep, int consistent, double lambda, double mu,
     E.c2 = lambda / (6 * lambda * mu + 4 * mu * mu);
     E.inv_mu = 1 / mu;
     E.consistent = consistent;
+    E.spectral = spectral;
     MCConst m;
     m.c = mc5[0];
     m.sinphi = mc5[1];

@@ -195,3 +195,38 @@ def test_consistent_tangent_bit_exact():
     print("consistent tangent: %d Newton iterations, %d CG iterations"
           % (sg.newton_iters, sg.cg_iters))
     assert sg.newton_iters < 45
+
+
+def test_plane_spectral_bit_exact():
+    """ipfem_set_spectral_mode(ctx, 1), the closed-form plane-strain
+    decomposition: the residual and tangent in a random state with plastic
+    points, and the 40 x 40 ten-step Newton solve, are bit-identical to the
+    oracle's variant (orc_set_spectral_mode(1)); the solve takes fewer Newton
+    iterations than with the reference's decomposition (45 on this
+    configuration), its residual no longer carrying the 1e-7 noise of the
+    reference's eigenvectors."""
+    sm, P = _pair(16, material_mode=2)
+    rng = np.random.default_rng(49)
+    u = rng.normal(size=sm.neq) * 2e-3
+    u[P.arr("fixed").astype(bool)] = 0.0
+    sm.SetLoadFactor(0.7)
+    sm.set_spectral_mode(1)
+    r = sm.assemble(u, np.zeros(sm.neq))
+    K = sm.stiffness()[2]
+    with po.plane_spectral():
+        ro = P.assemble(u.copy(), 0.7)
+        assert _eq(r, ro)
+        assert _eq(K, P.arr("K"))
+    sm2, P2 = _pair(40)
+    sm2.set_spectral_mode(1)
+    ug, uo = np.zeros(sm2.neq), np.zeros(sm2.neq)
+    sg, lg = sm2.newton(ug, 10, newton_max_it=30)
+    with po.plane_spectral():
+        so, lo = P2.solve_steps(uo, 10, newton_max_it=30)
+    assert sg.converged and so.converged
+    assert sg.newton_iters == so.newton_iters and sg.cg_iters == so.cg_iters
+    assert _eq(lg, lo) and _eq(ug, uo)
+    assert _eq(sm2.get_state(1), _soa4(P2.arr("sigma"), P2.n_ip))
+    print("closed-form decomposition: %d Newton iterations, %d CG iterations"
+          % (sg.newton_iters, sg.cg_iters))
+    assert sg.newton_iters < 45
