@@ -327,6 +327,7 @@ def run_gpu(args):
             M.set_inner_tolerance(**ip.CHOSEN_INNER)
         M.set_newton_predictor(args.predictor == "on")
         M.set_consistent_tangent(args.tangent == "consistent")
+        M.set_spectral_mode(1 if args.spectral == "plane" else 0)
 
     A = ip.ElastoPlasticIntPointsStructMatrix(wb)         # device-resident arm
     if mixed:
@@ -459,6 +460,8 @@ def run_gpu(args):
             inner += ", secant predictor of the load steps"
         if args.tangent == "consistent":
             inner += ", consistent spectral tangent"
+        if args.spectral == "plane":
+            inner += ", closed-form plane-strain spectral decomposition"
         chosen["method"] = ("mixed + learned: FP32 tangent, flexible CG preconditioned by the learned "
                             "triangular factor (weights shipped in intpointsfem_gb300/weights), %s, FP64 residual/"
                             "return mapping/Newton refinement" % inner)
@@ -580,6 +583,9 @@ def main():
     ap.add_argument("--tangent", default="consistent", choices=["consistent", "reference"],
                     help="tangent of the mixed methods: the consistent spectral tangent (the chosen method's "
                          "setting) or the reference's TangentOperator; the plain method keeps the reference's")
+    ap.add_argument("--spectral", default="reference", choices=["reference", "plane"],
+                    help="spectral decomposition of the mixed methods: the reference's (default) or the closed form "
+                         "of plane-strain tensors (ipfem_set_spectral_mode); the plain method keeps the reference's")
     ap.add_argument("--no-chosen", dest="chosen", action="store_false")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--residual32", action="store_true",
