@@ -326,7 +326,6 @@ inline float *fp32_values(const ipfem_ctx *c)
     return use_sym32(c) ? c->mx.Ks : c->mx.K;
 }
 
-cudaError_t upload_constants(const ElasticConstH &el);
 void launch_gather_strain(ipfem_ctx *c, const double *d_u, double *d_strain);
 void launch_compute_sigma(ipfem_ctx *c, int update_mem, const double *d_strain, double *d_sigma_w, double *d_dep);
 void launch_stress_residual(ipfem_ctx *c, const double *d_sigma_w, double *d_fe);
