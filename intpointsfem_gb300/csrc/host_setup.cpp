@@ -61,11 +61,6 @@ int32_t greedy_coloring_nn(int32_t n_el, int32_t n_nodes, int32_t nn, const int3
     return color;
 }
 
-int32_t greedy_coloring(int32_t n_el, int32_t n_nodes, const int32_t *connects, int32_t *el_color)
-{
-    return greedy_coloring_nn(n_el, n_nodes, 9, connects, el_color);
-}
-
 template <class F>
 static void parallel_for(int64_t n, F f)
 {

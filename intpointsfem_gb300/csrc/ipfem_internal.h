@@ -189,7 +189,6 @@ void build_row_stencils(SellLayout &L);
 // the upper-only FP32 layout with its row and transposed stencils; returns an
 // empty string, or why it cannot be built (the full layout is used then)
 std::string build_sell_sym(const Setup &s, SellLayout &L);
-int32_t greedy_coloring(int32_t n_el, int32_t n_nodes, const int32_t *connects, int32_t *el_color);
 void elastic_constants(double E, double nu, ElasticConstH &el);
 // message returned by ipfem_last_error(NULL) on the calling thread
 void set_thread_error(const std::string &msg);
