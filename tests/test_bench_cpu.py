@@ -38,3 +38,35 @@ def test_reference_arm_json_line():
     P.close()
     assert line["newton_iters_timed"] == k == 2
     assert line["cg_iters_per_newton"] == cg / k
+
+
+def test_clock_summary_from_nvidia_smi_lines():
+    """The clock record of the bench line: median SM clock under the samples,
+    the maximum, and every throttle reason seen Active (hw_slowdown,
+    hw_thermal_slowdown and sw_thermal_slowdown reject a run, sw_power_cap is
+    kept and noted); unparsable lines are skipped."""
+    import bench
+
+    class _Proc:
+        def terminate(self):
+            pass
+
+        def wait(self, timeout=None):
+            return 0
+
+    idle = "Not Active"
+    s = bench.ClockSampler(0)
+    s.proc = _Proc()
+    s.lines = ["2070, 2070, 812.4, 0x0000000000000000, %s, %s, %s, %s" % (idle, idle, idle, idle),
+               "1965, 2070, 1391.0, 0x0000000000000004, %s, %s, %s, Active" % (idle, idle, idle),
+               "2070, 2070, 1010.2, 0x0000000000000000, %s, %s, %s, %s" % (idle, idle, idle, idle),
+               "[N/A], [N/A], [N/A], [N/A], [N/A], [N/A], [N/A], [N/A]",
+               "truncated, line"]
+    rec = s.stop()
+    assert rec == {"sm_mhz": 2070.0, "sm_max_mhz": 2070.0, "reasons": ["sw_power_cap"], "samples": 3}
+    s2 = bench.ClockSampler(0)
+    s2.proc = _Proc()
+    s2.lines = ["1500, 2070, 700.0, 0x0000000000000008, Active, %s, %s, %s" % (idle, idle, idle)]
+    assert s2.stop()["reasons"] == ["hw_slowdown"]
+    s3 = bench.ClockSampler(0)
+    assert s3.stop() is None
